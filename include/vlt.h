@@ -1,0 +1,346 @@
+/*
+ * vlt.h — C ABI of the GB300-native per-pixel lighting back end of violet:
+ * ReSTIR GI temporal/spatial reservoir resampling (indirect diffuse and specular),
+ * the ReLAX/SVGF denoiser, and the spatial-hash-grid radiance-cache update.
+ *
+ * Boundary. In violet these passes are render-graph nodes recorded by
+ * RestirRenderer::add_passes (crates/violet-restir/src/restir_renderer.rs:258-1028)
+ * and Denoiser::add_passes (crates/violet-restir/src/denoising.rs:66-301). Each
+ * per-pass entry point below replaces one `rg.new_compute(...)` node: the same named
+ * textures/buffers (as device pointers) and the same push constants. The view API
+ * replaces the temporal state those two structs keep across frames (RGTemporal
+ * handles) and runs the whole pass sequence for a frame.
+ *
+ * Conventions.
+ *  - Images are row-major, width W, height H, pixel (x, y) at index y*W + x.
+ *  - All buffer arguments are device pointers (cudaMalloc'd or equivalent) unless
+ *    a comment says "host". Streams are cudaStream_t passed as void*.
+ *  - Every call is stream-ordered and asynchronous and returns a vlt_status; nothing
+ *    aborts or throws across the ABI. A view is used by one host thread at a time.
+ *  - The G-buffer is the reference's 4-layer R32_UINT array stored layer-planar:
+ *    layer l of pixel i at gbuffer[l*W*H + i] (gbuffer.hlsl:51-77 encoding).
+ *  - Depth is reverse-Z binary32, 0 = no geometry.
+ *  - "R11G11B10" means B10G11R11_UFLOAT_PACK32 bits (R bits 0-10, G 11-21, B 22-31).
+ *
+ * Reference-form (VLT_FORM_REF) records used by the per-pass entry points:
+ *  - diffuse reservoir: uint4 per pixel {ReservoirSimple::encode_32b (M8|W24),
+ *    HitPosNormal.x, HitPosNormal.y, hit radiance R11G11B10}; replaces the three
+ *    textures (R32_UINT, R32G32_UINT, B10G11R11) of IndirectDiffuseTextures
+ *    (restir_renderer.rs:75-79, :572-586).
+ *  - specular reservoir: three planes — hit_pos float4 {xyz, target function},
+ *    reservoir uint2 {M, asuint(W)}, hit radiance u32 R11G11B10
+ *    (restir_renderer.rs:661-679, IndirectSpecularTextures :81-85).
+ *  - AO history: half2 {ao, valid} (the x and a channels of the RGBA16F texture;
+ *    y and z are never written with anything but 0); filtered AO: half.
+ *  - denoiser colour: uint2 {diffuse R11G11B10, specular R11G11B10}; moments and
+ *    variance: half2 (R16G16_SFLOAT); history length: u8 (R8_UNORM)
+ *    (denoising.rs:108-125).
+ */
+#ifndef VLT_H
+#define VLT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VLT_ABI_VERSION 1
+
+typedef enum vlt_status {
+  VLT_OK = 0,
+  VLT_ERR_INVALID_ARG = 1,
+  VLT_ERR_OUT_OF_MEMORY = 2,
+  VLT_ERR_BUDGET_EXCEEDED = 3,
+  VLT_ERR_CUDA = 4,
+  VLT_ERR_DEVICE_TIMEOUT = 5,
+  VLT_ERR_BAD_STATE = 6,
+  VLT_ERR_NO_DEVICE = 7
+} vlt_status;
+
+/* Storage form of a view's resident state. */
+typedef enum vlt_form {
+  VLT_FORM_REF = 0, /* the reference's texture formats; bit-exact with the oracle */
+  VLT_FORM_F32 = 1, /* every stored float in binary32 */
+  VLT_FORM_F16 = 2  /* packed 16-byte reservoirs, fp16 history/moments */
+} vlt_form;
+
+/* FrameParams of crates/violet-app/src/render_loop.rs:66-85 / frame_bindings.hlsl:6-26
+ * (binary32, column-major glam Mat4). 384 bytes. Host memory. */
+typedef struct vlt_frame_params {
+  float view_proj[16];
+  float inv_view_proj[16];
+  float view_pos[4];
+  float view_ray_top_left[4];
+  float view_ray_right_shift[4];
+  float view_ray_down_shift[4];
+  float prev_view_proj[16];
+  float prev_inv_view_proj[16];
+  float prev_view_pos[4];
+  float jitter[4]; /* xy: this frame, zw: previous frame (NDC) */
+  float sun_dir[4];
+  float sun_inten[4];
+} vlt_frame_params;
+
+/* Algorithm knobs. vlt_params_reference() gives the constants compiled into the
+ * reference's shaders and RestirConfig/Denoiser defaults (restir_renderer.rs:51-74,
+ * denoising.rs:52-60). */
+typedef struct vlt_params {
+  uint32_t diff_m_cap;            /* ind_diff_temporal_resample.hlsl:136 (16) */
+  uint32_t spec_m_cap;            /* ind_spec_temporal_resample.hlsl:252 (16, x roughness) */
+  uint32_t use_input_pdf;         /* 0: source pdf 1/(2 pi) as in :161; 1: caller pdf */
+  uint32_t diff_spatial_passes;   /* 1 */
+  uint32_t diff_spatial_taps;     /* MAX_ITERATION, ind_diff_spatial_resample.hlsl:8 (9) */
+  float diff_spatial_radius_px;   /* 0: INIT_RADIUS_FACTOR 0.05 * min(W, H) */
+  uint32_t spec_spatial_passes;   /* 1 */
+  uint32_t spec_spatial_taps;     /* MAX_ITERATION, ind_spec_spatial_resample.hlsl:12 (4) */
+  float spec_spatial_radius_px;   /* 0: 0.05 * min(W, H) */
+  float ao_radius;                /* RestirConfig::ao_radius (2.0) */
+  uint32_t denoise;               /* RestirConfig::denoise (1) */
+  uint32_t disocclusion_fix;      /* Denoiser::disocclusion_fix (1) */
+  uint32_t fast_history_clamp;    /* Denoiser::fast_history_clamp (0) */
+  uint32_t atrous_iterations;     /* Denoiser::atrous_iterations (3), clamped to 5 */
+  float history_max_frames;       /* 1 / BLEND_FACTOR_DIFF, svgf_temporal_filter.hlsl:281 (20) */
+  uint32_t hg_enable;             /* hash-grid radiance cache update (1) */
+  uint32_t hg_decay;              /* RestirConfig::hash_grid_cache_decay (1) */
+  uint32_t hg_log2_buckets;       /* hash_grid.inc.hlsl:9 (16); 16 cells per bucket */
+  uint32_t hg_key_mode;           /* 0: position + LOD key; 1: also the normal octant */
+  uint32_t hg_max_queries;        /* HASH_GRID_MAX_NUM_QUERIES (131072); 0: W*H */
+} vlt_params;
+
+void vlt_params_reference(vlt_params* out);
+/* Knobs of the plain-method workloads: config 0 = 320x180 (temporal M cap 20, one
+ * spatial pass of 5 taps at 16 px, 32-frame history, 5 a-trous iterations); config 1
+ * = 1920x1080 (two spatial passes of 8 taps, 2^22-cell hash grid keyed by position
+ * and normal octant, one query per pixel). */
+void vlt_params_plain(vlt_params* out, int config);
+
+/* ------------------------------------------------------------ context / view */
+
+typedef struct vlt_ctx vlt_ctx;
+typedef struct vlt_view vlt_view;
+
+vlt_status vlt_ctx_create(int device, vlt_ctx** out);
+vlt_status vlt_ctx_destroy(vlt_ctx* ctx);
+const char* vlt_status_string(vlt_status s);
+/* Last CUDA error text seen by this thread (empty if none). */
+const char* vlt_last_error(void);
+
+/* Allocates the view's resident state (reservoirs, AO and denoiser history, hash
+ * grid, previous depth/G-buffer) for a W x H view. */
+vlt_status vlt_view_create(vlt_ctx* ctx, uint32_t width, uint32_t height, vlt_form form,
+                           const vlt_params* params, vlt_view** out);
+vlt_status vlt_view_destroy(vlt_view* view);
+/* Bytes of device memory the view holds (for admission by HBM budget). */
+size_t vlt_view_device_bytes(uint32_t width, uint32_t height, vlt_form form, const vlt_params* params);
+/* Drops all temporal history, like a freshly created RestirRenderer (all the
+ * `prev_*` Options None) and Denoiser::reset (denoising.rs:62-64). */
+vlt_status vlt_view_reset(vlt_view* view, void* stream);
+
+typedef struct vlt_frame_inputs {
+  const vlt_frame_params* params;     /* host */
+  uint32_t frame_index;               /* seeds FrameRand (restir_renderer.rs:274) */
+  const float* depth;                 /* W*H */
+  const uint32_t* gbuffer;            /* 4*W*H, layer-planar */
+  const float* prev_depth;            /* optional: NULL uses the view's retained copy */
+  const uint32_t* prev_gbuffer;       /* optional: NULL uses the view's retained copy */
+  const uint32_t* diff_hit_pos_normal;/* uint2 per pixel (HitPosNormal) */
+  const uint32_t* diff_hit_radiance;  /* R11G11B10 */
+  const float* diff_source_pdf;       /* optional (used when params.use_input_pdf) */
+  const float* spec_hit_pos;          /* float4 per pixel (xyz, w unused) */
+  const uint32_t* spec_hit_radiance;  /* R11G11B10 */
+} vlt_frame_inputs;
+
+/* Output element type follows the view's form: REF -> u32 R11G11B10 per pixel,
+ * F32 -> float4 (rgb, 0), F16 -> half4 (rgb, 0). Any pointer may be NULL. */
+typedef struct vlt_frame_outputs {
+  void* diffuse;        /* denoised indirect diffuse (raw if denoising is off) */
+  void* specular;       /* denoised indirect specular (demodulated) */
+  void* raw_diffuse;    /* spatial-resampling output before the denoiser */
+  void* raw_specular;
+} vlt_frame_outputs;
+
+/* Runs one frame in the pass order of RestirRenderer::add_passes and
+ * Denoiser::add_passes, with the same conditional FrameRand seed consumption. The
+ * caller's previous depth/G-buffer pointers, if given, must hold last frame's. */
+vlt_status vlt_frame_run(vlt_view* view, const vlt_frame_inputs* in, const vlt_frame_outputs* out,
+                         void* stream);
+
+/* Number of kernel launches the last vlt_frame_run issued. */
+uint32_t vlt_view_last_launch_count(const vlt_view* view);
+
+/* Per-pass GPU timers (the counterpart of the render graph's per-pass timestamp
+ * queries, render_graph.rs:2321-2326, and NamedProfiling, gpu_profiling.rs:221-340).
+ * When enabled, vlt_frame_run brackets every kernel with CUDA events on its stream.
+ * vlt_view_read_timing synchronizes the view's last stream, accumulates the elapsed
+ * times per pass name since the last read, writes up to `max` entries and returns
+ * the number of distinct passes. */
+typedef struct vlt_pass_time {
+  char name[48];
+  uint32_t launches;
+  double total_ms;
+} vlt_pass_time;
+vlt_status vlt_view_set_timing(vlt_view* view, int enable);
+uint32_t vlt_view_read_timing(vlt_view* view, vlt_pass_time* out, uint32_t max);
+
+/* Device pointers of the view's resident state, for inspection and tests.
+ * name: "diff_reservoir", "spec_hit_pos", "spec_reservoir", "spec_radiance",
+ * "ao_history", "hist_color", "hist_moments", "hist_len", "hg_storage", "hg_decay",
+ * "hg_queries", "hg_query_count", "prev_depth", "prev_gbuffer", "variance",
+ * "spec_ray_len". Returns NULL for an unknown name. */
+void* vlt_view_buffer(vlt_view* view, const char* name, size_t* bytes);
+
+/* --------------------------------------------- per-pass entry points (REF form) */
+
+/* restir/ind_diff_temporal_resample.hlsl; node "Ind. Diff. Temporal Resample"
+ * (restir_renderer.rs:589-607). Push constants: frame_rand, has_prev_frame,
+ * has_new_sample. new_source_pdf may be NULL. */
+vlt_status vlt_ind_diff_temporal_resample(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                                          const vlt_params* params, const float* prev_gbuffer_depth,
+                                          const float* gbuffer_depth, const uint32_t* new_hit_pos_normal,
+                                          const uint32_t* new_hit_radiance, const float* new_source_pdf,
+                                          const uint32_t* prev_reservoir, uint32_t* rw_reservoir,
+                                          uint32_t frame_rand, uint32_t has_prev_frame,
+                                          uint32_t has_new_sample, void* stream);
+
+/* restir/raytraced_ao_gen.hlsl; node "RayTraced AO Gen." (restir_renderer.rs:528-541).
+ * Push constants: has_new_sample, has_prev_frame, radius_ws. */
+vlt_status vlt_ao_gen(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                      const uint32_t* hit_pos_normal, const float* depth_buffer,
+                      const uint16_t* prev_ao, uint16_t* rw_ao, uint32_t has_new_sample,
+                      uint32_t has_prev_frame, float radius_ws, void* stream);
+
+/* restir/raytraced_ao_filter.hlsl; node "RayTraced AO Filter" (restir_renderer.rs:551-560). */
+vlt_status vlt_ao_filter(uint32_t width, uint32_t height, const float* depth_buffer, const uint16_t* ao,
+                         uint16_t* rw_filtered_ao, void* stream);
+
+/* restir/ind_diff_spatial_resample.hlsl; node "Ind. Diff. Spatial Resample"
+ * (restir_renderer.rs:632-652). Push constant: frame_rand. rw_lighting: R11G11B10. */
+vlt_status vlt_ind_diff_spatial_resample(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                                         const vlt_params* params, const uint32_t* gbuffer_color,
+                                         const float* gbuffer_depth, const uint16_t* ao_texture,
+                                         const uint32_t* temp_reservoir, uint32_t* rw_reservoir,
+                                         uint32_t* rw_lighting, uint32_t frame_rand, void* stream);
+
+/* restir/ind_spec_temporal_resample.hlsl; node "Ind. Spec. Temporal Resample"
+ * (restir_renderer.rs:743-761). The reference updates the new-sample textures in
+ * place; here the new samples are read-only inputs (new_hit_pos, new_hit_radiance)
+ * and the merged reservoir goes to rw_*. Push constants: frame_rand, has_prev_frame. */
+vlt_status vlt_ind_spec_temporal_resample(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                                          const vlt_params* params, const float* prev_gbuffer_depth,
+                                          const uint32_t* prev_gbuffer_color, const float* gbuffer_depth,
+                                          const uint32_t* gbuffer_color, const uint32_t* prev_reservoir,
+                                          const float* prev_hit_pos, const uint32_t* prev_hit_radiance,
+                                          const float* new_hit_pos, const uint32_t* new_hit_radiance,
+                                          uint32_t* rw_reservoir, float* rw_hit_pos,
+                                          uint32_t* rw_hit_radiance, uint32_t frame_rand,
+                                          uint32_t has_prev_frame, void* stream);
+
+/* restir/ind_spec_spatial_resample.hlsl; node "Ind. Spec. Spaital Resample"
+ * (restir_renderer.rs:770-784). Push constant: frame_rand. rw_lighting R11G11B10,
+ * rw_ray_len half. The optional rw_reservoir/rw_hit_pos/rw_hit_radiance receive the
+ * merged reservoir (used to chain a second spatial pass; the reference writes none). */
+vlt_status vlt_ind_spec_spatial_resample(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                                         const vlt_params* params, const uint32_t* gbuffer_color,
+                                         const float* gbuffer_depth, const uint32_t* reservoir,
+                                         const float* hit_pos, const uint32_t* hit_radiance,
+                                         uint32_t* rw_lighting, uint16_t* rw_ray_len,
+                                         uint32_t* rw_reservoir, float* rw_hit_pos,
+                                         uint32_t* rw_hit_radiance, uint32_t frame_rand, void* stream);
+
+/* denoise/svgf_temporal_filter.hlsl; node "Temporal Filter" (denoising.rs:136-160).
+ * Push constants: buffer_size (implied by width/height), has_history, fast_history.
+ * Fast-history buffers may be NULL when fast_history is 0. */
+vlt_status vlt_denoise_temporal(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                                const vlt_params* params, const float* depth_texture,
+                                const uint32_t* gbuffer_texture, const uint32_t* diff_source,
+                                const uint32_t* spec_source, const uint16_t* spec_ray_len,
+                                const float* prev_depth_texture, const uint32_t* prev_gbuffer_texture,
+                                const uint32_t* color_history, const uint16_t* moments_history,
+                                const uint8_t* history_len_texture, const uint32_t* fast_history,
+                                uint32_t* rw_color, uint16_t* rw_moments, uint8_t* rw_history_len,
+                                uint32_t* rw_fast_history, uint32_t has_history, uint32_t fast_history_on,
+                                void* stream);
+
+/* denoise/relax_disocclusion_fix.hlsl; node "Disocclusion Fix" (denoising.rs:164-188). */
+vlt_status vlt_denoise_disocclusion_fix(uint32_t width, uint32_t height, const float* depth_texture,
+                                        const uint32_t* gbuffer_texture, const uint8_t* history_len_texture,
+                                        const uint32_t* color, const uint16_t* moments, uint32_t* rw_color,
+                                        uint16_t* rw_moments, void* stream);
+
+/* denoise/relax_fast_history_clamp.hlsl; node "Fast History Clamp" (denoising.rs:192-207).
+ * Clamps rw_color in place against the 3x3 YCoCg statistics of fast_history. */
+vlt_status vlt_denoise_fast_history_clamp(uint32_t width, uint32_t height, const uint32_t* fast_history,
+                                          uint32_t* rw_color, void* stream);
+
+/* denoise/svgf_spatial_fallback_filter.hlsl; node "Spatial Fallback" (denoising.rs:219-242). */
+vlt_status vlt_denoise_spatial_fallback(uint32_t width, uint32_t height, const float* depth_texture,
+                                        const uint32_t* gbuffer_texture, const uint8_t* history_len_texture,
+                                        const uint32_t* color, const uint16_t* moments, uint32_t* rw_color,
+                                        uint16_t* rw_variance, void* stream);
+
+/* denoise/svgf_atrous_filter.hlsl; node "Spatial Filter: i" (denoising.rs:262-284).
+ * Push constant: step_size. */
+vlt_status vlt_denoise_atrous(uint32_t width, uint32_t height, const float* depth_texture,
+                              const uint32_t* gbuffer_texture, const uint32_t* color,
+                              const uint16_t* variance, uint32_t* rw_color, uint16_t* rw_variance,
+                              int32_t step_size, void* stream);
+
+/* Hash-grid radiance cache. Cell storage: 16 bytes per cell {checksum, radiance f32x3}
+ * (HashGridCell, hash_grid.inc.hlsl:112-122); decay: u8 per cell; query record: 32
+ * bytes {hit position f32x3, normal oct32, bucket hash, checksum, radiance R11G11B10,
+ * 0} (HashGridQuery, hash_grid.inc.hlsl:186-206, plus the radiance that the reference
+ * obtains by tracing, which the caller supplies here). num_buckets = 2^log2_buckets. */
+
+/* restir/hash_grid_decay.hlsl; node "HashGridCache Decay" (restir_renderer.rs:322-329). */
+vlt_status vlt_hg_decay(uint32_t log2_buckets, uint8_t* rw_decay, uint32_t* rw_storage, void* stream);
+
+/* restir/hash_grid_query_select.hlsl; node "HashGridCache Query Select"
+ * (restir_renderer.rs:366-373). Inserts each query's cell in query-index order
+ * (deterministic slots) and keeps one random query per cell in rw_selection
+ * (InterlockedMax of score|1<<31|index). rw_selection must be zero on entry.
+ * scratch: vlt_hg_select_scratch_bytes() bytes. Push constant: frame_hash. */
+size_t vlt_hg_select_scratch_bytes(uint32_t log2_buckets, uint32_t max_queries);
+vlt_status vlt_hg_query_select(uint32_t log2_buckets, uint32_t max_queries, const uint32_t* queries,
+                               const uint32_t* query_count, uint32_t* rw_storage, uint32_t* rw_selection,
+                               uint32_t frame_hash, void* scratch, void* stream);
+
+/* restir/hash_grid_query_compact.hlsl; node "HashGridCache Query Compact"
+ * (restir_renderer.rs:384-391). rw_compact_count must be zero on entry. The order
+ * of the compacted entries is unspecified (as in the reference). */
+vlt_status vlt_hg_query_compact(uint32_t log2_buckets, uint32_t max_queries, const uint32_t* selection,
+                                uint32_t* rw_compact_query_index, uint32_t* rw_compact_cell_addr,
+                                uint32_t* rw_compact_count, void* stream);
+
+/* Cell update of restir/hash_grid_raygen.hlsl:71-86 (tracing excluded): radiance =
+ * L/16 + prev*15/16 with L the query's supplied radiance, decay = 10. */
+vlt_status vlt_hg_update(uint32_t max_queries, const uint32_t* queries, const uint32_t* compact_query_index,
+                         const uint32_t* compact_cell_addr, const uint32_t* compact_count,
+                         uint32_t* rw_storage, uint8_t* rw_decay, void* stream);
+
+/* Query emission of raytrace.inc.hlsl:173-198: one query per pixel with geometry,
+ * from the diffuse candidate (hit position, hit normal, radiance), at index y*W+x
+ * (sky pixels emit an empty record); writes max(count) to *query_count. */
+vlt_status vlt_hg_emit_queries(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                               uint32_t log2_buckets, uint32_t key_mode, uint32_t max_queries,
+                               const float* depth, const uint32_t* hit_pos_normal,
+                               const uint32_t* hit_radiance, uint32_t* rw_queries,
+                               uint32_t* rw_query_count, void* stream);
+
+/* hash_grid_find (hash_grid.inc.hlsl:126-147) for n positions/normals: out_addr[i]
+ * = cell address or 0xFFFFFFFF, out_radiance[i] = cell radiance (float4, w=found). */
+vlt_status vlt_hg_find(const vlt_frame_params* fp, uint32_t log2_buckets, uint32_t key_mode,
+                       const uint32_t* storage, uint32_t n, const float* positions,
+                       const float* normals, uint32_t* out_addr, float* out_radiance, void* stream);
+
+/* Diagnostics (no counterpart in the reference): evaluates the library's own
+ * binary32 transcendentals on the device, elementwise: fn 0 exp2, 1 exp, 2 log2,
+ * 3 sin, 4 cos. x and y are device arrays of n floats. */
+vlt_status vlt_diag_math(int fn, const float* x, float* y, uint32_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VLT_H */

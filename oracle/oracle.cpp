@@ -1,0 +1,1701 @@
+// ORACLE — test infrastructure only (imported by tests/, __graft_entry__.smoke()
+// and bench.py's CPU-baseline leg; never by the product).
+//
+// CPU restatement of violet's per-pixel lighting back end, pass by pass, following
+// the HLSL line by line (citations are path:line in the reference project):
+//   shader/restir/raytraced_ao_gen.hlsl, raytraced_ao_filter.hlsl,
+//   ind_diff_temporal_resample.hlsl, ind_diff_spatial_resample.hlsl,
+//   ind_spec_temporal_resample.hlsl, ind_spec_spatial_resample.hlsl,
+//   hash_grid.inc.hlsl, hash_grid_decay.hlsl, hash_grid_query_select.hlsl,
+//   hash_grid_query_compact.hlsl, hash_grid_raygen.hlsl:71-86,
+//   raytrace.inc.hlsl:173-198, shader/denoise/*.hlsl,
+// driven per frame in the order of crates/violet-restir/src/restir_renderer.rs:258-1028
+// and denoising.rs:66-301. Storage uses the reference texture formats packed as in
+// include/vlt.h (the product's records), so results compare byte for byte.
+//
+// Parity pinning: the reference is HLSL run through DXC/Vulkan and a Rust host; none
+// of it can be compiled or run here (no dxc, no graphics stack, no cargo), and the
+// reference ships no tests, golden images or fixtures. Parity with the reference's
+// own outputs is therefore UNPINNED; this restatement is checked against known-answer
+// vectors derived by hand from the shader text (tests/golden/).
+//
+// Rows run in parallel with OpenMP (the stand-in for the Rust host's rayon); the
+// hash-grid insertion runs sequentially in query order, which defines its result.
+#include <omp.h>
+#include <stdlib.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../include/vlt.h"
+#include "omath.hpp"
+
+using namespace orc;
+
+namespace {
+
+// Texture2D<T>[coord]: out-of-range loads return zero (robust access).
+template <class T>
+struct Tex {
+  const T* p;
+  int w, h;
+  T operator()(int x, int y) const {
+    if (x < 0 || y < 0 || x >= w || y >= h) {
+      T z;
+      memset(&z, 0, sizeof(T));
+      return z;
+    }
+    return p[(size_t)y * w + x];
+  }
+};
+
+struct U2 { uint32_t x, y; };
+struct U4 { uint32_t x, y, z, w; };
+struct F4s { float x, y, z, w; };
+
+inline bool in_img(int x, int y, int w, int h) { return x >= 0 && y >= 0 && x < w && y < h; }
+
+// cs_depth_to_position (frame_bindings.hlsl:57-61).
+float3 cs_depth_to_position(const float* inv_vp, int x, int y, int w, int h, float depth) {
+  float2 uv = F2(((float)x + 0.5f) / (float)w, ((float)y + 0.5f) / (float)h);
+  float4 p = mul(inv_vp, F4(uv.x * 2.0f - 1.0f, uv.y * 2.0f - 1.0f, depth, 1.0f));
+  return F3(p.x / p.w, p.y / p.w, p.z / p.w);
+}
+
+// SampleLevel(sampler_linear_clamp, uv, 0): exact binary32 bilinear (see omath.hpp).
+struct Bilinear {
+  int x0, x1, y0, y1;
+  float fx, fy;
+};
+Bilinear bilinear(float2 uv, int w, int h) {
+  float sx = uv.x * (float)w - 0.5f, sy = uv.y * (float)h - 0.5f;
+  float bx = floorf(sx), by = floorf(sy);
+  Bilinear b;
+  b.fx = sx - bx;
+  b.fy = sy - by;
+  int ix = to_int(bx), iy = to_int(by);
+  b.x0 = std::min(std::max(ix, 0), w - 1);
+  b.x1 = std::min(std::max(ix + 1, 0), w - 1);
+  b.y0 = std::min(std::max(iy, 0), h - 1);
+  b.y1 = std::min(std::max(iy + 1, 0), h - 1);
+  return b;
+}
+inline float blerp(float a, float b, float c, float d, float fx, float fy) {
+  float top = a + fx * (b - a);
+  float bot = c + fx * (d - c);
+  return top + fy * (bot - top);
+}
+inline float3 blerp(float3 a, float3 b, float3 c, float3 d, float fx, float fy) {
+  return F3(blerp(a.x, b.x, c.x, d.x, fx, fy), blerp(a.y, b.y, c.y, d.y, fx, fy), blerp(a.z, b.z, c.z, d.z, fx, fy));
+}
+
+GBuffer load_gbuffer(const uint32_t* g, int x, int y, int w, int h) {
+  if (!in_img(x, y, w, h)) return decode_gbuffer(0, 0, 0, 0);
+  size_t pl = (size_t)w * h, i = (size_t)y * w + x;
+  return decode_gbuffer(g[i], g[pl + i], g[2 * pl + i], g[3 * pl + i]);
+}
+float3 load_gbuffer_normal(const uint32_t* g, int x, int y, int w, int h) {
+  uint32_t e = in_img(x, y, w, h) ? g[(size_t)w * h + (size_t)y * w + x] : 0u;
+  return gbuffer_normal_decode(e);
+}
+
+int g_threads = 0;
+inline int nthreads() { return g_threads > 0 ? g_threads : omp_get_max_threads(); }
+
+#define ROWS_PARALLEL _Pragma("omp parallel for schedule(dynamic, 4) num_threads(nthreads())")
+
+// ================================================================ AO gen
+// raytraced_ao_gen.hlsl:18-81; history stored as half2 {x, a} (y, z stay 0).
+void ao_gen(const vlt_frame_params& fp, int w, int h, const uint32_t* hpn, const float* depth_buf,
+            const uint32_t* prev_ao, uint32_t* out, uint32_t has_new_sample, uint32_t has_prev_frame,
+            float radius_ws) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float depth = depth_buf[i];
+      if (has_no_geometry_via_depth(depth)) {
+        out[i] = 0u;
+        continue;
+      }
+      float2 motion_vector;
+      {
+        float3 position = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+        float4 hpos = mul(fp.view_proj, F4(position.x, position.y, position.z, 1.0f));
+        float2 ndc = F2(hpos.x / hpos.w - fp.jitter[0], hpos.y / hpos.w - fp.jitter[1]);
+        float4 hpos_reproj = mul(fp.prev_view_proj, F4(position.x, position.y, position.z, 1.0f));
+        float2 ndc_reproj = F2(hpos_reproj.x / hpos_reproj.w - fp.jitter[2], hpos_reproj.y / hpos_reproj.w - fp.jitter[3]);
+        motion_vector = (ndc - ndc_reproj) * 0.5f;
+      }
+      float2 src_uv = F2(((float)x + 0.5f) / (float)w, ((float)y + 0.5f) / (float)h);
+      float2 history_uv = src_uv - motion_vector;
+      float hx, ha;
+      bool is_in_last_view = history_uv.x == saturate(history_uv.x) && history_uv.y == saturate(history_uv.y);
+      if (is_in_last_view && has_prev_frame) {
+        Bilinear b = bilinear(history_uv, w, h);
+        Tex<uint32_t> t = {prev_ao, w, h};
+        float2 a = load_half2(t(b.x0, b.y0)), bb = load_half2(t(b.x1, b.y0));
+        float2 c = load_half2(t(b.x0, b.y1)), d = load_half2(t(b.x1, b.y1));
+        hx = blerp(a.x, bb.x, c.x, d.x, b.fx, b.fy);
+        ha = blerp(a.y, bb.y, c.y, d.y, b.fx, b.fy);
+      } else {
+        hx = 0.0f;
+        ha = 0.0f;
+      }
+      if (has_new_sample) {
+        HitPosNormal hit = HitPosNormal::decode(hpn[2 * i], hpn[2 * i + 1]);
+        float3 position_ws = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+        float3 sample_offset = hit.pos - position_ws;
+        float sample_distance = length(sample_offset);
+        float ao = sample_distance < radius_ws ? 0.0f : 1.0f;
+        hx = lerp(ao, hx, ((32.0f - 1.0f) / 32.0f) * ha);
+        ha = 1.0f;
+      } else {
+        hx = ha > 0.0f ? hx : 1.0f;
+      }
+      out[i] = store_half2(F2(hx, ha));
+    }
+}
+
+// ============================================================= AO filter
+// raytraced_ao_filter.hlsl:12-70 (x channel; taps at uint(min(p + d, size))).
+void ao_filter(int w, int h, const float* depth_buf, const uint32_t* ao, uint16_t* out) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float depth = depth_buf[i];
+      if (has_no_geometry_via_depth(depth)) {
+        out[i] = 0;
+        continue;
+      }
+      float center_ao = f16tof32(ao[i]);
+      float col_med[3], col_min[3], col_max[3];
+      for (int dy = -1; dy <= 1; dy++) {
+        float row[3];
+        for (int dx = -1; dx <= 1; dx++) {
+          uint32_t cx = std::min((uint32_t)x + (uint32_t)dx, (uint32_t)w);
+          uint32_t cy = std::min((uint32_t)y + (uint32_t)dy, (uint32_t)h);
+          Tex<float> dt = {depth_buf, w, h};
+          float sample_depth = dt((int)cx, (int)cy);
+          if (fabsf(depth - sample_depth) > 0.0005f) {
+            row[dx + 1] = center_ao;
+            continue;
+          }
+          Tex<uint32_t> at = {ao, w, h};
+          row[dx + 1] = f16tof32(at((int)cx, (int)cy) & 0xFFFFu);
+        }
+        col_med[dy + 1] = hclamp(row[0], row[1], row[2]);
+        col_min[dy + 1] = hmin(hmin(row[0], row[1]), row[2]);
+        col_max[dy + 1] = hmax(hmax(row[0], row[1]), row[2]);
+      }
+      float A = hmin(hmin(col_max[0], col_max[1]), col_max[2]);
+      float B = hmax(hmax(col_min[0], col_min[1]), col_min[2]);
+      float Cc = hclamp(col_med[0], col_med[1], col_med[2]);
+      float med = hclamp(Cc, A, B);
+      float mn = hmin(hmin(col_min[0], col_min[1]), col_min[2]);
+      out[i] = (uint16_t)f32tof16(lerp(med, mn, 0.5f));
+    }
+}
+
+// ===================================================== diffuse temporal
+// ind_diff_temporal_resample.hlsl:49-200.
+void diff_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const float* prev_depth,
+                   const float* depth_buf, const uint32_t* new_hpn, const uint32_t* new_rad, const float* new_pdf,
+                   const uint32_t* prev_rsv, uint32_t* out, uint32_t frame_rand, uint32_t has_prev_frame,
+                   uint32_t has_new_sample) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      const float depth = depth_buf[i];
+      // (sky pixels: the shader stores 0 here and then overwrites it below)
+      float3 position_ws = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+      float4 hpos_reproj = mul(fp.prev_view_proj, F4(position_ws.x, position_ws.y, position_ws.z, 1.0f));
+      float3 ndc_reproj = F3(hpos_reproj.x / hpos_reproj.w - fp.jitter[2], hpos_reproj.y / hpos_reproj.w - fp.jitter[3],
+                             hpos_reproj.z / hpos_reproj.w - 0.0f);
+      float2 uv_reproj = F2(ndc_reproj.x * 0.5f + 0.5f, ndc_reproj.y * 0.5f + 0.5f);
+      bool in_view = fabsf(ndc_reproj.x) < 1.0f && fabsf(ndc_reproj.y) < 1.0f;
+      bool sample_prev_frame = has_prev_frame && in_view;
+      if (sample_prev_frame) {
+        float reproj_depth = ndc_reproj.z;
+        Bilinear b = bilinear(uv_reproj, w, h);
+        float pd = blerp(prev_depth[(size_t)b.y0 * w + b.x0], prev_depth[(size_t)b.y0 * w + b.x1],
+                         prev_depth[(size_t)b.y1 * w + b.x0], prev_depth[(size_t)b.y1 * w + b.x1], b.fx, b.fy);
+        if (fabsf(pd - reproj_depth) > 0.001f) sample_prev_frame = false;
+      }
+      uint32_t M, rad_bits, hpn0, hpn1;
+      float W;
+      if (sample_prev_frame) {
+        int px = (int)to_uint(uv_reproj.x * (float)w), py = (int)to_uint(uv_reproj.y * (float)h);
+        Tex<U4> t = {(const U4*)prev_rsv, w, h};
+        U4 r = t(px, py);
+        reservoir_simple_decode_32b(r.x, &M, &W);
+        rad_bits = r.w;  // R11G11B10 load then store of the same value keeps its bits
+        hpn0 = r.y;
+        hpn1 = r.z;
+        if (M == 0) {
+          rad_bits = 0;
+          hpn0 = hpn1 = 0;
+        }
+        M = std::min(M, P.diff_m_cap);
+      } else {
+        M = 0;
+        W = 0.0f;
+        rad_bits = 0;
+        hpn0 = hpn1 = 0;
+      }
+      if (has_new_sample) {
+        float reservoir_target_pdf = luminance(load_r11g11b10(rad_bits));
+        float prev_w = W * reservoir_target_pdf * (float)M;
+        float3 new_hit_radiance = load_r11g11b10(new_rad[i]);
+        float new_target_pdf = luminance(new_hit_radiance);
+        float new_w;
+        if (P.use_input_pdf) {
+          float pdf = new_pdf[i];
+          new_w = pdf > 0.0f ? new_target_pdf / pdf : 0.0f;
+        } else {
+          new_w = new_target_pdf * TWO_PI;  // source_pdf = 1 / TWO_PI
+        }
+        uint32_t rng_state = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
+        float w_sum = prev_w + new_w;
+        float chance = new_w / w_sum;
+        if (lcg_rand(rng_state) < chance) {
+          hpn0 = new_hpn[2 * i];
+          hpn1 = new_hpn[2 * i + 1];
+          rad_bits = new_rad[i];
+          reservoir_target_pdf = new_target_pdf;
+        }
+        M += 1;
+        if (reservoir_target_pdf > 0.0f)
+          W = w_sum / (reservoir_target_pdf * (float)M);
+        else
+          W = 0.0f;
+      }
+      U4* o = (U4*)out + i;
+      o->x = reservoir_simple_encode_32b(M, W);
+      o->y = hpn0;
+      o->z = hpn1;
+      o->w = rad_bits;
+    }
+}
+
+// ====================================================== diffuse spatial
+// ind_diff_spatial_resample.hlsl:62-91 (WorkingReservoir::load) and :94-337.
+struct WorkingReservoir {
+  uint32_t M;
+  float W;
+  float3 hit_radiance, hit_pos, hit_normal;
+  float target_pdf;
+};
+WorkingReservoir wr_load(const uint32_t* rsv, size_t j, float3 pix_position_ws, float3 pix_normal) {
+  const U4 r = ((const U4*)rsv)[j];
+  WorkingReservoir o;
+  reservoir_simple_decode_32b(r.x, &o.M, &o.W);
+  HitPosNormal hit = HitPosNormal::decode(r.y, r.z);
+  o.hit_pos = hit.pos;
+  o.hit_normal = hit.normal;
+  o.hit_radiance = load_r11g11b10(r.w);
+  float3 hit_offset = hit.pos - pix_position_ws;
+  float nol = saturate(dot(pix_normal, normalize(hit_offset)));
+  o.target_pdf = nol * luminance(o.hit_radiance);
+  return o;
+}
+
+void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const uint32_t* gbuf,
+                  const float* depth_buf, const uint16_t* ao_tex, const uint32_t* in, uint32_t* out,
+                  uint32_t* lighting, uint32_t frame_rand) {
+  const uint32_t MAX_ITERATION = P.diff_spatial_taps;
+  const float MIN_RADIUS = 1.5f;
+  // Golden spiral constants (:148-150): B = log(1.61803398)/(0.5 PI), A = 1/exp(B 2PI).
+  const float Bc = 0.3063489496707916f;
+  const float Ac = 0.14589804410934448f;
+  const float COS_TOL = 0.906307816505432128906f;  // cos(PI * 25/180)
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float depth = depth_buf[i];
+      if (has_no_geometry_via_depth(depth)) {
+        ((U4*)out)[i] = U4{0, 0, 0, 0};
+        if (lighting) lighting[i] = 0;
+        continue;
+      }
+      const float3 position_ws = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+      float3 gnormal = load_gbuffer_normal(gbuf, x, y, w, h);
+      float ao = f16tof32(ao_tex[i]);
+      WorkingReservoir reservoir = wr_load(in, i, position_ws, gnormal);
+      float w_sum = reservoir.W * reservoir.target_pdf * (float)reservoir.M;
+      float radius = P.diff_spatial_radius_px > 0.0f ? P.diff_spatial_radius_px
+                                                     : (float)std::min(w, h) * 0.05f;
+      radius = hmax(radius * ao, MIN_RADIUS);  // pow(ao, 1.0) == ao
+      uint32_t rng_state = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
+      float rand_angle = lcg_rand(rng_state) * TWO_PI;
+      for (uint32_t it = 0; it < MAX_ITERATION; it++) {
+        const float T = 0.6186f * (float)MAX_ITERATION;
+        float theta = TWO_PI * (((float)it + 1.0f) / (float)MAX_ITERATION);
+        float r = Ac * exp_own(Bc * theta);
+        float sn, cs;
+        sincos_own(theta * T + rand_angle, &sn, &cs);
+        float ox = r * cs, oy = r * sn;
+        int nx = std::min(std::max(x + to_int(ox * radius), 0), w - 1);
+        int ny = std::min(std::max(y + to_int(oy * radius), 0), h - 1);
+        float3 normal_n = load_gbuffer_normal(gbuf, nx, ny, w, h);
+        float depth_n = depth_buf[(size_t)ny * w + nx];
+        bool geometrical_diff = false;
+        geometrical_diff |= dot(gnormal, normal_n) < COS_TOL;
+        float3 position_ws_n = cs_depth_to_position(fp.inv_view_proj, nx, ny, w, h, depth_n);
+        float dist_to_plane = dot(position_ws_n - position_ws, gnormal);
+        geometrical_diff |= fabsf(dist_to_plane) > 0.05f;
+        if (geometrical_diff) {
+          radius = hmax(radius * 0.5f, MIN_RADIUS);
+          continue;
+        }
+        WorkingReservoir neighbor = wr_load(in, (size_t)ny * w + nx, position_ws, gnormal);
+        float3 offset_qq = position_ws_n - neighbor.hit_pos;
+        float3 offset_rq = position_ws - neighbor.hit_pos;
+        float L2_qq = dot(offset_qq, offset_qq);
+        float L2_rq = dot(offset_rq, offset_rq);
+        float cos_rq = dot(neighbor.hit_normal, offset_rq * rsqrt(L2_rq));
+        float cos_qq = dot(neighbor.hit_normal, offset_qq * rsqrt(L2_qq));
+        float reuse_jacobian = (cos_rq / cos_qq) * (L2_qq / L2_rq);
+        reuse_jacobian = hclamp(reuse_jacobian, 0.0f, 10.0f);
+        reuse_jacobian = hclamp(reuse_jacobian, 0.0f, 1.0f);
+        float target_pdf_neighbor = neighbor.target_pdf * reuse_jacobian;
+        if (target_pdf_neighbor <= 0.0f) continue;
+        neighbor.M = std::min(neighbor.M, 255u);
+        float w_sum_neighbor = neighbor.W * target_pdf_neighbor * (float)neighbor.M;
+        w_sum += w_sum_neighbor;
+        float chance = w_sum_neighbor / w_sum;
+        if (lcg_rand(rng_state) < chance) {
+          reservoir.hit_normal = neighbor.hit_normal;
+          reservoir.hit_pos = neighbor.hit_pos;
+          reservoir.hit_radiance = neighbor.hit_radiance;
+          reservoir.target_pdf = neighbor.target_pdf;
+        }
+        reservoir.M += neighbor.M;
+      }
+      {
+        float target_pdf = reservoir.target_pdf;
+        if (target_pdf > 0.0f) reservoir.W = w_sum / (target_pdf * (float)reservoir.M);
+      }
+      U4* o = (U4*)out + i;
+      o->x = reservoir_simple_encode_32b(reservoir.M, reservoir.W);
+      HitPosNormal hpn = {reservoir.hit_pos, reservoir.hit_normal};
+      uint32_t e[2];
+      hpn.encode(e);
+      o->y = e[0];
+      o->z = e[1];
+      o->w = store_r11g11b10(reservoir.hit_radiance);
+      if (lighting) {
+        float3 selected_dir = normalize(reservoir.hit_pos - position_ws);
+        float NoL = saturate(dot(gnormal, selected_dir));
+        float brdf = ONE_OVER_PI;
+        lighting[i] = store_r11g11b10(reservoir.hit_radiance * (brdf * NoL * reservoir.W));
+      }
+    }
+}
+
+// ==================================================== specular sampling
+// ind_spec_temporal_resample.hlsl:48-144 (== ind_spec_spatial_resample.hlsl:39-151).
+inline float smith_lambda_GGX_plus_one_mul_cos(float cos_theta, float roughness) {
+  float r2 = roughness * roughness;
+  float c = cos_theta;
+  return (c + sqrtf((-r2 * c + c) * c + r2)) / 2.0f;
+}
+struct Sampling {
+  float source_pdf;
+  float3 brdf_NoL_over_source_pdf;
+};
+Sampling calc_things(float3 view_pos, float3 position_ws, float3 normal, float perceptual_roughness,
+                     float3 specular_f0, float3 sample_hit_pos) {
+  Sampling ret;
+  float roughness = perceptual_roughness * perceptual_roughness;
+  roughness = hmax(roughness, 0.002f);  // IND_SPEC_R_MIN
+  float3 view_dir = normalize(view_pos - position_ws);
+  float3 light_dir = normalize(sample_hit_pos - position_ws);
+  float3 H = normalize(view_dir + light_dir);
+  float NoV = saturate(dot(normal, view_dir));
+  float NoH = saturate(dot(normal, H));
+  float D = D_GGX(NoH, roughness);
+  float lambda_pomc = smith_lambda_GGX_plus_one_mul_cos(NoV, roughness);
+  ret.source_pdf = 0.25f * D / lambda_pomc;
+  float NoL = saturate(dot(normal, light_dir));
+  float LoH = saturate(dot(light_dir, H));
+  float3 F = F_Schlick(LoH, specular_f0);
+  float G2_over_G1 = smith_G2_over_G1_height_correlated_GGX(NoL, NoV, roughness);
+  if (NoL <= 0.0f) G2_over_G1 = 0.0f;
+  if (NoV <= 0.0f) G2_over_G1 = 0.0f;
+  ret.brdf_NoL_over_source_pdf = F * G2_over_G1;
+  return ret;
+}
+inline float eval_target_function(const Sampling& s, float3 radiance) {
+  return luminance(radiance * s.brdf_NoL_over_source_pdf) * s.source_pdf;
+}
+inline float3 v3(const float* p) { return F3(p[0], p[1], p[2]); }
+
+// ==================================================== specular temporal
+// ind_spec_temporal_resample.hlsl:146-362. New samples are read from the inputs;
+// the merged reservoir goes to out_* (the shader updates the new-sample textures
+// in place, so sky pixels keep the new sample there).
+void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const float* prev_depth,
+                   const uint32_t* prev_gbuf, const float* depth_buf, const uint32_t* gbuf, const uint32_t* prev_rsv,
+                   const float* prev_hp, const uint32_t* prev_rad, const float* new_hp, const uint32_t* new_rad,
+                   uint32_t* out_rsv, float* out_hp, uint32_t* out_rad, uint32_t frame_rand,
+                   uint32_t has_prev_frame) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float depth = depth_buf[i];
+      if (has_no_geometry_via_depth(depth)) {
+        out_rsv[2 * i] = 0;
+        out_rsv[2 * i + 1] = 0;
+        memcpy(out_hp + 4 * i, new_hp + 4 * i, 16);
+        out_rad[i] = new_rad[i];
+        continue;
+      }
+      const float3 position_ws = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+      float4 hpos_reproj = mul(fp.prev_view_proj, F4(position_ws.x, position_ws.y, position_ws.z, 1.0f));
+      float3 ndc_reproj = F3(hpos_reproj.x / hpos_reproj.w - fp.jitter[2], hpos_reproj.y / hpos_reproj.w - fp.jitter[3],
+                             hpos_reproj.z / hpos_reproj.w - 0.0f);
+      float2 uv_reproj = F2(ndc_reproj.x * 0.5f + 0.5f, ndc_reproj.y * 0.5f + 0.5f);
+      bool sample_prev_frame =
+          uv_reproj.x == saturate(uv_reproj.x) && uv_reproj.y == saturate(uv_reproj.y) && has_prev_frame;
+      if (sample_prev_frame) {
+        Bilinear b = bilinear(uv_reproj, w, h);
+        float pd = blerp(prev_depth[(size_t)b.y0 * w + b.x0], prev_depth[(size_t)b.y0 * w + b.x1],
+                         prev_depth[(size_t)b.y1 * w + b.x0], prev_depth[(size_t)b.y1 * w + b.x1], b.fx, b.fy);
+        if (fabsf(pd - ndc_reproj.z) > 0.001f) sample_prev_frame = false;
+      }
+      uint32_t M;
+      float W;
+      float3 reservoir_hit_pos, reservoir_hit_radiance;
+      uint32_t reservoir_rad_bits;
+      float reservoir_target_function;
+      GBuffer prev_gbuffer;
+      if (sample_prev_frame) {
+        int px = (int)to_uint(uv_reproj.x * (float)w), py = (int)to_uint(uv_reproj.y * (float)h);
+        U2 r = Tex<U2>{(const U2*)prev_rsv, w, h}(px, py);
+        M = r.x;
+        W = asfloat(r.y);
+        F4s hp = Tex<F4s>{(const F4s*)prev_hp, w, h}(px, py);
+        reservoir_hit_pos = F3(hp.x, hp.y, hp.z);
+        reservoir_rad_bits = Tex<uint32_t>{prev_rad, w, h}(px, py);
+        reservoir_hit_radiance = load_r11g11b10(reservoir_rad_bits);
+        reservoir_target_function = hp.w;
+        prev_gbuffer = load_gbuffer(prev_gbuf, px, py, w, h);
+      } else {
+        M = 0;
+        W = 0.0f;
+        reservoir_hit_pos = F3(0.0f);
+        reservoir_hit_radiance = F3(0.0f);
+        reservoir_rad_bits = 0;
+        reservoir_target_function = 0.0f;
+        memset(&prev_gbuffer, 0, sizeof(prev_gbuffer));
+      }
+      float3 new_sample_hit_pos = F3(new_hp[4 * i], new_hp[4 * i + 1], new_hp[4 * i + 2]);
+      float3 new_sample_hit_radiance = load_r11g11b10(new_rad[i]);
+      GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
+      {
+        uint32_t M_max = to_uint((float)P.spec_m_cap * gbuffer.perceptual_roughness);
+        M = std::min(M, M_max);
+      }
+      float3 view_pos = v3(fp.view_pos);
+      float3 f0 = get_specular_f0(gbuffer.color, gbuffer.metallic);
+      Sampling curr_sampling = calc_things(view_pos, position_ws, gbuffer.normal, gbuffer.perceptual_roughness, f0,
+                                           new_sample_hit_pos);
+      float new_w = luminance(new_sample_hit_radiance * curr_sampling.brdf_NoL_over_source_pdf);
+      float new_target_function = new_w * curr_sampling.source_pdf;
+      float prev_w = W * (reservoir_target_function * (float)M);
+      if (M > 0) {
+        Sampling prev_on_curr =
+            calc_things(v3(fp.prev_view_pos), position_ws, prev_gbuffer.normal, prev_gbuffer.perceptual_roughness,
+                        get_specular_f0(prev_gbuffer.color, prev_gbuffer.metallic), new_sample_hit_pos);
+        float prev_target_function_on_curr =
+            luminance(new_sample_hit_radiance * prev_on_curr.brdf_NoL_over_source_pdf) * prev_on_curr.source_pdf;
+        float curr_m = new_target_function / (new_target_function + prev_target_function_on_curr * (float)M);
+        if (new_target_function == 0.0f) curr_m = 0.0f;
+        new_w = curr_m * new_w;
+        Sampling curr_on_prev = calc_things(view_pos, position_ws, gbuffer.normal, gbuffer.perceptual_roughness, f0,
+                                            reservoir_hit_pos);
+        float curr_target_function_on_prev =
+            luminance(reservoir_hit_radiance * curr_on_prev.brdf_NoL_over_source_pdf) * curr_on_prev.source_pdf;
+        float m_num = reservoir_target_function * (float)M;
+        float prev_m = m_num / (m_num + curr_target_function_on_prev);
+        if (m_num == 0.0f) prev_m = 0.0f;
+        prev_w = prev_m * (curr_target_function_on_prev * W);
+        reservoir_target_function = curr_target_function_on_prev;
+      }
+      uint32_t rng_state = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
+      const float w_sum = prev_w + new_w;
+      const float chance_prev = prev_w / w_sum;
+      const bool use_prev_sample = lcg_rand(rng_state) < chance_prev;
+      if (!use_prev_sample) {
+        reservoir_hit_pos = new_sample_hit_pos;
+        reservoir_rad_bits = new_rad[i];
+        reservoir_target_function = new_target_function;
+      }
+      M += 1;
+      if (reservoir_target_function > 0.0f) {
+        W = w_sum / (reservoir_target_function * (float)M);
+        W = w_sum / reservoir_target_function;  // 1/M is in w_sum (MIS weights)
+      } else {
+        W = 0.0f;
+      }
+      out_rsv[2 * i] = M;
+      out_rsv[2 * i + 1] = asuint(W);
+      out_hp[4 * i] = reservoir_hit_pos.x;
+      out_hp[4 * i + 1] = reservoir_hit_pos.y;
+      out_hp[4 * i + 2] = reservoir_hit_pos.z;
+      out_hp[4 * i + 3] = reservoir_target_function;
+      out_rad[i] = reservoir_rad_bits;
+    }
+}
+
+// ===================================================== specular spatial
+// ind_spec_spatial_resample.hlsl:169-448 (+ optional merged-reservoir output).
+void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const uint32_t* gbuf,
+                  const float* depth_buf, const uint32_t* rsv, const float* hp_tex, const uint32_t* rad_tex,
+                  uint32_t* lighting, uint16_t* ray_len_out, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
+                  uint32_t frame_rand) {
+  const uint32_t MAX_ITERATION = P.spec_spatial_taps;
+  const float COS_TOL = 0.906307816505432128906f;
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float depth = depth_buf[i];
+      if (has_no_geometry_via_depth(depth)) {
+        if (lighting) lighting[i] = 0;
+        if (ray_len_out) ray_len_out[i] = 0;
+        if (out_rsv) {
+          out_rsv[2 * i] = 0;
+          out_rsv[2 * i + 1] = 0;
+          memcpy(out_hp + 4 * i, hp_tex + 4 * i, 16);
+          out_rad[i] = rad_tex[i];
+        }
+        continue;
+      }
+      const float3 position_ws = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+      GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
+      uint32_t M = rsv[2 * i];
+      float W = asfloat(rsv[2 * i + 1]);
+      float3 hit_pos = F3(hp_tex[4 * i], hp_tex[4 * i + 1], hp_tex[4 * i + 2]);
+      uint32_t rad_bits = rad_tex[i];
+      float3 hit_radiance = load_r11g11b10(rad_bits);
+      float3 view_pos = v3(fp.view_pos);
+      float3 center_f0 = get_specular_f0(gbuffer.color, gbuffer.metallic);
+      float reservoir_target_function = hp_tex[4 * i + 3];
+      const uint32_t num_iteration = to_uint(lerp(0.0f, (float)MAX_ITERATION, gbuffer.perceptual_roughness));
+      float radius = P.spec_spatial_radius_px > 0.0f ? P.spec_spatial_radius_px : (float)std::min(w, h) * 0.05f;
+      uint32_t rng_state = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
+      for (uint32_t it = 0; it < num_iteration; it++) {
+        float u0 = lcg_rand(rng_state);
+        float u1 = lcg_rand(rng_state);
+        float r = sqrtf(u0);
+        float theta = TWO_PI * u1;
+        float sn, cs;
+        sincos_own(theta, &sn, &cs);
+        float ox = r * cs, oy = r * sn;
+        int nx = std::min(std::max(x + to_int(ox * radius), 0), w - 1);
+        int ny = std::min(std::max(y + to_int(oy * radius), 0), h - 1);
+        if (nx == x && ny == y) continue;
+        GBuffer gbuffer_n = load_gbuffer(gbuf, nx, ny, w, h);
+        size_t j = (size_t)ny * w + nx;
+        float depth_n = depth_buf[j];
+        bool geometrical_diff = false;
+        geometrical_diff |= dot(gbuffer.normal, gbuffer_n.normal) < COS_TOL;
+        float3 position_ws_n = cs_depth_to_position(fp.inv_view_proj, nx, ny, w, h, depth_n);
+        float dist_to_plane = dot(position_ws_n - position_ws, gbuffer.normal);
+        geometrical_diff |= fabsf(dist_to_plane) > 0.05f;
+        if (geometrical_diff) {
+          radius = hmax(radius * 0.5f, 1.5f);
+          continue;
+        }
+        uint32_t M_n = rsv[2 * j];
+        float W_n = asfloat(rsv[2 * j + 1]);
+        float3 hit_pos_n = F3(hp_tex[4 * j], hp_tex[4 * j + 1], hp_tex[4 * j + 2]);
+        uint32_t rad_n_bits = rad_tex[j];
+        float3 hit_radiance_n = load_r11g11b10(rad_n_bits);
+        float reservoir_target_function_n = hp_tex[4 * j + 3];
+        float w_neighb, w_center;
+        {
+          float center_tf_on_center = reservoir_target_function;
+          float neighb_tf_on_neighb = reservoir_target_function_n;
+          float center_tf_on_neighb = eval_target_function(
+              calc_things(view_pos, position_ws, gbuffer.normal, gbuffer.perceptual_roughness, center_f0, hit_pos_n),
+              hit_radiance_n);
+          float m_neighb = (neighb_tf_on_neighb * (float)M_n) /
+                           (neighb_tf_on_neighb * (float)M_n + center_tf_on_neighb * (float)M);
+          if (neighb_tf_on_neighb * (float)M_n == 0.0f) m_neighb = 0.0f;
+          w_neighb = m_neighb * neighb_tf_on_neighb * W_n;
+          float neighb_tf_on_center = eval_target_function(
+              calc_things(view_pos, position_ws_n, gbuffer_n.normal, gbuffer_n.perceptual_roughness,
+                          get_specular_f0(gbuffer_n.color, gbuffer_n.metallic), hit_pos),
+              hit_radiance);
+          float m_center = (center_tf_on_center * (float)M) /
+                           (center_tf_on_center * (float)M + neighb_tf_on_center * (float)M_n);
+          if (center_tf_on_center * (float)M == 0.0f) m_center = 0.0f;
+          w_center = m_center * center_tf_on_center * W;
+        }
+        float w_sum = w_center + w_neighb;
+        float chance = w_neighb / w_sum;
+        if (lcg_rand(rng_state) < chance) {
+          hit_pos = hit_pos_n;
+          hit_radiance = hit_radiance_n;
+          rad_bits = rad_n_bits;
+          reservoir_target_function = reservoir_target_function_n;
+        }
+        M += M_n;
+        if (reservoir_target_function > 0.0f)
+          W = w_sum / reservoir_target_function;
+        else
+          W = 0.0f;
+      }
+      float ray_len = length(hit_pos - position_ws);
+      if (out_rsv) {
+        out_rsv[2 * i] = M;
+        out_rsv[2 * i + 1] = asuint(W);
+        out_hp[4 * i] = hit_pos.x;
+        out_hp[4 * i + 1] = hit_pos.y;
+        out_hp[4 * i + 2] = hit_pos.z;
+        out_hp[4 * i + 3] = reservoir_target_function;
+        out_rad[i] = rad_bits;
+      }
+      if (lighting) {
+        float3 specular_f0 = center_f0;
+        float roughness = gbuffer.perceptual_roughness * gbuffer.perceptual_roughness;
+        roughness = hmax(roughness, 0.002f);
+        float3 selected_dir = normalize(hit_pos - position_ws);
+        float3 view_dir = normalize(view_pos - position_ws);
+        float3 H = normalize(view_dir + selected_dir);
+        float NoL = saturate(dot(gbuffer.normal, selected_dir));
+        float NoV = saturate(dot(gbuffer.normal, view_dir));
+        float NoH = saturate(dot(gbuffer.normal, H));
+        float LoH = saturate(dot(selected_dir, H));
+        float3 F = F_Schlick(LoH, specular_f0);
+        float D = D_GGX(NoH, roughness);
+        float lambda_pomc = smith_lambda_GGX_plus_one_mul_cos(NoV, roughness);
+        float vndf = 0.25f * D / lambda_pomc;
+        float G2_over_G1 = smith_G2_over_G1_height_correlated_GGX(NoL, NoV, roughness);
+        if (NoL <= 0.0f) G2_over_G1 = 0.0f;
+        if (NoV <= 0.0f) G2_over_G1 = 0.0f;
+        float3 lt = hit_radiance * ((F * G2_over_G1) * (vndf * W));
+        float3 specular_reflectance = hmax(ggx_brdf_integral_approx(NoV, roughness, specular_f0), 1.0f / 65536.0f);
+        lt = lt / specular_reflectance;
+        lighting[i] = store_r11g11b10(lt);
+      }
+      if (ray_len_out) ray_len_out[i] = (uint16_t)f32tof16(ray_len);
+    }
+}
+
+// ========================================================== denoiser
+const float HISTORY_LEN_UNIT = 1.0f / 255.0f;
+
+// EdgeStoppingFunc (svgf.inc.hlsl:6-84).
+struct EdgeStoppingFunc {
+  float depth_center, fwidth_z;
+  float3 normal_center;
+  float2 lumi_center, lumi_std;
+  bool use_lumi;
+  float sigma_z, sigma_n;
+  static EdgeStoppingFunc create(float depth, float fwidth_z, float3 normal) {
+    EdgeStoppingFunc r;
+    r.depth_center = depth;
+    r.fwidth_z = fwidth_z;
+    r.normal_center = normal;
+    r.use_lumi = false;
+    r.sigma_z = 1.0f;
+    r.sigma_n = 128.0f;
+    r.lumi_center = F2(0, 0);
+    r.lumi_std = F2(0, 0);
+    return r;
+  }
+  float2 weight(float tap_dist, float depth, float3 normal, float2 lumi) const {
+    const float sigma_l = 4.0f;
+    const float epsilon = 1e-8f;
+    float dist_z = fabsf(depth - depth_center);
+    float weight_z_log = -dist_z / ((sigma_z * fwidth_z) * tap_dist + epsilon);
+    float n_dot = saturate(dot(normal_center, normal));
+    float weight_n = pow_pow2(n_dot, sigma_n);
+    float2 weight_l_log = F2(0.0f, 0.0f);
+    if (use_lumi) {
+      float2 dist_l = F2(fabsf(lumi.x - lumi_center.x), fabsf(lumi.y - lumi_center.y));
+      weight_l_log = F2(-dist_l.x * rcp(sigma_l * lumi_std.x + epsilon), -dist_l.y * rcp(sigma_l * lumi_std.y + epsilon));
+    }
+    return F2(weight_n * exp_own(weight_l_log.x + weight_z_log), weight_n * exp_own(weight_l_log.y + weight_z_log));
+  }
+};
+
+inline float3 cdiff(const uint32_t* c, size_t j) { return load_r11g11b10(c[2 * j]); }
+inline float3 cspec(const uint32_t* c, size_t j) { return load_r11g11b10(c[2 * j + 1]); }
+
+// svgf_temporal_filter.hlsl:96-362. Sky pixels: the shader writes only history 0;
+// the colour/moments outputs are defined as 0 here.
+void dn_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const float* depth_tex,
+                 const uint32_t* gbuf, const uint32_t* diff_src, const uint32_t* spec_src, const uint16_t* ray_len_tex,
+                 const float* prev_depth, const uint32_t* prev_gbuf, const uint32_t* color_hist,
+                 const uint32_t* mom_hist, const uint8_t* len_hist, const uint32_t* fast_hist, uint32_t* out_color,
+                 uint32_t* out_mom, uint8_t* out_len, uint32_t* out_fast, uint32_t has_history, uint32_t fast_history) {
+  const float BLEND_FACTOR_DIFF = 1.0f / P.history_max_frames;
+  const float BLEND_FACTOR_FAST = 1.0f / 3.0f;
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float depth = depth_tex[i];
+      if (has_no_geometry_via_depth(depth)) {
+        out_len[i] = 0;
+        out_color[2 * i] = out_color[2 * i + 1] = 0;
+        out_mom[i] = 0;
+        if (fast_history) out_fast[2 * i] = out_fast[2 * i + 1] = 0;
+        continue;
+      }
+      const float2 buffer_size = F2((float)w, (float)h);
+      const float2 screen_uv = F2(((float)x + 0.5f) / buffer_size.x, ((float)y + 0.5f) / buffer_size.y);
+      GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
+      float3 momentum1_spec = F3(0.0f), momentum2_spec = F3(0.0f);
+      for (int dx = -1; dx <= 1; dx++)
+        for (int dy = -1; dy <= 1; dy++) {
+          int px = std::min(std::max(x + dx, 0), w - 1), py = std::min(std::max(y + dy, 0), h - 1);
+          float3 s = load_r11g11b10(spec_src[(size_t)py * w + px]);
+          momentum1_spec += s;
+          momentum2_spec += s * s;
+        }
+      momentum1_spec = momentum1_spec * (1.0f / 9.0f);
+      momentum2_spec = momentum2_spec * (1.0f / 9.0f);
+
+      float3 virtual_spec_history = F3(0.0f), virtual_spec_fast_history = F3(0.0f);
+      {
+        float4 ph = mul(fp.inv_view_proj, F4(screen_uv.x * 2.0f - 1.0f, screen_uv.y * 2.0f - 1.0f, depth, 1.0f));
+        float3 position = F3(ph.x / ph.w, ph.y / ph.w, ph.z / ph.w);
+        float3 view_ray_dir = normalize(position - v3(fp.view_pos));
+        float ray_len = f16tof32(ray_len_tex[i]);
+        float3 virtual_position = position + view_ray_dir * ray_len;
+        float4 hr = mul(fp.prev_view_proj, F4(virtual_position.x, virtual_position.y, virtual_position.z, 1.0f));
+        float2 ndc_reproj = F2(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3]);
+        float2 vuv = F2((ndc_reproj.x + fp.jitter[0]) * 0.5f + 0.5f, (ndc_reproj.y + fp.jitter[1]) * 0.5f + 0.5f);
+        bool valid = vuv.x == saturate(vuv.x) && vuv.y == saturate(vuv.y) && has_history;
+        if (valid) {
+          Bilinear b = bilinear(vuv, w, h);
+          size_t a = (size_t)b.y0 * w + b.x0, bb = (size_t)b.y0 * w + b.x1, c = (size_t)b.y1 * w + b.x0,
+                 d = (size_t)b.y1 * w + b.x1;
+          virtual_spec_history = blerp(cspec(color_hist, a), cspec(color_hist, bb), cspec(color_hist, c),
+                                       cspec(color_hist, d), b.fx, b.fy);
+          if (fast_history)
+            virtual_spec_fast_history = blerp(cspec(fast_hist, a), cspec(fast_hist, bb), cspec(fast_hist, c),
+                                              cspec(fast_hist, d), b.fx, b.fy);
+        }
+      }
+      float2 motion_vector;
+      float reproj_depth;
+      {
+        float4 ph = mul(fp.inv_view_proj, F4(screen_uv.x * 2.0f - 1.0f, screen_uv.y * 2.0f - 1.0f, depth, 1.0f));
+        float3 position = F3(ph.x / ph.w, ph.y / ph.w, ph.z / ph.w);
+        float4 hpos = mul(fp.view_proj, F4(position.x, position.y, position.z, 1.0f));
+        float2 ndc = F2(hpos.x / hpos.w - fp.jitter[0], hpos.y / hpos.w - fp.jitter[1]);
+        float4 hr = mul(fp.prev_view_proj, F4(position.x, position.y, position.z, 1.0f));
+        float2 ndc_reproj = F2(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3]);
+        motion_vector = (ndc - ndc_reproj) * 0.5f;
+        reproj_depth = hr.z / hr.w;
+      }
+      float2 history_uv = screen_uv - motion_vector;
+      float3 diff_history = F3(0.0f), spec_history = F3(0.0f), diff_fast_history = F3(0.0f),
+             spec_fast_history = F3(0.0f);
+      float2 sec_moments_history = F2(0.0f, 0.0f);
+      float history_len = 0.0f;
+      bool valid = history_uv.x == saturate(history_uv.x) && history_uv.y == saturate(history_uv.y) && has_history;
+      if (valid) {
+        float2 pcc = F2(history_uv.x * buffer_size.x - 0.5f, history_uv.y * buffer_size.y - 0.5f);
+        float2 frac = F2(pcc.x - floorf(pcc.x), pcc.y - floorf(pcc.y));
+        int bx = to_int(pcc.x), by = to_int(pcc.y);
+        float depth_tol = gbuffer.fwidth_z * 4.0f + 1e-4f;
+        float normal_tol = gbuffer.fwidth_n * 16.0f + 1e-2f;
+        float normal_tol_sq = normal_tol * normal_tol;
+        float b = frac.y, r = frac.x, t = 1.0f - b, l = 1.0f - r;
+        const float weights[2][2] = {{t * l, t * r}, {b * l, b * r}};
+        float3 diff_sum = F3(0.0f), spec_sum = F3(0.0f), diff_fast_sum = F3(0.0f), spec_fast_sum = F3(0.0f);
+        float2 moments_sum = F2(0.0f, 0.0f);
+        float history_len_sum = 0.0f, weight_sum = 0.0f;
+        for (int ox = 0; ox < 2; ++ox)
+          for (int oy = 0; oy < 2; ++oy) {
+            int px = bx + ox, py = by + oy;
+            bool coord_valid = px == std::min(std::max(px, 0), w - 1) && py == std::min(std::max(py, 0), h - 1);
+            float3 normal = load_gbuffer_normal(prev_gbuf, px, py, w, h);
+            float pdv = Tex<float>{prev_depth, w, h}(px, py);
+            float3 n_diff = normal - gbuffer.normal;
+            bool sample_valid =
+                coord_valid && (fabsf(pdv - reproj_depth) < depth_tol) && (dot(n_diff, n_diff) < normal_tol_sq);
+            if (sample_valid) {
+              size_t j = (size_t)py * w + px;
+              float wt = weights[oy][ox];
+              weight_sum += wt;
+              diff_sum += wt * cdiff(color_hist, j);
+              spec_sum += wt * cspec(color_hist, j);
+              moments_sum += wt * load_half2(mom_hist[j]);
+              history_len_sum += wt * load_unorm8(len_hist[j]);
+              if (fast_history) {
+                diff_fast_sum += wt * cdiff(fast_hist, j);
+                spec_fast_sum += wt * cspec(fast_hist, j);
+              }
+            }
+          }
+        valid = weight_sum > 0.00390625f;
+        if (valid) {
+          float w_sum_inv = rcp(weight_sum);
+          diff_history = diff_sum * w_sum_inv;
+          spec_history = spec_sum * w_sum_inv;
+          sec_moments_history = moments_sum * w_sum_inv;
+          history_len = history_len_sum * w_sum_inv;
+          diff_fast_history = diff_fast_sum * w_sum_inv;
+          spec_fast_history = spec_fast_sum * w_sum_inv;
+        }
+      }
+      if (!valid) {
+        diff_history = spec_history = diff_fast_history = spec_fast_history = F3(0.0f);
+        sec_moments_history = F2(0.0f, 0.0f);
+        history_len = 0.0f;
+      }
+      history_len += HISTORY_LEN_UNIT;
+      float3 diff_source = load_r11g11b10(diff_src[i]);
+      float3 spec_source = load_r11g11b10(spec_src[i]);
+      float2 lumi_source = F2(luminance(diff_source), luminance(spec_source));
+      float2 sec_moments_source = lumi_source * lumi_source;
+      float blurness = sqrtf(saturate(gbuffer.perceptual_roughness * 6.0f));
+      const float BLEND_FACTOR_SPEC = lerp(7.0f / 8.0f, BLEND_FACTOR_DIFF, blurness);
+      const float BLEND_FACTOR_SPEC_FAST = lerp(1.0f, BLEND_FACTOR_FAST, blurness);
+      float ratio = HISTORY_LEN_UNIT / history_len;
+      float2 alpha = F2(hmax(BLEND_FACTOR_DIFF, ratio), hmax(BLEND_FACTOR_SPEC, ratio));
+      float3 diff_filtered = lerp(diff_history, diff_source, alpha.x);
+      float3 spec_filtered = lerp(spec_history, spec_source, alpha.y);
+      float2 sec_moments_filtered = F2(lerp(sec_moments_history.x, sec_moments_source.x, alpha.x),
+                                       lerp(sec_moments_history.y, sec_moments_source.y, alpha.y));
+      float2 alpha_fast = F2(hmax(BLEND_FACTOR_FAST, ratio), hmax(BLEND_FACTOR_SPEC_FAST, ratio));
+      float3 diff_filtered_fast = lerp(diff_fast_history, diff_source, alpha_fast.x);
+      float3 spec_filtered_fast = lerp(spec_fast_history, spec_source, alpha_fast.y);
+      {
+        float3 spec_mean = momentum1_spec;
+        float3 spec_dev = hmax(sqrt3(abs3(momentum2_spec - spec_mean * spec_mean)), 1e-19f);
+        auto dsr_weight = [](float3 color, float3 mean, float3 deviation) {
+          float dist = luminance(abs3(color - mean) / deviation);
+          return exp2_own(-10.0f * dist);
+        };
+        float weight_virtual = dsr_weight(virtual_spec_history, spec_mean, spec_dev);
+        float weight_history = dsr_weight(spec_history, spec_mean, spec_dev);
+        float3 dual = weight_virtual * virtual_spec_history + weight_history * spec_history;
+        float w_sum = weight_virtual + weight_history;
+        dual = dual / hmax(w_sum, 1e-37f);
+        spec_filtered = lerp(dual, spec_source, alpha.y);
+        if (fast_history) {
+          float wv = dsr_weight(virtual_spec_fast_history, spec_mean, spec_dev);
+          float wh = dsr_weight(spec_fast_history, spec_mean, spec_dev);
+          float3 d2 = wv * virtual_spec_fast_history + wh * spec_fast_history;
+          float ws2 = wv + wh;
+          d2 = d2 / hmax(ws2, 1e-37f);
+          spec_filtered_fast = lerp(d2, spec_source, alpha_fast.y);
+        }
+      }
+      out_color[2 * i] = store_r11g11b10(diff_filtered);
+      out_color[2 * i + 1] = store_r11g11b10(spec_filtered);
+      out_mom[i] = store_half2(sec_moments_filtered);
+      out_len[i] = store_unorm8(history_len);
+      if (fast_history) {
+        out_fast[2 * i] = store_r11g11b10(diff_filtered_fast);
+        out_fast[2 * i + 1] = store_r11g11b10(spec_filtered_fast);
+      }
+    }
+}
+
+// Quad remap of the 8x8 groups (relax_disocclusion_fix.hlsl:33-48): the max history
+// length over the aligned 2x2 quad, out-of-range lanes reading 0.
+float quad_max_history(const uint8_t* len, int x, int y, int w, int h) {
+  int x0 = x & ~1, y0 = y & ~1;
+  Tex<uint8_t> t = {len, w, h};
+  float a = load_unorm8(t(x0, y0)), b = load_unorm8(t(x0 + 1, y0));
+  float c = load_unorm8(t(x0, y0 + 1)), d = load_unorm8(t(x0 + 1, y0 + 1));
+  // QuadReadAcrossX then QuadReadAcrossY (the max is order independent).
+  return hmax(hmax(hmax(0.0f, a), hmax(b, c)), d);
+}
+
+// relax_disocclusion_fix.hlsl:27-122 (history-0 pixels: outputs defined as 0).
+void dn_fix(int w, int h, const float* depth_tex, const uint32_t* gbuf, const uint8_t* len_tex,
+            const uint32_t* color, const uint32_t* mom, uint32_t* out_color, uint32_t* out_mom) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float histoty_len = load_unorm8(len_tex[i]);
+      float max_hisotry_len = quad_max_history(len_tex, x, y, w, h);
+      if (histoty_len == 0.0f) {
+        out_color[2 * i] = out_color[2 * i + 1] = 0;
+        out_mom[i] = 0;
+        continue;
+      }
+      histoty_len = max_hisotry_len;
+      if (histoty_len < (4.0f * HISTORY_LEN_UNIT)) {
+        const float depth_center = depth_tex[i];
+        const GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
+        EdgeStoppingFunc es = EdgeStoppingFunc::create(depth_center, gbuffer.fwidth_z, gbuffer.normal);
+        es.sigma_z = 5.0f;
+        es.sigma_n = 32.0f;
+        float2 weight_sum = F2(0.0f, 0.0f), sec_momoents_sum = F2(0.0f, 0.0f);
+        float3 diff_sum = F3(0.0f), spec_sum = F3(0.0f);
+        const int stride = to_int((14.0f * HISTORY_LEN_UNIT) / histoty_len);
+        const int radius = 2;
+        for (int oy = -radius; oy <= radius; oy++)
+          for (int ox = -radius; ox <= radius; ox++) {
+            int cx = ox * stride, cy = oy * stride;
+            int ux = x + cx, uy = y + cy;
+            int qx = std::min(std::max(ux, 0), w - 1), qy = std::min(std::max(uy, 0), h - 1);
+            if (!(ux == qx && uy == qy)) continue;
+            size_t j = (size_t)qy * w + qx;
+            float d = depth_tex[j];
+            float3 normal = load_gbuffer_normal(gbuf, qx, qy, w, h);
+            float2 wt = es.weight(length(F2((float)cx, (float)cy)), d, normal, F2(0.0f, 0.0f));
+            weight_sum += wt;
+            diff_sum += cdiff(color, j) * wt.x;
+            spec_sum += cspec(color, j) * wt.y;
+            sec_momoents_sum += load_half2(mom[j]) * wt;
+          }
+        out_color[2 * i] = store_r11g11b10(diff_sum / weight_sum.x);
+        out_color[2 * i + 1] = store_r11g11b10(spec_sum / weight_sum.y);
+        out_mom[i] = store_half2(sec_momoents_sum / weight_sum);
+      } else {
+        out_color[2 * i] = color[2 * i];
+        out_color[2 * i + 1] = color[2 * i + 1];
+        out_mom[i] = mom[i];
+      }
+    }
+}
+
+// relax_fast_history_clamp.hlsl:11-75 (in place on `color`).
+void dn_fast_clamp(int w, int h, const uint32_t* fast, uint32_t* color) {
+  std::vector<uint32_t> src(color, color + 2 * (size_t)w * h);
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float3 dm1 = F3(0.0f), dm2 = F3(0.0f), sm1 = F3(0.0f), sm2 = F3(0.0f);
+      for (int oy = -1; oy <= 1; oy++)
+        for (int ox = -1; ox <= 1; ox++) {
+          int cx = std::min(std::max(x + ox, 0), w - 1), cy = std::min(std::max(y + oy, 0), h - 1);
+          size_t j = (size_t)cy * w + cx;
+          float3 d = rgb_to_yCoCg(cdiff(fast, j)), s = rgb_to_yCoCg(cspec(fast, j));
+          dm1 += d;
+          dm2 += d * d;
+          sm1 += s;
+          sm2 += s * s;
+        }
+      const float weight_sum = 9.0f;
+      dm1 = dm1 / weight_sum;
+      dm2 = dm2 / weight_sum;
+      sm1 = sm1 / weight_sum;
+      sm2 = sm2 / weight_sum;
+      float3 ddev = sqrt3(dm2 - dm1 * dm1) * 0.75f;
+      float3 sdev = sqrt3(sm2 - sm1 * sm1) * 0.75f;
+      float3 d = rgb_to_yCoCg(cdiff(src.data(), i)), s = rgb_to_yCoCg(cspec(src.data(), i));
+      d = hclamp(d, dm1 - ddev, dm1 + ddev);
+      s = hclamp(s, sm1 - sdev, sm1 + sdev);
+      color[2 * i] = store_r11g11b10(yCoCg_to_rgb(d));
+      color[2 * i + 1] = store_r11g11b10(yCoCg_to_rgb(s));
+    }
+}
+
+// svgf_spatial_fallback_filter.hlsl:25-125 (history-0 pixels: outputs 0).
+void dn_fallback(int w, int h, const float* depth_tex, const uint32_t* gbuf, const uint8_t* len_tex,
+                 const uint32_t* color, const uint32_t* mom, uint32_t* out_color, uint32_t* out_var) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float histoty_len = load_unorm8(len_tex[i]);
+      float max_hisotry_len = quad_max_history(len_tex, x, y, w, h);
+      if (histoty_len == 0.0f) {
+        out_color[2 * i] = out_color[2 * i + 1] = 0;
+        out_var[i] = 0;
+        continue;
+      }
+      histoty_len = max_hisotry_len;
+      float3 diff, spec;
+      float2 sec_moments;
+      if (histoty_len < (4.0f * HISTORY_LEN_UNIT)) {
+        float depth_center = depth_tex[i];
+        GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
+        EdgeStoppingFunc es = EdgeStoppingFunc::create(depth_center, gbuffer.fwidth_z * 3.0f, gbuffer.normal);
+        float2 weight_sum = F2(0.0f, 0.0f), sec_momoents_sum = F2(0.0f, 0.0f);
+        float3 diff_sum = F3(0.0f), spec_sum = F3(0.0f);
+        for (int oy = -3; oy <= 3; oy++)
+          for (int ox = -3; ox <= 3; ox++) {
+            int ux = x + ox, uy = y + oy;
+            int qx = std::min(std::max(ux, 0), w - 1), qy = std::min(std::max(uy, 0), h - 1);
+            if (!(ux == qx && uy == qy)) continue;
+            size_t j = (size_t)qy * w + qx;
+            float d = depth_tex[j];
+            float3 normal = load_gbuffer_normal(gbuf, qx, qy, w, h);
+            float wt = es.weight(length(F2((float)ox, (float)oy)), d, normal, F2(0.0f, 0.0f)).x;
+            weight_sum += F2(wt, wt);
+            diff_sum += cdiff(color, j) * wt;
+            spec_sum += cspec(color, j) * wt;
+            sec_momoents_sum += load_half2(mom[j]) * wt;
+          }
+        diff = diff_sum / weight_sum.x;
+        spec = spec_sum / weight_sum.y;
+        sec_moments = sec_momoents_sum / weight_sum;
+      } else {
+        diff = cdiff(color, i);
+        spec = cspec(color, i);
+        sec_moments = load_half2(mom[i]);
+      }
+      float2 fst = F2(luminance(diff), luminance(spec));
+      float2 variance = F2(hmax(sec_moments.x - fst.x * fst.x, 0.0f), hmax(sec_moments.y - fst.y * fst.y, 0.0f));
+      variance = variance * hmax(1.0f, (4.0f * HISTORY_LEN_UNIT) / histoty_len);
+      out_color[2 * i] = store_r11g11b10(diff);
+      out_color[2 * i + 1] = store_r11g11b10(spec);
+      out_var[i] = store_half2(variance);
+    }
+}
+
+// svgf_atrous_filter.hlsl:23-88.
+void dn_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, const uint32_t* color,
+               const uint32_t* var_tex, uint32_t* out_color, uint32_t* out_var, uint32_t* out_diff,
+               uint32_t* out_spec, int step) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float depth_center = depth_tex[i];
+      GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
+      float3 diff_center = cdiff(color, i), spec_center = cspec(color, i);
+      float2 lumi_center = F2(luminance(diff_center), luminance(spec_center));
+      float2 variance_center = load_half2(var_tex[i]);
+      EdgeStoppingFunc es = EdgeStoppingFunc::create(depth_center, gbuffer.fwidth_z, gbuffer.normal);
+      es.use_lumi = true;
+      es.lumi_center = lumi_center;
+      es.lumi_std = F2(sqrtf(variance_center.x), sqrtf(variance_center.y));
+      const float kernel_weights[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
+      float3 diff_sum = diff_center, spec_sum = spec_center;
+      float2 variance_sum = variance_center;
+      float2 weight_sum = F2(1.0f, 1.0f);
+      for (int oy = -2; oy <= 2; oy++) {
+        float kernel_weight_y = kernel_weights[std::abs(oy)];
+        for (int ox = -2; ox <= 2; ox++) {
+          int cx = ox * step, cy = oy * step;
+          int ux = x + cx, uy = y + cy;
+          int qx = std::min(std::max(ux, 0), w - 1), qy = std::min(std::max(uy, 0), h - 1);
+          bool coord_valid = ux == qx && uy == qy;
+          bool not_center = (ox != 0) && (oy != 0);
+          if (coord_valid && not_center) {
+            float kw = kernel_weight_y * kernel_weights[std::abs(ox)];
+            size_t j = (size_t)qy * w + qx;
+            float3 diff = cdiff(color, j), spec = cspec(color, j);
+            float depth = depth_tex[j];
+            float3 normal = load_gbuffer_normal(gbuf, qx, qy, w, h);
+            float2 lumi = F2(luminance(diff), luminance(spec));
+            float2 e = es.weight(length(F2((float)cx, (float)cy)), depth, normal, lumi);
+            float2 weight = F2(kw * e.x, kw * e.y);
+            float2 weight_var = weight * weight;
+            diff_sum += weight.x * diff;
+            spec_sum += weight.y * spec;
+            variance_sum += weight_var * load_half2(var_tex[j]);
+            weight_sum += weight;
+          }
+        }
+      }
+      uint32_t pd = store_r11g11b10(diff_sum / weight_sum.x);
+      uint32_t ps = store_r11g11b10(spec_sum / weight_sum.y);
+      if (out_color) {
+        out_color[2 * i] = pd;
+        out_color[2 * i + 1] = ps;
+      }
+      if (out_var) out_var[i] = store_half2(variance_sum / (weight_sum * weight_sum));
+      if (out_diff) out_diff[i] = pd;
+      if (out_spec) out_spec[i] = ps;
+    }
+}
+
+// ======================================================= hash grid
+// hash_grid.inc.hlsl:32-105.
+struct VKey {
+  uint32_t hash, checksum;
+};
+VKey vertex_descriptor(float3 pos, float3 nrm, float3 camera_pos, uint32_t bucket_mask, uint32_t key_mode) {
+  float3 delta = pos - camera_pos;
+  float dist_sq = dot(delta, delta);
+  float lodf = hmax(0.5f * log2_own(dist_sq), 0.0f);
+  uint32_t lod = std::min(to_uint(lodf), 31u);
+  float cell_size = (1.0f / 16.0f) * (float)(1u << lod);
+  float inv = rcp(cell_size);
+  int32_t q[3] = {to_int(floorf(pos.x * inv)), to_int(floorf(pos.y * inv)), to_int(floorf(pos.z * inv))};
+  uint32_t pu[3] = {(uint32_t)q[0], (uint32_t)q[1], (uint32_t)q[2]};
+  uint32_t packed[2] = {pu[0] ^ (pu[1] << 22), (pu[1] >> 10) ^ (pu[2] << 22)};
+  XXHash32 hh = XXHash32::init(packed[0]).add(packed[1]).add(lod);
+  XXHash32 hc = XXHash32::init(pu[1]).add(pu[2]).add(pu[0]).add(lod);
+  if (key_mode == 1) {  // normal octant in the key
+    uint32_t oct = (nrm.x < 0.0f ? 1u : 0u) | (nrm.y < 0.0f ? 2u : 0u) | (nrm.z < 0.0f ? 4u : 0u);
+    hh = hh.add(oct);
+    hc = hc.add(oct);
+  }
+  return {hh.eval() & bucket_mask, hc.eval() | 0x1u};
+}
+
+// Query emission (raytrace.inc.hlsl:173-198) from the diffuse candidates.
+void hg_emit(const vlt_frame_params& fp, int w, int h, uint32_t log2_buckets, uint32_t key_mode, uint32_t max_q,
+             const float* depth, const uint32_t* hpn, const uint32_t* rad, uint32_t* queries, uint32_t* count) {
+  uint32_t n = (uint32_t)w * (uint32_t)h;
+  *count = std::min(n, max_q);
+  uint32_t mask = (1u << log2_buckets) - 1u;
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      uint32_t qi = (uint32_t)y * (uint32_t)w + (uint32_t)x;
+      if (qi >= max_q) continue;
+      uint32_t* rec = queries + (size_t)qi * 8;
+      if (depth[qi] == 0.0f) {
+        memset(rec, 0, 32);
+        continue;
+      }
+      HitPosNormal hit = HitPosNormal::decode(hpn[2 * qi], hpn[2 * qi + 1]);
+      VKey k = vertex_descriptor(hit.pos, hit.normal, v3(fp.view_pos), mask, key_mode);
+      rec[0] = asuint(hit.pos.x);
+      rec[1] = asuint(hit.pos.y);
+      rec[2] = asuint(hit.pos.z);
+      rec[3] = normal_encode_oct_u32(hit.normal);
+      rec[4] = k.hash;
+      rec[5] = k.checksum;
+      rec[6] = rad[qi];
+      rec[7] = 0;
+    }
+}
+
+// hash_grid_decay.hlsl:13-129.
+void hg_decay(uint32_t log2_buckets, uint8_t* decay, uint32_t* storage) {
+  uint32_t nb = 1u << log2_buckets;
+  ROWS_PARALLEL
+  for (int64_t bi = 0; bi < (int64_t)nb; ++bi) {
+    const uint32_t addr_offset = (uint32_t)bi * 16u;
+    uint32_t bucket_occupantion_mask = 0;
+    uint32_t local[4] = {0, 0, 0, 0};
+    uint32_t set = 0;
+    for (; set < 4;) {
+      uint32_t set_addr = addr_offset + set * 4;
+      uint32_t packed;
+      memcpy(&packed, decay + set_addr, 4);
+      if (packed == 0) break;
+      uint32_t updated = 0;
+      uint32_t dv = 0;
+      for (uint32_t i = 0; i < 4; ++i) {
+        uint32_t shift = i * 8;
+        dv = (packed >> shift) & 0xFF;
+        if (dv == 0) break;
+        dv = dv - 1;
+        if (dv == 0) {
+          memset(storage + (size_t)(set_addr + i) * 4, 0, 16);
+        } else {
+          updated |= (dv << shift);
+          bucket_occupantion_mask |= (1u << (set * 4 + i));
+        }
+      }
+      local[set] = updated;
+      ++set;
+      if (dv == 0) break;
+    }
+    if (bucket_occupantion_mask != 0) {
+      while (true) {
+        uint32_t last_cell_index = 31u - (uint32_t)__builtin_clz(bucket_occupantion_mask);
+        uint32_t first_space_index = (uint32_t)__builtin_ctz(~bucket_occupantion_mask);
+        if (first_space_index < last_cell_index) {
+          uint32_t src_set = last_cell_index >> 2, dst_set = first_space_index >> 2;
+          uint32_t last_cell_shift = (last_cell_index & 0x3) * 8;
+          uint32_t dv = local[src_set] >> last_cell_shift;
+          local[src_set] ^= (dv << last_cell_shift);
+          uint32_t first_space_shift = (first_space_index & 0x3) * 8;
+          local[dst_set] |= (dv << first_space_shift);
+          memcpy(storage + (size_t)(addr_offset + first_space_index) * 4,
+                 storage + (size_t)(addr_offset + last_cell_index) * 4, 16);
+          memset(storage + (size_t)(addr_offset + last_cell_index) * 4, 0, 16);
+          bucket_occupantion_mask |= (1u << first_space_index);
+          bucket_occupantion_mask ^= (1u << last_cell_index);
+        } else {
+          break;
+        }
+      }
+    }
+    for (uint32_t i = 0; i < set; ++i) memcpy(decay + addr_offset + i * 4, &local[i], 4);
+  }
+}
+
+uint32_t query_bits(uint32_t max_q) {
+  uint32_t b = 0;
+  while ((1u << b) < max_q && b < 30) ++b;
+  return b;
+}
+
+// hash_grid_query_select.hlsl:22-56 with hash_grid_find_or_insert
+// (hash_grid.inc.hlsl:149-184), processing queries sequentially in index order.
+void hg_select(uint32_t log2_buckets, uint32_t max_q, const uint32_t* queries, const uint32_t* count,
+               uint32_t* storage, uint32_t* selection, uint32_t frame_hash) {
+  uint32_t n = std::min(*count, max_q);
+  uint32_t qbits = query_bits(max_q);
+  (void)log2_buckets;
+  for (uint32_t q = 0; q < n; ++q) {
+    const uint32_t* rec = queries + (size_t)q * 8;
+    uint32_t cell_hash = rec[4], cell_checksum = rec[5];
+    if (cell_checksum == 0) continue;  // no query at this index (sky pixel)
+    uint32_t addr_beg = cell_hash << 4, addr_end = addr_beg + 16, addr = addr_beg;
+    bool ok = false;
+    for (; addr < addr_end; ++addr) {
+      uint32_t slot = storage[(size_t)addr * 4];
+      if (slot == cell_checksum) {
+        ok = true;
+        break;
+      }
+      if (slot == 0) {
+        storage[(size_t)addr * 4] = cell_checksum;  // InterlockedCompareExchange wins
+        ok = true;
+        break;
+      }
+    }
+    if (!ok) continue;
+    uint32_t lcg_state = jenkins_hash(q ^ frame_hash);
+    uint32_t rand_u32 = lcg_xorshift(lcg_state);
+    uint32_t score_quantized = rand_u32 & (0xFFFFFFFFu << (qbits + 1));
+    uint32_t compare_word = score_quantized | (0x1u << 31) | q;
+    selection[addr] = std::max(selection[addr], compare_word);
+  }
+}
+
+// hash_grid_query_compact.hlsl (cell order).
+void hg_compact(uint32_t log2_buckets, uint32_t max_q, const uint32_t* selection, uint32_t* idx, uint32_t* addr,
+                uint32_t* count) {
+  uint32_t nc = 16u << log2_buckets;
+  uint32_t mask = (1u << query_bits(max_q)) - 1u;
+  uint32_t k = *count;
+  for (uint32_t c = 0; c < nc; ++c) {
+    if (selection[c] == 0) continue;
+    idx[k] = selection[c] & mask;
+    addr[k] = c;
+    ++k;
+  }
+  *count = k;
+}
+
+// hash_grid_raygen.hlsl:71-86 (the traced radiance comes with the query).
+void hg_update(const uint32_t* queries, const uint32_t* idx, const uint32_t* addr, const uint32_t* count,
+               uint32_t* storage, uint8_t* decay) {
+  for (uint32_t k = 0; k < *count; ++k) {
+    uint32_t q = idx[k], a = addr[k];
+    float3 radiance = load_r11g11b10(queries[(size_t)q * 8 + 6]);
+    uint32_t* cell = storage + (size_t)a * 4;
+    float3 prev_radiance = F3(asfloat(cell[1]), asfloat(cell[2]), asfloat(cell[3]));
+    float blend_factor = 1.0f / 16.0f;
+    float3 blend = radiance * blend_factor + prev_radiance * (1.0f - blend_factor);
+    cell[1] = asuint(blend.x);
+    cell[2] = asuint(blend.y);
+    cell[3] = asuint(blend.z);
+    decay[a] = 10;
+  }
+}
+
+// hash_grid_find (hash_grid.inc.hlsl:126-147).
+void hg_find(const vlt_frame_params& fp, uint32_t log2_buckets, uint32_t key_mode, const uint32_t* storage,
+             uint32_t n, const float* pos, const float* nrm, uint32_t* out_addr, float* out_rad) {
+  for (uint32_t i = 0; i < n; ++i) {
+    VKey k = vertex_descriptor(F3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), F3(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]),
+                               v3(fp.view_pos), (1u << log2_buckets) - 1u, key_mode);
+    uint32_t addr_beg = k.hash << 4, found = 0xFFFFFFFFu;
+    const uint32_t* cell = nullptr;
+    for (uint32_t a = addr_beg; a < addr_beg + 16; ++a) {
+      const uint32_t* c = storage + (size_t)a * 4;
+      if (c[0] == k.checksum) {
+        found = a;
+        cell = c;
+        break;
+      }
+      if (c[0] == 0) break;
+    }
+    out_addr[i] = found;
+    if (out_rad) {
+      out_rad[4 * i] = cell ? asfloat(cell[1]) : 0.0f;
+      out_rad[4 * i + 1] = cell ? asfloat(cell[2]) : 0.0f;
+      out_rad[4 * i + 2] = cell ? asfloat(cell[3]) : 0.0f;
+      out_rad[4 * i + 3] = cell ? 1.0f : 0.0f;
+    }
+  }
+}
+
+// ===================================================== per-view driver
+struct OView {
+  int w, h;
+  vlt_params P;
+  uint32_t log2_buckets, max_q;
+  uint32_t frames = 0;
+  bool denoiser_history = false;
+  // Temporal resources (the RGTemporal handles of RestirRenderer / Denoiser).
+  std::vector<uint32_t> diff_prev, ao_prev, spec_rsv_prev, spec_rad_prev, hist_color, hist_mom, fast_prev;
+  std::vector<float> spec_hp_prev, prev_depth;
+  std::vector<uint8_t> hist_len;
+  std::vector<uint32_t> prev_gbuf;
+  std::vector<uint32_t> hg_storage, hg_queries;
+  std::vector<uint8_t> hg_decay;
+  uint32_t hg_qcount = 0;
+  // Transients kept for inspection.
+  std::vector<uint32_t> diff_light, spec_light, variance, sel, cidx, caddr;
+  std::vector<uint16_t> ray_len, ao_filtered;
+  uint32_t ccount = 0;
+};
+
+struct FrameRand {
+  uint32_t state;
+  uint32_t next() { return state = jenkins_hash(state); }
+};
+
+void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* out) {
+  const vlt_frame_params& fp = *in.params;
+  const int w = v.w, h = v.h;
+  const size_t n = (size_t)w * h;
+  const vlt_params& P = v.P;
+  const bool has_prev = v.frames > 0;
+  const float* prev_depth = v.prev_depth.data();
+  const uint32_t* prev_gbuf = v.prev_gbuf.data();
+  FrameRand frame_rand = {in.frame_index};
+
+  if (P.hg_enable && P.hg_decay) hg_decay(v.log2_buckets, v.hg_decay.data(), v.hg_storage.data());
+  if (has_prev) {  // restir_renderer.rs:357-433
+    uint32_t s_select = frame_rand.next();
+    (void)frame_rand.next();  // raygen seed
+    if (P.hg_enable) {
+      std::fill(v.sel.begin(), v.sel.end(), 0u);
+      hg_select(v.log2_buckets, v.max_q, v.hg_queries.data(), &v.hg_qcount, v.hg_storage.data(), v.sel.data(),
+                s_select);
+      v.ccount = 0;
+      hg_compact(v.log2_buckets, v.max_q, v.sel.data(), v.cidx.data(), v.caddr.data(), &v.ccount);
+      hg_update(v.hg_queries.data(), v.cidx.data(), v.caddr.data(), &v.ccount, v.hg_storage.data(),
+                v.hg_decay.data());
+    }
+  }
+  if (P.hg_enable)
+    hg_emit(fp, w, h, v.log2_buckets, P.hg_key_mode, v.max_q, in.depth, in.diff_hit_pos_normal,
+            in.diff_hit_radiance, v.hg_queries.data(), &v.hg_qcount);
+  (void)frame_rand.next();  // diffuse sample generation
+
+  std::vector<uint32_t> ao_cur(n);
+  ao_gen(fp, w, h, in.diff_hit_pos_normal, in.depth, v.ao_prev.data(), ao_cur.data(), 1u, has_prev ? 1u : 0u,
+         P.ao_radius);
+  ao_filter(w, h, in.depth, ao_cur.data(), v.ao_filtered.data());
+  v.ao_prev.swap(ao_cur);
+
+  std::vector<uint32_t> temp(4 * n), sp(4 * n);
+  diff_temporal(fp, w, h, P, prev_depth, in.depth, in.diff_hit_pos_normal, in.diff_hit_radiance,
+                in.diff_source_pdf, v.diff_prev.data(), temp.data(), frame_rand.next(), has_prev ? 1u : 0u, 1u);
+  for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
+    bool last = k + 1 == P.diff_spatial_passes;
+    diff_spatial(fp, w, h, P, in.gbuffer, in.depth, v.ao_filtered.data(), temp.data(), sp.data(),
+                 last ? v.diff_light.data() : nullptr, frame_rand.next());
+    temp.swap(sp);
+  }
+  v.diff_prev.swap(temp);
+
+  (void)frame_rand.next();  // specular sample generation
+  std::vector<uint32_t> srsv(2 * n), srad(n), srsv2(2 * n), srad2(n);
+  std::vector<float> shp(4 * n), shp2(4 * n);
+  spec_temporal(fp, w, h, P, prev_depth, prev_gbuf, in.depth, in.gbuffer, v.spec_rsv_prev.data(),
+                v.spec_hp_prev.data(), v.spec_rad_prev.data(), in.spec_hit_pos, in.spec_hit_radiance, srsv.data(),
+                shp.data(), srad.data(), frame_rand.next(), has_prev ? 1u : 0u);
+  {
+    const uint32_t* a_rsv = srsv.data();
+    const float* a_hp = shp.data();
+    const uint32_t* a_rad = srad.data();
+    std::vector<uint32_t> b_rsv(2 * n), b_rad(n), c_rsv(2 * n), c_rad(n);
+    std::vector<float> b_hp(4 * n), c_hp(4 * n);
+    bool use_b = true;
+    for (uint32_t k = 0; k < P.spec_spatial_passes; ++k) {
+      bool last = k + 1 == P.spec_spatial_passes;
+      uint32_t* o_rsv = use_b ? b_rsv.data() : c_rsv.data();
+      float* o_hp = use_b ? b_hp.data() : c_hp.data();
+      uint32_t* o_rad = use_b ? b_rad.data() : c_rad.data();
+      spec_spatial(fp, w, h, P, in.gbuffer, in.depth, a_rsv, a_hp, a_rad, last ? v.spec_light.data() : nullptr,
+                   last ? v.ray_len.data() : nullptr, last ? nullptr : o_rsv, last ? nullptr : o_hp,
+                   last ? nullptr : o_rad, frame_rand.next());
+      a_rsv = o_rsv;
+      a_hp = o_hp;
+      a_rad = o_rad;
+      use_b = !use_b;
+    }
+  }
+  v.spec_rsv_prev.swap(srsv);
+  v.spec_hp_prev.swap(shp);
+  v.spec_rad_prev.swap(srad);
+
+  if (P.denoise && has_prev) {
+    std::vector<uint32_t> tcolor(2 * n), tmom(n), tfast(P.fast_history_clamp ? 2 * n : 2);
+    std::vector<uint8_t> tlen(n);
+    dn_temporal(fp, w, h, P, in.depth, in.gbuffer, v.diff_light.data(), v.spec_light.data(), v.ray_len.data(),
+                prev_depth, prev_gbuf, v.hist_color.data(), v.hist_mom.data(), v.hist_len.data(), v.fast_prev.data(),
+                tcolor.data(), tmom.data(), tlen.data(), tfast.data(), v.denoiser_history ? 1u : 0u,
+                P.fast_history_clamp);
+    if (P.disocclusion_fix) {
+      std::vector<uint32_t> fcolor(2 * n), fmom(n);
+      dn_fix(w, h, in.depth, in.gbuffer, tlen.data(), tcolor.data(), tmom.data(), fcolor.data(), fmom.data());
+      tcolor.swap(fcolor);
+      tmom.swap(fmom);
+    }
+    if (P.fast_history_clamp) {
+      dn_fast_clamp(w, h, tfast.data(), tcolor.data());
+      v.fast_prev.swap(tfast);
+    }
+    v.hist_color.swap(tcolor);
+    v.hist_mom.swap(tmom);
+    v.hist_len.swap(tlen);
+    v.denoiser_history = true;
+    std::vector<uint32_t> color(2 * n), color2(2 * n), var2(n);
+    dn_fallback(w, h, in.depth, in.gbuffer, v.hist_len.data(), v.hist_color.data(), v.hist_mom.data(), color.data(),
+                v.variance.data());
+    std::vector<uint32_t> var_src(v.variance);
+    uint32_t iters = std::min(P.atrous_iterations, 5u);
+    for (uint32_t k = 0; k < iters; ++k) {
+      bool last = k + 1 == iters;
+      dn_atrous(w, h, in.depth, in.gbuffer, color.data(), var_src.data(), color2.data(), var2.data(),
+                last && out ? (uint32_t*)out->diffuse : nullptr, last && out ? (uint32_t*)out->specular : nullptr,
+                1 << k);
+      color.swap(color2);
+      var_src.swap(var2);
+    }
+    if (iters == 0 && out) {
+      for (size_t i = 0; i < n; ++i) {
+        if (out->diffuse) ((uint32_t*)out->diffuse)[i] = color[2 * i];
+        if (out->specular) ((uint32_t*)out->specular)[i] = color[2 * i + 1];
+      }
+    }
+  } else {
+    v.denoiser_history = false;
+    if (out && out->diffuse) memcpy(out->diffuse, v.diff_light.data(), 4 * n);
+    if (out && out->specular) memcpy(out->specular, v.spec_light.data(), 4 * n);
+  }
+  if (out && out->raw_diffuse) memcpy(out->raw_diffuse, v.diff_light.data(), 4 * n);
+  if (out && out->raw_specular) memcpy(out->raw_specular, v.spec_light.data(), 4 * n);
+  memcpy(v.prev_depth.data(), in.depth, 4 * n);
+  memcpy(v.prev_gbuf.data(), in.gbuffer, 16 * n);
+  v.frames += 1;
+}
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+void vlto_set_threads(int n) { g_threads = n; }
+int vlto_get_threads(void) { return nthreads(); }
+
+void* vlto_view_create(uint32_t w, uint32_t h, const vlt_params* p) {
+  OView* v = new OView;
+  v->w = (int)w;
+  v->h = (int)h;
+  v->P = *p;
+  v->log2_buckets = p->hg_log2_buckets;
+  uint64_t mq = p->hg_max_queries ? p->hg_max_queries : (uint64_t)w * h;
+  v->max_q = (uint32_t)std::min<uint64_t>(mq, 1u << 30);
+  size_t n = (size_t)w * h;
+  v->diff_prev.assign(4 * n, 0);
+  v->ao_prev.assign(n, 0);
+  v->ao_filtered.assign(n, 0);
+  v->spec_rsv_prev.assign(2 * n, 0);
+  v->spec_hp_prev.assign(4 * n, 0.0f);
+  v->spec_rad_prev.assign(n, 0);
+  v->hist_color.assign(2 * n, 0);
+  v->hist_mom.assign(n, 0);
+  v->hist_len.assign(n, 0);
+  v->fast_prev.assign(p->fast_history_clamp ? 2 * n : 2, 0);
+  v->prev_depth.assign(n, 0.0f);
+  v->prev_gbuf.assign(4 * n, 0);
+  v->diff_light.assign(n, 0);
+  v->spec_light.assign(n, 0);
+  v->ray_len.assign(n, 0);
+  v->variance.assign(n, 0);
+  if (p->hg_enable) {
+    size_t nc = (size_t)16 << v->log2_buckets;
+    v->hg_storage.assign(4 * nc, 0);
+    v->hg_decay.assign(nc, 0);
+    v->hg_queries.assign((size_t)v->max_q * 8, 0);
+    v->sel.assign(nc, 0);
+    size_t ncmp = std::min<size_t>(nc, v->max_q);
+    v->cidx.assign(ncmp, 0);
+    v->caddr.assign(ncmp, 0);
+  }
+  return v;
+}
+
+void vlto_view_destroy(void* h) { delete (OView*)h; }
+
+void vlto_frame_run(void* h, const vlt_frame_inputs* in, const vlt_frame_outputs* out) {
+  frame_run(*(OView*)h, *in, out);
+}
+
+void* vlto_view_buffer(void* h, const char* name, size_t* bytes) {
+  OView& v = *(OView*)h;
+  size_t n = (size_t)v.w * v.h;
+  struct E {
+    const char* nm;
+    void* p;
+    size_t sz;
+  } tab[] = {
+      {"diff_reservoir", v.diff_prev.data(), 16 * n},
+      {"spec_hit_pos", v.spec_hp_prev.data(), 16 * n},
+      {"spec_reservoir", v.spec_rsv_prev.data(), 8 * n},
+      {"spec_radiance", v.spec_rad_prev.data(), 4 * n},
+      {"ao_history", v.ao_prev.data(), 4 * n},
+      {"ao_filtered", v.ao_filtered.data(), 2 * n},
+      {"hist_color", v.hist_color.data(), 8 * n},
+      {"hist_moments", v.hist_mom.data(), 4 * n},
+      {"hist_len", v.hist_len.data(), n},
+      {"variance", v.variance.data(), 4 * n},
+      {"spec_ray_len", v.ray_len.data(), 2 * n},
+      {"raw_diffuse", v.diff_light.data(), 4 * n},
+      {"raw_specular", v.spec_light.data(), 4 * n},
+      {"hg_storage", v.hg_storage.data(), v.hg_storage.size() * 4},
+      {"hg_decay", v.hg_decay.data(), v.hg_decay.size()},
+      {"hg_queries", v.hg_queries.data(), v.hg_queries.size() * 4},
+      {"hg_query_count", &v.hg_qcount, 4},
+      {"hg_selection", v.sel.data(), v.sel.size() * 4},
+      {"prev_depth", v.prev_depth.data(), 4 * n},
+      {"prev_gbuffer", v.prev_gbuf.data(), 16 * n},
+  };
+  for (const E& e : tab)
+    if (strcmp(e.nm, name) == 0) {
+      if (bytes) *bytes = e.sz;
+      return e.p;
+    }
+  return nullptr;
+}
+
+// Per-pass entry points (host pointers; same argument meaning as include/vlt.h).
+void vlto_ao_gen(const vlt_frame_params* fp, uint32_t w, uint32_t h, const uint32_t* hpn, const float* depth,
+                 const uint32_t* prev_ao, uint32_t* ao, uint32_t has_new, uint32_t has_prev, float radius) {
+  ao_gen(*fp, (int)w, (int)h, hpn, depth, prev_ao, ao, has_new, has_prev, radius);
+}
+void vlto_ao_filter(uint32_t w, uint32_t h, const float* depth, const uint32_t* ao, uint16_t* out) {
+  ao_filter((int)w, (int)h, depth, ao, out);
+}
+void vlto_ind_diff_temporal_resample(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p,
+                                     const float* prev_depth, const float* depth, const uint32_t* new_hpn,
+                                     const uint32_t* new_rad, const float* new_pdf, const uint32_t* prev_rsv,
+                                     uint32_t* out, uint32_t frame_rand, uint32_t has_prev, uint32_t has_new) {
+  diff_temporal(*fp, (int)w, (int)h, *p, prev_depth, depth, new_hpn, new_rad, new_pdf, prev_rsv, out, frame_rand,
+                has_prev, has_new);
+}
+void vlto_ind_diff_spatial_resample(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p,
+                                    const uint32_t* gbuf, const float* depth, const uint16_t* ao, const uint32_t* in,
+                                    uint32_t* out, uint32_t* lighting, uint32_t frame_rand) {
+  diff_spatial(*fp, (int)w, (int)h, *p, gbuf, depth, ao, in, out, lighting, frame_rand);
+}
+void vlto_ind_spec_temporal_resample(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p,
+                                     const float* prev_depth, const uint32_t* prev_gbuf, const float* depth,
+                                     const uint32_t* gbuf, const uint32_t* prev_rsv, const float* prev_hp,
+                                     const uint32_t* prev_rad, const float* new_hp, const uint32_t* new_rad,
+                                     uint32_t* out_rsv, float* out_hp, uint32_t* out_rad, uint32_t frame_rand,
+                                     uint32_t has_prev) {
+  spec_temporal(*fp, (int)w, (int)h, *p, prev_depth, prev_gbuf, depth, gbuf, prev_rsv, prev_hp, prev_rad, new_hp,
+                new_rad, out_rsv, out_hp, out_rad, frame_rand, has_prev);
+}
+void vlto_ind_spec_spatial_resample(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p,
+                                    const uint32_t* gbuf, const float* depth, const uint32_t* rsv, const float* hp,
+                                    const uint32_t* rad, uint32_t* lighting, uint16_t* ray_len, uint32_t* out_rsv,
+                                    float* out_hp, uint32_t* out_rad, uint32_t frame_rand) {
+  spec_spatial(*fp, (int)w, (int)h, *p, gbuf, depth, rsv, hp, rad, lighting, ray_len, out_rsv, out_hp, out_rad,
+               frame_rand);
+}
+void vlto_denoise_temporal(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p, const float* depth,
+                           const uint32_t* gbuf, const uint32_t* diff_src, const uint32_t* spec_src,
+                           const uint16_t* ray_len, const float* prev_depth, const uint32_t* prev_gbuf,
+                           const uint32_t* color_hist, const uint32_t* mom_hist, const uint8_t* len_hist,
+                           const uint32_t* fast_hist, uint32_t* out_color, uint32_t* out_mom, uint8_t* out_len,
+                           uint32_t* out_fast, uint32_t has_history, uint32_t fast_on) {
+  dn_temporal(*fp, (int)w, (int)h, *p, depth, gbuf, diff_src, spec_src, ray_len, prev_depth, prev_gbuf, color_hist,
+              mom_hist, len_hist, fast_hist, out_color, out_mom, out_len, out_fast, has_history, fast_on);
+}
+void vlto_denoise_disocclusion_fix(uint32_t w, uint32_t h, const float* depth, const uint32_t* gbuf,
+                                   const uint8_t* len, const uint32_t* color, const uint32_t* mom, uint32_t* out_color,
+                                   uint32_t* out_mom) {
+  dn_fix((int)w, (int)h, depth, gbuf, len, color, mom, out_color, out_mom);
+}
+void vlto_denoise_fast_history_clamp(uint32_t w, uint32_t h, const uint32_t* fast, uint32_t* color) {
+  dn_fast_clamp((int)w, (int)h, fast, color);
+}
+void vlto_denoise_spatial_fallback(uint32_t w, uint32_t h, const float* depth, const uint32_t* gbuf,
+                                   const uint8_t* len, const uint32_t* color, const uint32_t* mom, uint32_t* out_color,
+                                   uint32_t* out_var) {
+  dn_fallback((int)w, (int)h, depth, gbuf, len, color, mom, out_color, out_var);
+}
+void vlto_denoise_atrous(uint32_t w, uint32_t h, const float* depth, const uint32_t* gbuf, const uint32_t* color,
+                         const uint32_t* var, uint32_t* out_color, uint32_t* out_var, int step) {
+  dn_atrous((int)w, (int)h, depth, gbuf, color, var, out_color, out_var, nullptr, nullptr, step);
+}
+void vlto_hg_decay(uint32_t log2_buckets, uint8_t* decay, uint32_t* storage) { hg_decay(log2_buckets, decay, storage); }
+void vlto_hg_emit_queries(const vlt_frame_params* fp, uint32_t w, uint32_t h, uint32_t log2_buckets, uint32_t key_mode,
+                          uint32_t max_q, const float* depth, const uint32_t* hpn, const uint32_t* rad,
+                          uint32_t* queries, uint32_t* count) {
+  hg_emit(*fp, (int)w, (int)h, log2_buckets, key_mode, max_q, depth, hpn, rad, queries, count);
+}
+void vlto_hg_query_select(uint32_t log2_buckets, uint32_t max_q, const uint32_t* queries, const uint32_t* count,
+                          uint32_t* storage, uint32_t* selection, uint32_t frame_hash) {
+  hg_select(log2_buckets, max_q, queries, count, storage, selection, frame_hash);
+}
+void vlto_hg_query_compact(uint32_t log2_buckets, uint32_t max_q, const uint32_t* selection, uint32_t* idx,
+                           uint32_t* addr, uint32_t* count) {
+  hg_compact(log2_buckets, max_q, selection, idx, addr, count);
+}
+void vlto_hg_update(const uint32_t* queries, const uint32_t* idx, const uint32_t* addr, const uint32_t* count,
+                    uint32_t* storage, uint8_t* decay) {
+  hg_update(queries, idx, addr, count, storage, decay);
+}
+void vlto_hg_find(const vlt_frame_params* fp, uint32_t log2_buckets, uint32_t key_mode, const uint32_t* storage,
+                  uint32_t n, const float* pos, const float* nrm, uint32_t* out_addr, float* out_rad) {
+  hg_find(*fp, log2_buckets, key_mode, storage, n, pos, nrm, out_addr, out_rad);
+}
+
+// Elementwise math of the numeric contract, for known-answer tests and for the
+// GPU cross-check of the product's own transcendentals.
+void vlto_math(int fn, const float* x, float* y, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) {
+    switch (fn) {
+      case 0: y[i] = exp2_own(x[i]); break;
+      case 1: y[i] = exp_own(x[i]); break;
+      case 2: y[i] = log2_own(x[i]); break;
+      case 3: y[i] = sin_own(x[i]); break;
+      case 4: y[i] = cos_own(x[i]); break;
+      default: y[i] = 0.0f;
+    }
+  }
+}
+void vlto_codec(int fn, const uint32_t* x, uint32_t* y, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) {
+    switch (fn) {
+      case 0: y[i] = f32tof16(asfloat(x[i])); break;
+      case 1: y[i] = asuint(f16tof32(x[i])); break;
+      case 2: y[i] = to_ufloat(asfloat(x[i]), 6); break;
+      case 3: y[i] = to_ufloat(asfloat(x[i]), 5); break;
+      case 4: y[i] = asuint(from_ufloat(x[i] & 0x7FF, 6)); break;
+      case 5: y[i] = jenkins_hash(x[i]); break;
+      case 6: { uint32_t s = x[i]; y[i] = lcg_xorshift(s); } break;
+      case 7: y[i] = XXHash32::init(x[i]).eval(); break;
+      case 8: y[i] = XXHash32::init(x[i]).add(x[i] ^ 0x9E3779B9u).add(7u).eval(); break;
+      default: y[i] = 0;
+    }
+  }
+}
+void vlto_oct(const float* n3, uint32_t* u16, uint32_t* u32, float* dec16, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) {
+    float3 v = F3(n3[3 * i], n3[3 * i + 1], n3[3 * i + 2]);
+    u16[i] = normal_encode_oct_u16(v);
+    u32[i] = normal_encode_oct_u32(v);
+    float3 d = normal_decode_oct_u16(u16[i]);
+    dec16[3 * i] = d.x;
+    dec16[3 * i + 1] = d.y;
+    dec16[3 * i + 2] = d.z;
+  }
+}
+uint32_t vlto_reservoir_encode(uint32_t M, float W) { return reservoir_simple_encode_32b(M, W); }
+void vlto_reservoir_decode(uint32_t u, uint32_t* M, float* W) { reservoir_simple_decode_32b(u, M, W); }
+
+}  // extern "C"

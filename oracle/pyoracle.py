@@ -1,0 +1,140 @@
+"""ORACLE — test infrastructure only: ctypes front end of libvlt_oracle.so.
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg; the
+product (violet_gb300) never imports it.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+from oracle import build as _build  # noqa: E402
+from violet_gb300 import _ffi  # noqa: E402  (struct layouts of include/vlt.h only)
+
+P = C.c_void_p
+U32 = C.c_uint32
+FP = C.POINTER(_ffi.FrameParams)
+PP = C.POINTER(_ffi.Params)
+
+SIGS = {
+    "vlto_set_threads": (None, [C.c_int]),
+    "vlto_get_threads": (C.c_int, []),
+    "vlto_view_create": (P, [U32, U32, PP]),
+    "vlto_view_destroy": (None, [P]),
+    "vlto_frame_run": (None, [P, C.POINTER(_ffi.FrameInputs), C.POINTER(_ffi.FrameOutputs)]),
+    "vlto_view_buffer": (P, [P, C.c_char_p, C.POINTER(C.c_size_t)]),
+    "vlto_ao_gen": (None, [FP, U32, U32, P, P, P, P, U32, U32, C.c_float]),
+    "vlto_ao_filter": (None, [U32, U32, P, P, P]),
+    "vlto_ind_diff_temporal_resample": (None, [FP, U32, U32, PP, P, P, P, P, P, P, P, U32, U32, U32]),
+    "vlto_ind_diff_spatial_resample": (None, [FP, U32, U32, PP, P, P, P, P, P, P, U32]),
+    "vlto_ind_spec_temporal_resample": (None, [FP, U32, U32, PP, P, P, P, P, P, P, P, P, P, P, P, P, U32, U32]),
+    "vlto_ind_spec_spatial_resample": (None, [FP, U32, U32, PP, P, P, P, P, P, P, P, P, P, P, U32]),
+    "vlto_denoise_temporal": (None, [FP, U32, U32, PP, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, U32, U32]),
+    "vlto_denoise_disocclusion_fix": (None, [U32, U32, P, P, P, P, P, P, P]),
+    "vlto_denoise_fast_history_clamp": (None, [U32, U32, P, P]),
+    "vlto_denoise_spatial_fallback": (None, [U32, U32, P, P, P, P, P, P, P]),
+    "vlto_denoise_atrous": (None, [U32, U32, P, P, P, P, P, P, C.c_int]),
+    "vlto_hg_decay": (None, [U32, P, P]),
+    "vlto_hg_emit_queries": (None, [FP, U32, U32, U32, U32, U32, P, P, P, P, P]),
+    "vlto_hg_query_select": (None, [U32, U32, P, P, P, P, U32]),
+    "vlto_hg_query_compact": (None, [U32, U32, P, P, P, P]),
+    "vlto_hg_update": (None, [P, P, P, P, P, P]),
+    "vlto_hg_find": (None, [FP, U32, U32, P, U32, P, P, P, P]),
+    "vlto_math": (None, [C.c_int, P, P, U32]),
+    "vlto_codec": (None, [C.c_int, P, P, U32]),
+    "vlto_oct": (None, [P, P, P, P, U32]),
+    "vlto_reservoir_encode": (U32, [U32, C.c_float]),
+    "vlto_reservoir_decode": (None, [U32, C.POINTER(U32), C.POINTER(C.c_float)]),
+}
+
+MATH = {"exp2": 0, "exp": 1, "log2": 2, "sin": 3, "cos": 4}
+CODEC = {"f32tof16": 0, "f16tof32": 1, "uf11": 2, "uf10": 3, "uf11_to_f32": 4, "jenkins": 5, "xorshift": 6,
+         "xxh1": 7, "xxh3": 8}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        for k, (r, a) in SIGS.items():
+            f = getattr(L, k)
+            f.restype = r
+            f.argtypes = a
+        _lib = L
+    return _lib
+
+
+def ptr(a):
+    if a is None:
+        return None
+    assert isinstance(a, np.ndarray) and a.flags["C_CONTIGUOUS"], "host arrays must be contiguous numpy arrays"
+    return a.ctypes.data
+
+
+def set_threads(n):
+    lib().vlto_set_threads(int(n))
+
+
+def threads():
+    return int(lib().vlto_get_threads())
+
+
+def math(fn, x):
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.empty_like(x)
+    lib().vlto_math(MATH[fn], ptr(x), ptr(y), x.size)
+    return y
+
+
+def codec(fn, x):
+    x = np.ascontiguousarray(x, dtype=np.uint32)
+    y = np.empty_like(x)
+    lib().vlto_codec(CODEC[fn], ptr(x), ptr(y), x.size)
+    return y
+
+
+class OracleView:
+    """CPU restatement of one view (the same buffer names as violet_gb300.View)."""
+
+    def __init__(self, width, height, params):
+        self.width, self.height = int(width), int(height)
+        self.params = params
+        self.handle = lib().vlto_view_create(self.width, self.height, C.byref(params))
+
+    def run(self, frame_params, frame_index, inputs, outputs=None):
+        fi = _ffi.FrameInputs()
+        fi.params = C.pointer(frame_params)
+        fi.frame_index = int(frame_index) & 0xFFFFFFFF
+        for k in ("depth", "gbuffer", "diff_hit_pos_normal", "diff_hit_radiance", "diff_source_pdf", "spec_hit_pos",
+                  "spec_hit_radiance"):
+            setattr(fi, k, ptr(inputs.get(k)))
+        fo = _ffi.FrameOutputs()
+        for k in ("diffuse", "specular", "raw_diffuse", "raw_specular"):
+            setattr(fo, k, ptr((outputs or {}).get(k)))
+        lib().vlto_frame_run(self.handle, C.byref(fi), C.byref(fo))
+
+    def buffer(self, name, dtype=np.uint8):
+        n = C.c_size_t(0)
+        p = lib().vlto_view_buffer(self.handle, name.encode(), C.byref(n))
+        if not p:
+            raise KeyError(name)
+        raw = (C.c_uint8 * n.value).from_address(p)
+        return np.frombuffer(raw, dtype=np.uint8).copy().view(dtype)
+
+    def close(self):
+        if self.handle:
+            lib().vlto_view_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

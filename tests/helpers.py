@@ -1,0 +1,68 @@
+"""Shared test helpers: host<->device copies through the CUDA runtime, frame upload."""
+import ctypes as C
+
+import numpy as np
+
+import violet_gb300 as vg
+
+_cudart = None
+
+
+def cudart():
+    global _cudart
+    if _cudart is None:
+        _cudart = C.CDLL("libcudart.so.13")
+    return _cudart
+
+
+def d2h(ptr, nbytes, dtype=np.uint8):
+    out = np.empty(nbytes, np.uint8)
+    if nbytes:
+        rc = cudart().cudaMemcpy(C.c_void_p(out.ctypes.data), C.c_void_p(ptr), C.c_size_t(nbytes), 2)
+        assert rc == 0, "cudaMemcpy D2H failed (%d)" % rc
+    return out.view(dtype)
+
+
+def h2d(ptr, arr):
+    arr = np.ascontiguousarray(arr)
+    rc = cudart().cudaMemcpy(C.c_void_p(ptr), C.c_void_p(arr.ctypes.data), C.c_size_t(arr.nbytes), 1)
+    assert rc == 0, "cudaMemcpy H2D failed (%d)" % rc
+
+
+def dev_zeros(nbytes):
+    import torch
+
+    return torch.zeros(max(int(nbytes), 16), dtype=torch.uint8, device="cuda")
+
+
+def upload(host):
+    """Host frame dict (numpy) -> device frame dict (torch uint8 tensors)."""
+    import torch
+
+    return {k: torch.from_numpy(np.ascontiguousarray(v).view(np.uint8)).cuda() for k, v in host.items()}
+
+
+def to_np(t, dtype):
+    return t.cpu().numpy().view(dtype)
+
+
+def float_bits_equal(a, b):
+    """Bitwise equality of float32 arrays, treating every NaN as equal."""
+    a = np.asarray(a).view(np.uint32)
+    b = np.asarray(b).view(np.uint32)
+    na = (a & 0x7FFFFFFF) > 0x7F800000
+    nb = (b & 0x7FFFFFFF) > 0x7F800000
+    return bool(np.all((a == b) | (na & nb)))
+
+
+def first_mismatch(a, b, width=None, rec=1):
+    a = np.asarray(a).reshape(-1)
+    b = np.asarray(b).reshape(-1)
+    idx = np.nonzero(a != b)[0]
+    if idx.size == 0:
+        return None
+    i = int(idx[0])
+    px = i // rec
+    where = (px % width, px // width) if width else px
+    return "%d mismatching words; first at word %d (pixel %s): got 0x%08x expected 0x%08x" % (
+        idx.size, i, where, int(a[i]), int(b[i]))

@@ -1,0 +1,930 @@
+// C ABI: parameter presets, context/view lifetime, the per-frame driver (the pass
+// sequence of RestirRenderer::add_passes and Denoiser::add_passes), and the
+// per-pass entry points.
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <new>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "vlt_internal.h"
+
+namespace vlt {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
+vlt_status cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return VLT_OK;
+  set_last_error(cudaGetErrorString(e));
+  if (e == cudaErrorMemoryAllocation) return VLT_ERR_OUT_OF_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return VLT_ERR_NO_DEVICE;
+  return VLT_ERR_CUDA;
+}
+
+// FrameRand (restir_renderer.rs:130-143): state = frame_index, next = jenkins_hash(state).
+struct FrameRand {
+  uint32_t state;
+  uint32_t next() {
+    state = jenkins_hash(state);
+    return state;
+  }
+};
+
+}  // namespace vlt
+
+using namespace vlt;
+
+struct vlt_ctx {
+  int device;
+};
+
+namespace {
+
+struct Alloc {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+// Resident state of one view (reference storage form).
+struct ViewBuffers {
+  uint32_t* diff_rsv[3];   // uint4 records
+  uint32_t* ao[2];         // half2 {ao, valid}
+  uint16_t* ao_filtered;   // half
+  uint32_t* diff_light;    // R11G11B10
+  float* spec_hp[3];       // float4
+  uint32_t* spec_rsv[3];   // uint2
+  uint32_t* spec_rad[3];   // R11G11B10
+  uint32_t* spec_light;    // R11G11B10
+  uint16_t* ray_len;       // half
+  uint32_t* color[3];      // uint2 {diff, spec}: history, fix output, temporal output
+  uint32_t* mom[3];        // half2
+  uint8_t* len[2];
+  uint32_t* var[3];        // half2: fallback output, a-trous ping-pong
+  uint32_t* color_c;       // fallback output
+  uint32_t* fast[2];       // uint2 fast history
+  uint32_t* hg_storage;
+  uint8_t* hg_decay;
+  uint32_t* hg_queries[2];
+  uint32_t* hg_qcount[2];
+  uint32_t* hg_sel;
+  uint32_t* hg_cidx;
+  uint32_t* hg_caddr;
+  uint32_t* hg_ccount;
+  void* hg_scratch;
+  float* prev_depth;
+  uint32_t* prev_gbuf;
+};
+
+}  // namespace
+
+namespace {
+// Per-pass CUDA-event timers of a view.
+struct Timing {
+  bool enabled = false;
+  cudaStream_t stream = 0;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  struct Rec {
+    const char* name;
+    size_t e0, e1;
+  };
+  std::vector<Rec> pending;
+  std::map<std::string, std::pair<uint32_t, double>> acc;
+  cudaEvent_t next() {
+    if (used == pool.size()) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+      pool.push_back(e);
+    }
+    return pool[used++];
+  }
+  ~Timing() {
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+  }
+};
+}  // namespace
+
+struct vlt_view {
+  vlt_ctx* ctx;
+  uint32_t w, h;
+  vlt_form form;
+  vlt_params p;
+  HashGridDims hg;
+  ViewBuffers b;
+  Alloc pool;
+  uint32_t frames;         // frames run since creation/reset
+  bool denoise_history;    // Denoiser::history is Some
+  bool fast_history_valid; // Denoiser::fast_history is Some
+  int diff_prev, spec_prev, ao_prev, hg_qcur;
+  uint32_t launches;
+  Timing* timing;
+};
+
+namespace {
+
+uint32_t eff_max_queries(const vlt_params& p, uint32_t w, uint32_t h) {
+  uint64_t n = p.hg_max_queries ? p.hg_max_queries : (uint64_t)w * h;
+  if (n > (1u << 30)) n = 1u << 30;
+  return (uint32_t)n;
+}
+
+// Lays out every buffer of a view in one allocation; with base == nullptr only
+// computes the size.
+size_t layout(vlt_view* v, char* base) {
+  size_t off = 0;
+  const size_t n = (size_t)v->w * v->h;
+  auto take = [&](size_t bytes) -> char* {
+    char* r = base ? base + off : nullptr;
+    off += (bytes + 255) & ~(size_t)255;
+    return r;
+  };
+  ViewBuffers& b = v->b;
+  for (int k = 0; k < 3; ++k) b.diff_rsv[k] = (uint32_t*)take(16 * n);
+  for (int k = 0; k < 2; ++k) b.ao[k] = (uint32_t*)take(4 * n);
+  b.ao_filtered = (uint16_t*)take(2 * n);
+  b.diff_light = (uint32_t*)take(4 * n);
+  for (int k = 0; k < 3; ++k) {
+    b.spec_hp[k] = (float*)take(16 * n);
+    b.spec_rsv[k] = (uint32_t*)take(8 * n);
+    b.spec_rad[k] = (uint32_t*)take(4 * n);
+  }
+  b.spec_light = (uint32_t*)take(4 * n);
+  b.ray_len = (uint16_t*)take(2 * n);
+  for (int k = 0; k < 3; ++k) {
+    b.color[k] = (uint32_t*)take(8 * n);
+    b.mom[k] = (uint32_t*)take(4 * n);
+  }
+  for (int k = 0; k < 2; ++k) {
+    b.len[k] = (uint8_t*)take(n);
+    b.fast[k] = (uint32_t*)take(v->p.fast_history_clamp ? 8 * n : 8);
+  }
+  for (int k = 0; k < 3; ++k) b.var[k] = (uint32_t*)take(4 * n);
+  b.color_c = (uint32_t*)take(8 * n);
+  if (v->p.hg_enable) {
+    const HashGridDims& d = v->hg;
+    b.hg_storage = (uint32_t*)take((size_t)d.num_cells() * 16);
+    b.hg_decay = (uint8_t*)take((size_t)d.num_cells());
+    for (int k = 0; k < 2; ++k) {
+      b.hg_queries[k] = (uint32_t*)take((size_t)d.max_queries * 32);
+      b.hg_qcount[k] = (uint32_t*)take(4);
+    }
+    b.hg_sel = (uint32_t*)take((size_t)d.num_cells() * 4);
+    size_t nc = d.max_queries < d.num_cells() ? d.max_queries : d.num_cells();
+    b.hg_cidx = (uint32_t*)take(nc * 4);
+    b.hg_caddr = (uint32_t*)take(nc * 4);
+    b.hg_ccount = (uint32_t*)take(4);
+    b.hg_scratch = (void*)take(hg_select_scratch_bytes(d));
+  } else {
+    b.hg_storage = nullptr;
+    b.hg_decay = nullptr;
+    b.hg_queries[0] = b.hg_queries[1] = nullptr;
+    b.hg_qcount[0] = b.hg_qcount[1] = nullptr;
+    b.hg_sel = b.hg_cidx = b.hg_caddr = b.hg_ccount = nullptr;
+    b.hg_scratch = nullptr;
+  }
+  b.prev_depth = (float*)take(4 * n);
+  b.prev_gbuf = (uint32_t*)take(16 * n);
+  return off;
+}
+
+bool params_ok(const vlt_params* p) {
+  if (!p) return false;
+  if (p->diff_spatial_taps > 64 || p->spec_spatial_taps > 64) return false;
+  if (p->diff_spatial_passes > 8 || p->spec_spatial_passes > 8) return false;
+  if (p->hg_log2_buckets < 4 || p->hg_log2_buckets > 24) return false;
+  if (p->hg_key_mode > 1) return false;
+  if (!(p->history_max_frames >= 1.0f)) return false;
+  return true;
+}
+
+DiffKnobs diff_knobs(const vlt_params& p) {
+  DiffKnobs k;
+  k.m_cap = p.diff_m_cap;
+  k.use_input_pdf = p.use_input_pdf;
+  k.taps = p.diff_spatial_taps;
+  k.radius_px = p.diff_spatial_radius_px;
+  return k;
+}
+
+#define VLT_TRY(expr)                   \
+  do {                                  \
+    vlt_status _s = cuda_status(expr);  \
+    if (_s != VLT_OK) return _s;        \
+  } while (0)
+
+vlt_status reset_state(vlt_view* v, cudaStream_t s) {
+  v->frames = 0;
+  v->denoise_history = false;
+  v->fast_history_valid = false;
+  v->diff_prev = 0;
+  v->spec_prev = 0;
+  v->ao_prev = 0;
+  v->hg_qcur = 0;
+  // Zero everything: cleared hash grid (restir_renderer.rs:296-306), empty queries.
+  VLT_TRY(cudaMemsetAsync(v->pool.p, 0, v->pool.bytes, s));
+  return VLT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void vlt_params_reference(vlt_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->diff_m_cap = 16;
+  p->spec_m_cap = 16;
+  p->use_input_pdf = 0;
+  p->diff_spatial_passes = 1;
+  p->diff_spatial_taps = 9;
+  p->diff_spatial_radius_px = 0.0f;
+  p->spec_spatial_passes = 1;
+  p->spec_spatial_taps = 4;
+  p->spec_spatial_radius_px = 0.0f;
+  p->ao_radius = 2.0f;
+  p->denoise = 1;
+  p->disocclusion_fix = 1;
+  p->fast_history_clamp = 0;
+  p->atrous_iterations = 3;
+  p->history_max_frames = 20.0f;
+  p->hg_enable = 1;
+  p->hg_decay = 1;
+  p->hg_log2_buckets = 16;
+  p->hg_key_mode = 0;
+  p->hg_max_queries = 131072;
+}
+
+void vlt_params_plain(vlt_params* p, int config) {
+  vlt_params_reference(p);
+  if (!p) return;
+  p->diff_m_cap = 20;
+  p->spec_m_cap = 20;
+  p->use_input_pdf = 1;
+  p->diff_spatial_taps = 5;
+  p->diff_spatial_radius_px = 16.0f;
+  p->spec_spatial_taps = 5;
+  p->spec_spatial_radius_px = 16.0f;
+  p->atrous_iterations = 5;
+  p->history_max_frames = 32.0f;
+  if (config >= 1) {
+    p->diff_spatial_passes = 2;
+    p->diff_spatial_taps = 8;
+    p->spec_spatial_passes = 2;
+    p->spec_spatial_taps = 8;
+    p->hg_log2_buckets = 18;  // 2^22 cells
+    p->hg_key_mode = 1;
+    p->hg_max_queries = 0;    // one query per pixel
+  }
+}
+
+const char* vlt_status_string(vlt_status s) {
+  switch (s) {
+    case VLT_OK: return "ok";
+    case VLT_ERR_INVALID_ARG: return "invalid argument";
+    case VLT_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case VLT_ERR_BUDGET_EXCEEDED: return "device-memory budget exceeded";
+    case VLT_ERR_CUDA: return "CUDA error";
+    case VLT_ERR_DEVICE_TIMEOUT: return "device-side wait timed out";
+    case VLT_ERR_BAD_STATE: return "bad state";
+    case VLT_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+const char* vlt_last_error(void) { return g_last_error.c_str(); }
+
+vlt_status vlt_ctx_create(int device, vlt_ctx** out) {
+  if (!out) return VLT_ERR_INVALID_ARG;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    set_last_error(e != cudaSuccess ? cudaGetErrorString(e) : "no CUDA device");
+    return VLT_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return VLT_ERR_INVALID_ARG;
+  VLT_TRY(cudaSetDevice(device));
+  vlt_ctx* c = new (std::nothrow) vlt_ctx;
+  if (!c) return VLT_ERR_OUT_OF_MEMORY;
+  c->device = device;
+  *out = c;
+  return VLT_OK;
+}
+
+vlt_status vlt_ctx_destroy(vlt_ctx* ctx) {
+  delete ctx;
+  return VLT_OK;
+}
+
+size_t vlt_view_device_bytes(uint32_t width, uint32_t height, vlt_form form, const vlt_params* params) {
+  if (!params_ok(params) || width == 0 || height == 0) return 0;
+  vlt_view v;
+  memset(&v, 0, sizeof(v));
+  v.w = width;
+  v.h = height;
+  v.form = form;
+  v.p = *params;
+  v.hg.log2_buckets = params->hg_log2_buckets;
+  v.hg.max_queries = eff_max_queries(*params, width, height);
+  return layout(&v, nullptr);
+}
+
+vlt_status vlt_view_create(vlt_ctx* ctx, uint32_t width, uint32_t height, vlt_form form, const vlt_params* params,
+                           vlt_view** out) {
+  if (!ctx || !out || !params_ok(params) || width == 0 || height == 0 || width > 16384 || height > 16384)
+    return VLT_ERR_INVALID_ARG;
+  if (form != VLT_FORM_REF) {
+    set_last_error("only the reference storage form is built");
+    return VLT_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  VLT_TRY(cudaSetDevice(ctx->device));
+  vlt_view* v = new (std::nothrow) vlt_view;
+  if (!v) return VLT_ERR_OUT_OF_MEMORY;
+  memset(v, 0, sizeof(*v));
+  v->ctx = ctx;
+  v->w = width;
+  v->h = height;
+  v->form = form;
+  v->p = *params;
+  if (v->p.atrous_iterations > 5) v->p.atrous_iterations = 5;  // denoising.rs:73
+  v->hg.log2_buckets = params->hg_log2_buckets;
+  v->hg.max_queries = eff_max_queries(*params, width, height);
+  size_t bytes = layout(v, nullptr);
+  cudaError_t e = cudaMalloc(&v->pool.p, bytes);
+  if (e != cudaSuccess) {
+    delete v;
+    return cuda_status(e);
+  }
+  v->pool.bytes = bytes;
+  layout(v, (char*)v->pool.p);
+  v->timing = new (std::nothrow) Timing;
+  if (!v->timing) {
+    cudaFree(v->pool.p);
+    delete v;
+    return VLT_ERR_OUT_OF_MEMORY;
+  }
+  vlt_status st = reset_state(v, 0);
+  if (st == VLT_OK) st = cuda_status(cudaStreamSynchronize(0));
+  if (st != VLT_OK) {
+    cudaFree(v->pool.p);
+    delete v->timing;
+    delete v;
+    return st;
+  }
+  *out = v;
+  return VLT_OK;
+}
+
+vlt_status vlt_view_destroy(vlt_view* v) {
+  if (!v) return VLT_OK;
+  if (v->pool.p) cudaFree(v->pool.p);
+  delete v->timing;
+  delete v;
+  return VLT_OK;
+}
+
+vlt_status vlt_view_reset(vlt_view* v, void* stream) {
+  if (!v) return VLT_ERR_INVALID_ARG;
+  return reset_state(v, (cudaStream_t)stream);
+}
+
+uint32_t vlt_view_last_launch_count(const vlt_view* v) { return v ? v->launches : 0; }
+
+vlt_status vlt_view_set_timing(vlt_view* v, int enable) {
+  if (!v) return VLT_ERR_INVALID_ARG;
+  v->timing->enabled = enable != 0;
+  return VLT_OK;
+}
+
+uint32_t vlt_view_read_timing(vlt_view* v, vlt_pass_time* out, uint32_t max) {
+  if (!v) return 0;
+  Timing& t = *v->timing;
+  if (!t.pending.empty()) {
+    cudaStreamSynchronize(t.stream);
+    for (const Timing::Rec& r : t.pending) {
+      float ms = 0.0f;
+      if (cudaEventElapsedTime(&ms, t.pool[r.e0], t.pool[r.e1]) != cudaSuccess) ms = 0.0f;
+      auto& a = t.acc[r.name];
+      a.first += 1;
+      a.second += ms;
+    }
+    t.pending.clear();
+    t.used = 0;
+  }
+  uint32_t k = 0;
+  for (auto& kv : t.acc) {
+    if (out && k < max) {
+      memset(out[k].name, 0, sizeof(out[k].name));
+      strncpy(out[k].name, kv.first.c_str(), sizeof(out[k].name) - 1);
+      out[k].launches = kv.second.first;
+      out[k].total_ms = kv.second.second;
+    }
+    ++k;
+  }
+  if (out) t.acc.clear();
+  return k;
+}
+
+void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
+  if (!v || !name) return nullptr;
+  const size_t n = (size_t)v->w * v->h;
+  ViewBuffers& b = v->b;
+  struct E {
+    const char* nm;
+    void* p;
+    size_t sz;
+  };
+  size_t nc = v->p.hg_enable ? v->hg.num_cells() : 0;
+  E tab[] = {
+      {"diff_reservoir", b.diff_rsv[v->diff_prev], 16 * n},
+      {"spec_hit_pos", b.spec_hp[v->spec_prev], 16 * n},
+      {"spec_reservoir", b.spec_rsv[v->spec_prev], 8 * n},
+      {"spec_radiance", b.spec_rad[v->spec_prev], 4 * n},
+      {"ao_history", b.ao[v->ao_prev], 4 * n},
+      {"ao_filtered", b.ao_filtered, 2 * n},
+      {"hist_color", b.color[0], 8 * n},
+      {"hist_moments", b.mom[0], 4 * n},
+      {"hist_len", b.len[0], n},
+      {"variance", b.var[0], 4 * n},
+      {"spec_ray_len", b.ray_len, 2 * n},
+      {"raw_diffuse", b.diff_light, 4 * n},
+      {"raw_specular", b.spec_light, 4 * n},
+      {"hg_storage", b.hg_storage, nc * 16},
+      {"hg_decay", b.hg_decay, nc},
+      {"hg_queries", b.hg_queries[v->hg_qcur], v->p.hg_enable ? (size_t)v->hg.max_queries * 32 : 0},
+      {"hg_query_count", b.hg_qcount[v->hg_qcur], v->p.hg_enable ? (size_t)4 : (size_t)0},
+      {"hg_selection", b.hg_sel, nc * 4},
+      {"prev_depth", b.prev_depth, 4 * n},
+      {"prev_gbuffer", b.prev_gbuf, 16 * n},
+  };
+  for (const E& e : tab) {
+    if (strcmp(e.nm, name) == 0) {
+      if (bytes) *bytes = e.sz;
+      return e.p;
+    }
+  }
+  return nullptr;
+}
+
+vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out, void* stream) {
+  if (!v || !in || !in->params || !in->depth || !in->gbuffer || !in->diff_hit_pos_normal ||
+      !in->diff_hit_radiance || !in->spec_hit_pos || !in->spec_hit_radiance)
+    return VLT_ERR_INVALID_ARG;
+  if (v->p.use_input_pdf && !in->diff_source_pdf) return VLT_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const vlt_frame_params& fp = *in->params;
+  const int w = (int)v->w, h = (int)v->h;
+  const size_t n = (size_t)w * h;
+  ViewBuffers& b = v->b;
+  const vlt_params& P = v->p;
+  uint32_t launches = 0;
+
+  const bool has_prev = v->frames > 0;  // prev depth / gbuffer / indirect diffuse / reservoirs
+  const float* prev_depth = has_prev && in->prev_depth ? in->prev_depth : b.prev_depth;
+  const uint32_t* prev_gbuf = has_prev && in->prev_gbuffer ? in->prev_gbuffer : b.prev_gbuf;
+  FrameRand fr = {in->frame_index};
+  Timing& tm = *v->timing;
+  tm.stream = s;
+#define STAGE(NAME, CALL)                                        \
+  do {                                                           \
+    size_t e0_ = 0;                                              \
+    if (tm.enabled) {                                            \
+      e0_ = tm.used;                                             \
+      cudaEvent_t ev = tm.next();                                \
+      if (ev) cudaEventRecord(ev, s);                            \
+    }                                                            \
+    CALL;                                                        \
+    if (tm.enabled && tm.used == e0_ + 1) {                      \
+      cudaEvent_t ev = tm.next();                                \
+      if (ev) {                                                  \
+        cudaEventRecord(ev, s);                                  \
+        tm.pending.push_back(Timing::Rec{NAME, e0_, e0_ + 1});   \
+      }                                                          \
+    }                                                            \
+  } while (0)
+
+  // Hash-grid radiance cache: decay, then (with history) select/compact/update of
+  // last frame's queries, then this frame's queries.
+  if (P.hg_enable) {
+    if (P.hg_decay) {
+      STAGE("hg_decay", launch_hg_decay(v->hg, b.hg_decay, b.hg_storage, s));
+      ++launches;
+    }
+  }
+  if (has_prev) {
+    uint32_t seed_select = fr.next();
+    uint32_t seed_update = fr.next();
+    (void)seed_update;  // consumed by the (out-of-scope) cache ray generation
+    if (P.hg_enable) {
+      VLT_TRY(cudaMemsetAsync(b.hg_sel, 0, (size_t)v->hg.num_cells() * 4, s));
+      VLT_TRY(cudaMemsetAsync(b.hg_ccount, 0, 4, s));
+      STAGE("hg_select", launch_hg_select(v->hg, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], b.hg_storage,
+                                          b.hg_sel, seed_select, b.hg_scratch, s));
+      STAGE("hg_compact", launch_hg_compact(v->hg, b.hg_sel, b.hg_cidx, b.hg_caddr, b.hg_ccount, s));
+      STAGE("hg_update", launch_hg_update(v->hg, b.hg_queries[v->hg_qcur], b.hg_cidx, b.hg_caddr, b.hg_ccount,
+                                          b.hg_storage, b.hg_decay, s));
+      launches += 6;
+      v->hg_qcur ^= 1;
+    }
+  }
+  if (P.hg_enable) {
+    STAGE("hg_emit", launch_hg_emit(fp, w, h, v->hg, P.hg_key_mode, in->depth, in->diff_hit_pos_normal,
+                                    in->diff_hit_radiance, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], s));
+    ++launches;
+  }
+  (void)fr.next();  // Ind. Diff. Sample Gen.
+
+  // AO.
+  int ao_cur = v->ao_prev ^ 1;
+  STAGE("ao_gen", launch_ao_gen(fp, w, h, in->diff_hit_pos_normal, in->depth, b.ao[v->ao_prev], b.ao[ao_cur], 1u,
+                                has_prev ? 1u : 0u, P.ao_radius, s));
+  STAGE("ao_filter", launch_ao_filter(w, h, in->depth, b.ao[ao_cur], b.ao_filtered, s));
+  launches += 2;
+  v->ao_prev = ao_cur;
+
+  // Indirect diffuse: temporal then spatial pass(es).
+  DiffKnobs dk = diff_knobs(P);
+  int p = v->diff_prev, t = (p + 1) % 3, o = (p + 2) % 3;
+  uint32_t seed_dt = fr.next();
+  STAGE("diff_temporal", launch_diff_temporal(fp, w, h, dk, prev_depth, in->depth, in->diff_hit_pos_normal,
+                                              in->diff_hit_radiance, in->diff_source_pdf, b.diff_rsv[p],
+                                              b.diff_rsv[t], seed_dt, has_prev ? 1u : 0u, 1u, s));
+  ++launches;
+  int src = t, dst = o;
+  for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
+    bool last = k + 1 == P.diff_spatial_passes;
+    uint32_t seed_ds = fr.next();
+    STAGE("diff_spatial", launch_diff_spatial(fp, w, h, dk, in->gbuffer, in->depth, b.ao_filtered, b.diff_rsv[src],
+                                              b.diff_rsv[dst], last ? b.diff_light : nullptr, seed_ds, s));
+    ++launches;
+    std::swap(src, dst);
+  }
+  v->diff_prev = P.diff_spatial_passes ? src : t;
+
+  // Indirect specular.
+  (void)fr.next();  // Ind. Spec. Sample Gen.
+  int sp = v->spec_prev, st = (sp + 1) % 3, so = (sp + 2) % 3;
+  uint32_t seed_st = fr.next();
+  STAGE("spec_temporal", launch_spec_temporal(fp, w, h, P.spec_m_cap, prev_depth, prev_gbuf, in->depth, in->gbuffer,
+                                              b.spec_rsv[sp], b.spec_hp[sp], b.spec_rad[sp], in->spec_hit_pos,
+                                              in->spec_hit_radiance, b.spec_rsv[st], b.spec_hp[st], b.spec_rad[st],
+                                              seed_st, has_prev ? 1u : 0u, s));
+  ++launches;
+  {
+    SpecKnobs sk = {P.spec_spatial_taps, P.spec_spatial_radius_px};
+    int ssrc = st, sdst = so;
+    for (uint32_t k = 0; k < P.spec_spatial_passes; ++k) {
+      bool last = k + 1 == P.spec_spatial_passes;
+      uint32_t seed_ss = fr.next();
+      STAGE("spec_spatial",
+            launch_spec_spatial(fp, w, h, sk, in->gbuffer, in->depth, b.spec_rsv[ssrc], b.spec_hp[ssrc],
+                                b.spec_rad[ssrc], last ? b.spec_light : nullptr, last ? b.ray_len : nullptr,
+                                last ? nullptr : b.spec_rsv[sdst], last ? nullptr : b.spec_hp[sdst],
+                                last ? nullptr : b.spec_rad[sdst], seed_ss, s));
+      ++launches;
+      std::swap(ssrc, sdst);
+    }
+  }
+  // The temporal reservoir is next frame's history (restir_renderer.rs:1018-1022).
+  v->spec_prev = st;
+
+  // Denoiser.
+  const bool run_denoiser = P.denoise && has_prev;
+  if (run_denoiser) {
+    DenoiseKnobs kn = {1.0f / P.history_max_frames, P.fast_history_clamp};
+    uint32_t has_history = v->denoise_history ? 1u : 0u;
+    // color[0]/mom[0]/len[0] = history; color[2]/mom[2]/len[1] = temporal output;
+    // color[1]/mom[1] = fix output.
+    STAGE("dn_temporal", launch_dn_temporal(fp, w, h, kn, in->depth, in->gbuffer, b.diff_light, b.spec_light,
+                                            b.ray_len, prev_depth, prev_gbuf, b.color[0], b.mom[0], b.len[0],
+                                            b.fast[0], b.color[2], b.mom[2], b.len[1], b.fast[1], has_history, s));
+    ++launches;
+    uint32_t* cur_color = b.color[2];
+    if (P.disocclusion_fix) {
+      STAGE("dn_fix", launch_dn_fix(w, h, in->depth, in->gbuffer, b.len[1], b.color[2], b.mom[2], b.color[1],
+                                    b.mom[1], s));
+      ++launches;
+      cur_color = b.color[1];
+    }
+    if (P.fast_history_clamp) {
+      STAGE("dn_fast_clamp", launch_dn_fast_clamp(w, h, b.fast[1], cur_color, s));
+      ++launches;
+      std::swap(b.fast[0], b.fast[1]);
+      v->fast_history_valid = true;
+    } else {
+      v->fast_history_valid = false;
+    }
+    // History feedback before the spatial passes (denoising.rs:209-216).
+    if (cur_color == b.color[1]) {
+      std::swap(b.color[0], b.color[1]);
+      std::swap(b.mom[0], b.mom[1]);
+    } else {
+      std::swap(b.color[0], b.color[2]);
+      std::swap(b.mom[0], b.mom[2]);
+    }
+    std::swap(b.len[0], b.len[1]);
+    v->denoise_history = true;
+    // Now color[0]/mom[0]/len[0] hold this frame's history.
+    STAGE("dn_fallback", launch_dn_fallback(w, h, in->depth, in->gbuffer, b.len[0], b.color[0], b.mom[0], b.color_c,
+                                            b.var[0], s));
+    ++launches;
+    uint32_t* csrc = b.color_c;
+    uint32_t* vsrc = b.var[0];
+    uint32_t* cdst = b.color[2];
+    uint32_t* vdst = b.var[1];
+    const uint32_t iters = P.atrous_iterations;
+    for (uint32_t k = 0; k < iters; ++k) {
+      bool last = k + 1 == iters;
+      uint32_t* od = last && out ? (uint32_t*)out->diffuse : nullptr;
+      uint32_t* os = last && out ? (uint32_t*)out->specular : nullptr;
+      STAGE("dn_atrous", launch_dn_atrous(w, h, in->depth, in->gbuffer, csrc, vsrc, cdst, vdst, od, os, 1 << k, s));
+      ++launches;
+      std::swap(csrc, cdst);
+      uint32_t* vnext = vdst == b.var[1] ? b.var[2] : b.var[1];
+      vsrc = vdst;
+      vdst = vnext;
+    }
+    if (iters == 0 && out && (out->diffuse || out->specular)) {
+      launch_split_color(w, h, csrc, (uint32_t*)out->diffuse, (uint32_t*)out->specular, s);
+      ++launches;
+    }
+  } else {
+    v->denoise_history = false;  // Denoiser::reset
+    v->fast_history_valid = false;
+    if (out && out->diffuse) VLT_TRY(cudaMemcpyAsync(out->diffuse, b.diff_light, 4 * n, cudaMemcpyDeviceToDevice, s));
+    if (out && out->specular)
+      VLT_TRY(cudaMemcpyAsync(out->specular, b.spec_light, 4 * n, cudaMemcpyDeviceToDevice, s));
+  }
+  if (out && out->raw_diffuse)
+    VLT_TRY(cudaMemcpyAsync(out->raw_diffuse, b.diff_light, 4 * n, cudaMemcpyDeviceToDevice, s));
+  if (out && out->raw_specular)
+    VLT_TRY(cudaMemcpyAsync(out->raw_specular, b.spec_light, 4 * n, cudaMemcpyDeviceToDevice, s));
+
+  // Retain depth / G-buffer for the next frame unless the caller keeps them.
+  if (!in->prev_depth) VLT_TRY(cudaMemcpyAsync(b.prev_depth, in->depth, 4 * n, cudaMemcpyDeviceToDevice, s));
+  if (!in->prev_gbuffer) VLT_TRY(cudaMemcpyAsync(b.prev_gbuf, in->gbuffer, 16 * n, cudaMemcpyDeviceToDevice, s));
+  v->frames += 1;
+  v->launches = launches;
+#undef STAGE
+  return cuda_status(cudaGetLastError());
+}
+
+// ------------------------------------------------------ per-pass entry points
+
+static bool dims_ok(uint32_t w, uint32_t h) { return w > 0 && h > 0 && w <= 16384 && h <= 16384; }
+
+vlt_status vlt_ind_diff_temporal_resample(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                                          const vlt_params* params, const float* prev_gbuffer_depth,
+                                          const float* gbuffer_depth, const uint32_t* new_hit_pos_normal,
+                                          const uint32_t* new_hit_radiance, const float* new_source_pdf,
+                                          const uint32_t* prev_reservoir, uint32_t* rw_reservoir,
+                                          uint32_t frame_rand, uint32_t has_prev_frame, uint32_t has_new_sample,
+                                          void* stream) {
+  if (!fp || !params_ok(params) || !dims_ok(width, height) || !gbuffer_depth || !rw_reservoir ||
+      (has_prev_frame && (!prev_gbuffer_depth || !prev_reservoir)) ||
+      (has_new_sample && (!new_hit_pos_normal || !new_hit_radiance)) ||
+      (has_new_sample && params->use_input_pdf && !new_source_pdf))
+    return VLT_ERR_INVALID_ARG;
+  launch_diff_temporal(*fp, width, height, diff_knobs(*params), prev_gbuffer_depth, gbuffer_depth, new_hit_pos_normal,
+                       new_hit_radiance, new_source_pdf, prev_reservoir, rw_reservoir, frame_rand, has_prev_frame,
+                       has_new_sample, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_ao_gen(const vlt_frame_params* fp, uint32_t width, uint32_t height, const uint32_t* hit_pos_normal,
+                      const float* depth_buffer, const uint16_t* prev_ao, uint16_t* rw_ao, uint32_t has_new_sample,
+                      uint32_t has_prev_frame, float radius_ws, void* stream) {
+  if (!fp || !dims_ok(width, height) || !depth_buffer || !rw_ao || (has_new_sample && !hit_pos_normal) ||
+      (has_prev_frame && !prev_ao))
+    return VLT_ERR_INVALID_ARG;
+  launch_ao_gen(*fp, width, height, hit_pos_normal, depth_buffer, (const uint32_t*)prev_ao, (uint32_t*)rw_ao,
+                has_new_sample, has_prev_frame, radius_ws, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_ao_filter(uint32_t width, uint32_t height, const float* depth_buffer, const uint16_t* ao,
+                         uint16_t* rw_filtered_ao, void* stream) {
+  if (!dims_ok(width, height) || !depth_buffer || !ao || !rw_filtered_ao) return VLT_ERR_INVALID_ARG;
+  launch_ao_filter(width, height, depth_buffer, (const uint32_t*)ao, rw_filtered_ao, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_ind_diff_spatial_resample(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                                         const vlt_params* params, const uint32_t* gbuffer_color,
+                                         const float* gbuffer_depth, const uint16_t* ao_texture,
+                                         const uint32_t* temp_reservoir, uint32_t* rw_reservoir,
+                                         uint32_t* rw_lighting, uint32_t frame_rand, void* stream) {
+  if (!fp || !params_ok(params) || !dims_ok(width, height) || !gbuffer_color || !gbuffer_depth || !ao_texture ||
+      !temp_reservoir || !rw_reservoir)
+    return VLT_ERR_INVALID_ARG;
+  launch_diff_spatial(*fp, width, height, diff_knobs(*params), gbuffer_color, gbuffer_depth, ao_texture,
+                      temp_reservoir, rw_reservoir, rw_lighting, frame_rand, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_ind_spec_temporal_resample(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                                          const vlt_params* params, const float* prev_gbuffer_depth,
+                                          const uint32_t* prev_gbuffer_color, const float* gbuffer_depth,
+                                          const uint32_t* gbuffer_color, const uint32_t* prev_reservoir,
+                                          const float* prev_hit_pos, const uint32_t* prev_hit_radiance,
+                                          const float* new_hit_pos, const uint32_t* new_hit_radiance,
+                                          uint32_t* rw_reservoir, float* rw_hit_pos, uint32_t* rw_hit_radiance,
+                                          uint32_t frame_rand, uint32_t has_prev_frame, void* stream) {
+  if (!fp || !params_ok(params) || !dims_ok(width, height) || !gbuffer_depth || !gbuffer_color || !new_hit_pos ||
+      !new_hit_radiance || !rw_reservoir || !rw_hit_pos || !rw_hit_radiance ||
+      (has_prev_frame && (!prev_gbuffer_depth || !prev_gbuffer_color || !prev_reservoir || !prev_hit_pos ||
+                          !prev_hit_radiance)))
+    return VLT_ERR_INVALID_ARG;
+  launch_spec_temporal(*fp, width, height, params->spec_m_cap, prev_gbuffer_depth, prev_gbuffer_color, gbuffer_depth,
+                       gbuffer_color, prev_reservoir, prev_hit_pos, prev_hit_radiance, new_hit_pos, new_hit_radiance,
+                       rw_reservoir, rw_hit_pos, rw_hit_radiance, frame_rand, has_prev_frame, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_ind_spec_spatial_resample(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                                         const vlt_params* params, const uint32_t* gbuffer_color,
+                                         const float* gbuffer_depth, const uint32_t* reservoir, const float* hit_pos,
+                                         const uint32_t* hit_radiance, uint32_t* rw_lighting, uint16_t* rw_ray_len,
+                                         uint32_t* rw_reservoir, float* rw_hit_pos, uint32_t* rw_hit_radiance,
+                                         uint32_t frame_rand, void* stream) {
+  if (!fp || !params_ok(params) || !dims_ok(width, height) || !gbuffer_color || !gbuffer_depth || !reservoir ||
+      !hit_pos || !hit_radiance)
+    return VLT_ERR_INVALID_ARG;
+  if ((rw_reservoir != nullptr) != (rw_hit_pos != nullptr) || (rw_reservoir != nullptr) != (rw_hit_radiance != nullptr))
+    return VLT_ERR_INVALID_ARG;
+  SpecKnobs sk = {params->spec_spatial_taps, params->spec_spatial_radius_px};
+  launch_spec_spatial(*fp, width, height, sk, gbuffer_color, gbuffer_depth, reservoir, hit_pos, hit_radiance,
+                      rw_lighting, rw_ray_len, rw_reservoir, rw_hit_pos, rw_hit_radiance, frame_rand,
+                      (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_denoise_temporal(const vlt_frame_params* fp, uint32_t width, uint32_t height, const vlt_params* params,
+                                const float* depth_texture, const uint32_t* gbuffer_texture,
+                                const uint32_t* diff_source, const uint32_t* spec_source, const uint16_t* spec_ray_len,
+                                const float* prev_depth_texture, const uint32_t* prev_gbuffer_texture,
+                                const uint32_t* color_history, const uint16_t* moments_history,
+                                const uint8_t* history_len_texture, const uint32_t* fast_history,
+                                uint32_t* rw_color, uint16_t* rw_moments, uint8_t* rw_history_len,
+                                uint32_t* rw_fast_history, uint32_t has_history, uint32_t fast_history_on,
+                                void* stream) {
+  if (!fp || !params_ok(params) || !dims_ok(width, height) || !depth_texture || !gbuffer_texture || !diff_source ||
+      !spec_source || !spec_ray_len || !rw_color || !rw_moments || !rw_history_len ||
+      (has_history && (!prev_depth_texture || !prev_gbuffer_texture || !color_history || !moments_history ||
+                       !history_len_texture)) ||
+      (fast_history_on && (!rw_fast_history || (has_history && !fast_history))))
+    return VLT_ERR_INVALID_ARG;
+  DenoiseKnobs kn = {1.0f / params->history_max_frames, fast_history_on};
+  launch_dn_temporal(*fp, width, height, kn, depth_texture, gbuffer_texture, diff_source, spec_source, spec_ray_len,
+                     prev_depth_texture, prev_gbuffer_texture, color_history, (const uint32_t*)moments_history,
+                     history_len_texture, fast_history, rw_color, (uint32_t*)rw_moments, rw_history_len,
+                     rw_fast_history, has_history, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_denoise_disocclusion_fix(uint32_t width, uint32_t height, const float* depth_texture,
+                                        const uint32_t* gbuffer_texture, const uint8_t* history_len_texture,
+                                        const uint32_t* color, const uint16_t* moments, uint32_t* rw_color,
+                                        uint16_t* rw_moments, void* stream) {
+  if (!dims_ok(width, height) || !depth_texture || !gbuffer_texture || !history_len_texture || !color || !moments ||
+      !rw_color || !rw_moments)
+    return VLT_ERR_INVALID_ARG;
+  launch_dn_fix(width, height, depth_texture, gbuffer_texture, history_len_texture, color, (const uint32_t*)moments,
+                rw_color, (uint32_t*)rw_moments, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_denoise_fast_history_clamp(uint32_t width, uint32_t height, const uint32_t* fast_history,
+                                          uint32_t* rw_color, void* stream) {
+  if (!dims_ok(width, height) || !fast_history || !rw_color) return VLT_ERR_INVALID_ARG;
+  launch_dn_fast_clamp(width, height, fast_history, rw_color, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_denoise_spatial_fallback(uint32_t width, uint32_t height, const float* depth_texture,
+                                        const uint32_t* gbuffer_texture, const uint8_t* history_len_texture,
+                                        const uint32_t* color, const uint16_t* moments, uint32_t* rw_color,
+                                        uint16_t* rw_variance, void* stream) {
+  if (!dims_ok(width, height) || !depth_texture || !gbuffer_texture || !history_len_texture || !color || !moments ||
+      !rw_color || !rw_variance)
+    return VLT_ERR_INVALID_ARG;
+  launch_dn_fallback(width, height, depth_texture, gbuffer_texture, history_len_texture, color,
+                     (const uint32_t*)moments, rw_color, (uint32_t*)rw_variance, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_denoise_atrous(uint32_t width, uint32_t height, const float* depth_texture,
+                              const uint32_t* gbuffer_texture, const uint32_t* color, const uint16_t* variance,
+                              uint32_t* rw_color, uint16_t* rw_variance, int32_t step_size, void* stream) {
+  if (!dims_ok(width, height) || !depth_texture || !gbuffer_texture || !color || !variance || !rw_color ||
+      !rw_variance || step_size < 1 || step_size > 4096)
+    return VLT_ERR_INVALID_ARG;
+  launch_dn_atrous(width, height, depth_texture, gbuffer_texture, color, (const uint32_t*)variance, rw_color,
+                   (uint32_t*)rw_variance, nullptr, nullptr, step_size, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+static bool hg_ok(uint32_t log2_buckets) { return log2_buckets >= 4 && log2_buckets <= 24; }
+
+vlt_status vlt_hg_decay(uint32_t log2_buckets, uint8_t* rw_decay, uint32_t* rw_storage, void* stream) {
+  if (!hg_ok(log2_buckets) || !rw_decay || !rw_storage) return VLT_ERR_INVALID_ARG;
+  HashGridDims d = {log2_buckets, 1};
+  launch_hg_decay(d, rw_decay, rw_storage, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+size_t vlt_hg_select_scratch_bytes(uint32_t log2_buckets, uint32_t max_queries) {
+  if (!hg_ok(log2_buckets) || max_queries == 0) return 0;
+  HashGridDims d = {log2_buckets, max_queries};
+  return hg_select_scratch_bytes(d);
+}
+
+vlt_status vlt_hg_query_select(uint32_t log2_buckets, uint32_t max_queries, const uint32_t* queries,
+                               const uint32_t* query_count, uint32_t* rw_storage, uint32_t* rw_selection,
+                               uint32_t frame_hash, void* scratch, void* stream) {
+  if (!hg_ok(log2_buckets) || max_queries == 0 || max_queries > (1u << 30) || !queries || !query_count ||
+      !rw_storage || !rw_selection || !scratch)
+    return VLT_ERR_INVALID_ARG;
+  HashGridDims d = {log2_buckets, max_queries};
+  launch_hg_select(d, queries, query_count, rw_storage, rw_selection, frame_hash, scratch, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_hg_query_compact(uint32_t log2_buckets, uint32_t max_queries, const uint32_t* selection,
+                                uint32_t* rw_compact_query_index, uint32_t* rw_compact_cell_addr,
+                                uint32_t* rw_compact_count, void* stream) {
+  if (!hg_ok(log2_buckets) || max_queries == 0 || !selection || !rw_compact_query_index || !rw_compact_cell_addr ||
+      !rw_compact_count)
+    return VLT_ERR_INVALID_ARG;
+  HashGridDims d = {log2_buckets, max_queries};
+  launch_hg_compact(d, selection, rw_compact_query_index, rw_compact_cell_addr, rw_compact_count,
+                    (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_hg_update(uint32_t max_queries, const uint32_t* queries, const uint32_t* compact_query_index,
+                         const uint32_t* compact_cell_addr, const uint32_t* compact_count, uint32_t* rw_storage,
+                         uint8_t* rw_decay, void* stream) {
+  if (max_queries == 0 || !queries || !compact_query_index || !compact_cell_addr || !compact_count || !rw_storage ||
+      !rw_decay)
+    return VLT_ERR_INVALID_ARG;
+  HashGridDims d = {24, max_queries};
+  launch_hg_update(d, queries, compact_query_index, compact_cell_addr, compact_count, rw_storage, rw_decay,
+                   (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_hg_emit_queries(const vlt_frame_params* fp, uint32_t width, uint32_t height, uint32_t log2_buckets,
+                               uint32_t key_mode, uint32_t max_queries, const float* depth,
+                               const uint32_t* hit_pos_normal, const uint32_t* hit_radiance, uint32_t* rw_queries,
+                               uint32_t* rw_query_count, void* stream) {
+  if (!fp || !dims_ok(width, height) || !hg_ok(log2_buckets) || key_mode > 1 || max_queries == 0 || !depth ||
+      !hit_pos_normal || !hit_radiance || !rw_queries || !rw_query_count)
+    return VLT_ERR_INVALID_ARG;
+  HashGridDims d = {log2_buckets, max_queries};
+  launch_hg_emit(*fp, width, height, d, key_mode, depth, hit_pos_normal, hit_radiance, rw_queries, rw_query_count,
+                 (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_hg_find(const vlt_frame_params* fp, uint32_t log2_buckets, uint32_t key_mode, const uint32_t* storage,
+                       uint32_t n, const float* positions, const float* normals, uint32_t* out_addr,
+                       float* out_radiance, void* stream) {
+  if (!fp || !hg_ok(log2_buckets) || key_mode > 1 || !storage || (n && (!positions || !normals || !out_addr)))
+    return VLT_ERR_INVALID_ARG;
+  HashGridDims d = {log2_buckets, 1};
+  launch_hg_find(*fp, d, key_mode, storage, n, positions, normals, out_addr, out_radiance, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
+
+}  // extern "C"
+
+namespace vlt {
+__global__ void k_diag_math(int fn, const float* __restrict__ x, float* __restrict__ y, uint32_t n) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float v = x[i];
+  float r;
+  switch (fn) {
+    case 0: r = exp2_(v); break;
+    case 1: r = exp_(v); break;
+    case 2: r = log2_(v); break;
+    case 3: r = sin_(v); break;
+    default: r = cos_(v); break;
+  }
+  y[i] = r;
+}
+}  // namespace vlt
+
+extern "C" vlt_status vlt_diag_math(int fn, const float* x, float* y, uint32_t n, void* stream) {
+  if (fn < 0 || fn > 4 || (n && (!x || !y))) return VLT_ERR_INVALID_ARG;
+  if (n == 0) return VLT_OK;
+  vlt::k_diag_math<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(fn, x, y, n);
+  return vlt::cuda_status(cudaGetLastError());
+}

@@ -1,0 +1,415 @@
+// Spatial-hash-grid radiance cache: per-bucket decay/compaction, query emission,
+// deterministic cell insertion + random per-cell query selection, compaction of
+// the selected queries, and the cell radiance update.
+//
+// Insertion order. The shader inserts cells with InterlockedCompareExchange, so
+// which of several racing new cells gets which slot depends on timing. Here the
+// result is defined as if the queries were processed one at a time in query-index
+// order (the CPU restatement does exactly that), and the GPU reproduces it:
+//   S1  every query probes its bucket; a hit selects immediately (atomicMax is
+//       order-independent); a miss with a free slot is counted per bucket;
+//   S2  each bucket with misses gets a contiguous segment of a miss list;
+//   S3  misses are scattered into their bucket's segment (any order);
+//   S4  one warp per bucket repeatedly takes the smallest unresolved query index,
+//       probes/inserts its checksum exactly as the sequential loop would, and
+//       resolves every listed query with that checksum.
+#include "vlt_internal.h"
+
+namespace vlt {
+
+// Query record, 8 words.
+enum { Q_PX = 0, Q_PY = 1, Q_PZ = 2, Q_NRM = 3, Q_HASH = 4, Q_CHECK = 5, Q_RAD = 6, Q_WORDS = 8 };
+// Cell record, 4 words: checksum, radiance xyz.
+
+struct VertexKey {
+  uint32_t hash;
+  uint32_t checksum;
+};
+
+// VertexDescriptor::create/hash/checksum (hash_grid.inc.hlsl:32-105). key_mode 1
+// adds the normal octant to both hashes.
+__device__ __forceinline__ VertexKey vertex_key(f3 pos, f3 nrm, f3 cam, uint32_t bucket_mask, uint32_t key_mode) {
+  f3 d = pos - cam;
+  float dist_sq = dot3(d, d);
+  float lodf = fmax_(0.5f * log2_(dist_sq), 0.0f);
+  uint32_t lod = f2u_rz(lodf);
+  lod = lod < 31u ? lod : 31u;
+  float cell_size = 0.0625f * (float)(1u << lod);
+  float inv = 1.0f / cell_size;
+  int32_t qx = f2i_rz(floor_(pos.x * inv));
+  int32_t qy = f2i_rz(floor_(pos.y * inv));
+  int32_t qz = f2i_rz(floor_(pos.z * inv));
+  uint32_t ux = (uint32_t)qx, uy = (uint32_t)qy, uz = (uint32_t)qz;
+  uint32_t p0 = ux ^ (uy << 22);
+  uint32_t p1 = (uy >> 10) ^ (uz << 22);
+  XXHash32 hh = XXHash32::init(p0).add(p1).add(lod);
+  XXHash32 hc = XXHash32::init(uy).add(uz).add(ux).add(lod);
+  if (key_mode == 1) {
+    uint32_t oct = (nrm.x < 0.0f ? 1u : 0u) | (nrm.y < 0.0f ? 2u : 0u) | (nrm.z < 0.0f ? 4u : 0u);
+    hh = hh.add(oct);
+    hc = hc.add(oct);
+  }
+  VertexKey k;
+  k.hash = hh.eval() & bucket_mask;
+  k.checksum = hc.eval() | 1u;
+  return k;
+}
+
+// --------------------------------------------------------------- emission
+
+__global__ void k_hg_emit(vlt_frame_params fp, int w, int h, uint32_t bucket_mask, uint32_t key_mode,
+                          uint32_t max_q, const float* __restrict__ depth, const uint2* __restrict__ hpn,
+                          const uint32_t* __restrict__ rad, uint32_t* __restrict__ queries,
+                          uint32_t* __restrict__ count) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  uint32_t q = (uint32_t)y * (uint32_t)w + (uint32_t)x;
+  if (q == 0) {
+    uint32_t n = (uint32_t)w * (uint32_t)h;
+    *count = n < max_q ? n : max_q;
+  }
+  if (q >= max_q) return;
+  uint4* rec = (uint4*)(queries + (size_t)q * Q_WORDS);
+  if (depth[q] == 0.0f) {
+    rec[0] = make_uint4(0u, 0u, 0u, 0u);
+    rec[1] = make_uint4(0u, 0u, 0u, 0u);
+    return;
+  }
+  uint2 e = hpn[q];
+  f3 pos = hpn_pos(e.x, e.y);
+  f3 nrm = hpn_normal(e.y);
+  VertexKey k = vertex_key(pos, nrm, mk3(fp.view_pos[0], fp.view_pos[1], fp.view_pos[2]), bucket_mask, key_mode);
+  rec[0] = make_uint4(as_uint(pos.x), as_uint(pos.y), as_uint(pos.z), normal_encode_oct_u32(nrm));
+  rec[1] = make_uint4(k.hash, k.checksum, rad[q], 0u);
+}
+
+// ------------------------------------------------------------------ decay
+
+// hash_grid_decay.hlsl:13-129, one thread per bucket (16 cells).
+__global__ void k_hg_decay(uint32_t num_buckets, uint32_t* __restrict__ decay_words, uint4* __restrict__ storage) {
+  uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= num_buckets) return;
+  const uint32_t base = b * 16u;
+  uint32_t mask = 0;
+  uint32_t local[4] = {0u, 0u, 0u, 0u};
+  uint32_t set = 0;
+  while (set < 4u) {
+    uint32_t set_addr = base + set * 4u;
+    uint32_t packed = decay_words[set_addr >> 2];
+    if (packed == 0u) break;
+    uint32_t updated = 0;
+    uint32_t dv = 0;
+    for (uint32_t i = 0; i < 4u; ++i) {
+      uint32_t sh = i * 8u;
+      dv = (packed >> sh) & 0xFFu;
+      if (dv == 0u) break;
+      dv = dv - 1u;
+      if (dv == 0u) {
+        storage[set_addr + i] = make_uint4(0u, 0u, 0u, 0u);
+      } else {
+        updated |= dv << sh;
+        mask |= 1u << (set * 4u + i);
+      }
+    }
+    local[set] = updated;
+    ++set;
+    if (dv == 0u) break;
+  }
+  if (mask != 0u) {
+    while (true) {
+      uint32_t last = 31u - (uint32_t)__clz(mask);
+      uint32_t first = (uint32_t)__ffs(~mask) - 1u;
+      if (first < last) {
+        uint32_t src = last >> 2, dst = first >> 2;
+        uint32_t lsh = (last & 3u) * 8u;
+        uint32_t dv = local[src] >> lsh;
+        local[src] ^= dv << lsh;
+        uint32_t fsh = (first & 3u) * 8u;
+        local[dst] |= dv << fsh;
+        storage[base + first] = storage[base + last];
+        storage[base + last] = make_uint4(0u, 0u, 0u, 0u);
+        mask |= 1u << first;
+        mask ^= 1u << last;
+      } else {
+        break;
+      }
+    }
+  }
+  for (uint32_t i = 0; i < set; ++i) decay_words[(base >> 2) + i] = local[i];
+}
+
+// ------------------------------------------------------------------ select
+
+struct SelectScratch {
+  uint32_t* need_count;   // [num_buckets]
+  uint32_t* need_offset;  // [num_buckets]
+  uint32_t* total;        // [1]
+  uint32_t* list;         // [max_queries]
+};
+
+__host__ __device__ inline size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
+
+static SelectScratch carve(const HashGridDims& d, void* base) {
+  SelectScratch s;
+  char* p = (char*)base;
+  s.need_count = (uint32_t*)p;
+  p += align256((size_t)d.num_buckets() * 4);
+  s.need_offset = (uint32_t*)p;
+  p += align256((size_t)d.num_buckets() * 4);
+  s.total = (uint32_t*)p;
+  p += 256;
+  s.list = (uint32_t*)p;
+  return s;
+}
+
+size_t hg_select_scratch_bytes(const HashGridDims& d) {
+  return 2 * align256((size_t)d.num_buckets() * 4) + 256 + align256((size_t)d.max_queries * 4);
+}
+
+__device__ __forceinline__ uint32_t select_word(uint32_t q, uint32_t frame_hash, uint32_t qbits) {
+  uint32_t st = jenkins_hash(q ^ frame_hash);
+  uint32_t r = lcg_xorshift(st);
+  uint32_t score = r & (0xFFFFFFFFu << (qbits + 1u));
+  return score | 0x80000000u | q;
+}
+
+// Probe of hash_grid_find_or_insert before any insertion: 0..15 = hit slot,
+// 16 = needs an insertion (an empty slot exists), 17 = bucket full.
+__device__ __forceinline__ uint32_t probe(const uint4* __restrict__ storage, uint32_t base, uint32_t c) {
+  for (uint32_t k = 0; k < 16u; ++k) {
+    uint32_t cs = storage[base + k].x;
+    if (cs == c) return k;
+    if (cs == 0u) return 16u;
+  }
+  return 17u;
+}
+
+__global__ void k_hg_sel_probe(uint32_t max_q, const uint32_t* __restrict__ queries,
+                               const uint32_t* __restrict__ count, const uint4* __restrict__ storage,
+                               uint32_t* __restrict__ selection, uint32_t frame_hash, uint32_t qbits,
+                               uint32_t* __restrict__ need_count) {
+  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t n = *count;
+  n = n < max_q ? n : max_q;
+  if (q >= n) return;
+  uint4 rec1 = ((const uint4*)(queries + (size_t)q * Q_WORDS))[1];
+  uint32_t c = rec1.y;
+  if (c == 0u) return;
+  uint32_t base = rec1.x * 16u;
+  uint32_t k = probe(storage, base, c);
+  if (k < 16u) {
+    atomicMax(selection + base + k, select_word(q, frame_hash, qbits));
+  } else if (k == 16u) {
+    atomicAdd(need_count + rec1.x, 1u);
+  }
+}
+
+__global__ void k_hg_sel_alloc(uint32_t num_buckets, uint32_t* __restrict__ need_count,
+                               uint32_t* __restrict__ need_offset, uint32_t* __restrict__ total) {
+  uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= num_buckets) return;
+  uint32_t n = need_count[b];
+  if (n == 0u) return;
+  need_offset[b] = atomicAdd(total, n);
+  need_count[b] = 0u;
+}
+
+__global__ void k_hg_sel_scatter(uint32_t max_q, const uint32_t* __restrict__ queries,
+                                 const uint32_t* __restrict__ count, const uint4* __restrict__ storage,
+                                 uint32_t* __restrict__ need_count, const uint32_t* __restrict__ need_offset,
+                                 uint32_t* __restrict__ list) {
+  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t n = *count;
+  n = n < max_q ? n : max_q;
+  if (q >= n) return;
+  uint4 rec1 = ((const uint4*)(queries + (size_t)q * Q_WORDS))[1];
+  uint32_t c = rec1.y;
+  if (c == 0u) return;
+  uint32_t base = rec1.x * 16u;
+  if (probe(storage, base, c) != 16u) return;
+  uint32_t pos = atomicAdd(need_count + rec1.x, 1u);
+  list[need_offset[rec1.x] + pos] = q;
+}
+
+// One warp per bucket: sequential-order insertion (see the file comment).
+__global__ void k_hg_sel_resolve(uint32_t num_buckets, const uint32_t* __restrict__ queries,
+                                 uint4* __restrict__ storage, uint32_t* __restrict__ selection,
+                                 const uint32_t* __restrict__ need_count, const uint32_t* __restrict__ need_offset,
+                                 uint32_t* __restrict__ list, uint32_t frame_hash, uint32_t qbits) {
+  uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  uint32_t lane = threadIdx.x & 31u;
+  if (warp >= num_buckets) return;
+  uint32_t n = need_count[warp];
+  if (n == 0u) return;
+  uint32_t off = need_offset[warp];
+  uint32_t base = warp * 16u;
+  uint32_t cs = lane < 16u ? storage[base + lane].x : 0xFFFFFFFFu;  // lanes >= 16 never match
+  const uint32_t RESOLVED = 0x80000000u;
+  for (int round = 0; round < 17; ++round) {
+    uint32_t qmin = 0xFFFFFFFFu;
+    for (uint32_t j = lane; j < n; j += 32u) {
+      uint32_t q = list[off + j];
+      if (!(q & RESOLVED)) qmin = q < qmin ? q : qmin;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      uint32_t other = __shfl_xor_sync(0xFFFFFFFFu, qmin, o);
+      qmin = other < qmin ? other : qmin;
+    }
+    if (qmin == 0xFFFFFFFFu) break;
+    uint32_t c = queries[(size_t)qmin * Q_WORDS + Q_CHECK];
+    uint32_t hit = __ballot_sync(0xFFFFFFFFu, lane < 16u && (cs == c || cs == 0u));
+    if (hit == 0u) break;  // bucket full: every remaining query fails
+    uint32_t k = (uint32_t)__ffs(hit) - 1u;
+    uint32_t kcs = __shfl_sync(0xFFFFFFFFu, cs, k);
+    if (kcs == 0u) {
+      if (lane == k) {
+        cs = c;
+        storage[base + k].x = c;
+      }
+    }
+    for (uint32_t j = lane; j < n; j += 32u) {
+      uint32_t q = list[off + j];
+      if (q & RESOLVED) continue;
+      if (queries[(size_t)q * Q_WORDS + Q_CHECK] != c) continue;
+      atomicMax(selection + base + k, select_word(q, frame_hash, qbits));
+      list[off + j] = q | RESOLVED;
+    }
+    __syncwarp();
+  }
+}
+
+// ----------------------------------------------------------------- compact
+
+// hash_grid_query_compact.hlsl:23-63: block-local append in cell order, one
+// global atomic per block.
+__global__ void __launch_bounds__(256) k_hg_compact(uint32_t num_cells, uint32_t qmask,
+                                                     const uint32_t* __restrict__ selection,
+                                                     uint32_t* __restrict__ idx, uint32_t* __restrict__ addr,
+                                                     uint32_t* __restrict__ count) {
+  __shared__ uint32_t warp_cnt[8];
+  __shared__ uint32_t block_base;
+  uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t sel = c < num_cells ? selection[c] : 0u;
+  uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+  uint32_t bal = __ballot_sync(0xFFFFFFFFu, sel != 0u);
+  if (lane == 0) warp_cnt[wid] = __popc(bal);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0;
+    for (int k = 0; k < 8; ++k) {
+      uint32_t v = warp_cnt[k];
+      warp_cnt[k] = tot;
+      tot += v;
+    }
+    block_base = tot ? atomicAdd(count, tot) : 0u;
+  }
+  __syncthreads();
+  if (sel != 0u) {
+    uint32_t pos = block_base + warp_cnt[wid] + __popc(bal & ((1u << lane) - 1u));
+    idx[pos] = sel & qmask;
+    addr[pos] = c;
+  }
+}
+
+// ------------------------------------------------------------------ update
+
+// hash_grid_raygen.hlsl:71-86 with the traced radiance supplied by the query.
+__global__ void k_hg_update(const uint32_t* __restrict__ queries, const uint32_t* __restrict__ idx,
+                            const uint32_t* __restrict__ addr, const uint32_t* __restrict__ count,
+                            uint4* __restrict__ storage, uint8_t* __restrict__ decay) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *count) return;
+  uint32_t q = idx[k], a = addr[k];
+  f3 L = unpack_r11g11b10(queries[(size_t)q * Q_WORDS + Q_RAD]);
+  uint4 cell = storage[a];
+  f3 prev = mk3(as_float(cell.y), as_float(cell.z), as_float(cell.w));
+  const float bf = 1.0f / 16.0f;
+  f3 bl = L * bf + prev * (1.0f - bf);
+  storage[a] = make_uint4(cell.x, as_uint(bl.x), as_uint(bl.y), as_uint(bl.z));
+  decay[a] = 10;
+}
+
+// ------------------------------------------------------------------- find
+
+__global__ void k_hg_find(vlt_frame_params fp, uint32_t bucket_mask, uint32_t key_mode,
+                          const uint4* __restrict__ storage, uint32_t n, const float* __restrict__ pos,
+                          const float* __restrict__ nrm, uint32_t* __restrict__ out_addr,
+                          float4* __restrict__ out_rad) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  f3 p = mk3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+  f3 nn = mk3(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+  VertexKey k = vertex_key(p, nn, mk3(fp.view_pos[0], fp.view_pos[1], fp.view_pos[2]), bucket_mask, key_mode);
+  uint32_t base = k.hash * 16u;
+  uint32_t found = 0xFFFFFFFFu;
+  uint4 cell = make_uint4(0u, 0u, 0u, 0u);
+  for (uint32_t s = 0; s < 16u; ++s) {
+    uint4 c = storage[base + s];
+    if (c.x == k.checksum) {
+      found = base + s;
+      cell = c;
+      break;
+    }
+    if (c.x == 0u) break;
+  }
+  out_addr[i] = found;
+  if (out_rad)
+    out_rad[i] = make_float4(as_float(cell.y), as_float(cell.z), as_float(cell.w), found != 0xFFFFFFFFu ? 1.0f : 0.0f);
+}
+
+// --------------------------------------------------------------- launchers
+
+void launch_hg_emit(const vlt_frame_params& fp, int w, int h, const HashGridDims& d, uint32_t key_mode,
+                    const float* depth, const uint32_t* hpn, const uint32_t* rad, uint32_t* queries,
+                    uint32_t* count, cudaStream_t s) {
+  dim3 blk(32, 4, 1);
+  k_hg_emit<<<grid2d(w, h, blk), blk, 0, s>>>(fp, w, h, d.num_buckets() - 1u, key_mode, d.max_queries, depth,
+                                               (const uint2*)hpn, rad, queries, count);
+}
+
+void launch_hg_decay(const HashGridDims& d, uint8_t* decay, uint32_t* storage, cudaStream_t s) {
+  uint32_t nb = d.num_buckets();
+  k_hg_decay<<<(nb + 127) / 128, 128, 0, s>>>(nb, (uint32_t*)decay, (uint4*)storage);
+}
+
+void launch_hg_select(const HashGridDims& d, const uint32_t* queries, const uint32_t* count, uint32_t* storage,
+                      uint32_t* selection, uint32_t frame_hash, void* scratch, cudaStream_t s) {
+  SelectScratch sc = carve(d, scratch);
+  uint32_t nb = d.num_buckets();
+  uint32_t qb = d.query_bits();
+  cudaMemsetAsync(sc.need_count, 0, (size_t)nb * 4, s);
+  cudaMemsetAsync(sc.total, 0, 4, s);
+  uint32_t nq = d.max_queries;
+  k_hg_sel_probe<<<(nq + 255) / 256, 256, 0, s>>>(nq, queries, count, (const uint4*)storage, selection, frame_hash,
+                                                   qb, sc.need_count);
+  k_hg_sel_alloc<<<(nb + 255) / 256, 256, 0, s>>>(nb, sc.need_count, sc.need_offset, sc.total);
+  k_hg_sel_scatter<<<(nq + 255) / 256, 256, 0, s>>>(nq, queries, count, (const uint4*)storage, sc.need_count,
+                                                     sc.need_offset, sc.list);
+  uint64_t threads = (uint64_t)nb * 32u;
+  k_hg_sel_resolve<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(nb, queries, (uint4*)storage, selection,
+                                                                      sc.need_count, sc.need_offset, sc.list,
+                                                                      frame_hash, qb);
+}
+
+void launch_hg_compact(const HashGridDims& d, const uint32_t* selection, uint32_t* idx, uint32_t* addr,
+                       uint32_t* count, cudaStream_t s) {
+  uint32_t nc = d.num_cells();
+  uint32_t qmask = (1u << d.query_bits()) - 1u;
+  k_hg_compact<<<(nc + 255) / 256, 256, 0, s>>>(nc, qmask, selection, idx, addr, count);
+}
+
+void launch_hg_update(const HashGridDims& d, const uint32_t* queries, const uint32_t* idx, const uint32_t* addr,
+                      const uint32_t* count, uint32_t* storage, uint8_t* decay, cudaStream_t s) {
+  uint32_t nmax = d.max_queries < d.num_cells() ? d.max_queries : d.num_cells();
+  k_hg_update<<<(nmax + 255) / 256, 256, 0, s>>>(queries, idx, addr, count, (uint4*)storage, decay);
+}
+
+void launch_hg_find(const vlt_frame_params& fp, const HashGridDims& d, uint32_t key_mode, const uint32_t* storage,
+                    uint32_t n, const float* pos, const float* nrm, uint32_t* out_addr, float* out_rad,
+                    cudaStream_t s) {
+  if (n == 0) return;
+  k_hg_find<<<(n + 255) / 256, 256, 0, s>>>(fp, d.num_buckets() - 1u, key_mode, (const uint4*)storage, n, pos, nrm,
+                                            out_addr, (float4*)out_rad);
+}
+
+}  // namespace vlt

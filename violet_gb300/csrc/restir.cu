@@ -1,0 +1,643 @@
+// ReSTIR GI passes: indirect-diffuse temporal and spatial resampling, ray-traced AO
+// temporal accumulation and filter, indirect-specular temporal and spatial
+// resampling. One thread per pixel; records are loaded as packed 128/64/32-bit
+// words; every random-walk decision follows the binary32 contract of vlt_math.cuh.
+#include "vlt_internal.h"
+
+namespace vlt {
+
+// ---------------------------------------------------------------- AO gen
+
+// raytraced_ao_gen.hlsl:18-81. AO history is {ao, valid} in half2 (the x and a
+// channels of the reference's RGBA16F texture).
+__global__ void __launch_bounds__(128) k_ao_gen(vlt_frame_params fp, int w, int h,
+                                                 const uint2* __restrict__ hit_pos_normal,
+                                                 const float* __restrict__ depth_buf,
+                                                 const uint32_t* __restrict__ prev_ao, uint32_t* __restrict__ ao,
+                                                 uint32_t has_new_sample, uint32_t has_prev_frame, float radius_ws) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  float depth = depth_buf[i];
+  if (depth == 0.0f) {
+    ao[i] = 0u;
+    return;
+  }
+  f3 position = depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+  f4 hpos = mul44(fp.view_proj, mk4(position.x, position.y, position.z, 1.0f));
+  f2 ndc = mk2(hpos.x / hpos.w - fp.jitter[0], hpos.y / hpos.w - fp.jitter[1]);
+  f4 hr = mul44(fp.prev_view_proj, mk4(position.x, position.y, position.z, 1.0f));
+  f2 ndc_r = mk2(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3]);
+  f2 mv = mk2((ndc.x - ndc_r.x) * 0.5f, (ndc.y - ndc_r.y) * 0.5f);
+  f2 src_uv = mk2(((float)x + 0.5f) / (float)w, ((float)y + 0.5f) / (float)h);
+  f2 huv = mk2(src_uv.x - mv.x, src_uv.y - mv.y);
+  float hx = 0.0f, ha = 0.0f;
+  bool in_last = huv.x == saturate(huv.x) && huv.y == saturate(huv.y);
+  if (in_last && has_prev_frame) {
+    BilinearTaps t = bilinear_taps(huv, w, h);
+    f2 a = ld_half2(prev_ao, t.x0, t.y0, w, h), b = ld_half2(prev_ao, t.x1, t.y0, w, h);
+    f2 c = ld_half2(prev_ao, t.x0, t.y1, w, h), d = ld_half2(prev_ao, t.x1, t.y1, w, h);
+    hx = bilerp(a.x, b.x, c.x, d.x, t.fx, t.fy);
+    ha = bilerp(a.y, b.y, c.y, d.y, t.fx, t.fy);
+  }
+  if (has_new_sample) {
+    uint2 e = hit_pos_normal[i];
+    f3 hp = hpn_pos(e.x, e.y);
+    f3 p2 = depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+    float dist = length3(hp - p2);
+    float a_o = dist < radius_ws ? 0.0f : 1.0f;
+    hx = lerpf(a_o, hx, (31.0f / 32.0f) * ha);
+    ha = 1.0f;
+  } else {
+    hx = ha > 0.0f ? hx : 1.0f;
+  }
+  ao[i] = pack_half2(mk2(hx, ha));
+}
+
+// ---------------------------------------------------------------- AO filter
+
+// raytraced_ao_filter.hlsl:12-70. Taps at min(p + (dx, dy), size) in unsigned
+// arithmetic as the shader computes them (so the left/top edge wraps to an
+// out-of-range coordinate, which reads as zero). Only the x channel is needed
+// downstream, so only it is filtered and stored.
+__global__ void __launch_bounds__(128) k_ao_filter(int w, int h, const float* __restrict__ depth_buf,
+                                                    const uint32_t* __restrict__ ao, uint16_t* __restrict__ out) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  float depth = depth_buf[i];
+  if (depth == 0.0f) {
+    out[i] = 0;
+    return;
+  }
+  float center = f16tof32(ao[i] & 0xFFFFu);
+  float col_med[3], col_min[3], col_max[3];
+  for (int dy = -1; dy <= 1; ++dy) {
+    float row[3];
+    for (int dx = -1; dx <= 1; ++dx) {
+      uint32_t cx = (uint32_t)x + (uint32_t)dx, cy = (uint32_t)y + (uint32_t)dy;
+      cx = cx < (uint32_t)w ? cx : (uint32_t)w;
+      cy = cy < (uint32_t)h ? cy : (uint32_t)h;
+      bool ok = cx < (uint32_t)w && cy < (uint32_t)h;
+      float sd = ok ? depth_buf[(size_t)cy * w + cx] : 0.0f;
+      if (fabs_(depth - sd) > 0.0005f) {
+        row[dx + 1] = center;
+        continue;
+      }
+      row[dx + 1] = ok ? f16tof32(ao[(size_t)cy * w + cx] & 0xFFFFu) : 0.0f;
+    }
+    col_med[dy + 1] = fmin_(fmax_(row[0], row[1]), row[2]);
+    col_min[dy + 1] = fmin_(fmin_(row[0], row[1]), row[2]);
+    col_max[dy + 1] = fmax_(fmax_(row[0], row[1]), row[2]);
+  }
+  float A = fmin_(fmin_(col_max[0], col_max[1]), col_max[2]);
+  float B = fmax_(fmax_(col_min[0], col_min[1]), col_min[2]);
+  float C = fmin_(fmax_(col_med[0], col_med[1]), col_med[2]);
+  float med = fmin_(fmax_(C, A), B);
+  float mn = fmin_(fmin_(col_min[0], col_min[1]), col_min[2]);
+  out[i] = (uint16_t)f32tof16(lerpf(med, mn, 0.5f));
+}
+
+// ------------------------------------------------------ diffuse temporal
+
+// ind_diff_temporal_resample.hlsl:49-200. Record = {M8|W24, HitPosNormal.xy, R11G11B10}.
+__global__ void __launch_bounds__(128) k_diff_temporal(vlt_frame_params fp, int w, int h, DiffKnobs kn,
+                                                        const float* __restrict__ prev_depth,
+                                                        const float* __restrict__ depth_buf,
+                                                        const uint2* __restrict__ new_hpn,
+                                                        const uint32_t* __restrict__ new_rad,
+                                                        const float* __restrict__ new_pdf,
+                                                        const uint4* __restrict__ prev_rsv, uint4* __restrict__ out,
+                                                        uint32_t frame_rand, uint32_t has_prev_frame,
+                                                        uint32_t has_new_sample) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  float depth = depth_buf[i];
+  f3 pos = depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+  f4 hr = mul44(fp.prev_view_proj, mk4(pos.x, pos.y, pos.z, 1.0f));
+  f3 ndc = mk3(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3], hr.z / hr.w - 0.0f);
+  f2 uv = mk2(ndc.x * 0.5f + 0.5f, ndc.y * 0.5f + 0.5f);
+  bool in_view = fabs_(ndc.x) < 1.0f && fabs_(ndc.y) < 1.0f;
+  bool sample_prev = has_prev_frame && in_view;
+  if (sample_prev) {
+    float pd = sample_depth(prev_depth, uv, w, h);
+    if (fabs_(pd - ndc.z) > 0.001f) sample_prev = false;
+  }
+  uint32_t M = 0, rad = 0, h0 = 0, h1 = 0;
+  float W = 0.0f;
+  if (sample_prev) {
+    int px = (int)f2u_rz(uv.x * (float)w), py = (int)f2u_rz(uv.y * (float)h);
+    uint4 r = ld(prev_rsv, px, py, w, h);
+    M = rsv_decode_M(r.x);
+    W = rsv_decode_W(r.x);
+    rad = r.w;
+    h0 = r.y;
+    h1 = r.z;
+    if (M == 0) {
+      rad = 0;
+      h0 = h1 = 0;
+    }
+    M = M < kn.m_cap ? M : kn.m_cap;
+  }
+  if (has_new_sample) {
+    float tp = luminance(unpack_r11g11b10(rad));
+    float prev_w = W * tp * (float)M;
+    uint32_t nrad = new_rad[i];
+    float ntp = luminance(unpack_r11g11b10(nrad));
+    float new_w;
+    if (kn.use_input_pdf) {
+      float pdf = new_pdf[i];
+      new_w = pdf > 0.0f ? ntp / pdf : 0.0f;
+    } else {
+      new_w = ntp * VLT_TWO_PI;
+    }
+    uint32_t rng = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
+    float w_sum = prev_w + new_w;
+    float chance = new_w / w_sum;
+    if (lcg_rand(rng) < chance) {
+      uint2 e = new_hpn[i];
+      h0 = e.x;
+      h1 = e.y;
+      rad = nrad;
+      tp = ntp;
+    }
+    M += 1;
+    W = tp > 0.0f ? w_sum / (tp * (float)M) : 0.0f;
+  }
+  out[i] = make_uint4(rsv_encode_32b(M, W), h0, h1, rad);
+}
+
+// ------------------------------------------------------- diffuse spatial
+
+struct DiffSample {
+  uint32_t M;
+  float W;
+  f3 pos, nrm, rad;
+  float tp;
+};
+
+__device__ __forceinline__ DiffSample load_diff(uint4 r, f3 pix_pos, f3 pix_n) {
+  DiffSample s;
+  s.M = rsv_decode_M(r.x);
+  s.W = rsv_decode_W(r.x);
+  s.pos = hpn_pos(r.y, r.z);
+  s.nrm = hpn_normal(r.z);
+  s.rad = unpack_r11g11b10(r.w);
+  float nol = saturate(dot3(pix_n, normalize3(s.pos - pix_pos)));
+  s.tp = nol * luminance(s.rad);
+  return s;
+}
+
+// ind_diff_spatial_resample.hlsl:94-337 (golden-spiral pattern, AO-guided and
+// adaptive radius, plane-distance test, Jacobian clamped to [0, 1]).
+__global__ void __launch_bounds__(128) k_diff_spatial(vlt_frame_params fp, int w, int h, DiffKnobs kn,
+                                                       const uint32_t* __restrict__ gbuf,
+                                                       const float* __restrict__ depth_buf,
+                                                       const uint16_t* __restrict__ ao_tex,
+                                                       const uint4* __restrict__ in, uint4* __restrict__ out,
+                                                       uint32_t* __restrict__ lighting, uint32_t frame_rand) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  float depth = depth_buf[i];
+  if (depth == 0.0f) {
+    out[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (lighting) lighting[i] = 0u;
+    return;
+  }
+  f3 pos = depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+  f3 nrm = gbuffer_normal(gbuf[(size_t)w * h + i]);
+  float ao = f16tof32(ao_tex[i]);
+  DiffSample r = load_diff(in[i], pos, nrm);
+  float w_sum = r.W * r.tp * (float)r.M;
+  float radius = kn.radius_px > 0.0f ? kn.radius_px : (float)(w < h ? w : h) * 0.05f;
+  radius = fmax_(radius * ao, 1.5f);
+  uint32_t rng = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
+  float rand_angle = lcg_rand(rng) * VLT_TWO_PI;
+  const int n = (int)kn.taps;
+  const float T = 0.6186f * (float)n;
+  for (int it = 0; it < n; ++it) {
+    float theta = VLT_TWO_PI * (((float)it + 1.0f) / (float)n);
+    float rr = VLT_SPIRAL_A * exp_(VLT_SPIRAL_B * theta);
+    float s, c;
+    sincos_(theta * T + rand_angle, &s, &c);
+    float ox = rr * c, oy = rr * s;
+    int nx = x + f2i_rz(ox * radius), ny = y + f2i_rz(oy * radius);
+    nx = nx < 0 ? 0 : (nx > w - 1 ? w - 1 : nx);
+    ny = ny < 0 ? 0 : (ny > h - 1 ? h - 1 : ny);
+    size_t j = (size_t)ny * w + nx;
+    f3 nn = gbuffer_normal(gbuf[(size_t)w * h + j]);
+    float dn = depth_buf[j];
+    bool diff = dot3(nrm, nn) < VLT_COS25;
+    f3 pn = depth_to_position(fp.inv_view_proj, nx, ny, w, h, dn);
+    float dist_to_plane = dot3(pn - pos, nrm);
+    diff = diff || fabs_(dist_to_plane) > 0.05f;
+    if (diff) {
+      radius = fmax_(radius * 0.5f, 1.5f);
+      continue;
+    }
+    DiffSample nb = load_diff(in[j], pos, nrm);
+    f3 qq = pn - nb.pos;
+    f3 rq = pos - nb.pos;
+    float l2qq = dot3(qq, qq);
+    float l2rq = dot3(rq, rq);
+    float cos_rq = dot3(nb.nrm, rq * rsqrt_(l2rq));
+    float cos_qq = dot3(nb.nrm, qq * rsqrt_(l2qq));
+    float jac = (cos_rq / cos_qq) * (l2qq / l2rq);
+    jac = clampf(jac, 0.0f, 10.0f);
+    jac = clampf(jac, 0.0f, 1.0f);
+    float tpn = nb.tp * jac;
+    if (tpn <= 0.0f) continue;
+    nb.M = nb.M < 255u ? nb.M : 255u;
+    float wsn = nb.W * tpn * (float)nb.M;
+    w_sum = w_sum + wsn;
+    float chance = wsn / w_sum;
+    if (lcg_rand(rng) < chance) {
+      r.nrm = nb.nrm;
+      r.pos = nb.pos;
+      r.rad = nb.rad;
+      r.tp = nb.tp;
+    }
+    r.M += nb.M;
+  }
+  if (r.tp > 0.0f) r.W = w_sum / (r.tp * (float)r.M);
+  uint32_t e[2];
+  hpn_encode(r.pos, r.nrm, e);
+  out[i] = make_uint4(rsv_encode_32b(r.M, r.W), e[0], e[1], pack_r11g11b10(r.rad));
+  if (lighting) {
+    f3 dir = normalize3(r.pos - pos);
+    float nol = saturate(dot3(nrm, dir));
+    f3 l = r.rad * (VLT_ONE_OVER_PI * nol * r.W);
+    lighting[i] = pack_r11g11b10(l);
+  }
+}
+
+// --------------------------------------------------- specular target function
+
+// D_GGX (brdf.hlsl:31-35).
+__device__ __forceinline__ float d_ggx(float noh, float roughness) {
+  float a = noh * roughness;
+  float k = roughness / (1.0f - noh * noh + a * a);
+  return k * k * VLT_ONE_OVER_PI;
+}
+
+// (smith_lambda + 1) * cos (ind_spec_temporal_resample.hlsl:48-53).
+__device__ __forceinline__ float lambda_pomc(float c, float roughness) {
+  float r2 = roughness * roughness;
+  return (c + sqrt_((-r2 * c + c) * c + r2)) / 2.0f;
+}
+
+// smith_G2_over_G1_height_correlated_GGX, optimized branch (brdf.hlsl:133-137).
+__device__ __forceinline__ float g2_over_g1(float nol, float nov, float roughness) {
+  float r2 = roughness * roughness;
+  float kv = sqrt_((-r2 * nov + nov) * nov + r2) / nov;
+  float kl = sqrt_((-r2 * nol + nol) * nol + r2) / nol;
+  return (1.0f + kv) / (kv + kl);
+}
+
+__device__ __forceinline__ f3 f_schlick(float u, f3 f0) {
+  float f = pow5(1.0f - u);
+  return mk3(f + f0.x * (1.0f - f), f + f0.y * (1.0f - f), f + f0.z * (1.0f - f));
+}
+
+struct SpecEval {
+  float source_pdf;
+  f3 brdf_nol_over_pdf;
+};
+
+// calc_things (ind_spec_temporal_resample.hlsl:63-144) == SpecTragetFunction::on_sample
+// (ind_spec_spatial_resample.hlsl:69-151).
+__device__ __forceinline__ SpecEval spec_eval(f3 view_pos, f3 pos, f3 n, float pr, f3 f0, f3 hit) {
+  SpecEval e;
+  float roughness = pr * pr;
+  roughness = fmax_(roughness, 0.002f);
+  f3 v = normalize3(view_pos - pos);
+  f3 l = normalize3(hit - pos);
+  f3 hv = normalize3(v + l);
+  float nov = saturate(dot3(n, v));
+  float noh = saturate(dot3(n, hv));
+  float D = d_ggx(noh, roughness);
+  float lp = lambda_pomc(nov, roughness);
+  e.source_pdf = 0.25f * D / lp;
+  float nol = saturate(dot3(n, l));
+  float loh = saturate(dot3(l, hv));
+  f3 F = f_schlick(loh, f0);
+  float g = g2_over_g1(nol, nov, roughness);
+  if (nol <= 0.0f) g = 0.0f;
+  if (nov <= 0.0f) g = 0.0f;
+  e.brdf_nol_over_pdf = F * g;
+  return e;
+}
+
+__device__ __forceinline__ float spec_tf(const SpecEval& e, f3 rad) {
+  return luminance(rad * e.brdf_nol_over_pdf) * e.source_pdf;
+}
+
+
+// ------------------------------------------------------ specular temporal
+
+// ind_spec_temporal_resample.hlsl:146-362 (VNDF source pdf, BRDF target function,
+// balance-heuristic MIS between previous and current domains).
+__global__ void __launch_bounds__(128) k_spec_temporal(vlt_frame_params fp, int w, int h, uint32_t m_cap,
+                                                        const float* __restrict__ prev_depth,
+                                                        const uint32_t* __restrict__ prev_gbuf,
+                                                        const float* __restrict__ depth_buf,
+                                                        const uint32_t* __restrict__ gbuf,
+                                                        const uint2* __restrict__ prev_rsv,
+                                                        const float4* __restrict__ prev_hp,
+                                                        const uint32_t* __restrict__ prev_rad,
+                                                        const float4* __restrict__ new_hp,
+                                                        const uint32_t* __restrict__ new_rad,
+                                                        uint2* __restrict__ out_rsv, float4* __restrict__ out_hp,
+                                                        uint32_t* __restrict__ out_rad, uint32_t frame_rand,
+                                                        uint32_t has_prev_frame) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  float depth = depth_buf[i];
+  float4 nhp4 = new_hp[i];
+  uint32_t nrad_bits = new_rad[i];
+  if (depth == 0.0f) {
+    out_rsv[i] = make_uint2(0u, 0u);
+    out_hp[i] = nhp4;
+    out_rad[i] = nrad_bits;
+    return;
+  }
+  f3 pos = depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+  f4 hr = mul44(fp.prev_view_proj, mk4(pos.x, pos.y, pos.z, 1.0f));
+  f3 ndc = mk3(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3], hr.z / hr.w - 0.0f);
+  f2 uv = mk2(ndc.x * 0.5f + 0.5f, ndc.y * 0.5f + 0.5f);
+  bool sample_prev = uv.x == saturate(uv.x) && uv.y == saturate(uv.y) && has_prev_frame;
+  if (sample_prev) {
+    float pd = sample_depth(prev_depth, uv, w, h);
+    if (fabs_(pd - ndc.z) > 0.001f) sample_prev = false;
+  }
+  uint32_t M = 0;
+  float W = 0.0f;
+  f3 rhp = mk3(0.0f), rrad = mk3(0.0f);
+  uint32_t rrad_bits = 0;
+  float rtf = 0.0f;
+  GBuffer pg;
+  pg.color = mk3(0.0f);
+  pg.metallic = 0.0f;
+  pg.normal = mk3(0.0f);
+  pg.perceptual_roughness = 0.0f;
+  if (sample_prev) {
+    int px = (int)f2u_rz(uv.x * (float)w), py = (int)f2u_rz(uv.y * (float)h);
+    uint2 rs = ld(prev_rsv, px, py, w, h);
+    M = rs.x;
+    W = as_float(rs.y);
+    float4 p4 = ld(prev_hp, px, py, w, h);
+    rhp = mk3(p4.x, p4.y, p4.z);
+    rrad_bits = ld(prev_rad, px, py, w, h);
+    rrad = unpack_r11g11b10(rrad_bits);
+    rtf = p4.w;
+    pg = load_gbuffer(prev_gbuf, px, py, w, h);
+  }
+  f3 nhp = mk3(nhp4.x, nhp4.y, nhp4.z);
+  f3 nrad = unpack_r11g11b10(nrad_bits);
+  GBuffer g = load_gbuffer(gbuf, x, y, w, h);
+  uint32_t mmax = f2u_rz((float)m_cap * g.perceptual_roughness);
+  M = M < mmax ? M : mmax;
+  f3 view_pos = vpos3(fp.view_pos);
+  f3 f0 = specular_f0(g.color, g.metallic);
+  SpecEval cur = spec_eval(view_pos, pos, g.normal, g.perceptual_roughness, f0, nhp);
+  float new_w = luminance(nrad * cur.brdf_nol_over_pdf);
+  float new_tf = new_w * cur.source_pdf;
+  float prev_w = W * (rtf * (float)M);
+  if (M > 0) {
+    SpecEval poc = spec_eval(vpos3(fp.prev_view_pos), pos, pg.normal, pg.perceptual_roughness,
+                             specular_f0(pg.color, pg.metallic), nhp);
+    float ptoc = luminance(nrad * poc.brdf_nol_over_pdf) * poc.source_pdf;
+    float curr_m = new_tf / (new_tf + ptoc * (float)M);
+    if (new_tf == 0.0f) curr_m = 0.0f;
+    new_w = curr_m * new_w;
+    SpecEval cop = spec_eval(view_pos, pos, g.normal, g.perceptual_roughness, f0, rhp);
+    float ctop = luminance(rrad * cop.brdf_nol_over_pdf) * cop.source_pdf;
+    float m_num = rtf * (float)M;
+    float prev_m = m_num / (m_num + ctop);
+    if (m_num == 0.0f) prev_m = 0.0f;
+    prev_w = prev_m * (ctop * W);
+    rtf = ctop;
+  }
+  uint32_t rng = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
+  float w_sum = prev_w + new_w;
+  float chance_prev = prev_w / w_sum;
+  bool use_prev = lcg_rand(rng) < chance_prev;
+  if (!use_prev) {
+    rhp = nhp;
+    rrad_bits = nrad_bits;
+    rtf = new_tf;
+  }
+  M += 1;
+  W = rtf > 0.0f ? w_sum / rtf : 0.0f;
+  out_rsv[i] = make_uint2(M, as_uint(W));
+  out_hp[i] = make_float4(rhp.x, rhp.y, rhp.z, rtf);
+  out_rad[i] = rrad_bits;
+}
+
+// ------------------------------------------------------- specular spatial
+
+// ggx_brdf_integral_approx (brdf.hlsl:180-199) [Hirvonen 2019].
+__device__ __forceinline__ f3 ggx_integral(float nov, float roughness, f3 f0) {
+  float a = roughness * roughness;
+  float a2 = a * a;
+  float a3 = a * a2;
+  float c = nov;
+  float c2 = c * c;
+  float c3 = c * c2;
+  float m0x = 0.99044f * 1.0f + -1.28514f * c;
+  float m0y = 1.29678f * 1.0f + -0.755907f * c;
+  float k0 = 1.0f * m0x + a * m0y;
+  float m1x = 1.0f * 1.0f + 2.92338f * c + 59.4188f * c3;
+  float m1y = 20.3225f * 1.0f + -27.0302f * c + 222.592f * c3;
+  float m1z = 121.563f * 1.0f + 626.13f * c + 316.627f * c3;
+  k0 = k0 / (1.0f * m1x + a * m1y + a3 * m1z);
+  float m2x = 0.0365463f * 1.0f + 3.32707f * c;
+  float m2y = 9.0632f * 1.0f + -9.04756f * c;
+  float k1 = 1.0f * m2x + a * m2y;
+  float m3x = 1.0f * 1.0f + 3.59685f * c2 + -1.36772f * c3;
+  float m3y = 9.04401f * 1.0f + -16.3174f * c2 + 9.22949f * c3;
+  float m3z = 5.56589f * 1.0f + 19.7886f * c2 + -20.2123f * c3;
+  k1 = k1 / (1.0f * m3x + a * m3y + a3 * m3z);
+  return mk3(k0 + k1 * f0.x, k0 + k1 * f0.y, k0 + k1 * f0.z);
+}
+
+// ind_spec_spatial_resample.hlsl:169-448. Optionally also stores the merged
+// reservoir (for chaining several spatial passes; the reference runs one).
+__global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w, int h, SpecKnobs kn,
+                                                       const uint32_t* __restrict__ gbuf,
+                                                       const float* __restrict__ depth_buf,
+                                                       const uint2* __restrict__ rsv,
+                                                       const float4* __restrict__ hp_tex,
+                                                       const uint32_t* __restrict__ rad_tex,
+                                                       uint32_t* __restrict__ lighting, uint16_t* __restrict__ ray_len_out,
+                                                       uint2* __restrict__ out_rsv, float4* __restrict__ out_hp,
+                                                       uint32_t* __restrict__ out_rad, uint32_t frame_rand) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  float depth = depth_buf[i];
+  if (depth == 0.0f) {
+    if (lighting) lighting[i] = 0u;
+    if (ray_len_out) ray_len_out[i] = 0;
+    if (out_rsv) {
+      out_rsv[i] = make_uint2(0u, 0u);
+      out_hp[i] = hp_tex[i];
+      out_rad[i] = rad_tex[i];
+    }
+    return;
+  }
+  f3 pos = depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+  GBuffer g = load_gbuffer(gbuf, x, y, w, h);
+  uint2 rs = rsv[i];
+  uint32_t M = rs.x;
+  float W = as_float(rs.y);
+  float4 hp4 = hp_tex[i];
+  f3 hit = mk3(hp4.x, hp4.y, hp4.z);
+  uint32_t rad_bits = rad_tex[i];
+  f3 rad = unpack_r11g11b10(rad_bits);
+  float ctf = hp4.w;
+  f3 view_pos = vpos3(fp.view_pos);
+  f3 f0 = specular_f0(g.color, g.metallic);
+  const uint32_t n_iter = f2u_rz(0.0f + g.perceptual_roughness * ((float)kn.taps - 0.0f));
+  float radius = kn.radius_px > 0.0f ? kn.radius_px : (float)(w < h ? w : h) * 0.05f;
+  uint32_t rng = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
+  for (uint32_t it = 0; it < n_iter; ++it) {
+    float u0 = lcg_rand(rng);
+    float u1 = lcg_rand(rng);
+    float rr = sqrt_(u0);
+    float s, c;
+    sincos_(VLT_TWO_PI * u1, &s, &c);
+    float ox = rr * c, oy = rr * s;
+    int nx = x + f2i_rz(ox * radius), ny = y + f2i_rz(oy * radius);
+    nx = nx < 0 ? 0 : (nx > w - 1 ? w - 1 : nx);
+    ny = ny < 0 ? 0 : (ny > h - 1 ? h - 1 : ny);
+    if (nx == x && ny == y) continue;
+    GBuffer gn = load_gbuffer(gbuf, nx, ny, w, h);
+    size_t j = (size_t)ny * w + nx;
+    float dn = depth_buf[j];
+    bool diff = dot3(g.normal, gn.normal) < VLT_COS25;
+    f3 pn = depth_to_position(fp.inv_view_proj, nx, ny, w, h, dn);
+    float dist_to_plane = dot3(pn - pos, g.normal);
+    diff = diff || fabs_(dist_to_plane) > 0.05f;
+    if (diff) {
+      radius = fmax_(radius * 0.5f, 1.5f);
+      continue;
+    }
+    uint2 rsn = rsv[j];
+    uint32_t Mn = rsn.x;
+    float Wn = as_float(rsn.y);
+    float4 hpn4 = hp_tex[j];
+    f3 hitn = mk3(hpn4.x, hpn4.y, hpn4.z);
+    uint32_t radn_bits = rad_tex[j];
+    f3 radn = unpack_r11g11b10(radn_bits);
+    float tfn = hpn4.w;
+    float w_nb, w_c;
+    {
+      SpecEval c_on_n = spec_eval(view_pos, pos, g.normal, g.perceptual_roughness, f0, hitn);
+      float ctf_on_n = spec_tf(c_on_n, radn);
+      float m_nb = (tfn * (float)Mn) / (tfn * (float)Mn + ctf_on_n * (float)M);
+      if (tfn * (float)Mn == 0.0f) m_nb = 0.0f;
+      w_nb = m_nb * tfn * Wn;
+      SpecEval n_on_c = spec_eval(view_pos, pn, gn.normal, gn.perceptual_roughness,
+                                  specular_f0(gn.color, gn.metallic), hit);
+      float ntf_on_c = spec_tf(n_on_c, rad);
+      float m_c = (ctf * (float)M) / (ctf * (float)M + ntf_on_c * (float)Mn);
+      if (ctf * (float)M == 0.0f) m_c = 0.0f;
+      w_c = m_c * ctf * W;
+    }
+    float w_sum = w_c + w_nb;
+    float chance = w_nb / w_sum;
+    if (lcg_rand(rng) < chance) {
+      hit = hitn;
+      rad = radn;
+      rad_bits = radn_bits;
+      ctf = tfn;
+    }
+    M += Mn;
+    W = ctf > 0.0f ? w_sum / ctf : 0.0f;
+  }
+  float ray_len = length3(hit - pos);
+  if (out_rsv) {
+    out_rsv[i] = make_uint2(M, as_uint(W));
+    out_hp[i] = make_float4(hit.x, hit.y, hit.z, ctf);
+    out_rad[i] = rad_bits;
+  }
+  if (lighting) {
+    float roughness = fmax_(g.perceptual_roughness * g.perceptual_roughness, 0.002f);
+    f3 l = normalize3(hit - pos);
+    f3 v = normalize3(view_pos - pos);
+    f3 hv = normalize3(v + l);
+    float nol = saturate(dot3(g.normal, l));
+    float nov = saturate(dot3(g.normal, v));
+    float noh = saturate(dot3(g.normal, hv));
+    float loh = saturate(dot3(l, hv));
+    f3 F = f_schlick(loh, f0);
+    float D = d_ggx(noh, roughness);
+    float lp = lambda_pomc(nov, roughness);
+    float vndf = 0.25f * D / lp;
+    float gg = g2_over_g1(nol, nov, roughness);
+    if (nol <= 0.0f) gg = 0.0f;
+    if (nov <= 0.0f) gg = 0.0f;
+    f3 li = rad * ((F * gg) * (vndf * W));
+    f3 refl = ggx_integral(nov, roughness, f0);
+    refl = mk3(fmax_(refl.x, 1.0f / 65536.0f), fmax_(refl.y, 1.0f / 65536.0f), fmax_(refl.z, 1.0f / 65536.0f));
+    li = li / refl;
+    lighting[i] = pack_r11g11b10(li);
+  }
+  if (ray_len_out) ray_len_out[i] = (uint16_t)f32tof16(ray_len);
+}
+
+// ------------------------------------------------------------- launchers
+
+static const dim3 kBlock(32, 4, 1);
+
+void launch_ao_gen(const vlt_frame_params& fp, int w, int h, const uint32_t* hpn, const float* depth,
+                   const uint32_t* prev_ao, uint32_t* ao, uint32_t has_new, uint32_t has_prev, float radius,
+                   cudaStream_t s) {
+  k_ao_gen<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, (const uint2*)hpn, depth, prev_ao, ao, has_new,
+                                                     has_prev, radius);
+}
+
+void launch_ao_filter(int w, int h, const float* depth, const uint32_t* ao, uint16_t* out, cudaStream_t s) {
+  k_ao_filter<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, depth, ao, out);
+}
+
+void launch_diff_temporal(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const float* prev_depth,
+                          const float* depth, const uint32_t* new_hpn, const uint32_t* new_rad, const float* new_pdf,
+                          const uint32_t* prev_rsv, uint32_t* out, uint32_t frame_rand, uint32_t has_prev,
+                          uint32_t has_new, cudaStream_t s) {
+  k_diff_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, prev_depth, depth, (const uint2*)new_hpn,
+                                                            new_rad, new_pdf, (const uint4*)prev_rsv, (uint4*)out,
+                                                            frame_rand, has_prev, has_new);
+}
+
+void launch_diff_spatial(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const uint32_t* gbuf,
+                         const float* depth, const uint16_t* ao, const uint32_t* in, uint32_t* out,
+                         uint32_t* lighting, uint32_t frame_rand, cudaStream_t s) {
+  k_diff_spatial<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, gbuf, depth, ao, (const uint4*)in,
+                                                           (uint4*)out, lighting, frame_rand);
+}
+
+void launch_spec_temporal(const vlt_frame_params& fp, int w, int h, uint32_t m_cap, const float* prev_depth,
+                          const uint32_t* prev_gbuf, const float* depth, const uint32_t* gbuf,
+                          const uint32_t* prev_rsv, const float* prev_hp, const uint32_t* prev_rad,
+                          const float* new_hp, const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp,
+                          uint32_t* out_rad, uint32_t frame_rand, uint32_t has_prev, cudaStream_t s) {
+  k_spec_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
+      fp, w, h, m_cap, prev_depth, prev_gbuf, depth, gbuf, (const uint2*)prev_rsv, (const float4*)prev_hp, prev_rad,
+      (const float4*)new_hp, new_rad, (uint2*)out_rsv, (float4*)out_hp, out_rad, frame_rand, has_prev);
+}
+
+void launch_spec_spatial(const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn, const uint32_t* gbuf,
+                         const float* depth, const uint32_t* rsv, const float* hp, const uint32_t* rad,
+                         uint32_t* lighting, uint16_t* ray_len, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
+                         uint32_t frame_rand, cudaStream_t s) {
+  k_spec_spatial<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, gbuf, depth, (const uint2*)rsv,
+                                                           (const float4*)hp, rad, lighting, ray_len,
+                                                           (uint2*)out_rsv, (float4*)out_hp, out_rad, frame_rand);
+}
+
+}  // namespace vlt

@@ -1,0 +1,103 @@
+// Internal launcher interface between the C ABI / frame driver and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/vlt.h"
+#include "vlt_device.cuh"
+
+namespace vlt {
+
+struct DiffKnobs {
+  uint32_t m_cap;
+  uint32_t use_input_pdf;
+  uint32_t taps;
+  float radius_px;
+};
+
+struct SpecKnobs {
+  uint32_t taps;
+  float radius_px;
+};
+
+struct DenoiseKnobs {
+  float blend_diff;  // 1 / history_max_frames
+  uint32_t fast_history;
+};
+
+// restir.cu
+void launch_ao_gen(const vlt_frame_params& fp, int w, int h, const uint32_t* hpn, const float* depth,
+                   const uint32_t* prev_ao, uint32_t* ao, uint32_t has_new, uint32_t has_prev, float radius,
+                   cudaStream_t s);
+void launch_ao_filter(int w, int h, const float* depth, const uint32_t* ao, uint16_t* out, cudaStream_t s);
+void launch_diff_temporal(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const float* prev_depth,
+                          const float* depth, const uint32_t* new_hpn, const uint32_t* new_rad, const float* new_pdf,
+                          const uint32_t* prev_rsv, uint32_t* out, uint32_t frame_rand, uint32_t has_prev,
+                          uint32_t has_new, cudaStream_t s);
+void launch_diff_spatial(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const uint32_t* gbuf,
+                         const float* depth, const uint16_t* ao, const uint32_t* in, uint32_t* out,
+                         uint32_t* lighting, uint32_t frame_rand, cudaStream_t s);
+void launch_spec_temporal(const vlt_frame_params& fp, int w, int h, uint32_t m_cap, const float* prev_depth,
+                          const uint32_t* prev_gbuf, const float* depth, const uint32_t* gbuf,
+                          const uint32_t* prev_rsv, const float* prev_hp, const uint32_t* prev_rad,
+                          const float* new_hp, const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp,
+                          uint32_t* out_rad, uint32_t frame_rand, uint32_t has_prev, cudaStream_t s);
+void launch_spec_spatial(const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn, const uint32_t* gbuf,
+                         const float* depth, const uint32_t* rsv, const float* hp, const uint32_t* rad,
+                         uint32_t* lighting, uint16_t* ray_len, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
+                         uint32_t frame_rand, cudaStream_t s);
+
+// denoise.cu
+void launch_dn_temporal(const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn, const float* depth,
+                        const uint32_t* gbuf, const uint32_t* diff_src, const uint32_t* spec_src,
+                        const uint16_t* ray_len, const float* prev_depth, const uint32_t* prev_gbuf,
+                        const uint32_t* color_hist, const uint32_t* mom_hist, const uint8_t* len_hist,
+                        const uint32_t* fast_hist, uint32_t* out_color, uint32_t* out_mom, uint8_t* out_len,
+                        uint32_t* out_fast, uint32_t has_history, cudaStream_t s);
+void launch_dn_fix(int w, int h, const float* depth, const uint32_t* gbuf, const uint8_t* len,
+                   const uint32_t* color, const uint32_t* mom, uint32_t* out_color, uint32_t* out_mom,
+                   cudaStream_t s);
+void launch_dn_fast_clamp(int w, int h, const uint32_t* fast, uint32_t* color, cudaStream_t s);
+void launch_dn_fallback(int w, int h, const float* depth, const uint32_t* gbuf, const uint8_t* len,
+                        const uint32_t* color, const uint32_t* mom, uint32_t* out_color, uint32_t* out_var,
+                        cudaStream_t s);
+// out_diff/out_spec (optional): write the result as two separate R11G11B10 planes
+// instead of the packed colour pair.
+void launch_dn_atrous(int w, int h, const float* depth, const uint32_t* gbuf, const uint32_t* color,
+                      const uint32_t* var, uint32_t* out_color, uint32_t* out_var, uint32_t* out_diff,
+                      uint32_t* out_spec, int step, cudaStream_t s);
+void launch_split_color(int w, int h, const uint32_t* color, uint32_t* diff, uint32_t* spec, cudaStream_t s);
+
+// hashgrid.cu
+struct HashGridDims {
+  uint32_t log2_buckets;
+  uint32_t max_queries;
+  uint32_t num_buckets() const { return 1u << log2_buckets; }
+  uint32_t num_cells() const { return 16u << log2_buckets; }
+  uint32_t query_bits() const {
+    uint32_t b = 0;
+    while ((1u << b) < max_queries && b < 30) ++b;
+    return b;
+  }
+};
+size_t hg_select_scratch_bytes(const HashGridDims& d);
+void launch_hg_decay(const HashGridDims& d, uint8_t* decay, uint32_t* storage, cudaStream_t s);
+void launch_hg_select(const HashGridDims& d, const uint32_t* queries, const uint32_t* count, uint32_t* storage,
+                      uint32_t* selection, uint32_t frame_hash, void* scratch, cudaStream_t s);
+void launch_hg_compact(const HashGridDims& d, const uint32_t* selection, uint32_t* idx, uint32_t* addr,
+                       uint32_t* count, cudaStream_t s);
+void launch_hg_update(const HashGridDims& d, const uint32_t* queries, const uint32_t* idx, const uint32_t* addr,
+                      const uint32_t* count, uint32_t* storage, uint8_t* decay, cudaStream_t s);
+void launch_hg_emit(const vlt_frame_params& fp, int w, int h, const HashGridDims& d, uint32_t key_mode,
+                    const float* depth, const uint32_t* hpn, const uint32_t* rad, uint32_t* queries,
+                    uint32_t* count, cudaStream_t s);
+void launch_hg_find(const vlt_frame_params& fp, const HashGridDims& d, uint32_t key_mode, const uint32_t* storage,
+                    uint32_t n, const float* pos, const float* nrm, uint32_t* out_addr, float* out_rad,
+                    cudaStream_t s);
+
+// Thread-local record of the last CUDA error text.
+void set_last_error(const char* msg);
+vlt_status cuda_status(cudaError_t e);
+
+}  // namespace vlt

@@ -1,0 +1,183 @@
+"""Python front end of the C ABI: views (RestirRenderer + Denoiser state) and the
+synthetic scene.
+
+The call sequence mirrors RestirRenderer::add_passes / Denoiser::add_passes of
+crates/violet-restir/src/{restir_renderer.rs,denoising.rs}: one `View.run` per
+frame with that frame's G-buffer, candidate samples and FrameParams.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _ffi
+
+# Per-frame input buffers: name -> (numpy dtype, elements per pixel).
+FRAME_BUFFERS = {
+    "depth": (np.float32, 1),
+    "gbuffer": (np.uint32, 4),  # layer-planar: 4 planes of W*H
+    "diff_hit_pos_normal": (np.uint32, 2),
+    "diff_hit_radiance": (np.uint32, 1),
+    "diff_source_pdf": (np.float32, 1),
+    "spec_hit_pos": (np.float32, 4),
+    "spec_hit_radiance": (np.uint32, 1),
+}
+
+
+def params_reference():
+    p = _ffi.Params()
+    _ffi.load().vlt_params_reference(C.byref(p))
+    return p
+
+
+def params_plain(config):
+    p = _ffi.Params()
+    _ffi.load().vlt_params_plain(C.byref(p), int(config))
+    return p
+
+
+def _ptr(x):
+    """Device/host address of a torch tensor, numpy array, int or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    raise TypeError("cannot take the address of %r" % type(x))
+
+
+class Context:
+    def __init__(self, device=0):
+        self._lib = _ffi.load()
+        h = C.c_void_p()
+        _ffi.check(self._lib.vlt_ctx_create(int(device), C.byref(h)), "vlt_ctx_create")
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            self._lib.vlt_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class View:
+    """Resident per-view state and the per-frame pass sequence (vlt_frame_run)."""
+
+    def __init__(self, ctx, width, height, form="ref", params=None):
+        self._lib = _ffi.load()
+        self.ctx = ctx
+        self.width, self.height = int(width), int(height)
+        self.form = form
+        self.params = params if params is not None else params_reference()
+        h = C.c_void_p()
+        _ffi.check(
+            self._lib.vlt_view_create(ctx.handle, self.width, self.height, _ffi.FORMS[form], C.byref(self.params),
+                                      C.byref(h)),
+            "vlt_view_create",
+        )
+        self.handle = h
+
+    @staticmethod
+    def device_bytes(width, height, form="ref", params=None):
+        lib = _ffi.load()
+        p = params if params is not None else params_reference()
+        return int(lib.vlt_view_device_bytes(int(width), int(height), _ffi.FORMS[form], C.byref(p)))
+
+    def run(self, frame_params, frame_index, inputs, outputs=None, stream=0):
+        fi = _ffi.FrameInputs()
+        fi.params = C.pointer(frame_params)
+        fi.frame_index = int(frame_index) & 0xFFFFFFFF
+        for name in ("depth", "gbuffer", "prev_depth", "prev_gbuffer", "diff_hit_pos_normal", "diff_hit_radiance",
+                     "diff_source_pdf", "spec_hit_pos", "spec_hit_radiance"):
+            setattr(fi, name, _ptr(inputs.get(name)))
+        fo = _ffi.FrameOutputs()
+        outputs = outputs or {}
+        for name in ("diffuse", "specular", "raw_diffuse", "raw_specular"):
+            setattr(fo, name, _ptr(outputs.get(name)))
+        _ffi.check(self._lib.vlt_frame_run(self.handle, C.byref(fi), C.byref(fo), C.c_void_p(stream)),
+                   "vlt_frame_run")
+
+    def buffer(self, name):
+        n = C.c_size_t(0)
+        p = self._lib.vlt_view_buffer(self.handle, name.encode(), C.byref(n))
+        if not p:
+            raise KeyError(name)
+        return int(p), int(n.value)
+
+    def reset(self, stream=0):
+        _ffi.check(self._lib.vlt_view_reset(self.handle, C.c_void_p(stream)), "vlt_view_reset")
+
+    def set_timing(self, enable=True):
+        _ffi.check(self._lib.vlt_view_set_timing(self.handle, 1 if enable else 0), "vlt_view_set_timing")
+
+    def read_timing(self):
+        """{pass name: (launches, total ms)} accumulated since the last read."""
+        n = self._lib.vlt_view_read_timing(self.handle, None, 0)
+        arr = (_ffi.PassTime * max(n, 1))()
+        n = self._lib.vlt_view_read_timing(self.handle, arr, n)
+        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms)) for i in range(n)}
+
+    @property
+    def launches(self):
+        return int(self._lib.vlt_view_last_launch_count(self.handle))
+
+    def close(self):
+        if self.handle:
+            self._lib.vlt_view_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scene:
+    """Seeded synthetic frames (G-buffer, camera, candidate samples)."""
+
+    def __init__(self, seed, width, height, disocclusion_frac=0.0, camera_speed=0.01, jitter_cycle=8):
+        self._lib = _ffi.load()
+        self.desc = _ffi.SceneDesc()
+        self._lib.vlt_scene_desc_default(C.byref(self.desc), int(seed), int(width), int(height))
+        self.desc.disocclusion_frac = float(disocclusion_frac)
+        self.desc.camera_speed = float(camera_speed)
+        self.desc.jitter_cycle = int(jitter_cycle)
+        self.width, self.height = int(width), int(height)
+
+    def frame_params(self, frame):
+        fp = _ffi.FrameParams()
+        _ffi.check(self._lib.vlt_scene_frame_params(C.byref(self.desc), int(frame), C.byref(fp)),
+                   "vlt_scene_frame_params")
+        return fp
+
+    def alloc_host(self):
+        n = self.width * self.height
+        return {k: np.zeros(n * c, dtype=dt) for k, (dt, c) in FRAME_BUFFERS.items()}
+
+    def _frame_struct(self, bufs):
+        f = _ffi.SceneFrame()
+        for k in FRAME_BUFFERS:
+            setattr(f, k, _ptr(bufs.get(k)))
+        return f
+
+    def generate_host(self, frame, bufs=None):
+        bufs = bufs if bufs is not None else self.alloc_host()
+        f = self._frame_struct(bufs)
+        _ffi.check(self._lib.vlt_scene_generate_host(C.byref(self.desc), int(frame), C.byref(f)),
+                   "vlt_scene_generate_host")
+        return bufs
+
+    def generate_device(self, frame, bufs, stream=0):
+        f = self._frame_struct(bufs)
+        _ffi.check(self._lib.vlt_scene_generate_device(C.byref(self.desc), int(frame), C.byref(f),
+                                                       C.c_void_p(stream)), "vlt_scene_generate_device")
+        return bufs
