@@ -306,6 +306,23 @@ vlt_status vlt_hg_query_select(uint32_t log2_buckets, uint32_t max_queries, cons
                                const uint32_t* query_count, uint32_t* rw_storage, uint32_t* rw_selection,
                                uint32_t frame_hash, void* scratch, void* stream);
 
+/* Query selection that allocates nothing. This entry point has no counterpart in
+ * the reference; it exists for callers that cannot allocate device memory — a host
+ * that owns a fixed device-memory budget or its own pool allocator, or a real-time
+ * frame loop where cudaMalloc's implicit synchronization would stall the frame.
+ * Same arguments and results as vlt_hg_query_select, without `scratch`: the
+ * scratch lives in a fixed array inside the library (VLT_HG_SELECT_NOALLOC_SCRATCH_BYTES
+ * of device memory, held on every GPU that loads the library until the process
+ * exits). Sizes whose scratch (vlt_hg_select_scratch_bytes) exceeds that limit are
+ * rejected with VLT_ERR_INVALID_ARG. The first call on a device looks up the array's
+ * device address; make that first call before any stream capture. All calls share
+ * the array, so calls that overlap on the GPU (different streams, or different
+ * threads on the same device) race and give wrong results: serialize them. */
+#define VLT_HG_SELECT_NOALLOC_SCRATCH_BYTES (12u * 1024u * 1024u)
+vlt_status vlt_hg_query_select_noalloc(uint32_t log2_buckets, uint32_t max_queries, const uint32_t* queries,
+                                       const uint32_t* query_count, uint32_t* rw_storage, uint32_t* rw_selection,
+                                       uint32_t frame_hash, void* stream);
+
 /* restir/hash_grid_query_compact.hlsl; node "HashGridCache Query Compact"
  * (restir_renderer.rs:384-391). rw_compact_count must be zero on entry. The order
  * of the compacted entries is unspecified (as in the reference). */

@@ -51,3 +51,17 @@ def test_invalid_arguments_are_reported_not_raised():
     assert lib.vlt_frame_run(None, None, None, None) == 1
     assert lib.vlt_hg_decay(2, None, None, None) == 1
     assert lib.vlt_denoise_atrous(0, 0, None, None, None, None, None, None, 1, None) == 1
+
+
+def test_noalloc_select_rejects_sizes_beyond_its_scratch():
+    # The allocation-free query selection keeps its scratch in a fixed 12 MiB array;
+    # larger sizes are refused before anything touches a GPU.
+    lib = vg.lib()
+    limit = 12 * 1024 * 1024
+    assert lib.vlt_hg_select_scratch_bytes(16, 131072) <= limit
+    assert lib.vlt_hg_select_scratch_bytes(18, 1920 * 1080) <= limit
+    assert lib.vlt_hg_select_scratch_bytes(24, 1 << 24) > limit
+    dummy = C.c_void_p(16)
+    rc = lib.vlt_hg_query_select_noalloc(24, 1 << 24, dummy, dummy, dummy, dummy, 0, None)
+    assert rc == 1
+    assert b"scratch" in lib.vlt_last_error()

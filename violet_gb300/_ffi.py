@@ -155,6 +155,7 @@ SIGNATURES = {
     "vlt_hg_decay": (C.c_int, [U32, P, P, P]),
     "vlt_hg_select_scratch_bytes": (C.c_size_t, [U32, U32]),
     "vlt_hg_query_select": (C.c_int, [U32, U32, P, P, P, P, U32, P, P]),
+    "vlt_hg_query_select_noalloc": (C.c_int, [U32, U32, P, P, P, P, U32, P]),
     "vlt_hg_query_compact": (C.c_int, [U32, U32, P, P, P, P, P]),
     "vlt_hg_update": (C.c_int, [U32, P, P, P, P, P, P, P]),
     "vlt_hg_emit_queries": (C.c_int, [FP, U32, U32, U32, U32, U32, P, P, P, P, P, P]),

@@ -13,6 +13,8 @@
 //   S4  one warp per bucket repeatedly takes the smallest unresolved query index,
 //       probes/inserts its checksum exactly as the sequential loop would, and
 //       resolves every listed query with that checksum.
+#include <mutex>
+
 #include "vlt_internal.h"
 
 namespace vlt {
@@ -412,4 +414,56 @@ void launch_hg_find(const vlt_frame_params& fp, const HashGridDims& d, uint32_t 
                                             out_addr, (float4*)out_rad);
 }
 
+// ------------------------------------------- query select without allocation
+
+// Scratch for vlt_hg_query_select_noalloc: a fixed array in the library's own
+// device memory, so that callers who cannot allocate device memory can still run
+// the query selection. It exists once per GPU that loads the library and stays
+// until the process exits. Every call uses the same array.
+static __device__ __align__(256) unsigned char g_hg_select_scratch[VLT_HG_SELECT_NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_hg_select_scratch, looked up once per device (host code
+// cannot use the symbol itself as a device pointer).
+static void* g_hg_select_scratch_ptr[64];
+static bool g_hg_select_scratch_ready[64];
+static std::mutex g_hg_select_scratch_mutex;
+
 }  // namespace vlt
+
+extern "C" vlt_status vlt_hg_query_select_noalloc(uint32_t log2_buckets, uint32_t max_queries,
+                                                  const uint32_t* queries, const uint32_t* query_count,
+                                                  uint32_t* rw_storage, uint32_t* rw_selection, uint32_t frame_hash,
+                                                  void* stream) {
+  using namespace vlt;
+  if (log2_buckets < 4 || log2_buckets > 24 || max_queries == 0 || max_queries > (1u << 30) || !queries ||
+      !query_count || !rw_storage || !rw_selection)
+    return VLT_ERR_INVALID_ARG;
+  HashGridDims d = {log2_buckets, max_queries};
+  if (hg_select_scratch_bytes(d) > (size_t)VLT_HG_SELECT_NOALLOC_SCRATCH_BYTES) {
+    set_last_error("vlt_hg_query_select_noalloc: 2^log2_buckets buckets and max_queries need more scratch than the "
+                   "fixed VLT_HG_SELECT_NOALLOC_SCRATCH_BYTES; use vlt_hg_query_select with caller scratch");
+    return VLT_ERR_INVALID_ARG;
+  }
+  int dev = 0;
+  vlt_status st = cuda_status(cudaGetDevice(&dev));
+  if (st != VLT_OK) return st;
+  if (dev < 0 || dev >= 64) return VLT_ERR_INVALID_ARG;
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_hg_select_scratch_mutex);
+    if (!g_hg_select_scratch_ready[dev]) {
+      // First call on this device: resolve the array's device address (device `dev`
+      // is current here).
+      void* p = nullptr;
+      st = cuda_status(cudaGetSymbolAddress(&p, g_hg_select_scratch));
+      if (st != VLT_OK) return st;
+      g_hg_select_scratch_ptr[dev] = p;
+      g_hg_select_scratch_ready[dev] = true;
+    }
+    scratch = g_hg_select_scratch_ptr[dev];
+  }
+  // launch_hg_select clears the per-bucket counters it needs at zero before use;
+  // the rest of the scratch is fully rewritten before it is read.
+  launch_hg_select(d, queries, query_count, rw_storage, rw_selection, frame_hash, scratch, (cudaStream_t)stream);
+  return cuda_status(cudaGetLastError());
+}
