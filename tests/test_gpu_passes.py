@@ -44,12 +44,17 @@ def world():
     return {"P": P, "fp": scene.frame_params(3), "prev": frames[2], "cur": h3, "state": state}
 
 
+_KEEP = []  # device copies stay alive for the module: a freed temporary's block would be reused
+
+
 def D(a):
     """numpy -> device tensor (bytes)."""
     import torch
 
     a = np.ascontiguousarray(a)
-    return torch.from_numpy(a.view(np.uint8).reshape(-1).copy()).cuda()
+    t = torch.from_numpy(a.view(np.uint8).reshape(-1).copy()).cuda()
+    _KEEP.append(t)
+    return t
 
 
 def Z(nbytes):

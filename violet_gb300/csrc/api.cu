@@ -77,7 +77,7 @@ struct ViewBuffers {
   uint32_t* hg_ccount;
   void* hg_scratch;
   float* prev_depth;
-  uint32_t* prev_gbuf;
+  float4* surf[2][3];      // per-frame surface planes {normal, depth}, {position, roughness}, {f0, fwidth_z}
 };
 
 }  // namespace
@@ -120,7 +120,7 @@ struct vlt_view {
   uint32_t frames;         // frames run since creation/reset
   bool denoise_history;    // Denoiser::history is Some
   bool fast_history_valid; // Denoiser::fast_history is Some
-  int diff_prev, spec_prev, ao_prev, hg_qcur;
+  int diff_prev, spec_prev, ao_prev, hg_qcur, surf_cur;
   uint32_t launches;
   Timing* timing;
 };
@@ -188,7 +188,8 @@ size_t layout(vlt_view* v, char* base) {
     b.hg_scratch = nullptr;
   }
   b.prev_depth = (float*)take(4 * n);
-  b.prev_gbuf = (uint32_t*)take(16 * n);
+  for (int k = 0; k < 2; ++k)
+    for (int j = 0; j < 3; ++j) b.surf[k][j] = (float4*)take(16 * n);
   return off;
 }
 
@@ -225,6 +226,7 @@ vlt_status reset_state(vlt_view* v, cudaStream_t s) {
   v->spec_prev = 0;
   v->ao_prev = 0;
   v->hg_qcur = 0;
+  v->surf_cur = 0;
   // Zero everything: cleared hash grid (restir_renderer.rs:296-306), empty queries.
   VLT_TRY(cudaMemsetAsync(v->pool.p, 0, v->pool.bytes, s));
   return VLT_OK;
@@ -461,7 +463,6 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
       {"hg_query_count", b.hg_qcount[v->hg_qcur], v->p.hg_enable ? (size_t)4 : (size_t)0},
       {"hg_selection", b.hg_sel, nc * 4},
       {"prev_depth", b.prev_depth, 4 * n},
-      {"prev_gbuffer", b.prev_gbuf, 16 * n},
   };
   for (const E& e : tab) {
     if (strcmp(e.nm, name) == 0) {
@@ -487,7 +488,6 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
 
   const bool has_prev = v->frames > 0;  // prev depth / gbuffer / indirect diffuse / reservoirs
   const float* prev_depth = has_prev && in->prev_depth ? in->prev_depth : b.prev_depth;
-  const uint32_t* prev_gbuf = has_prev && in->prev_gbuffer ? in->prev_gbuffer : b.prev_gbuf;
   FrameRand fr = {in->frame_index};
   Timing& tm = *v->timing;
   tm.stream = s;
@@ -508,6 +508,15 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
       }                                                          \
     }                                                            \
   } while (0)
+
+  // Surface attributes of this frame, decoded once (the previous frame's planes
+  // stay in the other slot).
+  const int sc = v->surf_cur ^ 1;
+  GeoArgs ga = {in->depth, in->gbuffer, fp.inv_view_proj, b.surf[sc][0], b.surf[sc][1], b.surf[sc][2]};
+  GeoArgs pga = {prev_depth, nullptr, fp.prev_inv_view_proj, b.surf[sc ^ 1][0], b.surf[sc ^ 1][1],
+                 b.surf[sc ^ 1][2]};
+  STAGE("surface", launch_surface(fp, w, h, in->depth, in->gbuffer, b.surf[sc][0], b.surf[sc][1], b.surf[sc][2], s));
+  ++launches;
 
   // Hash-grid radiance cache: decay, then (with history) select/compact/update of
   // last frame's queries, then this frame's queries.
@@ -542,7 +551,7 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
 
   // AO.
   int ao_cur = v->ao_prev ^ 1;
-  STAGE("ao_gen", launch_ao_gen(fp, w, h, in->diff_hit_pos_normal, in->depth, b.ao[v->ao_prev], b.ao[ao_cur], 1u,
+  STAGE("ao_gen", launch_ao_gen(fp, w, h, ga, in->diff_hit_pos_normal, b.ao[v->ao_prev], b.ao[ao_cur], 1u,
                                 has_prev ? 1u : 0u, P.ao_radius, s));
   STAGE("ao_filter", launch_ao_filter(w, h, in->depth, b.ao[ao_cur], b.ao_filtered, s));
   launches += 2;
@@ -552,7 +561,7 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
   DiffKnobs dk = diff_knobs(P);
   int p = v->diff_prev, t = (p + 1) % 3, o = (p + 2) % 3;
   uint32_t seed_dt = fr.next();
-  STAGE("diff_temporal", launch_diff_temporal(fp, w, h, dk, prev_depth, in->depth, in->diff_hit_pos_normal,
+  STAGE("diff_temporal", launch_diff_temporal(fp, w, h, dk, ga, prev_depth, in->diff_hit_pos_normal,
                                               in->diff_hit_radiance, in->diff_source_pdf, b.diff_rsv[p],
                                               b.diff_rsv[t], seed_dt, has_prev ? 1u : 0u, 1u, s));
   ++launches;
@@ -560,8 +569,8 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
   for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
     bool last = k + 1 == P.diff_spatial_passes;
     uint32_t seed_ds = fr.next();
-    STAGE("diff_spatial", launch_diff_spatial(fp, w, h, dk, in->gbuffer, in->depth, b.ao_filtered, b.diff_rsv[src],
-                                              b.diff_rsv[dst], last ? b.diff_light : nullptr, seed_ds, s));
+    STAGE("diff_spatial", launch_diff_spatial(fp, w, h, dk, ga, b.ao_filtered, b.diff_rsv[src], b.diff_rsv[dst],
+                                              last ? b.diff_light : nullptr, seed_ds, s));
     ++launches;
     std::swap(src, dst);
   }
@@ -571,10 +580,10 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
   (void)fr.next();  // Ind. Spec. Sample Gen.
   int sp = v->spec_prev, st = (sp + 1) % 3, so = (sp + 2) % 3;
   uint32_t seed_st = fr.next();
-  STAGE("spec_temporal", launch_spec_temporal(fp, w, h, P.spec_m_cap, prev_depth, prev_gbuf, in->depth, in->gbuffer,
-                                              b.spec_rsv[sp], b.spec_hp[sp], b.spec_rad[sp], in->spec_hit_pos,
-                                              in->spec_hit_radiance, b.spec_rsv[st], b.spec_hp[st], b.spec_rad[st],
-                                              seed_st, has_prev ? 1u : 0u, s));
+  STAGE("spec_temporal", launch_spec_temporal(fp, w, h, P.spec_m_cap, ga, pga, prev_depth, b.spec_rsv[sp],
+                                              b.spec_hp[sp], b.spec_rad[sp], in->spec_hit_pos, in->spec_hit_radiance,
+                                              b.spec_rsv[st], b.spec_hp[st], b.spec_rad[st], seed_st,
+                                              has_prev ? 1u : 0u, s));
   ++launches;
   {
     SpecKnobs sk = {P.spec_spatial_taps, P.spec_spatial_radius_px};
@@ -583,8 +592,8 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
       bool last = k + 1 == P.spec_spatial_passes;
       uint32_t seed_ss = fr.next();
       STAGE("spec_spatial",
-            launch_spec_spatial(fp, w, h, sk, in->gbuffer, in->depth, b.spec_rsv[ssrc], b.spec_hp[ssrc],
-                                b.spec_rad[ssrc], last ? b.spec_light : nullptr, last ? b.ray_len : nullptr,
+            launch_spec_spatial(fp, w, h, sk, ga, b.spec_rsv[ssrc], b.spec_hp[ssrc], b.spec_rad[ssrc],
+                                last ? b.spec_light : nullptr, last ? b.ray_len : nullptr,
                                 last ? nullptr : b.spec_rsv[sdst], last ? nullptr : b.spec_hp[sdst],
                                 last ? nullptr : b.spec_rad[sdst], seed_ss, s));
       ++launches;
@@ -601,14 +610,13 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
     uint32_t has_history = v->denoise_history ? 1u : 0u;
     // color[0]/mom[0]/len[0] = history; color[2]/mom[2]/len[1] = temporal output;
     // color[1]/mom[1] = fix output.
-    STAGE("dn_temporal", launch_dn_temporal(fp, w, h, kn, in->depth, in->gbuffer, b.diff_light, b.spec_light,
-                                            b.ray_len, prev_depth, prev_gbuf, b.color[0], b.mom[0], b.len[0],
-                                            b.fast[0], b.color[2], b.mom[2], b.len[1], b.fast[1], has_history, s));
+    STAGE("dn_temporal", launch_dn_temporal(fp, w, h, kn, ga, pga, b.diff_light, b.spec_light, b.ray_len, prev_depth,
+                                            b.color[0], b.mom[0], b.len[0], b.fast[0], b.color[2], b.mom[2], b.len[1],
+                                            b.fast[1], has_history, s));
     ++launches;
     uint32_t* cur_color = b.color[2];
     if (P.disocclusion_fix) {
-      STAGE("dn_fix", launch_dn_fix(w, h, in->depth, in->gbuffer, b.len[1], b.color[2], b.mom[2], b.color[1],
-                                    b.mom[1], s));
+      STAGE("dn_fix", launch_dn_fix(w, h, ga, b.len[1], b.color[2], b.mom[2], b.color[1], b.mom[1], s));
       ++launches;
       cur_color = b.color[1];
     }
@@ -631,8 +639,7 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
     std::swap(b.len[0], b.len[1]);
     v->denoise_history = true;
     // Now color[0]/mom[0]/len[0] hold this frame's history.
-    STAGE("dn_fallback", launch_dn_fallback(w, h, in->depth, in->gbuffer, b.len[0], b.color[0], b.mom[0], b.color_c,
-                                            b.var[0], s));
+    STAGE("dn_fallback", launch_dn_fallback(w, h, ga, b.len[0], b.color[0], b.mom[0], b.color_c, b.var[0], s));
     ++launches;
     uint32_t* csrc = b.color_c;
     uint32_t* vsrc = b.var[0];
@@ -643,7 +650,7 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
       bool last = k + 1 == iters;
       uint32_t* od = last && out ? (uint32_t*)out->diffuse : nullptr;
       uint32_t* os = last && out ? (uint32_t*)out->specular : nullptr;
-      STAGE("dn_atrous", launch_dn_atrous(w, h, in->depth, in->gbuffer, csrc, vsrc, cdst, vdst, od, os, 1 << k, s));
+      STAGE("dn_atrous", launch_dn_atrous(w, h, ga, csrc, vsrc, cdst, vdst, od, os, 1 << k, s));
       ++launches;
       std::swap(csrc, cdst);
       uint32_t* vnext = vdst == b.var[1] ? b.var[2] : b.var[1];
@@ -666,9 +673,10 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
   if (out && out->raw_specular)
     VLT_TRY(cudaMemcpyAsync(out->raw_specular, b.spec_light, 4 * n, cudaMemcpyDeviceToDevice, s));
 
-  // Retain depth / G-buffer for the next frame unless the caller keeps them.
+  // Retain depth for the next frame unless the caller keeps it (the previous
+  // frame's decoded G-buffer fields stay in the other surface slot).
   if (!in->prev_depth) VLT_TRY(cudaMemcpyAsync(b.prev_depth, in->depth, 4 * n, cudaMemcpyDeviceToDevice, s));
-  if (!in->prev_gbuffer) VLT_TRY(cudaMemcpyAsync(b.prev_gbuf, in->gbuffer, 16 * n, cudaMemcpyDeviceToDevice, s));
+  v->surf_cur = sc;
   v->frames += 1;
   v->launches = launches;
 #undef STAGE
@@ -691,7 +699,8 @@ vlt_status vlt_ind_diff_temporal_resample(const vlt_frame_params* fp, uint32_t w
       (has_new_sample && (!new_hit_pos_normal || !new_hit_radiance)) ||
       (has_new_sample && params->use_input_pdf && !new_source_pdf))
     return VLT_ERR_INVALID_ARG;
-  launch_diff_temporal(*fp, width, height, diff_knobs(*params), prev_gbuffer_depth, gbuffer_depth, new_hit_pos_normal,
+  GeoArgs ga = {gbuffer_depth, nullptr, fp->inv_view_proj, nullptr, nullptr, nullptr};
+  launch_diff_temporal(*fp, width, height, diff_knobs(*params), ga, prev_gbuffer_depth, new_hit_pos_normal,
                        new_hit_radiance, new_source_pdf, prev_reservoir, rw_reservoir, frame_rand, has_prev_frame,
                        has_new_sample, (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
@@ -703,8 +712,9 @@ vlt_status vlt_ao_gen(const vlt_frame_params* fp, uint32_t width, uint32_t heigh
   if (!fp || !dims_ok(width, height) || !depth_buffer || !rw_ao || (has_new_sample && !hit_pos_normal) ||
       (has_prev_frame && !prev_ao))
     return VLT_ERR_INVALID_ARG;
-  launch_ao_gen(*fp, width, height, hit_pos_normal, depth_buffer, (const uint32_t*)prev_ao, (uint32_t*)rw_ao,
-                has_new_sample, has_prev_frame, radius_ws, (cudaStream_t)stream);
+  GeoArgs ga = {depth_buffer, nullptr, fp->inv_view_proj, nullptr, nullptr, nullptr};
+  launch_ao_gen(*fp, width, height, ga, hit_pos_normal, (const uint32_t*)prev_ao, (uint32_t*)rw_ao, has_new_sample,
+                has_prev_frame, radius_ws, (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
 }
 
@@ -723,8 +733,9 @@ vlt_status vlt_ind_diff_spatial_resample(const vlt_frame_params* fp, uint32_t wi
   if (!fp || !params_ok(params) || !dims_ok(width, height) || !gbuffer_color || !gbuffer_depth || !ao_texture ||
       !temp_reservoir || !rw_reservoir)
     return VLT_ERR_INVALID_ARG;
-  launch_diff_spatial(*fp, width, height, diff_knobs(*params), gbuffer_color, gbuffer_depth, ao_texture,
-                      temp_reservoir, rw_reservoir, rw_lighting, frame_rand, (cudaStream_t)stream);
+  GeoArgs ga = {gbuffer_depth, gbuffer_color, fp->inv_view_proj, nullptr, nullptr, nullptr};
+  launch_diff_spatial(*fp, width, height, diff_knobs(*params), ga, ao_texture, temp_reservoir, rw_reservoir,
+                      rw_lighting, frame_rand, (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
 }
 
@@ -741,9 +752,11 @@ vlt_status vlt_ind_spec_temporal_resample(const vlt_frame_params* fp, uint32_t w
       (has_prev_frame && (!prev_gbuffer_depth || !prev_gbuffer_color || !prev_reservoir || !prev_hit_pos ||
                           !prev_hit_radiance)))
     return VLT_ERR_INVALID_ARG;
-  launch_spec_temporal(*fp, width, height, params->spec_m_cap, prev_gbuffer_depth, prev_gbuffer_color, gbuffer_depth,
-                       gbuffer_color, prev_reservoir, prev_hit_pos, prev_hit_radiance, new_hit_pos, new_hit_radiance,
-                       rw_reservoir, rw_hit_pos, rw_hit_radiance, frame_rand, has_prev_frame, (cudaStream_t)stream);
+  GeoArgs ga = {gbuffer_depth, gbuffer_color, fp->inv_view_proj, nullptr, nullptr, nullptr};
+  GeoArgs pga = {prev_gbuffer_depth, prev_gbuffer_color, fp->prev_inv_view_proj, nullptr, nullptr, nullptr};
+  launch_spec_temporal(*fp, width, height, params->spec_m_cap, ga, pga, prev_gbuffer_depth, prev_reservoir,
+                       prev_hit_pos, prev_hit_radiance, new_hit_pos, new_hit_radiance, rw_reservoir, rw_hit_pos,
+                       rw_hit_radiance, frame_rand, has_prev_frame, (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
 }
 
@@ -759,7 +772,8 @@ vlt_status vlt_ind_spec_spatial_resample(const vlt_frame_params* fp, uint32_t wi
   if ((rw_reservoir != nullptr) != (rw_hit_pos != nullptr) || (rw_reservoir != nullptr) != (rw_hit_radiance != nullptr))
     return VLT_ERR_INVALID_ARG;
   SpecKnobs sk = {params->spec_spatial_taps, params->spec_spatial_radius_px};
-  launch_spec_spatial(*fp, width, height, sk, gbuffer_color, gbuffer_depth, reservoir, hit_pos, hit_radiance,
+  GeoArgs ga = {gbuffer_depth, gbuffer_color, fp->inv_view_proj, nullptr, nullptr, nullptr};
+  launch_spec_spatial(*fp, width, height, sk, ga, reservoir, hit_pos, hit_radiance,
                       rw_lighting, rw_ray_len, rw_reservoir, rw_hit_pos, rw_hit_radiance, frame_rand,
                       (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
@@ -781,10 +795,11 @@ vlt_status vlt_denoise_temporal(const vlt_frame_params* fp, uint32_t width, uint
       (fast_history_on && (!rw_fast_history || (has_history && !fast_history))))
     return VLT_ERR_INVALID_ARG;
   DenoiseKnobs kn = {1.0f / params->history_max_frames, fast_history_on};
-  launch_dn_temporal(*fp, width, height, kn, depth_texture, gbuffer_texture, diff_source, spec_source, spec_ray_len,
-                     prev_depth_texture, prev_gbuffer_texture, color_history, (const uint32_t*)moments_history,
-                     history_len_texture, fast_history, rw_color, (uint32_t*)rw_moments, rw_history_len,
-                     rw_fast_history, has_history, (cudaStream_t)stream);
+  GeoArgs ga = {depth_texture, gbuffer_texture, fp->inv_view_proj, nullptr, nullptr, nullptr};
+  GeoArgs pga = {prev_depth_texture, prev_gbuffer_texture, fp->prev_inv_view_proj, nullptr, nullptr, nullptr};
+  launch_dn_temporal(*fp, width, height, kn, ga, pga, diff_source, spec_source, spec_ray_len, prev_depth_texture,
+                     color_history, (const uint32_t*)moments_history, history_len_texture, fast_history, rw_color,
+                     (uint32_t*)rw_moments, rw_history_len, rw_fast_history, has_history, (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
 }
 
@@ -795,7 +810,8 @@ vlt_status vlt_denoise_disocclusion_fix(uint32_t width, uint32_t height, const f
   if (!dims_ok(width, height) || !depth_texture || !gbuffer_texture || !history_len_texture || !color || !moments ||
       !rw_color || !rw_moments)
     return VLT_ERR_INVALID_ARG;
-  launch_dn_fix(width, height, depth_texture, gbuffer_texture, history_len_texture, color, (const uint32_t*)moments,
+  GeoArgs ga = {depth_texture, gbuffer_texture, nullptr, nullptr, nullptr, nullptr};
+  launch_dn_fix(width, height, ga, history_len_texture, color, (const uint32_t*)moments,
                 rw_color, (uint32_t*)rw_moments, (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
 }
@@ -814,7 +830,8 @@ vlt_status vlt_denoise_spatial_fallback(uint32_t width, uint32_t height, const f
   if (!dims_ok(width, height) || !depth_texture || !gbuffer_texture || !history_len_texture || !color || !moments ||
       !rw_color || !rw_variance)
     return VLT_ERR_INVALID_ARG;
-  launch_dn_fallback(width, height, depth_texture, gbuffer_texture, history_len_texture, color,
+  GeoArgs ga = {depth_texture, gbuffer_texture, nullptr, nullptr, nullptr, nullptr};
+  launch_dn_fallback(width, height, ga, history_len_texture, color,
                      (const uint32_t*)moments, rw_color, (uint32_t*)rw_variance, (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
 }
@@ -825,7 +842,8 @@ vlt_status vlt_denoise_atrous(uint32_t width, uint32_t height, const float* dept
   if (!dims_ok(width, height) || !depth_texture || !gbuffer_texture || !color || !variance || !rw_color ||
       !rw_variance || step_size < 1 || step_size > 4096)
     return VLT_ERR_INVALID_ARG;
-  launch_dn_atrous(width, height, depth_texture, gbuffer_texture, color, (const uint32_t*)variance, rw_color,
+  GeoArgs ga = {depth_texture, gbuffer_texture, nullptr, nullptr, nullptr, nullptr};
+  launch_dn_atrous(width, height, ga, color, (const uint32_t*)variance, rw_color,
                    (uint32_t*)rw_variance, nullptr, nullptr, step_size, (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
 }

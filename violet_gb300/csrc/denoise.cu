@@ -3,6 +3,7 @@
 // fallback / variance estimation, and the edge-stopping a-trous filter.
 // Colour history is a packed uint2 {diffuse, specular} of R11G11B10 words (one
 // 64-bit access per tap), moments/variance are half2, history length is R8_UNORM.
+// Kernels are templated on the geometry source (GeoRaw / GeoSurface).
 #include "vlt_internal.h"
 
 namespace vlt {
@@ -11,17 +12,27 @@ __device__ __forceinline__ f3 col_diff(uint2 c) { return unpack_r11g11b10(c.x); 
 __device__ __forceinline__ f3 col_spec(uint2 c) { return unpack_r11g11b10(c.y); }
 __device__ __forceinline__ f2 unpack_half2(uint32_t u) { return mk2(f16tof32(u & 0xFFFFu), f16tof32(u >> 16)); }
 
-// EdgeStoppingFunc (svgf.inc.hlsl:6-84).
+// EdgeStoppingFunc (svgf.inc.hlsl:6-84), with the per-centre reciprocals of the
+// luminance deviation, rcp(sigma_l * std + eps), computed once per pixel.
 struct EdgeStop {
   float depth_center, fwidth_z;
   f3 normal_center;
-  f2 lumi_center, lumi_std;
+  f2 lumi_center;
+  f2 lumi_rcp;
   bool use_lumi;
   float sigma_z;
   int sigma_n_log2;  // sigma_n = 2^k (128 -> 7, 32 -> 5)
 
-  __device__ __forceinline__ f2 weight(float tap_dist, float depth, f3 normal, f2 lumi) const {
+  __device__ __forceinline__ void set_lumi(f2 lumi, f2 var) {
     const float sigma_l = 4.0f;
+    const float eps = 1e-8f;
+    use_lumi = true;
+    lumi_center = lumi;
+    f2 sd = mk2(sqrt_(var.x), sqrt_(var.y));
+    lumi_rcp = mk2(1.0f / (sigma_l * sd.x + eps), 1.0f / (sigma_l * sd.y + eps));
+  }
+
+  __device__ __forceinline__ f2 weight(float tap_dist, float depth, f3 normal, f2 lumi) const {
     const float eps = 1e-8f;
     float dist_z = fabs_(depth - depth_center);
     float wz = -dist_z / ((sigma_z * fwidth_z) * tap_dist + eps);
@@ -30,7 +41,7 @@ struct EdgeStop {
     f2 wl = mk2(0.0f, 0.0f);
     if (use_lumi) {
       f2 dl = mk2(fabs_(lumi.x - lumi_center.x), fabs_(lumi.y - lumi_center.y));
-      wl = mk2(-dl.x * (1.0f / (sigma_l * lumi_std.x + eps)), -dl.y * (1.0f / (sigma_l * lumi_std.y + eps)));
+      wl = mk2(-dl.x * lumi_rcp.x, -dl.y * lumi_rcp.y);
     }
     return mk2(wn * exp_(wl.x + wz), wn * exp_(wl.y + wz));
   }
@@ -42,7 +53,7 @@ __device__ __forceinline__ EdgeStop make_edge_stop(float depth, float fwidth_z, 
   e.fwidth_z = fwidth_z;
   e.normal_center = normal;
   e.lumi_center = mk2(0.0f, 0.0f);
-  e.lumi_std = mk2(0.0f, 0.0f);
+  e.lumi_rcp = mk2(0.0f, 0.0f);
   e.use_lumi = false;
   e.sigma_z = 1.0f;
   e.sigma_n_log2 = 7;
@@ -58,14 +69,13 @@ __device__ __forceinline__ float dsr_weight(f3 color, f3 mean, f3 dev) {
 // --------------------------------------------------------------- temporal
 
 // svgf_temporal_filter.hlsl:96-362.
-__global__ void __launch_bounds__(128) k_dn_temporal(vlt_frame_params fp, int w, int h, DenoiseKnobs kn,
-                                                      const float* __restrict__ depth_tex,
-                                                      const uint32_t* __restrict__ gbuf,
+template <class Geo>
+__global__ void __launch_bounds__(128) k_dn_temporal(vlt_frame_params fp, int w, int h, DenoiseKnobs kn, Geo geo,
+                                                      Geo prev_geo, const uint32_t* __restrict__ gbuf,
                                                       const uint32_t* __restrict__ diff_src,
                                                       const uint32_t* __restrict__ spec_src,
                                                       const uint16_t* __restrict__ ray_len_tex,
                                                       const float* __restrict__ prev_depth,
-                                                      const uint32_t* __restrict__ prev_gbuf,
                                                       const uint2* __restrict__ color_hist,
                                                       const uint32_t* __restrict__ mom_hist,
                                                       const uint8_t* __restrict__ len_hist,
@@ -76,7 +86,7 @@ __global__ void __launch_bounds__(128) k_dn_temporal(vlt_frame_params fp, int w,
   int x = pix_x(), y = pix_y();
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
-  float depth = depth_tex[i];
+  float depth = geo.dep(i);
   if (depth == 0.0f) {
     out_len[i] = 0;
     out_color[i] = make_uint2(0u, 0u);
@@ -86,11 +96,16 @@ __global__ void __launch_bounds__(128) k_dn_temporal(vlt_frame_params fp, int w,
   }
   const float bw = (float)w, bh = (float)h;
   f2 screen_uv = mk2(((float)x + 0.5f) / bw, ((float)y + 0.5f) / bh);
-  GBuffer g = load_gbuffer(gbuf, x, y, w, h);
+  const f3 gnormal = geo.normal(i);
+  const float grough = geo.rough(i);
+  const float fwz = geo.fwz(i);
+  const float fwn = f16tof32(gbuf[2 * (size_t)w * h + i] >> 16);
 
   // 3x3 specular moments (x outer, y inner as in the shader).
   f3 m1 = mk3(0.0f), m2 = mk3(0.0f);
+#pragma unroll
   for (int dx = -1; dx <= 1; ++dx) {
+#pragma unroll
     for (int dy = -1; dy <= 1; ++dy) {
       int px = x + dx, py = y + dy;
       px = px < 0 ? 0 : (px > w - 1 ? w - 1 : px);
@@ -103,11 +118,12 @@ __global__ void __launch_bounds__(128) k_dn_temporal(vlt_frame_params fp, int w,
   m1 = m1 * (1.0f / 9.0f);
   m2 = m2 * (1.0f / 9.0f);
 
+  // The shader reconstructs the position from depth twice; both equal cs_depth_to_position.
+  const f3 position = geo.pos(x, y, i);
+
   // Virtual (hit-point) reprojection for specular.
   f3 vsh = mk3(0.0f), vsfh = mk3(0.0f);
   {
-    f4 ph = mul44(fp.inv_view_proj, mk4(screen_uv.x * 2.0f - 1.0f, screen_uv.y * 2.0f - 1.0f, depth, 1.0f));
-    f3 position = mk3(ph.x / ph.w, ph.y / ph.w, ph.z / ph.w);
     f3 vdir = normalize3(position - vpos3(fp.view_pos));
     float ray_len = f16tof32(ray_len_tex[i]);
     f3 vp = position + vdir * ray_len;
@@ -132,8 +148,6 @@ __global__ void __launch_bounds__(128) k_dn_temporal(vlt_frame_params fp, int w,
   f2 mv;
   float reproj_depth;
   {
-    f4 ph = mul44(fp.inv_view_proj, mk4(screen_uv.x * 2.0f - 1.0f, screen_uv.y * 2.0f - 1.0f, depth, 1.0f));
-    f3 position = mk3(ph.x / ph.w, ph.y / ph.w, ph.z / ph.w);
     f4 hp = mul44(fp.view_proj, mk4(position.x, position.y, position.z, 1.0f));
     f2 ndc = mk2(hp.x / hp.w - fp.jitter[0], hp.y / hp.w - fp.jitter[1]);
     f4 hr = mul44(fp.prev_view_proj, mk4(position.x, position.y, position.z, 1.0f));
@@ -151,22 +165,24 @@ __global__ void __launch_bounds__(128) k_dn_temporal(vlt_frame_params fp, int w,
     f2 pcc = mk2(huv.x * bw - 0.5f, huv.y * bh - 0.5f);
     f2 frac = mk2(pcc.x - floor_(pcc.x), pcc.y - floor_(pcc.y));
     int bx = f2i_rz(pcc.x), by = f2i_rz(pcc.y);
-    float depth_tol = g.fwidth_z * 4.0f + 1e-4f;
-    float normal_tol = g.fwidth_n * 16.0f + 1e-2f;
+    float depth_tol = fwz * 4.0f + 1e-4f;
+    float normal_tol = fwn * 16.0f + 1e-2f;
     float normal_tol_sq = normal_tol * normal_tol;
     float bb = frac.y, rr = frac.x, tt = 1.0f - bb, ll = 1.0f - rr;
     float wts[2][2] = {{tt * ll, tt * rr}, {bb * ll, bb * rr}};
     f3 ds = mk3(0.0f), ss = mk3(0.0f), dfs = mk3(0.0f), sfs = mk3(0.0f);
     f2 ms = mk2(0.0f, 0.0f);
     float hs = 0.0f, wsum = 0.0f;
+#pragma unroll
     for (int ox = 0; ox < 2; ++ox) {
+#pragma unroll
       for (int oy = 0; oy < 2; ++oy) {
         int px = bx + ox, py = by + oy;
         bool cv = px >= 0 && py >= 0 && px <= w - 1 && py <= h - 1;
         if (!cv) continue;
         size_t j = (size_t)py * w + px;
-        f3 n = gbuffer_normal(prev_gbuf[(size_t)w * h + j]);
-        f3 nd = n - g.normal;
+        f3 n = prev_geo.normal(j);
+        f3 nd = n - gnormal;
         bool ok = fabs_(prev_depth[j] - reproj_depth) < depth_tol && dot3(nd, nd) < normal_tol_sq;
         if (!ok) continue;
         float wt = wts[oy][ox];
@@ -208,13 +224,13 @@ __global__ void __launch_bounds__(128) k_dn_temporal(vlt_frame_params fp, int w,
 
   const float bfd = kn.blend_diff;
   const float bff = 1.0f / 3.0f;
-  float blurness = sqrt_(saturate(g.perceptual_roughness * 6.0f));
+  float blurness = sqrt_(saturate(grough * 6.0f));
   const float bfs = lerpf(7.0f / 8.0f, bfd, blurness);
   const float bfsf = lerpf(1.0f, bff, blurness);
   float ratio = VLT_HISTORY_LEN_UNIT / hl;
   f2 alpha = mk2(fmax_(bfd, ratio), fmax_(bfs, ratio));
   f3 df = lerp3(dh, dsrc, alpha.x);
-  f3 sf = lerp3(sh, ssrc, alpha.y);
+  f3 sf;
   f2 smf = mk2(lerpf(smh.x, smsrc.x, alpha.x), lerpf(smh.y, smsrc.y, alpha.y));
   f2 alpha_f = mk2(fmax_(bff, ratio), fmax_(bfsf, ratio));
   f3 dff = lerp3(dfh, dsrc, alpha_f.x);
@@ -249,6 +265,7 @@ __global__ void __launch_bounds__(128) k_dn_temporal(vlt_frame_params fp, int w,
 __device__ __forceinline__ float quad_max_len(const uint8_t* __restrict__ len, int x, int y, int w, int h) {
   int x0 = x & ~1, y0 = y & ~1;
   float m = 0.0f;
+#pragma unroll
   for (int k = 0; k < 4; ++k) {
     int px = x0 + (k & 1), py = y0 + (k >> 1);
     float v = inb(px, py, w, h) ? unorm8_load(len[(size_t)py * w + px]) : 0.0f;
@@ -261,9 +278,8 @@ __device__ __forceinline__ float quad_max_len(const uint8_t* __restrict__ len, i
 
 // relax_disocclusion_fix.hlsl:27-122. Pixels without geometry (history 0) are not
 // written by the shader; here they get zeros.
-__global__ void __launch_bounds__(128) k_dn_fix(int w, int h, const float* __restrict__ depth_tex,
-                                                 const uint32_t* __restrict__ gbuf,
-                                                 const uint8_t* __restrict__ len_tex,
+template <class Geo>
+__global__ void __launch_bounds__(128) k_dn_fix(int w, int h, Geo geo, const uint8_t* __restrict__ len_tex,
                                                  const uint2* __restrict__ color, const uint32_t* __restrict__ mom,
                                                  uint2* __restrict__ out_color, uint32_t* __restrict__ out_mom) {
   int x = pix_x(), y = pix_y();
@@ -278,9 +294,7 @@ __global__ void __launch_bounds__(128) k_dn_fix(int w, int h, const float* __res
   }
   hl = qmax;
   if (hl < 4.0f * VLT_HISTORY_LEN_UNIT) {
-    float dc = depth_tex[i];
-    GBuffer g = load_gbuffer(gbuf, x, y, w, h);
-    EdgeStop es = make_edge_stop(dc, g.fwidth_z, g.normal);
+    EdgeStop es = make_edge_stop(geo.dep(i), geo.fwz(i), geo.normal(i));
     es.sigma_z = 5.0f;
     es.sigma_n_log2 = 5;
     f2 ws = mk2(0.0f, 0.0f);
@@ -293,9 +307,7 @@ __global__ void __launch_bounds__(128) k_dn_fix(int w, int h, const float* __res
         int cx = x + offx, cy = y + offy;
         if (!(cx >= 0 && cy >= 0 && cx <= w - 1 && cy <= h - 1)) continue;
         size_t j = (size_t)cy * w + cx;
-        float d = depth_tex[j];
-        f3 n = gbuffer_normal(gbuf[(size_t)w * h + j]);
-        f2 wt = es.weight(length2(mk2((float)offx, (float)offy)), d, n, mk2(0.0f, 0.0f));
+        f2 wt = es.weight(length2(mk2((float)offx, (float)offy)), geo.dep(j), geo.normal(j), mk2(0.0f, 0.0f));
         uint2 c = color[j];
         f2 m = unpack_half2(mom[j]);
         ws = ws + wt;
@@ -364,9 +376,8 @@ __global__ void __launch_bounds__(128) k_dn_fast_clamp(int w, int h, const uint2
 // ---------------------------------------------------------- spatial fallback
 
 // svgf_spatial_fallback_filter.hlsl:25-125. History-0 pixels get zeros.
-__global__ void __launch_bounds__(128) k_dn_fallback(int w, int h, const float* __restrict__ depth_tex,
-                                                      const uint32_t* __restrict__ gbuf,
-                                                      const uint8_t* __restrict__ len_tex,
+template <class Geo>
+__global__ void __launch_bounds__(128) k_dn_fallback(int w, int h, Geo geo, const uint8_t* __restrict__ len_tex,
                                                       const uint2* __restrict__ color,
                                                       const uint32_t* __restrict__ mom, uint2* __restrict__ out_color,
                                                       uint32_t* __restrict__ out_var) {
@@ -384,9 +395,7 @@ __global__ void __launch_bounds__(128) k_dn_fallback(int w, int h, const float* 
   f3 dd, sd;
   f2 md;
   if (hl < 4.0f * VLT_HISTORY_LEN_UNIT) {
-    float dc = depth_tex[i];
-    GBuffer g = load_gbuffer(gbuf, x, y, w, h);
-    EdgeStop es = make_edge_stop(dc, g.fwidth_z * 3.0f, g.normal);
+    EdgeStop es = make_edge_stop(geo.dep(i), geo.fwz(i) * 3.0f, geo.normal(i));
     f2 ws = mk2(0.0f, 0.0f);
     f3 dsum = mk3(0.0f), ssum = mk3(0.0f);
     f2 msum = mk2(0.0f, 0.0f);
@@ -395,9 +404,7 @@ __global__ void __launch_bounds__(128) k_dn_fallback(int w, int h, const float* 
         int cx = x + ox, cy = y + oy;
         if (!(cx >= 0 && cy >= 0 && cx <= w - 1 && cy <= h - 1)) continue;
         size_t j = (size_t)cy * w + cx;
-        float d = depth_tex[j];
-        f3 n = gbuffer_normal(gbuf[(size_t)w * h + j]);
-        float wt = es.weight(length2(mk2((float)ox, (float)oy)), d, n, mk2(0.0f, 0.0f)).x;
+        float wt = es.weight(length2(mk2((float)ox, (float)oy)), geo.dep(j), geo.normal(j), mk2(0.0f, 0.0f)).x;
         uint2 c = color[j];
         f2 m = unpack_half2(mom[j]);
         ws = mk2(ws.x + wt, ws.y + wt);
@@ -425,10 +432,16 @@ __global__ void __launch_bounds__(128) k_dn_fallback(int w, int h, const float* 
 
 // --------------------------------------------------------------- a-trous
 
+// length(float2(coord_offset)) of the 16 off-axis taps at one step size,
+// tabulated once per launch (tap k = (oy+2)*4 + ox' over the non-zero offsets).
+struct AtrousTaps {
+  float dist[16];
+};
+
 // svgf_atrous_filter.hlsl:23-88: 5x5 taps at step 2^i, kernel {1, 2/3, 1/6}, only
 // the 16 taps off both centre axes (the shader's `(x != 0) && (y != 0)`).
-__global__ void __launch_bounds__(128) k_dn_atrous(int w, int h, const float* __restrict__ depth_tex,
-                                                    const uint32_t* __restrict__ gbuf,
+template <class Geo>
+__global__ void __launch_bounds__(128) k_dn_atrous(int w, int h, Geo geo, AtrousTaps taps,
                                                     const uint2* __restrict__ color,
                                                     const uint32_t* __restrict__ var_tex,
                                                     uint2* __restrict__ out_color, uint32_t* __restrict__ out_var,
@@ -437,37 +450,34 @@ __global__ void __launch_bounds__(128) k_dn_atrous(int w, int h, const float* __
   int x = pix_x(), y = pix_y();
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
-  const size_t plane = (size_t)w * h;
-  float dc = depth_tex[i];
-  GBuffer g = decode_gbuffer(gbuf[i], gbuf[plane + i], gbuf[2 * plane + i], gbuf[3 * plane + i]);
   uint2 cc = color[i];
   f3 diff_c = col_diff(cc), spec_c = col_spec(cc);
   f2 lumi_c = mk2(luminance(diff_c), luminance(spec_c));
   f2 var_c = unpack_half2(var_tex[i]);
-  EdgeStop es = make_edge_stop(dc, g.fwidth_z, g.normal);
-  es.use_lumi = true;
-  es.lumi_center = lumi_c;
-  es.lumi_std = mk2(sqrt_(var_c.x), sqrt_(var_c.y));
+  EdgeStop es = make_edge_stop(geo.dep(i), geo.fwz(i), geo.normal(i));
+  es.set_lumi(lumi_c, var_c);
   const float kw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
   f3 dsum = diff_c, ssum = spec_c;
   f2 vsum = var_c;
   f2 wsum = mk2(1.0f, 1.0f);
+  int tap = 0;
+#pragma unroll
   for (int oy = -2; oy <= 2; ++oy) {
-    float kwy = kw[oy < 0 ? -oy : oy];
+    if (oy == 0) continue;
+    const float kwy = kw[oy < 0 ? -oy : oy];
+#pragma unroll
     for (int ox = -2; ox <= 2; ++ox) {
-      int offx = ox * step, offy = oy * step;
-      int cx = x + offx, cy = y + offy;
+      if (ox == 0) continue;
+      const float tap_dist = taps.dist[tap++];
+      int cx = x + ox * step, cy = y + oy * step;
       bool cv = cx >= 0 && cy >= 0 && cx <= w - 1 && cy <= h - 1;
-      bool not_center = (ox != 0) && (oy != 0);
-      if (!(cv && not_center)) continue;
+      if (!cv) continue;
       float k = kwy * kw[ox < 0 ? -ox : ox];
       size_t j = (size_t)cy * w + cx;
       uint2 c = color[j];
       f3 d = col_diff(c), s = col_spec(c);
-      float dep = depth_tex[j];
-      f3 n = gbuffer_normal(gbuf[plane + j]);
       f2 lumi = mk2(luminance(d), luminance(s));
-      f2 e = es.weight(length2(mk2((float)offx, (float)offy)), dep, n, lumi);
+      f2 e = es.weight(tap_dist, geo.dep(j), geo.normal(j), lumi);
       f2 wt = mk2(k * e.x, k * e.y);
       f2 wv = wt * wt;
       dsum = dsum + wt.x * d;
@@ -499,41 +509,76 @@ __global__ void k_split_color(int n, const uint2* __restrict__ color, uint32_t* 
 
 static const dim3 kBlock(32, 4, 1);
 
-void launch_dn_temporal(const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn, const float* depth,
-                        const uint32_t* gbuf, const uint32_t* diff_src, const uint32_t* spec_src,
-                        const uint16_t* ray_len, const float* prev_depth, const uint32_t* prev_gbuf,
-                        const uint32_t* color_hist, const uint32_t* mom_hist, const uint8_t* len_hist,
-                        const uint32_t* fast_hist, uint32_t* out_color, uint32_t* out_mom, uint8_t* out_len,
-                        uint32_t* out_fast, uint32_t has_history, cudaStream_t s) {
-  k_dn_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
-      fp, w, h, kn, depth, gbuf, diff_src, spec_src, ray_len, prev_depth, prev_gbuf, (const uint2*)color_hist,
-      mom_hist, len_hist, (const uint2*)fast_hist, (uint2*)out_color, out_mom, out_len, (uint2*)out_fast,
-      has_history);
+static GeoRaw raw_geo(const GeoArgs& a, int w, int h) {
+  GeoRaw g = {a.depth, a.gbuf, a.inv_vp, w, h};
+  return g;
+}
+static GeoSurface surf_geo(const GeoArgs& a, int w, int h) {
+  GeoSurface g = {a.nd, a.pr, a.fz, w, h};
+  return g;
 }
 
-void launch_dn_fix(int w, int h, const float* depth, const uint32_t* gbuf, const uint8_t* len,
-                   const uint32_t* color, const uint32_t* mom, uint32_t* out_color, uint32_t* out_mom,
-                   cudaStream_t s) {
-  k_dn_fix<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, depth, gbuf, len, (const uint2*)color, mom,
-                                                     (uint2*)out_color, out_mom);
+void launch_dn_temporal(const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn, const GeoArgs& ga,
+                        const GeoArgs& prev_ga, const uint32_t* diff_src, const uint32_t* spec_src,
+                        const uint16_t* ray_len, const float* prev_depth, const uint32_t* color_hist,
+                        const uint32_t* mom_hist, const uint8_t* len_hist, const uint32_t* fast_hist,
+                        uint32_t* out_color, uint32_t* out_mom, uint8_t* out_len, uint32_t* out_fast,
+                        uint32_t has_history, cudaStream_t s) {
+  if (ga.nd)
+    k_dn_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
+        fp, w, h, kn, surf_geo(ga, w, h), surf_geo(prev_ga, w, h), ga.gbuf, diff_src, spec_src, ray_len, prev_depth,
+        (const uint2*)color_hist, mom_hist, len_hist, (const uint2*)fast_hist, (uint2*)out_color, out_mom, out_len,
+        (uint2*)out_fast, has_history);
+  else
+    k_dn_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
+        fp, w, h, kn, raw_geo(ga, w, h), raw_geo(prev_ga, w, h), ga.gbuf, diff_src, spec_src, ray_len, prev_depth,
+        (const uint2*)color_hist, mom_hist, len_hist, (const uint2*)fast_hist, (uint2*)out_color, out_mom, out_len,
+        (uint2*)out_fast, has_history);
+}
+
+void launch_dn_fix(int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color, const uint32_t* mom,
+                   uint32_t* out_color, uint32_t* out_mom, cudaStream_t s) {
+  if (ga.nd)
+    k_dn_fix<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, surf_geo(ga, w, h), len, (const uint2*)color, mom,
+                                                       (uint2*)out_color, out_mom);
+  else
+    k_dn_fix<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, raw_geo(ga, w, h), len, (const uint2*)color, mom,
+                                                       (uint2*)out_color, out_mom);
 }
 
 void launch_dn_fast_clamp(int w, int h, const uint32_t* fast, uint32_t* color, cudaStream_t s) {
   k_dn_fast_clamp<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, (const uint2*)fast, (uint2*)color);
 }
 
-void launch_dn_fallback(int w, int h, const float* depth, const uint32_t* gbuf, const uint8_t* len,
-                        const uint32_t* color, const uint32_t* mom, uint32_t* out_color, uint32_t* out_var,
-                        cudaStream_t s) {
-  k_dn_fallback<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, depth, gbuf, len, (const uint2*)color, mom,
-                                                          (uint2*)out_color, out_var);
+void launch_dn_fallback(int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color,
+                        const uint32_t* mom, uint32_t* out_color, uint32_t* out_var, cudaStream_t s) {
+  if (ga.nd)
+    k_dn_fallback<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, surf_geo(ga, w, h), len, (const uint2*)color, mom,
+                                                            (uint2*)out_color, out_var);
+  else
+    k_dn_fallback<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, raw_geo(ga, w, h), len, (const uint2*)color, mom,
+                                                            (uint2*)out_color, out_var);
 }
 
-void launch_dn_atrous(int w, int h, const float* depth, const uint32_t* gbuf, const uint32_t* color,
-                      const uint32_t* var, uint32_t* out_color, uint32_t* out_var, uint32_t* out_diff,
-                      uint32_t* out_spec, int step, cudaStream_t s) {
-  k_dn_atrous<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, depth, gbuf, (const uint2*)color, var,
-                                                        (uint2*)out_color, out_var, out_diff, out_spec, step);
+void launch_dn_atrous(int w, int h, const GeoArgs& ga, const uint32_t* color, const uint32_t* var,
+                      uint32_t* out_color, uint32_t* out_var, uint32_t* out_diff, uint32_t* out_spec, int step,
+                      cudaStream_t s) {
+  AtrousTaps taps;
+  int k = 0;
+  for (int oy = -2; oy <= 2; ++oy) {
+    if (oy == 0) continue;
+    for (int ox = -2; ox <= 2; ++ox) {
+      if (ox == 0) continue;
+      float fx = (float)(ox * step), fy = (float)(oy * step);
+      taps.dist[k++] = sqrtf(fx * fx + fy * fy);  // correctly rounded, == device sqrt.rn
+    }
+  }
+  if (ga.nd)
+    k_dn_atrous<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, surf_geo(ga, w, h), taps, (const uint2*)color, var,
+                                                          (uint2*)out_color, out_var, out_diff, out_spec, step);
+  else
+    k_dn_atrous<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, raw_geo(ga, w, h), taps, (const uint2*)color, var,
+                                                          (uint2*)out_color, out_var, out_diff, out_spec, step);
 }
 
 void launch_split_color(int w, int h, const uint32_t* color, uint32_t* diff, uint32_t* spec, cudaStream_t s) {

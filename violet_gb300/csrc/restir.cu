@@ -1,29 +1,51 @@
-// ReSTIR GI passes: indirect-diffuse temporal and spatial resampling, ray-traced AO
-// temporal accumulation and filter, indirect-specular temporal and spatial
-// resampling. One thread per pixel; records are loaded as packed 128/64/32-bit
-// words; every random-walk decision follows the binary32 contract of vlt_math.cuh.
+// ReSTIR GI passes: the per-frame surface decode, ray-traced AO temporal
+// accumulation and filter, indirect-diffuse temporal and spatial resampling,
+// indirect-specular temporal and spatial resampling. One thread per pixel; records
+// move as packed 128/64/32-bit words; every random-walk decision follows the
+// binary32 contract of vlt_math.cuh. Kernels are templated on the geometry source
+// (GeoRaw for the per-pass entry points, GeoSurface for the frame driver).
 #include "vlt_internal.h"
 
 namespace vlt {
+
+// ------------------------------------------------------------- surface
+
+// Decodes once per frame what the gathers would otherwise re-derive per tap.
+__global__ void __launch_bounds__(128) k_surface(vlt_frame_params fp, int w, int h, const float* __restrict__ depth,
+                                                  const uint32_t* __restrict__ g, float4* __restrict__ nd,
+                                                  float4* __restrict__ pr, float4* __restrict__ fz) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  size_t plane = (size_t)w * h;
+  float d = depth[i];
+  uint32_t e1 = g[plane + i];
+  f3 n = gbuffer_normal(e1);
+  f3 p = depth_to_position(fp.inv_view_proj, x, y, w, h, d);
+  f3 f0 = f0_from_layer0(g[i]);
+  nd[i] = make_float4(n.x, n.y, n.z, d);
+  pr[i] = make_float4(p.x, p.y, p.z, gbuffer_roughness(e1));
+  fz[i] = make_float4(f0.x, f0.y, f0.z, f16tof32(g[2 * plane + i] & 0xFFFFu));
+}
 
 // ---------------------------------------------------------------- AO gen
 
 // raytraced_ao_gen.hlsl:18-81. AO history is {ao, valid} in half2 (the x and a
 // channels of the reference's RGBA16F texture).
-__global__ void __launch_bounds__(128) k_ao_gen(vlt_frame_params fp, int w, int h,
+template <class Geo>
+__global__ void __launch_bounds__(128) k_ao_gen(vlt_frame_params fp, int w, int h, Geo geo,
                                                  const uint2* __restrict__ hit_pos_normal,
-                                                 const float* __restrict__ depth_buf,
                                                  const uint32_t* __restrict__ prev_ao, uint32_t* __restrict__ ao,
                                                  uint32_t has_new_sample, uint32_t has_prev_frame, float radius_ws) {
   int x = pix_x(), y = pix_y();
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
-  float depth = depth_buf[i];
+  float depth = geo.dep(i);
   if (depth == 0.0f) {
     ao[i] = 0u;
     return;
   }
-  f3 position = depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+  f3 position = geo.pos(x, y, i);
   f4 hpos = mul44(fp.view_proj, mk4(position.x, position.y, position.z, 1.0f));
   f2 ndc = mk2(hpos.x / hpos.w - fp.jitter[0], hpos.y / hpos.w - fp.jitter[1]);
   f4 hr = mul44(fp.prev_view_proj, mk4(position.x, position.y, position.z, 1.0f));
@@ -43,8 +65,7 @@ __global__ void __launch_bounds__(128) k_ao_gen(vlt_frame_params fp, int w, int 
   if (has_new_sample) {
     uint2 e = hit_pos_normal[i];
     f3 hp = hpn_pos(e.x, e.y);
-    f3 p2 = depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
-    float dist = length3(hp - p2);
+    float dist = length3(hp - position);
     float a_o = dist < radius_ws ? 0.0f : 1.0f;
     hx = lerpf(a_o, hx, (31.0f / 32.0f) * ha);
     ha = 1.0f;
@@ -72,8 +93,10 @@ __global__ void __launch_bounds__(128) k_ao_filter(int w, int h, const float* __
   }
   float center = f16tof32(ao[i] & 0xFFFFu);
   float col_med[3], col_min[3], col_max[3];
+#pragma unroll
   for (int dy = -1; dy <= 1; ++dy) {
     float row[3];
+#pragma unroll
     for (int dx = -1; dx <= 1; ++dx) {
       uint32_t cx = (uint32_t)x + (uint32_t)dx, cy = (uint32_t)y + (uint32_t)dy;
       cx = cx < (uint32_t)w ? cx : (uint32_t)w;
@@ -101,9 +124,9 @@ __global__ void __launch_bounds__(128) k_ao_filter(int w, int h, const float* __
 // ------------------------------------------------------ diffuse temporal
 
 // ind_diff_temporal_resample.hlsl:49-200. Record = {M8|W24, HitPosNormal.xy, R11G11B10}.
-__global__ void __launch_bounds__(128) k_diff_temporal(vlt_frame_params fp, int w, int h, DiffKnobs kn,
+template <class Geo>
+__global__ void __launch_bounds__(128) k_diff_temporal(vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo,
                                                         const float* __restrict__ prev_depth,
-                                                        const float* __restrict__ depth_buf,
                                                         const uint2* __restrict__ new_hpn,
                                                         const uint32_t* __restrict__ new_rad,
                                                         const float* __restrict__ new_pdf,
@@ -113,8 +136,7 @@ __global__ void __launch_bounds__(128) k_diff_temporal(vlt_frame_params fp, int 
   int x = pix_x(), y = pix_y();
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
-  float depth = depth_buf[i];
-  f3 pos = depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+  f3 pos = geo.pos(x, y, i);
   f4 hr = mul44(fp.prev_view_proj, mk4(pos.x, pos.y, pos.z, 1.0f));
   f3 ndc = mk3(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3], hr.z / hr.w - 0.0f);
   f2 uv = mk2(ndc.x * 0.5f + 0.5f, ndc.y * 0.5f + 0.5f);
@@ -191,23 +213,22 @@ __device__ __forceinline__ DiffSample load_diff(uint4 r, f3 pix_pos, f3 pix_n) {
 
 // ind_diff_spatial_resample.hlsl:94-337 (golden-spiral pattern, AO-guided and
 // adaptive radius, plane-distance test, Jacobian clamped to [0, 1]).
-__global__ void __launch_bounds__(128) k_diff_spatial(vlt_frame_params fp, int w, int h, DiffKnobs kn,
-                                                       const uint32_t* __restrict__ gbuf,
-                                                       const float* __restrict__ depth_buf,
+template <class Geo>
+__global__ void __launch_bounds__(128) k_diff_spatial(vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo,
                                                        const uint16_t* __restrict__ ao_tex,
                                                        const uint4* __restrict__ in, uint4* __restrict__ out,
                                                        uint32_t* __restrict__ lighting, uint32_t frame_rand) {
   int x = pix_x(), y = pix_y();
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
-  float depth = depth_buf[i];
+  float depth = geo.dep(i);
   if (depth == 0.0f) {
     out[i] = make_uint4(0u, 0u, 0u, 0u);
     if (lighting) lighting[i] = 0u;
     return;
   }
-  f3 pos = depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
-  f3 nrm = gbuffer_normal(gbuf[(size_t)w * h + i]);
+  f3 pos = geo.pos(x, y, i);
+  f3 nrm = geo.normal(i);
   float ao = f16tof32(ao_tex[i]);
   DiffSample r = load_diff(in[i], pos, nrm);
   float w_sum = r.W * r.tp * (float)r.M;
@@ -227,10 +248,9 @@ __global__ void __launch_bounds__(128) k_diff_spatial(vlt_frame_params fp, int w
     nx = nx < 0 ? 0 : (nx > w - 1 ? w - 1 : nx);
     ny = ny < 0 ? 0 : (ny > h - 1 ? h - 1 : ny);
     size_t j = (size_t)ny * w + nx;
-    f3 nn = gbuffer_normal(gbuf[(size_t)w * h + j]);
-    float dn = depth_buf[j];
+    f3 nn = geo.normal(j);
     bool diff = dot3(nrm, nn) < VLT_COS25;
-    f3 pn = depth_to_position(fp.inv_view_proj, nx, ny, w, h, dn);
+    f3 pn = geo.pos(nx, ny, j);
     float dist_to_plane = dot3(pn - pos, nrm);
     diff = diff || fabs_(dist_to_plane) > 0.05f;
     if (diff) {
@@ -288,62 +308,64 @@ __device__ __forceinline__ float lambda_pomc(float c, float roughness) {
   return (c + sqrt_((-r2 * c + c) * c + r2)) / 2.0f;
 }
 
-// smith_G2_over_G1_height_correlated_GGX, optimized branch (brdf.hlsl:133-137).
-__device__ __forceinline__ float g2_over_g1(float nol, float nov, float roughness) {
-  float r2 = roughness * roughness;
-  float kv = sqrt_((-r2 * nov + nov) * nov + r2) / nov;
-  float kl = sqrt_((-r2 * nol + nol) * nol + r2) / nol;
-  return (1.0f + kv) / (kv + kl);
-}
+// One factor of smith_G2_over_G1_height_correlated_GGX (brdf.hlsl:133-137).
+__device__ __forceinline__ float g_k(float c, float r2) { return sqrt_((-r2 * c + c) * c + r2) / c; }
 
 __device__ __forceinline__ f3 f_schlick(float u, f3 f0) {
   float f = pow5(1.0f - u);
   return mk3(f + f0.x * (1.0f - f), f + f0.y * (1.0f - f), f + f0.z * (1.0f - f));
 }
 
-struct SpecEval {
-  float source_pdf;
-  f3 brdf_nol_over_pdf;
-};
-
 // calc_things (ind_spec_temporal_resample.hlsl:63-144) == SpecTragetFunction::on_sample
-// (ind_spec_spatial_resample.hlsl:69-151).
-__device__ __forceinline__ SpecEval spec_eval(f3 view_pos, f3 pos, f3 n, float pr, f3 f0, f3 hit) {
-  SpecEval e;
-  float roughness = pr * pr;
-  roughness = fmax_(roughness, 0.002f);
-  f3 v = normalize3(view_pos - pos);
-  f3 l = normalize3(hit - pos);
-  f3 hv = normalize3(v + l);
-  float nov = saturate(dot3(n, v));
-  float noh = saturate(dot3(n, hv));
-  float D = d_ggx(noh, roughness);
-  float lp = lambda_pomc(nov, roughness);
-  e.source_pdf = 0.25f * D / lp;
-  float nol = saturate(dot3(n, l));
-  float loh = saturate(dot3(l, hv));
-  f3 F = f_schlick(loh, f0);
-  float g = g2_over_g1(nol, nov, roughness);
-  if (nol <= 0.0f) g = 0.0f;
-  if (nov <= 0.0f) g = 0.0f;
-  e.brdf_nol_over_pdf = F * g;
-  return e;
-}
+// (ind_spec_spatial_resample.hlsl:69-151), split into the part that depends only on
+// the shading point (view direction, NoV, Smith terms of V) and the per-sample part.
+struct SpecTarget {
+  f3 pos, n, f0, v;
+  float roughness, r2, nov, lp, kv;
 
-__device__ __forceinline__ float spec_tf(const SpecEval& e, f3 rad) {
-  return luminance(rad * e.brdf_nol_over_pdf) * e.source_pdf;
-}
-
+  __device__ __forceinline__ void init(f3 view_pos, f3 p, f3 nn, float pr, f3 f0v) {
+    pos = p;
+    n = nn;
+    f0 = f0v;
+    roughness = fmax_(pr * pr, 0.002f);
+    r2 = roughness * roughness;
+    v = normalize3(view_pos - p);
+    nov = saturate(dot3(n, v));
+    lp = lambda_pomc(nov, roughness);
+    kv = g_k(nov, r2);
+  }
+  // source pdf and luminance(radiance * brdf_NoL_over_source_pdf) * pdf.
+  __device__ __forceinline__ void eval(f3 hit, f3 rad, float* source_pdf, float* tf, float* w) const {
+    f3 l = normalize3(hit - pos);
+    f3 hv = normalize3(v + l);
+    float noh = saturate(dot3(n, hv));
+    float D = d_ggx(noh, roughness);
+    float sp = 0.25f * D / lp;
+    float nol = saturate(dot3(n, l));
+    float loh = saturate(dot3(l, hv));
+    f3 F = f_schlick(loh, f0);
+    float g = (1.0f + kv) / (kv + g_k(nol, r2));
+    if (nol <= 0.0f) g = 0.0f;
+    if (nov <= 0.0f) g = 0.0f;
+    float ww = luminance(rad * (F * g));
+    *source_pdf = sp;
+    *w = ww;
+    *tf = ww * sp;
+  }
+  __device__ __forceinline__ float tf(f3 hit, f3 rad) const {
+    float sp, t, ww;
+    eval(hit, rad, &sp, &t, &ww);
+    return t;
+  }
+};
 
 // ------------------------------------------------------ specular temporal
 
 // ind_spec_temporal_resample.hlsl:146-362 (VNDF source pdf, BRDF target function,
 // balance-heuristic MIS between previous and current domains).
-__global__ void __launch_bounds__(128) k_spec_temporal(vlt_frame_params fp, int w, int h, uint32_t m_cap,
-                                                        const float* __restrict__ prev_depth,
-                                                        const uint32_t* __restrict__ prev_gbuf,
-                                                        const float* __restrict__ depth_buf,
-                                                        const uint32_t* __restrict__ gbuf,
+template <class Geo>
+__global__ void __launch_bounds__(128) k_spec_temporal(vlt_frame_params fp, int w, int h, uint32_t m_cap, Geo geo,
+                                                        Geo prev_geo, const float* __restrict__ prev_depth,
                                                         const uint2* __restrict__ prev_rsv,
                                                         const float4* __restrict__ prev_hp,
                                                         const uint32_t* __restrict__ prev_rad,
@@ -355,7 +377,7 @@ __global__ void __launch_bounds__(128) k_spec_temporal(vlt_frame_params fp, int 
   int x = pix_x(), y = pix_y();
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
-  float depth = depth_buf[i];
+  float depth = geo.dep(i);
   float4 nhp4 = new_hp[i];
   uint32_t nrad_bits = new_rad[i];
   if (depth == 0.0f) {
@@ -364,7 +386,7 @@ __global__ void __launch_bounds__(128) k_spec_temporal(vlt_frame_params fp, int 
     out_rad[i] = nrad_bits;
     return;
   }
-  f3 pos = depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+  f3 pos = geo.pos(x, y, i);
   f4 hr = mul44(fp.prev_view_proj, mk4(pos.x, pos.y, pos.z, 1.0f));
   f3 ndc = mk3(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3], hr.z / hr.w - 0.0f);
   f2 uv = mk2(ndc.x * 0.5f + 0.5f, ndc.y * 0.5f + 0.5f);
@@ -378,11 +400,9 @@ __global__ void __launch_bounds__(128) k_spec_temporal(vlt_frame_params fp, int 
   f3 rhp = mk3(0.0f), rrad = mk3(0.0f);
   uint32_t rrad_bits = 0;
   float rtf = 0.0f;
-  GBuffer pg;
-  pg.color = mk3(0.0f);
-  pg.metallic = 0.0f;
-  pg.normal = mk3(0.0f);
-  pg.perceptual_roughness = 0.0f;
+  // `(GBuffer)0` of the shader when there is no previous sample (only used when M > 0).
+  f3 pn = mk3(0.0f), pf0 = specular_f0(mk3(0.0f), 0.0f);
+  float prough = 0.0f;
   if (sample_prev) {
     int px = (int)f2u_rz(uv.x * (float)w), py = (int)f2u_rz(uv.y * (float)h);
     uint2 rs = ld(prev_rsv, px, py, w, h);
@@ -393,28 +413,26 @@ __global__ void __launch_bounds__(128) k_spec_temporal(vlt_frame_params fp, int 
     rrad_bits = ld(prev_rad, px, py, w, h);
     rrad = unpack_r11g11b10(rrad_bits);
     rtf = p4.w;
-    pg = load_gbuffer(prev_gbuf, px, py, w, h);
+    prev_geo.material_or_zero(px, py, &pn, &prough, &pf0);
   }
   f3 nhp = mk3(nhp4.x, nhp4.y, nhp4.z);
   f3 nrad = unpack_r11g11b10(nrad_bits);
-  GBuffer g = load_gbuffer(gbuf, x, y, w, h);
-  uint32_t mmax = f2u_rz((float)m_cap * g.perceptual_roughness);
+  float rough = geo.rough(i);
+  uint32_t mmax = f2u_rz((float)m_cap * rough);
   M = M < mmax ? M : mmax;
-  f3 view_pos = vpos3(fp.view_pos);
-  f3 f0 = specular_f0(g.color, g.metallic);
-  SpecEval cur = spec_eval(view_pos, pos, g.normal, g.perceptual_roughness, f0, nhp);
-  float new_w = luminance(nrad * cur.brdf_nol_over_pdf);
-  float new_tf = new_w * cur.source_pdf;
+  SpecTarget cur;
+  cur.init(vpos3(fp.view_pos), pos, geo.normal(i), rough, geo.f0(i));
+  float sp_new, new_tf, new_w;
+  cur.eval(nhp, nrad, &sp_new, &new_tf, &new_w);
   float prev_w = W * (rtf * (float)M);
   if (M > 0) {
-    SpecEval poc = spec_eval(vpos3(fp.prev_view_pos), pos, pg.normal, pg.perceptual_roughness,
-                             specular_f0(pg.color, pg.metallic), nhp);
-    float ptoc = luminance(nrad * poc.brdf_nol_over_pdf) * poc.source_pdf;
+    SpecTarget prv;
+    prv.init(vpos3(fp.prev_view_pos), pos, pn, prough, pf0);
+    float ptoc = prv.tf(nhp, nrad);
     float curr_m = new_tf / (new_tf + ptoc * (float)M);
     if (new_tf == 0.0f) curr_m = 0.0f;
     new_w = curr_m * new_w;
-    SpecEval cop = spec_eval(view_pos, pos, g.normal, g.perceptual_roughness, f0, rhp);
-    float ctop = luminance(rrad * cop.brdf_nol_over_pdf) * cop.source_pdf;
+    float ctop = cur.tf(rhp, rrad);
     float m_num = rtf * (float)M;
     float prev_m = m_num / (m_num + ctop);
     if (m_num == 0.0f) prev_m = 0.0f;
@@ -466,9 +484,8 @@ __device__ __forceinline__ f3 ggx_integral(float nov, float roughness, f3 f0) {
 
 // ind_spec_spatial_resample.hlsl:169-448. Optionally also stores the merged
 // reservoir (for chaining several spatial passes; the reference runs one).
-__global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w, int h, SpecKnobs kn,
-                                                       const uint32_t* __restrict__ gbuf,
-                                                       const float* __restrict__ depth_buf,
+template <class Geo>
+__global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo,
                                                        const uint2* __restrict__ rsv,
                                                        const float4* __restrict__ hp_tex,
                                                        const uint32_t* __restrict__ rad_tex,
@@ -478,7 +495,7 @@ __global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w
   int x = pix_x(), y = pix_y();
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
-  float depth = depth_buf[i];
+  float depth = geo.dep(i);
   if (depth == 0.0f) {
     if (lighting) lighting[i] = 0u;
     if (ray_len_out) ray_len_out[i] = 0;
@@ -489,8 +506,11 @@ __global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w
     }
     return;
   }
-  f3 pos = depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
-  GBuffer g = load_gbuffer(gbuf, x, y, w, h);
+  f3 pos = geo.pos(x, y, i);
+  const f3 view_pos = vpos3(fp.view_pos);
+  float prc = geo.rough(i);
+  SpecTarget center;
+  center.init(view_pos, pos, geo.normal(i), prc, geo.f0(i));
   uint2 rs = rsv[i];
   uint32_t M = rs.x;
   float W = as_float(rs.y);
@@ -499,9 +519,7 @@ __global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w
   uint32_t rad_bits = rad_tex[i];
   f3 rad = unpack_r11g11b10(rad_bits);
   float ctf = hp4.w;
-  f3 view_pos = vpos3(fp.view_pos);
-  f3 f0 = specular_f0(g.color, g.metallic);
-  const uint32_t n_iter = f2u_rz(0.0f + g.perceptual_roughness * ((float)kn.taps - 0.0f));
+  const uint32_t n_iter = f2u_rz(0.0f + prc * ((float)kn.taps - 0.0f));
   float radius = kn.radius_px > 0.0f ? kn.radius_px : (float)(w < h ? w : h) * 0.05f;
   uint32_t rng = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
   for (uint32_t it = 0; it < n_iter; ++it) {
@@ -515,12 +533,11 @@ __global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w
     nx = nx < 0 ? 0 : (nx > w - 1 ? w - 1 : nx);
     ny = ny < 0 ? 0 : (ny > h - 1 ? h - 1 : ny);
     if (nx == x && ny == y) continue;
-    GBuffer gn = load_gbuffer(gbuf, nx, ny, w, h);
     size_t j = (size_t)ny * w + nx;
-    float dn = depth_buf[j];
-    bool diff = dot3(g.normal, gn.normal) < VLT_COS25;
-    f3 pn = depth_to_position(fp.inv_view_proj, nx, ny, w, h, dn);
-    float dist_to_plane = dot3(pn - pos, g.normal);
+    f3 nn = geo.normal(j);
+    bool diff = dot3(center.n, nn) < VLT_COS25;
+    f3 pn = geo.pos(nx, ny, j);
+    float dist_to_plane = dot3(pn - pos, center.n);
     diff = diff || fabs_(dist_to_plane) > 0.05f;
     if (diff) {
       radius = fmax_(radius * 0.5f, 1.5f);
@@ -536,14 +553,13 @@ __global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w
     float tfn = hpn4.w;
     float w_nb, w_c;
     {
-      SpecEval c_on_n = spec_eval(view_pos, pos, g.normal, g.perceptual_roughness, f0, hitn);
-      float ctf_on_n = spec_tf(c_on_n, radn);
+      float ctf_on_n = center.tf(hitn, radn);
       float m_nb = (tfn * (float)Mn) / (tfn * (float)Mn + ctf_on_n * (float)M);
       if (tfn * (float)Mn == 0.0f) m_nb = 0.0f;
       w_nb = m_nb * tfn * Wn;
-      SpecEval n_on_c = spec_eval(view_pos, pn, gn.normal, gn.perceptual_roughness,
-                                  specular_f0(gn.color, gn.metallic), hit);
-      float ntf_on_c = spec_tf(n_on_c, rad);
+      SpecTarget nbt;
+      nbt.init(view_pos, pn, nn, geo.rough(j), geo.f0(j));
+      float ntf_on_c = nbt.tf(hit, rad);
       float m_c = (ctf * (float)M) / (ctf * (float)M + ntf_on_c * (float)Mn);
       if (ctf * (float)M == 0.0f) m_c = 0.0f;
       w_c = m_c * ctf * W;
@@ -566,23 +582,21 @@ __global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w
     out_rad[i] = rad_bits;
   }
   if (lighting) {
-    float roughness = fmax_(g.perceptual_roughness * g.perceptual_roughness, 0.002f);
+    const float roughness = center.roughness;
     f3 l = normalize3(hit - pos);
-    f3 v = normalize3(view_pos - pos);
-    f3 hv = normalize3(v + l);
-    float nol = saturate(dot3(g.normal, l));
-    float nov = saturate(dot3(g.normal, v));
-    float noh = saturate(dot3(g.normal, hv));
+    f3 hv = normalize3(center.v + l);
+    float nol = saturate(dot3(center.n, l));
+    float nov = center.nov;
+    float noh = saturate(dot3(center.n, hv));
     float loh = saturate(dot3(l, hv));
-    f3 F = f_schlick(loh, f0);
+    f3 F = f_schlick(loh, center.f0);
     float D = d_ggx(noh, roughness);
-    float lp = lambda_pomc(nov, roughness);
-    float vndf = 0.25f * D / lp;
-    float gg = g2_over_g1(nol, nov, roughness);
+    float vndf = 0.25f * D / center.lp;
+    float gg = (1.0f + center.kv) / (center.kv + g_k(nol, center.r2));
     if (nol <= 0.0f) gg = 0.0f;
     if (nov <= 0.0f) gg = 0.0f;
     f3 li = rad * ((F * gg) * (vndf * W));
-    f3 refl = ggx_integral(nov, roughness, f0);
+    f3 refl = ggx_integral(nov, roughness, center.f0);
     refl = mk3(fmax_(refl.x, 1.0f / 65536.0f), fmax_(refl.y, 1.0f / 65536.0f), fmax_(refl.z, 1.0f / 65536.0f));
     li = li / refl;
     lighting[i] = pack_r11g11b10(li);
@@ -594,50 +608,98 @@ __global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w
 
 static const dim3 kBlock(32, 4, 1);
 
-void launch_ao_gen(const vlt_frame_params& fp, int w, int h, const uint32_t* hpn, const float* depth,
+template <class Geo>
+static Geo make_geo(const GeoArgs& a, int w, int h);
+
+template <>
+GeoRaw make_geo<GeoRaw>(const GeoArgs& a, int w, int h) {
+  GeoRaw g = {a.depth, a.gbuf, a.inv_vp, w, h};
+  return g;
+}
+template <>
+GeoSurface make_geo<GeoSurface>(const GeoArgs& a, int w, int h) {
+  GeoSurface g = {a.nd, a.pr, a.fz, w, h};
+  return g;
+}
+
+void launch_surface(const vlt_frame_params& fp, int w, int h, const float* depth, const uint32_t* gbuf, float4* nd,
+                    float4* pr, float4* fz, cudaStream_t s) {
+  k_surface<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, depth, gbuf, nd, pr, fz);
+}
+
+void launch_ao_gen(const vlt_frame_params& fp, int w, int h, const GeoArgs& ga, const uint32_t* hpn,
                    const uint32_t* prev_ao, uint32_t* ao, uint32_t has_new, uint32_t has_prev, float radius,
                    cudaStream_t s) {
-  k_ao_gen<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, (const uint2*)hpn, depth, prev_ao, ao, has_new,
-                                                     has_prev, radius);
+  if (ga.nd)
+    k_ao_gen<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, make_geo<GeoSurface>(ga, w, h), (const uint2*)hpn,
+                                                       prev_ao, ao, has_new, has_prev, radius);
+  else
+    k_ao_gen<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, make_geo<GeoRaw>(ga, w, h), (const uint2*)hpn,
+                                                       prev_ao, ao, has_new, has_prev, radius);
 }
 
 void launch_ao_filter(int w, int h, const float* depth, const uint32_t* ao, uint16_t* out, cudaStream_t s) {
   k_ao_filter<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, depth, ao, out);
 }
 
-void launch_diff_temporal(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const float* prev_depth,
-                          const float* depth, const uint32_t* new_hpn, const uint32_t* new_rad, const float* new_pdf,
-                          const uint32_t* prev_rsv, uint32_t* out, uint32_t frame_rand, uint32_t has_prev,
-                          uint32_t has_new, cudaStream_t s) {
-  k_diff_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, prev_depth, depth, (const uint2*)new_hpn,
-                                                            new_rad, new_pdf, (const uint4*)prev_rsv, (uint4*)out,
-                                                            frame_rand, has_prev, has_new);
+void launch_diff_temporal(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
+                          const float* prev_depth, const uint32_t* new_hpn, const uint32_t* new_rad,
+                          const float* new_pdf, const uint32_t* prev_rsv, uint32_t* out, uint32_t frame_rand,
+                          uint32_t has_prev, uint32_t has_new, cudaStream_t s) {
+  if (ga.nd)
+    k_diff_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, make_geo<GeoSurface>(ga, w, h), prev_depth,
+                                                              (const uint2*)new_hpn, new_rad, new_pdf,
+                                                              (const uint4*)prev_rsv, (uint4*)out, frame_rand,
+                                                              has_prev, has_new);
+  else
+    k_diff_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, make_geo<GeoRaw>(ga, w, h), prev_depth,
+                                                              (const uint2*)new_hpn, new_rad, new_pdf,
+                                                              (const uint4*)prev_rsv, (uint4*)out, frame_rand,
+                                                              has_prev, has_new);
 }
 
-void launch_diff_spatial(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const uint32_t* gbuf,
-                         const float* depth, const uint16_t* ao, const uint32_t* in, uint32_t* out,
-                         uint32_t* lighting, uint32_t frame_rand, cudaStream_t s) {
-  k_diff_spatial<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, gbuf, depth, ao, (const uint4*)in,
-                                                           (uint4*)out, lighting, frame_rand);
-}
-
-void launch_spec_temporal(const vlt_frame_params& fp, int w, int h, uint32_t m_cap, const float* prev_depth,
-                          const uint32_t* prev_gbuf, const float* depth, const uint32_t* gbuf,
-                          const uint32_t* prev_rsv, const float* prev_hp, const uint32_t* prev_rad,
-                          const float* new_hp, const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp,
-                          uint32_t* out_rad, uint32_t frame_rand, uint32_t has_prev, cudaStream_t s) {
-  k_spec_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
-      fp, w, h, m_cap, prev_depth, prev_gbuf, depth, gbuf, (const uint2*)prev_rsv, (const float4*)prev_hp, prev_rad,
-      (const float4*)new_hp, new_rad, (uint2*)out_rsv, (float4*)out_hp, out_rad, frame_rand, has_prev);
-}
-
-void launch_spec_spatial(const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn, const uint32_t* gbuf,
-                         const float* depth, const uint32_t* rsv, const float* hp, const uint32_t* rad,
-                         uint32_t* lighting, uint16_t* ray_len, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
+void launch_diff_spatial(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
+                         const uint16_t* ao, const uint32_t* in, uint32_t* out, uint32_t* lighting,
                          uint32_t frame_rand, cudaStream_t s) {
-  k_spec_spatial<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, gbuf, depth, (const uint2*)rsv,
-                                                           (const float4*)hp, rad, lighting, ray_len,
-                                                           (uint2*)out_rsv, (float4*)out_hp, out_rad, frame_rand);
+  if (ga.nd)
+    k_diff_spatial<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, make_geo<GeoSurface>(ga, w, h), ao,
+                                                             (const uint4*)in, (uint4*)out, lighting, frame_rand);
+  else
+    k_diff_spatial<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, make_geo<GeoRaw>(ga, w, h), ao,
+                                                             (const uint4*)in, (uint4*)out, lighting, frame_rand);
+}
+
+void launch_spec_temporal(const vlt_frame_params& fp, int w, int h, uint32_t m_cap, const GeoArgs& ga,
+                          const GeoArgs& prev_ga, const float* prev_depth, const uint32_t* prev_rsv,
+                          const float* prev_hp, const uint32_t* prev_rad, const float* new_hp,
+                          const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
+                          uint32_t frame_rand, uint32_t has_prev, cudaStream_t s) {
+  if (ga.nd)
+    k_spec_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
+        fp, w, h, m_cap, make_geo<GeoSurface>(ga, w, h), make_geo<GeoSurface>(prev_ga, w, h), prev_depth,
+        (const uint2*)prev_rsv, (const float4*)prev_hp, prev_rad, (const float4*)new_hp, new_rad, (uint2*)out_rsv,
+        (float4*)out_hp, out_rad, frame_rand, has_prev);
+  else
+    k_spec_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
+        fp, w, h, m_cap, make_geo<GeoRaw>(ga, w, h), make_geo<GeoRaw>(prev_ga, w, h), prev_depth,
+        (const uint2*)prev_rsv, (const float4*)prev_hp, prev_rad, (const float4*)new_hp, new_rad, (uint2*)out_rsv,
+        (float4*)out_hp, out_rad, frame_rand, has_prev);
+}
+
+void launch_spec_spatial(const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn, const GeoArgs& ga,
+                         const uint32_t* rsv, const float* hp, const uint32_t* rad, uint32_t* lighting,
+                         uint16_t* ray_len, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad, uint32_t frame_rand,
+                         cudaStream_t s) {
+  if (ga.nd)
+    k_spec_spatial<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, make_geo<GeoSurface>(ga, w, h),
+                                                             (const uint2*)rsv, (const float4*)hp, rad, lighting,
+                                                             ray_len, (uint2*)out_rsv, (float4*)out_hp, out_rad,
+                                                             frame_rand);
+  else
+    k_spec_spatial<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, make_geo<GeoRaw>(ga, w, h),
+                                                             (const uint2*)rsv, (const float4*)hp, rad, lighting,
+                                                             ray_len, (uint2*)out_rsv, (float4*)out_hp, out_rad,
+                                                             frame_rand);
 }
 
 }  // namespace vlt

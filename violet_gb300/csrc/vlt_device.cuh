@@ -120,6 +120,89 @@ __device__ __forceinline__ uint32_t ld_g1(const uint32_t* __restrict__ g, int x,
   return inb(x, y, w, h) ? g[(size_t)w * h + (size_t)y * w + x] : 0u;
 }
 
+// ----------------------------------------------------------- geometry sources
+//
+// The passes read per-pixel surface attributes (depth, decoded normal, world
+// position, perceptual roughness, specular f0, fwidth_z) of the current and the
+// previous frame many times per pixel. Two interchangeable sources give them,
+// with bit-identical values:
+//   GeoRaw     decodes the G-buffer/depth on every access (the per-pass entry
+//              points, which take only the reference's textures);
+//   GeoSurface loads them from three float4 planes written once per frame by
+//              k_surface (the frame driver): nd = {normal, depth},
+//              pr = {position, roughness}, fz = {f0, fwidth_z}.
+// Accesses with `_or_zero` may be out of range and then return what decoding an
+// all-zero G-buffer texel gives (the value of an out-of-range texture load).
+
+__device__ __forceinline__ f3 f0_from_layer0(uint32_t e0) {
+  f3 color = mk3((float)(e0 & 0xFFu) / 255.0f, (float)((e0 >> 8) & 0xFFu) / 255.0f,
+                 (float)((e0 >> 16) & 0xFFu) / 255.0f);
+  float metallic = (float)((e0 >> 24) & 0xFFu) / 255.0f;
+  return specular_f0(color, metallic);
+}
+
+struct GeoRaw {
+  const float* __restrict__ depth;
+  const uint32_t* __restrict__ g;
+  const float* inv_vp;  // may be null when positions are not needed
+  int w, h;
+  __device__ __forceinline__ size_t plane() const { return (size_t)w * h; }
+  __device__ __forceinline__ float dep(size_t i) const { return depth[i]; }
+  __device__ __forceinline__ f3 normal(size_t i) const { return gbuffer_normal(g[plane() + i]); }
+  __device__ __forceinline__ float rough(size_t i) const { return gbuffer_roughness(g[plane() + i]); }
+  __device__ __forceinline__ f3 f0(size_t i) const { return f0_from_layer0(g[i]); }
+  __device__ __forceinline__ float fwz(size_t i) const { return f16tof32(g[2 * plane() + i] & 0xFFFFu); }
+  __device__ __forceinline__ f3 pos(int x, int y, size_t i) const {
+    return depth_to_position(inv_vp, x, y, w, h, depth[i]);
+  }
+  // G-buffer fields at a possibly out-of-range texel (normal, roughness, f0).
+  __device__ __forceinline__ void material_or_zero(int x, int y, f3* n, float* r, f3* f0v) const {
+    uint32_t e0 = 0u, e1 = 0u;
+    if (inb(x, y, w, h)) {
+      size_t i = (size_t)y * w + x;
+      e0 = g[i];
+      e1 = g[plane() + i];
+    }
+    *n = gbuffer_normal(e1);
+    *r = gbuffer_roughness(e1);
+    *f0v = f0_from_layer0(e0);
+  }
+};
+
+struct GeoSurface {
+  const float4* __restrict__ nd;
+  const float4* __restrict__ pr;
+  const float4* __restrict__ fz;
+  int w, h;
+  __device__ __forceinline__ float dep(size_t i) const { return nd[i].w; }
+  __device__ __forceinline__ f3 normal(size_t i) const {
+    float4 v = nd[i];
+    return mk3(v.x, v.y, v.z);
+  }
+  __device__ __forceinline__ float rough(size_t i) const { return pr[i].w; }
+  __device__ __forceinline__ f3 f0(size_t i) const {
+    float4 v = fz[i];
+    return mk3(v.x, v.y, v.z);
+  }
+  __device__ __forceinline__ float fwz(size_t i) const { return fz[i].w; }
+  __device__ __forceinline__ f3 pos(int, int, size_t i) const {
+    float4 v = pr[i];
+    return mk3(v.x, v.y, v.z);
+  }
+  __device__ __forceinline__ void material_or_zero(int x, int y, f3* n, float* r, f3* f0v) const {
+    if (inb(x, y, w, h)) {
+      size_t i = (size_t)y * w + x;
+      *n = normal(i);
+      *r = rough(i);
+      *f0v = f0(i);
+    } else {
+      *n = gbuffer_normal(0u);
+      *r = gbuffer_roughness(0u);
+      *f0v = f0_from_layer0(0u);
+    }
+  }
+};
+
 inline dim3 grid2d(uint32_t w, uint32_t h, dim3 block) {
   return dim3((w + block.x - 1) / block.x, (h + block.y - 1) / block.y, 1);
 }

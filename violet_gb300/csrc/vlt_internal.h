@@ -26,47 +26,59 @@ struct DenoiseKnobs {
   uint32_t fast_history;
 };
 
+// Geometry source of a launch: the raw depth/G-buffer (decoded per access) or, when
+// `nd` is set, the per-frame surface planes written by launch_surface. The raw
+// pointers are always set (some passes read G-buffer fields the planes omit).
+struct GeoArgs {
+  const float* depth;
+  const uint32_t* gbuf;
+  const float* inv_vp;
+  const float4* nd;
+  const float4* pr;
+  const float4* fz;
+};
+
 // restir.cu
-void launch_ao_gen(const vlt_frame_params& fp, int w, int h, const uint32_t* hpn, const float* depth,
+void launch_surface(const vlt_frame_params& fp, int w, int h, const float* depth, const uint32_t* gbuf, float4* nd,
+                    float4* pr, float4* fz, cudaStream_t s);
+void launch_ao_gen(const vlt_frame_params& fp, int w, int h, const GeoArgs& ga, const uint32_t* hpn,
                    const uint32_t* prev_ao, uint32_t* ao, uint32_t has_new, uint32_t has_prev, float radius,
                    cudaStream_t s);
 void launch_ao_filter(int w, int h, const float* depth, const uint32_t* ao, uint16_t* out, cudaStream_t s);
-void launch_diff_temporal(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const float* prev_depth,
-                          const float* depth, const uint32_t* new_hpn, const uint32_t* new_rad, const float* new_pdf,
-                          const uint32_t* prev_rsv, uint32_t* out, uint32_t frame_rand, uint32_t has_prev,
-                          uint32_t has_new, cudaStream_t s);
-void launch_diff_spatial(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const uint32_t* gbuf,
-                         const float* depth, const uint16_t* ao, const uint32_t* in, uint32_t* out,
-                         uint32_t* lighting, uint32_t frame_rand, cudaStream_t s);
-void launch_spec_temporal(const vlt_frame_params& fp, int w, int h, uint32_t m_cap, const float* prev_depth,
-                          const uint32_t* prev_gbuf, const float* depth, const uint32_t* gbuf,
-                          const uint32_t* prev_rsv, const float* prev_hp, const uint32_t* prev_rad,
-                          const float* new_hp, const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp,
-                          uint32_t* out_rad, uint32_t frame_rand, uint32_t has_prev, cudaStream_t s);
-void launch_spec_spatial(const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn, const uint32_t* gbuf,
-                         const float* depth, const uint32_t* rsv, const float* hp, const uint32_t* rad,
-                         uint32_t* lighting, uint16_t* ray_len, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
+void launch_diff_temporal(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
+                          const float* prev_depth, const uint32_t* new_hpn, const uint32_t* new_rad,
+                          const float* new_pdf, const uint32_t* prev_rsv, uint32_t* out, uint32_t frame_rand,
+                          uint32_t has_prev, uint32_t has_new, cudaStream_t s);
+void launch_diff_spatial(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
+                         const uint16_t* ao, const uint32_t* in, uint32_t* out, uint32_t* lighting,
                          uint32_t frame_rand, cudaStream_t s);
+void launch_spec_temporal(const vlt_frame_params& fp, int w, int h, uint32_t m_cap, const GeoArgs& ga,
+                          const GeoArgs& prev_ga, const float* prev_depth, const uint32_t* prev_rsv,
+                          const float* prev_hp, const uint32_t* prev_rad, const float* new_hp,
+                          const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
+                          uint32_t frame_rand, uint32_t has_prev, cudaStream_t s);
+void launch_spec_spatial(const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn, const GeoArgs& ga,
+                         const uint32_t* rsv, const float* hp, const uint32_t* rad, uint32_t* lighting,
+                         uint16_t* ray_len, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad, uint32_t frame_rand,
+                         cudaStream_t s);
 
 // denoise.cu
-void launch_dn_temporal(const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn, const float* depth,
-                        const uint32_t* gbuf, const uint32_t* diff_src, const uint32_t* spec_src,
-                        const uint16_t* ray_len, const float* prev_depth, const uint32_t* prev_gbuf,
-                        const uint32_t* color_hist, const uint32_t* mom_hist, const uint8_t* len_hist,
-                        const uint32_t* fast_hist, uint32_t* out_color, uint32_t* out_mom, uint8_t* out_len,
-                        uint32_t* out_fast, uint32_t has_history, cudaStream_t s);
-void launch_dn_fix(int w, int h, const float* depth, const uint32_t* gbuf, const uint8_t* len,
-                   const uint32_t* color, const uint32_t* mom, uint32_t* out_color, uint32_t* out_mom,
-                   cudaStream_t s);
+void launch_dn_temporal(const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn, const GeoArgs& ga,
+                        const GeoArgs& prev_ga, const uint32_t* diff_src, const uint32_t* spec_src,
+                        const uint16_t* ray_len, const float* prev_depth, const uint32_t* color_hist,
+                        const uint32_t* mom_hist, const uint8_t* len_hist, const uint32_t* fast_hist,
+                        uint32_t* out_color, uint32_t* out_mom, uint8_t* out_len, uint32_t* out_fast,
+                        uint32_t has_history, cudaStream_t s);
+void launch_dn_fix(int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color, const uint32_t* mom,
+                   uint32_t* out_color, uint32_t* out_mom, cudaStream_t s);
 void launch_dn_fast_clamp(int w, int h, const uint32_t* fast, uint32_t* color, cudaStream_t s);
-void launch_dn_fallback(int w, int h, const float* depth, const uint32_t* gbuf, const uint8_t* len,
-                        const uint32_t* color, const uint32_t* mom, uint32_t* out_color, uint32_t* out_var,
-                        cudaStream_t s);
+void launch_dn_fallback(int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color,
+                        const uint32_t* mom, uint32_t* out_color, uint32_t* out_var, cudaStream_t s);
 // out_diff/out_spec (optional): write the result as two separate R11G11B10 planes
-// instead of the packed colour pair.
-void launch_dn_atrous(int w, int h, const float* depth, const uint32_t* gbuf, const uint32_t* color,
-                      const uint32_t* var, uint32_t* out_color, uint32_t* out_var, uint32_t* out_diff,
-                      uint32_t* out_spec, int step, cudaStream_t s);
+// instead of (or besides) the packed colour pair.
+void launch_dn_atrous(int w, int h, const GeoArgs& ga, const uint32_t* color, const uint32_t* var,
+                      uint32_t* out_color, uint32_t* out_var, uint32_t* out_diff, uint32_t* out_spec, int step,
+                      cudaStream_t s);
 void launch_split_color(int w, int h, const uint32_t* color, uint32_t* diff, uint32_t* spec, cudaStream_t s);
 
 // hashgrid.cu

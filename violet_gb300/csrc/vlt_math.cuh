@@ -426,11 +426,18 @@ VLT_HD uint32_t f32_to_ufloat(float f, uint32_t mb) {
 }
 
 VLT_HD float ufloat_to_f32(uint32_t c, uint32_t mb) {
+#if defined(__CUDA_ARCH__)
+  // Branch-free: place the code's exponent/mantissa in a binary32 bit pattern (a
+  // denormal when e == 0) and rescale by 2^112; the product is exact.
+  if (c >= (31u << mb)) return as_float(0x7F800000u | ((c & ((1u << mb) - 1u)) << (23u - mb)));
+  return as_float(c << (23u - mb)) * as_float(0x77800000u);
+#else
   uint32_t e = c >> mb;
   uint32_t m = c & ((1u << mb) - 1u);
   if (e == 0) return (float)m * as_float((uint32_t)(127 - 14 - (int)mb) << 23);
   if (e == 31) return as_float(0x7F800000u | (m << (23u - mb)));
   return as_float(((e + 112u) << 23) | (m << (23u - mb)));
+#endif
 }
 
 // B10G11R11_UFLOAT_PACK32: R bits 0-10, G bits 11-21, B bits 22-31.
