@@ -4,8 +4,10 @@
 Workload: one 1920x1080 view, seeded synthetic scene with 2% disocclusion pixels per
 frame, plain-method knobs (temporal M cap 20, two spatial passes of 8 taps at 16 px
 for diffuse and specular, 32-frame history, 5 a-trous iterations, 2^22-cell hash
-grid keyed by position and normal octant with one query per pixel), reference
-storage formats, binary32 arithmetic. A step is one frame of that view.
+grid keyed by position and normal octant with one query per pixel), FP32 storage
+form (VLT_FORM_F32: float reservoirs, AO, lighting and denoiser records), binary32
+arithmetic. A step is one frame of that view. The reference-storage-form
+(R11G11B10/half/M8W24 records) throughput of the same frames is reported beside it.
 
   value : Mpix/s with every frame's inputs already resident in HBM (CUDA events on
           the launching stream around exactly --steps frames; frames are distinct and
@@ -39,10 +41,12 @@ METRIC = "Mpix/s full ReSTIR GI+ReLAX frame, batched vs plain, rel-L2≤1e-3; p9
 W_DEFAULT, H_DEFAULT = 1920, 1080
 WORKLOAD = "restir_gi_relax_hashgrid_1920x1080_plain"
 
-# Algorithmic bytes per pixel (per cell for hg_decay/hg_compact) of each pass in the
-# reference storage form: inputs read once + outputs written once, counted from the
-# record layouts of include/vlt.h (unused G-buffer layers are not counted).
-PASS_BYTES_PER_PIXEL = {
+# Algorithmic bytes per pixel (per cell for hg_decay/hg_compact) of each pass:
+# inputs read once + outputs written once, counted from the record layouts of
+# include/vlt.h (unused G-buffer layers are not counted; the per-frame surface planes
+# are an implementation choice and count as the G-buffer/depth reads they replace).
+PASS_BYTES_PER_PIXEL_REF = {
+    "surface": 4 + 12 + 48,
     "hg_emit": 16 + 32,
     "hg_select": 32 + 4,
     "hg_update": 4 + 16 + 16 + 1,
@@ -55,8 +59,26 @@ PASS_BYTES_PER_PIXEL = {
     "dn_temporal": 4 + 8 + 4 + 4 + 2 + 4 + 4 + 8 + 4 + 1 + 8 + 4 + 1,
     "dn_fix": 1 + 8 + 4 + 8 + 4,
     "dn_fallback": 1 + 8 + 4 + 8 + 4,
+    "dn_fast_clamp": 8 + 8 + 8,
     "dn_atrous": 4 + 4 + 4 + 8 + 4 + 8 + 4,
 }
+# FP32 form: float2 AO history, float filtered AO, 48-byte diffuse records, float4
+# lighting, 32-byte denoiser records {diffuse.rgb|aux, specular.rgb|aux}, float
+# history length.
+PASS_BYTES_PER_PIXEL_F32 = dict(
+    PASS_BYTES_PER_PIXEL_REF,
+    ao_gen=8 + 4 + 8 + 8,
+    ao_filter=4 + 8 + 4,
+    diff_temporal=4 + 4 + 8 + 4 + 4 + 48 + 48,
+    diff_spatial=4 + 4 + 4 + 48 + 48 + 16,
+    dn_temporal=4 + 8 + 16 + 16 + 4 + 4 + 32 + 4 + 32 + 4,
+    dn_fix=4 + 32 + 32,
+    dn_fast_clamp=32 + 32 + 32,
+    dn_fallback=4 + 32 + 32,
+    dn_atrous=4 + 4 + 4 + 32 + 32,
+)
+PASS_BYTES_PER_PIXEL = {"ref": PASS_BYTES_PER_PIXEL_REF, "f32": PASS_BYTES_PER_PIXEL_F32}
+FORM = "f32"
 PASS_BYTES_PER_CELL = {"hg_decay": 2, "hg_compact": 4}
 # DRAM bytes per launch unit measured with ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum), see profiles/; None until captured.
@@ -174,7 +196,7 @@ def cpu_sample(width, height, frames, seed, threads=None):
         po.set_threads(threads)
     params = workload_params(vg)
     scene = vg.Scene(seed, width, height, disocclusion_frac=0.02)
-    ov = po.OracleView(width, height, params)
+    ov = po.OracleView(width, height, params, FORM)
     times = []
     for f in range(frames):
         host = scene.generate_host(f)
@@ -198,7 +220,7 @@ def run_reference(args, ws, rank):
 
     params = workload_params(vg)
     scene = vg.Scene(1000, sw, sh, disocclusion_frac=0.02)
-    ov = po.OracleView(sw, sh, params)
+    ov = po.OracleView(sw, sh, params, FORM)
     frames = [scene.generate_host(f) for f in range(args.warmup + args.steps)]
     fps = [scene.frame_params(f) for f in range(args.warmup + args.steps)]
     for f in range(args.warmup):
@@ -215,7 +237,7 @@ def run_reference(args, ws, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "width": W_DEFAULT, "height": H_DEFAULT, "storage": "reference formats",
+        "config": {"workload": WORKLOAD, "width": W_DEFAULT, "height": H_DEFAULT, "storage": "fp32",
                    "sample": "480x270 view per step"},
         "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": cores, "kind": "port",
                          "sample": "%d frames of a 480x270 view of the same scene and knobs after %d warm-up frames"
@@ -252,34 +274,47 @@ def run_ours(args, ws, rank, local):
         frames.append(bufs)
         fps.append(scene.frame_params(f))
     in_bytes = sum(v.numel() for v in frames[0].values())
-    out = {k: torch.empty(n * 4, dtype=torch.uint8, device=dev) for k in ("diffuse", "specular")}
+    out_px = 16 if FORM == "f32" else 4
+    out = {k: torch.empty(n * out_px, dtype=torch.uint8, device=dev) for k in ("diffuse", "specular")}
     ctx = vg.Context(local)
-    view = vg.View(ctx, W, H, "ref", params)
-    torch.cuda.synchronize()
-
-    # ---- device-resident throughput
-    for f in range(args.warmup):
-        view.run(fps[f], f, frames[f], out, sh)
-    torch.cuda.synchronize()
-    barrier(ws)
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    launches = 0
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for k in range(args.steps):
-        f = args.warmup + k
-        view.run(fps[f], f, frames[f], out, sh)
-        launches += view.launches
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+
+    def device_resident(form, o, clocks=None):
+        """Warm-up frames, then exactly --steps timed frames; returns (ms, launches)."""
+        v = vg.View(ctx, W, H, form, params)
+        for f in range(args.warmup):
+            v.run(fps[f], f, frames[f], o, sh)
+        torch.cuda.synchronize()
+        barrier(ws)
+        if clocks:
+            clocks.start()
+            time.sleep(0.3)
+        nl = 0
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for k in range(args.steps):
+            f = args.warmup + k
+            v.run(fps[f], f, frames[f], o, sh)
+            nl += v.launches
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1)
+        barrier(ws)
+        v.close()
+        return max_over_ranks(t, ws, dev), nl
+
+    # ---- device-resident throughput of the reference storage form (side figure)
+    out_ref = {k: torch.empty(n * 4, dtype=torch.uint8, device=dev) for k in ("diffuse", "specular")}
+    ms_ref, _ = device_resident("ref", out_ref)
+    value_ref = ws * args.steps * n / (ms_ref / 1e3) / 1e6
+    del out_ref
+
+    # ---- device-resident throughput (headline)
+    clocks = ClockSampler(local)
+    ms, launches = device_resident(FORM, out, clocks)
     clk = clocks.stop()
-    barrier(ws)
-    ms = max_over_ranks(ms, ws, dev)
     value = ws * args.steps * n / (ms / 1e3) / 1e6
+    view = vg.View(ctx, W, H, FORM, params)
 
     # ---- per-pass timers (separate run: the event records cost a little time)
     view.reset(sh)
@@ -301,7 +336,7 @@ def run_ours(args, ws, rank, local):
         per_unit = PASS_BYTES_PER_CELL[dom]
     else:
         units = n
-        per_unit = PASS_BYTES_PER_PIXEL[dom]
+        per_unit = PASS_BYTES_PER_PIXEL[FORM][dom]
     alg_bytes = per_unit * units
     peaks = measured_peaks()
     if peaks and peaks.get("hbm_gbs"):
@@ -313,7 +348,14 @@ def run_ours(args, ws, rank, local):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic * units if traffic else None, "kernel": dom,
                 "alg_bytes_per_launch": alg_bytes, "launch_ms": avg_s * 1e3, "peak_source": peak_src}
-    pass_table = {k: {"launches": v[0], "ms_per_frame": v[1] / prof_frames} for k, v in sorted(passes.items())}
+    pass_table = {}
+    for k, (nl, tot) in sorted(passes.items()):
+        if k in PASS_BYTES_PER_CELL:
+            b = PASS_BYTES_PER_CELL[k] * (16 << params.hg_log2_buckets)
+        else:
+            b = PASS_BYTES_PER_PIXEL[FORM].get(k, 0) * n
+        pass_table[k] = {"launches": nl, "ms_per_frame": tot / prof_frames,
+                         "alg_gbs": (b * nl / (tot / 1e3) / 1e9) if tot > 0 and b else None}
 
     # ---- end to end through the C ABI with host buffers
     host = []
@@ -321,7 +363,7 @@ def run_ours(args, ws, rank, local):
         host.append({k: torch.empty(v.numel(), dtype=torch.uint8, pin_memory=True).copy_(v) for k, v in
                      frames[f].items()})
     stage = {k: torch.empty_like(v) for k, v in frames[0].items()}
-    out_host = {k: torch.empty(n * 4, dtype=torch.uint8, pin_memory=True) for k in ("diffuse", "specular")}
+    out_host = {k: torch.empty(n * out_px, dtype=torch.uint8, pin_memory=True) for k in ("diffuse", "specular")}
     view.reset(sh)
 
     def e2e_step(f):
@@ -361,12 +403,13 @@ def run_ours(args, ws, rank, local):
             "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "width": W, "height": H, "storage": "reference formats",
+            "config": {"workload": WORKLOAD, "width": W, "height": H, "storage": FORM,
                        "parallelism": "replicas" if ws > 1 else "single view",
                        "l2": "inputs+state per frame > L2 (distinct frames, no flush)",
                        "knobs": {k: getattr(params, k) for k, _ in params._fields_}},
             "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": in_bytes,
-                    "d2h_bytes_per_step": 8 * n},
+                    "d2h_bytes_per_step": 2 * out_px * n},
+            "ref_storage_form": {"value": value_ref, "unit": "Mpix/s", "ms_per_step": ms_ref / args.steps},
             "gpu_launches": launches,
             "roofline": roofline,
             "passes": pass_table,

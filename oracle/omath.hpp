@@ -160,6 +160,7 @@ inline float2 operator*(float2 a, float2 b) { return {a.x * b.x, a.y * b.y}; }
 inline float2 operator/(float2 a, float2 b) { return {a.x / b.x, a.y / b.y}; }
 inline float2 operator*(float2 a, float s) { return {a.x * s, a.y * s}; }
 inline float2 operator*(float s, float2 a) { return {s * a.x, s * a.y}; }
+inline float2 operator/(float2 a, float s) { return {a.x / s, a.y / s}; }
 inline float2& operator+=(float2& a, float2 b) { a = a + b; return a; }
 
 inline float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }

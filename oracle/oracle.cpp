@@ -25,6 +25,7 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -106,17 +107,48 @@ inline int nthreads() { return g_threads > 0 ? g_threads : omp_get_max_threads()
 #define ROWS_PARALLEL _Pragma("omp parallel for schedule(dynamic, 4) num_threads(nthreads())")
 
 // ================================================================ AO gen
-// raytraced_ao_gen.hlsl:18-81; history stored as half2 {x, a} (y, z stay 0).
+// Storage forms. Reference form (F32 = false): AO history half2 {x, a}, filtered AO
+// half. F32 form: history float2, filtered AO float; nothing quantized.
+template <bool F32>
+inline float2 ao_hist(const void* p, size_t j) {
+  if constexpr (F32) {
+    const float* f = (const float*)p;
+    return F2(f[2 * j], f[2 * j + 1]);
+  } else {
+    return load_half2(((const uint32_t*)p)[j]);
+  }
+}
+template <bool F32>
+inline void ao_hist_store(void* p, size_t j, float2 v) {
+  if constexpr (F32) {
+    ((float*)p)[2 * j] = v.x;
+    ((float*)p)[2 * j + 1] = v.y;
+  } else {
+    ((uint32_t*)p)[j] = store_half2(v);
+  }
+}
+template <bool F32>
+inline float ao_filtered_load(const void* p, size_t j) {
+  if constexpr (F32) return ((const float*)p)[j];
+  else return f16tof32(((const uint16_t*)p)[j]);
+}
+template <bool F32>
+inline void ao_filtered_store(void* p, size_t j, float v) {
+  if constexpr (F32) ((float*)p)[j] = v;
+  else ((uint16_t*)p)[j] = (uint16_t)f32tof16(v);
+}
+
+// raytraced_ao_gen.hlsl:18-81; history {x, a} (the y, z channels stay 0).
+template <bool F32>
 void ao_gen(const vlt_frame_params& fp, int w, int h, const uint32_t* hpn, const float* depth_buf,
-            const uint32_t* prev_ao, uint32_t* out, uint32_t has_new_sample, uint32_t has_prev_frame,
-            float radius_ws) {
+            const void* prev_ao, void* out, uint32_t has_new_sample, uint32_t has_prev_frame, float radius_ws) {
   ROWS_PARALLEL
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t i = (size_t)y * w + x;
       float depth = depth_buf[i];
       if (has_no_geometry_via_depth(depth)) {
-        out[i] = 0u;
+        ao_hist_store<F32>(out, i, F2(0.0f, 0.0f));
         continue;
       }
       float2 motion_vector;
@@ -133,10 +165,9 @@ void ao_gen(const vlt_frame_params& fp, int w, int h, const uint32_t* hpn, const
       float hx, ha;
       bool is_in_last_view = history_uv.x == saturate(history_uv.x) && history_uv.y == saturate(history_uv.y);
       if (is_in_last_view && has_prev_frame) {
-        Bilinear b = bilinear(history_uv, w, h);
-        Tex<uint32_t> t = {prev_ao, w, h};
-        float2 a = load_half2(t(b.x0, b.y0)), bb = load_half2(t(b.x1, b.y0));
-        float2 c = load_half2(t(b.x0, b.y1)), d = load_half2(t(b.x1, b.y1));
+        Bilinear b = bilinear(history_uv, w, h);  // taps clamped to the image
+        float2 a = ao_hist<F32>(prev_ao, (size_t)b.y0 * w + b.x0), bb = ao_hist<F32>(prev_ao, (size_t)b.y0 * w + b.x1);
+        float2 c = ao_hist<F32>(prev_ao, (size_t)b.y1 * w + b.x0), d = ao_hist<F32>(prev_ao, (size_t)b.y1 * w + b.x1);
         hx = blerp(a.x, bb.x, c.x, d.x, b.fx, b.fy);
         ha = blerp(a.y, bb.y, c.y, d.y, b.fx, b.fy);
       } else {
@@ -154,23 +185,24 @@ void ao_gen(const vlt_frame_params& fp, int w, int h, const uint32_t* hpn, const
       } else {
         hx = ha > 0.0f ? hx : 1.0f;
       }
-      out[i] = store_half2(F2(hx, ha));
+      ao_hist_store<F32>(out, i, F2(hx, ha));
     }
 }
 
 // ============================================================= AO filter
 // raytraced_ao_filter.hlsl:12-70 (x channel; taps at uint(min(p + d, size))).
-void ao_filter(int w, int h, const float* depth_buf, const uint32_t* ao, uint16_t* out) {
+template <bool F32>
+void ao_filter(int w, int h, const float* depth_buf, const void* ao, void* out) {
   ROWS_PARALLEL
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t i = (size_t)y * w + x;
       float depth = depth_buf[i];
       if (has_no_geometry_via_depth(depth)) {
-        out[i] = 0;
+        ao_filtered_store<F32>(out, i, 0.0f);
         continue;
       }
-      float center_ao = f16tof32(ao[i]);
+      float center_ao = ao_hist<F32>(ao, i).x;
       float col_med[3], col_min[3], col_max[3];
       for (int dy = -1; dy <= 1; dy++) {
         float row[3];
@@ -183,8 +215,7 @@ void ao_filter(int w, int h, const float* depth_buf, const uint32_t* ao, uint16_
             row[dx + 1] = center_ao;
             continue;
           }
-          Tex<uint32_t> at = {ao, w, h};
-          row[dx + 1] = f16tof32(at((int)cx, (int)cy) & 0xFFFFu);
+          row[dx + 1] = in_img((int)cx, (int)cy, w, h) ? ao_hist<F32>(ao, (size_t)cy * w + cx).x : 0.0f;
         }
         col_med[dy + 1] = hclamp(row[0], row[1], row[2]);
         col_min[dy + 1] = hmin(hmin(row[0], row[1]), row[2]);
@@ -195,7 +226,7 @@ void ao_filter(int w, int h, const float* depth_buf, const uint32_t* ao, uint16_
       float Cc = hclamp(col_med[0], col_med[1], col_med[2]);
       float med = hclamp(Cc, A, B);
       float mn = hmin(hmin(col_min[0], col_min[1]), col_min[2]);
-      out[i] = (uint16_t)f32tof16(lerp(med, mn, 0.5f));
+      ao_filtered_store<F32>(out, i, lerp(med, mn, 0.5f));
     }
 }
 
@@ -281,6 +312,105 @@ void diff_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
     }
 }
 
+// F32 storage form of the diffuse reservoir: 12 floats per pixel,
+// {hit position, W}, {hit normal, asfloat(M)}, {radiance, 0}; the sample is kept
+// decoded (an empty HitPosNormal's normal decodes to (0, 0, -1)).
+struct DiffF32 {
+  uint32_t M;
+  float W;
+  float3 pos, nrm, rad;
+};
+inline DiffF32 diff_f32_load(const float* r, size_t j) {
+  const float* q = r + 12 * j;
+  DiffF32 o;
+  o.pos = F3(q[0], q[1], q[2]);
+  o.W = q[3];
+  o.nrm = F3(q[4], q[5], q[6]);
+  o.M = asuint(q[7]);
+  o.rad = F3(q[8], q[9], q[10]);
+  return o;
+}
+inline void diff_f32_store(float* r, size_t j, uint32_t M, float W, float3 pos, float3 nrm, float3 rad) {
+  float* q = r + 12 * j;
+  q[0] = pos.x, q[1] = pos.y, q[2] = pos.z, q[3] = W;
+  q[4] = nrm.x, q[5] = nrm.y, q[6] = nrm.z, q[7] = asfloat(M);
+  q[8] = rad.x, q[9] = rad.y, q[10] = rad.z, q[11] = 0.0f;
+}
+
+// ind_diff_temporal_resample.hlsl:49-200 in the F32 storage form.
+void diff_temporal_f32(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const float* prev_depth,
+                       const float* depth_buf, const uint32_t* new_hpn, const uint32_t* new_rad,
+                       const float* new_pdf, const float* prev_rsv, float* out, uint32_t frame_rand,
+                       uint32_t has_prev_frame, uint32_t has_new_sample) {
+  const float3 empty_n = HitPosNormal::decode(0u, 0u).normal;
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      const float depth = depth_buf[i];
+      float3 position_ws = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+      float4 hpos_reproj = mul(fp.prev_view_proj, F4(position_ws.x, position_ws.y, position_ws.z, 1.0f));
+      float3 ndc_reproj = F3(hpos_reproj.x / hpos_reproj.w - fp.jitter[2], hpos_reproj.y / hpos_reproj.w - fp.jitter[3],
+                             hpos_reproj.z / hpos_reproj.w - 0.0f);
+      float2 uv_reproj = F2(ndc_reproj.x * 0.5f + 0.5f, ndc_reproj.y * 0.5f + 0.5f);
+      bool in_view = fabsf(ndc_reproj.x) < 1.0f && fabsf(ndc_reproj.y) < 1.0f;
+      bool sample_prev_frame = has_prev_frame && in_view;
+      if (sample_prev_frame) {
+        float reproj_depth = ndc_reproj.z;
+        Bilinear b = bilinear(uv_reproj, w, h);
+        float pd = blerp(prev_depth[(size_t)b.y0 * w + b.x0], prev_depth[(size_t)b.y0 * w + b.x1],
+                         prev_depth[(size_t)b.y1 * w + b.x0], prev_depth[(size_t)b.y1 * w + b.x1], b.fx, b.fy);
+        if (fabsf(pd - reproj_depth) > 0.001f) sample_prev_frame = false;
+      }
+      uint32_t M = 0;
+      float W = 0.0f;
+      float3 hp = F3(0.0f), hn = empty_n, rad = F3(0.0f);
+      if (sample_prev_frame) {
+        int px = (int)to_uint(uv_reproj.x * (float)w), py = (int)to_uint(uv_reproj.y * (float)h);
+        if (in_img(px, py, w, h)) {
+          DiffF32 r = diff_f32_load(prev_rsv, (size_t)py * w + px);
+          M = r.M;
+          W = r.W;
+          hp = r.pos;
+          hn = r.nrm;
+          rad = r.rad;
+        }
+        if (M == 0) {
+          rad = F3(0.0f);
+          hp = F3(0.0f);
+          hn = empty_n;
+        }
+        M = std::min(M, P.diff_m_cap);
+      }
+      if (has_new_sample) {
+        float reservoir_target_pdf = luminance(rad);
+        float prev_w = W * reservoir_target_pdf * (float)M;
+        float3 new_hit_radiance = load_r11g11b10(new_rad[i]);
+        float new_target_pdf = luminance(new_hit_radiance);
+        float new_w;
+        if (P.use_input_pdf) {
+          float pdf = new_pdf[i];
+          new_w = pdf > 0.0f ? new_target_pdf / pdf : 0.0f;
+        } else {
+          new_w = new_target_pdf * TWO_PI;
+        }
+        uint32_t rng_state = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
+        float w_sum = prev_w + new_w;
+        float chance = new_w / w_sum;
+        if (lcg_rand(rng_state) < chance) {
+          HitPosNormal hit = HitPosNormal::decode(new_hpn[2 * i], new_hpn[2 * i + 1]);
+          hp = hit.pos;
+          hn = hit.normal;
+          rad = new_hit_radiance;
+          reservoir_target_pdf = new_target_pdf;
+        }
+        M += 1;
+        W = reservoir_target_pdf > 0.0f ? w_sum / (reservoir_target_pdf * (float)M) : 0.0f;
+      }
+      diff_f32_store(out, i, M, W, hp, hn, rad);
+    }
+}
+
 // ====================================================== diffuse spatial
 // ind_diff_spatial_resample.hlsl:62-91 (WorkingReservoir::load) and :94-337.
 struct WorkingReservoir {
@@ -289,23 +419,36 @@ struct WorkingReservoir {
   float3 hit_radiance, hit_pos, hit_normal;
   float target_pdf;
 };
-WorkingReservoir wr_load(const uint32_t* rsv, size_t j, float3 pix_position_ws, float3 pix_normal) {
-  const U4 r = ((const U4*)rsv)[j];
+template <bool F32>
+WorkingReservoir wr_load(const void* rsv, size_t j, float3 pix_position_ws, float3 pix_normal) {
   WorkingReservoir o;
-  reservoir_simple_decode_32b(r.x, &o.M, &o.W);
-  HitPosNormal hit = HitPosNormal::decode(r.y, r.z);
-  o.hit_pos = hit.pos;
-  o.hit_normal = hit.normal;
-  o.hit_radiance = load_r11g11b10(r.w);
-  float3 hit_offset = hit.pos - pix_position_ws;
+  if constexpr (F32) {
+    DiffF32 r = diff_f32_load((const float*)rsv, j);
+    o.M = r.M;
+    o.W = r.W;
+    o.hit_pos = r.pos;
+    o.hit_normal = r.nrm;
+    o.hit_radiance = r.rad;
+  } else {
+    const U4 r = ((const U4*)rsv)[j];
+    reservoir_simple_decode_32b(r.x, &o.M, &o.W);
+    HitPosNormal hit = HitPosNormal::decode(r.y, r.z);
+    o.hit_pos = hit.pos;
+    o.hit_normal = hit.normal;
+    o.hit_radiance = load_r11g11b10(r.w);
+  }
+  float3 hit_offset = o.hit_pos - pix_position_ws;
   float nol = saturate(dot(pix_normal, normalize(hit_offset)));
   o.target_pdf = nol * luminance(o.hit_radiance);
   return o;
 }
 
+// Lighting output: R11G11B10 (reference form) or float4 {rgb, 0} (F32 form).
+template <bool F32>
 void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const uint32_t* gbuf,
-                  const float* depth_buf, const uint16_t* ao_tex, const uint32_t* in, uint32_t* out,
-                  uint32_t* lighting, uint32_t frame_rand) {
+                  const float* depth_buf, const void* ao_tex, const void* in, void* out, void* lighting,
+                  uint32_t frame_rand) {
+  const float3 empty_n = HitPosNormal::decode(0u, 0u).normal;
   const uint32_t MAX_ITERATION = P.diff_spatial_taps;
   const float MIN_RADIUS = 1.5f;
   // Golden spiral constants (:148-150): B = log(1.61803398)/(0.5 PI), A = 1/exp(B 2PI).
@@ -318,14 +461,19 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
       size_t i = (size_t)y * w + x;
       float depth = depth_buf[i];
       if (has_no_geometry_via_depth(depth)) {
-        ((U4*)out)[i] = U4{0, 0, 0, 0};
-        if (lighting) lighting[i] = 0;
+        if constexpr (F32) {
+          diff_f32_store((float*)out, i, 0u, 0.0f, F3(0.0f), empty_n, F3(0.0f));
+          if (lighting) memset((float*)lighting + 4 * i, 0, 16);
+        } else {
+          ((U4*)out)[i] = U4{0, 0, 0, 0};
+          if (lighting) ((uint32_t*)lighting)[i] = 0;
+        }
         continue;
       }
       const float3 position_ws = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
       float3 gnormal = load_gbuffer_normal(gbuf, x, y, w, h);
-      float ao = f16tof32(ao_tex[i]);
-      WorkingReservoir reservoir = wr_load(in, i, position_ws, gnormal);
+      float ao = ao_filtered_load<F32>(ao_tex, i);
+      WorkingReservoir reservoir = wr_load<F32>(in, i, position_ws, gnormal);
       float w_sum = reservoir.W * reservoir.target_pdf * (float)reservoir.M;
       float radius = P.diff_spatial_radius_px > 0.0f ? P.diff_spatial_radius_px
                                                      : (float)std::min(w, h) * 0.05f;
@@ -352,7 +500,7 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
           radius = hmax(radius * 0.5f, MIN_RADIUS);
           continue;
         }
-        WorkingReservoir neighbor = wr_load(in, (size_t)ny * w + nx, position_ws, gnormal);
+        WorkingReservoir neighbor = wr_load<F32>(in, (size_t)ny * w + nx, position_ws, gnormal);
         float3 offset_qq = position_ws_n - neighbor.hit_pos;
         float3 offset_rq = position_ws - neighbor.hit_pos;
         float L2_qq = dot(offset_qq, offset_qq);
@@ -380,19 +528,30 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
         float target_pdf = reservoir.target_pdf;
         if (target_pdf > 0.0f) reservoir.W = w_sum / (target_pdf * (float)reservoir.M);
       }
-      U4* o = (U4*)out + i;
-      o->x = reservoir_simple_encode_32b(reservoir.M, reservoir.W);
-      HitPosNormal hpn = {reservoir.hit_pos, reservoir.hit_normal};
-      uint32_t e[2];
-      hpn.encode(e);
-      o->y = e[0];
-      o->z = e[1];
-      o->w = store_r11g11b10(reservoir.hit_radiance);
+      if constexpr (F32) {
+        diff_f32_store((float*)out, i, reservoir.M, reservoir.W, reservoir.hit_pos, reservoir.hit_normal,
+                       reservoir.hit_radiance);
+      } else {
+        U4* o = (U4*)out + i;
+        o->x = reservoir_simple_encode_32b(reservoir.M, reservoir.W);
+        HitPosNormal hpn = {reservoir.hit_pos, reservoir.hit_normal};
+        uint32_t e[2];
+        hpn.encode(e);
+        o->y = e[0];
+        o->z = e[1];
+        o->w = store_r11g11b10(reservoir.hit_radiance);
+      }
       if (lighting) {
         float3 selected_dir = normalize(reservoir.hit_pos - position_ws);
         float NoL = saturate(dot(gnormal, selected_dir));
         float brdf = ONE_OVER_PI;
-        lighting[i] = store_r11g11b10(reservoir.hit_radiance * (brdf * NoL * reservoir.W));
+        float3 l = reservoir.hit_radiance * (brdf * NoL * reservoir.W);
+        if constexpr (F32) {
+          float* q = (float*)lighting + 4 * i;
+          q[0] = l.x, q[1] = l.y, q[2] = l.z, q[3] = 0.0f;
+        } else {
+          ((uint32_t*)lighting)[i] = store_r11g11b10(l);
+        }
       }
     }
 }
@@ -556,10 +715,24 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
 
 // ===================================================== specular spatial
 // ind_spec_spatial_resample.hlsl:169-448 (+ optional merged-reservoir output).
+// Lighting output: R11G11B10 plus a half ray length (reference form), or float4
+// {rgb, ray length} (F32 form, ray_len_out unused).
+template <bool F32>
 void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const uint32_t* gbuf,
                   const float* depth_buf, const uint32_t* rsv, const float* hp_tex, const uint32_t* rad_tex,
-                  uint32_t* lighting, uint16_t* ray_len_out, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
+                  void* lighting, uint16_t* ray_len_out, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
                   uint32_t frame_rand) {
+  auto store_light = [&](size_t i, float3 v, float ray_len) {
+    if constexpr (F32) {
+      if (lighting) {
+        float* q = (float*)lighting + 4 * i;
+        q[0] = v.x, q[1] = v.y, q[2] = v.z, q[3] = ray_len;
+      }
+    } else {
+      if (lighting) ((uint32_t*)lighting)[i] = store_r11g11b10(v);
+      if (ray_len_out) ray_len_out[i] = (uint16_t)f32tof16(ray_len);
+    }
+  };
   const uint32_t MAX_ITERATION = P.spec_spatial_taps;
   const float COS_TOL = 0.906307816505432128906f;
   ROWS_PARALLEL
@@ -568,8 +741,7 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
       size_t i = (size_t)y * w + x;
       float depth = depth_buf[i];
       if (has_no_geometry_via_depth(depth)) {
-        if (lighting) lighting[i] = 0;
-        if (ray_len_out) ray_len_out[i] = 0;
+        store_light(i, F3(0.0f), 0.0f);
         if (out_rsv) {
           out_rsv[2 * i] = 0;
           out_rsv[2 * i + 1] = 0;
@@ -685,9 +857,10 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
         float3 lt = hit_radiance * ((F * G2_over_G1) * (vndf * W));
         float3 specular_reflectance = hmax(ggx_brdf_integral_approx(NoV, roughness, specular_f0), 1.0f / 65536.0f);
         lt = lt / specular_reflectance;
-        lighting[i] = store_r11g11b10(lt);
+        store_light(i, lt, ray_len);
+      } else if (!F32 && ray_len_out) {
+        ray_len_out[i] = (uint16_t)f32tof16(ray_len);
       }
-      if (ray_len_out) ray_len_out[i] = (uint16_t)f32tof16(ray_len);
     }
 }
 
@@ -1115,6 +1288,420 @@ void dn_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, const
     }
 }
 
+// ============================================= denoiser, F32 storage form
+// The same five passes with nothing quantized: one 8-float record per pixel,
+// {diffuse.rgb, aux.x, specular.rgb, aux.y}, aux = second moments (temporal and fix
+// outputs, history) or variance (fallback, a-trous); history length float.
+//
+// Numeric contract of this form: binary32 with explicit fused multiply-adds. Each
+// fma_() is one IEEE fusedMultiplyAdd (std::fmaf), every other operation is rounded
+// separately (-ffp-contract=off), and exp is exp_fma (the exp2 construction above
+// evaluated by FMA Horner steps). The product's f32-form kernels evaluate the same
+// expressions in the same order, so the results are reproduced bit for bit.
+inline float fma_(float a, float b, float c) { return std::fmaf(a, b, c); }
+inline float exp2_fma(float x) {
+  const float c[7] = {1.0f, 0.6931471824645996f, 0.24022646248340607f, 0.05550329014658928f,
+                      0.009618519805371761f, 0.0013399859890341759f, 0.00015337577497120947f};
+  if (isnan_(x)) return asfloat(0x7FFFFFFFu);
+  if (x >= 128.0f) return asfloat(0x7F800000u);
+  if (x < -151.0f) return 0.0f;
+  float n = rintf(x);
+  float f = x - n;
+  float p = c[6];
+  for (int k = 5; k >= 0; --k) p = fma_(p, f, c[k]);
+  int e = to_int(n);
+  if (e > 127) return (p * 2.0f) * asfloat(0x7F000000u);
+  if (e < -126) return (p * asfloat(0x00800000u)) * asfloat((uint32_t)(e + 126 + 127) << 23);
+  return p * asfloat((uint32_t)(e + 127) << 23);
+}
+inline float exp_fma(float x) { return exp2_fma(x * 1.44269502162933349609375f); }
+// luminance (util.hlsl:21-24) as r*0.2126, then two FMAs.
+inline float lum_fma(float3 c) { return fma_(c.z, 0.0722f, fma_(c.y, 0.7152f, c.x * 0.2126f)); }
+inline float3 fma3(float w, float3 v, float3 acc) {
+  return F3(fma_(w, v.x, acc.x), fma_(w, v.y, acc.y), fma_(w, v.z, acc.z));
+}
+
+// EdgeStoppingFunc (svgf.inc.hlsl:6-84) in this form's contract.
+struct EdgeStop32 {
+  float depth_center, fz_sigma;  // sigma_z * fwidth_z
+  float3 normal_center;
+  float2 lumi_center, lumi_rcp;  // rcp(sigma_l * lumi_std + epsilon)
+  bool use_lumi;
+  int n_log2;  // sigma_n = 2^n_log2
+  static EdgeStop32 create(float depth, float fwidth_z, float sigma_z, float3 normal, int n_log2) {
+    EdgeStop32 e;
+    e.depth_center = depth;
+    e.fz_sigma = sigma_z * fwidth_z;
+    e.normal_center = normal;
+    e.lumi_center = F2(0.0f, 0.0f);
+    e.lumi_rcp = F2(0.0f, 0.0f);
+    e.use_lumi = false;
+    e.n_log2 = n_log2;
+    return e;
+  }
+  float2 weight(float tap_dist, float depth, float3 normal, float2 lumi) const {
+    float dist_z = fabsf(depth - depth_center);
+    float wz = -dist_z / fma_(fz_sigma, tap_dist, 1e-8f);
+    float n_dot = saturate(fma_(normal_center.z, normal.z, fma_(normal_center.y, normal.y,
+                                                                  normal_center.x * normal.x)));
+    float wn = n_dot;
+    for (int k = 0; k < n_log2; ++k) wn = wn * wn;
+    float ax = wz, ay = wz;
+    if (use_lumi) {
+      ax = fma_(-fabsf(lumi.x - lumi_center.x), lumi_rcp.x, wz);
+      ay = fma_(-fabsf(lumi.y - lumi_center.y), lumi_rcp.y, wz);
+    }
+    return F2(wn * exp_fma(ax), wn * exp_fma(ay));
+  }
+};
+
+struct Rec32 {
+  float3 d, s;
+  float2 aux;
+};
+inline Rec32 rec_load(const float* r, size_t j) {
+  const float* q = r + 8 * j;
+  return Rec32{F3(q[0], q[1], q[2]), F3(q[4], q[5], q[6]), F2(q[3], q[7])};
+}
+inline void rec_store(float* r, size_t j, float3 d, float3 s, float2 aux) {
+  float* q = r + 8 * j;
+  q[0] = d.x, q[1] = d.y, q[2] = d.z, q[3] = aux.x;
+  q[4] = s.x, q[5] = s.y, q[6] = s.z, q[7] = aux.y;
+}
+inline float quad_max_history_f(const float* len, int x, int y, int w, int h) {
+  int x0 = x & ~1, y0 = y & ~1;
+  float m = 0.0f;
+  for (int k = 0; k < 4; ++k) {
+    int px = x0 + (k & 1), py = y0 + (k >> 1);
+    m = hmax(m, in_img(px, py, w, h) ? len[(size_t)py * w + px] : 0.0f);
+  }
+  return m;
+}
+
+// svgf_temporal_filter.hlsl:96-362. Inputs: diffuse lighting float4 {rgb, 0},
+// specular lighting float4 {rgb, ray length}.
+void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const float* depth_tex,
+                   const uint32_t* gbuf, const float* diff_src, const float* spec_src, const float* prev_depth,
+                   const uint32_t* prev_gbuf, const float* hist, const float* len_hist, const float* fast_hist,
+                   float* out, float* out_len, float* out_fast, uint32_t has_history, uint32_t fast_history) {
+  const float BLEND_FACTOR_DIFF = 1.0f / P.history_max_frames;
+  const float BLEND_FACTOR_FAST = 1.0f / 3.0f;
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float depth = depth_tex[i];
+      if (has_no_geometry_via_depth(depth)) {
+        out_len[i] = 0.0f;
+        rec_store(out, i, F3(0.0f), F3(0.0f), F2(0.0f, 0.0f));
+        if (fast_history) rec_store(out_fast, i, F3(0.0f), F3(0.0f), F2(0.0f, 0.0f));
+        continue;
+      }
+      const float2 screen_uv = F2(((float)x + 0.5f) / (float)w, ((float)y + 0.5f) / (float)h);
+      GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
+      float3 m1 = F3(0.0f), m2 = F3(0.0f);
+      for (int dx = -1; dx <= 1; dx++)
+        for (int dy = -1; dy <= 1; dy++) {
+          int px = std::min(std::max(x + dx, 0), w - 1), py = std::min(std::max(y + dy, 0), h - 1);
+          const float* q = spec_src + 4 * ((size_t)py * w + px);
+          float3 sv = F3(q[0], q[1], q[2]);
+          m1 += sv;
+          m2 += sv * sv;
+        }
+      m1 = m1 * (1.0f / 9.0f);
+      m2 = m2 * (1.0f / 9.0f);
+      const float3 position = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
+      float3 vsh = F3(0.0f), vsfh = F3(0.0f);
+      {
+        float3 view_ray_dir = normalize(position - v3(fp.view_pos));
+        float3 vp = position + view_ray_dir * spec_src[4 * i + 3];
+        float4 hr = mul(fp.prev_view_proj, F4(vp.x, vp.y, vp.z, 1.0f));
+        float2 ndc_reproj = F2(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3]);
+        float2 vuv = F2((ndc_reproj.x + fp.jitter[0]) * 0.5f + 0.5f, (ndc_reproj.y + fp.jitter[1]) * 0.5f + 0.5f);
+        bool valid = vuv.x == saturate(vuv.x) && vuv.y == saturate(vuv.y) && has_history;
+        if (valid) {
+          Bilinear b = bilinear(vuv, w, h);
+          size_t a = (size_t)b.y0 * w + b.x0, bb = (size_t)b.y0 * w + b.x1, c = (size_t)b.y1 * w + b.x0,
+                 d = (size_t)b.y1 * w + b.x1;
+          vsh = blerp(rec_load(hist, a).s, rec_load(hist, bb).s, rec_load(hist, c).s, rec_load(hist, d).s, b.fx,
+                      b.fy);
+          if (fast_history)
+            vsfh = blerp(rec_load(fast_hist, a).s, rec_load(fast_hist, bb).s, rec_load(fast_hist, c).s,
+                         rec_load(fast_hist, d).s, b.fx, b.fy);
+        }
+      }
+      float2 motion_vector;
+      float reproj_depth;
+      {
+        float4 hpos = mul(fp.view_proj, F4(position.x, position.y, position.z, 1.0f));
+        float2 ndc = F2(hpos.x / hpos.w - fp.jitter[0], hpos.y / hpos.w - fp.jitter[1]);
+        float4 hr = mul(fp.prev_view_proj, F4(position.x, position.y, position.z, 1.0f));
+        float2 ndc_reproj = F2(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3]);
+        motion_vector = (ndc - ndc_reproj) * 0.5f;
+        reproj_depth = hr.z / hr.w;
+      }
+      float2 history_uv = screen_uv - motion_vector;
+      float3 dh = F3(0.0f), sh = F3(0.0f), dfh = F3(0.0f), sfh = F3(0.0f);
+      float2 smh = F2(0.0f, 0.0f);
+      float hl = 0.0f;
+      bool valid = history_uv.x == saturate(history_uv.x) && history_uv.y == saturate(history_uv.y) && has_history;
+      if (valid) {
+        float2 pcc = F2(history_uv.x * (float)w - 0.5f, history_uv.y * (float)h - 0.5f);
+        float2 frac = F2(pcc.x - floorf(pcc.x), pcc.y - floorf(pcc.y));
+        int bx = to_int(pcc.x), by = to_int(pcc.y);
+        float depth_tol = gbuffer.fwidth_z * 4.0f + 1e-4f;
+        float normal_tol = gbuffer.fwidth_n * 16.0f + 1e-2f;
+        float normal_tol_sq = normal_tol * normal_tol;
+        float b = frac.y, r = frac.x, t = 1.0f - b, l = 1.0f - r;
+        const float weights[2][2] = {{t * l, t * r}, {b * l, b * r}};
+        float3 ds = F3(0.0f), ss = F3(0.0f), dfs = F3(0.0f), sfs = F3(0.0f);
+        float2 ms = F2(0.0f, 0.0f);
+        float hs = 0.0f, wsum = 0.0f;
+        for (int ox = 0; ox < 2; ++ox)
+          for (int oy = 0; oy < 2; ++oy) {
+            int px = bx + ox, py = by + oy;
+            if (!in_img(px, py, w, h)) continue;
+            size_t j = (size_t)py * w + px;
+            float3 n_diff = load_gbuffer_normal(prev_gbuf, px, py, w, h) - gbuffer.normal;
+            if (!(fabsf(prev_depth[j] - reproj_depth) < depth_tol && dot(n_diff, n_diff) < normal_tol_sq)) continue;
+            float wt = weights[oy][ox];
+            wsum += wt;
+            hs += wt * len_hist[j];
+            Rec32 rr = rec_load(hist, j);
+            ds = fma3(wt, rr.d, ds);
+            ss = fma3(wt, rr.s, ss);
+            ms = F2(fma_(wt, rr.aux.x, ms.x), fma_(wt, rr.aux.y, ms.y));
+            if (fast_history) {
+              Rec32 f = rec_load(fast_hist, j);
+              dfs = fma3(wt, f.d, dfs);
+              sfs = fma3(wt, f.s, sfs);
+            }
+          }
+        valid = wsum > 0.00390625f;
+        if (valid) {
+          float inv = 1.0f / wsum;
+          dh = ds * inv;
+          sh = ss * inv;
+          smh = ms * inv;
+          hl = hs * inv;
+          dfh = dfs * inv;
+          sfh = sfs * inv;
+        }
+      }
+      if (!valid) {
+        dh = sh = dfh = sfh = F3(0.0f);
+        smh = F2(0.0f, 0.0f);
+        hl = 0.0f;
+      }
+      hl += HISTORY_LEN_UNIT;
+      float3 dsrc = F3(diff_src[4 * i], diff_src[4 * i + 1], diff_src[4 * i + 2]);
+      float3 ssrc = F3(spec_src[4 * i], spec_src[4 * i + 1], spec_src[4 * i + 2]);
+      float2 lsrc = F2(lum_fma(dsrc), lum_fma(ssrc));
+      float2 smsrc = lsrc * lsrc;
+      float blurness = sqrtf(saturate(gbuffer.perceptual_roughness * 6.0f));
+      const float BLEND_FACTOR_SPEC = lerp(7.0f / 8.0f, BLEND_FACTOR_DIFF, blurness);
+      const float BLEND_FACTOR_SPEC_FAST = lerp(1.0f, BLEND_FACTOR_FAST, blurness);
+      float ratio = HISTORY_LEN_UNIT / hl;
+      float2 alpha = F2(hmax(BLEND_FACTOR_DIFF, ratio), hmax(BLEND_FACTOR_SPEC, ratio));
+      float3 df = lerp(dh, dsrc, alpha.x);
+      float2 smf = F2(lerp(smh.x, smsrc.x, alpha.x), lerp(smh.y, smsrc.y, alpha.y));
+      float2 alpha_fast = F2(hmax(BLEND_FACTOR_FAST, ratio), hmax(BLEND_FACTOR_SPEC_FAST, ratio));
+      float3 dff = lerp(dfh, dsrc, alpha_fast.x);
+      float3 sff = lerp(sfh, ssrc, alpha_fast.y);
+      float3 sf;
+      {
+        float3 dev = hmax(sqrt3(abs3(m2 - m1 * m1)), 1e-19f);
+        auto dsr_weight = [&](float3 c) { return exp2_own(-10.0f * luminance(abs3(c - m1) / dev)); };
+        float wv = dsr_weight(vsh), wh = dsr_weight(sh);
+        float3 dual = (wv * vsh + wh * sh) / hmax(wv + wh, 1e-37f);
+        sf = lerp(dual, ssrc, alpha.y);
+        if (fast_history) {
+          float wv2 = dsr_weight(vsfh), wh2 = dsr_weight(sfh);
+          float3 d2 = (wv2 * vsfh + wh2 * sfh) / hmax(wv2 + wh2, 1e-37f);
+          sff = lerp(d2, ssrc, alpha_fast.y);
+        }
+      }
+      rec_store(out, i, df, sf, smf);
+      out_len[i] = hl;
+      if (fast_history) rec_store(out_fast, i, dff, sff, F2(0.0f, 0.0f));
+    }
+}
+
+// relax_disocclusion_fix.hlsl:27-122.
+void dn32_fix(int w, int h, const float* depth_tex, const uint32_t* gbuf, const float* len, const float* in,
+              float* out) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float hl = len[i];
+      float qmax = quad_max_history_f(len, x, y, w, h);
+      if (hl == 0.0f) {
+        rec_store(out, i, F3(0.0f), F3(0.0f), F2(0.0f, 0.0f));
+        continue;
+      }
+      hl = qmax;
+      if (hl < 4.0f * HISTORY_LEN_UNIT) {
+        const GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
+        EdgeStop32 es = EdgeStop32::create(depth_tex[i], gbuffer.fwidth_z, 5.0f, gbuffer.normal, 5);
+        float2 ws = F2(0.0f, 0.0f), ms = F2(0.0f, 0.0f);
+        float3 dsum = F3(0.0f), ssum = F3(0.0f);
+        const int stride = to_int((14.0f * HISTORY_LEN_UNIT) / hl);
+        for (int oy = -2; oy <= 2; oy++)
+          for (int ox = -2; ox <= 2; ox++) {
+            int cx = ox * stride, cy = oy * stride;
+            int ux = x + cx, uy = y + cy;
+            if (!in_img(ux, uy, w, h)) continue;
+            size_t j = (size_t)uy * w + ux;
+            float2 wt = es.weight(length(F2((float)cx, (float)cy)), depth_tex[j],
+                                  load_gbuffer_normal(gbuf, ux, uy, w, h), F2(0.0f, 0.0f));
+            Rec32 r = rec_load(in, j);
+            ws += wt;
+            dsum = fma3(wt.x, r.d, dsum);
+            ssum = fma3(wt.y, r.s, ssum);
+            ms = F2(fma_(wt.x, r.aux.x, ms.x), fma_(wt.y, r.aux.y, ms.y));
+          }
+        rec_store(out, i, dsum * (1.0f / ws.x), ssum * (1.0f / ws.y), F2(ms.x / ws.x, ms.y / ws.y));
+      } else {
+        memcpy(out + 8 * i, in + 8 * i, 32);
+      }
+    }
+}
+
+// relax_fast_history_clamp.hlsl:11-75 (in place on `rec`).
+void dn32_fast_clamp(int w, int h, const float* fast, float* rec) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float3 dm1 = F3(0.0f), dm2 = F3(0.0f), sm1 = F3(0.0f), sm2 = F3(0.0f);
+      for (int oy = -1; oy <= 1; oy++)
+        for (int ox = -1; ox <= 1; ox++) {
+          int cx = std::min(std::max(x + ox, 0), w - 1), cy = std::min(std::max(y + oy, 0), h - 1);
+          Rec32 f = rec_load(fast, (size_t)cy * w + cx);
+          float3 d = rgb_to_yCoCg(f.d), s = rgb_to_yCoCg(f.s);
+          dm1 += d;
+          dm2 += d * d;
+          sm1 += s;
+          sm2 += s * s;
+        }
+      dm1 = dm1 / 9.0f;
+      dm2 = dm2 / 9.0f;
+      sm1 = sm1 / 9.0f;
+      sm2 = sm2 / 9.0f;
+      float3 ddev = sqrt3(dm2 - dm1 * dm1) * 0.75f;
+      float3 sdev = sqrt3(sm2 - sm1 * sm1) * 0.75f;
+      Rec32 c = rec_load(rec, i);
+      float3 d = hclamp(rgb_to_yCoCg(c.d), dm1 - ddev, dm1 + ddev);
+      float3 s = hclamp(rgb_to_yCoCg(c.s), sm1 - sdev, sm1 + sdev);
+      rec_store(rec, i, yCoCg_to_rgb(d), yCoCg_to_rgb(s), c.aux);
+    }
+}
+
+// svgf_spatial_fallback_filter.hlsl:25-125.
+void dn32_fallback(int w, int h, const float* depth_tex, const uint32_t* gbuf, const float* len, const float* in,
+                   float* out) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      float hl = len[i];
+      float qmax = quad_max_history_f(len, x, y, w, h);
+      if (hl == 0.0f) {
+        rec_store(out, i, F3(0.0f), F3(0.0f), F2(0.0f, 0.0f));
+        continue;
+      }
+      hl = qmax;
+      float3 dd, sd;
+      float2 md;
+      if (hl < 4.0f * HISTORY_LEN_UNIT) {
+        GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
+        EdgeStop32 es = EdgeStop32::create(depth_tex[i], gbuffer.fwidth_z * 3.0f, 1.0f, gbuffer.normal, 7);
+        float ws = 0.0f;
+        float2 ms = F2(0.0f, 0.0f);
+        float3 dsum = F3(0.0f), ssum = F3(0.0f);
+        for (int oy = -3; oy <= 3; oy++)
+          for (int ox = -3; ox <= 3; ox++) {
+            int ux = x + ox, uy = y + oy;
+            if (!in_img(ux, uy, w, h)) continue;
+            size_t j = (size_t)uy * w + ux;
+            float wt = es.weight(length(F2((float)ox, (float)oy)), depth_tex[j],
+                                 load_gbuffer_normal(gbuf, ux, uy, w, h), F2(0.0f, 0.0f)).x;
+            Rec32 r = rec_load(in, j);
+            ws += wt;
+            dsum = fma3(wt, r.d, dsum);
+            ssum = fma3(wt, r.s, ssum);
+            ms = F2(fma_(wt, r.aux.x, ms.x), fma_(wt, r.aux.y, ms.y));
+          }
+        float inv = 1.0f / ws;
+        dd = dsum * inv;
+        sd = ssum * inv;
+        md = ms * inv;
+      } else {
+        Rec32 r = rec_load(in, i);
+        dd = r.d;
+        sd = r.s;
+        md = r.aux;
+      }
+      float2 fst = F2(lum_fma(dd), lum_fma(sd));
+      float2 var = F2(hmax(fma_(-fst.x, fst.x, md.x), 0.0f), hmax(fma_(-fst.y, fst.y, md.y), 0.0f));
+      float boost = hmax(1.0f, (4.0f * HISTORY_LEN_UNIT) / hl);
+      rec_store(out, i, dd, sd, var * boost);
+    }
+}
+
+// svgf_atrous_filter.hlsl:23-88 (off-axis taps only, as the reference's loop
+// condition selects). out_diff / out_spec: float4 {rgb, 0}.
+void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, const float* in, float* out,
+                 float* out_diff, float* out_spec, int step) {
+  const float kernel_weights[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
+      Rec32 c = rec_load(in, i);
+      EdgeStop32 es = EdgeStop32::create(depth_tex[i], gbuffer.fwidth_z, 1.0f, gbuffer.normal, 7);
+      es.use_lumi = true;
+      es.lumi_center = F2(lum_fma(c.d), lum_fma(c.s));
+      es.lumi_rcp = F2(1.0f / fma_(4.0f, sqrtf(c.aux.x), 1e-8f), 1.0f / fma_(4.0f, sqrtf(c.aux.y), 1e-8f));
+      float3 dsum = c.d, ssum = c.s;
+      float2 vsum = c.aux, wsum = F2(1.0f, 1.0f);
+      for (int oy = -2; oy <= 2; oy++) {
+        if (oy == 0) continue;
+        const float kwy = kernel_weights[std::abs(oy)];
+        for (int ox = -2; ox <= 2; ox++) {
+          if (ox == 0) continue;
+          int cx = ox * step, cy = oy * step;
+          int ux = x + cx, uy = y + cy;
+          if (!in_img(ux, uy, w, h)) continue;
+          const float kw = kwy * kernel_weights[std::abs(ox)];
+          size_t j = (size_t)uy * w + ux;
+          Rec32 r = rec_load(in, j);
+          float2 e = es.weight(length(F2((float)cx, (float)cy)), depth_tex[j],
+                               load_gbuffer_normal(gbuf, ux, uy, w, h), F2(lum_fma(r.d), lum_fma(r.s)));
+          float2 wt = F2(kw * e.x, kw * e.y);
+          dsum = fma3(wt.x, r.d, dsum);
+          ssum = fma3(wt.y, r.s, ssum);
+          vsum = F2(fma_(wt.x * wt.x, r.aux.x, vsum.x), fma_(wt.y * wt.y, r.aux.y, vsum.y));
+          wsum += wt;
+        }
+      }
+      float2 inv = F2(1.0f / wsum.x, 1.0f / wsum.y);
+      float3 dd = dsum * inv.x, sd = ssum * inv.y;
+      float2 vd = F2(vsum.x * inv.x * inv.x, vsum.y * inv.y * inv.y);
+      if (out) rec_store(out, i, dd, sd, vd);
+      if (out_diff) {
+        float* q = out_diff + 4 * i;
+        q[0] = dd.x, q[1] = dd.y, q[2] = dd.z, q[3] = 0.0f;
+      }
+      if (out_spec) {
+        float* q = out_spec + 4 * i;
+        q[0] = sd.x, q[1] = sd.y, q[2] = sd.z, q[3] = 0.0f;
+      }
+    }
+}
+
 // ======================================================= hash grid
 // hash_grid.inc.hlsl:32-105.
 struct VKey {
@@ -1344,6 +1931,10 @@ struct OView {
   std::vector<uint32_t> diff_light, spec_light, variance, sel, cidx, caddr;
   std::vector<uint16_t> ray_len, ao_filtered;
   uint32_t ccount = 0;
+  // F32 storage form: these replace the reference-form buffers of the same role.
+  bool f32 = false;
+  std::vector<float> diff_prev32, ao_prev32, ao_filtered32, diff_light32, spec_light32, hist_rec, hist_len32,
+      fast_prev32, fallback_rec;
 };
 
 struct FrameRand {
@@ -1380,22 +1971,40 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
             in.diff_hit_radiance, v.hg_queries.data(), &v.hg_qcount);
   (void)frame_rand.next();  // diffuse sample generation
 
-  std::vector<uint32_t> ao_cur(n);
-  ao_gen(fp, w, h, in.diff_hit_pos_normal, in.depth, v.ao_prev.data(), ao_cur.data(), 1u, has_prev ? 1u : 0u,
-         P.ao_radius);
-  ao_filter(w, h, in.depth, ao_cur.data(), v.ao_filtered.data());
-  v.ao_prev.swap(ao_cur);
-
-  std::vector<uint32_t> temp(4 * n), sp(4 * n);
-  diff_temporal(fp, w, h, P, prev_depth, in.depth, in.diff_hit_pos_normal, in.diff_hit_radiance,
-                in.diff_source_pdf, v.diff_prev.data(), temp.data(), frame_rand.next(), has_prev ? 1u : 0u, 1u);
-  for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
-    bool last = k + 1 == P.diff_spatial_passes;
-    diff_spatial(fp, w, h, P, in.gbuffer, in.depth, v.ao_filtered.data(), temp.data(), sp.data(),
-                 last ? v.diff_light.data() : nullptr, frame_rand.next());
-    temp.swap(sp);
+  if (v.f32) {
+    std::vector<float> ao_cur(2 * n);
+    ao_gen<true>(fp, w, h, in.diff_hit_pos_normal, in.depth, v.ao_prev32.data(), ao_cur.data(), 1u,
+                 has_prev ? 1u : 0u, P.ao_radius);
+    ao_filter<true>(w, h, in.depth, ao_cur.data(), v.ao_filtered32.data());
+    v.ao_prev32.swap(ao_cur);
+    std::vector<float> temp(12 * n), sp(12 * n);
+    diff_temporal_f32(fp, w, h, P, prev_depth, in.depth, in.diff_hit_pos_normal, in.diff_hit_radiance,
+                      in.diff_source_pdf, v.diff_prev32.data(), temp.data(), frame_rand.next(), has_prev ? 1u : 0u,
+                      1u);
+    for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
+      bool last = k + 1 == P.diff_spatial_passes;
+      diff_spatial<true>(fp, w, h, P, in.gbuffer, in.depth, v.ao_filtered32.data(), temp.data(), sp.data(),
+                         last ? v.diff_light32.data() : nullptr, frame_rand.next());
+      temp.swap(sp);
+    }
+    v.diff_prev32.swap(temp);
+  } else {
+    std::vector<uint32_t> ao_cur(n);
+    ao_gen<false>(fp, w, h, in.diff_hit_pos_normal, in.depth, v.ao_prev.data(), ao_cur.data(), 1u,
+                  has_prev ? 1u : 0u, P.ao_radius);
+    ao_filter<false>(w, h, in.depth, ao_cur.data(), v.ao_filtered.data());
+    v.ao_prev.swap(ao_cur);
+    std::vector<uint32_t> temp(4 * n), sp(4 * n);
+    diff_temporal(fp, w, h, P, prev_depth, in.depth, in.diff_hit_pos_normal, in.diff_hit_radiance,
+                  in.diff_source_pdf, v.diff_prev.data(), temp.data(), frame_rand.next(), has_prev ? 1u : 0u, 1u);
+    for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
+      bool last = k + 1 == P.diff_spatial_passes;
+      diff_spatial<false>(fp, w, h, P, in.gbuffer, in.depth, v.ao_filtered.data(), temp.data(), sp.data(),
+                          last ? v.diff_light.data() : nullptr, frame_rand.next());
+      temp.swap(sp);
+    }
+    v.diff_prev.swap(temp);
   }
-  v.diff_prev.swap(temp);
 
   (void)frame_rand.next();  // specular sample generation
   std::vector<uint32_t> srsv(2 * n), srad(n), srsv2(2 * n), srad2(n);
@@ -1415,9 +2024,15 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
       uint32_t* o_rsv = use_b ? b_rsv.data() : c_rsv.data();
       float* o_hp = use_b ? b_hp.data() : c_hp.data();
       uint32_t* o_rad = use_b ? b_rad.data() : c_rad.data();
-      spec_spatial(fp, w, h, P, in.gbuffer, in.depth, a_rsv, a_hp, a_rad, last ? v.spec_light.data() : nullptr,
-                   last ? v.ray_len.data() : nullptr, last ? nullptr : o_rsv, last ? nullptr : o_hp,
-                   last ? nullptr : o_rad, frame_rand.next());
+      uint32_t seed = frame_rand.next();
+      if (v.f32)
+        spec_spatial<true>(fp, w, h, P, in.gbuffer, in.depth, a_rsv, a_hp, a_rad,
+                           last ? (void*)v.spec_light32.data() : nullptr, nullptr, last ? nullptr : o_rsv,
+                           last ? nullptr : o_hp, last ? nullptr : o_rad, seed);
+      else
+        spec_spatial<false>(fp, w, h, P, in.gbuffer, in.depth, a_rsv, a_hp, a_rad,
+                            last ? (void*)v.spec_light.data() : nullptr, last ? v.ray_len.data() : nullptr,
+                            last ? nullptr : o_rsv, last ? nullptr : o_hp, last ? nullptr : o_rad, seed);
       a_rsv = o_rsv;
       a_hp = o_hp;
       a_rad = o_rad;
@@ -1428,7 +2043,48 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
   v.spec_hp_prev.swap(shp);
   v.spec_rad_prev.swap(srad);
 
-  if (P.denoise && has_prev) {
+  const size_t light_bytes = (v.f32 ? 16 : 4) * n;
+  const void* diff_light = v.f32 ? (const void*)v.diff_light32.data() : (const void*)v.diff_light.data();
+  const void* spec_light = v.f32 ? (const void*)v.spec_light32.data() : (const void*)v.spec_light.data();
+  if (P.denoise && has_prev && v.f32) {
+    std::vector<float> trec(8 * n), tlen(n), tfast(P.fast_history_clamp ? 8 * n : 8);
+    dn32_temporal(fp, w, h, P, in.depth, in.gbuffer, v.diff_light32.data(), v.spec_light32.data(), prev_depth,
+                  prev_gbuf, v.hist_rec.data(), v.hist_len32.data(), v.fast_prev32.data(), trec.data(), tlen.data(),
+                  tfast.data(), v.denoiser_history ? 1u : 0u, P.fast_history_clamp);
+    if (P.disocclusion_fix) {
+      std::vector<float> frec(8 * n);
+      dn32_fix(w, h, in.depth, in.gbuffer, tlen.data(), trec.data(), frec.data());
+      trec.swap(frec);
+    }
+    if (P.fast_history_clamp) {
+      dn32_fast_clamp(w, h, tfast.data(), trec.data());
+      v.fast_prev32.swap(tfast);
+    }
+    v.hist_rec.swap(trec);
+    v.hist_len32.swap(tlen);
+    v.denoiser_history = true;
+    dn32_fallback(w, h, in.depth, in.gbuffer, v.hist_len32.data(), v.hist_rec.data(), v.fallback_rec.data());
+    std::vector<float> a(v.fallback_rec), b(8 * n);
+    uint32_t iters = std::min(P.atrous_iterations, 5u);
+    for (uint32_t k = 0; k < iters; ++k) {
+      bool last = k + 1 == iters;
+      dn32_atrous(w, h, in.depth, in.gbuffer, a.data(), b.data(), last && out ? (float*)out->diffuse : nullptr,
+                  last && out ? (float*)out->specular : nullptr, 1 << k);
+      a.swap(b);
+    }
+    if (iters == 0 && out) {
+      for (size_t i = 0; i < n; ++i) {
+        if (out->diffuse) {
+          float* q = (float*)out->diffuse + 4 * i;
+          q[0] = a[8 * i], q[1] = a[8 * i + 1], q[2] = a[8 * i + 2], q[3] = a[8 * i + 3];
+        }
+        if (out->specular) {
+          float* q = (float*)out->specular + 4 * i;
+          q[0] = a[8 * i + 4], q[1] = a[8 * i + 5], q[2] = a[8 * i + 6], q[3] = a[8 * i + 7];
+        }
+      }
+    }
+  } else if (P.denoise && has_prev) {
     std::vector<uint32_t> tcolor(2 * n), tmom(n), tfast(P.fast_history_clamp ? 2 * n : 2);
     std::vector<uint8_t> tlen(n);
     dn_temporal(fp, w, h, P, in.depth, in.gbuffer, v.diff_light.data(), v.spec_light.data(), v.ray_len.data(),
@@ -1470,11 +2126,11 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
     }
   } else {
     v.denoiser_history = false;
-    if (out && out->diffuse) memcpy(out->diffuse, v.diff_light.data(), 4 * n);
-    if (out && out->specular) memcpy(out->specular, v.spec_light.data(), 4 * n);
+    if (out && out->diffuse) memcpy(out->diffuse, diff_light, light_bytes);
+    if (out && out->specular) memcpy(out->specular, spec_light, light_bytes);
   }
-  if (out && out->raw_diffuse) memcpy(out->raw_diffuse, v.diff_light.data(), 4 * n);
-  if (out && out->raw_specular) memcpy(out->raw_specular, v.spec_light.data(), 4 * n);
+  if (out && out->raw_diffuse) memcpy(out->raw_diffuse, diff_light, light_bytes);
+  if (out && out->raw_specular) memcpy(out->raw_specular, spec_light, light_bytes);
   memcpy(v.prev_depth.data(), in.depth, 4 * n);
   memcpy(v.prev_gbuf.data(), in.gbuffer, 16 * n);
   v.frames += 1;
@@ -1488,8 +2144,9 @@ extern "C" {
 void vlto_set_threads(int n) { g_threads = n; }
 int vlto_get_threads(void) { return nthreads(); }
 
-void* vlto_view_create(uint32_t w, uint32_t h, const vlt_params* p) {
+void* vlto_view_create_form(uint32_t w, uint32_t h, const vlt_params* p, int form) {
   OView* v = new OView;
+  v->f32 = form == 1;
   v->w = (int)w;
   v->h = (int)h;
   v->P = *p;
@@ -1513,6 +2170,17 @@ void* vlto_view_create(uint32_t w, uint32_t h, const vlt_params* p) {
   v->spec_light.assign(n, 0);
   v->ray_len.assign(n, 0);
   v->variance.assign(n, 0);
+  if (v->f32) {
+    v->diff_prev32.assign(12 * n, 0.0f);
+    v->ao_prev32.assign(2 * n, 0.0f);
+    v->ao_filtered32.assign(n, 0.0f);
+    v->diff_light32.assign(4 * n, 0.0f);
+    v->spec_light32.assign(4 * n, 0.0f);
+    v->hist_rec.assign(8 * n, 0.0f);
+    v->hist_len32.assign(n, 0.0f);
+    v->fast_prev32.assign(p->fast_history_clamp ? 8 * n : 8, 0.0f);
+    v->fallback_rec.assign(8 * n, 0.0f);
+  }
   if (p->hg_enable) {
     size_t nc = (size_t)16 << v->log2_buckets;
     v->hg_storage.assign(4 * nc, 0);
@@ -1525,6 +2193,8 @@ void* vlto_view_create(uint32_t w, uint32_t h, const vlt_params* p) {
   }
   return v;
 }
+
+void* vlto_view_create(uint32_t w, uint32_t h, const vlt_params* p) { return vlto_view_create_form(w, h, p, 0); }
 
 void vlto_view_destroy(void* h) { delete (OView*)h; }
 
@@ -1539,7 +2209,29 @@ void* vlto_view_buffer(void* h, const char* name, size_t* bytes) {
     const char* nm;
     void* p;
     size_t sz;
-  } tab[] = {
+  };
+  if (v.f32) {
+    E t32[] = {
+        {"diff_reservoir", v.diff_prev32.data(), 48 * n},
+        {"ao_history", v.ao_prev32.data(), 8 * n},
+        {"ao_filtered", v.ao_filtered32.data(), 4 * n},
+        {"hist_record", v.hist_rec.data(), 32 * n},
+        {"fallback_record", v.fallback_rec.data(), 32 * n},
+        {"hist_len", v.hist_len32.data(), 4 * n},
+        {"raw_diffuse", v.diff_light32.data(), 16 * n},
+        {"raw_specular", v.spec_light32.data(), 16 * n},
+    };
+    for (const E& e : t32)
+      if (strcmp(e.nm, name) == 0) {
+        if (bytes) *bytes = e.sz;
+        return e.p;
+      }
+    static const char* ref_only[] = {"diff_reservoir", "ao_history", "ao_filtered", "hist_color", "hist_moments",
+                                     "hist_len", "variance", "spec_ray_len", "raw_diffuse", "raw_specular"};
+    for (const char* r : ref_only)
+      if (strcmp(r, name) == 0) return nullptr;
+  }
+  E tab[] = {
       {"diff_reservoir", v.diff_prev.data(), 16 * n},
       {"spec_hit_pos", v.spec_hp_prev.data(), 16 * n},
       {"spec_reservoir", v.spec_rsv_prev.data(), 8 * n},
@@ -1572,10 +2264,10 @@ void* vlto_view_buffer(void* h, const char* name, size_t* bytes) {
 // Per-pass entry points (host pointers; same argument meaning as include/vlt.h).
 void vlto_ao_gen(const vlt_frame_params* fp, uint32_t w, uint32_t h, const uint32_t* hpn, const float* depth,
                  const uint32_t* prev_ao, uint32_t* ao, uint32_t has_new, uint32_t has_prev, float radius) {
-  ao_gen(*fp, (int)w, (int)h, hpn, depth, prev_ao, ao, has_new, has_prev, radius);
+  ao_gen<false>(*fp, (int)w, (int)h, hpn, depth, prev_ao, ao, has_new, has_prev, radius);
 }
 void vlto_ao_filter(uint32_t w, uint32_t h, const float* depth, const uint32_t* ao, uint16_t* out) {
-  ao_filter((int)w, (int)h, depth, ao, out);
+  ao_filter<false>((int)w, (int)h, depth, ao, out);
 }
 void vlto_ind_diff_temporal_resample(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p,
                                      const float* prev_depth, const float* depth, const uint32_t* new_hpn,
@@ -1587,7 +2279,7 @@ void vlto_ind_diff_temporal_resample(const vlt_frame_params* fp, uint32_t w, uin
 void vlto_ind_diff_spatial_resample(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p,
                                     const uint32_t* gbuf, const float* depth, const uint16_t* ao, const uint32_t* in,
                                     uint32_t* out, uint32_t* lighting, uint32_t frame_rand) {
-  diff_spatial(*fp, (int)w, (int)h, *p, gbuf, depth, ao, in, out, lighting, frame_rand);
+  diff_spatial<false>(*fp, (int)w, (int)h, *p, gbuf, depth, ao, in, out, lighting, frame_rand);
 }
 void vlto_ind_spec_temporal_resample(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p,
                                      const float* prev_depth, const uint32_t* prev_gbuf, const float* depth,
@@ -1602,7 +2294,7 @@ void vlto_ind_spec_spatial_resample(const vlt_frame_params* fp, uint32_t w, uint
                                     const uint32_t* gbuf, const float* depth, const uint32_t* rsv, const float* hp,
                                     const uint32_t* rad, uint32_t* lighting, uint16_t* ray_len, uint32_t* out_rsv,
                                     float* out_hp, uint32_t* out_rad, uint32_t frame_rand) {
-  spec_spatial(*fp, (int)w, (int)h, *p, gbuf, depth, rsv, hp, rad, lighting, ray_len, out_rsv, out_hp, out_rad,
+  spec_spatial<false>(*fp, (int)w, (int)h, *p, gbuf, depth, rsv, hp, rad, lighting, ray_len, out_rsv, out_hp, out_rad,
                frame_rand);
 }
 void vlto_denoise_temporal(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p, const float* depth,

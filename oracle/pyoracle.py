@@ -24,6 +24,7 @@ SIGS = {
     "vlto_set_threads": (None, [C.c_int]),
     "vlto_get_threads": (C.c_int, []),
     "vlto_view_create": (P, [U32, U32, PP]),
+    "vlto_view_create_form": (P, [U32, U32, PP, C.c_int]),
     "vlto_view_destroy": (None, [P]),
     "vlto_frame_run": (None, [P, C.POINTER(_ffi.FrameInputs), C.POINTER(_ffi.FrameOutputs)]),
     "vlto_view_buffer": (P, [P, C.c_char_p, C.POINTER(C.c_size_t)]),
@@ -103,10 +104,11 @@ def codec(fn, x):
 class OracleView:
     """CPU restatement of one view (the same buffer names as violet_gb300.View)."""
 
-    def __init__(self, width, height, params):
+    def __init__(self, width, height, params, form="ref"):
         self.width, self.height = int(width), int(height)
         self.params = params
-        self.handle = lib().vlto_view_create(self.width, self.height, C.byref(params))
+        self.form = form
+        self.handle = lib().vlto_view_create_form(self.width, self.height, C.byref(params), _ffi.FORMS[form])
 
     def run(self, frame_params, frame_index, inputs, outputs=None):
         fi = _ffi.FrameInputs()

@@ -66,3 +66,28 @@ def first_mismatch(a, b, width=None, rec=1):
     where = (px % width, px // width) if width else px
     return "%d mismatching words; first at word %d (pixel %s): got 0x%08x expected 0x%08x" % (
         idx.size, i, where, int(a[i]), int(b[i]))
+
+
+def rel_l2(got, exp):
+    """||got - exp|| / ||exp|| over the finite entries, and whether the NaN/inf
+    patterns agree (both must be non-finite at the same places)."""
+    got = np.asarray(got, np.float64).reshape(-1)
+    exp = np.asarray(exp, np.float64).reshape(-1)
+    fg, fe = np.isfinite(got), np.isfinite(exp)
+    same_pattern = bool(np.array_equal(fg, fe))
+    m = fg & fe
+    den = float(np.sqrt(np.sum(exp[m] ** 2)))
+    num = float(np.sqrt(np.sum((got[m] - exp[m]) ** 2)))
+    return (num / den if den > 0 else num), same_pattern
+
+
+def first_float_mismatch(a, b, width=None, rec=1):
+    """first_mismatch over float32 words, treating any two NaNs as equal."""
+    a = np.asarray(a).reshape(-1).view(np.uint32)
+    b = np.asarray(b).reshape(-1).view(np.uint32)
+    na = (a & 0x7FFFFFFF) > 0x7F800000
+    nb = (b & 0x7FFFFFFF) > 0x7F800000
+    bad = (a != b) & ~(na & nb)
+    if not bad.any():
+        return None
+    return first_mismatch(np.where(bad, a, 0), np.where(bad, b, 0), width, rec)

@@ -51,22 +51,28 @@ struct Alloc {
 };
 
 // Resident state of one view (reference storage form).
+// Form-dependent element sizes are listed as "reference form / f32 form".
 struct ViewBuffers {
-  uint32_t* diff_rsv[3];   // uint4 records
-  uint32_t* ao[2];         // half2 {ao, valid}
-  uint16_t* ao_filtered;   // half
-  uint32_t* diff_light;    // R11G11B10
+  void* diff_rsv[3];       // 16 B uint4 records / 48 B DiffF32
+  void* ao[2];             // half2 {ao, valid} / float2
+  void* ao_filtered;       // half / float
+  void* diff_light;        // R11G11B10 / float4
   float* spec_hp[3];       // float4
   uint32_t* spec_rsv[3];   // uint2
   uint32_t* spec_rad[3];   // R11G11B10
-  uint32_t* spec_light;    // R11G11B10
-  uint16_t* ray_len;       // half
+  void* spec_light;        // R11G11B10 / float4 {rgb, ray length}
+  uint16_t* ray_len;       // half (reference form only)
+  // reference-form denoiser
   uint32_t* color[3];      // uint2 {diff, spec}: history, fix output, temporal output
   uint32_t* mom[3];        // half2
-  uint8_t* len[2];
   uint32_t* var[3];        // half2: fallback output, a-trous ping-pong
   uint32_t* color_c;       // fallback output
   uint32_t* fast[2];       // uint2 fast history
+  void* len[2];            // R8_UNORM / float history length
+  // f32-form denoiser: 32-byte records {diff.rgb|aux.x, spec.rgb|aux.y}: history,
+  // fix output, temporal output / a-trous ping-pong, a-trous ping-pong, fallback output
+  float4* rec[5];
+  float4* rec_fast[2];
   uint32_t* hg_storage;
   uint8_t* hg_decay;
   uint32_t* hg_queries[2];
@@ -144,27 +150,33 @@ size_t layout(vlt_view* v, char* base) {
     return r;
   };
   ViewBuffers& b = v->b;
-  for (int k = 0; k < 3; ++k) b.diff_rsv[k] = (uint32_t*)take(16 * n);
-  for (int k = 0; k < 2; ++k) b.ao[k] = (uint32_t*)take(4 * n);
-  b.ao_filtered = (uint16_t*)take(2 * n);
-  b.diff_light = (uint32_t*)take(4 * n);
+  memset(&b, 0, sizeof(b));
+  const bool f32 = v->form == VLT_FORM_F32;
+  const bool fast = v->p.fast_history_clamp != 0;
+  for (int k = 0; k < 3; ++k) b.diff_rsv[k] = take((f32 ? 48 : 16) * n);
+  for (int k = 0; k < 2; ++k) b.ao[k] = take((f32 ? 8 : 4) * n);
+  b.ao_filtered = take((f32 ? 4 : 2) * n);
+  b.diff_light = take((f32 ? 16 : 4) * n);
   for (int k = 0; k < 3; ++k) {
     b.spec_hp[k] = (float*)take(16 * n);
     b.spec_rsv[k] = (uint32_t*)take(8 * n);
     b.spec_rad[k] = (uint32_t*)take(4 * n);
   }
-  b.spec_light = (uint32_t*)take(4 * n);
-  b.ray_len = (uint16_t*)take(2 * n);
-  for (int k = 0; k < 3; ++k) {
-    b.color[k] = (uint32_t*)take(8 * n);
-    b.mom[k] = (uint32_t*)take(4 * n);
+  b.spec_light = take((f32 ? 16 : 4) * n);
+  for (int k = 0; k < 2; ++k) b.len[k] = take((f32 ? 4 : 1) * n);
+  if (f32) {
+    for (int k = 0; k < 5; ++k) b.rec[k] = (float4*)take(32 * n);
+    for (int k = 0; k < 2; ++k) b.rec_fast[k] = (float4*)take(fast ? 32 * n : 32);
+  } else {
+    b.ray_len = (uint16_t*)take(2 * n);
+    for (int k = 0; k < 3; ++k) {
+      b.color[k] = (uint32_t*)take(8 * n);
+      b.mom[k] = (uint32_t*)take(4 * n);
+    }
+    for (int k = 0; k < 2; ++k) b.fast[k] = (uint32_t*)take(fast ? 8 * n : 8);
+    for (int k = 0; k < 3; ++k) b.var[k] = (uint32_t*)take(4 * n);
+    b.color_c = (uint32_t*)take(8 * n);
   }
-  for (int k = 0; k < 2; ++k) {
-    b.len[k] = (uint8_t*)take(n);
-    b.fast[k] = (uint32_t*)take(v->p.fast_history_clamp ? 8 * n : 8);
-  }
-  for (int k = 0; k < 3; ++k) b.var[k] = (uint32_t*)take(4 * n);
-  b.color_c = (uint32_t*)take(8 * n);
   if (v->p.hg_enable) {
     const HashGridDims& d = v->hg;
     b.hg_storage = (uint32_t*)take((size_t)d.num_cells() * 16);
@@ -340,8 +352,8 @@ vlt_status vlt_view_create(vlt_ctx* ctx, uint32_t width, uint32_t height, vlt_fo
                            vlt_view** out) {
   if (!ctx || !out || !params_ok(params) || width == 0 || height == 0 || width > 16384 || height > 16384)
     return VLT_ERR_INVALID_ARG;
-  if (form != VLT_FORM_REF) {
-    set_last_error("only the reference storage form is built");
+  if (form != VLT_FORM_REF && form != VLT_FORM_F32) {
+    set_last_error("storage form not built: use VLT_FORM_REF or VLT_FORM_F32");
     return VLT_ERR_INVALID_ARG;
   }
   *out = nullptr;
@@ -443,20 +455,23 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
     size_t sz;
   };
   size_t nc = v->p.hg_enable ? v->hg.num_cells() : 0;
+  const bool f32 = v->form == VLT_FORM_F32;
   E tab[] = {
-      {"diff_reservoir", b.diff_rsv[v->diff_prev], 16 * n},
+      {"diff_reservoir", b.diff_rsv[v->diff_prev], (f32 ? 48 : 16) * n},
       {"spec_hit_pos", b.spec_hp[v->spec_prev], 16 * n},
       {"spec_reservoir", b.spec_rsv[v->spec_prev], 8 * n},
       {"spec_radiance", b.spec_rad[v->spec_prev], 4 * n},
-      {"ao_history", b.ao[v->ao_prev], 4 * n},
-      {"ao_filtered", b.ao_filtered, 2 * n},
-      {"hist_color", b.color[0], 8 * n},
-      {"hist_moments", b.mom[0], 4 * n},
-      {"hist_len", b.len[0], n},
-      {"variance", b.var[0], 4 * n},
-      {"spec_ray_len", b.ray_len, 2 * n},
-      {"raw_diffuse", b.diff_light, 4 * n},
-      {"raw_specular", b.spec_light, 4 * n},
+      {"ao_history", b.ao[v->ao_prev], (f32 ? 8 : 4) * n},
+      {"ao_filtered", b.ao_filtered, (f32 ? 4 : 2) * n},
+      {"hist_color", f32 ? nullptr : b.color[0], 8 * n},
+      {"hist_moments", f32 ? nullptr : b.mom[0], 4 * n},
+      {"hist_record", f32 ? b.rec[0] : nullptr, 32 * n},
+      {"fallback_record", f32 ? b.rec[4] : nullptr, 32 * n},
+      {"hist_len", b.len[0], (f32 ? 4 : 1) * n},
+      {"variance", f32 ? nullptr : b.var[0], 4 * n},
+      {"spec_ray_len", f32 ? nullptr : b.ray_len, 2 * n},
+      {"raw_diffuse", b.diff_light, (f32 ? 16 : 4) * n},
+      {"raw_specular", b.spec_light, (f32 ? 16 : 4) * n},
       {"hg_storage", b.hg_storage, nc * 16},
       {"hg_decay", b.hg_decay, nc},
       {"hg_queries", b.hg_queries[v->hg_qcur], v->p.hg_enable ? (size_t)v->hg.max_queries * 32 : 0},
@@ -466,6 +481,7 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
   };
   for (const E& e : tab) {
     if (strcmp(e.nm, name) == 0) {
+      if (!e.p) return nullptr;
       if (bytes) *bytes = e.sz;
       return e.p;
     }
@@ -550,10 +566,13 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
   (void)fr.next();  // Ind. Diff. Sample Gen.
 
   // AO.
+  const int form = (int)v->form;
+  const bool f32 = form == FORM_F32;
+  const size_t light_bytes = (f32 ? 16 : 4) * n;
   int ao_cur = v->ao_prev ^ 1;
-  STAGE("ao_gen", launch_ao_gen(fp, w, h, ga, in->diff_hit_pos_normal, b.ao[v->ao_prev], b.ao[ao_cur], 1u,
+  STAGE("ao_gen", launch_ao_gen(form, fp, w, h, ga, in->diff_hit_pos_normal, b.ao[v->ao_prev], b.ao[ao_cur], 1u,
                                 has_prev ? 1u : 0u, P.ao_radius, s));
-  STAGE("ao_filter", launch_ao_filter(w, h, in->depth, b.ao[ao_cur], b.ao_filtered, s));
+  STAGE("ao_filter", launch_ao_filter(form, w, h, in->depth, b.ao[ao_cur], b.ao_filtered, s));
   launches += 2;
   v->ao_prev = ao_cur;
 
@@ -561,7 +580,7 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
   DiffKnobs dk = diff_knobs(P);
   int p = v->diff_prev, t = (p + 1) % 3, o = (p + 2) % 3;
   uint32_t seed_dt = fr.next();
-  STAGE("diff_temporal", launch_diff_temporal(fp, w, h, dk, ga, prev_depth, in->diff_hit_pos_normal,
+  STAGE("diff_temporal", launch_diff_temporal(form, fp, w, h, dk, ga, prev_depth, in->diff_hit_pos_normal,
                                               in->diff_hit_radiance, in->diff_source_pdf, b.diff_rsv[p],
                                               b.diff_rsv[t], seed_dt, has_prev ? 1u : 0u, 1u, s));
   ++launches;
@@ -569,8 +588,8 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
   for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
     bool last = k + 1 == P.diff_spatial_passes;
     uint32_t seed_ds = fr.next();
-    STAGE("diff_spatial", launch_diff_spatial(fp, w, h, dk, ga, b.ao_filtered, b.diff_rsv[src], b.diff_rsv[dst],
-                                              last ? b.diff_light : nullptr, seed_ds, s));
+    STAGE("diff_spatial", launch_diff_spatial(form, fp, w, h, dk, ga, b.ao_filtered, b.diff_rsv[src],
+                                              b.diff_rsv[dst], last ? b.diff_light : nullptr, seed_ds, s));
     ++launches;
     std::swap(src, dst);
   }
@@ -592,7 +611,7 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
       bool last = k + 1 == P.spec_spatial_passes;
       uint32_t seed_ss = fr.next();
       STAGE("spec_spatial",
-            launch_spec_spatial(fp, w, h, sk, ga, b.spec_rsv[ssrc], b.spec_hp[ssrc], b.spec_rad[ssrc],
+            launch_spec_spatial(form, fp, w, h, sk, ga, b.spec_rsv[ssrc], b.spec_hp[ssrc], b.spec_rad[ssrc],
                                 last ? b.spec_light : nullptr, last ? b.ray_len : nullptr,
                                 last ? nullptr : b.spec_rsv[sdst], last ? nullptr : b.spec_hp[sdst],
                                 last ? nullptr : b.spec_rad[sdst], seed_ss, s));
@@ -605,18 +624,71 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
 
   // Denoiser.
   const bool run_denoiser = P.denoise && has_prev;
-  if (run_denoiser) {
+  if (run_denoiser && f32) {
+    DenoiseKnobs kn = {1.0f / P.history_max_frames, P.fast_history_clamp};
+    uint32_t has_history = v->denoise_history ? 1u : 0u;
+    // rec[0]/len[0] = history; rec[2]/len[1] = temporal output; rec[1] = fix output.
+    STAGE("dn_temporal", launch_dn32_temporal(fp, w, h, kn, ga, pga, (const float4*)b.diff_light,
+                                              (const float4*)b.spec_light, prev_depth, b.rec[0],
+                                              (const float*)b.len[0], b.rec_fast[0], b.rec[2], (float*)b.len[1],
+                                              b.rec_fast[1], has_history, s));
+    ++launches;
+    float4* cur = b.rec[2];
+    if (P.disocclusion_fix) {
+      STAGE("dn_fix", launch_dn32_fix(w, h, ga, (const float*)b.len[1], b.rec[2], b.rec[1], s));
+      ++launches;
+      cur = b.rec[1];
+    }
+    if (P.fast_history_clamp) {
+      STAGE("dn_fast_clamp", launch_dn32_fast_clamp(w, h, b.rec_fast[1], cur, s));
+      ++launches;
+      std::swap(b.rec_fast[0], b.rec_fast[1]);
+      v->fast_history_valid = true;
+    } else {
+      v->fast_history_valid = false;
+    }
+    // History feedback before the spatial passes (denoising.rs:209-216).
+    if (cur == b.rec[1])
+      std::swap(b.rec[0], b.rec[1]);
+    else
+      std::swap(b.rec[0], b.rec[2]);
+    std::swap(b.len[0], b.len[1]);
+    v->denoise_history = true;
+    STAGE("dn_fallback", launch_dn32_fallback(w, h, ga, (const float*)b.len[0], b.rec[0], b.rec[4], s));
+    ++launches;
+    float4* rsrc = b.rec[4];
+    float4* rdst = b.rec[2];
+    const uint32_t iters = P.atrous_iterations;
+    for (uint32_t k = 0; k < iters; ++k) {
+      bool last = k + 1 == iters;
+      float4* od = last && out ? (float4*)out->diffuse : nullptr;
+      float4* os = last && out ? (float4*)out->specular : nullptr;
+      STAGE("dn_atrous", launch_dn32_atrous(w, h, ga, rsrc, rdst, od, os, 1 << k, s));
+      ++launches;
+      rsrc = rdst;
+      rdst = rdst == b.rec[2] ? b.rec[3] : b.rec[2];
+    }
+    if (iters == 0 && out && (out->diffuse || out->specular)) {
+      // Zero iterations: the fallback output is the result (copy its colours out).
+      if (out->diffuse)
+        VLT_TRY(cudaMemcpy2DAsync(out->diffuse, 16, b.rec[4], 32, 16, n, cudaMemcpyDeviceToDevice, s));
+      if (out->specular)
+        VLT_TRY(cudaMemcpy2DAsync(out->specular, 16, (char*)b.rec[4] + 16, 32, 16, n, cudaMemcpyDeviceToDevice, s));
+    }
+  } else if (run_denoiser) {
     DenoiseKnobs kn = {1.0f / P.history_max_frames, P.fast_history_clamp};
     uint32_t has_history = v->denoise_history ? 1u : 0u;
     // color[0]/mom[0]/len[0] = history; color[2]/mom[2]/len[1] = temporal output;
     // color[1]/mom[1] = fix output.
-    STAGE("dn_temporal", launch_dn_temporal(fp, w, h, kn, ga, pga, b.diff_light, b.spec_light, b.ray_len, prev_depth,
-                                            b.color[0], b.mom[0], b.len[0], b.fast[0], b.color[2], b.mom[2], b.len[1],
-                                            b.fast[1], has_history, s));
+    STAGE("dn_temporal", launch_dn_temporal(fp, w, h, kn, ga, pga, (const uint32_t*)b.diff_light,
+                                            (const uint32_t*)b.spec_light, b.ray_len, prev_depth, b.color[0],
+                                            b.mom[0], (const uint8_t*)b.len[0], b.fast[0], b.color[2], b.mom[2],
+                                            (uint8_t*)b.len[1], b.fast[1], has_history, s));
     ++launches;
     uint32_t* cur_color = b.color[2];
     if (P.disocclusion_fix) {
-      STAGE("dn_fix", launch_dn_fix(w, h, ga, b.len[1], b.color[2], b.mom[2], b.color[1], b.mom[1], s));
+      STAGE("dn_fix", launch_dn_fix(w, h, ga, (const uint8_t*)b.len[1], b.color[2], b.mom[2], b.color[1], b.mom[1],
+                                    s));
       ++launches;
       cur_color = b.color[1];
     }
@@ -639,7 +711,8 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
     std::swap(b.len[0], b.len[1]);
     v->denoise_history = true;
     // Now color[0]/mom[0]/len[0] hold this frame's history.
-    STAGE("dn_fallback", launch_dn_fallback(w, h, ga, b.len[0], b.color[0], b.mom[0], b.color_c, b.var[0], s));
+    STAGE("dn_fallback", launch_dn_fallback(w, h, ga, (const uint8_t*)b.len[0], b.color[0], b.mom[0], b.color_c,
+                                            b.var[0], s));
     ++launches;
     uint32_t* csrc = b.color_c;
     uint32_t* vsrc = b.var[0];
@@ -664,14 +737,15 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
   } else {
     v->denoise_history = false;  // Denoiser::reset
     v->fast_history_valid = false;
-    if (out && out->diffuse) VLT_TRY(cudaMemcpyAsync(out->diffuse, b.diff_light, 4 * n, cudaMemcpyDeviceToDevice, s));
+    if (out && out->diffuse)
+      VLT_TRY(cudaMemcpyAsync(out->diffuse, b.diff_light, light_bytes, cudaMemcpyDeviceToDevice, s));
     if (out && out->specular)
-      VLT_TRY(cudaMemcpyAsync(out->specular, b.spec_light, 4 * n, cudaMemcpyDeviceToDevice, s));
+      VLT_TRY(cudaMemcpyAsync(out->specular, b.spec_light, light_bytes, cudaMemcpyDeviceToDevice, s));
   }
   if (out && out->raw_diffuse)
-    VLT_TRY(cudaMemcpyAsync(out->raw_diffuse, b.diff_light, 4 * n, cudaMemcpyDeviceToDevice, s));
+    VLT_TRY(cudaMemcpyAsync(out->raw_diffuse, b.diff_light, light_bytes, cudaMemcpyDeviceToDevice, s));
   if (out && out->raw_specular)
-    VLT_TRY(cudaMemcpyAsync(out->raw_specular, b.spec_light, 4 * n, cudaMemcpyDeviceToDevice, s));
+    VLT_TRY(cudaMemcpyAsync(out->raw_specular, b.spec_light, light_bytes, cudaMemcpyDeviceToDevice, s));
 
   // Retain depth for the next frame unless the caller keeps it (the previous
   // frame's decoded G-buffer fields stay in the other surface slot).
@@ -700,7 +774,7 @@ vlt_status vlt_ind_diff_temporal_resample(const vlt_frame_params* fp, uint32_t w
       (has_new_sample && params->use_input_pdf && !new_source_pdf))
     return VLT_ERR_INVALID_ARG;
   GeoArgs ga = {gbuffer_depth, nullptr, fp->inv_view_proj, nullptr, nullptr, nullptr};
-  launch_diff_temporal(*fp, width, height, diff_knobs(*params), ga, prev_gbuffer_depth, new_hit_pos_normal,
+  launch_diff_temporal(FORM_REF, *fp, width, height, diff_knobs(*params), ga, prev_gbuffer_depth, new_hit_pos_normal,
                        new_hit_radiance, new_source_pdf, prev_reservoir, rw_reservoir, frame_rand, has_prev_frame,
                        has_new_sample, (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
@@ -713,7 +787,7 @@ vlt_status vlt_ao_gen(const vlt_frame_params* fp, uint32_t width, uint32_t heigh
       (has_prev_frame && !prev_ao))
     return VLT_ERR_INVALID_ARG;
   GeoArgs ga = {depth_buffer, nullptr, fp->inv_view_proj, nullptr, nullptr, nullptr};
-  launch_ao_gen(*fp, width, height, ga, hit_pos_normal, (const uint32_t*)prev_ao, (uint32_t*)rw_ao, has_new_sample,
+  launch_ao_gen(FORM_REF, *fp, width, height, ga, hit_pos_normal, (const uint32_t*)prev_ao, (uint32_t*)rw_ao, has_new_sample,
                 has_prev_frame, radius_ws, (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
 }
@@ -721,7 +795,7 @@ vlt_status vlt_ao_gen(const vlt_frame_params* fp, uint32_t width, uint32_t heigh
 vlt_status vlt_ao_filter(uint32_t width, uint32_t height, const float* depth_buffer, const uint16_t* ao,
                          uint16_t* rw_filtered_ao, void* stream) {
   if (!dims_ok(width, height) || !depth_buffer || !ao || !rw_filtered_ao) return VLT_ERR_INVALID_ARG;
-  launch_ao_filter(width, height, depth_buffer, (const uint32_t*)ao, rw_filtered_ao, (cudaStream_t)stream);
+  launch_ao_filter(FORM_REF, width, height, depth_buffer, ao, rw_filtered_ao, (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
 }
 
@@ -734,7 +808,7 @@ vlt_status vlt_ind_diff_spatial_resample(const vlt_frame_params* fp, uint32_t wi
       !temp_reservoir || !rw_reservoir)
     return VLT_ERR_INVALID_ARG;
   GeoArgs ga = {gbuffer_depth, gbuffer_color, fp->inv_view_proj, nullptr, nullptr, nullptr};
-  launch_diff_spatial(*fp, width, height, diff_knobs(*params), ga, ao_texture, temp_reservoir, rw_reservoir,
+  launch_diff_spatial(FORM_REF, *fp, width, height, diff_knobs(*params), ga, ao_texture, temp_reservoir, rw_reservoir,
                       rw_lighting, frame_rand, (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());
 }
@@ -773,7 +847,7 @@ vlt_status vlt_ind_spec_spatial_resample(const vlt_frame_params* fp, uint32_t wi
     return VLT_ERR_INVALID_ARG;
   SpecKnobs sk = {params->spec_spatial_taps, params->spec_spatial_radius_px};
   GeoArgs ga = {gbuffer_depth, gbuffer_color, fp->inv_view_proj, nullptr, nullptr, nullptr};
-  launch_spec_spatial(*fp, width, height, sk, ga, reservoir, hit_pos, hit_radiance,
+  launch_spec_spatial(FORM_REF, *fp, width, height, sk, ga, reservoir, hit_pos, hit_radiance,
                       rw_lighting, rw_ray_len, rw_reservoir, rw_hit_pos, rw_hit_radiance, frame_rand,
                       (cudaStream_t)stream);
   return cuda_status(cudaGetLastError());

@@ -1,0 +1,559 @@
+// ReLAX/SVGF denoiser, f32 storage form.
+//
+// Same passes as denoise.cu (svgf_temporal_filter.hlsl, relax_disocclusion_fix.hlsl,
+// relax_fast_history_clamp.hlsl, svgf_spatial_fallback_filter.hlsl,
+// svgf_atrous_filter.hlsl) with every stored value in binary32 and one 32-byte record
+// per pixel: DnRec = {float4 diffuse.rgb|aux.x, float4 specular.rgb|aux.y}, where aux
+// holds the second moments (temporal/fix outputs and the history) or the variance
+// (fallback and a-trous). Nothing is quantized between passes.
+//
+// Arithmetic: binary32 with explicit fused multiply-adds. Every fma_() below is one
+// IEEE fusedMultiplyAdd (fmaf on the host gives the same bits), every other
+// operation is a separately rounded IEEE operation (the build disables contraction),
+// and exp is exp2_fma: the project's exp2 construction (n = rint(x), degree-6
+// polynomial on [-1/2, 1/2]) evaluated by FMA Horner steps. No approximate
+// hardware function is used, so the f32-form denoiser is bit-reproducible by the
+// CPU restatement. That matters here beyond testing: the a-trous luminance weight
+// divides by the square root of a variance computed as E[l^2] - E[l]^2, which
+// cancels near zero, so a last-bit difference upstream can change a weight
+// completely.
+#include "vlt_internal.h"
+
+namespace vlt {
+
+namespace {
+
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// 2^x: x = n + f, n = rint(x), p(f) by FMA Horner steps with the coefficients of
+// exp2_, then p * 2^n (two-step scale below 2^-126 keeps gradual underflow exact).
+__device__ __forceinline__ float exp2_fma(float x) {
+  if (is_nan(x)) return as_float(0x7FFFFFFFu);
+  if (x >= 128.0f) return as_float(0x7F800000u);
+  if (x < -151.0f) return 0.0f;
+  float n = rint_(x);
+  float f = x - n;
+  float p = VLT_EXP2_C6;
+  p = fma_(p, f, VLT_EXP2_C5);
+  p = fma_(p, f, VLT_EXP2_C4);
+  p = fma_(p, f, VLT_EXP2_C3);
+  p = fma_(p, f, VLT_EXP2_C2);
+  p = fma_(p, f, VLT_EXP2_C1);
+  p = fma_(p, f, VLT_EXP2_C0);
+  int32_t ni = f2i_rz(n);
+  if (ni > 127) return (p * 2.0f) * as_float(0x7F000000u);
+  if (ni < -126) return (p * as_float(0x00800000u)) * as_float((uint32_t)(ni + 126 + 127) << 23);
+  return p * as_float((uint32_t)(ni + 127) << 23);
+}
+__device__ __forceinline__ float exp_fma(float x) { return exp2_fma(x * VLT_LOG2E); }
+__device__ __forceinline__ float lum_fast(float r, float g, float b) {
+  return fma_(b, 0.0722f, fma_(g, 0.7152f, r * 0.2126f));
+}
+
+struct Rec {
+  f3 d, s;
+  f2 aux;
+};
+
+__device__ __forceinline__ Rec load_rec(const float4* __restrict__ p, size_t i) {
+  float4 a = p[2 * i], b = p[2 * i + 1];
+  Rec r;
+  r.d = mk3(a.x, a.y, a.z);
+  r.s = mk3(b.x, b.y, b.z);
+  r.aux = mk2(a.w, b.w);
+  return r;
+}
+__device__ __forceinline__ void store_rec(float4* __restrict__ p, size_t i, f3 d, f3 s, f2 aux) {
+  p[2 * i] = make_float4(d.x, d.y, d.z, aux.x);
+  p[2 * i + 1] = make_float4(s.x, s.y, s.z, aux.y);
+}
+
+// EdgeStoppingFunc (svgf.inc.hlsl:6-84).
+struct EdgeStopFast {
+  float depth_center, fz_sigma;  // sigma_z * fwidth_z
+  f3 normal_center;
+  f2 lumi_center, lumi_rcp;
+  bool use_lumi;
+  int sigma_n_log2;
+
+  __device__ __forceinline__ f2 weight(float tap_dist, float depth, f3 normal, f2 lumi) const {
+    float dist_z = fabsf(depth - depth_center);
+    float wz = -dist_z / fma_(fz_sigma, tap_dist, 1e-8f);
+    float n_dot = saturate(fma_(normal_center.z, normal.z, fma_(normal_center.y, normal.y, normal_center.x * normal.x)));
+    float wn = pow_2k(n_dot, sigma_n_log2);
+    float ax = wz, ay = wz;
+    if (use_lumi) {
+      ax = fma_(-fabsf(lumi.x - lumi_center.x), lumi_rcp.x, wz);
+      ay = fma_(-fabsf(lumi.y - lumi_center.y), lumi_rcp.y, wz);
+    }
+    return mk2(wn * exp_fma(ax), wn * exp_fma(ay));
+  }
+};
+
+__device__ __forceinline__ EdgeStopFast make_es(float depth, float fwidth_z, float sigma_z, f3 normal, int n_log2) {
+  EdgeStopFast e;
+  e.depth_center = depth;
+  e.fz_sigma = sigma_z * fwidth_z;
+  e.normal_center = normal;
+  e.lumi_center = mk2(0.0f, 0.0f);
+  e.lumi_rcp = mk2(0.0f, 0.0f);
+  e.use_lumi = false;
+  e.sigma_n_log2 = n_log2;
+  return e;
+}
+
+// dsr_weight (svgf_temporal_filter.hlsl:89-93), exact contract.
+__device__ __forceinline__ float dsr_weight_exact(f3 c, f3 mean, f3 dev) {
+  float dist = luminance(abs3(c - mean) / dev);
+  return exp2_(-10.0f * dist);
+}
+
+__device__ __forceinline__ f3 fma3(float w, f3 v, f3 acc) {
+  return mk3(fma_(w, v.x, acc.x), fma_(w, v.y, acc.y), fma_(w, v.z, acc.z));
+}
+
+__device__ __forceinline__ float quad_max_len(const float* __restrict__ len, int x, int y, int w, int h) {
+  int x0 = x & ~1, y0 = y & ~1;
+  float m = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    int px = x0 + (k & 1), py = y0 + (k >> 1);
+    float v = inb(px, py, w, h) ? len[(size_t)py * w + px] : 0.0f;
+    m = fmax_(m, v);
+  }
+  return m;
+}
+
+}  // namespace
+
+// --------------------------------------------------------------- temporal
+
+template <class Geo>
+__global__ void __launch_bounds__(128) k_dn32_temporal(vlt_frame_params fp, int w, int h, DenoiseKnobs kn, Geo geo,
+                                                        Geo prev_geo, const uint32_t* __restrict__ gbuf,
+                                                        const float4* __restrict__ diff_src,
+                                                        const float4* __restrict__ spec_src,
+                                                        const float* __restrict__ prev_depth,
+                                                        const float4* __restrict__ hist,
+                                                        const float* __restrict__ len_hist,
+                                                        const float4* __restrict__ fast_hist,
+                                                        float4* __restrict__ out, float* __restrict__ out_len,
+                                                        float4* __restrict__ out_fast, uint32_t has_history) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  float depth = geo.dep(i);
+  if (depth == 0.0f) {
+    out_len[i] = 0.0f;
+    store_rec(out, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
+    if (kn.fast_history) store_rec(out_fast, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
+    return;
+  }
+  const float bw = (float)w, bh = (float)h;
+  f2 screen_uv = mk2(((float)x + 0.5f) / bw, ((float)y + 0.5f) / bh);
+  const f3 gnormal = geo.normal(i);
+  const float grough = geo.rough(i);
+  const float fwz = geo.fwz(i);
+  const float fwn = f16tof32(gbuf[2 * (size_t)w * h + i] >> 16);
+
+  f3 m1 = mk3(0.0f), m2 = mk3(0.0f);
+#pragma unroll
+  for (int dx = -1; dx <= 1; ++dx) {
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy) {
+      int px = x + dx, py = y + dy;
+      px = px < 0 ? 0 : (px > w - 1 ? w - 1 : px);
+      py = py < 0 ? 0 : (py > h - 1 ? h - 1 : py);
+      float4 sv = spec_src[(size_t)py * w + px];
+      f3 s = mk3(sv.x, sv.y, sv.z);
+      m1 = m1 + s;
+      m2 = m2 + s * s;
+    }
+  }
+  m1 = m1 * (1.0f / 9.0f);
+  m2 = m2 * (1.0f / 9.0f);
+
+  const f3 position = geo.pos(x, y, i);
+  const float4 s_center = spec_src[i];
+  f3 vsh = mk3(0.0f), vsfh = mk3(0.0f);
+  {
+    f3 vdir = normalize3(position - vpos3(fp.view_pos));
+    f3 vp = position + vdir * s_center.w;  // w: specular ray length
+    f4 hr = mul44(fp.prev_view_proj, mk4(vp.x, vp.y, vp.z, 1.0f));
+    f2 ndc = mk2(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3]);
+    f2 vuv = mk2((ndc.x + fp.jitter[0]) * 0.5f + 0.5f, (ndc.y + fp.jitter[1]) * 0.5f + 0.5f);
+    bool valid = vuv.x == saturate(vuv.x) && vuv.y == saturate(vuv.y) && has_history;
+    if (valid) {
+      BilinearTaps t = bilinear_taps(vuv, w, h);
+      size_t a = (size_t)t.y0 * w + t.x0, b = (size_t)t.y0 * w + t.x1, c = (size_t)t.y1 * w + t.x0,
+             d = (size_t)t.y1 * w + t.x1;
+      vsh = bilerp3(load_rec(hist, a).s, load_rec(hist, b).s, load_rec(hist, c).s, load_rec(hist, d).s, t.fx, t.fy);
+      if (kn.fast_history)
+        vsfh = bilerp3(load_rec(fast_hist, a).s, load_rec(fast_hist, b).s, load_rec(fast_hist, c).s,
+                       load_rec(fast_hist, d).s, t.fx, t.fy);
+    }
+  }
+  f2 mv;
+  float reproj_depth;
+  {
+    f4 hp = mul44(fp.view_proj, mk4(position.x, position.y, position.z, 1.0f));
+    f2 ndc = mk2(hp.x / hp.w - fp.jitter[0], hp.y / hp.w - fp.jitter[1]);
+    f4 hr = mul44(fp.prev_view_proj, mk4(position.x, position.y, position.z, 1.0f));
+    f2 ndc_r = mk2(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3]);
+    mv = mk2((ndc.x - ndc_r.x) * 0.5f, (ndc.y - ndc_r.y) * 0.5f);
+    reproj_depth = hr.z / hr.w;
+  }
+  f2 huv = mk2(screen_uv.x - mv.x, screen_uv.y - mv.y);
+  f3 dh = mk3(0.0f), sh = mk3(0.0f), dfh = mk3(0.0f), sfh = mk3(0.0f);
+  f2 smh = mk2(0.0f, 0.0f);
+  float hl = 0.0f;
+  bool valid = huv.x == saturate(huv.x) && huv.y == saturate(huv.y) && has_history;
+  if (valid) {
+    f2 pcc = mk2(huv.x * bw - 0.5f, huv.y * bh - 0.5f);
+    f2 frac = mk2(pcc.x - floor_(pcc.x), pcc.y - floor_(pcc.y));
+    int bx = f2i_rz(pcc.x), by = f2i_rz(pcc.y);
+    float depth_tol = fwz * 4.0f + 1e-4f;
+    float normal_tol = fwn * 16.0f + 1e-2f;
+    float normal_tol_sq = normal_tol * normal_tol;
+    float bb = frac.y, rr = frac.x, tt = 1.0f - bb, ll = 1.0f - rr;
+    float wts[2][2] = {{tt * ll, tt * rr}, {bb * ll, bb * rr}};
+    f3 ds = mk3(0.0f), ss = mk3(0.0f), dfs = mk3(0.0f), sfs = mk3(0.0f);
+    f2 ms = mk2(0.0f, 0.0f);
+    float hs = 0.0f, wsum = 0.0f;
+#pragma unroll
+    for (int ox = 0; ox < 2; ++ox) {
+#pragma unroll
+      for (int oy = 0; oy < 2; ++oy) {
+        int px = bx + ox, py = by + oy;
+        bool cv = px >= 0 && py >= 0 && px <= w - 1 && py <= h - 1;
+        if (!cv) continue;
+        size_t j = (size_t)py * w + px;
+        f3 nd = prev_geo.normal(j) - gnormal;
+        bool ok = fabs_(prev_depth[j] - reproj_depth) < depth_tol && dot3(nd, nd) < normal_tol_sq;
+        if (!ok) continue;
+        float wt = wts[oy][ox];
+        wsum = wsum + wt;
+        hs = hs + wt * len_hist[j];
+        Rec r = load_rec(hist, j);
+        ds = fma3(wt, r.d, ds);
+        ss = fma3(wt, r.s, ss);
+        ms = mk2(fma_(wt, r.aux.x, ms.x), fma_(wt, r.aux.y, ms.y));
+        if (kn.fast_history) {
+          Rec f = load_rec(fast_hist, j);
+          dfs = fma3(wt, f.d, dfs);
+          sfs = fma3(wt, f.s, sfs);
+        }
+      }
+    }
+    valid = wsum > 0.00390625f;
+    if (valid) {
+      float inv = 1.0f / wsum;
+      dh = ds * inv;
+      sh = ss * inv;
+      smh = ms * inv;
+      hl = hs * inv;
+      dfh = dfs * inv;
+      sfh = sfs * inv;
+    }
+  }
+  if (!valid) {
+    dh = sh = dfh = sfh = mk3(0.0f);
+    smh = mk2(0.0f, 0.0f);
+    hl = 0.0f;
+  }
+  hl = hl + VLT_HISTORY_LEN_UNIT;
+
+  float4 dv = diff_src[i];
+  f3 dsrc = mk3(dv.x, dv.y, dv.z);
+  f3 ssrc = mk3(s_center.x, s_center.y, s_center.z);
+  f2 lsrc = mk2(lum_fast(dsrc.x, dsrc.y, dsrc.z), lum_fast(ssrc.x, ssrc.y, ssrc.z));
+  f2 smsrc = lsrc * lsrc;
+  const float bfd = kn.blend_diff;
+  const float bff = 1.0f / 3.0f;
+  float blurness = sqrt_(saturate(grough * 6.0f));
+  const float bfs = lerpf(7.0f / 8.0f, bfd, blurness);
+  const float bfsf = lerpf(1.0f, bff, blurness);
+  float ratio = VLT_HISTORY_LEN_UNIT / hl;
+  f2 alpha = mk2(fmax_(bfd, ratio), fmax_(bfs, ratio));
+  f3 df = lerp3(dh, dsrc, alpha.x);
+  f2 smf = mk2(lerpf(smh.x, smsrc.x, alpha.x), lerpf(smh.y, smsrc.y, alpha.y));
+  f2 alpha_f = mk2(fmax_(bff, ratio), fmax_(bfsf, ratio));
+  f3 dff = lerp3(dfh, dsrc, alpha_f.x);
+  f3 sff = lerp3(sfh, ssrc, alpha_f.y);
+  f3 sf;
+  {
+    f3 mean = m1;
+    f3 dev = sqrt3(abs3(m2 - mean * mean));
+    dev = mk3(fmax_(dev.x, 1e-19f), fmax_(dev.y, 1e-19f), fmax_(dev.z, 1e-19f));
+    float wv = dsr_weight_exact(vsh, mean, dev);
+    float wh = dsr_weight_exact(sh, mean, dev);
+    f3 dual = (wv * vsh + wh * sh) / fmax_(wv + wh, 1e-37f);
+    sf = lerp3(dual, ssrc, alpha.y);
+    if (kn.fast_history) {
+      float wv2 = dsr_weight_exact(vsfh, mean, dev);
+      float wh2 = dsr_weight_exact(sfh, mean, dev);
+      f3 dual2 = (wv2 * vsfh + wh2 * sfh) / fmax_(wv2 + wh2, 1e-37f);
+      sff = lerp3(dual2, ssrc, alpha_f.y);
+    }
+  }
+  store_rec(out, i, df, sf, smf);
+  out_len[i] = hl;
+  if (kn.fast_history) store_rec(out_fast, i, dff, sff, mk2(0.0f, 0.0f));
+}
+
+// ----------------------------------------------------------- disocclusion fix
+
+template <class Geo>
+__global__ void __launch_bounds__(128) k_dn32_fix(int w, int h, Geo geo, const float* __restrict__ len,
+                                                   const float4* __restrict__ in, float4* __restrict__ out) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  float hl = len[i];
+  float qmax = quad_max_len(len, x, y, w, h);
+  if (hl == 0.0f) {
+    store_rec(out, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
+    return;
+  }
+  hl = qmax;
+  if (hl < 4.0f * VLT_HISTORY_LEN_UNIT) {
+    EdgeStopFast es = make_es(geo.dep(i), geo.fwz(i), 5.0f, geo.normal(i), 5);
+    f2 ws = mk2(0.0f, 0.0f);
+    f3 dsum = mk3(0.0f), ssum = mk3(0.0f);
+    f2 msum = mk2(0.0f, 0.0f);
+    const int stride = f2i_rz((14.0f * VLT_HISTORY_LEN_UNIT) / hl);
+    for (int oy = -2; oy <= 2; ++oy) {
+      for (int ox = -2; ox <= 2; ++ox) {
+        int offx = ox * stride, offy = oy * stride;
+        int cx = x + offx, cy = y + offy;
+        if (!(cx >= 0 && cy >= 0 && cx <= w - 1 && cy <= h - 1)) continue;
+        size_t j = (size_t)cy * w + cx;
+        f2 wt = es.weight(length2(mk2((float)offx, (float)offy)), geo.dep(j), geo.normal(j), mk2(0.0f, 0.0f));
+        Rec r = load_rec(in, j);
+        ws = ws + wt;
+        dsum = fma3(wt.x, r.d, dsum);
+        ssum = fma3(wt.y, r.s, ssum);
+        msum = mk2(fma_(wt.x, r.aux.x, msum.x), fma_(wt.y, r.aux.y, msum.y));
+      }
+    }
+    store_rec(out, i, dsum * (1.0f / ws.x), ssum * (1.0f / ws.y), mk2(msum.x / ws.x, msum.y / ws.y));
+  } else {
+    out[2 * i] = in[2 * i];
+    out[2 * i + 1] = in[2 * i + 1];
+  }
+}
+
+// ------------------------------------------------------ fast history clamp
+
+__device__ __forceinline__ f3 ycocg(f3 c) {
+  return mk3(c.x * 0.25f + c.y * 0.5f + c.z * 0.25f, c.x * 0.5f - c.z * 0.5f, c.x * -0.25f + c.y * 0.5f - c.z * 0.25f);
+}
+__device__ __forceinline__ f3 ycocg_inv(f3 c) {
+  float tmp = c.x - c.z;
+  return mk3(tmp + c.y, c.x + c.z, tmp - c.y);
+}
+
+__global__ void __launch_bounds__(128) k_dn32_fast_clamp(int w, int h, const float4* __restrict__ fast,
+                                                          float4* __restrict__ rec) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  f3 dm1 = mk3(0.0f), dm2 = mk3(0.0f), sm1 = mk3(0.0f), sm2 = mk3(0.0f);
+  for (int oy = -1; oy <= 1; ++oy) {
+    for (int ox = -1; ox <= 1; ++ox) {
+      int cx = x + ox, cy = y + oy;
+      cx = cx < 0 ? 0 : (cx > w - 1 ? w - 1 : cx);
+      cy = cy < 0 ? 0 : (cy > h - 1 ? h - 1 : cy);
+      Rec f = load_rec(fast, (size_t)cy * w + cx);
+      f3 d = ycocg(f.d), s = ycocg(f.s);
+      dm1 = dm1 + d;
+      dm2 = dm2 + d * d;
+      sm1 = sm1 + s;
+      sm2 = sm2 + s * s;
+    }
+  }
+  dm1 = dm1 / 9.0f;
+  dm2 = dm2 / 9.0f;
+  sm1 = sm1 / 9.0f;
+  sm2 = sm2 / 9.0f;
+  f3 ddev = sqrt3(dm2 - dm1 * dm1) * 0.75f;
+  f3 sdev = sqrt3(sm2 - sm1 * sm1) * 0.75f;
+  Rec c = load_rec(rec, i);
+  f3 d = clamp3(ycocg(c.d), dm1 - ddev, dm1 + ddev);
+  f3 s = clamp3(ycocg(c.s), sm1 - sdev, sm1 + sdev);
+  store_rec(rec, i, ycocg_inv(d), ycocg_inv(s), c.aux);
+}
+
+// ---------------------------------------------------------- spatial fallback
+
+template <class Geo>
+__global__ void __launch_bounds__(128) k_dn32_fallback(int w, int h, Geo geo, const float* __restrict__ len,
+                                                        const float4* __restrict__ in, float4* __restrict__ out) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  float hl = len[i];
+  float qmax = quad_max_len(len, x, y, w, h);
+  if (hl == 0.0f) {
+    store_rec(out, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
+    return;
+  }
+  hl = qmax;
+  f3 dd, sd;
+  f2 md;
+  if (hl < 4.0f * VLT_HISTORY_LEN_UNIT) {
+    EdgeStopFast es = make_es(geo.dep(i), geo.fwz(i) * 3.0f, 1.0f, geo.normal(i), 7);
+    float ws = 0.0f;
+    f3 dsum = mk3(0.0f), ssum = mk3(0.0f);
+    f2 msum = mk2(0.0f, 0.0f);
+    for (int oy = -3; oy <= 3; ++oy) {
+      for (int ox = -3; ox <= 3; ++ox) {
+        int cx = x + ox, cy = y + oy;
+        if (!(cx >= 0 && cy >= 0 && cx <= w - 1 && cy <= h - 1)) continue;
+        size_t j = (size_t)cy * w + cx;
+        float wt = es.weight(length2(mk2((float)ox, (float)oy)), geo.dep(j), geo.normal(j), mk2(0.0f, 0.0f)).x;
+        Rec r = load_rec(in, j);
+        ws = ws + wt;
+        dsum = fma3(wt, r.d, dsum);
+        ssum = fma3(wt, r.s, ssum);
+        msum = mk2(fma_(wt, r.aux.x, msum.x), fma_(wt, r.aux.y, msum.y));
+      }
+    }
+    float inv = 1.0f / ws;
+    dd = dsum * inv;
+    sd = ssum * inv;
+    md = msum * inv;
+  } else {
+    Rec r = load_rec(in, i);
+    dd = r.d;
+    sd = r.s;
+    md = r.aux;
+  }
+  f2 fst = mk2(lum_fast(dd.x, dd.y, dd.z), lum_fast(sd.x, sd.y, sd.z));
+  f2 var = mk2(fmax_(fma_(-fst.x, fst.x, md.x), 0.0f), fmax_(fma_(-fst.y, fst.y, md.y), 0.0f));
+  float boost = fmax_(1.0f, (4.0f * VLT_HISTORY_LEN_UNIT) / hl);
+  store_rec(out, i, dd, sd, var * boost);
+}
+
+// --------------------------------------------------------------- a-trous
+
+struct AtrousTaps32 {
+  float dist[16];
+};
+
+template <class Geo>
+__global__ void __launch_bounds__(128) k_dn32_atrous(int w, int h, Geo geo, AtrousTaps32 taps,
+                                                      const float4* __restrict__ in, float4* __restrict__ out,
+                                                      float4* __restrict__ out_diff, float4* __restrict__ out_spec,
+                                                      int step) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  Rec c = load_rec(in, i);
+  EdgeStopFast es = make_es(geo.dep(i), geo.fwz(i), 1.0f, geo.normal(i), 7);
+  es.use_lumi = true;
+  es.lumi_center = mk2(lum_fast(c.d.x, c.d.y, c.d.z), lum_fast(c.s.x, c.s.y, c.s.z));
+  es.lumi_rcp = mk2(1.0f / fma_(4.0f, sqrt_(c.aux.x), 1e-8f), 1.0f / fma_(4.0f, sqrt_(c.aux.y), 1e-8f));
+  const float kw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
+  f3 dsum = c.d, ssum = c.s;
+  f2 vsum = c.aux;
+  f2 wsum = mk2(1.0f, 1.0f);
+  int tap = 0;
+#pragma unroll
+  for (int oy = -2; oy <= 2; ++oy) {
+    if (oy == 0) continue;
+    const float kwy = kw[oy < 0 ? -oy : oy];
+#pragma unroll
+    for (int ox = -2; ox <= 2; ++ox) {
+      if (ox == 0) continue;
+      const float tap_dist = taps.dist[tap++];
+      int cx = x + ox * step, cy = y + oy * step;
+      if (!(cx >= 0 && cy >= 0 && cx <= w - 1 && cy <= h - 1)) continue;
+      const float k = kwy * kw[ox < 0 ? -ox : ox];
+      size_t j = (size_t)cy * w + cx;
+      Rec r = load_rec(in, j);
+      f2 lumi = mk2(lum_fast(r.d.x, r.d.y, r.d.z), lum_fast(r.s.x, r.s.y, r.s.z));
+      f2 e = es.weight(tap_dist, geo.dep(j), geo.normal(j), lumi);
+      f2 wt = mk2(k * e.x, k * e.y);
+      dsum = fma3(wt.x, r.d, dsum);
+      ssum = fma3(wt.y, r.s, ssum);
+      vsum = mk2(fma_(wt.x * wt.x, r.aux.x, vsum.x), fma_(wt.y * wt.y, r.aux.y, vsum.y));
+      wsum = wsum + wt;
+    }
+  }
+  f2 inv = mk2(1.0f / wsum.x, 1.0f / wsum.y);
+  f3 dd = dsum * inv.x, sd = ssum * inv.y;
+  f2 vd = mk2(vsum.x * inv.x * inv.x, vsum.y * inv.y * inv.y);
+  if (out) store_rec(out, i, dd, sd, vd);
+  if (out_diff) out_diff[i] = make_float4(dd.x, dd.y, dd.z, 0.0f);
+  if (out_spec) out_spec[i] = make_float4(sd.x, sd.y, sd.z, 0.0f);
+}
+
+// ------------------------------------------------------------- launchers
+
+static const dim3 kBlock(32, 4, 1);
+
+#define VLT_GEO_DISPATCH(ga, ...)                \
+  do {                                           \
+    if ((ga).nd) {                               \
+      GeoSurface geo = {(ga).nd, (ga).pr, (ga).fz, w, h}; \
+      __VA_ARGS__;                               \
+    } else {                                     \
+      GeoRaw geo = {(ga).depth, (ga).gbuf, (ga).inv_vp, w, h}; \
+      __VA_ARGS__;                               \
+    }                                            \
+  } while (0)
+
+void launch_dn32_temporal(const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn, const GeoArgs& ga,
+                          const GeoArgs& prev_ga, const float4* diff_src, const float4* spec_src,
+                          const float* prev_depth, const float4* hist, const float* len_hist, const float4* fast_hist,
+                          float4* out, float* out_len, float4* out_fast, uint32_t has_history, cudaStream_t s) {
+  dim3 g = grid2d(w, h, kBlock);
+  if (ga.nd) {
+    GeoSurface geo = {ga.nd, ga.pr, ga.fz, w, h};
+    GeoSurface pgeo = {prev_ga.nd, prev_ga.pr, prev_ga.fz, w, h};
+    k_dn32_temporal<<<g, kBlock, 0, s>>>(fp, w, h, kn, geo, pgeo, ga.gbuf, diff_src, spec_src, prev_depth, hist,
+                                         len_hist, fast_hist, out, out_len, out_fast, has_history);
+  } else {
+    GeoRaw geo = {ga.depth, ga.gbuf, ga.inv_vp, w, h};
+    GeoRaw pgeo = {prev_ga.depth, prev_ga.gbuf, prev_ga.inv_vp, w, h};
+    k_dn32_temporal<<<g, kBlock, 0, s>>>(fp, w, h, kn, geo, pgeo, ga.gbuf, diff_src, spec_src, prev_depth, hist,
+                                         len_hist, fast_hist, out, out_len, out_fast, has_history);
+  }
+}
+
+void launch_dn32_fix(int w, int h, const GeoArgs& ga, const float* len, const float4* in, float4* out,
+                     cudaStream_t s) {
+  dim3 g = grid2d(w, h, kBlock);
+  VLT_GEO_DISPATCH(ga, k_dn32_fix<<<g, kBlock, 0, s>>>(w, h, geo, len, in, out));
+}
+
+void launch_dn32_fast_clamp(int w, int h, const float4* fast, float4* rec, cudaStream_t s) {
+  k_dn32_fast_clamp<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, fast, rec);
+}
+
+void launch_dn32_fallback(int w, int h, const GeoArgs& ga, const float* len, const float4* in, float4* out,
+                          cudaStream_t s) {
+  dim3 g = grid2d(w, h, kBlock);
+  VLT_GEO_DISPATCH(ga, k_dn32_fallback<<<g, kBlock, 0, s>>>(w, h, geo, len, in, out));
+}
+
+void launch_dn32_atrous(int w, int h, const GeoArgs& ga, const float4* in, float4* out, float4* out_diff,
+                        float4* out_spec, int step, cudaStream_t s) {
+  AtrousTaps32 taps;
+  int k = 0;
+  for (int oy = -2; oy <= 2; ++oy) {
+    if (oy == 0) continue;
+    for (int ox = -2; ox <= 2; ++ox) {
+      if (ox == 0) continue;
+      float fx = (float)(ox * step), fy = (float)(oy * step);
+      taps.dist[k++] = sqrtf(fx * fx + fy * fy);
+    }
+  }
+  dim3 g = grid2d(w, h, kBlock);
+  VLT_GEO_DISPATCH(ga, k_dn32_atrous<<<g, kBlock, 0, s>>>(w, h, geo, taps, in, out, out_diff, out_spec, step));
+}
+
+#undef VLT_GEO_DISPATCH
+
+}  // namespace vlt

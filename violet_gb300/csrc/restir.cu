@@ -30,19 +30,47 @@ __global__ void __launch_bounds__(128) k_surface(vlt_frame_params fp, int w, int
 
 // ---------------------------------------------------------------- AO gen
 
-// raytraced_ao_gen.hlsl:18-81. AO history is {ao, valid} in half2 (the x and a
-// channels of the reference's RGBA16F texture).
-template <class Geo>
+// AO history {ao, valid}: the x and a channels of the reference's RGBA16F texture
+// (half2 in the reference form, float2 in the f32 form); filtered AO: half / float.
+template <int FORM>
+struct AoStore;
+template <>
+struct AoStore<FORM_REF> {
+  using Hist = uint32_t;
+  using Filt = uint16_t;
+  static __device__ __forceinline__ f2 hist(const Hist* p, int x, int y, int w, int h) { return ld_half2(p, x, y, w, h); }
+  static __device__ __forceinline__ Hist pack(f2 v) { return pack_half2(v); }
+  static __device__ __forceinline__ float hist_x(const Hist* p, size_t i) { return f16tof32(p[i] & 0xFFFFu); }
+  static __device__ __forceinline__ Filt pack_filt(float v) { return (uint16_t)f32tof16(v); }
+};
+template <>
+struct AoStore<FORM_F32> {
+  using Hist = float2;
+  using Filt = float;
+  static __device__ __forceinline__ f2 hist(const Hist* p, int x, int y, int w, int h) {
+    if (!inb(x, y, w, h)) return mk2(0.0f, 0.0f);
+    float2 v = p[(size_t)y * w + x];
+    return mk2(v.x, v.y);
+  }
+  static __device__ __forceinline__ Hist pack(f2 v) { return make_float2(v.x, v.y); }
+  static __device__ __forceinline__ float hist_x(const Hist* p, size_t i) { return p[i].x; }
+  static __device__ __forceinline__ Filt pack_filt(float v) { return v; }
+};
+
+// raytraced_ao_gen.hlsl:18-81.
+template <class Geo, int FORM>
 __global__ void __launch_bounds__(128) k_ao_gen(vlt_frame_params fp, int w, int h, Geo geo,
                                                  const uint2* __restrict__ hit_pos_normal,
-                                                 const uint32_t* __restrict__ prev_ao, uint32_t* __restrict__ ao,
+                                                 const typename AoStore<FORM>::Hist* __restrict__ prev_ao,
+                                                 typename AoStore<FORM>::Hist* __restrict__ ao,
                                                  uint32_t has_new_sample, uint32_t has_prev_frame, float radius_ws) {
+  using S = AoStore<FORM>;
   int x = pix_x(), y = pix_y();
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float depth = geo.dep(i);
   if (depth == 0.0f) {
-    ao[i] = 0u;
+    ao[i] = S::pack(mk2(0.0f, 0.0f));
     return;
   }
   f3 position = geo.pos(x, y, i);
@@ -57,8 +85,8 @@ __global__ void __launch_bounds__(128) k_ao_gen(vlt_frame_params fp, int w, int 
   bool in_last = huv.x == saturate(huv.x) && huv.y == saturate(huv.y);
   if (in_last && has_prev_frame) {
     BilinearTaps t = bilinear_taps(huv, w, h);
-    f2 a = ld_half2(prev_ao, t.x0, t.y0, w, h), b = ld_half2(prev_ao, t.x1, t.y0, w, h);
-    f2 c = ld_half2(prev_ao, t.x0, t.y1, w, h), d = ld_half2(prev_ao, t.x1, t.y1, w, h);
+    f2 a = S::hist(prev_ao, t.x0, t.y0, w, h), b = S::hist(prev_ao, t.x1, t.y0, w, h);
+    f2 c = S::hist(prev_ao, t.x0, t.y1, w, h), d = S::hist(prev_ao, t.x1, t.y1, w, h);
     hx = bilerp(a.x, b.x, c.x, d.x, t.fx, t.fy);
     ha = bilerp(a.y, b.y, c.y, d.y, t.fx, t.fy);
   }
@@ -72,7 +100,7 @@ __global__ void __launch_bounds__(128) k_ao_gen(vlt_frame_params fp, int w, int 
   } else {
     hx = ha > 0.0f ? hx : 1.0f;
   }
-  ao[i] = pack_half2(mk2(hx, ha));
+  ao[i] = S::pack(mk2(hx, ha));
 }
 
 // ---------------------------------------------------------------- AO filter
@@ -81,17 +109,20 @@ __global__ void __launch_bounds__(128) k_ao_gen(vlt_frame_params fp, int w, int 
 // arithmetic as the shader computes them (so the left/top edge wraps to an
 // out-of-range coordinate, which reads as zero). Only the x channel is needed
 // downstream, so only it is filtered and stored.
+template <int FORM>
 __global__ void __launch_bounds__(128) k_ao_filter(int w, int h, const float* __restrict__ depth_buf,
-                                                    const uint32_t* __restrict__ ao, uint16_t* __restrict__ out) {
+                                                    const typename AoStore<FORM>::Hist* __restrict__ ao,
+                                                    typename AoStore<FORM>::Filt* __restrict__ out) {
+  using S = AoStore<FORM>;
   int x = pix_x(), y = pix_y();
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float depth = depth_buf[i];
   if (depth == 0.0f) {
-    out[i] = 0;
+    out[i] = S::pack_filt(0.0f);
     return;
   }
-  float center = f16tof32(ao[i] & 0xFFFFu);
+  float center = S::hist_x(ao, i);
   float col_med[3], col_min[3], col_max[3];
 #pragma unroll
   for (int dy = -1; dy <= 1; ++dy) {
@@ -107,7 +138,7 @@ __global__ void __launch_bounds__(128) k_ao_filter(int w, int h, const float* __
         row[dx + 1] = center;
         continue;
       }
-      row[dx + 1] = ok ? f16tof32(ao[(size_t)cy * w + cx] & 0xFFFFu) : 0.0f;
+      row[dx + 1] = ok ? S::hist_x(ao, (size_t)cy * w + cx) : 0.0f;
     }
     col_med[dy + 1] = fmin_(fmax_(row[0], row[1]), row[2]);
     col_min[dy + 1] = fmin_(fmin_(row[0], row[1]), row[2]);
@@ -118,10 +149,115 @@ __global__ void __launch_bounds__(128) k_ao_filter(int w, int h, const float* __
   float C = fmin_(fmax_(col_med[0], col_med[1]), col_med[2]);
   float med = fmin_(fmax_(C, A), B);
   float mn = fmin_(fmin_(col_min[0], col_min[1]), col_min[2]);
-  out[i] = (uint16_t)f32tof16(lerpf(med, mn, 0.5f));
+  out[i] = S::pack_filt(lerpf(med, mn, 0.5f));
 }
 
 // ------------------------------------------------------ diffuse temporal
+
+// Diffuse reservoir records. Reference form: uint4 {M8|W24, HitPosNormal.xy,
+// R11G11B10}. F32 form: {hit position, W}, {hit normal, asfloat(M)}, {radiance, 0}.
+struct DiffF32 {
+  float4 a, b, c;
+};
+template <int FORM>
+struct DiffStore;
+template <>
+struct DiffStore<FORM_REF> {
+  using Rec = uint4;
+  using Light = uint32_t;
+  static __device__ __forceinline__ Light light(f3 l) { return pack_r11g11b10(l); }
+  static __device__ __forceinline__ Light zero_light() { return 0u; }
+};
+template <>
+struct DiffStore<FORM_F32> {
+  using Rec = DiffF32;
+  using Light = float4;
+  static __device__ __forceinline__ Light light(f3 l) { return make_float4(l.x, l.y, l.z, 0.0f); }
+  static __device__ __forceinline__ Light zero_light() { return make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
+};
+
+__device__ __forceinline__ DiffF32 diff_f32(uint32_t M, float W, f3 pos, f3 nrm, f3 rad) {
+  DiffF32 r;
+  r.a = make_float4(pos.x, pos.y, pos.z, W);
+  r.b = make_float4(nrm.x, nrm.y, nrm.z, as_float(M));
+  r.c = make_float4(rad.x, rad.y, rad.z, 0.0f);
+  return r;
+}
+
+// ind_diff_temporal_resample.hlsl:49-200 in the f32 storage form: the sample is kept
+// decoded (the hit normal of an empty HitPosNormal decodes to (0,0,-1)).
+template <class Geo>
+__global__ void __launch_bounds__(128) k_diff_temporal_f32(vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo,
+                                                            const float* __restrict__ prev_depth,
+                                                            const uint2* __restrict__ new_hpn,
+                                                            const uint32_t* __restrict__ new_rad,
+                                                            const float* __restrict__ new_pdf,
+                                                            const DiffF32* __restrict__ prev_rsv,
+                                                            DiffF32* __restrict__ out, uint32_t frame_rand,
+                                                            uint32_t has_prev_frame, uint32_t has_new_sample) {
+  int x = pix_x(), y = pix_y();
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  f3 pos = geo.pos(x, y, i);
+  f4 hr = mul44(fp.prev_view_proj, mk4(pos.x, pos.y, pos.z, 1.0f));
+  f3 ndc = mk3(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3], hr.z / hr.w - 0.0f);
+  f2 uv = mk2(ndc.x * 0.5f + 0.5f, ndc.y * 0.5f + 0.5f);
+  bool in_view = fabs_(ndc.x) < 1.0f && fabs_(ndc.y) < 1.0f;
+  bool sample_prev = has_prev_frame && in_view;
+  if (sample_prev) {
+    float pd = sample_depth(prev_depth, uv, w, h);
+    if (fabs_(pd - ndc.z) > 0.001f) sample_prev = false;
+  }
+  const f3 empty_n = hpn_normal(0u);
+  uint32_t M = 0;
+  float W = 0.0f;
+  f3 hp = mk3(0.0f), hn = empty_n, rad = mk3(0.0f);
+  if (sample_prev) {
+    int px = (int)f2u_rz(uv.x * (float)w), py = (int)f2u_rz(uv.y * (float)h);
+    if (inb(px, py, w, h)) {
+      DiffF32 r = prev_rsv[(size_t)py * w + px];
+      M = as_uint(r.b.w);
+      W = r.a.w;
+      hp = mk3(r.a.x, r.a.y, r.a.z);
+      hn = mk3(r.b.x, r.b.y, r.b.z);
+      rad = mk3(r.c.x, r.c.y, r.c.z);
+    } else {
+      hn = empty_n;
+    }
+    if (M == 0) {
+      rad = mk3(0.0f);
+      hp = mk3(0.0f);
+      hn = empty_n;
+    }
+    M = M < kn.m_cap ? M : kn.m_cap;
+  }
+  if (has_new_sample) {
+    float tp = luminance(rad);
+    float prev_w = W * tp * (float)M;
+    f3 nrad = unpack_r11g11b10(new_rad[i]);
+    float ntp = luminance(nrad);
+    float new_w;
+    if (kn.use_input_pdf) {
+      float pdf = new_pdf[i];
+      new_w = pdf > 0.0f ? ntp / pdf : 0.0f;
+    } else {
+      new_w = ntp * VLT_TWO_PI;
+    }
+    uint32_t rng = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
+    float w_sum = prev_w + new_w;
+    float chance = new_w / w_sum;
+    if (lcg_rand(rng) < chance) {
+      uint2 e = new_hpn[i];
+      hp = hpn_pos(e.x, e.y);
+      hn = hpn_normal(e.y);
+      rad = nrad;
+      tp = ntp;
+    }
+    M += 1;
+    W = tp > 0.0f ? w_sum / (tp * (float)M) : 0.0f;
+  }
+  out[i] = diff_f32(M, W, hp, hn, rad);
+}
 
 // ind_diff_temporal_resample.hlsl:49-200. Record = {M8|W24, HitPosNormal.xy, R11G11B10}.
 template <class Geo>
@@ -211,25 +347,56 @@ __device__ __forceinline__ DiffSample load_diff(uint4 r, f3 pix_pos, f3 pix_n) {
   return s;
 }
 
+__device__ __forceinline__ DiffSample load_diff(const DiffF32& r, f3 pix_pos, f3 pix_n) {
+  DiffSample s;
+  s.M = as_uint(r.b.w);
+  s.W = r.a.w;
+  s.pos = mk3(r.a.x, r.a.y, r.a.z);
+  s.nrm = mk3(r.b.x, r.b.y, r.b.z);
+  s.rad = mk3(r.c.x, r.c.y, r.c.z);
+  float nol = saturate(dot3(pix_n, normalize3(s.pos - pix_pos)));
+  s.tp = nol * luminance(s.rad);
+  return s;
+}
+
+__device__ __forceinline__ float load_ao(const uint16_t* p, size_t i) { return f16tof32(p[i]); }
+__device__ __forceinline__ float load_ao(const float* p, size_t i) { return p[i]; }
+
+__device__ __forceinline__ void store_diff(uint4* out, size_t i, const DiffSample& r) {
+  uint32_t e[2];
+  hpn_encode(r.pos, r.nrm, e);
+  out[i] = make_uint4(rsv_encode_32b(r.M, r.W), e[0], e[1], pack_r11g11b10(r.rad));
+}
+__device__ __forceinline__ void store_diff(DiffF32* out, size_t i, const DiffSample& r) {
+  out[i] = diff_f32(r.M, r.W, r.pos, r.nrm, r.rad);
+}
+__device__ __forceinline__ void store_empty_diff(uint4* out, size_t i) { out[i] = make_uint4(0u, 0u, 0u, 0u); }
+__device__ __forceinline__ void store_empty_diff(DiffF32* out, size_t i) {
+  out[i] = diff_f32(0u, 0.0f, mk3(0.0f), hpn_normal(0u), mk3(0.0f));
+}
+
 // ind_diff_spatial_resample.hlsl:94-337 (golden-spiral pattern, AO-guided and
 // adaptive radius, plane-distance test, Jacobian clamped to [0, 1]).
-template <class Geo>
+template <class Geo, int FORM>
 __global__ void __launch_bounds__(128) k_diff_spatial(vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo,
-                                                       const uint16_t* __restrict__ ao_tex,
-                                                       const uint4* __restrict__ in, uint4* __restrict__ out,
-                                                       uint32_t* __restrict__ lighting, uint32_t frame_rand) {
+                                                       const typename AoStore<FORM>::Filt* __restrict__ ao_tex,
+                                                       const typename DiffStore<FORM>::Rec* __restrict__ in,
+                                                       typename DiffStore<FORM>::Rec* __restrict__ out,
+                                                       typename DiffStore<FORM>::Light* __restrict__ lighting,
+                                                       uint32_t frame_rand) {
+  using S = DiffStore<FORM>;
   int x = pix_x(), y = pix_y();
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float depth = geo.dep(i);
   if (depth == 0.0f) {
-    out[i] = make_uint4(0u, 0u, 0u, 0u);
-    if (lighting) lighting[i] = 0u;
+    store_empty_diff(out, i);
+    if (lighting) lighting[i] = S::zero_light();
     return;
   }
   f3 pos = geo.pos(x, y, i);
   f3 nrm = geo.normal(i);
-  float ao = f16tof32(ao_tex[i]);
+  float ao = load_ao(ao_tex, i);
   DiffSample r = load_diff(in[i], pos, nrm);
   float w_sum = r.W * r.tp * (float)r.M;
   float radius = kn.radius_px > 0.0f ? kn.radius_px : (float)(w < h ? w : h) * 0.05f;
@@ -282,14 +449,12 @@ __global__ void __launch_bounds__(128) k_diff_spatial(vlt_frame_params fp, int w
     r.M += nb.M;
   }
   if (r.tp > 0.0f) r.W = w_sum / (r.tp * (float)r.M);
-  uint32_t e[2];
-  hpn_encode(r.pos, r.nrm, e);
-  out[i] = make_uint4(rsv_encode_32b(r.M, r.W), e[0], e[1], pack_r11g11b10(r.rad));
+  store_diff(out, i, r);
   if (lighting) {
     f3 dir = normalize3(r.pos - pos);
     float nol = saturate(dot3(nrm, dir));
     f3 l = r.rad * (VLT_ONE_OVER_PI * nol * r.W);
-    lighting[i] = pack_r11g11b10(l);
+    lighting[i] = S::light(l);
   }
 }
 
@@ -484,12 +649,22 @@ __device__ __forceinline__ f3 ggx_integral(float nov, float roughness, f3 f0) {
 
 // ind_spec_spatial_resample.hlsl:169-448. Optionally also stores the merged
 // reservoir (for chaining several spatial passes; the reference runs one).
-template <class Geo>
+// Specular lighting output: R11G11B10 + a separate half ray length (reference
+// form), or float4 {rgb, ray length} (f32 form).
+__device__ __forceinline__ void store_spec_light(uint32_t* l, uint16_t* rl, size_t i, f3 v, float ray_len) {
+  if (l) l[i] = pack_r11g11b10(v);
+  if (rl) rl[i] = (uint16_t)f32tof16(ray_len);
+}
+__device__ __forceinline__ void store_spec_light(float4* l, uint16_t*, size_t i, f3 v, float ray_len) {
+  if (l) l[i] = make_float4(v.x, v.y, v.z, ray_len);
+}
+
+template <class Geo, class Light>
 __global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo,
                                                        const uint2* __restrict__ rsv,
                                                        const float4* __restrict__ hp_tex,
                                                        const uint32_t* __restrict__ rad_tex,
-                                                       uint32_t* __restrict__ lighting, uint16_t* __restrict__ ray_len_out,
+                                                       Light* __restrict__ lighting, uint16_t* __restrict__ ray_len_out,
                                                        uint2* __restrict__ out_rsv, float4* __restrict__ out_hp,
                                                        uint32_t* __restrict__ out_rad, uint32_t frame_rand) {
   int x = pix_x(), y = pix_y();
@@ -497,8 +672,7 @@ __global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w
   size_t i = (size_t)y * w + x;
   float depth = geo.dep(i);
   if (depth == 0.0f) {
-    if (lighting) lighting[i] = 0u;
-    if (ray_len_out) ray_len_out[i] = 0;
+    store_spec_light(lighting, ray_len_out, i, mk3(0.0f), 0.0f);
     if (out_rsv) {
       out_rsv[i] = make_uint2(0u, 0u);
       out_hp[i] = hp_tex[i];
@@ -599,74 +773,89 @@ __global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w
     f3 refl = ggx_integral(nov, roughness, center.f0);
     refl = mk3(fmax_(refl.x, 1.0f / 65536.0f), fmax_(refl.y, 1.0f / 65536.0f), fmax_(refl.z, 1.0f / 65536.0f));
     li = li / refl;
-    lighting[i] = pack_r11g11b10(li);
+    store_spec_light(lighting, ray_len_out, i, li, ray_len);
+  } else if (ray_len_out) {
+    ray_len_out[i] = (uint16_t)f32tof16(ray_len);
   }
-  if (ray_len_out) ray_len_out[i] = (uint16_t)f32tof16(ray_len);
 }
 
 // ------------------------------------------------------------- launchers
 
 static const dim3 kBlock(32, 4, 1);
 
-template <class Geo>
-static Geo make_geo(const GeoArgs& a, int w, int h);
-
-template <>
-GeoRaw make_geo<GeoRaw>(const GeoArgs& a, int w, int h) {
+static GeoRaw raw_geo(const GeoArgs& a, int w, int h) {
   GeoRaw g = {a.depth, a.gbuf, a.inv_vp, w, h};
   return g;
 }
-template <>
-GeoSurface make_geo<GeoSurface>(const GeoArgs& a, int w, int h) {
+static GeoSurface surf_geo(const GeoArgs& a, int w, int h) {
   GeoSurface g = {a.nd, a.pr, a.fz, w, h};
   return g;
 }
+
+// Instantiates KERNEL<Geo, ...> for the geometry source in `ga`.
+#define VLT_GEO_DISPATCH(ga, ...)              \
+  do {                                         \
+    if ((ga).nd) {                             \
+      GeoSurface geo = surf_geo(ga, w, h);     \
+      __VA_ARGS__;                             \
+    } else {                                   \
+      GeoRaw geo = raw_geo(ga, w, h);          \
+      __VA_ARGS__;                             \
+    }                                          \
+  } while (0)
 
 void launch_surface(const vlt_frame_params& fp, int w, int h, const float* depth, const uint32_t* gbuf, float4* nd,
                     float4* pr, float4* fz, cudaStream_t s) {
   k_surface<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, depth, gbuf, nd, pr, fz);
 }
 
-void launch_ao_gen(const vlt_frame_params& fp, int w, int h, const GeoArgs& ga, const uint32_t* hpn,
-                   const uint32_t* prev_ao, uint32_t* ao, uint32_t has_new, uint32_t has_prev, float radius,
-                   cudaStream_t s) {
-  if (ga.nd)
-    k_ao_gen<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, make_geo<GeoSurface>(ga, w, h), (const uint2*)hpn,
-                                                       prev_ao, ao, has_new, has_prev, radius);
+void launch_ao_gen(int form, const vlt_frame_params& fp, int w, int h, const GeoArgs& ga, const uint32_t* hpn,
+                   const void* prev_ao, void* ao, uint32_t has_new, uint32_t has_prev, float radius, cudaStream_t s) {
+  dim3 g = grid2d(w, h, kBlock);
+  if (form == FORM_F32)
+    VLT_GEO_DISPATCH(ga, (k_ao_gen<decltype(geo), FORM_F32><<<g, kBlock, 0, s>>>(
+                             fp, w, h, geo, (const uint2*)hpn, (const float2*)prev_ao, (float2*)ao, has_new, has_prev,
+                             radius)));
   else
-    k_ao_gen<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, make_geo<GeoRaw>(ga, w, h), (const uint2*)hpn,
-                                                       prev_ao, ao, has_new, has_prev, radius);
+    VLT_GEO_DISPATCH(ga, (k_ao_gen<decltype(geo), FORM_REF><<<g, kBlock, 0, s>>>(
+                             fp, w, h, geo, (const uint2*)hpn, (const uint32_t*)prev_ao, (uint32_t*)ao, has_new,
+                             has_prev, radius)));
 }
 
-void launch_ao_filter(int w, int h, const float* depth, const uint32_t* ao, uint16_t* out, cudaStream_t s) {
-  k_ao_filter<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, depth, ao, out);
+void launch_ao_filter(int form, int w, int h, const float* depth, const void* ao, void* out, cudaStream_t s) {
+  if (form == FORM_F32)
+    k_ao_filter<FORM_F32><<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, depth, (const float2*)ao, (float*)out);
+  else
+    k_ao_filter<FORM_REF><<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, depth, (const uint32_t*)ao, (uint16_t*)out);
 }
 
-void launch_diff_temporal(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
+void launch_diff_temporal(int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
                           const float* prev_depth, const uint32_t* new_hpn, const uint32_t* new_rad,
-                          const float* new_pdf, const uint32_t* prev_rsv, uint32_t* out, uint32_t frame_rand,
+                          const float* new_pdf, const void* prev_rsv, void* out, uint32_t frame_rand,
                           uint32_t has_prev, uint32_t has_new, cudaStream_t s) {
-  if (ga.nd)
-    k_diff_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, make_geo<GeoSurface>(ga, w, h), prev_depth,
-                                                              (const uint2*)new_hpn, new_rad, new_pdf,
-                                                              (const uint4*)prev_rsv, (uint4*)out, frame_rand,
-                                                              has_prev, has_new);
+  dim3 g = grid2d(w, h, kBlock);
+  if (form == FORM_F32)
+    VLT_GEO_DISPATCH(ga, (k_diff_temporal_f32<<<g, kBlock, 0, s>>>(
+                             fp, w, h, kn, geo, prev_depth, (const uint2*)new_hpn, new_rad, new_pdf,
+                             (const DiffF32*)prev_rsv, (DiffF32*)out, frame_rand, has_prev, has_new)));
   else
-    k_diff_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, make_geo<GeoRaw>(ga, w, h), prev_depth,
-                                                              (const uint2*)new_hpn, new_rad, new_pdf,
-                                                              (const uint4*)prev_rsv, (uint4*)out, frame_rand,
-                                                              has_prev, has_new);
+    VLT_GEO_DISPATCH(ga, (k_diff_temporal<<<g, kBlock, 0, s>>>(fp, w, h, kn, geo, prev_depth, (const uint2*)new_hpn,
+                                                                new_rad, new_pdf, (const uint4*)prev_rsv,
+                                                                (uint4*)out, frame_rand, has_prev, has_new)));
 }
 
-void launch_diff_spatial(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
-                         const uint16_t* ao, const uint32_t* in, uint32_t* out, uint32_t* lighting,
-                         uint32_t frame_rand, cudaStream_t s) {
-  if (ga.nd)
-    k_diff_spatial<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, make_geo<GeoSurface>(ga, w, h), ao,
-                                                             (const uint4*)in, (uint4*)out, lighting, frame_rand);
+void launch_diff_spatial(int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
+                         const void* ao, const void* in, void* out, void* lighting, uint32_t frame_rand,
+                         cudaStream_t s) {
+  dim3 g = grid2d(w, h, kBlock);
+  if (form == FORM_F32)
+    VLT_GEO_DISPATCH(ga, (k_diff_spatial<decltype(geo), FORM_F32><<<g, kBlock, 0, s>>>(
+                             fp, w, h, kn, geo, (const float*)ao, (const DiffF32*)in, (DiffF32*)out, (float4*)lighting,
+                             frame_rand)));
   else
-    k_diff_spatial<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, make_geo<GeoRaw>(ga, w, h), ao,
-                                                             (const uint4*)in, (uint4*)out, lighting, frame_rand);
+    VLT_GEO_DISPATCH(ga, (k_diff_spatial<decltype(geo), FORM_REF><<<g, kBlock, 0, s>>>(
+                             fp, w, h, kn, geo, (const uint16_t*)ao, (const uint4*)in, (uint4*)out,
+                             (uint32_t*)lighting, frame_rand)));
 }
 
 void launch_spec_temporal(const vlt_frame_params& fp, int w, int h, uint32_t m_cap, const GeoArgs& ga,
@@ -676,30 +865,32 @@ void launch_spec_temporal(const vlt_frame_params& fp, int w, int h, uint32_t m_c
                           uint32_t frame_rand, uint32_t has_prev, cudaStream_t s) {
   if (ga.nd)
     k_spec_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
-        fp, w, h, m_cap, make_geo<GeoSurface>(ga, w, h), make_geo<GeoSurface>(prev_ga, w, h), prev_depth,
-        (const uint2*)prev_rsv, (const float4*)prev_hp, prev_rad, (const float4*)new_hp, new_rad, (uint2*)out_rsv,
-        (float4*)out_hp, out_rad, frame_rand, has_prev);
+        fp, w, h, m_cap, surf_geo(ga, w, h), surf_geo(prev_ga, w, h), prev_depth, (const uint2*)prev_rsv,
+        (const float4*)prev_hp, prev_rad, (const float4*)new_hp, new_rad, (uint2*)out_rsv, (float4*)out_hp, out_rad,
+        frame_rand, has_prev);
   else
     k_spec_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
-        fp, w, h, m_cap, make_geo<GeoRaw>(ga, w, h), make_geo<GeoRaw>(prev_ga, w, h), prev_depth,
-        (const uint2*)prev_rsv, (const float4*)prev_hp, prev_rad, (const float4*)new_hp, new_rad, (uint2*)out_rsv,
-        (float4*)out_hp, out_rad, frame_rand, has_prev);
+        fp, w, h, m_cap, raw_geo(ga, w, h), raw_geo(prev_ga, w, h), prev_depth, (const uint2*)prev_rsv,
+        (const float4*)prev_hp, prev_rad, (const float4*)new_hp, new_rad, (uint2*)out_rsv, (float4*)out_hp, out_rad,
+        frame_rand, has_prev);
 }
 
-void launch_spec_spatial(const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn, const GeoArgs& ga,
-                         const uint32_t* rsv, const float* hp, const uint32_t* rad, uint32_t* lighting,
-                         uint16_t* ray_len, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad, uint32_t frame_rand,
-                         cudaStream_t s) {
-  if (ga.nd)
-    k_spec_spatial<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, make_geo<GeoSurface>(ga, w, h),
-                                                             (const uint2*)rsv, (const float4*)hp, rad, lighting,
-                                                             ray_len, (uint2*)out_rsv, (float4*)out_hp, out_rad,
-                                                             frame_rand);
+void launch_spec_spatial(int form, const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn, const GeoArgs& ga,
+                         const uint32_t* rsv, const float* hp, const uint32_t* rad, void* lighting, uint16_t* ray_len,
+                         uint32_t* out_rsv, float* out_hp, uint32_t* out_rad, uint32_t frame_rand, cudaStream_t s) {
+  dim3 g = grid2d(w, h, kBlock);
+  if (form == FORM_F32)
+    VLT_GEO_DISPATCH(ga, (k_spec_spatial<<<g, kBlock, 0, s>>>(fp, w, h, kn, geo, (const uint2*)rsv,
+                                                               (const float4*)hp, rad, (float4*)lighting, nullptr,
+                                                               (uint2*)out_rsv, (float4*)out_hp, out_rad,
+                                                               frame_rand)));
   else
-    k_spec_spatial<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, kn, make_geo<GeoRaw>(ga, w, h),
-                                                             (const uint2*)rsv, (const float4*)hp, rad, lighting,
-                                                             ray_len, (uint2*)out_rsv, (float4*)out_hp, out_rad,
-                                                             frame_rand);
+    VLT_GEO_DISPATCH(ga, (k_spec_spatial<<<g, kBlock, 0, s>>>(fp, w, h, kn, geo, (const uint2*)rsv,
+                                                               (const float4*)hp, rad, (uint32_t*)lighting, ray_len,
+                                                               (uint2*)out_rsv, (float4*)out_hp, out_rad,
+                                                               frame_rand)));
 }
+
+#undef VLT_GEO_DISPATCH
 
 }  // namespace vlt

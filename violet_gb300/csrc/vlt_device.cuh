@@ -23,6 +23,9 @@ namespace vlt {
 #define VLT_SPIRAL_B 0.3063489496707916f  // 0x3e9cd9c5
 #define VLT_SPIRAL_A 0.14589804410934448f  // 0x3e15664c
 
+// Storage forms (vlt_form).
+enum { FORM_REF = 0, FORM_F32 = 1, FORM_F16 = 2 };
+
 __device__ __forceinline__ int pix_x() { return (int)(blockIdx.x * blockDim.x + threadIdx.x); }
 __device__ __forceinline__ int pix_y() { return (int)(blockIdx.y * blockDim.y + threadIdx.y); }
 

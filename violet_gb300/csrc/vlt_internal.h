@@ -41,26 +41,42 @@ struct GeoArgs {
 // restir.cu
 void launch_surface(const vlt_frame_params& fp, int w, int h, const float* depth, const uint32_t* gbuf, float4* nd,
                     float4* pr, float4* fz, cudaStream_t s);
-void launch_ao_gen(const vlt_frame_params& fp, int w, int h, const GeoArgs& ga, const uint32_t* hpn,
-                   const uint32_t* prev_ao, uint32_t* ao, uint32_t has_new, uint32_t has_prev, float radius,
-                   cudaStream_t s);
-void launch_ao_filter(int w, int h, const float* depth, const uint32_t* ao, uint16_t* out, cudaStream_t s);
-void launch_diff_temporal(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
+// Form-dependent buffers are void*: reference form uses the R11G11B10/half/M8W24
+// records of include/vlt.h; f32 form uses float2 AO history, float filtered AO,
+// 48-byte diffuse records {pos,W}{normal,M}{rad,0}, float4 lighting.
+void launch_ao_gen(int form, const vlt_frame_params& fp, int w, int h, const GeoArgs& ga, const uint32_t* hpn,
+                   const void* prev_ao, void* ao, uint32_t has_new, uint32_t has_prev, float radius, cudaStream_t s);
+void launch_ao_filter(int form, int w, int h, const float* depth, const void* ao, void* out, cudaStream_t s);
+void launch_diff_temporal(int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
                           const float* prev_depth, const uint32_t* new_hpn, const uint32_t* new_rad,
-                          const float* new_pdf, const uint32_t* prev_rsv, uint32_t* out, uint32_t frame_rand,
+                          const float* new_pdf, const void* prev_rsv, void* out, uint32_t frame_rand,
                           uint32_t has_prev, uint32_t has_new, cudaStream_t s);
-void launch_diff_spatial(const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
-                         const uint16_t* ao, const uint32_t* in, uint32_t* out, uint32_t* lighting,
-                         uint32_t frame_rand, cudaStream_t s);
+void launch_diff_spatial(int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
+                         const void* ao, const void* in, void* out, void* lighting, uint32_t frame_rand,
+                         cudaStream_t s);
 void launch_spec_temporal(const vlt_frame_params& fp, int w, int h, uint32_t m_cap, const GeoArgs& ga,
                           const GeoArgs& prev_ga, const float* prev_depth, const uint32_t* prev_rsv,
                           const float* prev_hp, const uint32_t* prev_rad, const float* new_hp,
                           const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
                           uint32_t frame_rand, uint32_t has_prev, cudaStream_t s);
-void launch_spec_spatial(const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn, const GeoArgs& ga,
-                         const uint32_t* rsv, const float* hp, const uint32_t* rad, uint32_t* lighting,
-                         uint16_t* ray_len, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad, uint32_t frame_rand,
-                         cudaStream_t s);
+void launch_spec_spatial(int form, const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn, const GeoArgs& ga,
+                         const uint32_t* rsv, const float* hp, const uint32_t* rad, void* lighting, uint16_t* ray_len,
+                         uint32_t* out_rsv, float* out_hp, uint32_t* out_rad, uint32_t frame_rand, cudaStream_t s);
+
+// denoise_f32.cu — the f32 storage form of the denoiser. Records: DnRec
+// {float4 diffuse.rgb|aux.x, float4 specular.rgb|aux.y} with aux = moments (temporal /
+// fix outputs, history) or variance (fallback / a-trous); history length float.
+void launch_dn32_temporal(const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn, const GeoArgs& ga,
+                          const GeoArgs& prev_ga, const float4* diff_src, const float4* spec_src,
+                          const float* prev_depth, const float4* hist, const float* len_hist, const float4* fast_hist,
+                          float4* out, float* out_len, float4* out_fast, uint32_t has_history, cudaStream_t s);
+void launch_dn32_fix(int w, int h, const GeoArgs& ga, const float* len, const float4* in, float4* out,
+                     cudaStream_t s);
+void launch_dn32_fast_clamp(int w, int h, const float4* fast, float4* rec, cudaStream_t s);
+void launch_dn32_fallback(int w, int h, const GeoArgs& ga, const float* len, const float4* in, float4* out,
+                          cudaStream_t s);
+void launch_dn32_atrous(int w, int h, const GeoArgs& ga, const float4* in, float4* out, float4* out_diff,
+                        float4* out_spec, int step, cudaStream_t s);
 
 // denoise.cu
 void launch_dn_temporal(const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn, const GeoArgs& ga,
