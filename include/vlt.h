@@ -170,6 +170,48 @@ vlt_status vlt_frame_run(vlt_view* view, const vlt_frame_inputs* in, const vlt_f
 /* Number of kernel launches the last vlt_frame_run issued. */
 uint32_t vlt_view_last_launch_count(const vlt_view* view);
 
+/* ------------------------------------------------------------ batched frames
+ *
+ * No counterpart in the reference (one RestirRenderer per view there). A batch
+ * runs one frame of each of n views (any sizes, forms and parameters) as one
+ * stream of launches: each pass that several views run next becomes a single
+ * persistent kernel over the concatenated tile lists of those views. Every view's
+ * results are identical to what vlt_frame_run gives it alone. The step (one
+ * host-to-device copy of all launch arguments, then the kernels) is captured in a
+ * CUDA graph and replayed while the sequence of batched launches repeats. */
+typedef struct vlt_batch vlt_batch;
+vlt_status vlt_batch_create(vlt_ctx* ctx, vlt_batch** out);
+vlt_status vlt_batch_destroy(vlt_batch* batch);
+/* views[k] runs with inputs[k] and outputs[k] (outputs may be NULL: no outputs for
+ * any view). A view may appear once per call. All views belong to the batch's
+ * context. Inputs are validated for every view before any view's state changes. */
+vlt_status vlt_batch_run(vlt_batch* batch, vlt_view* const* views, const vlt_frame_inputs* inputs,
+                         const vlt_frame_outputs* outputs, uint32_t n, void* stream);
+/* CUDA-graph capture and replay of the batch step (default on). */
+vlt_status vlt_batch_set_graphs(vlt_batch* batch, int enable);
+/* Tile-shape autotuner: the next 2 x VLT_TILE_CANDIDATES frames each run every 2D
+ * pass with one candidate tile shape (results do not depend on it), timing every
+ * batched launch; then each pass keeps the shape with the least time per pixel. */
+#define VLT_TILE_CANDIDATES 5
+vlt_status vlt_batch_autotune(vlt_batch* batch);
+typedef struct vlt_tile_choice {
+  char pass[32];
+  uint16_t bx, by;        /* chosen block (tile) shape */
+  float ns_per_kpix[VLT_TILE_CANDIDATES]; /* measured per candidate, 0 if not run */
+} vlt_tile_choice;
+/* Writes up to max entries (one per 2D pass seen by the tuner); returns the count. */
+uint32_t vlt_batch_tile_table(const vlt_batch* batch, vlt_tile_choice* out, uint32_t max);
+typedef struct vlt_batch_stats {
+  uint64_t frames;          /* vlt_batch_run calls */
+  uint64_t launches;        /* batched kernel launches issued (replays count) */
+  uint64_t graph_replays;   /* steps replayed from a cached graph */
+  uint64_t graph_captures;  /* steps captured into a new graph */
+  uint64_t arena_bytes;     /* launch-argument bytes of the last step */
+  uint32_t last_launches;   /* batched launches of the last step */
+  uint32_t last_jobs;       /* per-view passes of the last step */
+} vlt_batch_stats;
+vlt_status vlt_batch_get_stats(const vlt_batch* batch, vlt_batch_stats* out);
+
 /* Per-pass GPU timers (the counterpart of the render graph's per-pass timestamp
  * queries, render_graph.rs:2321-2326, and NamedProfiling, gpu_profiling.rs:221-340).
  * When enabled, vlt_frame_run brackets every kernel with CUDA events on its stream.

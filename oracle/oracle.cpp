@@ -1353,6 +1353,18 @@ struct EdgeStop32 {
     }
     return F2(wn * exp_fma(ax), wn * exp_fma(ay));
   }
+  // The a-trous form: depth term -dist_z * r_z with r_z = 1 / (fz_sigma * d + 1e-8)
+  // computed once per distinct tap distance d, luminance term always on.
+  float2 weight_rz(float r_z, float depth, float3 normal, float2 lumi) const {
+    float wz = -fabsf(depth - depth_center) * r_z;
+    float n_dot = saturate(fma_(normal_center.z, normal.z, fma_(normal_center.y, normal.y,
+                                                                  normal_center.x * normal.x)));
+    float wn = n_dot;
+    for (int k = 0; k < n_log2; ++k) wn = wn * wn;
+    float ax = fma_(-fabsf(lumi.x - lumi_center.x), lumi_rcp.x, wz);
+    float ay = fma_(-fabsf(lumi.y - lumi_center.y), lumi_rcp.y, wz);
+    return F2(wn * exp_fma(ax), wn * exp_fma(ay));
+  }
 };
 
 struct Rec32 {
@@ -1665,6 +1677,13 @@ void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, con
       es.use_lumi = true;
       es.lumi_center = F2(lum_fma(c.d), lum_fma(c.s));
       es.lumi_rcp = F2(1.0f / fma_(4.0f, sqrtf(c.aux.x), 1e-8f), 1.0f / fma_(4.0f, sqrtf(c.aux.y), 1e-8f));
+      // r_z per |offset| class (1,1), (1,2)/(2,1), (2,2).
+      float rz[3][3];
+      for (int ay = 1; ay <= 2; ++ay)
+        for (int ax = 1; ax <= 2; ++ax) {
+          float fx = (float)(ax * step), fy = (float)(ay * step);
+          rz[ay][ax] = 1.0f / fma_(es.fz_sigma, sqrtf(fx * fx + fy * fy), 1e-8f);
+        }
       float3 dsum = c.d, ssum = c.s;
       float2 vsum = c.aux, wsum = F2(1.0f, 1.0f);
       for (int oy = -2; oy <= 2; oy++) {
@@ -1678,8 +1697,8 @@ void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, con
           const float kw = kwy * kernel_weights[std::abs(ox)];
           size_t j = (size_t)uy * w + ux;
           Rec32 r = rec_load(in, j);
-          float2 e = es.weight(length(F2((float)cx, (float)cy)), depth_tex[j],
-                               load_gbuffer_normal(gbuf, ux, uy, w, h), F2(lum_fma(r.d), lum_fma(r.s)));
+          float2 e = es.weight_rz(rz[std::abs(oy)][std::abs(ox)], depth_tex[j],
+                                  load_gbuffer_normal(gbuf, ux, uy, w, h), F2(lum_fma(r.d), lum_fma(r.s)));
           float2 wt = F2(kw * e.x, kw * e.y);
           dsum = fma3(wt.x, r.d, dsum);
           ssum = fma3(wt.y, r.s, ssum);

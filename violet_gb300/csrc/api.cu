@@ -215,6 +215,12 @@ bool params_ok(const vlt_params* p) {
   return true;
 }
 
+Exec stream_exec(void* stream) {
+  Exec e;
+  e.stream = (cudaStream_t)stream;
+  return e;
+}
+
 DiffKnobs diff_knobs(const vlt_params& p) {
   DiffKnobs k;
   k.m_cap = p.diff_m_cap;
@@ -245,6 +251,28 @@ vlt_status reset_state(vlt_view* v, cudaStream_t s) {
 }
 
 }  // namespace
+
+static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out,
+                                 cudaStream_t s, Recorder* rec);
+
+namespace vlt {
+
+bool frame_inputs_ok(const vlt_view* v, const vlt_frame_inputs* in) {
+  if (!v || !in || !in->params || !in->depth || !in->gbuffer || !in->diff_hit_pos_normal ||
+      !in->diff_hit_radiance || !in->spec_hit_pos || !in->spec_hit_radiance)
+    return false;
+  if (v->p.use_input_pdf && !in->diff_source_pdf) return false;
+  return true;
+}
+
+vlt_status record_frame(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out, Recorder* rec) {
+  return frame_run_impl(v, in, out, 0, rec);
+}
+
+int view_device(const vlt_view* v) { return v->ctx->device; }
+int ctx_device(const vlt_ctx* c) { return c->device; }
+
+}  // namespace vlt
 
 extern "C" {
 
@@ -489,12 +517,14 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
   return nullptr;
 }
 
-vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out, void* stream) {
-  if (!v || !in || !in->params || !in->depth || !in->gbuffer || !in->diff_hit_pos_normal ||
-      !in->diff_hit_radiance || !in->spec_hit_pos || !in->spec_hit_radiance)
-    return VLT_ERR_INVALID_ARG;
-  if (v->p.use_input_pdf && !in->diff_source_pdf) return VLT_ERR_INVALID_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
+}  // extern "C"
+
+static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out,
+                                 cudaStream_t s, Recorder* rec) {
+  if (!vlt::frame_inputs_ok(v, in)) return VLT_ERR_INVALID_ARG;
+  Exec ex;
+  ex.stream = s;
+  ex.rec = rec;
   const vlt_frame_params& fp = *in->params;
   const int w = (int)v->w, h = (int)v->h;
   const size_t n = (size_t)w * h;
@@ -510,16 +540,16 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
 #define STAGE(NAME, CALL)                                        \
   do {                                                           \
     size_t e0_ = 0;                                              \
-    if (tm.enabled) {                                            \
+    if (tm.enabled && !rec) {                                    \
       e0_ = tm.used;                                             \
       cudaEvent_t ev = tm.next();                                \
-      if (ev) cudaEventRecord(ev, s);                            \
+      if (ev) cudaEventRecord(ev, s);                         \
     }                                                            \
     CALL;                                                        \
-    if (tm.enabled && tm.used == e0_ + 1) {                      \
+    if (tm.enabled && !rec && tm.used == e0_ + 1) {              \
       cudaEvent_t ev = tm.next();                                \
       if (ev) {                                                  \
-        cudaEventRecord(ev, s);                                  \
+        cudaEventRecord(ev, s);                               \
         tm.pending.push_back(Timing::Rec{NAME, e0_, e0_ + 1});   \
       }                                                          \
     }                                                            \
@@ -531,14 +561,14 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
   GeoArgs ga = {in->depth, in->gbuffer, fp.inv_view_proj, b.surf[sc][0], b.surf[sc][1], b.surf[sc][2]};
   GeoArgs pga = {prev_depth, nullptr, fp.prev_inv_view_proj, b.surf[sc ^ 1][0], b.surf[sc ^ 1][1],
                  b.surf[sc ^ 1][2]};
-  STAGE("surface", launch_surface(fp, w, h, in->depth, in->gbuffer, b.surf[sc][0], b.surf[sc][1], b.surf[sc][2], s));
+  STAGE("surface", launch_surface(ex, fp, w, h, in->depth, in->gbuffer, b.surf[sc][0], b.surf[sc][1], b.surf[sc][2]));
   ++launches;
 
   // Hash-grid radiance cache: decay, then (with history) select/compact/update of
   // last frame's queries, then this frame's queries.
   if (P.hg_enable) {
     if (P.hg_decay) {
-      STAGE("hg_decay", launch_hg_decay(v->hg, b.hg_decay, b.hg_storage, s));
+      STAGE("hg_decay", launch_hg_decay(ex, v->hg, b.hg_decay, b.hg_storage));
       ++launches;
     }
   }
@@ -547,20 +577,20 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
     uint32_t seed_update = fr.next();
     (void)seed_update;  // consumed by the (out-of-scope) cache ray generation
     if (P.hg_enable) {
-      VLT_TRY(cudaMemsetAsync(b.hg_sel, 0, (size_t)v->hg.num_cells() * 4, s));
-      VLT_TRY(cudaMemsetAsync(b.hg_ccount, 0, 4, s));
-      STAGE("hg_select", launch_hg_select(v->hg, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], b.hg_storage,
-                                          b.hg_sel, seed_select, b.hg_scratch, s));
-      STAGE("hg_compact", launch_hg_compact(v->hg, b.hg_sel, b.hg_cidx, b.hg_caddr, b.hg_ccount, s));
-      STAGE("hg_update", launch_hg_update(v->hg, b.hg_queries[v->hg_qcur], b.hg_cidx, b.hg_caddr, b.hg_ccount,
-                                          b.hg_storage, b.hg_decay, s));
+      ex_fill32(ex, b.hg_sel, 0u, (size_t)v->hg.num_cells() * 4);
+      ex_fill32(ex, b.hg_ccount, 0u, 4);
+      STAGE("hg_select", launch_hg_select(ex, v->hg, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], b.hg_storage,
+                                          b.hg_sel, seed_select, b.hg_scratch));
+      STAGE("hg_compact", launch_hg_compact(ex, v->hg, b.hg_sel, b.hg_cidx, b.hg_caddr, b.hg_ccount));
+      STAGE("hg_update", launch_hg_update(ex, v->hg, b.hg_queries[v->hg_qcur], b.hg_cidx, b.hg_caddr, b.hg_ccount,
+                                          b.hg_storage, b.hg_decay));
       launches += 6;
       v->hg_qcur ^= 1;
     }
   }
   if (P.hg_enable) {
-    STAGE("hg_emit", launch_hg_emit(fp, w, h, v->hg, P.hg_key_mode, in->depth, in->diff_hit_pos_normal,
-                                    in->diff_hit_radiance, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], s));
+    STAGE("hg_emit", launch_hg_emit(ex, fp, w, h, v->hg, P.hg_key_mode, in->depth, in->diff_hit_pos_normal,
+                                    in->diff_hit_radiance, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur]));
     ++launches;
   }
   (void)fr.next();  // Ind. Diff. Sample Gen.
@@ -570,9 +600,9 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
   const bool f32 = form == FORM_F32;
   const size_t light_bytes = (f32 ? 16 : 4) * n;
   int ao_cur = v->ao_prev ^ 1;
-  STAGE("ao_gen", launch_ao_gen(form, fp, w, h, ga, in->diff_hit_pos_normal, b.ao[v->ao_prev], b.ao[ao_cur], 1u,
-                                has_prev ? 1u : 0u, P.ao_radius, s));
-  STAGE("ao_filter", launch_ao_filter(form, w, h, in->depth, b.ao[ao_cur], b.ao_filtered, s));
+  STAGE("ao_gen", launch_ao_gen(ex, form, fp, w, h, ga, in->diff_hit_pos_normal, b.ao[v->ao_prev], b.ao[ao_cur], 1u,
+                                has_prev ? 1u : 0u, P.ao_radius));
+  STAGE("ao_filter", launch_ao_filter(ex, form, w, h, in->depth, b.ao[ao_cur], b.ao_filtered));
   launches += 2;
   v->ao_prev = ao_cur;
 
@@ -580,16 +610,16 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
   DiffKnobs dk = diff_knobs(P);
   int p = v->diff_prev, t = (p + 1) % 3, o = (p + 2) % 3;
   uint32_t seed_dt = fr.next();
-  STAGE("diff_temporal", launch_diff_temporal(form, fp, w, h, dk, ga, prev_depth, in->diff_hit_pos_normal,
+  STAGE("diff_temporal", launch_diff_temporal(ex, form, fp, w, h, dk, ga, prev_depth, in->diff_hit_pos_normal,
                                               in->diff_hit_radiance, in->diff_source_pdf, b.diff_rsv[p],
-                                              b.diff_rsv[t], seed_dt, has_prev ? 1u : 0u, 1u, s));
+                                              b.diff_rsv[t], seed_dt, has_prev ? 1u : 0u, 1u));
   ++launches;
   int src = t, dst = o;
   for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
     bool last = k + 1 == P.diff_spatial_passes;
     uint32_t seed_ds = fr.next();
-    STAGE("diff_spatial", launch_diff_spatial(form, fp, w, h, dk, ga, b.ao_filtered, b.diff_rsv[src],
-                                              b.diff_rsv[dst], last ? b.diff_light : nullptr, seed_ds, s));
+    STAGE("diff_spatial", launch_diff_spatial(ex, form, fp, w, h, dk, ga, b.ao_filtered, b.diff_rsv[src],
+                                              b.diff_rsv[dst], last ? b.diff_light : nullptr, seed_ds));
     ++launches;
     std::swap(src, dst);
   }
@@ -599,10 +629,10 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
   (void)fr.next();  // Ind. Spec. Sample Gen.
   int sp = v->spec_prev, st = (sp + 1) % 3, so = (sp + 2) % 3;
   uint32_t seed_st = fr.next();
-  STAGE("spec_temporal", launch_spec_temporal(fp, w, h, P.spec_m_cap, ga, pga, prev_depth, b.spec_rsv[sp],
+  STAGE("spec_temporal", launch_spec_temporal(ex, fp, w, h, P.spec_m_cap, ga, pga, prev_depth, b.spec_rsv[sp],
                                               b.spec_hp[sp], b.spec_rad[sp], in->spec_hit_pos, in->spec_hit_radiance,
                                               b.spec_rsv[st], b.spec_hp[st], b.spec_rad[st], seed_st,
-                                              has_prev ? 1u : 0u, s));
+                                              has_prev ? 1u : 0u));
   ++launches;
   {
     SpecKnobs sk = {P.spec_spatial_taps, P.spec_spatial_radius_px};
@@ -611,10 +641,10 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
       bool last = k + 1 == P.spec_spatial_passes;
       uint32_t seed_ss = fr.next();
       STAGE("spec_spatial",
-            launch_spec_spatial(form, fp, w, h, sk, ga, b.spec_rsv[ssrc], b.spec_hp[ssrc], b.spec_rad[ssrc],
+            launch_spec_spatial(ex, form, fp, w, h, sk, ga, b.spec_rsv[ssrc], b.spec_hp[ssrc], b.spec_rad[ssrc],
                                 last ? b.spec_light : nullptr, last ? b.ray_len : nullptr,
                                 last ? nullptr : b.spec_rsv[sdst], last ? nullptr : b.spec_hp[sdst],
-                                last ? nullptr : b.spec_rad[sdst], seed_ss, s));
+                                last ? nullptr : b.spec_rad[sdst], seed_ss));
       ++launches;
       std::swap(ssrc, sdst);
     }
@@ -628,19 +658,19 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
     DenoiseKnobs kn = {1.0f / P.history_max_frames, P.fast_history_clamp};
     uint32_t has_history = v->denoise_history ? 1u : 0u;
     // rec[0]/len[0] = history; rec[2]/len[1] = temporal output; rec[1] = fix output.
-    STAGE("dn_temporal", launch_dn32_temporal(fp, w, h, kn, ga, pga, (const float4*)b.diff_light,
+    STAGE("dn_temporal", launch_dn32_temporal(ex, fp, w, h, kn, ga, pga, (const float4*)b.diff_light,
                                               (const float4*)b.spec_light, prev_depth, b.rec[0],
                                               (const float*)b.len[0], b.rec_fast[0], b.rec[2], (float*)b.len[1],
-                                              b.rec_fast[1], has_history, s));
+                                              b.rec_fast[1], has_history));
     ++launches;
     float4* cur = b.rec[2];
     if (P.disocclusion_fix) {
-      STAGE("dn_fix", launch_dn32_fix(w, h, ga, (const float*)b.len[1], b.rec[2], b.rec[1], s));
+      STAGE("dn_fix", launch_dn32_fix(ex, w, h, ga, (const float*)b.len[1], b.rec[2], b.rec[1]));
       ++launches;
       cur = b.rec[1];
     }
     if (P.fast_history_clamp) {
-      STAGE("dn_fast_clamp", launch_dn32_fast_clamp(w, h, b.rec_fast[1], cur, s));
+      STAGE("dn_fast_clamp", launch_dn32_fast_clamp(ex, w, h, b.rec_fast[1], cur));
       ++launches;
       std::swap(b.rec_fast[0], b.rec_fast[1]);
       v->fast_history_valid = true;
@@ -654,7 +684,7 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
       std::swap(b.rec[0], b.rec[2]);
     std::swap(b.len[0], b.len[1]);
     v->denoise_history = true;
-    STAGE("dn_fallback", launch_dn32_fallback(w, h, ga, (const float*)b.len[0], b.rec[0], b.rec[4], s));
+    STAGE("dn_fallback", launch_dn32_fallback(ex, w, h, ga, (const float*)b.len[0], b.rec[0], b.rec[4]));
     ++launches;
     float4* rsrc = b.rec[4];
     float4* rdst = b.rec[2];
@@ -663,7 +693,7 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
       bool last = k + 1 == iters;
       float4* od = last && out ? (float4*)out->diffuse : nullptr;
       float4* os = last && out ? (float4*)out->specular : nullptr;
-      STAGE("dn_atrous", launch_dn32_atrous(w, h, ga, rsrc, rdst, od, os, 1 << k, s));
+      STAGE("dn_atrous", launch_dn32_atrous(ex, w, h, ga, rsrc, rdst, od, os, 1 << k));
       ++launches;
       rsrc = rdst;
       rdst = rdst == b.rec[2] ? b.rec[3] : b.rec[2];
@@ -671,29 +701,28 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
     if (iters == 0 && out && (out->diffuse || out->specular)) {
       // Zero iterations: the fallback output is the result (copy its colours out).
       if (out->diffuse)
-        VLT_TRY(cudaMemcpy2DAsync(out->diffuse, 16, b.rec[4], 32, 16, n, cudaMemcpyDeviceToDevice, s));
+        ex_copy_rows16(ex, out->diffuse, 16, b.rec[4], 32, n);
       if (out->specular)
-        VLT_TRY(cudaMemcpy2DAsync(out->specular, 16, (char*)b.rec[4] + 16, 32, 16, n, cudaMemcpyDeviceToDevice, s));
+        ex_copy_rows16(ex, out->specular, 16, (char*)b.rec[4] + 16, 32, n);
     }
   } else if (run_denoiser) {
     DenoiseKnobs kn = {1.0f / P.history_max_frames, P.fast_history_clamp};
     uint32_t has_history = v->denoise_history ? 1u : 0u;
     // color[0]/mom[0]/len[0] = history; color[2]/mom[2]/len[1] = temporal output;
     // color[1]/mom[1] = fix output.
-    STAGE("dn_temporal", launch_dn_temporal(fp, w, h, kn, ga, pga, (const uint32_t*)b.diff_light,
+    STAGE("dn_temporal", launch_dn_temporal(ex, fp, w, h, kn, ga, pga, (const uint32_t*)b.diff_light,
                                             (const uint32_t*)b.spec_light, b.ray_len, prev_depth, b.color[0],
                                             b.mom[0], (const uint8_t*)b.len[0], b.fast[0], b.color[2], b.mom[2],
-                                            (uint8_t*)b.len[1], b.fast[1], has_history, s));
+                                            (uint8_t*)b.len[1], b.fast[1], has_history));
     ++launches;
     uint32_t* cur_color = b.color[2];
     if (P.disocclusion_fix) {
-      STAGE("dn_fix", launch_dn_fix(w, h, ga, (const uint8_t*)b.len[1], b.color[2], b.mom[2], b.color[1], b.mom[1],
-                                    s));
+      STAGE("dn_fix", launch_dn_fix(ex, w, h, ga, (const uint8_t*)b.len[1], b.color[2], b.mom[2], b.color[1], b.mom[1]));
       ++launches;
       cur_color = b.color[1];
     }
     if (P.fast_history_clamp) {
-      STAGE("dn_fast_clamp", launch_dn_fast_clamp(w, h, b.fast[1], cur_color, s));
+      STAGE("dn_fast_clamp", launch_dn_fast_clamp(ex, w, h, b.fast[1], cur_color));
       ++launches;
       std::swap(b.fast[0], b.fast[1]);
       v->fast_history_valid = true;
@@ -711,8 +740,8 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
     std::swap(b.len[0], b.len[1]);
     v->denoise_history = true;
     // Now color[0]/mom[0]/len[0] hold this frame's history.
-    STAGE("dn_fallback", launch_dn_fallback(w, h, ga, (const uint8_t*)b.len[0], b.color[0], b.mom[0], b.color_c,
-                                            b.var[0], s));
+    STAGE("dn_fallback", launch_dn_fallback(ex, w, h, ga, (const uint8_t*)b.len[0], b.color[0], b.mom[0], b.color_c,
+                                            b.var[0]));
     ++launches;
     uint32_t* csrc = b.color_c;
     uint32_t* vsrc = b.var[0];
@@ -723,7 +752,7 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
       bool last = k + 1 == iters;
       uint32_t* od = last && out ? (uint32_t*)out->diffuse : nullptr;
       uint32_t* os = last && out ? (uint32_t*)out->specular : nullptr;
-      STAGE("dn_atrous", launch_dn_atrous(w, h, ga, csrc, vsrc, cdst, vdst, od, os, 1 << k, s));
+      STAGE("dn_atrous", launch_dn_atrous(ex, w, h, ga, csrc, vsrc, cdst, vdst, od, os, 1 << k));
       ++launches;
       std::swap(csrc, cdst);
       uint32_t* vnext = vdst == b.var[1] ? b.var[2] : b.var[1];
@@ -731,30 +760,36 @@ vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_fram
       vdst = vnext;
     }
     if (iters == 0 && out && (out->diffuse || out->specular)) {
-      launch_split_color(w, h, csrc, (uint32_t*)out->diffuse, (uint32_t*)out->specular, s);
+      launch_split_color(ex, w, h, csrc, (uint32_t*)out->diffuse, (uint32_t*)out->specular);
       ++launches;
     }
   } else {
     v->denoise_history = false;  // Denoiser::reset
     v->fast_history_valid = false;
     if (out && out->diffuse)
-      VLT_TRY(cudaMemcpyAsync(out->diffuse, b.diff_light, light_bytes, cudaMemcpyDeviceToDevice, s));
+      ex_copy(ex, out->diffuse, b.diff_light, light_bytes);
     if (out && out->specular)
-      VLT_TRY(cudaMemcpyAsync(out->specular, b.spec_light, light_bytes, cudaMemcpyDeviceToDevice, s));
+      ex_copy(ex, out->specular, b.spec_light, light_bytes);
   }
   if (out && out->raw_diffuse)
-    VLT_TRY(cudaMemcpyAsync(out->raw_diffuse, b.diff_light, light_bytes, cudaMemcpyDeviceToDevice, s));
+    ex_copy(ex, out->raw_diffuse, b.diff_light, light_bytes);
   if (out && out->raw_specular)
-    VLT_TRY(cudaMemcpyAsync(out->raw_specular, b.spec_light, light_bytes, cudaMemcpyDeviceToDevice, s));
+    ex_copy(ex, out->raw_specular, b.spec_light, light_bytes);
 
   // Retain depth for the next frame unless the caller keeps it (the previous
   // frame's decoded G-buffer fields stay in the other surface slot).
-  if (!in->prev_depth) VLT_TRY(cudaMemcpyAsync(b.prev_depth, in->depth, 4 * n, cudaMemcpyDeviceToDevice, s));
+  if (!in->prev_depth) ex_copy(ex, b.prev_depth, in->depth, 4 * n);
   v->surf_cur = sc;
   v->frames += 1;
   v->launches = launches;
 #undef STAGE
   return cuda_status(cudaGetLastError());
+}
+
+extern "C" {
+
+vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out, void* stream) {
+  return frame_run_impl(v, in, out, (cudaStream_t)stream, nullptr);
 }
 
 // ------------------------------------------------------ per-pass entry points
@@ -774,9 +809,9 @@ vlt_status vlt_ind_diff_temporal_resample(const vlt_frame_params* fp, uint32_t w
       (has_new_sample && params->use_input_pdf && !new_source_pdf))
     return VLT_ERR_INVALID_ARG;
   GeoArgs ga = {gbuffer_depth, nullptr, fp->inv_view_proj, nullptr, nullptr, nullptr};
-  launch_diff_temporal(FORM_REF, *fp, width, height, diff_knobs(*params), ga, prev_gbuffer_depth, new_hit_pos_normal,
+  launch_diff_temporal(stream_exec(stream), FORM_REF, *fp, width, height, diff_knobs(*params), ga, prev_gbuffer_depth, new_hit_pos_normal,
                        new_hit_radiance, new_source_pdf, prev_reservoir, rw_reservoir, frame_rand, has_prev_frame,
-                       has_new_sample, (cudaStream_t)stream);
+                       has_new_sample);
   return cuda_status(cudaGetLastError());
 }
 
@@ -787,15 +822,15 @@ vlt_status vlt_ao_gen(const vlt_frame_params* fp, uint32_t width, uint32_t heigh
       (has_prev_frame && !prev_ao))
     return VLT_ERR_INVALID_ARG;
   GeoArgs ga = {depth_buffer, nullptr, fp->inv_view_proj, nullptr, nullptr, nullptr};
-  launch_ao_gen(FORM_REF, *fp, width, height, ga, hit_pos_normal, (const uint32_t*)prev_ao, (uint32_t*)rw_ao, has_new_sample,
-                has_prev_frame, radius_ws, (cudaStream_t)stream);
+  launch_ao_gen(stream_exec(stream), FORM_REF, *fp, width, height, ga, hit_pos_normal, (const uint32_t*)prev_ao, (uint32_t*)rw_ao, has_new_sample,
+                has_prev_frame, radius_ws);
   return cuda_status(cudaGetLastError());
 }
 
 vlt_status vlt_ao_filter(uint32_t width, uint32_t height, const float* depth_buffer, const uint16_t* ao,
                          uint16_t* rw_filtered_ao, void* stream) {
   if (!dims_ok(width, height) || !depth_buffer || !ao || !rw_filtered_ao) return VLT_ERR_INVALID_ARG;
-  launch_ao_filter(FORM_REF, width, height, depth_buffer, ao, rw_filtered_ao, (cudaStream_t)stream);
+  launch_ao_filter(stream_exec(stream), FORM_REF, width, height, depth_buffer, ao, rw_filtered_ao);
   return cuda_status(cudaGetLastError());
 }
 
@@ -808,8 +843,8 @@ vlt_status vlt_ind_diff_spatial_resample(const vlt_frame_params* fp, uint32_t wi
       !temp_reservoir || !rw_reservoir)
     return VLT_ERR_INVALID_ARG;
   GeoArgs ga = {gbuffer_depth, gbuffer_color, fp->inv_view_proj, nullptr, nullptr, nullptr};
-  launch_diff_spatial(FORM_REF, *fp, width, height, diff_knobs(*params), ga, ao_texture, temp_reservoir, rw_reservoir,
-                      rw_lighting, frame_rand, (cudaStream_t)stream);
+  launch_diff_spatial(stream_exec(stream), FORM_REF, *fp, width, height, diff_knobs(*params), ga, ao_texture, temp_reservoir, rw_reservoir,
+                      rw_lighting, frame_rand);
   return cuda_status(cudaGetLastError());
 }
 
@@ -828,9 +863,9 @@ vlt_status vlt_ind_spec_temporal_resample(const vlt_frame_params* fp, uint32_t w
     return VLT_ERR_INVALID_ARG;
   GeoArgs ga = {gbuffer_depth, gbuffer_color, fp->inv_view_proj, nullptr, nullptr, nullptr};
   GeoArgs pga = {prev_gbuffer_depth, prev_gbuffer_color, fp->prev_inv_view_proj, nullptr, nullptr, nullptr};
-  launch_spec_temporal(*fp, width, height, params->spec_m_cap, ga, pga, prev_gbuffer_depth, prev_reservoir,
+  launch_spec_temporal(stream_exec(stream), *fp, width, height, params->spec_m_cap, ga, pga, prev_gbuffer_depth, prev_reservoir,
                        prev_hit_pos, prev_hit_radiance, new_hit_pos, new_hit_radiance, rw_reservoir, rw_hit_pos,
-                       rw_hit_radiance, frame_rand, has_prev_frame, (cudaStream_t)stream);
+                       rw_hit_radiance, frame_rand, has_prev_frame);
   return cuda_status(cudaGetLastError());
 }
 
@@ -847,9 +882,8 @@ vlt_status vlt_ind_spec_spatial_resample(const vlt_frame_params* fp, uint32_t wi
     return VLT_ERR_INVALID_ARG;
   SpecKnobs sk = {params->spec_spatial_taps, params->spec_spatial_radius_px};
   GeoArgs ga = {gbuffer_depth, gbuffer_color, fp->inv_view_proj, nullptr, nullptr, nullptr};
-  launch_spec_spatial(FORM_REF, *fp, width, height, sk, ga, reservoir, hit_pos, hit_radiance,
-                      rw_lighting, rw_ray_len, rw_reservoir, rw_hit_pos, rw_hit_radiance, frame_rand,
-                      (cudaStream_t)stream);
+  launch_spec_spatial(stream_exec(stream), FORM_REF, *fp, width, height, sk, ga, reservoir, hit_pos, hit_radiance,
+                      rw_lighting, rw_ray_len, rw_reservoir, rw_hit_pos, rw_hit_radiance, frame_rand);
   return cuda_status(cudaGetLastError());
 }
 
@@ -871,9 +905,9 @@ vlt_status vlt_denoise_temporal(const vlt_frame_params* fp, uint32_t width, uint
   DenoiseKnobs kn = {1.0f / params->history_max_frames, fast_history_on};
   GeoArgs ga = {depth_texture, gbuffer_texture, fp->inv_view_proj, nullptr, nullptr, nullptr};
   GeoArgs pga = {prev_depth_texture, prev_gbuffer_texture, fp->prev_inv_view_proj, nullptr, nullptr, nullptr};
-  launch_dn_temporal(*fp, width, height, kn, ga, pga, diff_source, spec_source, spec_ray_len, prev_depth_texture,
+  launch_dn_temporal(stream_exec(stream), *fp, width, height, kn, ga, pga, diff_source, spec_source, spec_ray_len, prev_depth_texture,
                      color_history, (const uint32_t*)moments_history, history_len_texture, fast_history, rw_color,
-                     (uint32_t*)rw_moments, rw_history_len, rw_fast_history, has_history, (cudaStream_t)stream);
+                     (uint32_t*)rw_moments, rw_history_len, rw_fast_history, has_history);
   return cuda_status(cudaGetLastError());
 }
 
@@ -885,15 +919,15 @@ vlt_status vlt_denoise_disocclusion_fix(uint32_t width, uint32_t height, const f
       !rw_color || !rw_moments)
     return VLT_ERR_INVALID_ARG;
   GeoArgs ga = {depth_texture, gbuffer_texture, nullptr, nullptr, nullptr, nullptr};
-  launch_dn_fix(width, height, ga, history_len_texture, color, (const uint32_t*)moments,
-                rw_color, (uint32_t*)rw_moments, (cudaStream_t)stream);
+  launch_dn_fix(stream_exec(stream), width, height, ga, history_len_texture, color, (const uint32_t*)moments,
+                rw_color, (uint32_t*)rw_moments);
   return cuda_status(cudaGetLastError());
 }
 
 vlt_status vlt_denoise_fast_history_clamp(uint32_t width, uint32_t height, const uint32_t* fast_history,
                                           uint32_t* rw_color, void* stream) {
   if (!dims_ok(width, height) || !fast_history || !rw_color) return VLT_ERR_INVALID_ARG;
-  launch_dn_fast_clamp(width, height, fast_history, rw_color, (cudaStream_t)stream);
+  launch_dn_fast_clamp(stream_exec(stream), width, height, fast_history, rw_color);
   return cuda_status(cudaGetLastError());
 }
 
@@ -905,8 +939,8 @@ vlt_status vlt_denoise_spatial_fallback(uint32_t width, uint32_t height, const f
       !rw_color || !rw_variance)
     return VLT_ERR_INVALID_ARG;
   GeoArgs ga = {depth_texture, gbuffer_texture, nullptr, nullptr, nullptr, nullptr};
-  launch_dn_fallback(width, height, ga, history_len_texture, color,
-                     (const uint32_t*)moments, rw_color, (uint32_t*)rw_variance, (cudaStream_t)stream);
+  launch_dn_fallback(stream_exec(stream), width, height, ga, history_len_texture, color,
+                     (const uint32_t*)moments, rw_color, (uint32_t*)rw_variance);
   return cuda_status(cudaGetLastError());
 }
 
@@ -917,8 +951,8 @@ vlt_status vlt_denoise_atrous(uint32_t width, uint32_t height, const float* dept
       !rw_variance || step_size < 1 || step_size > 4096)
     return VLT_ERR_INVALID_ARG;
   GeoArgs ga = {depth_texture, gbuffer_texture, nullptr, nullptr, nullptr, nullptr};
-  launch_dn_atrous(width, height, ga, color, (const uint32_t*)variance, rw_color,
-                   (uint32_t*)rw_variance, nullptr, nullptr, step_size, (cudaStream_t)stream);
+  launch_dn_atrous(stream_exec(stream), width, height, ga, color, (const uint32_t*)variance, rw_color,
+                   (uint32_t*)rw_variance, nullptr, nullptr, step_size);
   return cuda_status(cudaGetLastError());
 }
 
@@ -927,7 +961,7 @@ static bool hg_ok(uint32_t log2_buckets) { return log2_buckets >= 4 && log2_buck
 vlt_status vlt_hg_decay(uint32_t log2_buckets, uint8_t* rw_decay, uint32_t* rw_storage, void* stream) {
   if (!hg_ok(log2_buckets) || !rw_decay || !rw_storage) return VLT_ERR_INVALID_ARG;
   HashGridDims d = {log2_buckets, 1};
-  launch_hg_decay(d, rw_decay, rw_storage, (cudaStream_t)stream);
+  launch_hg_decay(stream_exec(stream), d, rw_decay, rw_storage);
   return cuda_status(cudaGetLastError());
 }
 
@@ -944,7 +978,7 @@ vlt_status vlt_hg_query_select(uint32_t log2_buckets, uint32_t max_queries, cons
       !rw_storage || !rw_selection || !scratch)
     return VLT_ERR_INVALID_ARG;
   HashGridDims d = {log2_buckets, max_queries};
-  launch_hg_select(d, queries, query_count, rw_storage, rw_selection, frame_hash, scratch, (cudaStream_t)stream);
+  launch_hg_select(stream_exec(stream), d, queries, query_count, rw_storage, rw_selection, frame_hash, scratch);
   return cuda_status(cudaGetLastError());
 }
 
@@ -955,8 +989,7 @@ vlt_status vlt_hg_query_compact(uint32_t log2_buckets, uint32_t max_queries, con
       !rw_compact_count)
     return VLT_ERR_INVALID_ARG;
   HashGridDims d = {log2_buckets, max_queries};
-  launch_hg_compact(d, selection, rw_compact_query_index, rw_compact_cell_addr, rw_compact_count,
-                    (cudaStream_t)stream);
+  launch_hg_compact(stream_exec(stream), d, selection, rw_compact_query_index, rw_compact_cell_addr, rw_compact_count);
   return cuda_status(cudaGetLastError());
 }
 
@@ -967,8 +1000,7 @@ vlt_status vlt_hg_update(uint32_t max_queries, const uint32_t* queries, const ui
       !rw_decay)
     return VLT_ERR_INVALID_ARG;
   HashGridDims d = {24, max_queries};
-  launch_hg_update(d, queries, compact_query_index, compact_cell_addr, compact_count, rw_storage, rw_decay,
-                   (cudaStream_t)stream);
+  launch_hg_update(stream_exec(stream), d, queries, compact_query_index, compact_cell_addr, compact_count, rw_storage, rw_decay);
   return cuda_status(cudaGetLastError());
 }
 
@@ -980,8 +1012,7 @@ vlt_status vlt_hg_emit_queries(const vlt_frame_params* fp, uint32_t width, uint3
       !hit_pos_normal || !hit_radiance || !rw_queries || !rw_query_count)
     return VLT_ERR_INVALID_ARG;
   HashGridDims d = {log2_buckets, max_queries};
-  launch_hg_emit(*fp, width, height, d, key_mode, depth, hit_pos_normal, hit_radiance, rw_queries, rw_query_count,
-                 (cudaStream_t)stream);
+  launch_hg_emit(stream_exec(stream), *fp, width, height, d, key_mode, depth, hit_pos_normal, hit_radiance, rw_queries, rw_query_count);
   return cuda_status(cudaGetLastError());
 }
 
@@ -991,7 +1022,7 @@ vlt_status vlt_hg_find(const vlt_frame_params* fp, uint32_t log2_buckets, uint32
   if (!fp || !hg_ok(log2_buckets) || key_mode > 1 || !storage || (n && (!positions || !normals || !out_addr)))
     return VLT_ERR_INVALID_ARG;
   HashGridDims d = {log2_buckets, 1};
-  launch_hg_find(*fp, d, key_mode, storage, n, positions, normals, out_addr, out_radiance, (cudaStream_t)stream);
+  launch_hg_find(stream_exec(stream), *fp, d, key_mode, storage, n, positions, normals, out_addr, out_radiance);
   return cuda_status(cudaGetLastError());
 }
 

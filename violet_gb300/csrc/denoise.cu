@@ -70,20 +70,9 @@ __device__ __forceinline__ float dsr_weight(f3 color, f3 mean, f3 dev) {
 
 // svgf_temporal_filter.hlsl:96-362.
 template <class Geo>
-__global__ void __launch_bounds__(128) k_dn_temporal(vlt_frame_params fp, int w, int h, DenoiseKnobs kn, Geo geo,
-                                                      Geo prev_geo, const uint32_t* __restrict__ gbuf,
-                                                      const uint32_t* __restrict__ diff_src,
-                                                      const uint32_t* __restrict__ spec_src,
-                                                      const uint16_t* __restrict__ ray_len_tex,
-                                                      const float* __restrict__ prev_depth,
-                                                      const uint2* __restrict__ color_hist,
-                                                      const uint32_t* __restrict__ mom_hist,
-                                                      const uint8_t* __restrict__ len_hist,
-                                                      const uint2* __restrict__ fast_hist,
-                                                      uint2* __restrict__ out_color, uint32_t* __restrict__ out_mom,
-                                                      uint8_t* __restrict__ out_len, uint2* __restrict__ out_fast,
-                                                      uint32_t has_history) {
-  int x = pix_x(), y = pix_y();
+struct DnTemporalF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DenoiseKnobs kn, Geo geo, Geo prev_geo, const uint32_t* __restrict__ gbuf, const uint32_t* __restrict__ diff_src, const uint32_t* __restrict__ spec_src, const uint16_t* __restrict__ ray_len_tex, const float* __restrict__ prev_depth, const uint2* __restrict__ color_hist, const uint32_t* __restrict__ mom_hist, const uint8_t* __restrict__ len_hist, const uint2* __restrict__ fast_hist, uint2* __restrict__ out_color, uint32_t* __restrict__ out_mom, uint8_t* __restrict__ out_len, uint2* __restrict__ out_fast, uint32_t has_history) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float depth = geo.dep(i);
@@ -259,6 +248,7 @@ __global__ void __launch_bounds__(128) k_dn_temporal(vlt_frame_params fp, int w,
   out_len[i] = (uint8_t)unorm8_store(hl);
   if (kn.fast_history) out_fast[i] = make_uint2(pack_r11g11b10(dff), pack_r11g11b10(sff));
 }
+};
 
 // Max history length over the aligned 2x2 quad (QuadReadAcrossX/Y of the
 // quad-remapped 8x8 groups); out-of-range quad members read as 0.
@@ -279,10 +269,9 @@ __device__ __forceinline__ float quad_max_len(const uint8_t* __restrict__ len, i
 // relax_disocclusion_fix.hlsl:27-122. Pixels without geometry (history 0) are not
 // written by the shader; here they get zeros.
 template <class Geo>
-__global__ void __launch_bounds__(128) k_dn_fix(int w, int h, Geo geo, const uint8_t* __restrict__ len_tex,
-                                                 const uint2* __restrict__ color, const uint32_t* __restrict__ mom,
-                                                 uint2* __restrict__ out_color, uint32_t* __restrict__ out_mom) {
-  int x = pix_x(), y = pix_y();
+struct DnFixF {
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, const uint8_t* __restrict__ len_tex, const uint2* __restrict__ color, const uint32_t* __restrict__ mom, uint2* __restrict__ out_color, uint32_t* __restrict__ out_mom) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float hl = unorm8_load(len_tex[i]);
@@ -326,6 +315,7 @@ __global__ void __launch_bounds__(128) k_dn_fix(int w, int h, Geo geo, const uin
     out_mom[i] = mom[i];
   }
 }
+};
 
 // ------------------------------------------------------ fast history clamp
 
@@ -338,9 +328,9 @@ __device__ __forceinline__ f3 ycocg_to_rgb(f3 c) {
 }
 
 // relax_fast_history_clamp.hlsl:11-75 (in place on the slow colour).
-__global__ void __launch_bounds__(128) k_dn_fast_clamp(int w, int h, const uint2* __restrict__ fast,
-                                                        uint2* __restrict__ color) {
-  int x = pix_x(), y = pix_y();
+struct DnFastClampF {
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, const uint2* __restrict__ fast, uint2* __restrict__ color) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   f3 dm1 = mk3(0.0f), dm2 = mk3(0.0f), sm1 = mk3(0.0f), sm2 = mk3(0.0f);
@@ -372,16 +362,15 @@ __global__ void __launch_bounds__(128) k_dn_fast_clamp(int w, int h, const uint2
   s = clamp3(s, sm1 - sdev, sm1 + sdev);
   color[i] = make_uint2(pack_r11g11b10(ycocg_to_rgb(d)), pack_r11g11b10(ycocg_to_rgb(s)));
 }
+};
 
 // ---------------------------------------------------------- spatial fallback
 
 // svgf_spatial_fallback_filter.hlsl:25-125. History-0 pixels get zeros.
 template <class Geo>
-__global__ void __launch_bounds__(128) k_dn_fallback(int w, int h, Geo geo, const uint8_t* __restrict__ len_tex,
-                                                      const uint2* __restrict__ color,
-                                                      const uint32_t* __restrict__ mom, uint2* __restrict__ out_color,
-                                                      uint32_t* __restrict__ out_var) {
-  int x = pix_x(), y = pix_y();
+struct DnFallbackF {
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, const uint8_t* __restrict__ len_tex, const uint2* __restrict__ color, const uint32_t* __restrict__ mom, uint2* __restrict__ out_color, uint32_t* __restrict__ out_var) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float hl = unorm8_load(len_tex[i]);
@@ -429,6 +418,7 @@ __global__ void __launch_bounds__(128) k_dn_fallback(int w, int h, Geo geo, cons
   out_color[i] = make_uint2(pack_r11g11b10(dd), pack_r11g11b10(sd));
   out_var[i] = pack_half2(var);
 }
+};
 
 // --------------------------------------------------------------- a-trous
 
@@ -441,13 +431,9 @@ struct AtrousTaps {
 // svgf_atrous_filter.hlsl:23-88: 5x5 taps at step 2^i, kernel {1, 2/3, 1/6}, only
 // the 16 taps off both centre axes (the shader's `(x != 0) && (y != 0)`).
 template <class Geo>
-__global__ void __launch_bounds__(128) k_dn_atrous(int w, int h, Geo geo, AtrousTaps taps,
-                                                    const uint2* __restrict__ color,
-                                                    const uint32_t* __restrict__ var_tex,
-                                                    uint2* __restrict__ out_color, uint32_t* __restrict__ out_var,
-                                                    uint32_t* __restrict__ out_diff, uint32_t* __restrict__ out_spec,
-                                                    int step) {
-  int x = pix_x(), y = pix_y();
+struct DnAtrousF {
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, AtrousTaps taps, const uint2* __restrict__ color, const uint32_t* __restrict__ var_tex, uint2* __restrict__ out_color, uint32_t* __restrict__ out_var, uint32_t* __restrict__ out_diff, uint32_t* __restrict__ out_spec, int step) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   uint2 cc = color[i];
@@ -495,22 +481,22 @@ __global__ void __launch_bounds__(128) k_dn_atrous(int w, int h, Geo geo, Atrous
   if (out_diff) out_diff[i] = pd;
   if (out_spec) out_spec[i] = ps;
 }
+};
 
-__global__ void k_split_color(int n, const uint2* __restrict__ color, uint32_t* __restrict__ d,
-                              uint32_t* __restrict__ s) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+struct SplitColorF {
+  static __device__ __forceinline__ void run(int x0, int y0, int n, const uint2* __restrict__ color, uint32_t* __restrict__ d, uint32_t* __restrict__ s) {
+  int i = x0 + (int)threadIdx.x;
   if (i >= n) return;
   uint2 c = color[i];
   if (d) d[i] = c.x;
   if (s) s[i] = c.y;
 }
+};
 
 // ------------------------------------------------------------- launchers
 
-static const dim3 kBlock(32, 4, 1);
-
 static GeoRaw raw_geo(const GeoArgs& a, int w, int h) {
-  GeoRaw g = {a.depth, a.gbuf, a.inv_vp, w, h};
+  GeoRaw g = make_geo_raw(a.depth, a.gbuf, a.inv_vp, w, h);
   return g;
 }
 static GeoSurface surf_geo(const GeoArgs& a, int w, int h) {
@@ -518,51 +504,50 @@ static GeoSurface surf_geo(const GeoArgs& a, int w, int h) {
   return g;
 }
 
-void launch_dn_temporal(const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn, const GeoArgs& ga,
-                        const GeoArgs& prev_ga, const uint32_t* diff_src, const uint32_t* spec_src,
+void launch_dn_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn,
+                        const GeoArgs& ga, const GeoArgs& prev_ga, const uint32_t* diff_src, const uint32_t* spec_src,
                         const uint16_t* ray_len, const float* prev_depth, const uint32_t* color_hist,
                         const uint32_t* mom_hist, const uint8_t* len_hist, const uint32_t* fast_hist,
                         uint32_t* out_color, uint32_t* out_mom, uint8_t* out_len, uint32_t* out_fast,
-                        uint32_t has_history, cudaStream_t s) {
+                        uint32_t has_history) {
   if (ga.nd)
-    k_dn_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
-        fp, w, h, kn, surf_geo(ga, w, h), surf_geo(prev_ga, w, h), ga.gbuf, diff_src, spec_src, ray_len, prev_depth,
-        (const uint2*)color_hist, mom_hist, len_hist, (const uint2*)fast_hist, (uint2*)out_color, out_mom, out_len,
-        (uint2*)out_fast, has_history);
+    launch2d<DnTemporalF<GeoSurface>>(ex, "dn_temporal", w, h, fp, w, h, kn, surf_geo(ga, w, h),
+                                      surf_geo(prev_ga, w, h), ga.gbuf, diff_src, spec_src, ray_len, prev_depth,
+                                      (const uint2*)color_hist, mom_hist, len_hist, (const uint2*)fast_hist,
+                                      (uint2*)out_color, out_mom, out_len, (uint2*)out_fast, has_history);
   else
-    k_dn_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
-        fp, w, h, kn, raw_geo(ga, w, h), raw_geo(prev_ga, w, h), ga.gbuf, diff_src, spec_src, ray_len, prev_depth,
-        (const uint2*)color_hist, mom_hist, len_hist, (const uint2*)fast_hist, (uint2*)out_color, out_mom, out_len,
-        (uint2*)out_fast, has_history);
+    launch2d<DnTemporalF<GeoRaw>>(ex, "dn_temporal", w, h, fp, w, h, kn, raw_geo(ga, w, h), raw_geo(prev_ga, w, h),
+                                  ga.gbuf, diff_src, spec_src, ray_len, prev_depth, (const uint2*)color_hist,
+                                  mom_hist, len_hist, (const uint2*)fast_hist, (uint2*)out_color, out_mom, out_len,
+                                  (uint2*)out_fast, has_history);
 }
 
-void launch_dn_fix(int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color, const uint32_t* mom,
-                   uint32_t* out_color, uint32_t* out_mom, cudaStream_t s) {
+void launch_dn_fix(const Exec& ex, int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color,
+                   const uint32_t* mom, uint32_t* out_color, uint32_t* out_mom) {
   if (ga.nd)
-    k_dn_fix<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, surf_geo(ga, w, h), len, (const uint2*)color, mom,
-                                                       (uint2*)out_color, out_mom);
+    launch2d<DnFixF<GeoSurface>>(ex, "dn_fix", w, h, w, h, surf_geo(ga, w, h), len, (const uint2*)color, mom,
+                                 (uint2*)out_color, out_mom);
   else
-    k_dn_fix<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, raw_geo(ga, w, h), len, (const uint2*)color, mom,
-                                                       (uint2*)out_color, out_mom);
+    launch2d<DnFixF<GeoRaw>>(ex, "dn_fix", w, h, w, h, raw_geo(ga, w, h), len, (const uint2*)color, mom,
+                             (uint2*)out_color, out_mom);
 }
 
-void launch_dn_fast_clamp(int w, int h, const uint32_t* fast, uint32_t* color, cudaStream_t s) {
-  k_dn_fast_clamp<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, (const uint2*)fast, (uint2*)color);
+void launch_dn_fast_clamp(const Exec& ex, int w, int h, const uint32_t* fast, uint32_t* color) {
+  launch2d<DnFastClampF>(ex, "dn_fast_clamp", w, h, w, h, (const uint2*)fast, (uint2*)color);
 }
 
-void launch_dn_fallback(int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color,
-                        const uint32_t* mom, uint32_t* out_color, uint32_t* out_var, cudaStream_t s) {
+void launch_dn_fallback(const Exec& ex, int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color,
+                        const uint32_t* mom, uint32_t* out_color, uint32_t* out_var) {
   if (ga.nd)
-    k_dn_fallback<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, surf_geo(ga, w, h), len, (const uint2*)color, mom,
-                                                            (uint2*)out_color, out_var);
+    launch2d<DnFallbackF<GeoSurface>>(ex, "dn_fallback", w, h, w, h, surf_geo(ga, w, h), len, (const uint2*)color,
+                                      mom, (uint2*)out_color, out_var);
   else
-    k_dn_fallback<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, raw_geo(ga, w, h), len, (const uint2*)color, mom,
-                                                            (uint2*)out_color, out_var);
+    launch2d<DnFallbackF<GeoRaw>>(ex, "dn_fallback", w, h, w, h, raw_geo(ga, w, h), len, (const uint2*)color, mom,
+                                  (uint2*)out_color, out_var);
 }
 
-void launch_dn_atrous(int w, int h, const GeoArgs& ga, const uint32_t* color, const uint32_t* var,
-                      uint32_t* out_color, uint32_t* out_var, uint32_t* out_diff, uint32_t* out_spec, int step,
-                      cudaStream_t s) {
+void launch_dn_atrous(const Exec& ex, int w, int h, const GeoArgs& ga, const uint32_t* color, const uint32_t* var,
+                      uint32_t* out_color, uint32_t* out_var, uint32_t* out_diff, uint32_t* out_spec, int step) {
   AtrousTaps taps;
   int k = 0;
   for (int oy = -2; oy <= 2; ++oy) {
@@ -574,16 +559,16 @@ void launch_dn_atrous(int w, int h, const GeoArgs& ga, const uint32_t* color, co
     }
   }
   if (ga.nd)
-    k_dn_atrous<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, surf_geo(ga, w, h), taps, (const uint2*)color, var,
-                                                          (uint2*)out_color, out_var, out_diff, out_spec, step);
+    launch2d<DnAtrousF<GeoSurface>>(ex, "dn_atrous", w, h, w, h, surf_geo(ga, w, h), taps, (const uint2*)color, var,
+                                    (uint2*)out_color, out_var, out_diff, out_spec, step);
   else
-    k_dn_atrous<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, raw_geo(ga, w, h), taps, (const uint2*)color, var,
-                                                          (uint2*)out_color, out_var, out_diff, out_spec, step);
+    launch2d<DnAtrousF<GeoRaw>>(ex, "dn_atrous", w, h, w, h, raw_geo(ga, w, h), taps, (const uint2*)color, var,
+                                (uint2*)out_color, out_var, out_diff, out_spec, step);
 }
 
-void launch_split_color(int w, int h, const uint32_t* color, uint32_t* diff, uint32_t* spec, cudaStream_t s) {
+void launch_split_color(const Exec& ex, int w, int h, const uint32_t* color, uint32_t* diff, uint32_t* spec) {
   int n = w * h;
-  k_split_color<<<(n + 255) / 256, 256, 0, s>>>(n, (const uint2*)color, diff, spec);
+  launch1d<SplitColorF>(ex, "split_color", (uint32_t)n, n, (const uint2*)color, diff, spec);
 }
 
 }  // namespace vlt

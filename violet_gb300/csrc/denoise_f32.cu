@@ -88,6 +88,17 @@ struct EdgeStopFast {
     }
     return mk2(wn * exp_fma(ax), wn * exp_fma(ay));
   }
+  // The same with the depth term as -dist_z * r_z, r_z = 1 / (fz_sigma * d + 1e-8)
+  // precomputed by the caller for the tap's distance d (the a-trous taps have only
+  // three distinct distances).
+  __device__ __forceinline__ f2 weight_rz(float r_z, float depth, f3 normal, f2 lumi) const {
+    float wz = -fabsf(depth - depth_center) * r_z;
+    float n_dot = saturate(fma_(normal_center.z, normal.z, fma_(normal_center.y, normal.y, normal_center.x * normal.x)));
+    float wn = pow_2k(n_dot, sigma_n_log2);
+    float ax = fma_(-fabsf(lumi.x - lumi_center.x), lumi_rcp.x, wz);
+    float ay = fma_(-fabsf(lumi.y - lumi_center.y), lumi_rcp.y, wz);
+    return mk2(wn * exp_fma(ax), wn * exp_fma(ay));
+  }
 };
 
 __device__ __forceinline__ EdgeStopFast make_es(float depth, float fwidth_z, float sigma_z, f3 normal, int n_log2) {
@@ -129,17 +140,9 @@ __device__ __forceinline__ float quad_max_len(const float* __restrict__ len, int
 // --------------------------------------------------------------- temporal
 
 template <class Geo>
-__global__ void __launch_bounds__(128) k_dn32_temporal(vlt_frame_params fp, int w, int h, DenoiseKnobs kn, Geo geo,
-                                                        Geo prev_geo, const uint32_t* __restrict__ gbuf,
-                                                        const float4* __restrict__ diff_src,
-                                                        const float4* __restrict__ spec_src,
-                                                        const float* __restrict__ prev_depth,
-                                                        const float4* __restrict__ hist,
-                                                        const float* __restrict__ len_hist,
-                                                        const float4* __restrict__ fast_hist,
-                                                        float4* __restrict__ out, float* __restrict__ out_len,
-                                                        float4* __restrict__ out_fast, uint32_t has_history) {
-  int x = pix_x(), y = pix_y();
+struct Dn32TemporalF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DenoiseKnobs kn, Geo geo, Geo prev_geo, const uint32_t* __restrict__ gbuf, const float4* __restrict__ diff_src, const float4* __restrict__ spec_src, const float* __restrict__ prev_depth, const float4* __restrict__ hist, const float* __restrict__ len_hist, const float4* __restrict__ fast_hist, float4* __restrict__ out, float* __restrict__ out_len, float4* __restrict__ out_fast, uint32_t has_history) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float depth = geo.dep(i);
@@ -300,13 +303,14 @@ __global__ void __launch_bounds__(128) k_dn32_temporal(vlt_frame_params fp, int 
   out_len[i] = hl;
   if (kn.fast_history) store_rec(out_fast, i, dff, sff, mk2(0.0f, 0.0f));
 }
+};
 
 // ----------------------------------------------------------- disocclusion fix
 
 template <class Geo>
-__global__ void __launch_bounds__(128) k_dn32_fix(int w, int h, Geo geo, const float* __restrict__ len,
-                                                   const float4* __restrict__ in, float4* __restrict__ out) {
-  int x = pix_x(), y = pix_y();
+struct Dn32FixF {
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, const float* __restrict__ len, const float4* __restrict__ in, float4* __restrict__ out) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float hl = len[i];
@@ -342,6 +346,7 @@ __global__ void __launch_bounds__(128) k_dn32_fix(int w, int h, Geo geo, const f
     out[2 * i + 1] = in[2 * i + 1];
   }
 }
+};
 
 // ------------------------------------------------------ fast history clamp
 
@@ -353,9 +358,9 @@ __device__ __forceinline__ f3 ycocg_inv(f3 c) {
   return mk3(tmp + c.y, c.x + c.z, tmp - c.y);
 }
 
-__global__ void __launch_bounds__(128) k_dn32_fast_clamp(int w, int h, const float4* __restrict__ fast,
-                                                          float4* __restrict__ rec) {
-  int x = pix_x(), y = pix_y();
+struct Dn32FastClampF {
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, const float4* __restrict__ fast, float4* __restrict__ rec) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   f3 dm1 = mk3(0.0f), dm2 = mk3(0.0f), sm1 = mk3(0.0f), sm2 = mk3(0.0f);
@@ -383,13 +388,14 @@ __global__ void __launch_bounds__(128) k_dn32_fast_clamp(int w, int h, const flo
   f3 s = clamp3(ycocg(c.s), sm1 - sdev, sm1 + sdev);
   store_rec(rec, i, ycocg_inv(d), ycocg_inv(s), c.aux);
 }
+};
 
 // ---------------------------------------------------------- spatial fallback
 
 template <class Geo>
-__global__ void __launch_bounds__(128) k_dn32_fallback(int w, int h, Geo geo, const float* __restrict__ len,
-                                                        const float4* __restrict__ in, float4* __restrict__ out) {
-  int x = pix_x(), y = pix_y();
+struct Dn32FallbackF {
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, const float* __restrict__ len, const float4* __restrict__ in, float4* __restrict__ out) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float hl = len[i];
@@ -434,46 +440,53 @@ __global__ void __launch_bounds__(128) k_dn32_fallback(int w, int h, Geo geo, co
   float boost = fmax_(1.0f, (4.0f * VLT_HISTORY_LEN_UNIT) / hl);
   store_rec(out, i, dd, sd, var * boost);
 }
+};
 
 // --------------------------------------------------------------- a-trous
 
-struct AtrousTaps32 {
-  float dist[16];
+// Tap distances of one iteration: |offset| for (|ox|, |oy|) = (1,1), (1,2) or (2,1),
+// and (2,2), times the step (computed on the host with IEEE sqrtf).
+struct AtrousDist {
+  float d11, d12, d22;
 };
 
-template <class Geo>
-__global__ void __launch_bounds__(128) k_dn32_atrous(int w, int h, Geo geo, AtrousTaps32 taps,
-                                                      const float4* __restrict__ in, float4* __restrict__ out,
-                                                      float4* __restrict__ out_diff, float4* __restrict__ out_spec,
-                                                      int step) {
-  int x = pix_x(), y = pix_y();
-  if (!inb(x, y, w, h)) return;
+// svgf_atrous_filter.hlsl:23-88: 5x5 taps at `step`, kernel weights {1, 2/3, 1/6},
+// off-axis taps only (the reference's loop condition), variance filtered with w^2.
+// CHECK = false is the path of blocks whose whole 5x5 footprint is inside the image.
+template <bool CHECK, class Geo>
+__device__ __forceinline__ void atrous_px(int x, int y, int w, int h, const Geo& geo, AtrousDist td,
+                                          const float4* __restrict__ in, float4* __restrict__ out,
+                                          float4* __restrict__ out_diff, float4* __restrict__ out_spec, int step) {
   size_t i = (size_t)y * w + x;
   Rec c = load_rec(in, i);
   EdgeStopFast es = make_es(geo.dep(i), geo.fwz(i), 1.0f, geo.normal(i), 7);
   es.use_lumi = true;
   es.lumi_center = mk2(lum_fast(c.d.x, c.d.y, c.d.z), lum_fast(c.s.x, c.s.y, c.s.z));
   es.lumi_rcp = mk2(1.0f / fma_(4.0f, sqrt_(c.aux.x), 1e-8f), 1.0f / fma_(4.0f, sqrt_(c.aux.y), 1e-8f));
+  const float r11 = 1.0f / fma_(es.fz_sigma, td.d11, 1e-8f);
+  const float r12 = 1.0f / fma_(es.fz_sigma, td.d12, 1e-8f);
+  const float r22 = 1.0f / fma_(es.fz_sigma, td.d22, 1e-8f);
   const float kw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
   f3 dsum = c.d, ssum = c.s;
   f2 vsum = c.aux;
   f2 wsum = mk2(1.0f, 1.0f);
-  int tap = 0;
 #pragma unroll
   for (int oy = -2; oy <= 2; ++oy) {
     if (oy == 0) continue;
-    const float kwy = kw[oy < 0 ? -oy : oy];
+    const int ay = oy < 0 ? -oy : oy;
+    const float kwy = kw[ay];
 #pragma unroll
     for (int ox = -2; ox <= 2; ++ox) {
       if (ox == 0) continue;
-      const float tap_dist = taps.dist[tap++];
+      const int ax = ox < 0 ? -ox : ox;
       int cx = x + ox * step, cy = y + oy * step;
-      if (!(cx >= 0 && cy >= 0 && cx <= w - 1 && cy <= h - 1)) continue;
-      const float k = kwy * kw[ox < 0 ? -ox : ox];
+      if (CHECK && !(cx >= 0 && cy >= 0 && cx <= w - 1 && cy <= h - 1)) continue;
+      const float k = kwy * kw[ax];
+      const float rz = (ax == 1 && ay == 1) ? r11 : ((ax == 2 && ay == 2) ? r22 : r12);
       size_t j = (size_t)cy * w + cx;
       Rec r = load_rec(in, j);
       f2 lumi = mk2(lum_fast(r.d.x, r.d.y, r.d.z), lum_fast(r.s.x, r.s.y, r.s.z));
-      f2 e = es.weight(tap_dist, geo.dep(j), geo.normal(j), lumi);
+      f2 e = es.weight_rz(rz, geo.dep(j), geo.normal(j), lumi);
       f2 wt = mk2(k * e.x, k * e.y);
       dsum = fma3(wt.x, r.d, dsum);
       ssum = fma3(wt.y, r.s, ssum);
@@ -489,69 +502,75 @@ __global__ void __launch_bounds__(128) k_dn32_atrous(int w, int h, Geo geo, Atro
   if (out_spec) out_spec[i] = make_float4(sd.x, sd.y, sd.z, 0.0f);
 }
 
+template <class Geo>
+struct Dn32AtrousF {
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, AtrousDist td, const float4* __restrict__ in, float4* __restrict__ out, float4* __restrict__ out_diff, float4* __restrict__ out_spec, int step) {
+  const int m = 2 * step;
+  const bool interior = x0 - m >= 0 && y0 - m >= 0 && x0 + (int)blockDim.x - 1 + m <= w - 1 &&
+                        y0 + (int)blockDim.y - 1 + m <= h - 1;
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
+  if (interior) {
+    atrous_px<false>(x, y, w, h, geo, td, in, out, out_diff, out_spec, step);
+  } else {
+    if (!inb(x, y, w, h)) return;
+    atrous_px<true>(x, y, w, h, geo, td, in, out, out_diff, out_spec, step);
+  }
+}
+};
+
 // ------------------------------------------------------------- launchers
 
-static const dim3 kBlock(32, 4, 1);
-
-#define VLT_GEO_DISPATCH(ga, ...)                \
-  do {                                           \
-    if ((ga).nd) {                               \
-      GeoSurface geo = {(ga).nd, (ga).pr, (ga).fz, w, h}; \
-      __VA_ARGS__;                               \
-    } else {                                     \
-      GeoRaw geo = {(ga).depth, (ga).gbuf, (ga).inv_vp, w, h}; \
-      __VA_ARGS__;                               \
-    }                                            \
+#define VLT_GEO_DISPATCH(ga, ...)                                \
+  do {                                                           \
+    if ((ga).nd) {                                               \
+      using Geo = GeoSurface;                                    \
+      GeoSurface geo = {(ga).nd, (ga).pr, (ga).fz, w, h};        \
+      __VA_ARGS__;                                               \
+    } else {                                                     \
+      using Geo = GeoRaw;                                        \
+      GeoRaw geo = make_geo_raw((ga).depth, (ga).gbuf, (ga).inv_vp, w, h); \
+      __VA_ARGS__;                                               \
+    }                                                            \
   } while (0)
 
-void launch_dn32_temporal(const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn, const GeoArgs& ga,
-                          const GeoArgs& prev_ga, const float4* diff_src, const float4* spec_src,
+void launch_dn32_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn,
+                          const GeoArgs& ga, const GeoArgs& prev_ga, const float4* diff_src, const float4* spec_src,
                           const float* prev_depth, const float4* hist, const float* len_hist, const float4* fast_hist,
-                          float4* out, float* out_len, float4* out_fast, uint32_t has_history, cudaStream_t s) {
-  dim3 g = grid2d(w, h, kBlock);
+                          float4* out, float* out_len, float4* out_fast, uint32_t has_history) {
   if (ga.nd) {
     GeoSurface geo = {ga.nd, ga.pr, ga.fz, w, h};
     GeoSurface pgeo = {prev_ga.nd, prev_ga.pr, prev_ga.fz, w, h};
-    k_dn32_temporal<<<g, kBlock, 0, s>>>(fp, w, h, kn, geo, pgeo, ga.gbuf, diff_src, spec_src, prev_depth, hist,
-                                         len_hist, fast_hist, out, out_len, out_fast, has_history);
+    launch2d<Dn32TemporalF<GeoSurface>>(ex, "dn_temporal", w, h, fp, w, h, kn, geo, pgeo, ga.gbuf, diff_src,
+                                        spec_src, prev_depth, hist, len_hist, fast_hist, out, out_len, out_fast,
+                                        has_history);
   } else {
-    GeoRaw geo = {ga.depth, ga.gbuf, ga.inv_vp, w, h};
-    GeoRaw pgeo = {prev_ga.depth, prev_ga.gbuf, prev_ga.inv_vp, w, h};
-    k_dn32_temporal<<<g, kBlock, 0, s>>>(fp, w, h, kn, geo, pgeo, ga.gbuf, diff_src, spec_src, prev_depth, hist,
-                                         len_hist, fast_hist, out, out_len, out_fast, has_history);
+    GeoRaw geo = make_geo_raw(ga.depth, ga.gbuf, ga.inv_vp, w, h);
+    GeoRaw pgeo = make_geo_raw(prev_ga.depth, prev_ga.gbuf, prev_ga.inv_vp, w, h);
+    launch2d<Dn32TemporalF<GeoRaw>>(ex, "dn_temporal", w, h, fp, w, h, kn, geo, pgeo, ga.gbuf, diff_src, spec_src,
+                                    prev_depth, hist, len_hist, fast_hist, out, out_len, out_fast, has_history);
   }
 }
 
-void launch_dn32_fix(int w, int h, const GeoArgs& ga, const float* len, const float4* in, float4* out,
-                     cudaStream_t s) {
-  dim3 g = grid2d(w, h, kBlock);
-  VLT_GEO_DISPATCH(ga, k_dn32_fix<<<g, kBlock, 0, s>>>(w, h, geo, len, in, out));
+void launch_dn32_fix(const Exec& ex, int w, int h, const GeoArgs& ga, const float* len, const float4* in,
+                     float4* out) {
+  VLT_GEO_DISPATCH(ga, launch2d<Dn32FixF<Geo>>(ex, "dn_fix", w, h, w, h, geo, len, in, out));
 }
 
-void launch_dn32_fast_clamp(int w, int h, const float4* fast, float4* rec, cudaStream_t s) {
-  k_dn32_fast_clamp<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, fast, rec);
+void launch_dn32_fast_clamp(const Exec& ex, int w, int h, const float4* fast, float4* rec) {
+  launch2d<Dn32FastClampF>(ex, "dn_fast_clamp", w, h, w, h, fast, rec);
 }
 
-void launch_dn32_fallback(int w, int h, const GeoArgs& ga, const float* len, const float4* in, float4* out,
-                          cudaStream_t s) {
-  dim3 g = grid2d(w, h, kBlock);
-  VLT_GEO_DISPATCH(ga, k_dn32_fallback<<<g, kBlock, 0, s>>>(w, h, geo, len, in, out));
+void launch_dn32_fallback(const Exec& ex, int w, int h, const GeoArgs& ga, const float* len, const float4* in,
+                          float4* out) {
+  VLT_GEO_DISPATCH(ga, launch2d<Dn32FallbackF<Geo>>(ex, "dn_fallback", w, h, w, h, geo, len, in, out));
 }
 
-void launch_dn32_atrous(int w, int h, const GeoArgs& ga, const float4* in, float4* out, float4* out_diff,
-                        float4* out_spec, int step, cudaStream_t s) {
-  AtrousTaps32 taps;
-  int k = 0;
-  for (int oy = -2; oy <= 2; ++oy) {
-    if (oy == 0) continue;
-    for (int ox = -2; ox <= 2; ++ox) {
-      if (ox == 0) continue;
-      float fx = (float)(ox * step), fy = (float)(oy * step);
-      taps.dist[k++] = sqrtf(fx * fx + fy * fy);
-    }
-  }
-  dim3 g = grid2d(w, h, kBlock);
-  VLT_GEO_DISPATCH(ga, k_dn32_atrous<<<g, kBlock, 0, s>>>(w, h, geo, taps, in, out, out_diff, out_spec, step));
+void launch_dn32_atrous(const Exec& ex, int w, int h, const GeoArgs& ga, const float4* in, float4* out,
+                        float4* out_diff, float4* out_spec, int step) {
+  const float s1 = (float)step, s2 = (float)(2 * step);
+  AtrousDist td = {sqrtf(s1 * s1 + s1 * s1), sqrtf(s1 * s1 + s2 * s2), sqrtf(s2 * s2 + s2 * s2)};
+  VLT_GEO_DISPATCH(ga, launch2d<Dn32AtrousF<Geo>>(ex, "dn_atrous", w, h, w, h, geo, td, in, out, out_diff, out_spec,
+                                                  step));
 }
 
 #undef VLT_GEO_DISPATCH

@@ -59,11 +59,9 @@ __device__ __forceinline__ VertexKey vertex_key(f3 pos, f3 nrm, f3 cam, uint32_t
 
 // --------------------------------------------------------------- emission
 
-__global__ void k_hg_emit(vlt_frame_params fp, int w, int h, uint32_t bucket_mask, uint32_t key_mode,
-                          uint32_t max_q, const float* __restrict__ depth, const uint2* __restrict__ hpn,
-                          const uint32_t* __restrict__ rad, uint32_t* __restrict__ queries,
-                          uint32_t* __restrict__ count) {
-  int x = pix_x(), y = pix_y();
+struct HgEmitF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, uint32_t bucket_mask, uint32_t key_mode, uint32_t max_q, const float* __restrict__ depth, const uint2* __restrict__ hpn, const uint32_t* __restrict__ rad, uint32_t* __restrict__ queries, uint32_t* __restrict__ count) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   uint32_t q = (uint32_t)y * (uint32_t)w + (uint32_t)x;
   if (q == 0) {
@@ -84,12 +82,14 @@ __global__ void k_hg_emit(vlt_frame_params fp, int w, int h, uint32_t bucket_mas
   rec[0] = make_uint4(as_uint(pos.x), as_uint(pos.y), as_uint(pos.z), normal_encode_oct_u32(nrm));
   rec[1] = make_uint4(k.hash, k.checksum, rad[q], 0u);
 }
+};
 
 // ------------------------------------------------------------------ decay
 
 // hash_grid_decay.hlsl:13-129, one thread per bucket (16 cells).
-__global__ void k_hg_decay(uint32_t num_buckets, uint32_t* __restrict__ decay_words, uint4* __restrict__ storage) {
-  uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+struct HgDecayF {
+  static __device__ __forceinline__ void run(int x0, int y0, uint32_t num_buckets, uint32_t* __restrict__ decay_words, uint4* __restrict__ storage) {
+  uint32_t b = (uint32_t)x0 + threadIdx.x;
   if (b >= num_buckets) return;
   const uint32_t base = b * 16u;
   uint32_t mask = 0;
@@ -139,6 +139,7 @@ __global__ void k_hg_decay(uint32_t num_buckets, uint32_t* __restrict__ decay_wo
   }
   for (uint32_t i = 0; i < set; ++i) decay_words[(base >> 2) + i] = local[i];
 }
+};
 
 // ------------------------------------------------------------------ select
 
@@ -186,11 +187,9 @@ __device__ __forceinline__ uint32_t probe(const uint4* __restrict__ storage, uin
   return 17u;
 }
 
-__global__ void k_hg_sel_probe(uint32_t max_q, const uint32_t* __restrict__ queries,
-                               const uint32_t* __restrict__ count, const uint4* __restrict__ storage,
-                               uint32_t* __restrict__ selection, uint32_t frame_hash, uint32_t qbits,
-                               uint32_t* __restrict__ need_count) {
-  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+struct HgSelProbeF {
+  static __device__ __forceinline__ void run(int x0, int y0, uint32_t max_q, const uint32_t* __restrict__ queries, const uint32_t* __restrict__ count, const uint4* __restrict__ storage, uint32_t* __restrict__ selection, uint32_t frame_hash, uint32_t qbits, uint32_t* __restrict__ need_count) {
+  uint32_t q = (uint32_t)x0 + threadIdx.x;
   uint32_t n = *count;
   n = n < max_q ? n : max_q;
   if (q >= n) return;
@@ -205,22 +204,22 @@ __global__ void k_hg_sel_probe(uint32_t max_q, const uint32_t* __restrict__ quer
     atomicAdd(need_count + rec1.x, 1u);
   }
 }
+};
 
-__global__ void k_hg_sel_alloc(uint32_t num_buckets, uint32_t* __restrict__ need_count,
-                               uint32_t* __restrict__ need_offset, uint32_t* __restrict__ total) {
-  uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+struct HgSelAllocF {
+  static __device__ __forceinline__ void run(int x0, int y0, uint32_t num_buckets, uint32_t* __restrict__ need_count, uint32_t* __restrict__ need_offset, uint32_t* __restrict__ total) {
+  uint32_t b = (uint32_t)x0 + threadIdx.x;
   if (b >= num_buckets) return;
   uint32_t n = need_count[b];
   if (n == 0u) return;
   need_offset[b] = atomicAdd(total, n);
   need_count[b] = 0u;
 }
+};
 
-__global__ void k_hg_sel_scatter(uint32_t max_q, const uint32_t* __restrict__ queries,
-                                 const uint32_t* __restrict__ count, const uint4* __restrict__ storage,
-                                 uint32_t* __restrict__ need_count, const uint32_t* __restrict__ need_offset,
-                                 uint32_t* __restrict__ list) {
-  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+struct HgSelScatterF {
+  static __device__ __forceinline__ void run(int x0, int y0, uint32_t max_q, const uint32_t* __restrict__ queries, const uint32_t* __restrict__ count, const uint4* __restrict__ storage, uint32_t* __restrict__ need_count, const uint32_t* __restrict__ need_offset, uint32_t* __restrict__ list) {
+  uint32_t q = (uint32_t)x0 + threadIdx.x;
   uint32_t n = *count;
   n = n < max_q ? n : max_q;
   if (q >= n) return;
@@ -232,13 +231,12 @@ __global__ void k_hg_sel_scatter(uint32_t max_q, const uint32_t* __restrict__ qu
   uint32_t pos = atomicAdd(need_count + rec1.x, 1u);
   list[need_offset[rec1.x] + pos] = q;
 }
+};
 
 // One warp per bucket: sequential-order insertion (see the file comment).
-__global__ void k_hg_sel_resolve(uint32_t num_buckets, const uint32_t* __restrict__ queries,
-                                 uint4* __restrict__ storage, uint32_t* __restrict__ selection,
-                                 const uint32_t* __restrict__ need_count, const uint32_t* __restrict__ need_offset,
-                                 uint32_t* __restrict__ list, uint32_t frame_hash, uint32_t qbits) {
-  uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+struct HgSelResolveF {
+  static __device__ __forceinline__ void run(int x0, int y0, uint32_t num_buckets, const uint32_t* __restrict__ queries, uint4* __restrict__ storage, uint32_t* __restrict__ selection, const uint32_t* __restrict__ need_count, const uint32_t* __restrict__ need_offset, uint32_t* __restrict__ list, uint32_t frame_hash, uint32_t qbits) {
+  uint32_t warp = ((uint32_t)x0 + threadIdx.x) >> 5;
   uint32_t lane = threadIdx.x & 31u;
   if (warp >= num_buckets) return;
   uint32_t n = need_count[warp];
@@ -279,18 +277,18 @@ __global__ void k_hg_sel_resolve(uint32_t num_buckets, const uint32_t* __restric
     __syncwarp();
   }
 }
+};
 
 // ----------------------------------------------------------------- compact
 
 // hash_grid_query_compact.hlsl:23-63: block-local append in cell order, one
 // global atomic per block.
-__global__ void __launch_bounds__(256) k_hg_compact(uint32_t num_cells, uint32_t qmask,
-                                                     const uint32_t* __restrict__ selection,
-                                                     uint32_t* __restrict__ idx, uint32_t* __restrict__ addr,
-                                                     uint32_t* __restrict__ count) {
-  __shared__ uint32_t warp_cnt[8];
+struct HgCompactF {
+  static __device__ __forceinline__ void run(int x0, int y0, uint32_t num_cells, uint32_t qmask, const uint32_t* __restrict__ selection, uint32_t* __restrict__ idx, uint32_t* __restrict__ addr, uint32_t* __restrict__ count) {
+  __shared__ uint32_t warp_cnt[kMaxThreads / 32];
   __shared__ uint32_t block_base;
-  uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n_warps = (int)blockDim.x >> 5;
+  uint32_t c = (uint32_t)x0 + threadIdx.x;
   uint32_t sel = c < num_cells ? selection[c] : 0u;
   uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
   uint32_t bal = __ballot_sync(0xFFFFFFFFu, sel != 0u);
@@ -298,7 +296,7 @@ __global__ void __launch_bounds__(256) k_hg_compact(uint32_t num_cells, uint32_t
   __syncthreads();
   if (threadIdx.x == 0) {
     uint32_t tot = 0;
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < n_warps; ++k) {
       uint32_t v = warp_cnt[k];
       warp_cnt[k] = tot;
       tot += v;
@@ -312,14 +310,14 @@ __global__ void __launch_bounds__(256) k_hg_compact(uint32_t num_cells, uint32_t
     addr[pos] = c;
   }
 }
+};
 
 // ------------------------------------------------------------------ update
 
 // hash_grid_raygen.hlsl:71-86 with the traced radiance supplied by the query.
-__global__ void k_hg_update(const uint32_t* __restrict__ queries, const uint32_t* __restrict__ idx,
-                            const uint32_t* __restrict__ addr, const uint32_t* __restrict__ count,
-                            uint4* __restrict__ storage, uint8_t* __restrict__ decay) {
-  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+struct HgUpdateF {
+  static __device__ __forceinline__ void run(int x0, int y0, const uint32_t* __restrict__ queries, const uint32_t* __restrict__ idx, const uint32_t* __restrict__ addr, const uint32_t* __restrict__ count, uint4* __restrict__ storage, uint8_t* __restrict__ decay) {
+  uint32_t k = (uint32_t)x0 + threadIdx.x;
   if (k >= *count) return;
   uint32_t q = idx[k], a = addr[k];
   f3 L = unpack_r11g11b10(queries[(size_t)q * Q_WORDS + Q_RAD]);
@@ -330,14 +328,13 @@ __global__ void k_hg_update(const uint32_t* __restrict__ queries, const uint32_t
   storage[a] = make_uint4(cell.x, as_uint(bl.x), as_uint(bl.y), as_uint(bl.z));
   decay[a] = 10;
 }
+};
 
 // ------------------------------------------------------------------- find
 
-__global__ void k_hg_find(vlt_frame_params fp, uint32_t bucket_mask, uint32_t key_mode,
-                          const uint4* __restrict__ storage, uint32_t n, const float* __restrict__ pos,
-                          const float* __restrict__ nrm, uint32_t* __restrict__ out_addr,
-                          float4* __restrict__ out_rad) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+struct HgFindF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, uint32_t bucket_mask, uint32_t key_mode, const uint4* __restrict__ storage, uint32_t n, const float* __restrict__ pos, const float* __restrict__ nrm, uint32_t* __restrict__ out_addr, float4* __restrict__ out_rad) {
+  uint32_t i = (uint32_t)x0 + threadIdx.x;
   if (i >= n) return;
   f3 p = mk3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
   f3 nn = mk3(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
@@ -358,60 +355,57 @@ __global__ void k_hg_find(vlt_frame_params fp, uint32_t bucket_mask, uint32_t ke
   if (out_rad)
     out_rad[i] = make_float4(as_float(cell.y), as_float(cell.z), as_float(cell.w), found != 0xFFFFFFFFu ? 1.0f : 0.0f);
 }
+};
 
 // --------------------------------------------------------------- launchers
 
-void launch_hg_emit(const vlt_frame_params& fp, int w, int h, const HashGridDims& d, uint32_t key_mode,
-                    const float* depth, const uint32_t* hpn, const uint32_t* rad, uint32_t* queries,
-                    uint32_t* count, cudaStream_t s) {
-  dim3 blk(32, 4, 1);
-  k_hg_emit<<<grid2d(w, h, blk), blk, 0, s>>>(fp, w, h, d.num_buckets() - 1u, key_mode, d.max_queries, depth,
-                                               (const uint2*)hpn, rad, queries, count);
+void launch_hg_emit(const Exec& ex, const vlt_frame_params& fp, int w, int h, const HashGridDims& d,
+                    uint32_t key_mode, const float* depth, const uint32_t* hpn, const uint32_t* rad,
+                    uint32_t* queries, uint32_t* count) {
+  launch2d<HgEmitF>(ex, "hg_emit", w, h, fp, w, h, d.num_buckets() - 1u, key_mode, d.max_queries, depth,
+                    (const uint2*)hpn, rad, queries, count);
 }
 
-void launch_hg_decay(const HashGridDims& d, uint8_t* decay, uint32_t* storage, cudaStream_t s) {
+void launch_hg_decay(const Exec& ex, const HashGridDims& d, uint8_t* decay, uint32_t* storage) {
   uint32_t nb = d.num_buckets();
-  k_hg_decay<<<(nb + 127) / 128, 128, 0, s>>>(nb, (uint32_t*)decay, (uint4*)storage);
+  launch1d<HgDecayF>(ex, "hg_decay", nb, nb, (uint32_t*)decay, (uint4*)storage);
 }
 
-void launch_hg_select(const HashGridDims& d, const uint32_t* queries, const uint32_t* count, uint32_t* storage,
-                      uint32_t* selection, uint32_t frame_hash, void* scratch, cudaStream_t s) {
+void launch_hg_select(const Exec& ex, const HashGridDims& d, const uint32_t* queries, const uint32_t* count,
+                      uint32_t* storage, uint32_t* selection, uint32_t frame_hash, void* scratch) {
   SelectScratch sc = carve(d, scratch);
   uint32_t nb = d.num_buckets();
   uint32_t qb = d.query_bits();
-  cudaMemsetAsync(sc.need_count, 0, (size_t)nb * 4, s);
-  cudaMemsetAsync(sc.total, 0, 4, s);
+  ex_fill32(ex, sc.need_count, 0u, (size_t)nb * 4);
+  ex_fill32(ex, sc.total, 0u, 4);
   uint32_t nq = d.max_queries;
-  k_hg_sel_probe<<<(nq + 255) / 256, 256, 0, s>>>(nq, queries, count, (const uint4*)storage, selection, frame_hash,
-                                                   qb, sc.need_count);
-  k_hg_sel_alloc<<<(nb + 255) / 256, 256, 0, s>>>(nb, sc.need_count, sc.need_offset, sc.total);
-  k_hg_sel_scatter<<<(nq + 255) / 256, 256, 0, s>>>(nq, queries, count, (const uint4*)storage, sc.need_count,
-                                                     sc.need_offset, sc.list);
-  uint64_t threads = (uint64_t)nb * 32u;
-  k_hg_sel_resolve<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(nb, queries, (uint4*)storage, selection,
-                                                                      sc.need_count, sc.need_offset, sc.list,
-                                                                      frame_hash, qb);
+  launch1d<HgSelProbeF>(ex, "hg_select", nq, nq, queries, count, (const uint4*)storage, selection, frame_hash, qb,
+                        sc.need_count);
+  launch1d<HgSelAllocF>(ex, "hg_select", nb, nb, sc.need_count, sc.need_offset, sc.total);
+  launch1d<HgSelScatterF>(ex, "hg_select", nq, nq, queries, count, (const uint4*)storage, sc.need_count,
+                          (const uint32_t*)sc.need_offset, sc.list);
+  launch1d<HgSelResolveF>(ex, "hg_select", nb * 32u, nb, queries, (uint4*)storage, selection,
+                          (const uint32_t*)sc.need_count, (const uint32_t*)sc.need_offset, sc.list, frame_hash, qb);
 }
 
-void launch_hg_compact(const HashGridDims& d, const uint32_t* selection, uint32_t* idx, uint32_t* addr,
-                       uint32_t* count, cudaStream_t s) {
+void launch_hg_compact(const Exec& ex, const HashGridDims& d, const uint32_t* selection, uint32_t* idx,
+                       uint32_t* addr, uint32_t* count) {
   uint32_t nc = d.num_cells();
   uint32_t qmask = (1u << d.query_bits()) - 1u;
-  k_hg_compact<<<(nc + 255) / 256, 256, 0, s>>>(nc, qmask, selection, idx, addr, count);
+  launch1d<HgCompactF>(ex, "hg_compact", nc, nc, qmask, selection, idx, addr, count);
 }
 
-void launch_hg_update(const HashGridDims& d, const uint32_t* queries, const uint32_t* idx, const uint32_t* addr,
-                      const uint32_t* count, uint32_t* storage, uint8_t* decay, cudaStream_t s) {
+void launch_hg_update(const Exec& ex, const HashGridDims& d, const uint32_t* queries, const uint32_t* idx,
+                      const uint32_t* addr, const uint32_t* count, uint32_t* storage, uint8_t* decay) {
   uint32_t nmax = d.max_queries < d.num_cells() ? d.max_queries : d.num_cells();
-  k_hg_update<<<(nmax + 255) / 256, 256, 0, s>>>(queries, idx, addr, count, (uint4*)storage, decay);
+  launch1d<HgUpdateF>(ex, "hg_update", nmax, queries, idx, addr, count, (uint4*)storage, decay);
 }
 
-void launch_hg_find(const vlt_frame_params& fp, const HashGridDims& d, uint32_t key_mode, const uint32_t* storage,
-                    uint32_t n, const float* pos, const float* nrm, uint32_t* out_addr, float* out_rad,
-                    cudaStream_t s) {
-  if (n == 0) return;
-  k_hg_find<<<(n + 255) / 256, 256, 0, s>>>(fp, d.num_buckets() - 1u, key_mode, (const uint4*)storage, n, pos, nrm,
-                                            out_addr, (float4*)out_rad);
+void launch_hg_find(const Exec& ex, const vlt_frame_params& fp, const HashGridDims& d, uint32_t key_mode,
+                    const uint32_t* storage, uint32_t n, const float* pos, const float* nrm, uint32_t* out_addr,
+                    float* out_rad) {
+  launch1d<HgFindF>(ex, "hg_find", n, fp, d.num_buckets() - 1u, key_mode, (const uint4*)storage, n, pos, nrm,
+                    out_addr, (float4*)out_rad);
 }
 
 // ------------------------------------------- query select without allocation
@@ -464,6 +458,8 @@ extern "C" vlt_status vlt_hg_query_select_noalloc(uint32_t log2_buckets, uint32_
   }
   // launch_hg_select clears the per-bucket counters it needs at zero before use;
   // the rest of the scratch is fully rewritten before it is read.
-  launch_hg_select(d, queries, query_count, rw_storage, rw_selection, frame_hash, scratch, (cudaStream_t)stream);
+  Exec ex;
+  ex.stream = (cudaStream_t)stream;
+  launch_hg_select(ex, d, queries, query_count, rw_storage, rw_selection, frame_hash, scratch);
   return cuda_status(cudaGetLastError());
 }

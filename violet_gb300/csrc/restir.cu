@@ -11,10 +11,9 @@ namespace vlt {
 // ------------------------------------------------------------- surface
 
 // Decodes once per frame what the gathers would otherwise re-derive per tap.
-__global__ void __launch_bounds__(128) k_surface(vlt_frame_params fp, int w, int h, const float* __restrict__ depth,
-                                                  const uint32_t* __restrict__ g, float4* __restrict__ nd,
-                                                  float4* __restrict__ pr, float4* __restrict__ fz) {
-  int x = pix_x(), y = pix_y();
+struct SurfaceF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, const float* __restrict__ depth, const uint32_t* __restrict__ g, float4* __restrict__ nd, float4* __restrict__ pr, float4* __restrict__ fz) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   size_t plane = (size_t)w * h;
@@ -27,6 +26,7 @@ __global__ void __launch_bounds__(128) k_surface(vlt_frame_params fp, int w, int
   pr[i] = make_float4(p.x, p.y, p.z, gbuffer_roughness(e1));
   fz[i] = make_float4(f0.x, f0.y, f0.z, f16tof32(g[2 * plane + i] & 0xFFFFu));
 }
+};
 
 // ---------------------------------------------------------------- AO gen
 
@@ -59,13 +59,10 @@ struct AoStore<FORM_F32> {
 
 // raytraced_ao_gen.hlsl:18-81.
 template <class Geo, int FORM>
-__global__ void __launch_bounds__(128) k_ao_gen(vlt_frame_params fp, int w, int h, Geo geo,
-                                                 const uint2* __restrict__ hit_pos_normal,
-                                                 const typename AoStore<FORM>::Hist* __restrict__ prev_ao,
-                                                 typename AoStore<FORM>::Hist* __restrict__ ao,
-                                                 uint32_t has_new_sample, uint32_t has_prev_frame, float radius_ws) {
+struct AoGenF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, Geo geo, const uint2* __restrict__ hit_pos_normal, const typename AoStore<FORM>::Hist* __restrict__ prev_ao, typename AoStore<FORM>::Hist* __restrict__ ao, uint32_t has_new_sample, uint32_t has_prev_frame, float radius_ws) {
   using S = AoStore<FORM>;
-  int x = pix_x(), y = pix_y();
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float depth = geo.dep(i);
@@ -102,6 +99,7 @@ __global__ void __launch_bounds__(128) k_ao_gen(vlt_frame_params fp, int w, int 
   }
   ao[i] = S::pack(mk2(hx, ha));
 }
+};
 
 // ---------------------------------------------------------------- AO filter
 
@@ -110,11 +108,10 @@ __global__ void __launch_bounds__(128) k_ao_gen(vlt_frame_params fp, int w, int 
 // out-of-range coordinate, which reads as zero). Only the x channel is needed
 // downstream, so only it is filtered and stored.
 template <int FORM>
-__global__ void __launch_bounds__(128) k_ao_filter(int w, int h, const float* __restrict__ depth_buf,
-                                                    const typename AoStore<FORM>::Hist* __restrict__ ao,
-                                                    typename AoStore<FORM>::Filt* __restrict__ out) {
+struct AoFilterF {
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, const float* __restrict__ depth_buf, const typename AoStore<FORM>::Hist* __restrict__ ao, typename AoStore<FORM>::Filt* __restrict__ out) {
   using S = AoStore<FORM>;
-  int x = pix_x(), y = pix_y();
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float depth = depth_buf[i];
@@ -151,6 +148,7 @@ __global__ void __launch_bounds__(128) k_ao_filter(int w, int h, const float* __
   float mn = fmin_(fmin_(col_min[0], col_min[1]), col_min[2]);
   out[i] = S::pack_filt(lerpf(med, mn, 0.5f));
 }
+};
 
 // ------------------------------------------------------ diffuse temporal
 
@@ -187,15 +185,9 @@ __device__ __forceinline__ DiffF32 diff_f32(uint32_t M, float W, f3 pos, f3 nrm,
 // ind_diff_temporal_resample.hlsl:49-200 in the f32 storage form: the sample is kept
 // decoded (the hit normal of an empty HitPosNormal decodes to (0,0,-1)).
 template <class Geo>
-__global__ void __launch_bounds__(128) k_diff_temporal_f32(vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo,
-                                                            const float* __restrict__ prev_depth,
-                                                            const uint2* __restrict__ new_hpn,
-                                                            const uint32_t* __restrict__ new_rad,
-                                                            const float* __restrict__ new_pdf,
-                                                            const DiffF32* __restrict__ prev_rsv,
-                                                            DiffF32* __restrict__ out, uint32_t frame_rand,
-                                                            uint32_t has_prev_frame, uint32_t has_new_sample) {
-  int x = pix_x(), y = pix_y();
+struct DiffTemporalF32F {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo, const float* __restrict__ prev_depth, const uint2* __restrict__ new_hpn, const uint32_t* __restrict__ new_rad, const float* __restrict__ new_pdf, const DiffF32* __restrict__ prev_rsv, DiffF32* __restrict__ out, uint32_t frame_rand, uint32_t has_prev_frame, uint32_t has_new_sample) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   f3 pos = geo.pos(x, y, i);
@@ -258,18 +250,13 @@ __global__ void __launch_bounds__(128) k_diff_temporal_f32(vlt_frame_params fp, 
   }
   out[i] = diff_f32(M, W, hp, hn, rad);
 }
+};
 
 // ind_diff_temporal_resample.hlsl:49-200. Record = {M8|W24, HitPosNormal.xy, R11G11B10}.
 template <class Geo>
-__global__ void __launch_bounds__(128) k_diff_temporal(vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo,
-                                                        const float* __restrict__ prev_depth,
-                                                        const uint2* __restrict__ new_hpn,
-                                                        const uint32_t* __restrict__ new_rad,
-                                                        const float* __restrict__ new_pdf,
-                                                        const uint4* __restrict__ prev_rsv, uint4* __restrict__ out,
-                                                        uint32_t frame_rand, uint32_t has_prev_frame,
-                                                        uint32_t has_new_sample) {
-  int x = pix_x(), y = pix_y();
+struct DiffTemporalF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo, const float* __restrict__ prev_depth, const uint2* __restrict__ new_hpn, const uint32_t* __restrict__ new_rad, const float* __restrict__ new_pdf, const uint4* __restrict__ prev_rsv, uint4* __restrict__ out, uint32_t frame_rand, uint32_t has_prev_frame, uint32_t has_new_sample) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   f3 pos = geo.pos(x, y, i);
@@ -325,6 +312,7 @@ __global__ void __launch_bounds__(128) k_diff_temporal(vlt_frame_params fp, int 
   }
   out[i] = make_uint4(rsv_encode_32b(M, W), h0, h1, rad);
 }
+};
 
 // ------------------------------------------------------- diffuse spatial
 
@@ -378,14 +366,10 @@ __device__ __forceinline__ void store_empty_diff(DiffF32* out, size_t i) {
 // ind_diff_spatial_resample.hlsl:94-337 (golden-spiral pattern, AO-guided and
 // adaptive radius, plane-distance test, Jacobian clamped to [0, 1]).
 template <class Geo, int FORM>
-__global__ void __launch_bounds__(128) k_diff_spatial(vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo,
-                                                       const typename AoStore<FORM>::Filt* __restrict__ ao_tex,
-                                                       const typename DiffStore<FORM>::Rec* __restrict__ in,
-                                                       typename DiffStore<FORM>::Rec* __restrict__ out,
-                                                       typename DiffStore<FORM>::Light* __restrict__ lighting,
-                                                       uint32_t frame_rand) {
+struct DiffSpatialF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo, const typename AoStore<FORM>::Filt* __restrict__ ao_tex, const typename DiffStore<FORM>::Rec* __restrict__ in, typename DiffStore<FORM>::Rec* __restrict__ out, typename DiffStore<FORM>::Light* __restrict__ lighting, uint32_t frame_rand) {
   using S = DiffStore<FORM>;
-  int x = pix_x(), y = pix_y();
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float depth = geo.dep(i);
@@ -457,6 +441,7 @@ __global__ void __launch_bounds__(128) k_diff_spatial(vlt_frame_params fp, int w
     lighting[i] = S::light(l);
   }
 }
+};
 
 // --------------------------------------------------- specular target function
 
@@ -529,17 +514,9 @@ struct SpecTarget {
 // ind_spec_temporal_resample.hlsl:146-362 (VNDF source pdf, BRDF target function,
 // balance-heuristic MIS between previous and current domains).
 template <class Geo>
-__global__ void __launch_bounds__(128) k_spec_temporal(vlt_frame_params fp, int w, int h, uint32_t m_cap, Geo geo,
-                                                        Geo prev_geo, const float* __restrict__ prev_depth,
-                                                        const uint2* __restrict__ prev_rsv,
-                                                        const float4* __restrict__ prev_hp,
-                                                        const uint32_t* __restrict__ prev_rad,
-                                                        const float4* __restrict__ new_hp,
-                                                        const uint32_t* __restrict__ new_rad,
-                                                        uint2* __restrict__ out_rsv, float4* __restrict__ out_hp,
-                                                        uint32_t* __restrict__ out_rad, uint32_t frame_rand,
-                                                        uint32_t has_prev_frame) {
-  int x = pix_x(), y = pix_y();
+struct SpecTemporalF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, uint32_t m_cap, Geo geo, Geo prev_geo, const float* __restrict__ prev_depth, const uint2* __restrict__ prev_rsv, const float4* __restrict__ prev_hp, const uint32_t* __restrict__ prev_rad, const float4* __restrict__ new_hp, const uint32_t* __restrict__ new_rad, uint2* __restrict__ out_rsv, float4* __restrict__ out_hp, uint32_t* __restrict__ out_rad, uint32_t frame_rand, uint32_t has_prev_frame) {
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float depth = geo.dep(i);
@@ -619,6 +596,7 @@ __global__ void __launch_bounds__(128) k_spec_temporal(vlt_frame_params fp, int 
   out_hp[i] = make_float4(rhp.x, rhp.y, rhp.z, rtf);
   out_rad[i] = rrad_bits;
 }
+};
 
 // ------------------------------------------------------- specular spatial
 
@@ -660,14 +638,50 @@ __device__ __forceinline__ void store_spec_light(float4* l, uint16_t*, size_t i,
 }
 
 template <class Geo, class Light>
-__global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo,
-                                                       const uint2* __restrict__ rsv,
-                                                       const float4* __restrict__ hp_tex,
-                                                       const uint32_t* __restrict__ rad_tex,
-                                                       Light* __restrict__ lighting, uint16_t* __restrict__ ray_len_out,
-                                                       uint2* __restrict__ out_rsv, float4* __restrict__ out_hp,
-                                                       uint32_t* __restrict__ out_rad, uint32_t frame_rand) {
-  int x = pix_x(), y = pix_y();
+struct SpecSpatialF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo, const uint2* __restrict__ rsv, const float4* __restrict__ hp_tex, const uint32_t* __restrict__ rad_tex, Light* __restrict__ lighting, uint16_t* __restrict__ ray_len_out, uint2* __restrict__ out_rsv, float4* __restrict__ out_hp, uint32_t* __restrict__ out_rad, uint32_t frame_rand) {
+  // The tap count of a pixel is uint(roughness * taps), so neighbouring lanes can
+  // run very different loop lengths. The pixels of the tile are therefore
+  // reordered by tap count (counting sort in shared memory) before the loop, so a
+  // warp's lanes run similar counts. Each pixel's result does not depend on which
+  // lane computes it. Needs 64..256 threads per block.
+  __shared__ uint32_t s_count[64];
+  __shared__ uint32_t s_offset[64];
+  __shared__ uint8_t s_order[kMaxThreads];
+  const int bx = (int)blockDim.x;
+  const int tid = (int)threadIdx.y * bx + (int)threadIdx.x;
+  {
+    int px = x0 + (int)threadIdx.x, py = y0 + (int)threadIdx.y;
+    uint32_t key = 0;
+    if (inb(px, py, w, h)) {
+      size_t pi = (size_t)py * w + px;
+      if (geo.dep(pi) != 0.0f) {
+        uint32_t nt = f2u_rz(0.0f + geo.rough(pi) * ((float)kn.taps - 0.0f));
+        key = nt < 63u ? nt : 63u;
+      }
+    }
+    if (tid < 64) s_count[tid] = 0u;
+    __syncthreads();
+    uint32_t slot = atomicAdd(&s_count[key], 1u);
+    __syncthreads();
+    if (tid < 32) {
+      uint32_t a = s_count[2 * tid], b = s_count[2 * tid + 1];
+      uint32_t incl = a + b;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (tid >= d) incl += v;
+      }
+      uint32_t excl = incl - (a + b);
+      s_offset[2 * tid] = excl;
+      s_offset[2 * tid + 1] = excl + a;
+    }
+    __syncthreads();
+    s_order[s_offset[key] + slot] = (uint8_t)tid;
+    __syncthreads();
+  }
+  const int lp = s_order[tid];
+  int x = x0 + lp % bx, y = y0 + lp / bx;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float depth = geo.dep(i);
@@ -778,13 +792,12 @@ __global__ void __launch_bounds__(128) k_spec_spatial(vlt_frame_params fp, int w
     ray_len_out[i] = (uint16_t)f32tof16(ray_len);
   }
 }
+};
 
 // ------------------------------------------------------------- launchers
 
-static const dim3 kBlock(32, 4, 1);
-
 static GeoRaw raw_geo(const GeoArgs& a, int w, int h) {
-  GeoRaw g = {a.depth, a.gbuf, a.inv_vp, w, h};
+  GeoRaw g = make_geo_raw(a.depth, a.gbuf, a.inv_vp, w, h);
   return g;
 }
 static GeoSurface surf_geo(const GeoArgs& a, int w, int h) {
@@ -792,103 +805,107 @@ static GeoSurface surf_geo(const GeoArgs& a, int w, int h) {
   return g;
 }
 
-// Instantiates KERNEL<Geo, ...> for the geometry source in `ga`.
+// Runs the statement with `geo` (and its type `Geo`) bound to the geometry source
+// of `ga`.
 #define VLT_GEO_DISPATCH(ga, ...)              \
   do {                                         \
     if ((ga).nd) {                             \
+      using Geo = GeoSurface;                  \
       GeoSurface geo = surf_geo(ga, w, h);     \
       __VA_ARGS__;                             \
     } else {                                   \
+      using Geo = GeoRaw;                      \
       GeoRaw geo = raw_geo(ga, w, h);          \
       __VA_ARGS__;                             \
     }                                          \
   } while (0)
 
-void launch_surface(const vlt_frame_params& fp, int w, int h, const float* depth, const uint32_t* gbuf, float4* nd,
-                    float4* pr, float4* fz, cudaStream_t s) {
-  k_surface<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(fp, w, h, depth, gbuf, nd, pr, fz);
+void launch_surface(const Exec& ex, const vlt_frame_params& fp, int w, int h, const float* depth,
+                    const uint32_t* gbuf, float4* nd, float4* pr, float4* fz) {
+  launch2d<SurfaceF>(ex, "surface", w, h, fp, w, h, depth, gbuf, nd, pr, fz);
 }
 
-void launch_ao_gen(int form, const vlt_frame_params& fp, int w, int h, const GeoArgs& ga, const uint32_t* hpn,
-                   const void* prev_ao, void* ao, uint32_t has_new, uint32_t has_prev, float radius, cudaStream_t s) {
-  dim3 g = grid2d(w, h, kBlock);
+void launch_ao_gen(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const GeoArgs& ga,
+                   const uint32_t* hpn, const void* prev_ao, void* ao, uint32_t has_new, uint32_t has_prev,
+                   float radius) {
   if (form == FORM_F32)
-    VLT_GEO_DISPATCH(ga, (k_ao_gen<decltype(geo), FORM_F32><<<g, kBlock, 0, s>>>(
-                             fp, w, h, geo, (const uint2*)hpn, (const float2*)prev_ao, (float2*)ao, has_new, has_prev,
-                             radius)));
+    VLT_GEO_DISPATCH(ga, (launch2d<AoGenF<Geo, FORM_F32>>(ex, "ao_gen", w, h, fp, w, h, geo, (const uint2*)hpn,
+                                                         (const float2*)prev_ao, (float2*)ao, has_new, has_prev,
+                                                         radius)));
   else
-    VLT_GEO_DISPATCH(ga, (k_ao_gen<decltype(geo), FORM_REF><<<g, kBlock, 0, s>>>(
-                             fp, w, h, geo, (const uint2*)hpn, (const uint32_t*)prev_ao, (uint32_t*)ao, has_new,
-                             has_prev, radius)));
+    VLT_GEO_DISPATCH(ga, (launch2d<AoGenF<Geo, FORM_REF>>(ex, "ao_gen", w, h, fp, w, h, geo, (const uint2*)hpn,
+                                                         (const uint32_t*)prev_ao, (uint32_t*)ao, has_new, has_prev,
+                                                         radius)));
 }
 
-void launch_ao_filter(int form, int w, int h, const float* depth, const void* ao, void* out, cudaStream_t s) {
+void launch_ao_filter(const Exec& ex, int form, int w, int h, const float* depth, const void* ao, void* out) {
   if (form == FORM_F32)
-    k_ao_filter<FORM_F32><<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, depth, (const float2*)ao, (float*)out);
+    launch2d<AoFilterF<FORM_F32>>(ex, "ao_filter", w, h, w, h, depth, (const float2*)ao, (float*)out);
   else
-    k_ao_filter<FORM_REF><<<grid2d(w, h, kBlock), kBlock, 0, s>>>(w, h, depth, (const uint32_t*)ao, (uint16_t*)out);
+    launch2d<AoFilterF<FORM_REF>>(ex, "ao_filter", w, h, w, h, depth, (const uint32_t*)ao, (uint16_t*)out);
 }
 
-void launch_diff_temporal(int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
-                          const float* prev_depth, const uint32_t* new_hpn, const uint32_t* new_rad,
-                          const float* new_pdf, const void* prev_rsv, void* out, uint32_t frame_rand,
-                          uint32_t has_prev, uint32_t has_new, cudaStream_t s) {
-  dim3 g = grid2d(w, h, kBlock);
+void launch_diff_temporal(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn,
+                          const GeoArgs& ga, const float* prev_depth, const uint32_t* new_hpn,
+                          const uint32_t* new_rad, const float* new_pdf, const void* prev_rsv, void* out,
+                          uint32_t frame_rand, uint32_t has_prev, uint32_t has_new) {
   if (form == FORM_F32)
-    VLT_GEO_DISPATCH(ga, (k_diff_temporal_f32<<<g, kBlock, 0, s>>>(
-                             fp, w, h, kn, geo, prev_depth, (const uint2*)new_hpn, new_rad, new_pdf,
-                             (const DiffF32*)prev_rsv, (DiffF32*)out, frame_rand, has_prev, has_new)));
+    VLT_GEO_DISPATCH(ga, (launch2d<DiffTemporalF32F<Geo>>(ex, "diff_temporal", w, h, fp, w, h, kn, geo, prev_depth,
+                                                          (const uint2*)new_hpn, new_rad, new_pdf,
+                                                          (const DiffF32*)prev_rsv, (DiffF32*)out, frame_rand,
+                                                          has_prev, has_new)));
   else
-    VLT_GEO_DISPATCH(ga, (k_diff_temporal<<<g, kBlock, 0, s>>>(fp, w, h, kn, geo, prev_depth, (const uint2*)new_hpn,
-                                                                new_rad, new_pdf, (const uint4*)prev_rsv,
-                                                                (uint4*)out, frame_rand, has_prev, has_new)));
+    VLT_GEO_DISPATCH(ga, (launch2d<DiffTemporalF<Geo>>(ex, "diff_temporal", w, h, fp, w, h, kn, geo, prev_depth,
+                                                       (const uint2*)new_hpn, new_rad, new_pdf,
+                                                       (const uint4*)prev_rsv, (uint4*)out, frame_rand, has_prev,
+                                                       has_new)));
 }
 
-void launch_diff_spatial(int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
-                         const void* ao, const void* in, void* out, void* lighting, uint32_t frame_rand,
-                         cudaStream_t s) {
-  dim3 g = grid2d(w, h, kBlock);
+void launch_diff_spatial(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn,
+                         const GeoArgs& ga, const void* ao, const void* in, void* out, void* lighting,
+                         uint32_t frame_rand) {
   if (form == FORM_F32)
-    VLT_GEO_DISPATCH(ga, (k_diff_spatial<decltype(geo), FORM_F32><<<g, kBlock, 0, s>>>(
-                             fp, w, h, kn, geo, (const float*)ao, (const DiffF32*)in, (DiffF32*)out, (float4*)lighting,
-                             frame_rand)));
+    VLT_GEO_DISPATCH(ga, (launch2d<DiffSpatialF<Geo, FORM_F32>>(ex, "diff_spatial", w, h, fp, w, h, kn, geo,
+                                                               (const float*)ao, (const DiffF32*)in, (DiffF32*)out,
+                                                               (float4*)lighting, frame_rand)));
   else
-    VLT_GEO_DISPATCH(ga, (k_diff_spatial<decltype(geo), FORM_REF><<<g, kBlock, 0, s>>>(
-                             fp, w, h, kn, geo, (const uint16_t*)ao, (const uint4*)in, (uint4*)out,
-                             (uint32_t*)lighting, frame_rand)));
+    VLT_GEO_DISPATCH(ga, (launch2d<DiffSpatialF<Geo, FORM_REF>>(ex, "diff_spatial", w, h, fp, w, h, kn, geo,
+                                                               (const uint16_t*)ao, (const uint4*)in, (uint4*)out,
+                                                               (uint32_t*)lighting, frame_rand)));
 }
 
-void launch_spec_temporal(const vlt_frame_params& fp, int w, int h, uint32_t m_cap, const GeoArgs& ga,
-                          const GeoArgs& prev_ga, const float* prev_depth, const uint32_t* prev_rsv,
-                          const float* prev_hp, const uint32_t* prev_rad, const float* new_hp,
-                          const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
-                          uint32_t frame_rand, uint32_t has_prev, cudaStream_t s) {
+void launch_spec_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h, uint32_t m_cap,
+                          const GeoArgs& ga, const GeoArgs& prev_ga, const float* prev_depth,
+                          const uint32_t* prev_rsv, const float* prev_hp, const uint32_t* prev_rad,
+                          const float* new_hp, const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp,
+                          uint32_t* out_rad, uint32_t frame_rand, uint32_t has_prev) {
   if (ga.nd)
-    k_spec_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
-        fp, w, h, m_cap, surf_geo(ga, w, h), surf_geo(prev_ga, w, h), prev_depth, (const uint2*)prev_rsv,
-        (const float4*)prev_hp, prev_rad, (const float4*)new_hp, new_rad, (uint2*)out_rsv, (float4*)out_hp, out_rad,
-        frame_rand, has_prev);
+    launch2d<SpecTemporalF<GeoSurface>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, surf_geo(ga, w, h),
+                                        surf_geo(prev_ga, w, h), prev_depth, (const uint2*)prev_rsv,
+                                        (const float4*)prev_hp, prev_rad, (const float4*)new_hp, new_rad,
+                                        (uint2*)out_rsv, (float4*)out_hp, out_rad, frame_rand, has_prev);
   else
-    k_spec_temporal<<<grid2d(w, h, kBlock), kBlock, 0, s>>>(
-        fp, w, h, m_cap, raw_geo(ga, w, h), raw_geo(prev_ga, w, h), prev_depth, (const uint2*)prev_rsv,
-        (const float4*)prev_hp, prev_rad, (const float4*)new_hp, new_rad, (uint2*)out_rsv, (float4*)out_hp, out_rad,
-        frame_rand, has_prev);
+    launch2d<SpecTemporalF<GeoRaw>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, raw_geo(ga, w, h),
+                                    raw_geo(prev_ga, w, h), prev_depth, (const uint2*)prev_rsv,
+                                    (const float4*)prev_hp, prev_rad, (const float4*)new_hp, new_rad,
+                                    (uint2*)out_rsv, (float4*)out_hp, out_rad, frame_rand, has_prev);
 }
 
-void launch_spec_spatial(int form, const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn, const GeoArgs& ga,
-                         const uint32_t* rsv, const float* hp, const uint32_t* rad, void* lighting, uint16_t* ray_len,
-                         uint32_t* out_rsv, float* out_hp, uint32_t* out_rad, uint32_t frame_rand, cudaStream_t s) {
-  dim3 g = grid2d(w, h, kBlock);
+void launch_spec_spatial(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn,
+                         const GeoArgs& ga, const uint32_t* rsv, const float* hp, const uint32_t* rad,
+                         void* lighting, uint16_t* ray_len, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
+                         uint32_t frame_rand) {
   if (form == FORM_F32)
-    VLT_GEO_DISPATCH(ga, (k_spec_spatial<<<g, kBlock, 0, s>>>(fp, w, h, kn, geo, (const uint2*)rsv,
-                                                               (const float4*)hp, rad, (float4*)lighting, nullptr,
-                                                               (uint2*)out_rsv, (float4*)out_hp, out_rad,
-                                                               frame_rand)));
+    VLT_GEO_DISPATCH(ga, (launch2d<SpecSpatialF<Geo, float4>>(ex, "spec_spatial", w, h, fp, w, h, kn, geo,
+                                                              (const uint2*)rsv, (const float4*)hp, rad,
+                                                              (float4*)lighting, (uint16_t*)nullptr,
+                                                              (uint2*)out_rsv, (float4*)out_hp, out_rad,
+                                                              frame_rand)));
   else
-    VLT_GEO_DISPATCH(ga, (k_spec_spatial<<<g, kBlock, 0, s>>>(fp, w, h, kn, geo, (const uint2*)rsv,
-                                                               (const float4*)hp, rad, (uint32_t*)lighting, ray_len,
-                                                               (uint2*)out_rsv, (float4*)out_hp, out_rad,
-                                                               frame_rand)));
+    VLT_GEO_DISPATCH(ga, (launch2d<SpecSpatialF<Geo, uint32_t>>(ex, "spec_spatial", w, h, fp, w, h, kn, geo,
+                                                                (const uint2*)rsv, (const float4*)hp, rad,
+                                                                (uint32_t*)lighting, ray_len, (uint2*)out_rsv,
+                                                                (float4*)out_hp, out_rad, frame_rand)));
 }
 
 #undef VLT_GEO_DISPATCH

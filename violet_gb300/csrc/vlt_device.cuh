@@ -147,7 +147,7 @@ __device__ __forceinline__ f3 f0_from_layer0(uint32_t e0) {
 struct GeoRaw {
   const float* __restrict__ depth;
   const uint32_t* __restrict__ g;
-  const float* inv_vp;  // may be null when positions are not needed
+  float inv_vp[16];  // inverse view-projection, held by value (kernel parameter space)
   int w, h;
   __device__ __forceinline__ size_t plane() const { return (size_t)w * h; }
   __device__ __forceinline__ float dep(size_t i) const { return depth[i]; }
@@ -171,6 +171,17 @@ struct GeoRaw {
     *f0v = f0_from_layer0(e0);
   }
 };
+
+// inv_vp may be null when no pass reads positions (the matrix is then zero).
+inline GeoRaw make_geo_raw(const float* depth, const uint32_t* g, const float* inv_vp, int w, int h) {
+  GeoRaw r;
+  r.depth = depth;
+  r.g = g;
+  for (int k = 0; k < 16; ++k) r.inv_vp[k] = inv_vp ? inv_vp[k] : 0.0f;
+  r.w = w;
+  r.h = h;
+  return r;
+}
 
 struct GeoSurface {
   const float4* __restrict__ nd;

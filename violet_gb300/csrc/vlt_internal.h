@@ -6,6 +6,7 @@
 
 #include "../../include/vlt.h"
 #include "vlt_device.cuh"
+#include "vlt_launch.cuh"
 
 namespace vlt {
 
@@ -38,64 +39,68 @@ struct GeoArgs {
   const float4* fz;
 };
 
+// Every launcher runs its pass through the launch layer (vlt_launch.cuh): at once
+// on ex.stream, or recorded for batched execution when ex.rec is set.
+
 // restir.cu
-void launch_surface(const vlt_frame_params& fp, int w, int h, const float* depth, const uint32_t* gbuf, float4* nd,
-                    float4* pr, float4* fz, cudaStream_t s);
+void launch_surface(const Exec& ex, const vlt_frame_params& fp, int w, int h, const float* depth,
+                    const uint32_t* gbuf, float4* nd, float4* pr, float4* fz);
 // Form-dependent buffers are void*: reference form uses the R11G11B10/half/M8W24
 // records of include/vlt.h; f32 form uses float2 AO history, float filtered AO,
 // 48-byte diffuse records {pos,W}{normal,M}{rad,0}, float4 lighting.
-void launch_ao_gen(int form, const vlt_frame_params& fp, int w, int h, const GeoArgs& ga, const uint32_t* hpn,
-                   const void* prev_ao, void* ao, uint32_t has_new, uint32_t has_prev, float radius, cudaStream_t s);
-void launch_ao_filter(int form, int w, int h, const float* depth, const void* ao, void* out, cudaStream_t s);
-void launch_diff_temporal(int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
-                          const float* prev_depth, const uint32_t* new_hpn, const uint32_t* new_rad,
-                          const float* new_pdf, const void* prev_rsv, void* out, uint32_t frame_rand,
-                          uint32_t has_prev, uint32_t has_new, cudaStream_t s);
-void launch_diff_spatial(int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn, const GeoArgs& ga,
-                         const void* ao, const void* in, void* out, void* lighting, uint32_t frame_rand,
-                         cudaStream_t s);
-void launch_spec_temporal(const vlt_frame_params& fp, int w, int h, uint32_t m_cap, const GeoArgs& ga,
-                          const GeoArgs& prev_ga, const float* prev_depth, const uint32_t* prev_rsv,
-                          const float* prev_hp, const uint32_t* prev_rad, const float* new_hp,
-                          const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
-                          uint32_t frame_rand, uint32_t has_prev, cudaStream_t s);
-void launch_spec_spatial(int form, const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn, const GeoArgs& ga,
-                         const uint32_t* rsv, const float* hp, const uint32_t* rad, void* lighting, uint16_t* ray_len,
-                         uint32_t* out_rsv, float* out_hp, uint32_t* out_rad, uint32_t frame_rand, cudaStream_t s);
+void launch_ao_gen(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const GeoArgs& ga,
+                   const uint32_t* hpn, const void* prev_ao, void* ao, uint32_t has_new, uint32_t has_prev,
+                   float radius);
+void launch_ao_filter(const Exec& ex, int form, int w, int h, const float* depth, const void* ao, void* out);
+void launch_diff_temporal(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn,
+                          const GeoArgs& ga, const float* prev_depth, const uint32_t* new_hpn,
+                          const uint32_t* new_rad, const float* new_pdf, const void* prev_rsv, void* out,
+                          uint32_t frame_rand, uint32_t has_prev, uint32_t has_new);
+void launch_diff_spatial(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn,
+                         const GeoArgs& ga, const void* ao, const void* in, void* out, void* lighting,
+                         uint32_t frame_rand);
+void launch_spec_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h, uint32_t m_cap,
+                          const GeoArgs& ga, const GeoArgs& prev_ga, const float* prev_depth,
+                          const uint32_t* prev_rsv, const float* prev_hp, const uint32_t* prev_rad,
+                          const float* new_hp, const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp,
+                          uint32_t* out_rad, uint32_t frame_rand, uint32_t has_prev);
+void launch_spec_spatial(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn,
+                         const GeoArgs& ga, const uint32_t* rsv, const float* hp, const uint32_t* rad,
+                         void* lighting, uint16_t* ray_len, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
+                         uint32_t frame_rand);
 
 // denoise_f32.cu — the f32 storage form of the denoiser. Records: DnRec
 // {float4 diffuse.rgb|aux.x, float4 specular.rgb|aux.y} with aux = moments (temporal /
 // fix outputs, history) or variance (fallback / a-trous); history length float.
-void launch_dn32_temporal(const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn, const GeoArgs& ga,
-                          const GeoArgs& prev_ga, const float4* diff_src, const float4* spec_src,
+void launch_dn32_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn,
+                          const GeoArgs& ga, const GeoArgs& prev_ga, const float4* diff_src, const float4* spec_src,
                           const float* prev_depth, const float4* hist, const float* len_hist, const float4* fast_hist,
-                          float4* out, float* out_len, float4* out_fast, uint32_t has_history, cudaStream_t s);
-void launch_dn32_fix(int w, int h, const GeoArgs& ga, const float* len, const float4* in, float4* out,
-                     cudaStream_t s);
-void launch_dn32_fast_clamp(int w, int h, const float4* fast, float4* rec, cudaStream_t s);
-void launch_dn32_fallback(int w, int h, const GeoArgs& ga, const float* len, const float4* in, float4* out,
-                          cudaStream_t s);
-void launch_dn32_atrous(int w, int h, const GeoArgs& ga, const float4* in, float4* out, float4* out_diff,
-                        float4* out_spec, int step, cudaStream_t s);
+                          float4* out, float* out_len, float4* out_fast, uint32_t has_history);
+void launch_dn32_fix(const Exec& ex, int w, int h, const GeoArgs& ga, const float* len, const float4* in,
+                     float4* out);
+void launch_dn32_fast_clamp(const Exec& ex, int w, int h, const float4* fast, float4* rec);
+void launch_dn32_fallback(const Exec& ex, int w, int h, const GeoArgs& ga, const float* len, const float4* in,
+                          float4* out);
+void launch_dn32_atrous(const Exec& ex, int w, int h, const GeoArgs& ga, const float4* in, float4* out,
+                        float4* out_diff, float4* out_spec, int step);
 
 // denoise.cu
-void launch_dn_temporal(const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn, const GeoArgs& ga,
-                        const GeoArgs& prev_ga, const uint32_t* diff_src, const uint32_t* spec_src,
+void launch_dn_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn,
+                        const GeoArgs& ga, const GeoArgs& prev_ga, const uint32_t* diff_src, const uint32_t* spec_src,
                         const uint16_t* ray_len, const float* prev_depth, const uint32_t* color_hist,
                         const uint32_t* mom_hist, const uint8_t* len_hist, const uint32_t* fast_hist,
                         uint32_t* out_color, uint32_t* out_mom, uint8_t* out_len, uint32_t* out_fast,
-                        uint32_t has_history, cudaStream_t s);
-void launch_dn_fix(int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color, const uint32_t* mom,
-                   uint32_t* out_color, uint32_t* out_mom, cudaStream_t s);
-void launch_dn_fast_clamp(int w, int h, const uint32_t* fast, uint32_t* color, cudaStream_t s);
-void launch_dn_fallback(int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color,
-                        const uint32_t* mom, uint32_t* out_color, uint32_t* out_var, cudaStream_t s);
+                        uint32_t has_history);
+void launch_dn_fix(const Exec& ex, int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color,
+                   const uint32_t* mom, uint32_t* out_color, uint32_t* out_mom);
+void launch_dn_fast_clamp(const Exec& ex, int w, int h, const uint32_t* fast, uint32_t* color);
+void launch_dn_fallback(const Exec& ex, int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color,
+                        const uint32_t* mom, uint32_t* out_color, uint32_t* out_var);
 // out_diff/out_spec (optional): write the result as two separate R11G11B10 planes
 // instead of (or besides) the packed colour pair.
-void launch_dn_atrous(int w, int h, const GeoArgs& ga, const uint32_t* color, const uint32_t* var,
-                      uint32_t* out_color, uint32_t* out_var, uint32_t* out_diff, uint32_t* out_spec, int step,
-                      cudaStream_t s);
-void launch_split_color(int w, int h, const uint32_t* color, uint32_t* diff, uint32_t* spec, cudaStream_t s);
+void launch_dn_atrous(const Exec& ex, int w, int h, const GeoArgs& ga, const uint32_t* color, const uint32_t* var,
+                      uint32_t* out_color, uint32_t* out_var, uint32_t* out_diff, uint32_t* out_spec, int step);
+void launch_split_color(const Exec& ex, int w, int h, const uint32_t* color, uint32_t* diff, uint32_t* spec);
 
 // hashgrid.cu
 struct HashGridDims {
@@ -110,19 +115,27 @@ struct HashGridDims {
   }
 };
 size_t hg_select_scratch_bytes(const HashGridDims& d);
-void launch_hg_decay(const HashGridDims& d, uint8_t* decay, uint32_t* storage, cudaStream_t s);
-void launch_hg_select(const HashGridDims& d, const uint32_t* queries, const uint32_t* count, uint32_t* storage,
-                      uint32_t* selection, uint32_t frame_hash, void* scratch, cudaStream_t s);
-void launch_hg_compact(const HashGridDims& d, const uint32_t* selection, uint32_t* idx, uint32_t* addr,
-                       uint32_t* count, cudaStream_t s);
-void launch_hg_update(const HashGridDims& d, const uint32_t* queries, const uint32_t* idx, const uint32_t* addr,
-                      const uint32_t* count, uint32_t* storage, uint8_t* decay, cudaStream_t s);
-void launch_hg_emit(const vlt_frame_params& fp, int w, int h, const HashGridDims& d, uint32_t key_mode,
-                    const float* depth, const uint32_t* hpn, const uint32_t* rad, uint32_t* queries,
-                    uint32_t* count, cudaStream_t s);
-void launch_hg_find(const vlt_frame_params& fp, const HashGridDims& d, uint32_t key_mode, const uint32_t* storage,
-                    uint32_t n, const float* pos, const float* nrm, uint32_t* out_addr, float* out_rad,
-                    cudaStream_t s);
+void launch_hg_decay(const Exec& ex, const HashGridDims& d, uint8_t* decay, uint32_t* storage);
+void launch_hg_select(const Exec& ex, const HashGridDims& d, const uint32_t* queries, const uint32_t* count,
+                      uint32_t* storage, uint32_t* selection, uint32_t frame_hash, void* scratch);
+void launch_hg_compact(const Exec& ex, const HashGridDims& d, const uint32_t* selection, uint32_t* idx,
+                       uint32_t* addr, uint32_t* count);
+void launch_hg_update(const Exec& ex, const HashGridDims& d, const uint32_t* queries, const uint32_t* idx,
+                      const uint32_t* addr, const uint32_t* count, uint32_t* storage, uint8_t* decay);
+void launch_hg_emit(const Exec& ex, const vlt_frame_params& fp, int w, int h, const HashGridDims& d,
+                    uint32_t key_mode, const float* depth, const uint32_t* hpn, const uint32_t* rad,
+                    uint32_t* queries, uint32_t* count);
+void launch_hg_find(const Exec& ex, const vlt_frame_params& fp, const HashGridDims& d, uint32_t key_mode,
+                    const uint32_t* storage, uint32_t n, const float* pos, const float* nrm, uint32_t* out_addr,
+                    float* out_rad);
+
+// api.cu: frame recording for batched execution.
+bool frame_inputs_ok(const vlt_view* v, const vlt_frame_inputs* in);
+// Runs the frame driver for `v` with every launch recorded into `rec` (the view's
+// host-side state advances as if the frame ran).
+vlt_status record_frame(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out, Recorder* rec);
+int view_device(const vlt_view* v);
+int ctx_device(const vlt_ctx* c);
 
 // Thread-local record of the last CUDA error text.
 void set_last_error(const char* msg);

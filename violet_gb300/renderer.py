@@ -68,6 +68,20 @@ class Context:
             pass
 
 
+def _frame_structs(frame_params, frame_index, inputs, outputs):
+    fi = _ffi.FrameInputs()
+    fi.params = C.pointer(frame_params)
+    fi.frame_index = int(frame_index) & 0xFFFFFFFF
+    for name in ("depth", "gbuffer", "prev_depth", "prev_gbuffer", "diff_hit_pos_normal", "diff_hit_radiance",
+                 "diff_source_pdf", "spec_hit_pos", "spec_hit_radiance"):
+        setattr(fi, name, _ptr(inputs.get(name)))
+    fo = _ffi.FrameOutputs()
+    outputs = outputs or {}
+    for name in ("diffuse", "specular", "raw_diffuse", "raw_specular"):
+        setattr(fo, name, _ptr(outputs.get(name)))
+    return fi, fo
+
+
 class View:
     """Resident per-view state and the per-frame pass sequence (vlt_frame_run)."""
 
@@ -92,16 +106,7 @@ class View:
         return int(lib.vlt_view_device_bytes(int(width), int(height), _ffi.FORMS[form], C.byref(p)))
 
     def run(self, frame_params, frame_index, inputs, outputs=None, stream=0):
-        fi = _ffi.FrameInputs()
-        fi.params = C.pointer(frame_params)
-        fi.frame_index = int(frame_index) & 0xFFFFFFFF
-        for name in ("depth", "gbuffer", "prev_depth", "prev_gbuffer", "diff_hit_pos_normal", "diff_hit_radiance",
-                     "diff_source_pdf", "spec_hit_pos", "spec_hit_radiance"):
-            setattr(fi, name, _ptr(inputs.get(name)))
-        fo = _ffi.FrameOutputs()
-        outputs = outputs or {}
-        for name in ("diffuse", "specular", "raw_diffuse", "raw_specular"):
-            setattr(fo, name, _ptr(outputs.get(name)))
+        fi, fo = _frame_structs(frame_params, frame_index, inputs, outputs)
         _ffi.check(self._lib.vlt_frame_run(self.handle, C.byref(fi), C.byref(fo), C.c_void_p(stream)),
                    "vlt_frame_run")
 
@@ -181,3 +186,59 @@ class Scene:
         _ffi.check(self._lib.vlt_scene_generate_device(C.byref(self.desc), int(frame), C.byref(f),
                                                        C.c_void_p(stream)), "vlt_scene_generate_device")
         return bufs
+
+
+class Batch:
+    """One frame of many views per call, as batched launches (vlt_batch_run)."""
+
+    def __init__(self, ctx):
+        self._lib = _ffi.load()
+        self.ctx = ctx
+        h = C.c_void_p()
+        _ffi.check(self._lib.vlt_batch_create(ctx.handle, C.byref(h)), "vlt_batch_create")
+        self.handle = h
+
+    def run(self, views, frame_params, frame_indices, inputs, outputs=None, stream=0):
+        """views[k] runs frame frame_indices[k] with frame_params[k], inputs[k] and
+        outputs[k] (dicts of device buffers, as View.run takes)."""
+        n = len(views)
+        fis = (_ffi.FrameInputs * n)()
+        fos = (_ffi.FrameOutputs * n)()
+        keep = []
+        for k in range(n):
+            fi, fo = _frame_structs(frame_params[k], frame_indices[k], inputs[k], outputs[k] if outputs else None)
+            fis[k] = fi
+            fos[k] = fo
+            keep.append(frame_params[k])
+        vh = (C.c_void_p * n)(*[v.handle.value for v in views])
+        _ffi.check(self._lib.vlt_batch_run(self.handle, vh, fis, fos if outputs else None, n, C.c_void_p(stream)),
+                   "vlt_batch_run")
+
+    def set_graphs(self, enable=True):
+        _ffi.check(self._lib.vlt_batch_set_graphs(self.handle, 1 if enable else 0), "vlt_batch_set_graphs")
+
+    def autotune(self):
+        _ffi.check(self._lib.vlt_batch_autotune(self.handle), "vlt_batch_autotune")
+
+    def tile_table(self):
+        n = self._lib.vlt_batch_tile_table(self.handle, None, 0)
+        arr = (_ffi.TileChoice * max(n, 1))()
+        n = self._lib.vlt_batch_tile_table(self.handle, arr, n)
+        return {arr[i].pass_.decode(): {"tile": (arr[i].bx, arr[i].by),
+                                        "ns_per_kpix": list(arr[i].ns_per_kpix)} for i in range(n)}
+
+    def stats(self):
+        st = _ffi.BatchStats()
+        _ffi.check(self._lib.vlt_batch_get_stats(self.handle, C.byref(st)), "vlt_batch_get_stats")
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def close(self):
+        if self.handle:
+            self._lib.vlt_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
