@@ -391,6 +391,10 @@ def run_ours(args, ws, rank, local):
     ctx.close()
     del frames, host
 
+    batched = None
+    if not args.no_batched:
+        batched = batched_leg(args, ws, dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         mpix, cores, times = cpu_sample(W, H, args.cpu_frames, 1000)
@@ -415,8 +419,131 @@ def run_ours(args, ws, rank, local):
             "passes": pass_table,
             "cpu_baseline": cpu,
             "clocks": clk,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
+
+
+def batch_view_set(n_views, seed):
+    """Resolutions drawn log-uniformly from 256x144 to 2560x1440 (by width), aspect
+    16:9, 4:3 or 1:1, each view with its own scene seed."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    views = []
+    for k in range(n_views):
+        w = float(np.exp(rng.uniform(np.log(256.0), np.log(2560.0))))
+        aspect = [16.0 / 9.0, 4.0 / 3.0, 1.0][int(rng.integers(0, 3))]
+        w = int(round(w / 2.0)) * 2
+        h = max(2, int(round(w / aspect / 2.0)) * 2)
+        views.append((w, h, 7000 + k))
+    return views
+
+
+def batched_leg(args, ws, dev):
+    """Many views of uneven size per step: every view's frames run one by one
+    through vlt_frame_run (plain), then the same frames through vlt_batch_run
+    (batched persistent kernels, CUDA graphs, autotuned tiles). Inputs are resident;
+    both arms time the same steps after the same warm-up frames."""
+    import torch
+
+    import violet_gb300 as vg
+
+    specs = batch_view_set(args.batch_views, 42)
+    frames_total = args.batch_frames
+    warm = 3
+    params = workload_params(vg)
+    ctx = vg.Context(dev.index)
+    # A created stream: CUDA graphs cannot capture the legacy default stream.
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+    total_px = sum(w * h for w, h, _ in specs)
+    per_frame_in = sum(w * h * sum(c * 4 for _, c in vg.FRAME_BUFFERS.values()) for w, h, _ in specs)
+    state = sum(vg.View.device_bytes(w, h, FORM, params) for w, h, _ in specs)
+    need = per_frame_in * frames_total + state + total_px * 64
+    if need > 150e9:
+        return {"skipped": "needs %.0f GB of HBM" % (need / 1e9)}
+    scenes = [vg.Scene(seed, w, h, disocclusion_frac=0.02) for w, h, seed in specs]
+    frames = []
+    for f in range(frames_total):
+        fr = []
+        for k, (w, h, seed) in enumerate(specs):
+            bufs = {b: torch.empty(w * h * c * 4, dtype=torch.uint8, device=dev) for b, (dt, c) in
+                    vg.FRAME_BUFFERS.items()}
+            scenes[k].generate_device(f, bufs, sh)
+            fr.append(bufs)
+        frames.append(fr)
+    fps = [[scenes[k].frame_params(f) for k in range(len(specs))] for f in range(frames_total)]
+    out_px = 16 if FORM == "f32" else 4
+    outs = [{o: torch.empty(w * h * out_px, dtype=torch.uint8, device=dev) for o in ("diffuse", "specular")}
+            for w, h, _ in specs]
+    views = [vg.View(ctx, w, h, FORM, params) for w, h, _ in specs]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = frames_total - warm
+
+    # plain: each view's frame through vlt_frame_run, view after view
+    for f in range(warm):
+        for k, v in enumerate(views):
+            v.run(fps[f][k], f, frames[f][k], outs[k], sh)
+    torch.cuda.synchronize()
+    barrier(ws)
+    e0.record(stream)
+    for f in range(warm, frames_total):
+        for k, v in enumerate(views):
+            v.run(fps[f][k], f, frames[f][k], outs[k], sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = max_over_ranks(e0.elapsed_time(e1), ws, dev)
+
+    # tile-shape tuning on the same views (results do not depend on the shapes)
+    batch = vg.Batch(ctx)
+    for v in views:
+        v.reset(sh)
+    batch.autotune()
+    tune_frames = 2 * vg._ffi.TILE_CANDIDATES + 1
+    for f in range(tune_frames):
+        ff = f % frames_total
+        batch.run(views, fps[ff], [ff] * len(views), frames[ff], outs, stream=sh)
+    tiles = batch.tile_table()
+
+    # batched: the same frames through vlt_batch_run
+    for v in views:
+        v.reset(sh)
+    for f in range(warm):
+        batch.run(views, fps[f], [f] * len(views), frames[f], outs, stream=sh)
+    torch.cuda.synchronize()
+    st0 = batch.stats()
+    barrier(ws)
+    e0.record(stream)
+    for f in range(warm, frames_total):
+        batch.run(views, fps[f], [f] * len(views), frames[f], outs, stream=sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batch_ms = max_over_ranks(e0.elapsed_time(e1), ws, dev)
+    st1 = batch.stats()
+    batch.close()
+    for v in views:
+        v.close()
+    ctx.close()
+    del frames
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    px = ws * total_px * steps
+    return {
+        "workload": "%d views, %d frames each, widths log-uniform 256..2560, aspect 16:9/4:3/1:1" % (
+            len(specs), frames_total),
+        "storage": FORM, "views": len(specs), "frames": frames_total, "timed_steps": steps,
+        "mpix_per_step": total_px / 1e6,
+        "value": px / (batch_ms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": batch_ms / steps,
+        "plain_value": px / (plain_ms / 1e3) / 1e6, "plain_ms_per_step": plain_ms / steps,
+        "speedup_vs_plain": plain_ms / batch_ms,
+        "launches_per_step": st1["last_launches"], "view_passes_per_step": st1["last_jobs"],
+        "graph_replays": st1["graph_replays"] - st0["graph_replays"],
+        "graph_captures": st1["graph_captures"] - st0["graph_captures"],
+        "arena_bytes": st1["arena_bytes"],
+        "tiles": {k: list(v["tile"]) + (["persistent"] if v["persistent"] else []) for k, v in tiles.items()},
+        "sizes": [[w, h] for w, h, _ in specs],
+    }
 
 
 def main():
@@ -429,6 +556,9 @@ def main():
     ap.add_argument("--height", type=int, default=H_DEFAULT)
     ap.add_argument("--cpu-frames", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-views", type=int, default=48)
+    ap.add_argument("--batch-frames", type=int, default=32)
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 steps")

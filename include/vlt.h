@@ -176,9 +176,10 @@ uint32_t vlt_view_last_launch_count(const vlt_view* view);
  * runs one frame of each of n views (any sizes, forms and parameters) as one
  * stream of launches: each pass that several views run next becomes a single
  * persistent kernel over the concatenated tile lists of those views. Every view's
- * results are identical to what vlt_frame_run gives it alone. The step (one
- * host-to-device copy of all launch arguments, then the kernels) is captured in a
- * CUDA graph and replayed while the sequence of batched launches repeats. */
+ * results are identical to what vlt_frame_run gives it alone. The views' arguments
+ * travel in each batched kernel's parameter block. With graphs on, the step is
+ * captured into a CUDA graph; a cached graph with the same launch sequence is
+ * updated with the new parameters and replayed. */
 typedef struct vlt_batch vlt_batch;
 vlt_status vlt_batch_create(vlt_ctx* ctx, vlt_batch** out);
 vlt_status vlt_batch_destroy(vlt_batch* batch);
@@ -189,14 +190,25 @@ vlt_status vlt_batch_run(vlt_batch* batch, vlt_view* const* views, const vlt_fra
                          const vlt_frame_outputs* outputs, uint32_t n, void* stream);
 /* CUDA-graph capture and replay of the batch step (default on). */
 vlt_status vlt_batch_set_graphs(vlt_batch* batch, int enable);
-/* Tile-shape autotuner: the next 2 x VLT_TILE_CANDIDATES frames each run every 2D
- * pass with one candidate tile shape (results do not depend on it), timing every
- * batched launch; then each pass keeps the shape with the least time per pixel. */
-#define VLT_TILE_CANDIDATES 5
+/* Views are packed into chunks of at most this many pixels (default: no limit, one
+ * chunk; a view larger than the limit forms a chunk alone); a chunk's whole frame
+ * runs before the next chunk's so that each pass finds the previous pass's output
+ * of the same views in L2. */
+vlt_status vlt_batch_set_chunk_pixels(vlt_batch* batch, uint64_t pixels);
+/* Launch mode of passes the tuner has not decided: 1 = a persistent grid of
+ * resident blocks looping over the tiles; 0 (default) = one block per tile. */
+vlt_status vlt_batch_set_persistent(vlt_batch* batch, int enable);
+/* Launch-shape autotuner: the next 2 x VLT_TILE_CANDIDATES frames each run every
+ * 2D pass with one candidate (tile shapes 32x4, 16x8, 32x8, 16x16, 64x4, each with
+ * one block per tile and persistent), timing every batched launch (results do not
+ * depend on the shape); then each pass keeps the candidate with the least time per
+ * pixel. */
+#define VLT_TILE_CANDIDATES 10
 vlt_status vlt_batch_autotune(vlt_batch* batch);
 typedef struct vlt_tile_choice {
   char pass[32];
   uint16_t bx, by;        /* chosen block (tile) shape */
+  uint16_t persistent;    /* chosen launch mode */
   float ns_per_kpix[VLT_TILE_CANDIDATES]; /* measured per candidate, 0 if not run */
 } vlt_tile_choice;
 /* Writes up to max entries (one per 2D pass seen by the tuner); returns the count. */
@@ -206,9 +218,10 @@ typedef struct vlt_batch_stats {
   uint64_t launches;        /* batched kernel launches issued (replays count) */
   uint64_t graph_replays;   /* steps replayed from a cached graph */
   uint64_t graph_captures;  /* steps captured into a new graph */
-  uint64_t arena_bytes;     /* launch-argument bytes of the last step */
+  uint64_t arena_bytes;     /* kernel-parameter bytes of the last step */
   uint32_t last_launches;   /* batched launches of the last step */
   uint32_t last_jobs;       /* per-view passes of the last step */
+  uint32_t last_chunks;     /* view chunks of the last step */
 } vlt_batch_stats;
 vlt_status vlt_batch_get_stats(const vlt_batch* batch, vlt_batch_stats* out);
 

@@ -58,7 +58,7 @@ def state_of(view, form):
     return res
 
 
-def run_pair(frames, graphs=True, autotune=False, use_stream=True):
+def run_pair(frames, graphs=True, autotune=False, use_stream=True, chunk_pixels=None):
     import torch
 
     ctx = vg.Context(0)
@@ -68,6 +68,8 @@ def run_pair(frames, graphs=True, autotune=False, use_stream=True):
     batched = [vg.View(ctx, w, h, form, p) for (w, h, form, p, seed, f0) in specs]
     batch = vg.Batch(ctx)
     batch.set_graphs(graphs)
+    if chunk_pixels:
+        batch.set_chunk_pixels(chunk_pixels)
     if autotune:
         batch.autotune()
     stream = torch.cuda.Stream() if use_stream else None
@@ -128,6 +130,12 @@ def test_batch_matches_alone_with_graphs():
 def test_batch_matches_alone_default_stream_no_graphs():
     stats, _ = run_pair(4, graphs=False, use_stream=False)
     assert stats["graph_captures"] == 0
+
+
+def test_batch_chunked_matches_alone():
+    # chunks of at most 10k pixels: the larger views run in chunks of their own
+    stats, _ = run_pair(4, graphs=True, chunk_pixels=10000)
+    assert stats["last_chunks"] >= 4
 
 
 def test_batch_autotune_keeps_results():

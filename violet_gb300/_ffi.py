@@ -93,18 +93,18 @@ class PassTime(C.Structure):
     _fields_ = [("name", C.c_char * 48), ("launches", C.c_uint32), ("total_ms", C.c_double)]
 
 
-TILE_CANDIDATES = 5  # VLT_TILE_CANDIDATES
+TILE_CANDIDATES = 10  # VLT_TILE_CANDIDATES
 
 
 class TileChoice(C.Structure):
-    _fields_ = [("pass_", C.c_char * 32), ("bx", C.c_uint16), ("by", C.c_uint16),
+    _fields_ = [("pass_", C.c_char * 32), ("bx", C.c_uint16), ("by", C.c_uint16), ("persistent", C.c_uint16),
                 ("ns_per_kpix", C.c_float * TILE_CANDIDATES)]
 
 
 class BatchStats(C.Structure):
     _fields_ = [("frames", C.c_uint64), ("launches", C.c_uint64), ("graph_replays", C.c_uint64),
                 ("graph_captures", C.c_uint64), ("arena_bytes", C.c_uint64), ("last_launches", C.c_uint32),
-                ("last_jobs", C.c_uint32)]
+                ("last_jobs", C.c_uint32), ("last_chunks", C.c_uint32)]
 
 
 class SceneDesc(C.Structure):
@@ -156,6 +156,8 @@ SIGNATURES = {
     "vlt_batch_destroy": (C.c_int, [P]),
     "vlt_batch_run": (C.c_int, [P, C.POINTER(P), C.POINTER(FrameInputs), C.POINTER(FrameOutputs), U32, P]),
     "vlt_batch_set_graphs": (C.c_int, [P, C.c_int]),
+    "vlt_batch_set_chunk_pixels": (C.c_int, [P, C.c_uint64]),
+    "vlt_batch_set_persistent": (C.c_int, [P, C.c_int]),
     "vlt_batch_autotune": (C.c_int, [P]),
     "vlt_batch_tile_table": (U32, [P, C.POINTER(TileChoice), U32]),
     "vlt_batch_get_stats": (C.c_int, [P, C.POINTER(BatchStats)]),

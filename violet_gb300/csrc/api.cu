@@ -270,6 +270,8 @@ vlt_status record_frame(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame
 }
 
 int view_device(const vlt_view* v) { return v->ctx->device; }
+uint32_t view_width(const vlt_view* v) { return v->w; }
+uint32_t view_height(const vlt_view* v) { return v->h; }
 int ctx_device(const vlt_ctx* c) { return c->device; }
 
 }  // namespace vlt

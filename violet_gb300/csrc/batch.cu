@@ -3,13 +3,13 @@
 // Each view's frame driver runs in recording mode (every launch becomes a Job with
 // its parameter tuple). The executor then repeatedly takes the next job of every
 // view, picks the kernel that most views run next, and turns those views' jobs into
-// one persistent k_batched launch over their concatenated tile lists. Jobs of one
+// one persistent k_batched launch over their concatenated tile lists, with the
+// views' parameter tuples and tile map in the kernel's parameter block. Jobs of one
 // view stay in order (they are dependent); jobs of different views are independent,
-// so grouping them changes no result. All tile maps and parameter tuples of the
-// step go into one argument arena (pinned host memory, double-buffered), copied to
-// the device with one cudaMemcpyAsync ahead of the kernels; the step is captured in
-// a CUDA graph, cached under the signature of its launch sequence, and replayed on
-// later steps with the same sequence (only the arena's contents change).
+// so grouping them changes no result. With graphs on, the step's launches are
+// captured into a CUDA graph; a cached executable graph with the same launch
+// sequence is updated in place with the new parameters (cudaGraphExecUpdate) and
+// replayed, otherwise a new one is instantiated.
 #include <stdio.h>
 #include <string.h>
 
@@ -26,25 +26,19 @@ using namespace vlt;
 
 namespace {
 
-struct Arena {
-  uint8_t* host = nullptr;
-  uint8_t* dev = nullptr;
-  size_t cap = 0;
-  cudaEvent_t copied = nullptr;  // recorded after the step's upload from this arena
-  bool pending = false;
-};
-
 struct GraphEntry {
   cudaGraphExec_t exec = nullptr;
   uint64_t last_use = 0;
 };
 
-const TileShape kCandidates[VLT_TILE_CANDIDATES] = {{32, 4}, {16, 8}, {32, 8}, {16, 16}, {64, 4}};
+// Candidate launch shapes: five tile shapes, each one tile per block and persistent.
+const TileShape kCandidates[VLT_TILE_CANDIDATES] = {{32, 4, 0}, {16, 8, 0}, {32, 8, 0}, {16, 16, 0}, {64, 4, 0},
+                                                    {32, 4, 1}, {16, 8, 1}, {32, 8, 1}, {16, 16, 1}, {64, 4, 1}};
 
 struct TuneRec {
   std::string name;
-  double ns[VLT_TILE_CANDIDATES] = {0, 0, 0, 0, 0};
-  double kpix[VLT_TILE_CANDIDATES] = {0, 0, 0, 0, 0};
+  double ns[VLT_TILE_CANDIDATES] = {};
+  double kpix[VLT_TILE_CANDIDATES] = {};
   int chosen = 0;
 };
 
@@ -52,9 +46,10 @@ struct TuneRec {
 
 struct vlt_batch {
   vlt_ctx* ctx;
-  Arena arena[2];
-  int parity = 0;
+  std::vector<uint8_t> params;  // parameter blocks of the step being issued
   bool graphs = true;
+  uint64_t chunk_pixels = ~(uint64_t)0;  // no chunking
+  bool persistent = false;
   std::unordered_map<std::string, GraphEntry> cache;
   uint64_t tick = 0;
   std::map<const void*, TileShape> shapes;  // per kernel (PrepareFn) chosen tile shape
@@ -70,50 +65,21 @@ namespace {
 
 const size_t kMaxGraphs = 32;
 
-vlt_status ensure_arena(Arena& a, size_t bytes) {
-  if (a.cap >= bytes) return VLT_OK;
-  if (a.pending) {
-    cudaEventSynchronize(a.copied);
-    a.pending = false;
-  }
-  if (a.host) cudaFreeHost(a.host);
-  if (a.dev) cudaFree(a.dev);
-  a.host = nullptr;
-  a.dev = nullptr;
-  a.cap = 0;
-  size_t cap = 1 << 16;
-  while (cap < bytes) cap <<= 1;
-  vlt_status st = cuda_status(cudaHostAlloc((void**)&a.host, cap, cudaHostAllocDefault));
-  if (st != VLT_OK) return st;
-  st = cuda_status(cudaMalloc((void**)&a.dev, cap));
-  if (st != VLT_OK) {
-    cudaFreeHost(a.host);
-    a.host = nullptr;
-    return st;
-  }
-  if (!a.copied) {
-    st = cuda_status(cudaEventCreateWithFlags(&a.copied, cudaEventDisableTiming));
-    if (st != VLT_OK) return st;
-  }
-  a.cap = cap;
-  return VLT_OK;
-}
-
 // Grouping of the recorded jobs into batched launches (see the file comment).
 struct Group {
   PrepareFn key;
   std::vector<const Job*> jobs;
 };
 
-std::vector<Group> group_jobs(const std::vector<Recorder>& recs) {
+std::vector<Group> group_jobs(const std::vector<const Recorder*>& recs) {
   std::vector<Group> groups;
   std::vector<size_t> head(recs.size(), 0);
   for (;;) {
     // Count heads per kernel; pick the most common (first seen on ties).
     std::vector<std::pair<PrepareFn, uint32_t>> counts;
     for (size_t k = 0; k < recs.size(); ++k) {
-      if (head[k] >= recs[k].jobs.size()) continue;
-      PrepareFn f = recs[k].jobs[head[k]].prepare;
+      if (head[k] >= recs[k]->jobs.size()) continue;
+      PrepareFn f = recs[k]->jobs[head[k]].prepare;
       bool found = false;
       for (auto& c : counts)
         if (c.first == f) {
@@ -134,8 +100,8 @@ std::vector<Group> group_jobs(const std::vector<Recorder>& recs) {
     Group g;
     g.key = best;
     for (size_t k = 0; k < recs.size(); ++k) {
-      if (head[k] >= recs[k].jobs.size()) continue;
-      const Job& j = recs[k].jobs[head[k]];
+      if (head[k] >= recs[k]->jobs.size()) continue;
+      const Job& j = recs[k]->jobs[head[k]];
       if (j.prepare != best) continue;
       g.jobs.push_back(&j);
       ++head[k];
@@ -146,10 +112,14 @@ std::vector<Group> group_jobs(const std::vector<Recorder>& recs) {
 }
 
 TileShape shape_for(vlt_batch* b, const Job& j) {
-  if (j.one_d) return TileShape();
-  if (b->tune_left > 0) return kCandidates[b->tune_index % VLT_TILE_CANDIDATES];
-  auto it = b->shapes.find((const void*)j.prepare);
-  return it == b->shapes.end() ? TileShape() : it->second;
+  if (!j.one_d) {
+    if (b->tune_left > 0) return kCandidates[b->tune_index % VLT_TILE_CANDIDATES];
+    auto it = b->shapes.find((const void*)j.prepare);
+    if (it != b->shapes.end()) return it->second;
+  }
+  TileShape t;
+  t.persistent = b->persistent ? 1 : 0;
+  return t;
 }
 
 void finish_tuning(vlt_batch* b) {
@@ -192,12 +162,6 @@ vlt_status vlt_batch_create(vlt_ctx* ctx, vlt_batch** out) {
 vlt_status vlt_batch_destroy(vlt_batch* b) {
   if (!b) return VLT_OK;
   cudaSetDevice(ctx_device(b->ctx));
-  for (auto& a : b->arena) {
-    if (a.pending) cudaEventSynchronize(a.copied);
-    if (a.copied) cudaEventDestroy(a.copied);
-    if (a.host) cudaFreeHost(a.host);
-    if (a.dev) cudaFree(a.dev);
-  }
   for (auto& kv : b->cache) cudaGraphExecDestroy(kv.second.exec);
   for (cudaEvent_t e : b->events) cudaEventDestroy(e);
   delete b;
@@ -207,6 +171,18 @@ vlt_status vlt_batch_destroy(vlt_batch* b) {
 vlt_status vlt_batch_set_graphs(vlt_batch* b, int enable) {
   if (!b) return VLT_ERR_INVALID_ARG;
   b->graphs = enable != 0;
+  return VLT_OK;
+}
+
+vlt_status vlt_batch_set_chunk_pixels(vlt_batch* b, uint64_t pixels) {
+  if (!b || pixels == 0) return VLT_ERR_INVALID_ARG;
+  b->chunk_pixels = pixels;
+  return VLT_OK;
+}
+
+vlt_status vlt_batch_set_persistent(vlt_batch* b, int enable) {
+  if (!b) return VLT_ERR_INVALID_ARG;
+  b->persistent = enable != 0;
   return VLT_OK;
 }
 
@@ -230,6 +206,7 @@ uint32_t vlt_batch_tile_table(const vlt_batch* b, vlt_tile_choice* out, uint32_t
       TileShape s = it == b->shapes.end() ? TileShape() : it->second;
       c.bx = s.bx;
       c.by = s.by;
+      c.persistent = s.persistent;
       for (int i = 0; i < VLT_TILE_CANDIDATES; ++i)
         c.ns_per_kpix[i] = kv.second.kpix[i] > 0 ? (float)(kv.second.ns[i] / kv.second.kpix[i]) : 0.0f;
     }
@@ -268,63 +245,54 @@ vlt_status vlt_batch_run(vlt_batch* b, vlt_view* const* views, const vlt_frame_i
     jobs += (uint32_t)recs[k].jobs.size();
   }
 
-  // 2. Group and prepare into the argument arena.
-  std::vector<Group> groups = group_jobs(recs);
-  const bool tuning = b->tune_left > 0;
-  Arena& a = b->arena[b->parity];
-  if (a.pending) {  // the upload two steps ago must be done before the host arena is rewritten
-    cudaEventSynchronize(a.copied);
-    a.pending = false;
-  }
-  std::vector<Prepared> preps(groups.size());
-  size_t used = 0;
-  for (int attempt = 0; attempt < 2; ++attempt) {
-    used = 0;
-    bool fits = true;
-    for (size_t g = 0; g < groups.size(); ++g) {
-      const Job& j0 = *groups[g].jobs[0];
-      // worst-case size: tile map + tuples, 16-byte aligned
-      size_t need = (2 * groups[g].jobs.size() + 1) * 4 + 16 + groups[g].jobs.size() * (j0.args.size() + 16) + 16;
-      if (used + need > a.cap) {
-        fits = false;
-        used += need;
-        continue;
-      }
-      used += groups[g].key(groups[g].jobs.data(), (uint32_t)groups[g].jobs.size(), shape_for(b, j0), a.host, used,
-                            &preps[g]);
+  // 2. Pack the views into chunks of at most chunk_pixels (first fit, largest
+  // first; a larger view is a chunk of its own). A chunk's whole frame runs before
+  // the next chunk's, so what one pass writes is still in L2 when the next pass of
+  // the same views reads it. Then group each chunk's jobs into batched launches.
+  std::vector<uint32_t> order(n);
+  for (uint32_t k = 0; k < n; ++k) order[k] = k;
+  auto px = [&](uint32_t k) { return (uint64_t)view_width(views[k]) * view_height(views[k]); };
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c) { return px(a) > px(c); });
+  std::vector<std::vector<uint32_t>> chunks;
+  std::vector<uint64_t> fill;
+  for (uint32_t k : order) {
+    size_t c = 0;
+    while (c < chunks.size() && fill[c] + px(k) > b->chunk_pixels) ++c;
+    if (c == chunks.size()) {
+      chunks.emplace_back();
+      fill.push_back(0);
     }
-    if (fits) break;
-    // A new arena invalidates every captured graph (their copy and kernel nodes
-    // hold the old addresses).
-    for (auto& kv : b->cache) cudaGraphExecDestroy(kv.second.exec);
-    b->cache.clear();
-    st = ensure_arena(a, used + (1 << 12));
-    if (st != VLT_OK) return st;
+    chunks[c].push_back(k);
+    fill[c] += px(k);
   }
-  for (Prepared& p : preps) p.dev_base = a.dev;
+  std::vector<Group> groups;
+  for (const auto& ch : chunks) {
+    std::vector<const Recorder*> rs;
+    for (uint32_t k : ch) rs.push_back(&recs[k]);
+    std::vector<Group> g = group_jobs(rs);
+    for (Group& x : g) groups.push_back(std::move(x));
+  }
+  b->stats.last_chunks = (uint32_t)chunks.size();
+  const bool tuning = b->tune_left > 0;
+  b->params.clear();
+  std::vector<Prepared> preps;
+  std::vector<size_t> group_of;  // prepared launch -> group
+  for (size_t g = 0; g < groups.size(); ++g) {
+    size_t before = preps.size();
+    groups[g].key(groups[g].jobs.data(), (uint32_t)groups[g].jobs.size(), shape_for(b, *groups[g].jobs[0]),
+                  b->params, preps);
+    for (size_t k = before; k < preps.size(); ++k) group_of.push_back(g);
+  }
+  const uint8_t* params = b->params.data();
 
-  // 3. Issue: the upload, then the launches (from a cached graph when possible).
+  // 3. Issue the launches (through a CUDA graph when possible).
   // The legacy default stream cannot be captured: steps on it are issued directly.
   const bool use_graph = b->graphs && !tuning && s != 0;
-  std::string sig;
-  if (use_graph) {
-    sig.reserve(groups.size() * 40 + 16);
-    char buf[96];
-    snprintf(buf, sizeof(buf), "%d:%zu:%p;", b->parity, used, (void*)a.dev);
-    sig += buf;
-    for (const Prepared& p : preps) {
-      snprintf(buf, sizeof(buf), "%p,%u,%u,%u,%u,%u,%zu;", p.key, p.n_jobs, p.total_tiles, p.grid, p.block.x,
-               p.block.y, p.arena_off);
-      sig += buf;
-    }
-  }
   auto issue = [&](bool timed) -> vlt_status {
-    vlt_status e = cuda_status(cudaMemcpyAsync(a.dev, a.host, used, cudaMemcpyHostToDevice, s));
-    if (e != VLT_OK) return e;
-    for (size_t g = 0; g < preps.size(); ++g) {
-      if (timed) cudaEventRecord(b->events[2 * g], s);
-      preps[g].launch(preps[g], s);
-      if (timed) cudaEventRecord(b->events[2 * g + 1], s);
+    for (size_t k = 0; k < preps.size(); ++k) {
+      if (timed) cudaEventRecord(b->events[2 * k], s);
+      preps[k].launch(preps[k], params, s);
+      if (timed) cudaEventRecord(b->events[2 * k + 1], s);
     }
     return cuda_status(cudaGetLastError());
   };
@@ -337,28 +305,61 @@ vlt_status vlt_batch_run(vlt_batch* b, vlt_view* const* views, const vlt_frame_i
     }
     st = issue(true);
     if (st != VLT_OK) return st;
-    st = cuda_status(cudaEventRecord(a.copied, s));
-    if (st != VLT_OK) return st;
     st = cuda_status(cudaStreamSynchronize(s));
     if (st != VLT_OK) return st;
     const int cand = b->tune_index % VLT_TILE_CANDIDATES;
-    for (size_t g = 0; g < preps.size(); ++g) {
-      const Job& j0 = *groups[g].jobs[0];
+    for (size_t k = 0; k < preps.size(); ++k) {
+      const Group& gr = groups[group_of[k]];
+      const Job& j0 = *gr.jobs[0];
       if (j0.one_d) continue;
       float ms = 0.0f;
-      cudaEventElapsedTime(&ms, b->events[2 * g], b->events[2 * g + 1]);
-      double kpix = 0;
-      for (const Job* j : groups[g].jobs) kpix += (double)j->w * j->h / 1e3;
-      TuneRec& t = b->tune[(const void*)groups[g].key];
+      cudaEventElapsedTime(&ms, b->events[2 * k], b->events[2 * k + 1]);
+      TuneRec& t = b->tune[(const void*)gr.key];
       if (t.name.empty()) t.name = j0.name;
       t.ns[cand] += ms * 1e6;
-      t.kpix[cand] += kpix;
+    }
+    for (const Group& gr : groups) {
+      if (gr.jobs[0]->one_d) continue;
+      double kpix = 0;
+      for (const Job* j : gr.jobs) kpix += (double)j->w * j->h / 1e3;
+      b->tune[(const void*)gr.key].kpix[cand] += kpix;
     }
     ++b->tune_index;
     if (--b->tune_left == 0) finish_tuning(b);
   } else if (use_graph) {
+    std::string sig;
+    sig.reserve(preps.size() * 48);
+    char buf[96];
+    for (const Prepared& p : preps) {
+      snprintf(buf, sizeof(buf), "%p,%u,%u,%u,%zu;", p.key, p.grid, p.block.x, p.block.y, p.param_bytes);
+      sig += buf;
+    }
+    cudaGraph_t graph = nullptr;
+    st = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    if (st != VLT_OK) return st;
+    vlt_status ist = issue(false);
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (ist != VLT_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return ist;
+    }
+    st = cuda_status(ce);
+    if (st != VLT_OK) return st;
     auto it = b->cache.find(sig);
-    if (it == b->cache.end()) {
+    bool updated = false;
+    if (it != b->cache.end()) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(it->second.exec, graph, &info) == cudaSuccess) {
+        updated = true;
+        ++b->stats.graph_replays;
+      } else {
+        cudaGetLastError();
+        cudaGraphExecDestroy(it->second.exec);
+        b->cache.erase(it);
+        it = b->cache.end();
+      }
+    }
+    if (!updated) {
       if (b->cache.size() >= kMaxGraphs) {  // evict the least recently used
         auto victim = b->cache.begin();
         for (auto c = b->cache.begin(); c != b->cache.end(); ++c)
@@ -366,44 +367,28 @@ vlt_status vlt_batch_run(vlt_batch* b, vlt_view* const* views, const vlt_frame_i
         cudaGraphExecDestroy(victim->second.exec);
         b->cache.erase(victim);
       }
-      cudaGraph_t graph = nullptr;
-      st = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      if (st != VLT_OK) return st;
-      vlt_status ist = issue(false);
-      cudaError_t ce = cudaStreamEndCapture(s, &graph);
-      if (ist != VLT_OK) {
-        if (graph) cudaGraphDestroy(graph);
-        return ist;
-      }
-      st = cuda_status(ce);
-      if (st != VLT_OK) return st;
       GraphEntry ge;
       st = cuda_status(cudaGraphInstantiate(&ge.exec, graph, 0));
-      cudaGraphDestroy(graph);
-      if (st != VLT_OK) return st;
+      if (st != VLT_OK) {
+        cudaGraphDestroy(graph);
+        return st;
+      }
       it = b->cache.emplace(sig, ge).first;
       ++b->stats.graph_captures;
-    } else {
-      ++b->stats.graph_replays;
     }
+    cudaGraphDestroy(graph);
     it->second.last_use = ++b->tick;
     st = cuda_status(cudaGraphLaunch(it->second.exec, s));
-    if (st != VLT_OK) return st;
-    st = cuda_status(cudaEventRecord(a.copied, s));
     if (st != VLT_OK) return st;
   } else {
     st = issue(false);
     if (st != VLT_OK) return st;
-    st = cuda_status(cudaEventRecord(a.copied, s));
-    if (st != VLT_OK) return st;
   }
-  a.pending = true;
-  b->parity ^= 1;
   ++b->stats.frames;
   b->stats.launches += preps.size();
   b->stats.last_launches = (uint32_t)preps.size();
   b->stats.last_jobs = jobs;
-  b->stats.arena_bytes = used;
+  b->stats.arena_bytes = b->params.size();
   return VLT_OK;
 }
 

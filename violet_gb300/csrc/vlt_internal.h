@@ -135,6 +135,8 @@ bool frame_inputs_ok(const vlt_view* v, const vlt_frame_inputs* in);
 // host-side state advances as if the frame ran).
 vlt_status record_frame(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out, Recorder* rec);
 int view_device(const vlt_view* v);
+uint32_t view_width(const vlt_view* v);
+uint32_t view_height(const vlt_view* v);
 int ctx_device(const vlt_ctx* c);
 
 // Thread-local record of the last CUDA error text.

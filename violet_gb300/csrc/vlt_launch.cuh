@@ -42,25 +42,26 @@ struct Exec {
 // kBlock1D threads per block.
 struct TileShape {
   uint16_t bx = 32, by = 4;
+  uint16_t persistent = 1;  // 1: grid capped at the resident blocks (tile loop); 0: one tile per block
 };
 static constexpr int kBlock1D = 128;
 static constexpr int kMaxThreads = 256;  // largest tile the autotuner tries
 
-// A prepared batched launch: what k_batched needs once the argument arena is on
-// the device.
+// A prepared batched launch: a kernel and its parameter block (host bytes at
+// `param_off` in the executor's parameter buffer).
 struct Prepared {
-  void (*launch)(const Prepared&, cudaStream_t);
+  void (*launch)(const Prepared&, const uint8_t* params, cudaStream_t);
   const void* key;
   uint32_t n_jobs, total_tiles, grid;
   dim3 block;
-  size_t arena_off;  // tile_start[n+1], tiles_x[n], tuples (16-byte aligned)
-  const uint8_t* dev_base;
+  size_t param_off, param_bytes;
 };
 
-// Groups jobs of one kernel (same key) into a batched launch: writes the tile map
-// and the tuples into the host arena at `off` and fills `p`; returns bytes used.
-using PrepareFn = size_t (*)(const Job* const* jobs, uint32_t n, TileShape shape, uint8_t* host_arena, size_t off,
-                             Prepared* p);
+// Groups jobs of one kernel (same key) into batched launches (several when the
+// jobs exceed one parameter block): appends their parameter blocks to `params`
+// and the launches to `out`.
+using PrepareFn = void (*)(const Job* const* jobs, uint32_t n, TileShape shape, std::vector<uint8_t>& params,
+                           std::vector<Prepared>& out);
 
 struct Job {
   PrepareFn prepare;   // also the grouping key
@@ -77,69 +78,60 @@ __global__ void __launch_bounds__(kMaxThreads) k_grid(A... a) {
   F::run((int)(blockIdx.x * blockDim.x), (int)(blockIdx.y * blockDim.y), a...);
 }
 
+// Kernel parameter block of a batched launch: the views' parameter tuples and
+// their tile map, passed by value (kernel parameters live in the constant bank, so
+// the bodies read their arguments as uniform constant loads, as k_grid does).
+// kCapacity views fit in the 32 KB parameter limit.
+template <class Tup>
+struct BatchCap {
+  static constexpr uint32_t kRaw = (uint32_t)((32000 - 16) / (sizeof(Tup) + 8));
+  static constexpr uint32_t kCapacity = kRaw < 64 ? kRaw : 64;
+};
+
+template <class Tup>
+struct BatchParams {
+  static constexpr uint32_t N = BatchCap<Tup>::kCapacity;
+  Tup tup[N];
+  uint32_t tile_start[N + 1];
+  uint32_t tiles_x[N];
+  uint32_t n_jobs, total_tiles;
+};
+
 template <class F, class Tup>
-__global__ void __launch_bounds__(kMaxThreads) k_batched(const uint8_t* __restrict__ base, uint32_t n_jobs,
-                                                         uint32_t total_tiles) {
-  constexpr uint32_t kWords = (uint32_t)(sizeof(Tup) / 4);
-  static_assert(sizeof(Tup) % 4 == 0, "parameter tuple must be a whole number of words");
-  __shared__ __align__(16) uint32_t s_args[kWords];
-  const uint32_t* tile_start = (const uint32_t*)base;
-  const uint32_t* tiles_x = tile_start + n_jobs + 1;
-  const size_t tup_off = ((size_t)(2 * n_jobs + 1) * 4 + 15) & ~(size_t)15;
-  const Tup* tuples = (const Tup*)(base + tup_off);
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  const int nt = blockDim.x * blockDim.y;
-  uint32_t cur = 0xFFFFFFFFu;
-  for (uint32_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
-    uint32_t lo = 0, hi = n_jobs;  // last job whose first tile is <= t
+__global__ void __launch_bounds__(kMaxThreads) k_batched(const __grid_constant__ BatchParams<Tup> p) {
+  for (uint32_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
+    uint32_t lo = 0, hi = p.n_jobs;  // last job whose first tile is <= t
     while (hi - lo > 1) {
       uint32_t mid = (lo + hi) >> 1;
-      if (tile_start[mid] <= t) lo = mid;
+      if (p.tile_start[mid] <= t) lo = mid;
       else hi = mid;
     }
-    if (lo != cur) {
-      __syncthreads();
-      const uint32_t* src = (const uint32_t*)(tuples + lo);
-      for (uint32_t k = tid; k < kWords; k += nt) s_args[k] = src[k];
-      __syncthreads();
-      cur = lo;
-    }
-    const uint32_t lt = t - tile_start[lo];
-    const uint32_t tx = tiles_x[lo];
+    const uint32_t lt = t - p.tile_start[lo];
+    const uint32_t tx = p.tiles_x[lo];
     const int x0 = (int)((lt % tx) * blockDim.x), y0 = (int)((lt / tx) * blockDim.y);
-    const Tup& a = *reinterpret_cast<const Tup*>(s_args);
-    cuda::std::apply([&](auto const&... p) { F::run(x0, y0, p...); }, a);
+    cuda::std::apply([&](auto const&... a) { F::run(x0, y0, a...); }, p.tup[lo]);
   }
 }
 
 // ------------------------------------------------------------- host side
 
 int device_sm_count();
-// Resident blocks per SM of a kernel at a block size (cached by the caller's key).
+// Resident blocks per SM of a kernel at a block size.
 int occupancy_blocks(const void* kernel, int threads);
 
 template <class F, class Tup>
-void launch_prepared(const Prepared& p, cudaStream_t s) {
-  k_batched<F, Tup><<<p.grid, p.block, 0, s>>>(p.dev_base + p.arena_off, p.n_jobs, p.total_tiles);
+void launch_prepared(const Prepared& p, const uint8_t* params, cudaStream_t s) {
+  static_assert(sizeof(BatchParams<Tup>) <= 32764, "batched parameter block exceeds the kernel parameter limit");
+  const BatchParams<Tup>& bp = *reinterpret_cast<const BatchParams<Tup>*>(params + p.param_off);
+  k_batched<F, Tup><<<p.grid, p.block, 0, s>>>(bp);
 }
 
 template <class F, class Tup>
-size_t prepare_batched(const Job* const* jobs, uint32_t n, TileShape shape, uint8_t* host, size_t off, Prepared* p) {
+void prepare_batched(const Job* const* jobs, uint32_t n, TileShape shape, std::vector<uint8_t>& params,
+                     std::vector<Prepared>& out) {
+  using BP = BatchParams<Tup>;
   const bool one_d = jobs[0]->one_d;
   const uint32_t bx = one_d ? (uint32_t)kBlock1D : shape.bx, by = one_d ? 1u : shape.by;
-  uint32_t* tile_start = (uint32_t*)(host + off);
-  uint32_t* tiles_x = tile_start + n + 1;
-  const size_t tup_off = ((size_t)(2 * n + 1) * 4 + 15) & ~(size_t)15;
-  uint32_t total = 0;
-  for (uint32_t j = 0; j < n; ++j) {
-    uint32_t tx = (jobs[j]->w + bx - 1) / bx, ty = (jobs[j]->h + by - 1) / by;
-    tile_start[j] = total;
-    tiles_x[j] = tx ? tx : 1;
-    total += tx * ty;
-  }
-  tile_start[n] = total;
-  for (uint32_t j = 0; j < n; ++j) memcpy(host + off + tup_off + (size_t)j * sizeof(Tup), jobs[j]->args.data(),
-                                          sizeof(Tup));
   // Resident blocks per SM for this block size, cached as (threads << 32 | blocks).
   static std::atomic<uint64_t> occ{0};
   uint64_t o = occ.load(std::memory_order_relaxed);
@@ -148,15 +140,40 @@ size_t prepare_batched(const Job* const* jobs, uint32_t n, TileShape shape, uint
     bps = (uint32_t)occupancy_blocks((const void*)k_batched<F, Tup>, (int)(bx * by));
     occ.store(((uint64_t)(bx * by) << 32) | bps, std::memory_order_relaxed);
   }
-  uint32_t cap = (bps > 0 ? bps : 1u) * (uint32_t)device_sm_count();
-  p->launch = &launch_prepared<F, Tup>;
-  p->key = (const void*)&prepare_batched<F, Tup>;
-  p->n_jobs = n;
-  p->total_tiles = total;
-  p->grid = total < cap ? total : cap;
-  p->block = dim3(bx, by, 1);
-  p->arena_off = off;
-  return (tup_off + (size_t)n * sizeof(Tup) + 15) & ~(size_t)15;
+  const uint32_t cap = (bps > 0 ? bps : 1u) * (uint32_t)device_sm_count();
+  for (uint32_t first = 0; first < n; first += BP::N) {
+    const uint32_t m = n - first < BP::N ? n - first : BP::N;
+    size_t off = (params.size() + 15) & ~(size_t)15;
+    params.resize(off + sizeof(BP));
+    BP* bp = reinterpret_cast<BP*>(params.data() + off);
+    memset((void*)bp, 0, sizeof(BP));
+    uint32_t total = 0;
+    for (uint32_t j = 0; j < m; ++j) {
+      const Job& jb = *jobs[first + j];
+      uint32_t tx = (jb.w + bx - 1) / bx, ty = (jb.h + by - 1) / by;
+      bp->tile_start[j] = total;
+      bp->tiles_x[j] = tx ? tx : 1;
+      total += tx * ty;
+      memcpy((void*)&bp->tup[j], jb.args.data(), sizeof(Tup));
+    }
+    bp->tile_start[m] = total;
+    bp->n_jobs = m;
+    bp->total_tiles = total;
+    if (total == 0) {
+      params.resize(off);
+      continue;
+    }
+    Prepared p;
+    p.launch = &launch_prepared<F, Tup>;
+    p.key = (const void*)&prepare_batched<F, Tup>;
+    p.n_jobs = m;
+    p.total_tiles = total;
+    p.grid = (shape.persistent && total > cap) ? cap : total;
+    p.block = dim3(bx, by, 1);
+    p.param_off = off;
+    p.param_bytes = sizeof(BP);
+    out.push_back(p);
+  }
 }
 
 template <class F, class... A>

@@ -217,6 +217,12 @@ class Batch:
     def set_graphs(self, enable=True):
         _ffi.check(self._lib.vlt_batch_set_graphs(self.handle, 1 if enable else 0), "vlt_batch_set_graphs")
 
+    def set_chunk_pixels(self, pixels):
+        _ffi.check(self._lib.vlt_batch_set_chunk_pixels(self.handle, int(pixels)), "vlt_batch_set_chunk_pixels")
+
+    def set_persistent(self, enable=True):
+        _ffi.check(self._lib.vlt_batch_set_persistent(self.handle, 1 if enable else 0), "vlt_batch_set_persistent")
+
     def autotune(self):
         _ffi.check(self._lib.vlt_batch_autotune(self.handle), "vlt_batch_autotune")
 
@@ -224,7 +230,7 @@ class Batch:
         n = self._lib.vlt_batch_tile_table(self.handle, None, 0)
         arr = (_ffi.TileChoice * max(n, 1))()
         n = self._lib.vlt_batch_tile_table(self.handle, arr, n)
-        return {arr[i].pass_.decode(): {"tile": (arr[i].bx, arr[i].by),
+        return {arr[i].pass_.decode(): {"tile": (arr[i].bx, arr[i].by), "persistent": bool(arr[i].persistent),
                                         "ns_per_kpix": list(arr[i].ns_per_kpix)} for i in range(n)}
 
     def stats(self):
