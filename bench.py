@@ -395,6 +395,10 @@ def run_ours(args, ws, rank, local):
     if not args.no_batched:
         batched = batched_leg(args, ws, dev)
 
+    serving = None
+    if not args.no_serving:
+        serving = serving_leg(args, ws, dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         mpix, cores, times = cpu_sample(W, H, args.cpu_frames, 1000)
@@ -420,6 +424,7 @@ def run_ours(args, ws, rank, local):
             "cpu_baseline": cpu,
             "clocks": clk,
             "batched": batched,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
 
@@ -546,6 +551,121 @@ def batched_leg(args, ws, dev):
     }
 
 
+SERVE_CLASSES = [("720p", 1280, 720, 0.3), ("1080p", 1920, 1080, 0.4), ("1440p", 2560, 1440, 0.2),
+                 ("2160p", 3840, 2160, 0.1)]
+POOL_FRAMES = 16
+
+
+def serving_leg(args, ws, dev):
+    """Poisson arrivals of view-sessions through the server (vlt_server_*): each
+    admitted session keeps one frame queued (the next is submitted when the last
+    completes); every step batches the queued frames of all admitted sessions.
+    Per-frame latency is submit-to-completion on the host clock. Frame inputs come
+    from a pool of POOL_FRAMES consecutive frames per resolution class, walked
+    forth and back, so the timed loop runs only the lighting path."""
+    import numpy as np
+    import torch
+
+    import violet_gb300 as vg
+
+    rng = np.random.default_rng(4242)
+    params = workload_params(vg)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+    pools = {}
+    for name, w, h, _ in SERVE_CLASSES:
+        sc = vg.Scene(900 + w, w, h, disocclusion_frac=0.02)
+        frames = []
+        for f in range(POOL_FRAMES):
+            bufs = {b: torch.empty(w * h * c * 4, dtype=torch.uint8, device=dev) for b, (dt, c) in
+                    vg.FRAME_BUFFERS.items()}
+            sc.generate_device(f, bufs, sh)
+            frames.append((bufs, sc.frame_params(f)))
+        pools[name] = frames
+    torch.cuda.synchronize()
+    ctx = vg.Context(dev.index)
+    server = vg.Server(ctx, int(args.serve_hbm_gb * 1e9), int(args.serve_step_mpix * 1e6))
+    # arrivals
+    t_arr, classes, lengths = [], [], []
+    t = 0.0
+    while True:
+        t += rng.exponential(1.0 / args.serve_rate)
+        if t > args.serve_seconds:
+            break
+        t_arr.append(t)
+        k = int(rng.choice(len(SERVE_CLASSES), p=[c[3] for c in SERVE_CLASSES]))
+        classes.append(k)
+        lengths.append(int(rng.integers(30, 301)))
+    out_px = 16 if FORM == "f32" else 4
+    live = {}  # session id -> state
+    lat_all, lat_cls = [], {c[0]: [] for c in SERVE_CLASSES}
+    frames_done = 0
+    pix_done = 0
+    nxt = 0
+    barrier(ws)
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        now = time.perf_counter() - t0
+        while nxt < len(t_arr) and t_arr[nxt] <= now:
+            name, w, h, _ = SERVE_CLASSES[classes[nxt]]
+            sid = server.open(w, h, FORM, params)
+            live[sid] = {"cls": name, "w": w, "h": h, "n": lengths[nxt], "sent": 0, "done": 0,
+                         "out": {o: torch.empty(w * h * out_px, dtype=torch.uint8, device=dev)
+                                 for o in ("diffuse", "specular")}}
+            nxt += 1
+        if now > args.serve_seconds:
+            break
+        for sid, st in live.items():
+            if st["sent"] == st["done"] and st["sent"] < st["n"]:
+                f = st["sent"]
+                pi = f % (2 * POOL_FRAMES - 2)
+                pi = pi if pi < POOL_FRAMES else 2 * POOL_FRAMES - 2 - pi
+                bufs, fp = pools[st["cls"]][pi]
+                server.submit(sid, fp, f, bufs, st["out"], tag=f)
+                st["sent"] += 1
+        issued = server.step(sh)
+        if issued:
+            steps += 1
+        for sid, tag, lat, step_ms in server.poll(wait=True):
+            st = live[sid]
+            st["done"] += 1
+            lat_all.append(lat)
+            lat_cls[st["cls"]].append(lat)
+            frames_done += 1
+            pix_done += st["w"] * st["h"]
+            if st["done"] == st["n"]:
+                server.close_session(sid)
+        for sid in [k for k, v in live.items() if v["done"] == v["n"]]:
+            del live[sid]
+        if not issued and nxt < len(t_arr):
+            time.sleep(max(0.0, min(0.002, t_arr[nxt] - (time.perf_counter() - t0))))
+    elapsed = time.perf_counter() - t0
+    stats = server.stats()
+    server.close()
+    ctx.close()
+    del pools
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
+    def pct(x, q):
+        return float(np.percentile(x, q)) if x else None
+
+    return {
+        "workload": "Poisson %.0f sessions/s for %.0f s; 720p/1080p/1440p/2160p with p=0.3/0.4/0.2/0.1; 30-300 "
+                    "frames each; HBM budget %.0f GB; step pixel budget %.1f Mpix" % (
+                        args.serve_rate, args.serve_seconds, args.serve_hbm_gb, args.serve_step_mpix),
+        "storage": FORM, "sessions_arrived": len(t_arr), "sessions_admitted": stats["sessions_admitted"],
+        "sessions_completed": stats["sessions_closed"], "sessions_waiting_at_end": stats["sessions_waiting"],
+        "frames": frames_done, "steps": steps, "frames_per_step": frames_done / max(steps, 1),
+        "value": pix_done / elapsed / 1e6, "unit": "Mpix/s", "seconds": elapsed,
+        "latency_ms": {"p50": pct(lat_all, 50), "p99": pct(lat_all, 99)},
+        "latency_ms_by_class": {k: {"p50": pct(v, 50), "p99": pct(v, 99), "frames": len(v)}
+                                for k, v in lat_cls.items()},
+        "admit_wait_ms_mean": stats["admit_wait_ms_total"] / max(stats["sessions_admitted"], 1),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -557,6 +677,11 @@ def main():
     ap.add_argument("--cpu-frames", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-hbm-gb", type=float, default=150.0)
+    ap.add_argument("--serve-step-mpix", type=float, default=6.0)
     ap.add_argument("--batch-views", type=int, default=48)
     ap.add_argument("--batch-frames", type=int, default=32)
     args = ap.parse_args()

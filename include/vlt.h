@@ -225,6 +225,57 @@ typedef struct vlt_batch_stats {
 } vlt_batch_stats;
 vlt_status vlt_batch_get_stats(const vlt_batch* batch, vlt_batch_stats* out);
 
+/* ---------------------------------------------------------------- serving
+ *
+ * No counterpart in the reference. A server holds view-sessions whose state stays
+ * on the device across their frames. Sessions are admitted in arrival order as soon
+ * as the sum of admitted views' device bytes stays within hbm_budget_bytes and the
+ * sum of their pixels within step_pixel_budget (the per-step work, i.e. the latency
+ * knob; 0 = unlimited; a session is always admitted when none is live). Each step
+ * runs the next queued frame of every admitted session as one batch (vlt_batch_run)
+ * on the given stream; sessions admitted while steps are on the GPU join the next
+ * step. A frame's results are identical to running its session alone. */
+typedef struct vlt_server vlt_server;
+typedef struct vlt_server_config {
+  uint64_t hbm_budget_bytes;   /* admission: device bytes of the admitted views */
+  uint64_t step_pixel_budget;  /* admission: pixels of the admitted views (0: unlimited) */
+  uint32_t max_sessions;       /* admission: admitted sessions (0: unlimited) */
+} vlt_server_config;
+vlt_status vlt_server_create(vlt_ctx* ctx, const vlt_server_config* config, vlt_server** out);
+/* Waits for in-flight steps, frees every session's view. */
+vlt_status vlt_server_destroy(vlt_server* server);
+/* The server's batch executor (for vlt_batch_autotune, graphs, chunking). */
+vlt_batch* vlt_server_batch(vlt_server* server);
+/* Queues a new session; *session receives its id. VLT_ERR_BUDGET_EXCEEDED if its
+ * view alone exceeds the HBM budget. */
+vlt_status vlt_server_open(vlt_server* server, uint32_t width, uint32_t height, vlt_form form,
+                           const vlt_params* params, uint64_t* session);
+/* Queues one frame of an open session (frames run in submission order, one per
+ * step). The frame params are copied; the device inputs and outputs must stay
+ * valid until the frame is reported by vlt_server_poll. */
+vlt_status vlt_server_submit(vlt_server* server, uint64_t session, const vlt_frame_inputs* in,
+                             const vlt_frame_outputs* out, uint64_t tag);
+/* No more frames: the session's view is freed after its queued frames complete. */
+vlt_status vlt_server_close(vlt_server* server, uint64_t session);
+/* Admits waiting sessions that fit, then issues one step; *issued = frames in it. */
+vlt_status vlt_server_step(vlt_server* server, void* stream, uint32_t* issued);
+typedef struct vlt_server_completion {
+  uint64_t session, tag;
+  double latency_ms;  /* host clock: vlt_server_submit to completion seen by poll */
+  double step_ms;     /* host clock: the step's issue to completion seen by poll */
+} vlt_server_completion;
+/* Reports the frames of finished steps (oldest first, whole steps only, up to max);
+ * with wait != 0 blocks until the oldest in-flight step is done. */
+uint32_t vlt_server_poll(vlt_server* server, vlt_server_completion* out, uint32_t max, int wait);
+typedef struct vlt_server_stats {
+  uint64_t sessions_opened, sessions_admitted, sessions_closed;
+  uint64_t steps, frames_issued, frames_done, pixels_issued;
+  double admit_wait_ms_total;
+  uint32_t sessions_live, sessions_waiting, steps_in_flight;
+  uint64_t bytes_in_use, pixels_in_use;
+} vlt_server_stats;
+vlt_status vlt_server_get_stats(const vlt_server* server, vlt_server_stats* out);
+
 /* Per-pass GPU timers (the counterpart of the render graph's per-pass timestamp
  * queries, render_graph.rs:2321-2326, and NamedProfiling, gpu_profiling.rs:221-340).
  * When enabled, vlt_frame_run brackets every kernel with CUDA events on its stream.

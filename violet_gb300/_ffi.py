@@ -101,6 +101,22 @@ class TileChoice(C.Structure):
                 ("ns_per_kpix", C.c_float * TILE_CANDIDATES)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("step_pixel_budget", C.c_uint64), ("max_sessions", C.c_uint32)]
+
+
+class ServerCompletion(C.Structure):
+    _fields_ = [("session", C.c_uint64), ("tag", C.c_uint64), ("latency_ms", C.c_double), ("step_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("sessions_opened", C.c_uint64), ("sessions_admitted", C.c_uint64), ("sessions_closed", C.c_uint64),
+                ("steps", C.c_uint64), ("frames_issued", C.c_uint64), ("frames_done", C.c_uint64),
+                ("pixels_issued", C.c_uint64), ("admit_wait_ms_total", C.c_double), ("sessions_live", C.c_uint32),
+                ("sessions_waiting", C.c_uint32), ("steps_in_flight", C.c_uint32), ("bytes_in_use", C.c_uint64),
+                ("pixels_in_use", C.c_uint64)]
+
+
 class BatchStats(C.Structure):
     _fields_ = [("frames", C.c_uint64), ("launches", C.c_uint64), ("graph_replays", C.c_uint64),
                 ("graph_captures", C.c_uint64), ("arena_bytes", C.c_uint64), ("last_launches", C.c_uint32),
@@ -161,6 +177,15 @@ SIGNATURES = {
     "vlt_batch_autotune": (C.c_int, [P]),
     "vlt_batch_tile_table": (U32, [P, C.POINTER(TileChoice), U32]),
     "vlt_batch_get_stats": (C.c_int, [P, C.POINTER(BatchStats)]),
+    "vlt_server_create": (C.c_int, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
+    "vlt_server_destroy": (C.c_int, [P]),
+    "vlt_server_batch": (P, [P]),
+    "vlt_server_open": (C.c_int, [P, U32, U32, C.c_int, C.POINTER(Params), C.POINTER(C.c_uint64)]),
+    "vlt_server_submit": (C.c_int, [P, C.c_uint64, C.POINTER(FrameInputs), C.POINTER(FrameOutputs), C.c_uint64]),
+    "vlt_server_close": (C.c_int, [P, C.c_uint64]),
+    "vlt_server_step": (C.c_int, [P, P, C.POINTER(U32)]),
+    "vlt_server_poll": (U32, [P, C.POINTER(ServerCompletion), U32, C.c_int]),
+    "vlt_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
     "vlt_view_buffer": (P, [P, C.c_char_p, C.POINTER(C.c_size_t)]),
     "vlt_view_set_timing": (C.c_int, [P, C.c_int]),
     "vlt_view_read_timing": (U32, [P, C.POINTER(PassTime), U32]),

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libvlt.so")
 
-SOURCES = ["restir.cu", "denoise.cu", "denoise_f32.cu", "hashgrid.cu", "scene.cu", "launch.cu", "api.cu", "batch.cu"]
+SOURCES = ["restir.cu", "denoise.cu", "denoise_f32.cu", "hashgrid.cu", "scene.cu", "launch.cu", "api.cu", "batch.cu", "server.cu"]
 HEADERS = ["vlt_math.cuh", "vlt_device.cuh", "vlt_launch.cuh", "vlt_internal.h", "scene_gen.cuh"]
 
 NVCC_FLAGS = [

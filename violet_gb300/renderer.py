@@ -248,3 +248,65 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """View-sessions admitted by HBM and per-step pixel budgets; each step batches
+    the next queued frame of every admitted session (vlt_server_*)."""
+
+    def __init__(self, ctx, hbm_budget_bytes, step_pixel_budget=0, max_sessions=0):
+        self._lib = _ffi.load()
+        self.ctx = ctx
+        cfg = _ffi.ServerConfig(int(hbm_budget_bytes), int(step_pixel_budget), int(max_sessions))
+        h = C.c_void_p()
+        _ffi.check(self._lib.vlt_server_create(ctx.handle, C.byref(cfg), C.byref(h)), "vlt_server_create")
+        self.handle = h
+        self._keep = {}  # frame params / structs referenced by queued frames
+
+    def open(self, width, height, form="ref", params=None):
+        p = params if params is not None else params_reference()
+        sid = C.c_uint64()
+        _ffi.check(self._lib.vlt_server_open(self.handle, int(width), int(height), _ffi.FORMS[form], C.byref(p),
+                                             C.byref(sid)), "vlt_server_open")
+        return sid.value
+
+    def submit(self, session, frame_params, frame_index, inputs, outputs=None, tag=0):
+        fi, fo = _frame_structs(frame_params, frame_index, inputs, outputs)
+        _ffi.check(self._lib.vlt_server_submit(self.handle, C.c_uint64(session), C.byref(fi),
+                                               C.byref(fo) if outputs else None, C.c_uint64(tag)),
+                   "vlt_server_submit")
+
+    def close_session(self, session):
+        _ffi.check(self._lib.vlt_server_close(self.handle, C.c_uint64(session)), "vlt_server_close")
+
+    def step(self, stream=0):
+        n = C.c_uint32()
+        _ffi.check(self._lib.vlt_server_step(self.handle, C.c_void_p(stream), C.byref(n)), "vlt_server_step")
+        return n.value
+
+    def poll(self, wait=False, max_items=4096):
+        arr = (_ffi.ServerCompletion * max_items)()
+        n = self._lib.vlt_server_poll(self.handle, arr, max_items, 1 if wait else 0)
+        return [(arr[i].session, arr[i].tag, arr[i].latency_ms, arr[i].step_ms) for i in range(n)]
+
+    def batch_handle(self):
+        return self._lib.vlt_server_batch(self.handle)
+
+    def autotune(self):
+        _ffi.check(self._lib.vlt_batch_autotune(C.c_void_p(self.batch_handle())), "vlt_batch_autotune")
+
+    def stats(self):
+        st = _ffi.ServerStats()
+        _ffi.check(self._lib.vlt_server_get_stats(self.handle, C.byref(st)), "vlt_server_get_stats")
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def close(self):
+        if self.handle:
+            self._lib.vlt_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
