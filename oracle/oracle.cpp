@@ -337,11 +337,56 @@ inline void diff_f32_store(float* r, size_t j, uint32_t M, float W, float3 pos, 
   q[8] = rad.x, q[9] = rad.y, q[10] = rad.z, q[11] = 0.0f;
 }
 
-// ind_diff_temporal_resample.hlsl:49-200 in the F32 storage form.
+// f16 storage form of the diffuse reservoir: the 16-byte records of all n pixels
+// {HitPosNormal, radiance f16 x3, W f16}, then one M byte per pixel (M <= 255);
+// stores saturate to the largest finite f16, NaN -> 0.
+inline uint32_t f16sat_d(float f) {
+  if (isnan_(f)) return 0u;
+  return f32tof16(hmin(hmax(f, -65504.0f), 65504.0f));
+}
+inline DiffF32 diff_f16_load(const uint8_t* base, size_t n, size_t j) {
+  const uint32_t* r = (const uint32_t*)(base + 16 * j);
+  DiffF32 o;
+  HitPosNormal hit = HitPosNormal::decode(r[0], r[1]);
+  o.pos = hit.pos;
+  o.nrm = hit.normal;
+  o.rad = F3(f16tof32(r[2] & 0xFFFFu), f16tof32(r[2] >> 16), f16tof32(r[3] & 0xFFFFu));
+  o.W = f16tof32(r[3] >> 16);
+  o.M = base[16 * n + j];
+  return o;
+}
+inline void diff_f16_store(uint8_t* base, size_t n, size_t j, uint32_t M, float W, float3 pos, float3 nrm,
+                           float3 rad) {
+  uint32_t* r = (uint32_t*)(base + 16 * j);
+  HitPosNormal hpn = {F3(f16tof32(f16sat_d(pos.x)), f16tof32(f16sat_d(pos.y)), f16tof32(f16sat_d(pos.z))), nrm};
+  uint32_t e[2];
+  hpn.encode(e);
+  r[0] = e[0];
+  r[1] = e[1];
+  r[2] = f16sat_d(rad.x) | (f16sat_d(rad.y) << 16);
+  r[3] = f16sat_d(rad.z) | (f16sat_d(W) << 16);
+  base[16 * n + j] = (uint8_t)std::min(M, 255u);
+}
+// Form-generic access (FORM 1 = f32 records, 2 = f16 records).
+template <int FORM>
+inline DiffF32 diff_load(const void* p, size_t n, size_t j) {
+  if constexpr (FORM == 2) return diff_f16_load((const uint8_t*)p, n, j);
+  else return diff_f32_load((const float*)p, j);
+}
+template <int FORM>
+inline void diff_store(void* p, size_t n, size_t j, uint32_t M, float W, float3 pos, float3 nrm, float3 rad) {
+  if constexpr (FORM == 2) diff_f16_store((uint8_t*)p, n, j, M, W, pos, nrm, rad);
+  else diff_f32_store((float*)p, j, M, W, pos, nrm, rad);
+}
+
+// ind_diff_temporal_resample.hlsl:49-200 in the f32 / f16 storage forms (the sample
+// kept decoded).
+template <int FORM>
 void diff_temporal_f32(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const float* prev_depth,
                        const float* depth_buf, const uint32_t* new_hpn, const uint32_t* new_rad,
-                       const float* new_pdf, const float* prev_rsv, float* out, uint32_t frame_rand,
+                       const float* new_pdf, const void* prev_rsv, void* out, uint32_t frame_rand,
                        uint32_t has_prev_frame, uint32_t has_new_sample) {
+  const size_t npx = (size_t)w * h;
   const float3 empty_n = HitPosNormal::decode(0u, 0u).normal;
   ROWS_PARALLEL
   for (int y = 0; y < h; ++y)
@@ -368,7 +413,7 @@ void diff_temporal_f32(const vlt_frame_params& fp, int w, int h, const vlt_param
       if (sample_prev_frame) {
         int px = (int)to_uint(uv_reproj.x * (float)w), py = (int)to_uint(uv_reproj.y * (float)h);
         if (in_img(px, py, w, h)) {
-          DiffF32 r = diff_f32_load(prev_rsv, (size_t)py * w + px);
+          DiffF32 r = diff_load<FORM>(prev_rsv, npx, (size_t)py * w + px);
           M = r.M;
           W = r.W;
           hp = r.pos;
@@ -407,7 +452,7 @@ void diff_temporal_f32(const vlt_frame_params& fp, int w, int h, const vlt_param
         M += 1;
         W = reservoir_target_pdf > 0.0f ? w_sum / (reservoir_target_pdf * (float)M) : 0.0f;
       }
-      diff_f32_store(out, i, M, W, hp, hn, rad);
+      diff_store<FORM>(out, npx, i, M, W, hp, hn, rad);
     }
 }
 
@@ -419,11 +464,11 @@ struct WorkingReservoir {
   float3 hit_radiance, hit_pos, hit_normal;
   float target_pdf;
 };
-template <bool F32>
-WorkingReservoir wr_load(const void* rsv, size_t j, float3 pix_position_ws, float3 pix_normal) {
+template <int FORM>
+WorkingReservoir wr_load(const void* rsv, size_t n, size_t j, float3 pix_position_ws, float3 pix_normal) {
   WorkingReservoir o;
-  if constexpr (F32) {
-    DiffF32 r = diff_f32_load((const float*)rsv, j);
+  if constexpr (FORM != 0) {
+    DiffF32 r = diff_load<FORM>(rsv, n, j);
     o.M = r.M;
     o.W = r.W;
     o.hit_pos = r.pos;
@@ -443,12 +488,15 @@ WorkingReservoir wr_load(const void* rsv, size_t j, float3 pix_position_ws, floa
   return o;
 }
 
-// Lighting output: R11G11B10 (reference form) or float4 {rgb, 0} (F32 form).
-template <bool F32>
+// Lighting output: R11G11B10 (reference form), float4 {rgb, 0} (f32 form) or half4
+// {rgb, 0} (f16 form).
+template <int FORM>
 void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const uint32_t* gbuf,
                   const float* depth_buf, const void* ao_tex, const void* in, void* out, void* lighting,
                   uint32_t frame_rand) {
   const float3 empty_n = HitPosNormal::decode(0u, 0u).normal;
+  const size_t npx = (size_t)w * h;
+  constexpr bool F32 = FORM == 1;
   const uint32_t MAX_ITERATION = P.diff_spatial_taps;
   const float MIN_RADIUS = 1.5f;
   // Golden spiral constants (:148-150): B = log(1.61803398)/(0.5 PI), A = 1/exp(B 2PI).
@@ -464,6 +512,10 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
         if constexpr (F32) {
           diff_f32_store((float*)out, i, 0u, 0.0f, F3(0.0f), empty_n, F3(0.0f));
           if (lighting) memset((float*)lighting + 4 * i, 0, 16);
+        } else if constexpr (FORM == 2) {
+          memset((uint8_t*)out + 16 * i, 0, 16);
+          ((uint8_t*)out)[16 * npx + i] = 0;
+          if (lighting) memset((uint16_t*)lighting + 4 * i, 0, 8);
         } else {
           ((U4*)out)[i] = U4{0, 0, 0, 0};
           if (lighting) ((uint32_t*)lighting)[i] = 0;
@@ -473,7 +525,7 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
       const float3 position_ws = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
       float3 gnormal = load_gbuffer_normal(gbuf, x, y, w, h);
       float ao = ao_filtered_load<F32>(ao_tex, i);
-      WorkingReservoir reservoir = wr_load<F32>(in, i, position_ws, gnormal);
+      WorkingReservoir reservoir = wr_load<FORM>(in, npx, i, position_ws, gnormal);
       float w_sum = reservoir.W * reservoir.target_pdf * (float)reservoir.M;
       float radius = P.diff_spatial_radius_px > 0.0f ? P.diff_spatial_radius_px
                                                      : (float)std::min(w, h) * 0.05f;
@@ -500,7 +552,7 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
           radius = hmax(radius * 0.5f, MIN_RADIUS);
           continue;
         }
-        WorkingReservoir neighbor = wr_load<F32>(in, (size_t)ny * w + nx, position_ws, gnormal);
+        WorkingReservoir neighbor = wr_load<FORM>(in, npx, (size_t)ny * w + nx, position_ws, gnormal);
         float3 offset_qq = position_ws_n - neighbor.hit_pos;
         float3 offset_rq = position_ws - neighbor.hit_pos;
         float L2_qq = dot(offset_qq, offset_qq);
@@ -528,9 +580,9 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
         float target_pdf = reservoir.target_pdf;
         if (target_pdf > 0.0f) reservoir.W = w_sum / (target_pdf * (float)reservoir.M);
       }
-      if constexpr (F32) {
-        diff_f32_store((float*)out, i, reservoir.M, reservoir.W, reservoir.hit_pos, reservoir.hit_normal,
-                       reservoir.hit_radiance);
+      if constexpr (FORM != 0) {
+        diff_store<FORM>(out, npx, i, reservoir.M, reservoir.W, reservoir.hit_pos, reservoir.hit_normal,
+                         reservoir.hit_radiance);
       } else {
         U4* o = (U4*)out + i;
         o->x = reservoir_simple_encode_32b(reservoir.M, reservoir.W);
@@ -549,6 +601,9 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
         if constexpr (F32) {
           float* q = (float*)lighting + 4 * i;
           q[0] = l.x, q[1] = l.y, q[2] = l.z, q[3] = 0.0f;
+        } else if constexpr (FORM == 2) {
+          uint16_t* q = (uint16_t*)lighting + 4 * i;
+          q[0] = (uint16_t)f16sat_d(l.x), q[1] = (uint16_t)f16sat_d(l.y), q[2] = (uint16_t)f16sat_d(l.z), q[3] = 0;
         } else {
           ((uint32_t*)lighting)[i] = store_r11g11b10(l);
         }
@@ -597,7 +652,73 @@ inline float3 v3(const float* p) { return F3(p[0], p[1], p[2]); }
 // ==================================================== specular temporal
 // ind_spec_temporal_resample.hlsl:146-362. New samples are read from the inputs;
 // the merged reservoir goes to out_* (the shader updates the new-sample textures
+// Specular reservoir storage. Reference and f32 forms: three planes {M, asuint(W)},
+// {hit xyz, target function}, R11G11B10 radiance. f16 form: one 24-byte record per
+// pixel {hit f16 x3 | M u16, target function f32, W f32, radiance f16 x3}, passed in
+// the `hp` argument (rsv and rad unused); stores saturate.
+struct SpecRec {
+  uint32_t M;
+  float W;
+  float3 hit;
+  float tf;
+  float3 rad;
+  uint32_t rad_bits;  // three-plane forms: carried bit-exactly
+};
+inline uint32_t f16sat(float f) {
+  if (isnan_(f)) return 0u;
+  return f32tof16(hmin(hmax(f, -65504.0f), 65504.0f));
+}
+inline float q16(float f) { return f16tof32(f16sat(f)); }
+template <bool F16>
+SpecRec spec_load(const uint32_t* rsv, const float* hp, const uint32_t* rad, int x, int y, int w, int h) {
+  SpecRec r;
+  if constexpr (F16) {
+    uint32_t a0 = 0, a1 = 0, b0 = 0, b1 = 0, c0 = 0, c1 = 0;
+    if (in_img(x, y, w, h)) {
+      const uint32_t* q = (const uint32_t*)hp + 6 * ((size_t)y * w + x);
+      a0 = q[0], a1 = q[1], b0 = q[2], b1 = q[3], c0 = q[4], c1 = q[5];
+    }
+    r.hit = F3(f16tof32(a0 & 0xFFFFu), f16tof32(a0 >> 16), f16tof32(a1 & 0xFFFFu));
+    r.M = a1 >> 16;
+    r.tf = asfloat(b0);
+    r.W = asfloat(b1);
+    r.rad = F3(f16tof32(c0 & 0xFFFFu), f16tof32(c0 >> 16), f16tof32(c1 & 0xFFFFu));
+    r.rad_bits = 0;
+  } else {
+    U2 rs = Tex<U2>{(const U2*)rsv, w, h}(x, y);
+    F4s p4 = Tex<F4s>{(const F4s*)hp, w, h}(x, y);
+    r.M = rs.x;
+    r.W = asfloat(rs.y);
+    r.hit = F3(p4.x, p4.y, p4.z);
+    r.tf = p4.w;
+    r.rad_bits = Tex<uint32_t>{rad, w, h}(x, y);
+    r.rad = load_r11g11b10(r.rad_bits);
+  }
+  return r;
+}
+template <bool F16>
+void spec_store(uint32_t* rsv, float* hp, uint32_t* rad, size_t i, const SpecRec& r) {
+  if constexpr (F16) {
+    uint32_t* q = (uint32_t*)hp + 6 * i;
+    q[0] = f16sat(r.hit.x) | (f16sat(r.hit.y) << 16);
+    q[1] = f16sat(r.hit.z) | (std::min(r.M, 65535u) << 16);
+    q[2] = asuint(r.tf);
+    q[3] = asuint(r.W);
+    q[4] = f16sat(r.rad.x) | (f16sat(r.rad.y) << 16);
+    q[5] = f16sat(r.rad.z);
+  } else {
+    rsv[2 * i] = r.M;
+    rsv[2 * i + 1] = asuint(r.W);
+    hp[4 * i] = r.hit.x;
+    hp[4 * i + 1] = r.hit.y;
+    hp[4 * i + 2] = r.hit.z;
+    hp[4 * i + 3] = r.tf;
+    rad[i] = r.rad_bits;
+  }
+}
+
 // in place, so sky pixels keep the new sample there).
+template <bool F16>
 void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const float* prev_depth,
                    const uint32_t* prev_gbuf, const float* depth_buf, const uint32_t* gbuf, const uint32_t* prev_rsv,
                    const float* prev_hp, const uint32_t* prev_rad, const float* new_hp, const uint32_t* new_rad,
@@ -609,10 +730,14 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       size_t i = (size_t)y * w + x;
       float depth = depth_buf[i];
       if (has_no_geometry_via_depth(depth)) {
-        out_rsv[2 * i] = 0;
-        out_rsv[2 * i + 1] = 0;
-        memcpy(out_hp + 4 * i, new_hp + 4 * i, 16);
-        out_rad[i] = new_rad[i];
+        SpecRec z;
+        z.M = 0;
+        z.W = 0.0f;
+        z.hit = F3(new_hp[4 * i], new_hp[4 * i + 1], new_hp[4 * i + 2]);
+        z.tf = new_hp[4 * i + 3];
+        z.rad_bits = new_rad[i];
+        z.rad = load_r11g11b10(new_rad[i]);
+        spec_store<F16>(out_rsv, out_hp, out_rad, i, z);
         continue;
       }
       const float3 position_ws = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
@@ -636,14 +761,13 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       GBuffer prev_gbuffer;
       if (sample_prev_frame) {
         int px = (int)to_uint(uv_reproj.x * (float)w), py = (int)to_uint(uv_reproj.y * (float)h);
-        U2 r = Tex<U2>{(const U2*)prev_rsv, w, h}(px, py);
-        M = r.x;
-        W = asfloat(r.y);
-        F4s hp = Tex<F4s>{(const F4s*)prev_hp, w, h}(px, py);
-        reservoir_hit_pos = F3(hp.x, hp.y, hp.z);
-        reservoir_rad_bits = Tex<uint32_t>{prev_rad, w, h}(px, py);
-        reservoir_hit_radiance = load_r11g11b10(reservoir_rad_bits);
-        reservoir_target_function = hp.w;
+        SpecRec r = spec_load<F16>(prev_rsv, prev_hp, prev_rad, px, py, w, h);
+        M = r.M;
+        W = r.W;
+        reservoir_hit_pos = r.hit;
+        reservoir_rad_bits = r.rad_bits;
+        reservoir_hit_radiance = r.rad;
+        reservoir_target_function = r.tf;
         prev_gbuffer = load_gbuffer(prev_gbuf, px, py, w, h);
       } else {
         M = 0;
@@ -694,6 +818,7 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       if (!use_prev_sample) {
         reservoir_hit_pos = new_sample_hit_pos;
         reservoir_rad_bits = new_rad[i];
+        reservoir_hit_radiance = new_sample_hit_radiance;
         reservoir_target_function = new_target_function;
       }
       M += 1;
@@ -703,13 +828,14 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       } else {
         W = 0.0f;
       }
-      out_rsv[2 * i] = M;
-      out_rsv[2 * i + 1] = asuint(W);
-      out_hp[4 * i] = reservoir_hit_pos.x;
-      out_hp[4 * i + 1] = reservoir_hit_pos.y;
-      out_hp[4 * i + 2] = reservoir_hit_pos.z;
-      out_hp[4 * i + 3] = reservoir_target_function;
-      out_rad[i] = reservoir_rad_bits;
+      SpecRec o;
+      o.M = M;
+      o.W = W;
+      o.hit = reservoir_hit_pos;
+      o.tf = reservoir_target_function;
+      o.rad = reservoir_hit_radiance;
+      o.rad_bits = reservoir_rad_bits;
+      spec_store<F16>(out_rsv, out_hp, out_rad, i, o);
     }
 }
 
@@ -717,16 +843,23 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
 // ind_spec_spatial_resample.hlsl:169-448 (+ optional merged-reservoir output).
 // Lighting output: R11G11B10 plus a half ray length (reference form), or float4
 // {rgb, ray length} (F32 form, ray_len_out unused).
-template <bool F32>
+template <int FORM>
 void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const uint32_t* gbuf,
                   const float* depth_buf, const uint32_t* rsv, const float* hp_tex, const uint32_t* rad_tex,
                   void* lighting, uint16_t* ray_len_out, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
                   uint32_t frame_rand) {
+  constexpr bool F16 = FORM == 2;
   auto store_light = [&](size_t i, float3 v, float ray_len) {
-    if constexpr (F32) {
+    if constexpr (FORM == 1) {
       if (lighting) {
         float* q = (float*)lighting + 4 * i;
         q[0] = v.x, q[1] = v.y, q[2] = v.z, q[3] = ray_len;
+      }
+    } else if constexpr (FORM == 2) {
+      if (lighting) {
+        uint16_t* q = (uint16_t*)lighting + 4 * i;
+        q[0] = (uint16_t)f16sat(v.x), q[1] = (uint16_t)f16sat(v.y), q[2] = (uint16_t)f16sat(v.z);
+        q[3] = (uint16_t)f16sat(ray_len);
       }
     } else {
       if (lighting) ((uint32_t*)lighting)[i] = store_r11g11b10(v);
@@ -742,24 +875,25 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
       float depth = depth_buf[i];
       if (has_no_geometry_via_depth(depth)) {
         store_light(i, F3(0.0f), 0.0f);
-        if (out_rsv) {
-          out_rsv[2 * i] = 0;
-          out_rsv[2 * i + 1] = 0;
-          memcpy(out_hp + 4 * i, hp_tex + 4 * i, 16);
-          out_rad[i] = rad_tex[i];
+        if (out_hp) {
+          SpecRec z = spec_load<F16>(rsv, hp_tex, rad_tex, x, y, w, h);
+          z.M = 0;
+          z.W = 0.0f;
+          spec_store<F16>(out_rsv, out_hp, out_rad, i, z);
         }
         continue;
       }
       const float3 position_ws = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
       GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
-      uint32_t M = rsv[2 * i];
-      float W = asfloat(rsv[2 * i + 1]);
-      float3 hit_pos = F3(hp_tex[4 * i], hp_tex[4 * i + 1], hp_tex[4 * i + 2]);
-      uint32_t rad_bits = rad_tex[i];
-      float3 hit_radiance = load_r11g11b10(rad_bits);
+      const SpecRec c0 = spec_load<F16>(rsv, hp_tex, rad_tex, x, y, w, h);
+      uint32_t M = c0.M;
+      float W = c0.W;
+      float3 hit_pos = c0.hit;
+      uint32_t rad_bits = c0.rad_bits;
+      float3 hit_radiance = c0.rad;
       float3 view_pos = v3(fp.view_pos);
       float3 center_f0 = get_specular_f0(gbuffer.color, gbuffer.metallic);
-      float reservoir_target_function = hp_tex[4 * i + 3];
+      float reservoir_target_function = c0.tf;
       const uint32_t num_iteration = to_uint(lerp(0.0f, (float)MAX_ITERATION, gbuffer.perceptual_roughness));
       float radius = P.spec_spatial_radius_px > 0.0f ? P.spec_spatial_radius_px : (float)std::min(w, h) * 0.05f;
       uint32_t rng_state = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
@@ -786,12 +920,13 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
           radius = hmax(radius * 0.5f, 1.5f);
           continue;
         }
-        uint32_t M_n = rsv[2 * j];
-        float W_n = asfloat(rsv[2 * j + 1]);
-        float3 hit_pos_n = F3(hp_tex[4 * j], hp_tex[4 * j + 1], hp_tex[4 * j + 2]);
-        uint32_t rad_n_bits = rad_tex[j];
-        float3 hit_radiance_n = load_r11g11b10(rad_n_bits);
-        float reservoir_target_function_n = hp_tex[4 * j + 3];
+        const SpecRec nb = spec_load<F16>(rsv, hp_tex, rad_tex, nx, ny, w, h);
+        uint32_t M_n = nb.M;
+        float W_n = nb.W;
+        float3 hit_pos_n = nb.hit;
+        uint32_t rad_n_bits = nb.rad_bits;
+        float3 hit_radiance_n = nb.rad;
+        float reservoir_target_function_n = nb.tf;
         float w_neighb, w_center;
         {
           float center_tf_on_center = reservoir_target_function;
@@ -827,14 +962,15 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
           W = 0.0f;
       }
       float ray_len = length(hit_pos - position_ws);
-      if (out_rsv) {
-        out_rsv[2 * i] = M;
-        out_rsv[2 * i + 1] = asuint(W);
-        out_hp[4 * i] = hit_pos.x;
-        out_hp[4 * i + 1] = hit_pos.y;
-        out_hp[4 * i + 2] = hit_pos.z;
-        out_hp[4 * i + 3] = reservoir_target_function;
-        out_rad[i] = rad_bits;
+      if (out_hp) {
+        SpecRec o;
+        o.M = M;
+        o.W = W;
+        o.hit = hit_pos;
+        o.tf = reservoir_target_function;
+        o.rad = hit_radiance;
+        o.rad_bits = rad_bits;
+        spec_store<F16>(out_rsv, out_hp, out_rad, i, o);
       }
       if (lighting) {
         float3 specular_f0 = center_f0;
@@ -858,7 +994,7 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
         float3 specular_reflectance = hmax(ggx_brdf_integral_approx(NoV, roughness, specular_f0), 1.0f / 65536.0f);
         lt = lt / specular_reflectance;
         store_light(i, lt, ray_len);
-      } else if (!F32 && ray_len_out) {
+      } else if (FORM == 0 && ray_len_out) {
         ray_len_out[i] = (uint16_t)f32tof16(ray_len);
       }
     }
@@ -1380,22 +1516,72 @@ inline void rec_store(float* r, size_t j, float3 d, float3 s, float2 aux) {
   q[0] = d.x, q[1] = d.y, q[2] = d.z, q[3] = aux.x;
   q[4] = s.x, q[5] = s.y, q[6] = s.z, q[7] = aux.y;
 }
-inline float quad_max_history_f(const float* len, int x, int y, int w, int h) {
+// Storage of the f32 form (FORM 1: 8 floats per record, float history length,
+// float4 lighting) and the f16 form (FORM 2: 8 halves per record, half history
+// length, half4 lighting; stores saturate).
+template <int FORM>
+struct Dio;
+template <>
+struct Dio<1> {
+  static Rec32 load(const void* p, size_t j) { return rec_load((const float*)p, j); }
+  static void store(void* p, size_t j, float3 d, float3 s, float2 aux) { rec_store((float*)p, j, d, s, aux); }
+  static void copy(void* o, const void* in, size_t j) { memcpy((char*)o + 32 * j, (const char*)in + 32 * j, 32); }
+  static float len(const void* p, size_t j) { return ((const float*)p)[j]; }
+  static void set_len(void* p, size_t j, float v) { ((float*)p)[j] = v; }
+  static float4 light(const void* p, size_t j) {
+    const float* q = (const float*)p + 4 * j;
+    return F4(q[0], q[1], q[2], q[3]);
+  }
+  static void out(void* p, size_t j, float3 v) {
+    float* q = (float*)p + 4 * j;
+    q[0] = v.x, q[1] = v.y, q[2] = v.z, q[3] = 0.0f;
+  }
+};
+template <>
+struct Dio<2> {
+  static Rec32 load(const void* p, size_t j) {
+    const uint16_t* q = (const uint16_t*)p + 8 * j;
+    return Rec32{F3(f16tof32(q[0]), f16tof32(q[1]), f16tof32(q[2])), F3(f16tof32(q[4]), f16tof32(q[5]), f16tof32(q[6])),
+                 F2(f16tof32(q[3]), f16tof32(q[7]))};
+  }
+  static void store(void* p, size_t j, float3 d, float3 s, float2 aux) {
+    uint16_t* q = (uint16_t*)p + 8 * j;
+    q[0] = (uint16_t)f16sat(d.x), q[1] = (uint16_t)f16sat(d.y), q[2] = (uint16_t)f16sat(d.z);
+    q[3] = (uint16_t)f16sat(aux.x);
+    q[4] = (uint16_t)f16sat(s.x), q[5] = (uint16_t)f16sat(s.y), q[6] = (uint16_t)f16sat(s.z);
+    q[7] = (uint16_t)f16sat(aux.y);
+  }
+  static void copy(void* o, const void* in, size_t j) { memcpy((char*)o + 16 * j, (const char*)in + 16 * j, 16); }
+  static float len(const void* p, size_t j) { return f16tof32(((const uint16_t*)p)[j]); }
+  static void set_len(void* p, size_t j, float v) { ((uint16_t*)p)[j] = (uint16_t)f16sat(v); }
+  static float4 light(const void* p, size_t j) {
+    const uint16_t* q = (const uint16_t*)p + 4 * j;
+    return F4(f16tof32(q[0]), f16tof32(q[1]), f16tof32(q[2]), f16tof32(q[3]));
+  }
+  static void out(void* p, size_t j, float3 v) {
+    uint16_t* q = (uint16_t*)p + 4 * j;
+    q[0] = (uint16_t)f16sat(v.x), q[1] = (uint16_t)f16sat(v.y), q[2] = (uint16_t)f16sat(v.z), q[3] = 0;
+  }
+};
+template <int FORM>
+inline float quad_max_history_f(const void* len, int x, int y, int w, int h) {
   int x0 = x & ~1, y0 = y & ~1;
   float m = 0.0f;
   for (int k = 0; k < 4; ++k) {
     int px = x0 + (k & 1), py = y0 + (k >> 1);
-    m = hmax(m, in_img(px, py, w, h) ? len[(size_t)py * w + px] : 0.0f);
+    m = hmax(m, in_img(px, py, w, h) ? Dio<FORM>::len(len, (size_t)py * w + px) : 0.0f);
   }
   return m;
 }
 
 // svgf_temporal_filter.hlsl:96-362. Inputs: diffuse lighting float4 {rgb, 0},
 // specular lighting float4 {rgb, ray length}.
+template <int FORM>
 void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P, const float* depth_tex,
-                   const uint32_t* gbuf, const float* diff_src, const float* spec_src, const float* prev_depth,
-                   const uint32_t* prev_gbuf, const float* hist, const float* len_hist, const float* fast_hist,
-                   float* out, float* out_len, float* out_fast, uint32_t has_history, uint32_t fast_history) {
+                   const uint32_t* gbuf, const void* diff_src, const void* spec_src, const float* prev_depth,
+                   const uint32_t* prev_gbuf, const void* hist, const void* len_hist, const void* fast_hist,
+                   void* out, void* out_len, void* out_fast, uint32_t has_history, uint32_t fast_history) {
+  using IO = Dio<FORM>;
   const float BLEND_FACTOR_DIFF = 1.0f / P.history_max_frames;
   const float BLEND_FACTOR_FAST = 1.0f / 3.0f;
   ROWS_PARALLEL
@@ -1404,9 +1590,9 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       size_t i = (size_t)y * w + x;
       float depth = depth_tex[i];
       if (has_no_geometry_via_depth(depth)) {
-        out_len[i] = 0.0f;
-        rec_store(out, i, F3(0.0f), F3(0.0f), F2(0.0f, 0.0f));
-        if (fast_history) rec_store(out_fast, i, F3(0.0f), F3(0.0f), F2(0.0f, 0.0f));
+        IO::set_len(out_len, i, 0.0f);
+        IO::store(out, i, F3(0.0f), F3(0.0f), F2(0.0f, 0.0f));
+        if (fast_history) IO::store(out_fast, i, F3(0.0f), F3(0.0f), F2(0.0f, 0.0f));
         continue;
       }
       const float2 screen_uv = F2(((float)x + 0.5f) / (float)w, ((float)y + 0.5f) / (float)h);
@@ -1415,8 +1601,8 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       for (int dx = -1; dx <= 1; dx++)
         for (int dy = -1; dy <= 1; dy++) {
           int px = std::min(std::max(x + dx, 0), w - 1), py = std::min(std::max(y + dy, 0), h - 1);
-          const float* q = spec_src + 4 * ((size_t)py * w + px);
-          float3 sv = F3(q[0], q[1], q[2]);
+          float4 q = IO::light(spec_src, (size_t)py * w + px);
+          float3 sv = F3(q.x, q.y, q.z);
           m1 += sv;
           m2 += sv * sv;
         }
@@ -1426,7 +1612,7 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       float3 vsh = F3(0.0f), vsfh = F3(0.0f);
       {
         float3 view_ray_dir = normalize(position - v3(fp.view_pos));
-        float3 vp = position + view_ray_dir * spec_src[4 * i + 3];
+        float3 vp = position + view_ray_dir * IO::light(spec_src, i).w;
         float4 hr = mul(fp.prev_view_proj, F4(vp.x, vp.y, vp.z, 1.0f));
         float2 ndc_reproj = F2(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3]);
         float2 vuv = F2((ndc_reproj.x + fp.jitter[0]) * 0.5f + 0.5f, (ndc_reproj.y + fp.jitter[1]) * 0.5f + 0.5f);
@@ -1435,11 +1621,11 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
           Bilinear b = bilinear(vuv, w, h);
           size_t a = (size_t)b.y0 * w + b.x0, bb = (size_t)b.y0 * w + b.x1, c = (size_t)b.y1 * w + b.x0,
                  d = (size_t)b.y1 * w + b.x1;
-          vsh = blerp(rec_load(hist, a).s, rec_load(hist, bb).s, rec_load(hist, c).s, rec_load(hist, d).s, b.fx,
+          vsh = blerp(IO::load(hist, a).s, IO::load(hist, bb).s, IO::load(hist, c).s, IO::load(hist, d).s, b.fx,
                       b.fy);
           if (fast_history)
-            vsfh = blerp(rec_load(fast_hist, a).s, rec_load(fast_hist, bb).s, rec_load(fast_hist, c).s,
-                         rec_load(fast_hist, d).s, b.fx, b.fy);
+            vsfh = blerp(IO::load(fast_hist, a).s, IO::load(fast_hist, bb).s, IO::load(fast_hist, c).s,
+                         IO::load(fast_hist, d).s, b.fx, b.fy);
         }
       }
       float2 motion_vector;
@@ -1478,13 +1664,13 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
             if (!(fabsf(prev_depth[j] - reproj_depth) < depth_tol && dot(n_diff, n_diff) < normal_tol_sq)) continue;
             float wt = weights[oy][ox];
             wsum += wt;
-            hs += wt * len_hist[j];
-            Rec32 rr = rec_load(hist, j);
+            hs += wt * IO::len(len_hist, j);
+            Rec32 rr = IO::load(hist, j);
             ds = fma3(wt, rr.d, ds);
             ss = fma3(wt, rr.s, ss);
             ms = F2(fma_(wt, rr.aux.x, ms.x), fma_(wt, rr.aux.y, ms.y));
             if (fast_history) {
-              Rec32 f = rec_load(fast_hist, j);
+              Rec32 f = IO::load(fast_hist, j);
               dfs = fma3(wt, f.d, dfs);
               sfs = fma3(wt, f.s, sfs);
             }
@@ -1506,8 +1692,9 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
         hl = 0.0f;
       }
       hl += HISTORY_LEN_UNIT;
-      float3 dsrc = F3(diff_src[4 * i], diff_src[4 * i + 1], diff_src[4 * i + 2]);
-      float3 ssrc = F3(spec_src[4 * i], spec_src[4 * i + 1], spec_src[4 * i + 2]);
+      const float4 dl = IO::light(diff_src, i), sl = IO::light(spec_src, i);
+      float3 dsrc = F3(dl.x, dl.y, dl.z);
+      float3 ssrc = F3(sl.x, sl.y, sl.z);
       float2 lsrc = F2(lum_fma(dsrc), lum_fma(ssrc));
       float2 smsrc = lsrc * lsrc;
       float blurness = sqrtf(saturate(gbuffer.perceptual_roughness * 6.0f));
@@ -1533,23 +1720,24 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
           sff = lerp(d2, ssrc, alpha_fast.y);
         }
       }
-      rec_store(out, i, df, sf, smf);
-      out_len[i] = hl;
-      if (fast_history) rec_store(out_fast, i, dff, sff, F2(0.0f, 0.0f));
+      IO::store(out, i, df, sf, smf);
+      IO::set_len(out_len, i, hl);
+      if (fast_history) IO::store(out_fast, i, dff, sff, F2(0.0f, 0.0f));
     }
 }
 
 // relax_disocclusion_fix.hlsl:27-122.
-void dn32_fix(int w, int h, const float* depth_tex, const uint32_t* gbuf, const float* len, const float* in,
-              float* out) {
+template <int FORM>
+void dn32_fix(int w, int h, const float* depth_tex, const uint32_t* gbuf, const void* len, const void* in, void* out) {
+  using IO = Dio<FORM>;
   ROWS_PARALLEL
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t i = (size_t)y * w + x;
-      float hl = len[i];
-      float qmax = quad_max_history_f(len, x, y, w, h);
+      float hl = IO::len(len, i);
+      float qmax = quad_max_history_f<FORM>(len, x, y, w, h);
       if (hl == 0.0f) {
-        rec_store(out, i, F3(0.0f), F3(0.0f), F2(0.0f, 0.0f));
+        IO::store(out, i, F3(0.0f), F3(0.0f), F2(0.0f, 0.0f));
         continue;
       }
       hl = qmax;
@@ -1567,21 +1755,23 @@ void dn32_fix(int w, int h, const float* depth_tex, const uint32_t* gbuf, const 
             size_t j = (size_t)uy * w + ux;
             float2 wt = es.weight(length(F2((float)cx, (float)cy)), depth_tex[j],
                                   load_gbuffer_normal(gbuf, ux, uy, w, h), F2(0.0f, 0.0f));
-            Rec32 r = rec_load(in, j);
+            Rec32 r = IO::load(in, j);
             ws += wt;
             dsum = fma3(wt.x, r.d, dsum);
             ssum = fma3(wt.y, r.s, ssum);
             ms = F2(fma_(wt.x, r.aux.x, ms.x), fma_(wt.y, r.aux.y, ms.y));
           }
-        rec_store(out, i, dsum * (1.0f / ws.x), ssum * (1.0f / ws.y), F2(ms.x / ws.x, ms.y / ws.y));
+        IO::store(out, i, dsum * (1.0f / ws.x), ssum * (1.0f / ws.y), F2(ms.x / ws.x, ms.y / ws.y));
       } else {
-        memcpy(out + 8 * i, in + 8 * i, 32);
+        IO::copy(out, in, i);
       }
     }
 }
 
 // relax_fast_history_clamp.hlsl:11-75 (in place on `rec`).
-void dn32_fast_clamp(int w, int h, const float* fast, float* rec) {
+template <int FORM>
+void dn32_fast_clamp(int w, int h, const void* fast, void* rec) {
+  using IO = Dio<FORM>;
   ROWS_PARALLEL
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
@@ -1590,7 +1780,7 @@ void dn32_fast_clamp(int w, int h, const float* fast, float* rec) {
       for (int oy = -1; oy <= 1; oy++)
         for (int ox = -1; ox <= 1; ox++) {
           int cx = std::min(std::max(x + ox, 0), w - 1), cy = std::min(std::max(y + oy, 0), h - 1);
-          Rec32 f = rec_load(fast, (size_t)cy * w + cx);
+          Rec32 f = IO::load(fast, (size_t)cy * w + cx);
           float3 d = rgb_to_yCoCg(f.d), s = rgb_to_yCoCg(f.s);
           dm1 += d;
           dm2 += d * d;
@@ -1603,24 +1793,26 @@ void dn32_fast_clamp(int w, int h, const float* fast, float* rec) {
       sm2 = sm2 / 9.0f;
       float3 ddev = sqrt3(dm2 - dm1 * dm1) * 0.75f;
       float3 sdev = sqrt3(sm2 - sm1 * sm1) * 0.75f;
-      Rec32 c = rec_load(rec, i);
+      Rec32 c = IO::load(rec, i);
       float3 d = hclamp(rgb_to_yCoCg(c.d), dm1 - ddev, dm1 + ddev);
       float3 s = hclamp(rgb_to_yCoCg(c.s), sm1 - sdev, sm1 + sdev);
-      rec_store(rec, i, yCoCg_to_rgb(d), yCoCg_to_rgb(s), c.aux);
+      IO::store(rec, i, yCoCg_to_rgb(d), yCoCg_to_rgb(s), c.aux);
     }
 }
 
 // svgf_spatial_fallback_filter.hlsl:25-125.
-void dn32_fallback(int w, int h, const float* depth_tex, const uint32_t* gbuf, const float* len, const float* in,
-                   float* out) {
+template <int FORM>
+void dn32_fallback(int w, int h, const float* depth_tex, const uint32_t* gbuf, const void* len, const void* in,
+                   void* out) {
+  using IO = Dio<FORM>;
   ROWS_PARALLEL
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t i = (size_t)y * w + x;
-      float hl = len[i];
-      float qmax = quad_max_history_f(len, x, y, w, h);
+      float hl = IO::len(len, i);
+      float qmax = quad_max_history_f<FORM>(len, x, y, w, h);
       if (hl == 0.0f) {
-        rec_store(out, i, F3(0.0f), F3(0.0f), F2(0.0f, 0.0f));
+        IO::store(out, i, F3(0.0f), F3(0.0f), F2(0.0f, 0.0f));
         continue;
       }
       hl = qmax;
@@ -1639,7 +1831,7 @@ void dn32_fallback(int w, int h, const float* depth_tex, const uint32_t* gbuf, c
             size_t j = (size_t)uy * w + ux;
             float wt = es.weight(length(F2((float)ox, (float)oy)), depth_tex[j],
                                  load_gbuffer_normal(gbuf, ux, uy, w, h), F2(0.0f, 0.0f)).x;
-            Rec32 r = rec_load(in, j);
+            Rec32 r = IO::load(in, j);
             ws += wt;
             dsum = fma3(wt, r.d, dsum);
             ssum = fma3(wt, r.s, ssum);
@@ -1650,7 +1842,7 @@ void dn32_fallback(int w, int h, const float* depth_tex, const uint32_t* gbuf, c
         sd = ssum * inv;
         md = ms * inv;
       } else {
-        Rec32 r = rec_load(in, i);
+        Rec32 r = IO::load(in, i);
         dd = r.d;
         sd = r.s;
         md = r.aux;
@@ -1658,21 +1850,23 @@ void dn32_fallback(int w, int h, const float* depth_tex, const uint32_t* gbuf, c
       float2 fst = F2(lum_fma(dd), lum_fma(sd));
       float2 var = F2(hmax(fma_(-fst.x, fst.x, md.x), 0.0f), hmax(fma_(-fst.y, fst.y, md.y), 0.0f));
       float boost = hmax(1.0f, (4.0f * HISTORY_LEN_UNIT) / hl);
-      rec_store(out, i, dd, sd, var * boost);
+      IO::store(out, i, dd, sd, var * boost);
     }
 }
 
 // svgf_atrous_filter.hlsl:23-88 (off-axis taps only, as the reference's loop
 // condition selects). out_diff / out_spec: float4 {rgb, 0}.
-void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, const float* in, float* out,
-                 float* out_diff, float* out_spec, int step) {
+template <int FORM>
+void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, const void* in, void* out,
+                 void* out_diff, void* out_spec, int step) {
+  using IO = Dio<FORM>;
   const float kernel_weights[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
   ROWS_PARALLEL
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t i = (size_t)y * w + x;
       GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
-      Rec32 c = rec_load(in, i);
+      Rec32 c = IO::load(in, i);
       EdgeStop32 es = EdgeStop32::create(depth_tex[i], gbuffer.fwidth_z, 1.0f, gbuffer.normal, 7);
       es.use_lumi = true;
       es.lumi_center = F2(lum_fma(c.d), lum_fma(c.s));
@@ -1696,7 +1890,7 @@ void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, con
           if (!in_img(ux, uy, w, h)) continue;
           const float kw = kwy * kernel_weights[std::abs(ox)];
           size_t j = (size_t)uy * w + ux;
-          Rec32 r = rec_load(in, j);
+          Rec32 r = IO::load(in, j);
           float2 e = es.weight_rz(rz[std::abs(oy)][std::abs(ox)], depth_tex[j],
                                   load_gbuffer_normal(gbuf, ux, uy, w, h), F2(lum_fma(r.d), lum_fma(r.s)));
           float2 wt = F2(kw * e.x, kw * e.y);
@@ -1709,15 +1903,9 @@ void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, con
       float2 inv = F2(1.0f / wsum.x, 1.0f / wsum.y);
       float3 dd = dsum * inv.x, sd = ssum * inv.y;
       float2 vd = F2(vsum.x * inv.x * inv.x, vsum.y * inv.y * inv.y);
-      if (out) rec_store(out, i, dd, sd, vd);
-      if (out_diff) {
-        float* q = out_diff + 4 * i;
-        q[0] = dd.x, q[1] = dd.y, q[2] = dd.z, q[3] = 0.0f;
-      }
-      if (out_spec) {
-        float* q = out_spec + 4 * i;
-        q[0] = sd.x, q[1] = sd.y, q[2] = sd.z, q[3] = 0.0f;
-      }
+      if (out) IO::store(out, i, dd, sd, vd);
+      if (out_diff) IO::out(out_diff, i, dd);
+      if (out_spec) IO::out(out_spec, i, sd);
     }
 }
 
@@ -1950,10 +2138,12 @@ struct OView {
   std::vector<uint32_t> diff_light, spec_light, variance, sel, cidx, caddr;
   std::vector<uint16_t> ray_len, ao_filtered;
   uint32_t ccount = 0;
-  // F32 storage form: these replace the reference-form buffers of the same role.
-  bool f32 = false;
-  std::vector<float> diff_prev32, ao_prev32, ao_filtered32, diff_light32, spec_light32, hist_rec, hist_len32,
-      fast_prev32, fallback_rec;
+  // Float storage forms (1 = f32, 2 = f16): these byte buffers replace the
+  // reference-form buffers of the same role (the f16 form's specular records live in
+  // spec_hp_prev, 24 bytes per pixel).
+  int form = 0;
+  std::vector<uint8_t> fdiff_prev, fao_prev, fao_filtered, fdiff_light, fspec_light, fhist_rec, fhist_len, ffast_prev,
+      ffallback;
 };
 
 struct FrameRand {
@@ -1990,23 +2180,39 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
             in.diff_hit_radiance, v.hg_queries.data(), &v.hg_qcount);
   (void)frame_rand.next();  // diffuse sample generation
 
-  if (v.f32) {
-    std::vector<float> ao_cur(2 * n);
-    ao_gen<true>(fp, w, h, in.diff_hit_pos_normal, in.depth, v.ao_prev32.data(), ao_cur.data(), 1u,
-                 has_prev ? 1u : 0u, P.ao_radius);
-    ao_filter<true>(w, h, in.depth, ao_cur.data(), v.ao_filtered32.data());
-    v.ao_prev32.swap(ao_cur);
-    std::vector<float> temp(12 * n), sp(12 * n);
-    diff_temporal_f32(fp, w, h, P, prev_depth, in.depth, in.diff_hit_pos_normal, in.diff_hit_radiance,
-                      in.diff_source_pdf, v.diff_prev32.data(), temp.data(), frame_rand.next(), has_prev ? 1u : 0u,
-                      1u);
+  if (v.form != 0) {
+    const bool f32 = v.form == 1;
+    std::vector<uint8_t> ao_cur(v.fao_prev.size());
+    if (f32) {
+      ao_gen<true>(fp, w, h, in.diff_hit_pos_normal, in.depth, v.fao_prev.data(), ao_cur.data(), 1u,
+                   has_prev ? 1u : 0u, P.ao_radius);
+      ao_filter<true>(w, h, in.depth, ao_cur.data(), v.fao_filtered.data());
+    } else {
+      ao_gen<false>(fp, w, h, in.diff_hit_pos_normal, in.depth, v.fao_prev.data(), ao_cur.data(), 1u,
+                    has_prev ? 1u : 0u, P.ao_radius);
+      ao_filter<false>(w, h, in.depth, ao_cur.data(), v.fao_filtered.data());
+    }
+    v.fao_prev.swap(ao_cur);
+    std::vector<uint8_t> temp(v.fdiff_prev.size()), sp(v.fdiff_prev.size());
+    const uint32_t seed_dt = frame_rand.next();
+    if (f32)
+      diff_temporal_f32<1>(fp, w, h, P, prev_depth, in.depth, in.diff_hit_pos_normal, in.diff_hit_radiance,
+                           in.diff_source_pdf, v.fdiff_prev.data(), temp.data(), seed_dt, has_prev ? 1u : 0u, 1u);
+    else
+      diff_temporal_f32<2>(fp, w, h, P, prev_depth, in.depth, in.diff_hit_pos_normal, in.diff_hit_radiance,
+                           in.diff_source_pdf, v.fdiff_prev.data(), temp.data(), seed_dt, has_prev ? 1u : 0u, 1u);
     for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
       bool last = k + 1 == P.diff_spatial_passes;
-      diff_spatial<true>(fp, w, h, P, in.gbuffer, in.depth, v.ao_filtered32.data(), temp.data(), sp.data(),
-                         last ? v.diff_light32.data() : nullptr, frame_rand.next());
+      const uint32_t seed = frame_rand.next();
+      if (f32)
+        diff_spatial<1>(fp, w, h, P, in.gbuffer, in.depth, v.fao_filtered.data(), temp.data(), sp.data(),
+                        last ? v.fdiff_light.data() : nullptr, seed);
+      else
+        diff_spatial<2>(fp, w, h, P, in.gbuffer, in.depth, v.fao_filtered.data(), temp.data(), sp.data(),
+                        last ? v.fdiff_light.data() : nullptr, seed);
       temp.swap(sp);
     }
-    v.diff_prev32.swap(temp);
+    v.fdiff_prev.swap(temp);
   } else {
     std::vector<uint32_t> ao_cur(n);
     ao_gen<false>(fp, w, h, in.diff_hit_pos_normal, in.depth, v.ao_prev.data(), ao_cur.data(), 1u,
@@ -2026,17 +2232,29 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
   }
 
   (void)frame_rand.next();  // specular sample generation
-  std::vector<uint32_t> srsv(2 * n), srad(n), srsv2(2 * n), srad2(n);
-  std::vector<float> shp(4 * n), shp2(4 * n);
-  spec_temporal(fp, w, h, P, prev_depth, prev_gbuf, in.depth, in.gbuffer, v.spec_rsv_prev.data(),
-                v.spec_hp_prev.data(), v.spec_rad_prev.data(), in.spec_hit_pos, in.spec_hit_radiance, srsv.data(),
-                shp.data(), srad.data(), frame_rand.next(), has_prev ? 1u : 0u);
+  // f16 form: one 24-byte record per pixel in the `hp` buffers (6 words), no
+  // separate M/W and radiance planes.
+  const bool s16 = v.form == 2;
+  const size_t hpw = s16 ? 6 : 4;
+  std::vector<uint32_t> srsv(s16 ? 0 : 2 * n), srad(s16 ? 0 : n);
+  std::vector<float> shp(hpw * n);
+  {
+    const uint32_t seed = frame_rand.next();
+    if (s16)
+      spec_temporal<true>(fp, w, h, P, prev_depth, prev_gbuf, in.depth, in.gbuffer, nullptr, v.spec_hp_prev.data(),
+                          nullptr, in.spec_hit_pos, in.spec_hit_radiance, nullptr, shp.data(), nullptr, seed,
+                          has_prev ? 1u : 0u);
+    else
+      spec_temporal<false>(fp, w, h, P, prev_depth, prev_gbuf, in.depth, in.gbuffer, v.spec_rsv_prev.data(),
+                           v.spec_hp_prev.data(), v.spec_rad_prev.data(), in.spec_hit_pos, in.spec_hit_radiance,
+                           srsv.data(), shp.data(), srad.data(), seed, has_prev ? 1u : 0u);
+  }
   {
     const uint32_t* a_rsv = srsv.data();
     const float* a_hp = shp.data();
     const uint32_t* a_rad = srad.data();
-    std::vector<uint32_t> b_rsv(2 * n), b_rad(n), c_rsv(2 * n), c_rad(n);
-    std::vector<float> b_hp(4 * n), c_hp(4 * n);
+    std::vector<uint32_t> b_rsv(s16 ? 0 : 2 * n), b_rad(s16 ? 0 : n), c_rsv(s16 ? 0 : 2 * n), c_rad(s16 ? 0 : n);
+    std::vector<float> b_hp(hpw * n), c_hp(hpw * n);
     bool use_b = true;
     for (uint32_t k = 0; k < P.spec_spatial_passes; ++k) {
       bool last = k + 1 == P.spec_spatial_passes;
@@ -2044,14 +2262,18 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
       float* o_hp = use_b ? b_hp.data() : c_hp.data();
       uint32_t* o_rad = use_b ? b_rad.data() : c_rad.data();
       uint32_t seed = frame_rand.next();
-      if (v.f32)
-        spec_spatial<true>(fp, w, h, P, in.gbuffer, in.depth, a_rsv, a_hp, a_rad,
-                           last ? (void*)v.spec_light32.data() : nullptr, nullptr, last ? nullptr : o_rsv,
-                           last ? nullptr : o_hp, last ? nullptr : o_rad, seed);
+      if (v.form == 1)
+        spec_spatial<1>(fp, w, h, P, in.gbuffer, in.depth, a_rsv, a_hp, a_rad,
+                        last ? (void*)v.fspec_light.data() : nullptr, nullptr, last ? nullptr : o_rsv,
+                        last ? nullptr : o_hp, last ? nullptr : o_rad, seed);
+      else if (v.form == 2)
+        spec_spatial<2>(fp, w, h, P, in.gbuffer, in.depth, nullptr, a_hp, nullptr,
+                        last ? (void*)v.fspec_light.data() : nullptr, nullptr, nullptr, last ? nullptr : o_hp,
+                        nullptr, seed);
       else
-        spec_spatial<false>(fp, w, h, P, in.gbuffer, in.depth, a_rsv, a_hp, a_rad,
-                            last ? (void*)v.spec_light.data() : nullptr, last ? v.ray_len.data() : nullptr,
-                            last ? nullptr : o_rsv, last ? nullptr : o_hp, last ? nullptr : o_rad, seed);
+        spec_spatial<0>(fp, w, h, P, in.gbuffer, in.depth, a_rsv, a_hp, a_rad,
+                        last ? (void*)v.spec_light.data() : nullptr, last ? v.ray_len.data() : nullptr,
+                        last ? nullptr : o_rsv, last ? nullptr : o_hp, last ? nullptr : o_rad, seed);
       a_rsv = o_rsv;
       a_hp = o_hp;
       a_rad = o_rad;
@@ -2062,45 +2284,54 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
   v.spec_hp_prev.swap(shp);
   v.spec_rad_prev.swap(srad);
 
-  const size_t light_bytes = (v.f32 ? 16 : 4) * n;
-  const void* diff_light = v.f32 ? (const void*)v.diff_light32.data() : (const void*)v.diff_light.data();
-  const void* spec_light = v.f32 ? (const void*)v.spec_light32.data() : (const void*)v.spec_light.data();
-  if (P.denoise && has_prev && v.f32) {
-    std::vector<float> trec(8 * n), tlen(n), tfast(P.fast_history_clamp ? 8 * n : 8);
-    dn32_temporal(fp, w, h, P, in.depth, in.gbuffer, v.diff_light32.data(), v.spec_light32.data(), prev_depth,
-                  prev_gbuf, v.hist_rec.data(), v.hist_len32.data(), v.fast_prev32.data(), trec.data(), tlen.data(),
-                  tfast.data(), v.denoiser_history ? 1u : 0u, P.fast_history_clamp);
+  const bool ff = v.form != 0;
+  const size_t light_bytes = (v.form == 1 ? 16 : (v.form == 2 ? 8 : 4)) * n;
+  const void* diff_light = ff ? (const void*)v.fdiff_light.data() : (const void*)v.diff_light.data();
+  const void* spec_light = ff ? (const void*)v.fspec_light.data() : (const void*)v.spec_light.data();
+  if (P.denoise && has_prev && ff) {
+    const bool f32 = v.form == 1;
+    const size_t rb = f32 ? 32 : 16;  // bytes per record
+    std::vector<uint8_t> trec(rb * n), tlen(v.fhist_len.size()), tfast(P.fast_history_clamp ? rb * n : rb);
+    const uint32_t hh = v.denoiser_history ? 1u : 0u;
+    if (f32)
+      dn32_temporal<1>(fp, w, h, P, in.depth, in.gbuffer, v.fdiff_light.data(), v.fspec_light.data(), prev_depth,
+                       prev_gbuf, v.fhist_rec.data(), v.fhist_len.data(), v.ffast_prev.data(), trec.data(),
+                       tlen.data(), tfast.data(), hh, P.fast_history_clamp);
+    else
+      dn32_temporal<2>(fp, w, h, P, in.depth, in.gbuffer, v.fdiff_light.data(), v.fspec_light.data(), prev_depth,
+                       prev_gbuf, v.fhist_rec.data(), v.fhist_len.data(), v.ffast_prev.data(), trec.data(),
+                       tlen.data(), tfast.data(), hh, P.fast_history_clamp);
     if (P.disocclusion_fix) {
-      std::vector<float> frec(8 * n);
-      dn32_fix(w, h, in.depth, in.gbuffer, tlen.data(), trec.data(), frec.data());
+      std::vector<uint8_t> frec(rb * n);
+      if (f32) dn32_fix<1>(w, h, in.depth, in.gbuffer, tlen.data(), trec.data(), frec.data());
+      else dn32_fix<2>(w, h, in.depth, in.gbuffer, tlen.data(), trec.data(), frec.data());
       trec.swap(frec);
     }
     if (P.fast_history_clamp) {
-      dn32_fast_clamp(w, h, tfast.data(), trec.data());
-      v.fast_prev32.swap(tfast);
+      if (f32) dn32_fast_clamp<1>(w, h, tfast.data(), trec.data());
+      else dn32_fast_clamp<2>(w, h, tfast.data(), trec.data());
+      v.ffast_prev.swap(tfast);
     }
-    v.hist_rec.swap(trec);
-    v.hist_len32.swap(tlen);
+    v.fhist_rec.swap(trec);
+    v.fhist_len.swap(tlen);
     v.denoiser_history = true;
-    dn32_fallback(w, h, in.depth, in.gbuffer, v.hist_len32.data(), v.hist_rec.data(), v.fallback_rec.data());
-    std::vector<float> a(v.fallback_rec), b(8 * n);
+    if (f32) dn32_fallback<1>(w, h, in.depth, in.gbuffer, v.fhist_len.data(), v.fhist_rec.data(), v.ffallback.data());
+    else dn32_fallback<2>(w, h, in.depth, in.gbuffer, v.fhist_len.data(), v.fhist_rec.data(), v.ffallback.data());
+    std::vector<uint8_t> a(v.ffallback), b(rb * n);
     uint32_t iters = std::min(P.atrous_iterations, 5u);
     for (uint32_t k = 0; k < iters; ++k) {
       bool last = k + 1 == iters;
-      dn32_atrous(w, h, in.depth, in.gbuffer, a.data(), b.data(), last && out ? (float*)out->diffuse : nullptr,
-                  last && out ? (float*)out->specular : nullptr, 1 << k);
+      void* od = last && out ? out->diffuse : nullptr;
+      void* os = last && out ? out->specular : nullptr;
+      if (f32) dn32_atrous<1>(w, h, in.depth, in.gbuffer, a.data(), b.data(), od, os, 1 << k);
+      else dn32_atrous<2>(w, h, in.depth, in.gbuffer, a.data(), b.data(), od, os, 1 << k);
       a.swap(b);
     }
-    if (iters == 0 && out) {
+    if (iters == 0 && out) {  // the diffuse / specular halves of the fallback records
+      const size_t half = rb / 2;
       for (size_t i = 0; i < n; ++i) {
-        if (out->diffuse) {
-          float* q = (float*)out->diffuse + 4 * i;
-          q[0] = a[8 * i], q[1] = a[8 * i + 1], q[2] = a[8 * i + 2], q[3] = a[8 * i + 3];
-        }
-        if (out->specular) {
-          float* q = (float*)out->specular + 4 * i;
-          q[0] = a[8 * i + 4], q[1] = a[8 * i + 5], q[2] = a[8 * i + 6], q[3] = a[8 * i + 7];
-        }
+        if (out->diffuse) memcpy((uint8_t*)out->diffuse + half * i, a.data() + rb * i, half);
+        if (out->specular) memcpy((uint8_t*)out->specular + half * i, a.data() + rb * i + half, half);
       }
     }
   } else if (P.denoise && has_prev) {
@@ -2165,7 +2396,7 @@ int vlto_get_threads(void) { return nthreads(); }
 
 void* vlto_view_create_form(uint32_t w, uint32_t h, const vlt_params* p, int form) {
   OView* v = new OView;
-  v->f32 = form == 1;
+  v->form = form;
   v->w = (int)w;
   v->h = (int)h;
   v->P = *p;
@@ -2189,16 +2420,19 @@ void* vlto_view_create_form(uint32_t w, uint32_t h, const vlt_params* p, int for
   v->spec_light.assign(n, 0);
   v->ray_len.assign(n, 0);
   v->variance.assign(n, 0);
-  if (v->f32) {
-    v->diff_prev32.assign(12 * n, 0.0f);
-    v->ao_prev32.assign(2 * n, 0.0f);
-    v->ao_filtered32.assign(n, 0.0f);
-    v->diff_light32.assign(4 * n, 0.0f);
-    v->spec_light32.assign(4 * n, 0.0f);
-    v->hist_rec.assign(8 * n, 0.0f);
-    v->hist_len32.assign(n, 0.0f);
-    v->fast_prev32.assign(p->fast_history_clamp ? 8 * n : 8, 0.0f);
-    v->fallback_rec.assign(8 * n, 0.0f);
+  if (form == 1 || form == 2) {
+    const bool f32 = form == 1;
+    auto by = [&](size_t a, size_t c) { return (f32 ? a : c) * n; };
+    v->fdiff_prev.assign(by(48, 17), 0);
+    v->fao_prev.assign(by(8, 4), 0);
+    v->fao_filtered.assign(by(4, 2), 0);
+    v->fdiff_light.assign(by(16, 8), 0);
+    v->fspec_light.assign(by(16, 8), 0);
+    v->fhist_rec.assign(by(32, 16), 0);
+    v->fhist_len.assign(by(4, 2), 0);
+    v->ffast_prev.assign(p->fast_history_clamp ? by(32, 16) : (f32 ? 32 : 16), 0);
+    v->ffallback.assign(by(32, 16), 0);
+    if (form == 2) v->spec_hp_prev.assign(6 * n, 0.0f);
   }
   if (p->hg_enable) {
     size_t nc = (size_t)16 << v->log2_buckets;
@@ -2229,22 +2463,27 @@ void* vlto_view_buffer(void* h, const char* name, size_t* bytes) {
     void* p;
     size_t sz;
   };
-  if (v.f32) {
+  if (v.form != 0) {
+    const bool f32 = v.form == 1;
     E t32[] = {
-        {"diff_reservoir", v.diff_prev32.data(), 48 * n},
-        {"ao_history", v.ao_prev32.data(), 8 * n},
-        {"ao_filtered", v.ao_filtered32.data(), 4 * n},
-        {"hist_record", v.hist_rec.data(), 32 * n},
-        {"fallback_record", v.fallback_rec.data(), 32 * n},
-        {"hist_len", v.hist_len32.data(), 4 * n},
-        {"raw_diffuse", v.diff_light32.data(), 16 * n},
-        {"raw_specular", v.spec_light32.data(), 16 * n},
+        {"diff_reservoir", v.fdiff_prev.data(), v.fdiff_prev.size()},
+        {"ao_history", v.fao_prev.data(), v.fao_prev.size()},
+        {"ao_filtered", v.fao_filtered.data(), v.fao_filtered.size()},
+        {"hist_record", v.fhist_rec.data(), v.fhist_rec.size()},
+        {"fallback_record", v.ffallback.data(), v.ffallback.size()},
+        {"hist_len", v.fhist_len.data(), v.fhist_len.size()},
+        {"raw_diffuse", v.fdiff_light.data(), v.fdiff_light.size()},
+        {"raw_specular", v.fspec_light.data(), v.fspec_light.size()},
+        {"spec_record", f32 ? nullptr : v.spec_hp_prev.data(), f32 ? 0 : 24 * n},
     };
     for (const E& e : t32)
       if (strcmp(e.nm, name) == 0) {
+        if (!e.p) return nullptr;
         if (bytes) *bytes = e.sz;
         return e.p;
       }
+    if (!f32 && (!strcmp(name, "spec_hit_pos") || !strcmp(name, "spec_reservoir") || !strcmp(name, "spec_radiance")))
+      return nullptr;
     static const char* ref_only[] = {"diff_reservoir", "ao_history", "ao_filtered", "hist_color", "hist_moments",
                                      "hist_len", "variance", "spec_ray_len", "raw_diffuse", "raw_specular"};
     for (const char* r : ref_only)
@@ -2298,7 +2537,7 @@ void vlto_ind_diff_temporal_resample(const vlt_frame_params* fp, uint32_t w, uin
 void vlto_ind_diff_spatial_resample(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p,
                                     const uint32_t* gbuf, const float* depth, const uint16_t* ao, const uint32_t* in,
                                     uint32_t* out, uint32_t* lighting, uint32_t frame_rand) {
-  diff_spatial<false>(*fp, (int)w, (int)h, *p, gbuf, depth, ao, in, out, lighting, frame_rand);
+  diff_spatial<0>(*fp, (int)w, (int)h, *p, gbuf, depth, ao, in, out, lighting, frame_rand);
 }
 void vlto_ind_spec_temporal_resample(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p,
                                      const float* prev_depth, const uint32_t* prev_gbuf, const float* depth,
@@ -2306,14 +2545,14 @@ void vlto_ind_spec_temporal_resample(const vlt_frame_params* fp, uint32_t w, uin
                                      const uint32_t* prev_rad, const float* new_hp, const uint32_t* new_rad,
                                      uint32_t* out_rsv, float* out_hp, uint32_t* out_rad, uint32_t frame_rand,
                                      uint32_t has_prev) {
-  spec_temporal(*fp, (int)w, (int)h, *p, prev_depth, prev_gbuf, depth, gbuf, prev_rsv, prev_hp, prev_rad, new_hp,
+  spec_temporal<false>(*fp, (int)w, (int)h, *p, prev_depth, prev_gbuf, depth, gbuf, prev_rsv, prev_hp, prev_rad, new_hp,
                 new_rad, out_rsv, out_hp, out_rad, frame_rand, has_prev);
 }
 void vlto_ind_spec_spatial_resample(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p,
                                     const uint32_t* gbuf, const float* depth, const uint32_t* rsv, const float* hp,
                                     const uint32_t* rad, uint32_t* lighting, uint16_t* ray_len, uint32_t* out_rsv,
                                     float* out_hp, uint32_t* out_rad, uint32_t frame_rand) {
-  spec_spatial<false>(*fp, (int)w, (int)h, *p, gbuf, depth, rsv, hp, rad, lighting, ray_len, out_rsv, out_hp, out_rad,
+  spec_spatial<0>(*fp, (int)w, (int)h, *p, gbuf, depth, rsv, hp, rad, lighting, ray_len, out_rsv, out_hp, out_rad,
                frame_rand);
 }
 void vlto_denoise_temporal(const vlt_frame_params* fp, uint32_t w, uint32_t h, const vlt_params* p, const float* depth,

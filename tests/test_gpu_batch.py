@@ -15,8 +15,8 @@ from tests.helpers import d2h, upload
 
 pytestmark = pytest.mark.gpu
 
-BUFFERS = ["diff_reservoir", "spec_hit_pos", "spec_reservoir", "spec_radiance", "ao_history", "ao_filtered",
-           "raw_diffuse", "raw_specular", "hist_len", "hg_storage", "hg_decay", "hg_query_count"]
+BUFFERS = ["diff_reservoir", "spec_hit_pos", "spec_reservoir", "spec_radiance", "spec_record", "ao_history",
+           "ao_filtered", "raw_diffuse", "raw_specular", "hist_len", "hg_storage", "hg_decay", "hg_query_count"]
 REF_ONLY = ["hist_color", "hist_moments", "variance", "spec_ray_len"]
 F32_ONLY = ["hist_record", "fallback_record"]
 
@@ -36,18 +36,20 @@ def view_specs():
         (128, 72, "ref", small_plain1(), 4, 0),
         (64, 64, "f32", small_plain1(), 5, 2),  # joins at frame 2
         (1, 1, "ref", vg.params_reference(), 6, 1),
+        (48, 40, "f16", vg.params_plain(0), 7, 0),
+        (20, 12, "f16", vg.params_reference(), 8, 1),
     ]
 
 
 def out_bytes(form, n):
-    return (16 if form == "f32" else 4) * n
+    return {"ref": 4, "f32": 16, "f16": 8}[form] * n
 
 
 def state_of(view, form):
     import torch
 
     torch.cuda.synchronize()
-    names = BUFFERS + (F32_ONLY if form == "f32" else REF_ONLY)
+    names = BUFFERS + (REF_ONLY if form == "ref" else F32_ONLY)
     res = {}
     for name in names:
         try:

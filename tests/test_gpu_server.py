@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 
 def out_bytes(form, n):
-    return (16 if form == "f32" else 4) * n
+    return {"ref": 4, "f32": 16, "f16": 8}[form] * n
 
 
 def test_server_mix_equals_alone_and_respects_budget():
@@ -28,6 +28,7 @@ def test_server_mix_equals_alone_and_respects_budget():
         (1, 64, 64, "f32", vg.params_reference(), 13, 3),
         (2, 48, 32, "ref", vg.params_plain(0), 14, 4),
         (6, 72, 40, "f32", vg.params_reference(), 15, 2),
+        (7, 56, 40, "f16", vg.params_plain(0), 16, 3),
     ]
     bytes_each = [vg.View.device_bytes(w, h, form, p) for (_, w, h, form, p, _, _) in plan]
     # Room for the two largest sessions only: later arrivals wait for memory.

@@ -152,21 +152,31 @@ size_t layout(vlt_view* v, char* base) {
   ViewBuffers& b = v->b;
   memset(&b, 0, sizeof(b));
   const bool f32 = v->form == VLT_FORM_F32;
+  const bool f16 = v->form == VLT_FORM_F16;
   const bool fast = v->p.fast_history_clamp != 0;
-  for (int k = 0; k < 3; ++k) b.diff_rsv[k] = take((f32 ? 48 : 16) * n);
-  for (int k = 0; k < 2; ++k) b.ao[k] = take((f32 ? 8 : 4) * n);
-  b.ao_filtered = take((f32 ? 4 : 2) * n);
-  b.diff_light = take((f32 ? 16 : 4) * n);
+  // element sizes per form: reference / f32 / f16
+  auto by = [&](size_t r, size_t a, size_t c) { return f32 ? a : (f16 ? c : r); };
+  for (int k = 0; k < 3; ++k) b.diff_rsv[k] = take(by(16, 48, 17) * n);
+  for (int k = 0; k < 2; ++k) b.ao[k] = take(by(4, 8, 4) * n);
+  b.ao_filtered = take(by(2, 4, 2) * n);
+  b.diff_light = take(by(4, 16, 8) * n);
   for (int k = 0; k < 3; ++k) {
-    b.spec_hp[k] = (float*)take(16 * n);
-    b.spec_rsv[k] = (uint32_t*)take(8 * n);
-    b.spec_rad[k] = (uint32_t*)take(4 * n);
+    if (f16) {  // one 24-byte record per pixel
+      b.spec_hp[k] = (float*)take(24 * n);
+      b.spec_rsv[k] = nullptr;
+      b.spec_rad[k] = nullptr;
+    } else {
+      b.spec_hp[k] = (float*)take(16 * n);
+      b.spec_rsv[k] = (uint32_t*)take(8 * n);
+      b.spec_rad[k] = (uint32_t*)take(4 * n);
+    }
   }
-  b.spec_light = take((f32 ? 16 : 4) * n);
-  for (int k = 0; k < 2; ++k) b.len[k] = take((f32 ? 4 : 1) * n);
-  if (f32) {
-    for (int k = 0; k < 5; ++k) b.rec[k] = (float4*)take(32 * n);
-    for (int k = 0; k < 2; ++k) b.rec_fast[k] = (float4*)take(fast ? 32 * n : 32);
+  b.spec_light = take(by(4, 16, 8) * n);
+  for (int k = 0; k < 2; ++k) b.len[k] = take(by(1, 4, 2) * n);
+  if (f32 || f16) {
+    const size_t rb = f32 ? 32 : 16;
+    for (int k = 0; k < 5; ++k) b.rec[k] = (float4*)take(rb * n);
+    for (int k = 0; k < 2; ++k) b.rec_fast[k] = (float4*)take(fast ? rb * n : rb);
   } else {
     b.ray_len = (uint16_t*)take(2 * n);
     for (int k = 0; k < 3; ++k) {
@@ -382,8 +392,8 @@ vlt_status vlt_view_create(vlt_ctx* ctx, uint32_t width, uint32_t height, vlt_fo
                            vlt_view** out) {
   if (!ctx || !out || !params_ok(params) || width == 0 || height == 0 || width > 16384 || height > 16384)
     return VLT_ERR_INVALID_ARG;
-  if (form != VLT_FORM_REF && form != VLT_FORM_F32) {
-    set_last_error("storage form not built: use VLT_FORM_REF or VLT_FORM_F32");
+  if (form != VLT_FORM_REF && form != VLT_FORM_F32 && form != VLT_FORM_F16) {
+    set_last_error("unknown storage form");
     return VLT_ERR_INVALID_ARG;
   }
   *out = nullptr;
@@ -486,22 +496,26 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
   };
   size_t nc = v->p.hg_enable ? v->hg.num_cells() : 0;
   const bool f32 = v->form == VLT_FORM_F32;
+  const bool f16 = v->form == VLT_FORM_F16;
+  const bool ref = !f32 && !f16;
+  auto by = [&](size_t r, size_t a, size_t c) { return f32 ? a : (f16 ? c : r); };
   E tab[] = {
-      {"diff_reservoir", b.diff_rsv[v->diff_prev], (f32 ? 48 : 16) * n},
-      {"spec_hit_pos", b.spec_hp[v->spec_prev], 16 * n},
-      {"spec_reservoir", b.spec_rsv[v->spec_prev], 8 * n},
-      {"spec_radiance", b.spec_rad[v->spec_prev], 4 * n},
-      {"ao_history", b.ao[v->ao_prev], (f32 ? 8 : 4) * n},
-      {"ao_filtered", b.ao_filtered, (f32 ? 4 : 2) * n},
-      {"hist_color", f32 ? nullptr : b.color[0], 8 * n},
-      {"hist_moments", f32 ? nullptr : b.mom[0], 4 * n},
-      {"hist_record", f32 ? b.rec[0] : nullptr, 32 * n},
-      {"fallback_record", f32 ? b.rec[4] : nullptr, 32 * n},
-      {"hist_len", b.len[0], (f32 ? 4 : 1) * n},
-      {"variance", f32 ? nullptr : b.var[0], 4 * n},
-      {"spec_ray_len", f32 ? nullptr : b.ray_len, 2 * n},
-      {"raw_diffuse", b.diff_light, (f32 ? 16 : 4) * n},
-      {"raw_specular", b.spec_light, (f32 ? 16 : 4) * n},
+      {"diff_reservoir", b.diff_rsv[v->diff_prev], by(16, 48, 17) * n},
+      {"spec_hit_pos", f16 ? nullptr : b.spec_hp[v->spec_prev], 16 * n},
+      {"spec_reservoir", f16 ? nullptr : b.spec_rsv[v->spec_prev], 8 * n},
+      {"spec_radiance", f16 ? nullptr : b.spec_rad[v->spec_prev], 4 * n},
+      {"spec_record", f16 ? b.spec_hp[v->spec_prev] : nullptr, 24 * n},
+      {"ao_history", b.ao[v->ao_prev], by(4, 8, 4) * n},
+      {"ao_filtered", b.ao_filtered, by(2, 4, 2) * n},
+      {"hist_color", ref ? b.color[0] : nullptr, 8 * n},
+      {"hist_moments", ref ? b.mom[0] : nullptr, 4 * n},
+      {"hist_record", ref ? nullptr : b.rec[0], by(0, 32, 16) * n},
+      {"fallback_record", ref ? nullptr : b.rec[4], by(0, 32, 16) * n},
+      {"hist_len", b.len[0], by(1, 4, 2) * n},
+      {"variance", ref ? b.var[0] : nullptr, 4 * n},
+      {"spec_ray_len", ref ? b.ray_len : nullptr, 2 * n},
+      {"raw_diffuse", b.diff_light, by(4, 16, 8) * n},
+      {"raw_specular", b.spec_light, by(4, 16, 8) * n},
       {"hg_storage", b.hg_storage, nc * 16},
       {"hg_decay", b.hg_decay, nc},
       {"hg_queries", b.hg_queries[v->hg_qcur], v->p.hg_enable ? (size_t)v->hg.max_queries * 32 : 0},
@@ -600,7 +614,8 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   // AO.
   const int form = (int)v->form;
   const bool f32 = form == FORM_F32;
-  const size_t light_bytes = (f32 ? 16 : 4) * n;
+  const bool f16 = form == FORM_F16;
+  const size_t light_bytes = (f32 ? 16 : (f16 ? 8 : 4)) * n;
   int ao_cur = v->ao_prev ^ 1;
   STAGE("ao_gen", launch_ao_gen(ex, form, fp, w, h, ga, in->diff_hit_pos_normal, b.ao[v->ao_prev], b.ao[ao_cur], 1u,
                                 has_prev ? 1u : 0u, P.ao_radius));
@@ -631,7 +646,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   (void)fr.next();  // Ind. Spec. Sample Gen.
   int sp = v->spec_prev, st = (sp + 1) % 3, so = (sp + 2) % 3;
   uint32_t seed_st = fr.next();
-  STAGE("spec_temporal", launch_spec_temporal(ex, fp, w, h, P.spec_m_cap, ga, pga, prev_depth, b.spec_rsv[sp],
+  STAGE("spec_temporal", launch_spec_temporal(ex, form, fp, w, h, P.spec_m_cap, ga, pga, prev_depth, b.spec_rsv[sp],
                                               b.spec_hp[sp], b.spec_rad[sp], in->spec_hit_pos, in->spec_hit_radiance,
                                               b.spec_rsv[st], b.spec_hp[st], b.spec_rad[st], seed_st,
                                               has_prev ? 1u : 0u));
@@ -656,23 +671,22 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
 
   // Denoiser.
   const bool run_denoiser = P.denoise && has_prev;
-  if (run_denoiser && f32) {
+  if (run_denoiser && (f32 || f16)) {
     DenoiseKnobs kn = {1.0f / P.history_max_frames, P.fast_history_clamp};
     uint32_t has_history = v->denoise_history ? 1u : 0u;
     // rec[0]/len[0] = history; rec[2]/len[1] = temporal output; rec[1] = fix output.
-    STAGE("dn_temporal", launch_dn32_temporal(ex, fp, w, h, kn, ga, pga, (const float4*)b.diff_light,
-                                              (const float4*)b.spec_light, prev_depth, b.rec[0],
-                                              (const float*)b.len[0], b.rec_fast[0], b.rec[2], (float*)b.len[1],
+    STAGE("dn_temporal", launch_dn32_temporal(ex, form, fp, w, h, kn, ga, pga, b.diff_light, b.spec_light,
+                                              prev_depth, b.rec[0], b.len[0], b.rec_fast[0], b.rec[2], b.len[1],
                                               b.rec_fast[1], has_history));
     ++launches;
     float4* cur = b.rec[2];
     if (P.disocclusion_fix) {
-      STAGE("dn_fix", launch_dn32_fix(ex, w, h, ga, (const float*)b.len[1], b.rec[2], b.rec[1]));
+      STAGE("dn_fix", launch_dn32_fix(ex, form, w, h, ga, b.len[1], b.rec[2], b.rec[1]));
       ++launches;
       cur = b.rec[1];
     }
     if (P.fast_history_clamp) {
-      STAGE("dn_fast_clamp", launch_dn32_fast_clamp(ex, w, h, b.rec_fast[1], cur));
+      STAGE("dn_fast_clamp", launch_dn32_fast_clamp(ex, form, w, h, b.rec_fast[1], cur));
       ++launches;
       std::swap(b.rec_fast[0], b.rec_fast[1]);
       v->fast_history_valid = true;
@@ -686,26 +700,27 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
       std::swap(b.rec[0], b.rec[2]);
     std::swap(b.len[0], b.len[1]);
     v->denoise_history = true;
-    STAGE("dn_fallback", launch_dn32_fallback(ex, w, h, ga, (const float*)b.len[0], b.rec[0], b.rec[4]));
+    STAGE("dn_fallback", launch_dn32_fallback(ex, form, w, h, ga, b.len[0], b.rec[0], b.rec[4]));
     ++launches;
     float4* rsrc = b.rec[4];
     float4* rdst = b.rec[2];
     const uint32_t iters = P.atrous_iterations;
     for (uint32_t k = 0; k < iters; ++k) {
       bool last = k + 1 == iters;
-      float4* od = last && out ? (float4*)out->diffuse : nullptr;
-      float4* os = last && out ? (float4*)out->specular : nullptr;
-      STAGE("dn_atrous", launch_dn32_atrous(ex, w, h, ga, rsrc, rdst, od, os, 1 << k));
+      void* od = last && out ? out->diffuse : nullptr;
+      void* os = last && out ? out->specular : nullptr;
+      STAGE("dn_atrous", launch_dn32_atrous(ex, form, w, h, ga, rsrc, rdst, od, os, 1 << k));
       ++launches;
       rsrc = rdst;
       rdst = rdst == b.rec[2] ? b.rec[3] : b.rec[2];
     }
     if (iters == 0 && out && (out->diffuse || out->specular)) {
       // Zero iterations: the fallback output is the result (copy its colours out).
-      if (out->diffuse)
-        ex_copy_rows16(ex, out->diffuse, 16, b.rec[4], 32, n);
+      // The diffuse / specular half of each fallback record {rgb, aux}.
+      const size_t half_rec = f32 ? 16 : 8;
+      if (out->diffuse) ex_copy_rows(ex, out->diffuse, half_rec, b.rec[4], 2 * half_rec, half_rec, n);
       if (out->specular)
-        ex_copy_rows16(ex, out->specular, 16, (char*)b.rec[4] + 16, 32, n);
+        ex_copy_rows(ex, out->specular, half_rec, (char*)b.rec[4] + half_rec, 2 * half_rec, half_rec, n);
     }
   } else if (run_denoiser) {
     DenoiseKnobs kn = {1.0f / P.history_max_frames, P.fast_history_clamp};
@@ -865,7 +880,7 @@ vlt_status vlt_ind_spec_temporal_resample(const vlt_frame_params* fp, uint32_t w
     return VLT_ERR_INVALID_ARG;
   GeoArgs ga = {gbuffer_depth, gbuffer_color, fp->inv_view_proj, nullptr, nullptr, nullptr};
   GeoArgs pga = {prev_gbuffer_depth, prev_gbuffer_color, fp->prev_inv_view_proj, nullptr, nullptr, nullptr};
-  launch_spec_temporal(stream_exec(stream), *fp, width, height, params->spec_m_cap, ga, pga, prev_gbuffer_depth, prev_reservoir,
+  launch_spec_temporal(stream_exec(stream), FORM_REF, *fp, width, height, params->spec_m_cap, ga, pga, prev_gbuffer_depth, prev_reservoir,
                        prev_hit_pos, prev_hit_radiance, new_hit_pos, new_hit_radiance, rw_reservoir, rw_hit_pos,
                        rw_hit_radiance, frame_rand, has_prev_frame);
   return cuda_status(cudaGetLastError());

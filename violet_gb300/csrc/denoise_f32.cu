@@ -68,6 +68,63 @@ __device__ __forceinline__ void store_rec(float4* __restrict__ p, size_t i, f3 d
   p[2 * i + 1] = make_float4(s.x, s.y, s.z, aux.y);
 }
 
+// f16 form: one uint4 per pixel = 8 halves {d.rgb, aux.x, s.rgb, aux.y}; stores
+// saturate (f32tof16_sat).
+__device__ __forceinline__ Rec load_rec(const uint4* __restrict__ p, size_t i) {
+  uint4 v = p[i];
+  Rec r;
+  r.d = mk3(f16tof32(v.x & 0xFFFFu), f16tof32(v.x >> 16), f16tof32(v.y & 0xFFFFu));
+  r.s = mk3(f16tof32(v.z & 0xFFFFu), f16tof32(v.z >> 16), f16tof32(v.w & 0xFFFFu));
+  r.aux = mk2(f16tof32(v.y >> 16), f16tof32(v.w >> 16));
+  return r;
+}
+__device__ __forceinline__ void store_rec(uint4* __restrict__ p, size_t i, f3 d, f3 s, f2 aux) {
+  p[i] = make_uint4(f32tof16_sat(d.x) | (f32tof16_sat(d.y) << 16), f32tof16_sat(d.z) | (f32tof16_sat(aux.x) << 16),
+                    f32tof16_sat(s.x) | (f32tof16_sat(s.y) << 16), f32tof16_sat(s.z) | (f32tof16_sat(aux.y) << 16));
+}
+__device__ __forceinline__ void copy_rec(float4* __restrict__ out, const float4* __restrict__ in, size_t i) {
+  out[2 * i] = in[2 * i];
+  out[2 * i + 1] = in[2 * i + 1];
+}
+__device__ __forceinline__ void copy_rec(uint4* __restrict__ out, const uint4* __restrict__ in, size_t i) {
+  out[i] = in[i];
+}
+// History length: float (f32 form) or f16 (f16 form).
+__device__ __forceinline__ float ld_len(const float* __restrict__ p, size_t i) { return p[i]; }
+__device__ __forceinline__ float ld_len(const uint16_t* __restrict__ p, size_t i) { return f16tof32(p[i]); }
+__device__ __forceinline__ void st_len(float* __restrict__ p, size_t i, float v) { p[i] = v; }
+__device__ __forceinline__ void st_len(uint16_t* __restrict__ p, size_t i, float v) {
+  p[i] = (uint16_t)f32tof16_sat(v);
+}
+// Lighting inputs {rgb, w} and outputs {rgb, 0}: float4 or half4.
+__device__ __forceinline__ float4 ld_light(const float4* __restrict__ p, size_t i) { return p[i]; }
+__device__ __forceinline__ float4 ld_light(const uint2* __restrict__ p, size_t i) {
+  uint2 v = p[i];
+  return make_float4(f16tof32(v.x & 0xFFFFu), f16tof32(v.x >> 16), f16tof32(v.y & 0xFFFFu), f16tof32(v.y >> 16));
+}
+__device__ __forceinline__ void st_out(float4* __restrict__ p, size_t i, f3 v) {
+  p[i] = make_float4(v.x, v.y, v.z, 0.0f);
+}
+__device__ __forceinline__ void st_out(uint2* __restrict__ p, size_t i, f3 v) {
+  p[i] = make_uint2(f32tof16_sat(v.x) | (f32tof16_sat(v.y) << 16), f32tof16_sat(v.z));
+}
+
+// Element types per form: record unit R, history length N, lighting L.
+template <int FORM>
+struct DnT;
+template <>
+struct DnT<FORM_F32> {
+  using R = float4;
+  using N = float;
+  using L = float4;
+};
+template <>
+struct DnT<FORM_F16> {
+  using R = uint4;
+  using N = uint16_t;
+  using L = uint2;
+};
+
 // EdgeStoppingFunc (svgf.inc.hlsl:6-84).
 struct EdgeStopFast {
   float depth_center, fz_sigma;  // sigma_z * fwidth_z
@@ -123,13 +180,14 @@ __device__ __forceinline__ f3 fma3(float w, f3 v, f3 acc) {
   return mk3(fma_(w, v.x, acc.x), fma_(w, v.y, acc.y), fma_(w, v.z, acc.z));
 }
 
-__device__ __forceinline__ float quad_max_len(const float* __restrict__ len, int x, int y, int w, int h) {
+template <class N>
+__device__ __forceinline__ float quad_max_len(const N* __restrict__ len, int x, int y, int w, int h) {
   int x0 = x & ~1, y0 = y & ~1;
   float m = 0.0f;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     int px = x0 + (k & 1), py = y0 + (k >> 1);
-    float v = inb(px, py, w, h) ? len[(size_t)py * w + px] : 0.0f;
+    float v = inb(px, py, w, h) ? ld_len(len, (size_t)py * w + px) : 0.0f;
     m = fmax_(m, v);
   }
   return m;
@@ -139,15 +197,18 @@ __device__ __forceinline__ float quad_max_len(const float* __restrict__ len, int
 
 // --------------------------------------------------------------- temporal
 
-template <class Geo>
+template <class Geo, int FORM>
 struct Dn32TemporalF {
-  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DenoiseKnobs kn, Geo geo, Geo prev_geo, const uint32_t* __restrict__ gbuf, const float4* __restrict__ diff_src, const float4* __restrict__ spec_src, const float* __restrict__ prev_depth, const float4* __restrict__ hist, const float* __restrict__ len_hist, const float4* __restrict__ fast_hist, float4* __restrict__ out, float* __restrict__ out_len, float4* __restrict__ out_fast, uint32_t has_history) {
+  using R = typename DnT<FORM>::R;
+  using N = typename DnT<FORM>::N;
+  using L = typename DnT<FORM>::L;
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DenoiseKnobs kn, Geo geo, Geo prev_geo, const uint32_t* __restrict__ gbuf, const L* __restrict__ diff_src, const L* __restrict__ spec_src, const float* __restrict__ prev_depth, const R* __restrict__ hist, const N* __restrict__ len_hist, const R* __restrict__ fast_hist, R* __restrict__ out, N* __restrict__ out_len, R* __restrict__ out_fast, uint32_t has_history) {
   int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
   float depth = geo.dep(i);
   if (depth == 0.0f) {
-    out_len[i] = 0.0f;
+    st_len(out_len, i, 0.0f);
     store_rec(out, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
     if (kn.fast_history) store_rec(out_fast, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
     return;
@@ -167,7 +228,7 @@ struct Dn32TemporalF {
       int px = x + dx, py = y + dy;
       px = px < 0 ? 0 : (px > w - 1 ? w - 1 : px);
       py = py < 0 ? 0 : (py > h - 1 ? h - 1 : py);
-      float4 sv = spec_src[(size_t)py * w + px];
+      float4 sv = ld_light(spec_src, (size_t)py * w + px);
       f3 s = mk3(sv.x, sv.y, sv.z);
       m1 = m1 + s;
       m2 = m2 + s * s;
@@ -177,7 +238,7 @@ struct Dn32TemporalF {
   m2 = m2 * (1.0f / 9.0f);
 
   const f3 position = geo.pos(x, y, i);
-  const float4 s_center = spec_src[i];
+  const float4 s_center = ld_light(spec_src, i);
   f3 vsh = mk3(0.0f), vsfh = mk3(0.0f);
   {
     f3 vdir = normalize3(position - vpos3(fp.view_pos));
@@ -236,7 +297,7 @@ struct Dn32TemporalF {
         if (!ok) continue;
         float wt = wts[oy][ox];
         wsum = wsum + wt;
-        hs = hs + wt * len_hist[j];
+        hs = hs + wt * ld_len(len_hist, j);
         Rec r = load_rec(hist, j);
         ds = fma3(wt, r.d, ds);
         ss = fma3(wt, r.s, ss);
@@ -266,7 +327,7 @@ struct Dn32TemporalF {
   }
   hl = hl + VLT_HISTORY_LEN_UNIT;
 
-  float4 dv = diff_src[i];
+  float4 dv = ld_light(diff_src, i);
   f3 dsrc = mk3(dv.x, dv.y, dv.z);
   f3 ssrc = mk3(s_center.x, s_center.y, s_center.z);
   f2 lsrc = mk2(lum_fast(dsrc.x, dsrc.y, dsrc.z), lum_fast(ssrc.x, ssrc.y, ssrc.z));
@@ -300,20 +361,22 @@ struct Dn32TemporalF {
     }
   }
   store_rec(out, i, df, sf, smf);
-  out_len[i] = hl;
+  st_len(out_len, i, hl);
   if (kn.fast_history) store_rec(out_fast, i, dff, sff, mk2(0.0f, 0.0f));
 }
 };
 
 // ----------------------------------------------------------- disocclusion fix
 
-template <class Geo>
+template <class Geo, int FORM>
 struct Dn32FixF {
-  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, const float* __restrict__ len, const float4* __restrict__ in, float4* __restrict__ out) {
+  using R = typename DnT<FORM>::R;
+  using N = typename DnT<FORM>::N;
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, const N* __restrict__ len, const R* __restrict__ in, R* __restrict__ out) {
   int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
-  float hl = len[i];
+  float hl = ld_len(len, i);
   float qmax = quad_max_len(len, x, y, w, h);
   if (hl == 0.0f) {
     store_rec(out, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
@@ -342,8 +405,7 @@ struct Dn32FixF {
     }
     store_rec(out, i, dsum * (1.0f / ws.x), ssum * (1.0f / ws.y), mk2(msum.x / ws.x, msum.y / ws.y));
   } else {
-    out[2 * i] = in[2 * i];
-    out[2 * i + 1] = in[2 * i + 1];
+    copy_rec(out, in, i);
   }
 }
 };
@@ -358,8 +420,10 @@ __device__ __forceinline__ f3 ycocg_inv(f3 c) {
   return mk3(tmp + c.y, c.x + c.z, tmp - c.y);
 }
 
+template <int FORM>
 struct Dn32FastClampF {
-  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, const float4* __restrict__ fast, float4* __restrict__ rec) {
+  using R = typename DnT<FORM>::R;
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, const R* __restrict__ fast, R* __restrict__ rec) {
   int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
@@ -392,13 +456,15 @@ struct Dn32FastClampF {
 
 // ---------------------------------------------------------- spatial fallback
 
-template <class Geo>
+template <class Geo, int FORM>
 struct Dn32FallbackF {
-  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, const float* __restrict__ len, const float4* __restrict__ in, float4* __restrict__ out) {
+  using R = typename DnT<FORM>::R;
+  using N = typename DnT<FORM>::N;
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, const N* __restrict__ len, const R* __restrict__ in, R* __restrict__ out) {
   int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
-  float hl = len[i];
+  float hl = ld_len(len, i);
   float qmax = quad_max_len(len, x, y, w, h);
   if (hl == 0.0f) {
     store_rec(out, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
@@ -453,10 +519,10 @@ struct AtrousDist {
 // svgf_atrous_filter.hlsl:23-88: 5x5 taps at `step`, kernel weights {1, 2/3, 1/6},
 // off-axis taps only (the reference's loop condition), variance filtered with w^2.
 // CHECK = false is the path of blocks whose whole 5x5 footprint is inside the image.
-template <bool CHECK, class Geo>
+template <bool CHECK, class Geo, class R, class L>
 __device__ __forceinline__ void atrous_px(int x, int y, int w, int h, const Geo& geo, AtrousDist td,
-                                          const float4* __restrict__ in, float4* __restrict__ out,
-                                          float4* __restrict__ out_diff, float4* __restrict__ out_spec, int step) {
+                                          const R* __restrict__ in, R* __restrict__ out, L* __restrict__ out_diff,
+                                          L* __restrict__ out_spec, int step) {
   size_t i = (size_t)y * w + x;
   Rec c = load_rec(in, i);
   EdgeStopFast es = make_es(geo.dep(i), geo.fwz(i), 1.0f, geo.normal(i), 7);
@@ -498,13 +564,15 @@ __device__ __forceinline__ void atrous_px(int x, int y, int w, int h, const Geo&
   f3 dd = dsum * inv.x, sd = ssum * inv.y;
   f2 vd = mk2(vsum.x * inv.x * inv.x, vsum.y * inv.y * inv.y);
   if (out) store_rec(out, i, dd, sd, vd);
-  if (out_diff) out_diff[i] = make_float4(dd.x, dd.y, dd.z, 0.0f);
-  if (out_spec) out_spec[i] = make_float4(sd.x, sd.y, sd.z, 0.0f);
+  if (out_diff) st_out(out_diff, i, dd);
+  if (out_spec) st_out(out_spec, i, sd);
 }
 
-template <class Geo>
+template <class Geo, int FORM>
 struct Dn32AtrousF {
-  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, AtrousDist td, const float4* __restrict__ in, float4* __restrict__ out, float4* __restrict__ out_diff, float4* __restrict__ out_spec, int step) {
+  using R = typename DnT<FORM>::R;
+  using L = typename DnT<FORM>::L;
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, AtrousDist td, const R* __restrict__ in, R* __restrict__ out, L* __restrict__ out_diff, L* __restrict__ out_spec, int step) {
   const int m = 2 * step;
   const bool interior = x0 - m >= 0 && y0 - m >= 0 && x0 + (int)blockDim.x - 1 + m <= w - 1 &&
                         y0 + (int)blockDim.y - 1 + m <= h - 1;
@@ -533,46 +601,75 @@ struct Dn32AtrousF {
     }                                                            \
   } while (0)
 
-void launch_dn32_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn,
-                          const GeoArgs& ga, const GeoArgs& prev_ga, const float4* diff_src, const float4* spec_src,
-                          const float* prev_depth, const float4* hist, const float* len_hist, const float4* fast_hist,
-                          float4* out, float* out_len, float4* out_fast, uint32_t has_history) {
+// Runs the statement with T = DnT<FORM> element types for the form.
+#define VLT_FORM_DISPATCH(form, ...)            \
+  do {                                          \
+    if ((form) == FORM_F16) {                   \
+      constexpr int F = FORM_F16;               \
+      using T = DnT<FORM_F16>;                  \
+      __VA_ARGS__;                              \
+    } else {                                    \
+      constexpr int F = FORM_F32;               \
+      using T = DnT<FORM_F32>;                  \
+      __VA_ARGS__;                              \
+    }                                           \
+  } while (0)
+
+void launch_dn32_temporal(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn,
+                          const GeoArgs& ga, const GeoArgs& prev_ga, const void* diff_src, const void* spec_src,
+                          const float* prev_depth, const void* hist, const void* len_hist, const void* fast_hist,
+                          void* out, void* out_len, void* out_fast, uint32_t has_history) {
   if (ga.nd) {
     GeoSurface geo = {ga.nd, ga.pr, ga.fz, w, h};
     GeoSurface pgeo = {prev_ga.nd, prev_ga.pr, prev_ga.fz, w, h};
-    launch2d<Dn32TemporalF<GeoSurface>>(ex, "dn_temporal", w, h, fp, w, h, kn, geo, pgeo, ga.gbuf, diff_src,
-                                        spec_src, prev_depth, hist, len_hist, fast_hist, out, out_len, out_fast,
-                                        has_history);
+    VLT_FORM_DISPATCH(form, (launch2d<Dn32TemporalF<GeoSurface, F>>(
+                                ex, "dn_temporal", w, h, fp, w, h, kn, geo, pgeo, ga.gbuf,
+                                (const typename T::L*)diff_src, (const typename T::L*)spec_src, prev_depth,
+                                (const typename T::R*)hist, (const typename T::N*)len_hist,
+                                (const typename T::R*)fast_hist, (typename T::R*)out, (typename T::N*)out_len,
+                                (typename T::R*)out_fast, has_history)));
   } else {
     GeoRaw geo = make_geo_raw(ga.depth, ga.gbuf, ga.inv_vp, w, h);
     GeoRaw pgeo = make_geo_raw(prev_ga.depth, prev_ga.gbuf, prev_ga.inv_vp, w, h);
-    launch2d<Dn32TemporalF<GeoRaw>>(ex, "dn_temporal", w, h, fp, w, h, kn, geo, pgeo, ga.gbuf, diff_src, spec_src,
-                                    prev_depth, hist, len_hist, fast_hist, out, out_len, out_fast, has_history);
+    VLT_FORM_DISPATCH(form, (launch2d<Dn32TemporalF<GeoRaw, F>>(
+                                ex, "dn_temporal", w, h, fp, w, h, kn, geo, pgeo, ga.gbuf,
+                                (const typename T::L*)diff_src, (const typename T::L*)spec_src, prev_depth,
+                                (const typename T::R*)hist, (const typename T::N*)len_hist,
+                                (const typename T::R*)fast_hist, (typename T::R*)out, (typename T::N*)out_len,
+                                (typename T::R*)out_fast, has_history)));
   }
 }
 
-void launch_dn32_fix(const Exec& ex, int w, int h, const GeoArgs& ga, const float* len, const float4* in,
-                     float4* out) {
-  VLT_GEO_DISPATCH(ga, launch2d<Dn32FixF<Geo>>(ex, "dn_fix", w, h, w, h, geo, len, in, out));
+void launch_dn32_fix(const Exec& ex, int form, int w, int h, const GeoArgs& ga, const void* len, const void* in,
+                     void* out) {
+  VLT_FORM_DISPATCH(form, VLT_GEO_DISPATCH(ga, (launch2d<Dn32FixF<Geo, F>>(
+                                                   ex, "dn_fix", w, h, w, h, geo, (const typename T::N*)len,
+                                                   (const typename T::R*)in, (typename T::R*)out))));
 }
 
-void launch_dn32_fast_clamp(const Exec& ex, int w, int h, const float4* fast, float4* rec) {
-  launch2d<Dn32FastClampF>(ex, "dn_fast_clamp", w, h, w, h, fast, rec);
+void launch_dn32_fast_clamp(const Exec& ex, int form, int w, int h, const void* fast, void* rec) {
+  VLT_FORM_DISPATCH(form, (launch2d<Dn32FastClampF<F>>(ex, "dn_fast_clamp", w, h, w, h, (const typename T::R*)fast,
+                                                       (typename T::R*)rec)));
 }
 
-void launch_dn32_fallback(const Exec& ex, int w, int h, const GeoArgs& ga, const float* len, const float4* in,
-                          float4* out) {
-  VLT_GEO_DISPATCH(ga, launch2d<Dn32FallbackF<Geo>>(ex, "dn_fallback", w, h, w, h, geo, len, in, out));
+void launch_dn32_fallback(const Exec& ex, int form, int w, int h, const GeoArgs& ga, const void* len, const void* in,
+                          void* out) {
+  VLT_FORM_DISPATCH(form, VLT_GEO_DISPATCH(ga, (launch2d<Dn32FallbackF<Geo, F>>(
+                                                   ex, "dn_fallback", w, h, w, h, geo, (const typename T::N*)len,
+                                                   (const typename T::R*)in, (typename T::R*)out))));
 }
 
-void launch_dn32_atrous(const Exec& ex, int w, int h, const GeoArgs& ga, const float4* in, float4* out,
-                        float4* out_diff, float4* out_spec, int step) {
+void launch_dn32_atrous(const Exec& ex, int form, int w, int h, const GeoArgs& ga, const void* in, void* out,
+                        void* out_diff, void* out_spec, int step) {
   const float s1 = (float)step, s2 = (float)(2 * step);
   AtrousDist td = {sqrtf(s1 * s1 + s1 * s1), sqrtf(s1 * s1 + s2 * s2), sqrtf(s2 * s2 + s2 * s2)};
-  VLT_GEO_DISPATCH(ga, launch2d<Dn32AtrousF<Geo>>(ex, "dn_atrous", w, h, w, h, geo, td, in, out, out_diff, out_spec,
-                                                  step));
+  VLT_FORM_DISPATCH(form, VLT_GEO_DISPATCH(ga, (launch2d<Dn32AtrousF<Geo, F>>(
+                                                   ex, "dn_atrous", w, h, w, h, geo, td, (const typename T::R*)in,
+                                                   (typename T::R*)out, (typename T::L*)out_diff,
+                                                   (typename T::L*)out_spec, step))));
 }
 
+#undef VLT_FORM_DISPATCH
 #undef VLT_GEO_DISPATCH
 
 }  // namespace vlt

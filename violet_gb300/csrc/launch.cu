@@ -26,10 +26,11 @@ struct CopyF {
   }
 };
 
-// rows x (one uint4) with pitches in uint4 units.
+// rows x (one T) with pitches in units of T.
+template <class T>
 struct Copy2DF {
-  static __device__ __forceinline__ void run(int x0, int, uint4* __restrict__ dst, uint32_t dpitch,
-                                             const uint4* __restrict__ src, uint32_t spitch, uint32_t rows) {
+  static __device__ __forceinline__ void run(int x0, int, T* __restrict__ dst, uint32_t dpitch,
+                                             const T* __restrict__ src, uint32_t spitch, uint32_t rows) {
     uint32_t r = (uint32_t)x0 + threadIdx.x;
     if (r < rows) dst[(size_t)r * dpitch] = src[(size_t)r * spitch];
   }
@@ -65,14 +66,19 @@ void ex_copy(const Exec& ex, void* dst, const void* src, size_t bytes) {
   }
 }
 
-void ex_copy_rows16(const Exec& ex, void* dst, size_t dpitch, const void* src, size_t spitch, size_t rows) {
+void ex_copy_rows(const Exec& ex, void* dst, size_t dpitch, const void* src, size_t spitch, size_t width,
+                  size_t rows) {
   if (!rows) return;
   if (!ex.rec) {
-    cudaMemcpy2DAsync(dst, dpitch, src, spitch, 16, rows, cudaMemcpyDeviceToDevice, ex.stream);
+    cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, cudaMemcpyDeviceToDevice, ex.stream);
     return;
   }
-  launch1d<Copy2DF>(ex, "copy", (uint32_t)rows, (uint4*)dst, (uint32_t)(dpitch / 16), (const uint4*)src,
-                    (uint32_t)(spitch / 16), (uint32_t)rows);
+  if (width == 16)
+    launch1d<Copy2DF<uint4>>(ex, "copy", (uint32_t)rows, (uint4*)dst, (uint32_t)(dpitch / 16), (const uint4*)src,
+                             (uint32_t)(spitch / 16), (uint32_t)rows);
+  else
+    launch1d<Copy2DF<uint2>>(ex, "copy", (uint32_t)rows, (uint2*)dst, (uint32_t)(dpitch / 8), (const uint2*)src,
+                             (uint32_t)(spitch / 8), (uint32_t)rows);
 }
 
 int device_sm_count() {

@@ -56,6 +56,9 @@ struct AoStore<FORM_F32> {
   static __device__ __forceinline__ float hist_x(const Hist* p, size_t i) { return p[i].x; }
   static __device__ __forceinline__ Filt pack_filt(float v) { return v; }
 };
+// f16 form: the reference's half2 / half (AO values lie in [0, 1]).
+template <>
+struct AoStore<FORM_F16> : AoStore<FORM_REF> {};
 
 // raytraced_ao_gen.hlsl:18-81.
 template <class Geo, int FORM>
@@ -162,6 +165,8 @@ struct DiffStore;
 template <>
 struct DiffStore<FORM_REF> {
   using Rec = uint4;
+  using CPtr = const uint4*;
+  using Ptr = uint4*;
   using Light = uint32_t;
   static __device__ __forceinline__ Light light(f3 l) { return pack_r11g11b10(l); }
   static __device__ __forceinline__ Light zero_light() { return 0u; }
@@ -169,10 +174,68 @@ struct DiffStore<FORM_REF> {
 template <>
 struct DiffStore<FORM_F32> {
   using Rec = DiffF32;
+  using CPtr = const DiffF32*;
+  using Ptr = DiffF32*;
   using Light = float4;
   static __device__ __forceinline__ Light light(f3 l) { return make_float4(l.x, l.y, l.z, 0.0f); }
   static __device__ __forceinline__ Light zero_light() { return make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
 };
+
+// f16-form diffuse reservoir: 16 bytes {HitPosNormal (hit position f16 x3, octahedral
+// 16-bit normal), radiance f16 x3, W f16} plus M in a separate byte plane (M <= 255).
+// Stores saturate (f32tof16_sat).
+struct DiffF16Ptr {
+  uint4* __restrict__ main;
+  uint8_t* __restrict__ m;
+};
+struct DiffF16CPtr {
+  const uint4* __restrict__ main;
+  const uint8_t* __restrict__ m;
+};
+
+__device__ __forceinline__ void diff_f16_store(DiffF16Ptr p, size_t i, uint32_t M, float W, f3 pos, f3 nrm, f3 rad) {
+  uint32_t e[2];
+  hpn_encode(mk3(q16(pos.x), q16(pos.y), q16(pos.z)), nrm, e);
+  p.main[i] = make_uint4(e[0], e[1], f32tof16_sat(rad.x) | (f32tof16_sat(rad.y) << 16),
+                         f32tof16_sat(rad.z) | (f32tof16_sat(W) << 16));
+  p.m[i] = (uint8_t)(M < 255u ? M : 255u);
+}
+// Record at (x, y); out of range reads the empty record.
+__device__ __forceinline__ void diff_f16_load(DiffF16CPtr p, size_t i, uint32_t* M, float* W, f3* pos, f3* nrm,
+                                              f3* rad) {
+  uint4 r = p.main[i];
+  *M = p.m[i];
+  *pos = hpn_pos(r.x, r.y);
+  *nrm = hpn_normal(r.y);
+  *rad = mk3(f16tof32(r.z & 0xFFFFu), f16tof32(r.z >> 16), f16tof32(r.w & 0xFFFFu));
+  *W = f16tof32(r.w >> 16);
+}
+
+template <>
+struct DiffStore<FORM_F16> {
+  using CPtr = DiffF16CPtr;
+  using Ptr = DiffF16Ptr;
+  using Light = uint2;  // half4 {rgb, 0}
+  static __device__ __forceinline__ Light light(f3 l) {
+    return make_uint2(f32tof16_sat(l.x) | (f32tof16_sat(l.y) << 16), f32tof16_sat(l.z));
+  }
+  static __device__ __forceinline__ Light zero_light() { return make_uint2(0u, 0u); }
+};
+
+// Loads / stores of the decoded diffuse reservoir (f32 and f16 forms).
+__device__ __forceinline__ void diff_load(const DiffF32* p, size_t i, uint32_t* M, float* W, f3* pos, f3* nrm,
+                                          f3* rad) {
+  DiffF32 r = p[i];
+  *M = as_uint(r.b.w);
+  *W = r.a.w;
+  *pos = mk3(r.a.x, r.a.y, r.a.z);
+  *nrm = mk3(r.b.x, r.b.y, r.b.z);
+  *rad = mk3(r.c.x, r.c.y, r.c.z);
+}
+__device__ __forceinline__ void diff_load(DiffF16CPtr p, size_t i, uint32_t* M, float* W, f3* pos, f3* nrm,
+                                          f3* rad) {
+  diff_f16_load(p, i, M, W, pos, nrm, rad);
+}
 
 __device__ __forceinline__ DiffF32 diff_f32(uint32_t M, float W, f3 pos, f3 nrm, f3 rad) {
   DiffF32 r;
@@ -181,12 +244,18 @@ __device__ __forceinline__ DiffF32 diff_f32(uint32_t M, float W, f3 pos, f3 nrm,
   r.c = make_float4(rad.x, rad.y, rad.z, 0.0f);
   return r;
 }
+__device__ __forceinline__ void diff_store(DiffF32* p, size_t i, uint32_t M, float W, f3 pos, f3 nrm, f3 rad) {
+  p[i] = diff_f32(M, W, pos, nrm, rad);
+}
+__device__ __forceinline__ void diff_store(DiffF16Ptr p, size_t i, uint32_t M, float W, f3 pos, f3 nrm, f3 rad) {
+  diff_f16_store(p, i, M, W, pos, nrm, rad);
+}
 
 // ind_diff_temporal_resample.hlsl:49-200 in the f32 storage form: the sample is kept
 // decoded (the hit normal of an empty HitPosNormal decodes to (0,0,-1)).
-template <class Geo>
+template <class Geo, int FORM>
 struct DiffTemporalF32F {
-  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo, const float* __restrict__ prev_depth, const uint2* __restrict__ new_hpn, const uint32_t* __restrict__ new_rad, const float* __restrict__ new_pdf, const DiffF32* __restrict__ prev_rsv, DiffF32* __restrict__ out, uint32_t frame_rand, uint32_t has_prev_frame, uint32_t has_new_sample) {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo, const float* __restrict__ prev_depth, const uint2* __restrict__ new_hpn, const uint32_t* __restrict__ new_rad, const float* __restrict__ new_pdf, typename DiffStore<FORM>::CPtr prev_rsv, typename DiffStore<FORM>::Ptr out, uint32_t frame_rand, uint32_t has_prev_frame, uint32_t has_new_sample) {
   int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
@@ -207,12 +276,7 @@ struct DiffTemporalF32F {
   if (sample_prev) {
     int px = (int)f2u_rz(uv.x * (float)w), py = (int)f2u_rz(uv.y * (float)h);
     if (inb(px, py, w, h)) {
-      DiffF32 r = prev_rsv[(size_t)py * w + px];
-      M = as_uint(r.b.w);
-      W = r.a.w;
-      hp = mk3(r.a.x, r.a.y, r.a.z);
-      hn = mk3(r.b.x, r.b.y, r.b.z);
-      rad = mk3(r.c.x, r.c.y, r.c.z);
+      diff_load(prev_rsv, (size_t)py * w + px, &M, &W, &hp, &hn, &rad);
     } else {
       hn = empty_n;
     }
@@ -248,7 +312,7 @@ struct DiffTemporalF32F {
     M += 1;
     W = tp > 0.0f ? w_sum / (tp * (float)M) : 0.0f;
   }
-  out[i] = diff_f32(M, W, hp, hn, rad);
+  diff_store(out, i, M, W, hp, hn, rad);
 }
 };
 
@@ -323,7 +387,9 @@ struct DiffSample {
   float tp;
 };
 
-__device__ __forceinline__ DiffSample load_diff(uint4 r, f3 pix_pos, f3 pix_n) {
+
+
+__device__ __forceinline__ DiffSample load_diff_rec(uint4 r, f3 pix_pos, f3 pix_n) {
   DiffSample s;
   s.M = rsv_decode_M(r.x);
   s.W = rsv_decode_W(r.x);
@@ -335,13 +401,13 @@ __device__ __forceinline__ DiffSample load_diff(uint4 r, f3 pix_pos, f3 pix_n) {
   return s;
 }
 
-__device__ __forceinline__ DiffSample load_diff(const DiffF32& r, f3 pix_pos, f3 pix_n) {
+__device__ __forceinline__ DiffSample load_diff(const uint4* p, size_t i, f3 pix_pos, f3 pix_n) {
+  return load_diff_rec(p[i], pix_pos, pix_n);
+}
+template <class CPtr>
+__device__ __forceinline__ DiffSample load_diff(CPtr p, size_t i, f3 pix_pos, f3 pix_n) {
   DiffSample s;
-  s.M = as_uint(r.b.w);
-  s.W = r.a.w;
-  s.pos = mk3(r.a.x, r.a.y, r.a.z);
-  s.nrm = mk3(r.b.x, r.b.y, r.b.z);
-  s.rad = mk3(r.c.x, r.c.y, r.c.z);
+  diff_load(p, i, &s.M, &s.W, &s.pos, &s.nrm, &s.rad);
   float nol = saturate(dot3(pix_n, normalize3(s.pos - pix_pos)));
   s.tp = nol * luminance(s.rad);
   return s;
@@ -355,19 +421,24 @@ __device__ __forceinline__ void store_diff(uint4* out, size_t i, const DiffSampl
   hpn_encode(r.pos, r.nrm, e);
   out[i] = make_uint4(rsv_encode_32b(r.M, r.W), e[0], e[1], pack_r11g11b10(r.rad));
 }
-__device__ __forceinline__ void store_diff(DiffF32* out, size_t i, const DiffSample& r) {
-  out[i] = diff_f32(r.M, r.W, r.pos, r.nrm, r.rad);
+template <class Ptr>
+__device__ __forceinline__ void store_diff(Ptr out, size_t i, const DiffSample& r) {
+  diff_store(out, i, r.M, r.W, r.pos, r.nrm, r.rad);
 }
 __device__ __forceinline__ void store_empty_diff(uint4* out, size_t i) { out[i] = make_uint4(0u, 0u, 0u, 0u); }
 __device__ __forceinline__ void store_empty_diff(DiffF32* out, size_t i) {
   out[i] = diff_f32(0u, 0.0f, mk3(0.0f), hpn_normal(0u), mk3(0.0f));
+}
+__device__ __forceinline__ void store_empty_diff(DiffF16Ptr out, size_t i) {
+  out.main[i] = make_uint4(0u, 0u, 0u, 0u);
+  out.m[i] = 0;
 }
 
 // ind_diff_spatial_resample.hlsl:94-337 (golden-spiral pattern, AO-guided and
 // adaptive radius, plane-distance test, Jacobian clamped to [0, 1]).
 template <class Geo, int FORM>
 struct DiffSpatialF {
-  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo, const typename AoStore<FORM>::Filt* __restrict__ ao_tex, const typename DiffStore<FORM>::Rec* __restrict__ in, typename DiffStore<FORM>::Rec* __restrict__ out, typename DiffStore<FORM>::Light* __restrict__ lighting, uint32_t frame_rand) {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo, const typename AoStore<FORM>::Filt* __restrict__ ao_tex, typename DiffStore<FORM>::CPtr in, typename DiffStore<FORM>::Ptr out, typename DiffStore<FORM>::Light* __restrict__ lighting, uint32_t frame_rand) {
   using S = DiffStore<FORM>;
   int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
@@ -381,7 +452,7 @@ struct DiffSpatialF {
   f3 pos = geo.pos(x, y, i);
   f3 nrm = geo.normal(i);
   float ao = load_ao(ao_tex, i);
-  DiffSample r = load_diff(in[i], pos, nrm);
+  DiffSample r = load_diff(in, i, pos, nrm);
   float w_sum = r.W * r.tp * (float)r.M;
   float radius = kn.radius_px > 0.0f ? kn.radius_px : (float)(w < h ? w : h) * 0.05f;
   radius = fmax_(radius * ao, 1.5f);
@@ -408,7 +479,7 @@ struct DiffSpatialF {
       radius = fmax_(radius * 0.5f, 1.5f);
       continue;
     }
-    DiffSample nb = load_diff(in[j], pos, nrm);
+    DiffSample nb = load_diff(in, j, pos, nrm);
     f3 qq = pn - nb.pos;
     f3 rq = pos - nb.pos;
     float l2qq = dot3(qq, qq);
@@ -509,13 +580,101 @@ struct SpecTarget {
   }
 };
 
+// ------------------------------------------------- specular reservoir storage
+
+// Decoded specular reservoir. rad_bits: the R11G11B10 radiance of the three-plane
+// forms, carried bit-exactly when the sample moves (the reference copies it).
+struct SpecSample {
+  uint32_t M;
+  float W;
+  f3 hit;
+  float tf;  // target function of the sample at the pixel that stored it
+  f3 rad;
+  uint32_t rad_bits;
+};
+
+// Reference and f32 forms: the reference's three planes {M, asuint(W)},
+// {hit xyz, target function}, R11G11B10 radiance.
+struct SpecPlanesC {
+  const uint2* __restrict__ rsv;
+  const float4* __restrict__ hp;
+  const uint32_t* __restrict__ rad;
+};
+struct SpecPlanes {
+  uint2* __restrict__ rsv;
+  float4* __restrict__ hp;
+  uint32_t* __restrict__ rad;
+};
+// f16 form: one 24-byte record {hit f16 x3 | M u16}, {target function f32, W f32},
+// {radiance f16 x3}. The target function and W stay binary32: VNDF pdfs of smooth
+// surfaces exceed the f16 range.
+struct SpecF16 {
+  uint2 a, b, c;
+};
+
+template <int FORM>
+struct SpecStore {
+  using CPtr = SpecPlanesC;
+  using Ptr = SpecPlanes;
+};
+template <>
+struct SpecStore<FORM_F16> {
+  using CPtr = const SpecF16*;
+  using Ptr = SpecF16*;
+};
+
+// Record at (x, y); out of range reads the all-zero record (robust load).
+__device__ __forceinline__ SpecSample spec_ld(SpecPlanesC p, int x, int y, int w, int h) {
+  SpecSample s;
+  uint2 rs = ld(p.rsv, x, y, w, h);
+  float4 p4 = ld(p.hp, x, y, w, h);
+  s.rad_bits = ld(p.rad, x, y, w, h);
+  s.M = rs.x;
+  s.W = as_float(rs.y);
+  s.hit = mk3(p4.x, p4.y, p4.z);
+  s.tf = p4.w;
+  s.rad = unpack_r11g11b10(s.rad_bits);
+  return s;
+}
+__device__ __forceinline__ SpecSample spec_ld(const SpecF16* p, int x, int y, int w, int h) {
+  SpecF16 r;
+  if (inb(x, y, w, h)) {
+    r = p[(size_t)y * w + x];
+  } else {
+    r.a = r.b = r.c = make_uint2(0u, 0u);
+  }
+  SpecSample s;
+  s.hit = mk3(f16tof32(r.a.x & 0xFFFFu), f16tof32(r.a.x >> 16), f16tof32(r.a.y & 0xFFFFu));
+  s.M = r.a.y >> 16;
+  s.tf = as_float(r.b.x);
+  s.W = as_float(r.b.y);
+  s.rad = mk3(f16tof32(r.c.x & 0xFFFFu), f16tof32(r.c.x >> 16), f16tof32(r.c.y & 0xFFFFu));
+  s.rad_bits = 0u;
+  return s;
+}
+__device__ __forceinline__ bool spec_has(SpecPlanes p) { return p.rsv != nullptr; }
+__device__ __forceinline__ bool spec_has(SpecF16* p) { return p != nullptr; }
+__device__ __forceinline__ void spec_st(SpecPlanes p, size_t i, const SpecSample& s) {
+  p.rsv[i] = make_uint2(s.M, as_uint(s.W));
+  p.hp[i] = make_float4(s.hit.x, s.hit.y, s.hit.z, s.tf);
+  p.rad[i] = s.rad_bits;
+}
+__device__ __forceinline__ void spec_st(SpecF16* p, size_t i, const SpecSample& s) {
+  SpecF16 r;
+  r.a = make_uint2(f32tof16_sat(s.hit.x) | (f32tof16_sat(s.hit.y) << 16),
+                   f32tof16_sat(s.hit.z) | ((s.M < 65535u ? s.M : 65535u) << 16));
+  r.b = make_uint2(as_uint(s.tf), as_uint(s.W));
+  r.c = make_uint2(f32tof16_sat(s.rad.x) | (f32tof16_sat(s.rad.y) << 16), f32tof16_sat(s.rad.z));
+  p[i] = r;
+}
+
 // ------------------------------------------------------ specular temporal
 
 // ind_spec_temporal_resample.hlsl:146-362 (VNDF source pdf, BRDF target function,
 // balance-heuristic MIS between previous and current domains).
-template <class Geo>
+template <class Geo, int FORM>
 struct SpecTemporalF {
-  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, uint32_t m_cap, Geo geo, Geo prev_geo, const float* __restrict__ prev_depth, const uint2* __restrict__ prev_rsv, const float4* __restrict__ prev_hp, const uint32_t* __restrict__ prev_rad, const float4* __restrict__ new_hp, const uint32_t* __restrict__ new_rad, uint2* __restrict__ out_rsv, float4* __restrict__ out_hp, uint32_t* __restrict__ out_rad, uint32_t frame_rand, uint32_t has_prev_frame) {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, uint32_t m_cap, Geo geo, Geo prev_geo, const float* __restrict__ prev_depth, typename SpecStore<FORM>::CPtr prev, const float4* __restrict__ new_hp, const uint32_t* __restrict__ new_rad, typename SpecStore<FORM>::Ptr out, uint32_t frame_rand, uint32_t has_prev_frame) {
   int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
@@ -523,9 +682,14 @@ struct SpecTemporalF {
   float4 nhp4 = new_hp[i];
   uint32_t nrad_bits = new_rad[i];
   if (depth == 0.0f) {
-    out_rsv[i] = make_uint2(0u, 0u);
-    out_hp[i] = nhp4;
-    out_rad[i] = nrad_bits;
+    SpecSample z;
+    z.M = 0u;
+    z.W = 0.0f;
+    z.hit = mk3(nhp4.x, nhp4.y, nhp4.z);
+    z.tf = nhp4.w;
+    z.rad_bits = nrad_bits;
+    z.rad = unpack_r11g11b10(nrad_bits);
+    spec_st(out, i, z);
     return;
   }
   f3 pos = geo.pos(x, y, i);
@@ -547,14 +711,13 @@ struct SpecTemporalF {
   float prough = 0.0f;
   if (sample_prev) {
     int px = (int)f2u_rz(uv.x * (float)w), py = (int)f2u_rz(uv.y * (float)h);
-    uint2 rs = ld(prev_rsv, px, py, w, h);
-    M = rs.x;
-    W = as_float(rs.y);
-    float4 p4 = ld(prev_hp, px, py, w, h);
-    rhp = mk3(p4.x, p4.y, p4.z);
-    rrad_bits = ld(prev_rad, px, py, w, h);
-    rrad = unpack_r11g11b10(rrad_bits);
-    rtf = p4.w;
+    SpecSample r = spec_ld(prev, px, py, w, h);
+    M = r.M;
+    W = r.W;
+    rhp = r.hit;
+    rrad_bits = r.rad_bits;
+    rrad = r.rad;
+    rtf = r.tf;
     prev_geo.material_or_zero(px, py, &pn, &prough, &pf0);
   }
   f3 nhp = mk3(nhp4.x, nhp4.y, nhp4.z);
@@ -588,13 +751,19 @@ struct SpecTemporalF {
   if (!use_prev) {
     rhp = nhp;
     rrad_bits = nrad_bits;
+    rrad = nrad;
     rtf = new_tf;
   }
   M += 1;
   W = rtf > 0.0f ? w_sum / rtf : 0.0f;
-  out_rsv[i] = make_uint2(M, as_uint(W));
-  out_hp[i] = make_float4(rhp.x, rhp.y, rhp.z, rtf);
-  out_rad[i] = rrad_bits;
+  SpecSample o;
+  o.M = M;
+  o.W = W;
+  o.hit = rhp;
+  o.tf = rtf;
+  o.rad = rrad;
+  o.rad_bits = rrad_bits;
+  spec_st(out, i, o);
 }
 };
 
@@ -636,10 +805,28 @@ __device__ __forceinline__ void store_spec_light(uint32_t* l, uint16_t* rl, size
 __device__ __forceinline__ void store_spec_light(float4* l, uint16_t*, size_t i, f3 v, float ray_len) {
   if (l) l[i] = make_float4(v.x, v.y, v.z, ray_len);
 }
+__device__ __forceinline__ void store_spec_light(uint2* l, uint16_t*, size_t i, f3 v, float ray_len) {
+  if (l) l[i] = make_uint2(f32tof16_sat(v.x) | (f32tof16_sat(v.y) << 16), f32tof16_sat(v.z) | (f32tof16_sat(ray_len) << 16));
+}
+template <int FORM>
+struct SpecLight;
+template <>
+struct SpecLight<FORM_REF> {
+  using T = uint32_t;  // R11G11B10 (+ the separate half ray-length plane)
+};
+template <>
+struct SpecLight<FORM_F32> {
+  using T = float4;  // {rgb, ray length}
+};
+template <>
+struct SpecLight<FORM_F16> {
+  using T = uint2;  // half4 {rgb, ray length}
+};
 
-template <class Geo, class Light>
+template <class Geo, int FORM>
 struct SpecSpatialF {
-  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo, const uint2* __restrict__ rsv, const float4* __restrict__ hp_tex, const uint32_t* __restrict__ rad_tex, Light* __restrict__ lighting, uint16_t* __restrict__ ray_len_out, uint2* __restrict__ out_rsv, float4* __restrict__ out_hp, uint32_t* __restrict__ out_rad, uint32_t frame_rand) {
+  using Light = typename SpecLight<FORM>::T;
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo, typename SpecStore<FORM>::CPtr in, Light* __restrict__ lighting, uint16_t* __restrict__ ray_len_out, typename SpecStore<FORM>::Ptr out, uint32_t frame_rand) {
   // The tap count of a pixel is uint(roughness * taps), so neighbouring lanes can
   // run very different loop lengths. The pixels of the tile are therefore
   // reordered by tap count (counting sort in shared memory) before the loop, so a
@@ -687,10 +874,11 @@ struct SpecSpatialF {
   float depth = geo.dep(i);
   if (depth == 0.0f) {
     store_spec_light(lighting, ray_len_out, i, mk3(0.0f), 0.0f);
-    if (out_rsv) {
-      out_rsv[i] = make_uint2(0u, 0u);
-      out_hp[i] = hp_tex[i];
-      out_rad[i] = rad_tex[i];
+    if (spec_has(out)) {
+      SpecSample z = spec_ld(in, x, y, w, h);
+      z.M = 0u;
+      z.W = 0.0f;
+      spec_st(out, i, z);
     }
     return;
   }
@@ -699,14 +887,13 @@ struct SpecSpatialF {
   float prc = geo.rough(i);
   SpecTarget center;
   center.init(view_pos, pos, geo.normal(i), prc, geo.f0(i));
-  uint2 rs = rsv[i];
-  uint32_t M = rs.x;
-  float W = as_float(rs.y);
-  float4 hp4 = hp_tex[i];
-  f3 hit = mk3(hp4.x, hp4.y, hp4.z);
-  uint32_t rad_bits = rad_tex[i];
-  f3 rad = unpack_r11g11b10(rad_bits);
-  float ctf = hp4.w;
+  const SpecSample c0 = spec_ld(in, x, y, w, h);
+  uint32_t M = c0.M;
+  float W = c0.W;
+  f3 hit = c0.hit;
+  uint32_t rad_bits = c0.rad_bits;
+  f3 rad = c0.rad;
+  float ctf = c0.tf;
   const uint32_t n_iter = f2u_rz(0.0f + prc * ((float)kn.taps - 0.0f));
   float radius = kn.radius_px > 0.0f ? kn.radius_px : (float)(w < h ? w : h) * 0.05f;
   uint32_t rng = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
@@ -731,14 +918,13 @@ struct SpecSpatialF {
       radius = fmax_(radius * 0.5f, 1.5f);
       continue;
     }
-    uint2 rsn = rsv[j];
-    uint32_t Mn = rsn.x;
-    float Wn = as_float(rsn.y);
-    float4 hpn4 = hp_tex[j];
-    f3 hitn = mk3(hpn4.x, hpn4.y, hpn4.z);
-    uint32_t radn_bits = rad_tex[j];
-    f3 radn = unpack_r11g11b10(radn_bits);
-    float tfn = hpn4.w;
+    const SpecSample nb = spec_ld(in, nx, ny, w, h);
+    uint32_t Mn = nb.M;
+    float Wn = nb.W;
+    f3 hitn = nb.hit;
+    uint32_t radn_bits = nb.rad_bits;
+    f3 radn = nb.rad;
+    float tfn = nb.tf;
     float w_nb, w_c;
     {
       float ctf_on_n = center.tf(hitn, radn);
@@ -764,10 +950,15 @@ struct SpecSpatialF {
     W = ctf > 0.0f ? w_sum / ctf : 0.0f;
   }
   float ray_len = length3(hit - pos);
-  if (out_rsv) {
-    out_rsv[i] = make_uint2(M, as_uint(W));
-    out_hp[i] = make_float4(hit.x, hit.y, hit.z, ctf);
-    out_rad[i] = rad_bits;
+  if (spec_has(out)) {
+    SpecSample o;
+    o.M = M;
+    o.W = W;
+    o.hit = hit;
+    o.tf = ctf;
+    o.rad = rad;
+    o.rad_bits = rad_bits;
+    spec_st(out, i, o);
   }
   if (lighting) {
     const float roughness = center.roughness;
@@ -820,6 +1011,16 @@ static GeoSurface surf_geo(const GeoArgs& a, int w, int h) {
     }                                          \
   } while (0)
 
+// f16-form diffuse buffers: the 16-byte records of all pixels, then the M bytes.
+static DiffF16CPtr diff_f16_cptr(const void* base, int w, int h) {
+  DiffF16CPtr p = {(const uint4*)base, (const uint8_t*)base + (size_t)16 * w * h};
+  return p;
+}
+static DiffF16Ptr diff_f16_ptr(void* base, int w, int h) {
+  DiffF16Ptr p = {(uint4*)base, (uint8_t*)base + (size_t)16 * w * h};
+  return p;
+}
+
 void launch_surface(const Exec& ex, const vlt_frame_params& fp, int w, int h, const float* depth,
                     const uint32_t* gbuf, float4* nd, float4* pr, float4* fz) {
   launch2d<SurfaceF>(ex, "surface", w, h, fp, w, h, depth, gbuf, nd, pr, fz);
@@ -832,6 +1033,10 @@ void launch_ao_gen(const Exec& ex, int form, const vlt_frame_params& fp, int w, 
     VLT_GEO_DISPATCH(ga, (launch2d<AoGenF<Geo, FORM_F32>>(ex, "ao_gen", w, h, fp, w, h, geo, (const uint2*)hpn,
                                                          (const float2*)prev_ao, (float2*)ao, has_new, has_prev,
                                                          radius)));
+  else if (form == FORM_F16)
+    VLT_GEO_DISPATCH(ga, (launch2d<AoGenF<Geo, FORM_F16>>(ex, "ao_gen", w, h, fp, w, h, geo, (const uint2*)hpn,
+                                                         (const uint32_t*)prev_ao, (uint32_t*)ao, has_new, has_prev,
+                                                         radius)));
   else
     VLT_GEO_DISPATCH(ga, (launch2d<AoGenF<Geo, FORM_REF>>(ex, "ao_gen", w, h, fp, w, h, geo, (const uint2*)hpn,
                                                          (const uint32_t*)prev_ao, (uint32_t*)ao, has_new, has_prev,
@@ -841,6 +1046,8 @@ void launch_ao_gen(const Exec& ex, int form, const vlt_frame_params& fp, int w, 
 void launch_ao_filter(const Exec& ex, int form, int w, int h, const float* depth, const void* ao, void* out) {
   if (form == FORM_F32)
     launch2d<AoFilterF<FORM_F32>>(ex, "ao_filter", w, h, w, h, depth, (const float2*)ao, (float*)out);
+  else if (form == FORM_F16)
+    launch2d<AoFilterF<FORM_F16>>(ex, "ao_filter", w, h, w, h, depth, (const uint32_t*)ao, (uint16_t*)out);
   else
     launch2d<AoFilterF<FORM_REF>>(ex, "ao_filter", w, h, w, h, depth, (const uint32_t*)ao, (uint16_t*)out);
 }
@@ -850,10 +1057,15 @@ void launch_diff_temporal(const Exec& ex, int form, const vlt_frame_params& fp, 
                           const uint32_t* new_rad, const float* new_pdf, const void* prev_rsv, void* out,
                           uint32_t frame_rand, uint32_t has_prev, uint32_t has_new) {
   if (form == FORM_F32)
-    VLT_GEO_DISPATCH(ga, (launch2d<DiffTemporalF32F<Geo>>(ex, "diff_temporal", w, h, fp, w, h, kn, geo, prev_depth,
-                                                          (const uint2*)new_hpn, new_rad, new_pdf,
-                                                          (const DiffF32*)prev_rsv, (DiffF32*)out, frame_rand,
-                                                          has_prev, has_new)));
+    VLT_GEO_DISPATCH(ga, (launch2d<DiffTemporalF32F<Geo, FORM_F32>>(ex, "diff_temporal", w, h, fp, w, h, kn, geo,
+                                                                    prev_depth, (const uint2*)new_hpn, new_rad,
+                                                                    new_pdf, (const DiffF32*)prev_rsv, (DiffF32*)out,
+                                                                    frame_rand, has_prev, has_new)));
+  else if (form == FORM_F16)
+    VLT_GEO_DISPATCH(ga, (launch2d<DiffTemporalF32F<Geo, FORM_F16>>(
+                             ex, "diff_temporal", w, h, fp, w, h, kn, geo, prev_depth, (const uint2*)new_hpn, new_rad,
+                             new_pdf, diff_f16_cptr(prev_rsv, w, h), diff_f16_ptr(out, w, h), frame_rand, has_prev,
+                             has_new)));
   else
     VLT_GEO_DISPATCH(ga, (launch2d<DiffTemporalF<Geo>>(ex, "diff_temporal", w, h, fp, w, h, kn, geo, prev_depth,
                                                        (const uint2*)new_hpn, new_rad, new_pdf,
@@ -868,44 +1080,62 @@ void launch_diff_spatial(const Exec& ex, int form, const vlt_frame_params& fp, i
     VLT_GEO_DISPATCH(ga, (launch2d<DiffSpatialF<Geo, FORM_F32>>(ex, "diff_spatial", w, h, fp, w, h, kn, geo,
                                                                (const float*)ao, (const DiffF32*)in, (DiffF32*)out,
                                                                (float4*)lighting, frame_rand)));
+  else if (form == FORM_F16)
+    VLT_GEO_DISPATCH(ga, (launch2d<DiffSpatialF<Geo, FORM_F16>>(ex, "diff_spatial", w, h, fp, w, h, kn, geo,
+                                                               (const uint16_t*)ao, diff_f16_cptr(in, w, h),
+                                                               diff_f16_ptr(out, w, h), (uint2*)lighting,
+                                                               frame_rand)));
   else
     VLT_GEO_DISPATCH(ga, (launch2d<DiffSpatialF<Geo, FORM_REF>>(ex, "diff_spatial", w, h, fp, w, h, kn, geo,
                                                                (const uint16_t*)ao, (const uint4*)in, (uint4*)out,
                                                                (uint32_t*)lighting, frame_rand)));
 }
 
-void launch_spec_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h, uint32_t m_cap,
+void launch_spec_temporal(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, uint32_t m_cap,
                           const GeoArgs& ga, const GeoArgs& prev_ga, const float* prev_depth,
                           const uint32_t* prev_rsv, const float* prev_hp, const uint32_t* prev_rad,
                           const float* new_hp, const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp,
                           uint32_t* out_rad, uint32_t frame_rand, uint32_t has_prev) {
-  if (ga.nd)
-    launch2d<SpecTemporalF<GeoSurface>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, surf_geo(ga, w, h),
-                                        surf_geo(prev_ga, w, h), prev_depth, (const uint2*)prev_rsv,
-                                        (const float4*)prev_hp, prev_rad, (const float4*)new_hp, new_rad,
-                                        (uint2*)out_rsv, (float4*)out_hp, out_rad, frame_rand, has_prev);
-  else
-    launch2d<SpecTemporalF<GeoRaw>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, raw_geo(ga, w, h),
-                                    raw_geo(prev_ga, w, h), prev_depth, (const uint2*)prev_rsv,
-                                    (const float4*)prev_hp, prev_rad, (const float4*)new_hp, new_rad,
-                                    (uint2*)out_rsv, (float4*)out_hp, out_rad, frame_rand, has_prev);
+  SpecPlanesC pin = {(const uint2*)prev_rsv, (const float4*)prev_hp, prev_rad};
+  SpecPlanes pout = {(uint2*)out_rsv, (float4*)out_hp, out_rad};
+  if (ga.nd) {
+    GeoSurface g = surf_geo(ga, w, h), pg = surf_geo(prev_ga, w, h);
+    if (form == FORM_F16)
+      launch2d<SpecTemporalF<GeoSurface, FORM_F16>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, g, pg, prev_depth,
+                                                    (const SpecF16*)prev_hp, (const float4*)new_hp, new_rad,
+                                                    (SpecF16*)out_hp, frame_rand, has_prev);
+    else
+      launch2d<SpecTemporalF<GeoSurface, FORM_REF>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, g, pg, prev_depth,
+                                                    pin, (const float4*)new_hp, new_rad, pout, frame_rand, has_prev);
+  } else {
+    GeoRaw g = raw_geo(ga, w, h), pg = raw_geo(prev_ga, w, h);
+    if (form == FORM_F16)
+      launch2d<SpecTemporalF<GeoRaw, FORM_F16>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, g, pg, prev_depth,
+                                                (const SpecF16*)prev_hp, (const float4*)new_hp, new_rad,
+                                                (SpecF16*)out_hp, frame_rand, has_prev);
+    else
+      launch2d<SpecTemporalF<GeoRaw, FORM_REF>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, g, pg, prev_depth, pin,
+                                                (const float4*)new_hp, new_rad, pout, frame_rand, has_prev);
+  }
 }
 
 void launch_spec_spatial(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const SpecKnobs& kn,
                          const GeoArgs& ga, const uint32_t* rsv, const float* hp, const uint32_t* rad,
                          void* lighting, uint16_t* ray_len, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
                          uint32_t frame_rand) {
+  SpecPlanesC pin = {(const uint2*)rsv, (const float4*)hp, rad};
+  SpecPlanes pout = {(uint2*)out_rsv, (float4*)out_hp, out_rad};
   if (form == FORM_F32)
-    VLT_GEO_DISPATCH(ga, (launch2d<SpecSpatialF<Geo, float4>>(ex, "spec_spatial", w, h, fp, w, h, kn, geo,
-                                                              (const uint2*)rsv, (const float4*)hp, rad,
-                                                              (float4*)lighting, (uint16_t*)nullptr,
-                                                              (uint2*)out_rsv, (float4*)out_hp, out_rad,
-                                                              frame_rand)));
+    VLT_GEO_DISPATCH(ga, (launch2d<SpecSpatialF<Geo, FORM_F32>>(ex, "spec_spatial", w, h, fp, w, h, kn, geo, pin,
+                                                               (float4*)lighting, (uint16_t*)nullptr, pout,
+                                                               frame_rand)));
+  else if (form == FORM_F16)
+    VLT_GEO_DISPATCH(ga, (launch2d<SpecSpatialF<Geo, FORM_F16>>(ex, "spec_spatial", w, h, fp, w, h, kn, geo,
+                                                               (const SpecF16*)hp, (uint2*)lighting,
+                                                               (uint16_t*)nullptr, (SpecF16*)out_hp, frame_rand)));
   else
-    VLT_GEO_DISPATCH(ga, (launch2d<SpecSpatialF<Geo, uint32_t>>(ex, "spec_spatial", w, h, fp, w, h, kn, geo,
-                                                                (const uint2*)rsv, (const float4*)hp, rad,
-                                                                (uint32_t*)lighting, ray_len, (uint2*)out_rsv,
-                                                                (float4*)out_hp, out_rad, frame_rand)));
+    VLT_GEO_DISPATCH(ga, (launch2d<SpecSpatialF<Geo, FORM_REF>>(ex, "spec_spatial", w, h, fp, w, h, kn, geo, pin,
+                                                               (uint32_t*)lighting, ray_len, pout, frame_rand)));
 }
 
 #undef VLT_GEO_DISPATCH

@@ -59,7 +59,10 @@ void launch_diff_temporal(const Exec& ex, int form, const vlt_frame_params& fp, 
 void launch_diff_spatial(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn,
                          const GeoArgs& ga, const void* ao, const void* in, void* out, void* lighting,
                          uint32_t frame_rand);
-void launch_spec_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h, uint32_t m_cap,
+// Specular reservoirs: reference and f32 forms pass the three planes (rsv, hp, rad);
+// the f16 form passes its 24-byte records as `hp` (rsv and rad unused). f16-form
+// diffuse buffers hold the 16-byte records of all pixels followed by the M bytes.
+void launch_spec_temporal(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, uint32_t m_cap,
                           const GeoArgs& ga, const GeoArgs& prev_ga, const float* prev_depth,
                           const uint32_t* prev_rsv, const float* prev_hp, const uint32_t* prev_rad,
                           const float* new_hp, const uint32_t* new_rad, uint32_t* out_rsv, float* out_hp,
@@ -69,20 +72,21 @@ void launch_spec_spatial(const Exec& ex, int form, const vlt_frame_params& fp, i
                          void* lighting, uint16_t* ray_len, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
                          uint32_t frame_rand);
 
-// denoise_f32.cu — the f32 storage form of the denoiser. Records: DnRec
-// {float4 diffuse.rgb|aux.x, float4 specular.rgb|aux.y} with aux = moments (temporal /
-// fix outputs, history) or variance (fallback / a-trous); history length float.
-void launch_dn32_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn,
-                          const GeoArgs& ga, const GeoArgs& prev_ga, const float4* diff_src, const float4* spec_src,
-                          const float* prev_depth, const float4* hist, const float* len_hist, const float4* fast_hist,
-                          float4* out, float* out_len, float4* out_fast, uint32_t has_history);
-void launch_dn32_fix(const Exec& ex, int w, int h, const GeoArgs& ga, const float* len, const float4* in,
-                     float4* out);
-void launch_dn32_fast_clamp(const Exec& ex, int w, int h, const float4* fast, float4* rec);
-void launch_dn32_fallback(const Exec& ex, int w, int h, const GeoArgs& ga, const float* len, const float4* in,
-                          float4* out);
-void launch_dn32_atrous(const Exec& ex, int w, int h, const GeoArgs& ga, const float4* in, float4* out,
-                        float4* out_diff, float4* out_spec, int step);
+// denoise_f32.cu — the denoiser of the f32 and f16 storage forms (`form`). Records:
+// {diffuse.rgb, aux.x, specular.rgb, aux.y} as 2 float4 (f32) or 8 halves (f16),
+// aux = moments (temporal / fix outputs, history) or variance (fallback / a-trous);
+// history length float / half; lighting inputs and outputs float4 / half4.
+void launch_dn32_temporal(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn,
+                          const GeoArgs& ga, const GeoArgs& prev_ga, const void* diff_src, const void* spec_src,
+                          const float* prev_depth, const void* hist, const void* len_hist, const void* fast_hist,
+                          void* out, void* out_len, void* out_fast, uint32_t has_history);
+void launch_dn32_fix(const Exec& ex, int form, int w, int h, const GeoArgs& ga, const void* len, const void* in,
+                     void* out);
+void launch_dn32_fast_clamp(const Exec& ex, int form, int w, int h, const void* fast, void* rec);
+void launch_dn32_fallback(const Exec& ex, int form, int w, int h, const GeoArgs& ga, const void* len, const void* in,
+                          void* out);
+void launch_dn32_atrous(const Exec& ex, int form, int w, int h, const GeoArgs& ga, const void* in, void* out,
+                        void* out_diff, void* out_spec, int step);
 
 // denoise.cu
 void launch_dn_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn,

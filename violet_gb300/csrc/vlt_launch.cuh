@@ -217,7 +217,8 @@ void launch1d(const Exec& ex, const char* name, uint32_t n, A... a) {
 // Stream-ordered fill / copy that batch recording can capture as kernels.
 void ex_fill32(const Exec& ex, void* dst, uint32_t value, size_t bytes);
 void ex_copy(const Exec& ex, void* dst, const void* src, size_t bytes);
-// `rows` copies of 16 bytes from src + r * spitch to dst + r * dpitch.
-void ex_copy_rows16(const Exec& ex, void* dst, size_t dpitch, const void* src, size_t spitch, size_t rows);
+// `rows` copies of `width` (8 or 16) bytes from src + r * spitch to dst + r * dpitch.
+void ex_copy_rows(const Exec& ex, void* dst, size_t dpitch, const void* src, size_t spitch, size_t width,
+                  size_t rows);
 
 }  // namespace vlt

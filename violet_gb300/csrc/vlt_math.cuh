@@ -395,6 +395,17 @@ VLT_HD float f16tof32(uint32_t h) {
 #endif
 }
 
+// Storage conversion of the f16 form: RNE, saturating to +-65504, NaN -> 0 (an
+// overflow must not turn into inf, which the variance and MIS arithmetic would turn
+// into NaN).
+VLT_HD uint32_t f32tof16_sat(float f) {
+  if (is_nan(f)) return 0u;
+  float c = fmin_(fmax_(f, -65504.0f), 65504.0f);
+  return f32tof16(c);
+}
+// The value an f16-form store keeps.
+VLT_HD float q16(float f) { return f16tof32(f32tof16_sat(f)); }
+
 // ---------------------------------------- unsigned small floats (R11G11B10)
 
 // binary32 -> unsigned float with 5 exponent bits (bias 15) and `mb` mantissa
