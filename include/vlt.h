@@ -462,6 +462,14 @@ vlt_status vlt_hg_find(const vlt_frame_params* fp, uint32_t log2_buckets, uint32
  * 3 sin, 4 cos. x and y are device arrays of n floats. */
 vlt_status vlt_diag_math(int fn, const float* x, float* y, uint32_t n, void* stream);
 
+/* Diagnostics (no counterpart in the reference): image-wide sums in binary64 on the
+ * device, for energy and error statistics of outputs. out (8 device doubles, zeroed
+ * by the call): [0..2] sum of a.rgb, [3..5] sum of b.rgb, [6] sum of |a - b|^2,
+ * [7] sum of |b|^2. Element types: 0 float4 {rgb, -}, 1 half4 {rgb, -}, 2 R11G11B10.
+ * b may be NULL (then out[3..7] stay 0). */
+vlt_status vlt_image_stats(const void* a, int a_type, const void* b, int b_type, uint32_t n, double* out,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,7 +1,8 @@
 """ORACLE build recipe (test infrastructure only).
 
-Compiles the CPU restatement (oracle.cpp) into oracle/_build/libvlt_oracle.so with
-g++ (OpenMP, binary32 without FMA contraction). The reference itself (HLSL + a
+Compiles the CPU restatement (oracle.cpp, binary32 without FMA contraction) and its
+binary64 denoiser (oracle64.cpp) into oracle/_build/libvlt_oracle.so with g++
+(OpenMP). The reference itself (HLSL + a
 Rust/Vulkan host) cannot be compiled here, so there is no oracle/_ref build.
 """
 import os
@@ -10,7 +11,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build", "libvlt_oracle.so")
-SRCS = [os.path.join(HERE, "oracle.cpp")]
+SRCS = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "oracle64.cpp")]
 DEPS = SRCS + [os.path.join(HERE, "omath.hpp"), os.path.join(os.path.dirname(HERE), "include", "vlt.h")]
 FLAGS = ["-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
 

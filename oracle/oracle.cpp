@@ -1516,9 +1516,10 @@ inline void rec_store(float* r, size_t j, float3 d, float3 s, float2 aux) {
   q[0] = d.x, q[1] = d.y, q[2] = d.z, q[3] = aux.x;
   q[4] = s.x, q[5] = s.y, q[6] = s.z, q[7] = aux.y;
 }
-// Storage of the f32 form (FORM 1: 8 floats per record, float history length,
-// float4 lighting) and the f16 form (FORM 2: 8 halves per record, half history
-// length, half4 lighting; stores saturate).
+// Storage of the f32 form (FORM 1: 8 floats per record, float4 lighting) and the f16
+// form (FORM 2: 8 halves per record {d.rgb, sqrt(aux.x), s.rgb, sqrt(aux.y)}, half4
+// lighting; stores saturate). The history length is a frame count stored as the
+// reference does (R8_UNORM) in both.
 template <int FORM>
 struct Dio;
 template <>
@@ -1526,8 +1527,8 @@ struct Dio<1> {
   static Rec32 load(const void* p, size_t j) { return rec_load((const float*)p, j); }
   static void store(void* p, size_t j, float3 d, float3 s, float2 aux) { rec_store((float*)p, j, d, s, aux); }
   static void copy(void* o, const void* in, size_t j) { memcpy((char*)o + 32 * j, (const char*)in + 32 * j, 32); }
-  static float len(const void* p, size_t j) { return ((const float*)p)[j]; }
-  static void set_len(void* p, size_t j, float v) { ((float*)p)[j] = v; }
+  static float len(const void* p, size_t j) { return load_unorm8(((const uint8_t*)p)[j]); }
+  static void set_len(void* p, size_t j, float v) { ((uint8_t*)p)[j] = store_unorm8(v); }
   static float4 light(const void* p, size_t j) {
     const float* q = (const float*)p + 4 * j;
     return F4(q[0], q[1], q[2], q[3]);
@@ -1541,19 +1542,20 @@ template <>
 struct Dio<2> {
   static Rec32 load(const void* p, size_t j) {
     const uint16_t* q = (const uint16_t*)p + 8 * j;
+    float ax = f16tof32(q[3]), ay = f16tof32(q[7]);
     return Rec32{F3(f16tof32(q[0]), f16tof32(q[1]), f16tof32(q[2])), F3(f16tof32(q[4]), f16tof32(q[5]), f16tof32(q[6])),
-                 F2(f16tof32(q[3]), f16tof32(q[7]))};
+                 F2(ax * ax, ay * ay)};
   }
   static void store(void* p, size_t j, float3 d, float3 s, float2 aux) {
     uint16_t* q = (uint16_t*)p + 8 * j;
     q[0] = (uint16_t)f16sat(d.x), q[1] = (uint16_t)f16sat(d.y), q[2] = (uint16_t)f16sat(d.z);
-    q[3] = (uint16_t)f16sat(aux.x);
+    q[3] = (uint16_t)f16sat(sqrtf(hmax(aux.x, 0.0f)));
     q[4] = (uint16_t)f16sat(s.x), q[5] = (uint16_t)f16sat(s.y), q[6] = (uint16_t)f16sat(s.z);
-    q[7] = (uint16_t)f16sat(aux.y);
+    q[7] = (uint16_t)f16sat(sqrtf(hmax(aux.y, 0.0f)));
   }
   static void copy(void* o, const void* in, size_t j) { memcpy((char*)o + 16 * j, (const char*)in + 16 * j, 16); }
-  static float len(const void* p, size_t j) { return f16tof32(((const uint16_t*)p)[j]); }
-  static void set_len(void* p, size_t j, float v) { ((uint16_t*)p)[j] = (uint16_t)f16sat(v); }
+  static float len(const void* p, size_t j) { return load_unorm8(((const uint8_t*)p)[j]); }
+  static void set_len(void* p, size_t j, float v) { ((uint8_t*)p)[j] = store_unorm8(v); }
   static float4 light(const void* p, size_t j) {
     const uint16_t* q = (const uint16_t*)p + 4 * j;
     return F4(f16tof32(q[0]), f16tof32(q[1]), f16tof32(q[2]), f16tof32(q[3]));
@@ -2429,7 +2431,7 @@ void* vlto_view_create_form(uint32_t w, uint32_t h, const vlt_params* p, int for
     v->fdiff_light.assign(by(16, 8), 0);
     v->fspec_light.assign(by(16, 8), 0);
     v->fhist_rec.assign(by(32, 16), 0);
-    v->fhist_len.assign(by(4, 2), 0);
+    v->fhist_len.assign(n, 0);
     v->ffast_prev.assign(p->fast_history_clamp ? by(32, 16) : (f32 ? 32 : 16), 0);
     v->ffallback.assign(by(32, 16), 0);
     if (form == 2) v->spec_hp_prev.assign(6 * n, 0.0f);

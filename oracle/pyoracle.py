@@ -25,6 +25,10 @@ SIGS = {
     "vlto_get_threads": (C.c_int, []),
     "vlto_view_create": (P, [U32, U32, PP]),
     "vlto_view_create_form": (P, [U32, U32, PP, C.c_int]),
+    "vlto64_create": (P, [U32, U32, PP]),
+    "vlto64_destroy": (None, [P]),
+    "vlto64_frame": (None, [P, FP, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                             C.c_void_p, C.c_void_p]),
     "vlto_view_destroy": (None, [P]),
     "vlto_frame_run": (None, [P, C.POINTER(_ffi.FrameInputs), C.POINTER(_ffi.FrameOutputs)]),
     "vlto_view_buffer": (P, [P, C.c_char_p, C.POINTER(C.c_size_t)]),
@@ -133,6 +137,39 @@ class OracleView:
     def close(self):
         if self.handle:
             lib().vlto_view_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Denoiser64:
+    """Binary64 denoiser fed with a form's raw lighting (precision reference)."""
+
+    def __init__(self, width, height, params):
+        self.width, self.height = int(width), int(height)
+        self.params = params
+        self.handle = lib().vlto64_create(self.width, self.height, C.byref(params))
+
+    def frame(self, frame_params, host_inputs, diff_rgb, spec_rgb, ray_len, run_denoiser):
+        """diff_rgb / spec_rgb: float32 (n, 3); ray_len: float32 (n,). Returns two
+        float64 (n, 3) arrays (meaningful when the denoiser ran)."""
+        n = self.width * self.height
+        d = np.ascontiguousarray(diff_rgb, np.float32)
+        s = np.ascontiguousarray(spec_rgb, np.float32)
+        r = np.ascontiguousarray(ray_len, np.float32)
+        od = np.zeros((n, 3), np.float64)
+        os_ = np.zeros((n, 3), np.float64)
+        lib().vlto64_frame(self.handle, C.byref(frame_params), ptr(host_inputs["depth"]), ptr(host_inputs["gbuffer"]),
+                           ptr(d), ptr(s), ptr(r), 1 if run_denoiser else 0, ptr(od), ptr(os_))
+        return od, os_
+
+    def close(self):
+        if self.handle:
+            lib().vlto64_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

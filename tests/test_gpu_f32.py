@@ -30,7 +30,7 @@ BUFFERS = {
             ("raw_diffuse", 2), ("raw_specular", 2)],
 }
 DENOISE = {
-    "f32": [("hist_len", 1), ("hist_record", 8), ("fallback_record", 8)],
+    "f32": [("hist_len", None), ("hist_record", 8), ("fallback_record", 8)],
     "f16": [("hist_len", None), ("hist_record", 4), ("fallback_record", 4)],
 }
 OUT_PX = {"f32": 16, "f16": 8}

@@ -208,6 +208,7 @@ SIGNATURES = {
     "vlt_hg_update": (C.c_int, [U32, P, P, P, P, P, P, P]),
     "vlt_hg_emit_queries": (C.c_int, [FP, U32, U32, U32, U32, U32, P, P, P, P, P, P]),
     "vlt_hg_find": (C.c_int, [FP, U32, U32, P, U32, P, P, P, P, P]),
+    "vlt_image_stats": (C.c_int, [P, C.c_int, P, C.c_int, U32, P, P]),
     "vlt_diag_math": (C.c_int, [C.c_int, P, P, U32, P]),
     "vlt_scene_desc_default": (None, [C.POINTER(SceneDesc), C.c_uint64, U32, U32]),
     "vlt_scene_frame_params": (C.c_int, [C.POINTER(SceneDesc), U32, FP]),

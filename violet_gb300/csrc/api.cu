@@ -68,7 +68,7 @@ struct ViewBuffers {
   uint32_t* var[3];        // half2: fallback output, a-trous ping-pong
   uint32_t* color_c;       // fallback output
   uint32_t* fast[2];       // uint2 fast history
-  void* len[2];            // R8_UNORM / float history length
+  void* len[2];            // history length, R8_UNORM in every form
   // f32-form denoiser: 32-byte records {diff.rgb|aux.x, spec.rgb|aux.y}: history,
   // fix output, temporal output / a-trous ping-pong, a-trous ping-pong, fallback output
   float4* rec[5];
@@ -172,7 +172,7 @@ size_t layout(vlt_view* v, char* base) {
     }
   }
   b.spec_light = take(by(4, 16, 8) * n);
-  for (int k = 0; k < 2; ++k) b.len[k] = take(by(1, 4, 2) * n);
+  for (int k = 0; k < 2; ++k) b.len[k] = take(n);  // R8_UNORM in every form
   if (f32 || f16) {
     const size_t rb = f32 ? 32 : 16;
     for (int k = 0; k < 5; ++k) b.rec[k] = (float4*)take(rb * n);
@@ -511,7 +511,7 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
       {"hist_moments", ref ? b.mom[0] : nullptr, 4 * n},
       {"hist_record", ref ? nullptr : b.rec[0], by(0, 32, 16) * n},
       {"fallback_record", ref ? nullptr : b.rec[4], by(0, 32, 16) * n},
-      {"hist_len", b.len[0], by(1, 4, 2) * n},
+      {"hist_len", b.len[0], n},
       {"variance", ref ? b.var[0] : nullptr, 4 * n},
       {"spec_ray_len", ref ? b.ray_len : nullptr, 2 * n},
       {"raw_diffuse", b.diff_light, by(4, 16, 8) * n},
@@ -1066,5 +1066,59 @@ extern "C" vlt_status vlt_diag_math(int fn, const float* x, float* y, uint32_t n
   if (fn < 0 || fn > 4 || (n && (!x || !y))) return VLT_ERR_INVALID_ARG;
   if (n == 0) return VLT_OK;
   vlt::k_diag_math<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(fn, x, y, n);
+  return vlt::cuda_status(cudaGetLastError());
+}
+
+namespace vlt {
+
+// One pixel of an image of element type t: 0 float4 {rgb, -}, 1 half4, 2 R11G11B10.
+__device__ __forceinline__ f3 image_px(const void* p, int t, uint32_t i) {
+  if (t == 0) {
+    float4 v = ((const float4*)p)[i];
+    return mk3(v.x, v.y, v.z);
+  }
+  if (t == 1) {
+    uint2 v = ((const uint2*)p)[i];
+    return mk3(f16tof32(v.x & 0xFFFFu), f16tof32(v.x >> 16), f16tof32(v.y & 0xFFFFu));
+  }
+  return unpack_r11g11b10(((const uint32_t*)p)[i]);
+}
+
+// Image-wide sums in binary64: out[0..2] sum a.rgb, out[3..5] sum b.rgb,
+// out[6] sum |a - b|^2, out[7] sum |b|^2. Grid-stride; warp shuffles, then one
+// double atomic per warp and sum.
+__global__ void k_image_stats(const void* __restrict__ a, int at, const void* __restrict__ b, int bt, uint32_t n,
+                              double* __restrict__ out) {
+  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    f3 x = image_px(a, at, i);
+    s[0] += x.x, s[1] += x.y, s[2] += x.z;
+    if (b) {
+      f3 y = image_px(b, bt, i);
+      s[3] += y.x, s[4] += y.y, s[5] += y.z;
+      double dx = (double)x.x - y.x, dy = (double)x.y - y.y, dz = (double)x.z - y.z;
+      s[6] += dx * dx + dy * dy + dz * dz;
+      s[7] += (double)y.x * y.x + (double)y.y * y.y + (double)y.z * y.z;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    double v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    if ((threadIdx.x & 31u) == 0 && v != 0.0) atomicAdd(out + k, v);
+  }
+}
+
+}  // namespace vlt
+
+extern "C" vlt_status vlt_image_stats(const void* a, int a_type, const void* b, int b_type, uint32_t n, double* out,
+                                      void* stream) {
+  if (!a || !out || a_type < 0 || a_type > 2 || (b && (b_type < 0 || b_type > 2))) return VLT_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  vlt_status st = vlt::cuda_status(cudaMemsetAsync(out, 0, 8 * sizeof(double), s));
+  if (st != VLT_OK || n == 0) return st;
+  uint32_t blocks = (n + 255) / 256;
+  uint32_t cap = 4u * (uint32_t)vlt::device_sm_count();
+  vlt::k_image_stats<<<blocks < cap ? blocks : cap, 256, 0, s>>>(a, a_type, b, b_type, n, out);
   return vlt::cuda_status(cudaGetLastError());
 }

@@ -68,19 +68,23 @@ __device__ __forceinline__ void store_rec(float4* __restrict__ p, size_t i, f3 d
   p[2 * i + 1] = make_float4(s.x, s.y, s.z, aux.y);
 }
 
-// f16 form: one uint4 per pixel = 8 halves {d.rgb, aux.x, s.rgb, aux.y}; stores
-// saturate (f32tof16_sat).
+// f16 form: one uint4 per pixel = 8 halves {d.rgb, sqrt(aux.x), s.rgb, sqrt(aux.y)};
+// stores saturate (f32tof16_sat). The second moments and variances (aux >= 0) are
+// stored as their square roots: luminance^2 of bright pixels exceeds the f16 range
+// (~7e6 for a x100 firefly), the root keeps the radiance's range.
 __device__ __forceinline__ Rec load_rec(const uint4* __restrict__ p, size_t i) {
   uint4 v = p[i];
   Rec r;
   r.d = mk3(f16tof32(v.x & 0xFFFFu), f16tof32(v.x >> 16), f16tof32(v.y & 0xFFFFu));
   r.s = mk3(f16tof32(v.z & 0xFFFFu), f16tof32(v.z >> 16), f16tof32(v.w & 0xFFFFu));
-  r.aux = mk2(f16tof32(v.y >> 16), f16tof32(v.w >> 16));
+  float ax = f16tof32(v.y >> 16), ay = f16tof32(v.w >> 16);
+  r.aux = mk2(ax * ax, ay * ay);
   return r;
 }
 __device__ __forceinline__ void store_rec(uint4* __restrict__ p, size_t i, f3 d, f3 s, f2 aux) {
-  p[i] = make_uint4(f32tof16_sat(d.x) | (f32tof16_sat(d.y) << 16), f32tof16_sat(d.z) | (f32tof16_sat(aux.x) << 16),
-                    f32tof16_sat(s.x) | (f32tof16_sat(s.y) << 16), f32tof16_sat(s.z) | (f32tof16_sat(aux.y) << 16));
+  uint32_t ax = f32tof16_sat(sqrt_(fmax_(aux.x, 0.0f))), ay = f32tof16_sat(sqrt_(fmax_(aux.y, 0.0f)));
+  p[i] = make_uint4(f32tof16_sat(d.x) | (f32tof16_sat(d.y) << 16), f32tof16_sat(d.z) | (ax << 16),
+                    f32tof16_sat(s.x) | (f32tof16_sat(s.y) << 16), f32tof16_sat(s.z) | (ay << 16));
 }
 __device__ __forceinline__ void copy_rec(float4* __restrict__ out, const float4* __restrict__ in, size_t i) {
   out[2 * i] = in[2 * i];
@@ -89,13 +93,11 @@ __device__ __forceinline__ void copy_rec(float4* __restrict__ out, const float4*
 __device__ __forceinline__ void copy_rec(uint4* __restrict__ out, const uint4* __restrict__ in, size_t i) {
   out[i] = in[i];
 }
-// History length: float (f32 form) or f16 (f16 form).
-__device__ __forceinline__ float ld_len(const float* __restrict__ p, size_t i) { return p[i]; }
-__device__ __forceinline__ float ld_len(const uint16_t* __restrict__ p, size_t i) { return f16tof32(p[i]); }
-__device__ __forceinline__ void st_len(float* __restrict__ p, size_t i, float v) { p[i] = v; }
-__device__ __forceinline__ void st_len(uint16_t* __restrict__ p, size_t i, float v) {
-  p[i] = (uint16_t)f32tof16_sat(v);
-}
+// History length: a frame count, stored as the reference does (R8_UNORM, k/255).
+// Unquantized, the fix/fallback tests `len < 4/255` would compare values a rounding
+// away from the threshold.
+__device__ __forceinline__ float ld_len(const uint8_t* __restrict__ p, size_t i) { return unorm8_load(p[i]); }
+__device__ __forceinline__ void st_len(uint8_t* __restrict__ p, size_t i, float v) { p[i] = (uint8_t)unorm8_store(v); }
 // Lighting inputs {rgb, w} and outputs {rgb, 0}: float4 or half4.
 __device__ __forceinline__ float4 ld_light(const float4* __restrict__ p, size_t i) { return p[i]; }
 __device__ __forceinline__ float4 ld_light(const uint2* __restrict__ p, size_t i) {
@@ -115,13 +117,13 @@ struct DnT;
 template <>
 struct DnT<FORM_F32> {
   using R = float4;
-  using N = float;
+  using N = uint8_t;
   using L = float4;
 };
 template <>
 struct DnT<FORM_F16> {
   using R = uint4;
-  using N = uint16_t;
+  using N = uint8_t;
   using L = uint2;
 };
 

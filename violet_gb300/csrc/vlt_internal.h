@@ -75,7 +75,8 @@ void launch_spec_spatial(const Exec& ex, int form, const vlt_frame_params& fp, i
 // denoise_f32.cu — the denoiser of the f32 and f16 storage forms (`form`). Records:
 // {diffuse.rgb, aux.x, specular.rgb, aux.y} as 2 float4 (f32) or 8 halves (f16),
 // aux = moments (temporal / fix outputs, history) or variance (fallback / a-trous);
-// history length float / half; lighting inputs and outputs float4 / half4.
+// f16 records hold sqrt(aux); history length R8_UNORM (both forms); lighting inputs
+// and outputs float4 / half4.
 void launch_dn32_temporal(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn,
                           const GeoArgs& ga, const GeoArgs& prev_ga, const void* diff_src, const void* spec_src,
                           const float* prev_depth, const void* hist, const void* len_hist, const void* fast_hist,
