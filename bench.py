@@ -26,6 +26,7 @@ CPU restatement is the stand-in). Under torchrun each rank runs an independent
 replica (the path does not shard within a view); rank 0 prints one JSON line.
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -395,6 +396,10 @@ def run_ours(args, ws, rank, local):
     if not args.no_batched:
         batched = batched_leg(args, ws, dev)
 
+    precision = None
+    if not args.no_precision:
+        precision = precision_leg(args, ws, dev)
+
     serving = None
     if not args.no_serving:
         serving = serving_leg(args, ws, dev)
@@ -425,6 +430,7 @@ def run_ours(args, ws, rank, local):
             "clocks": clk,
             "batched": batched,
             "serving": serving,
+            "precision": precision,
         }
         print(json.dumps(line), flush=True)
 
@@ -464,7 +470,7 @@ def batched_leg(args, ws, dev):
     sh = stream.cuda_stream
     total_px = sum(w * h for w, h, _ in specs)
     per_frame_in = sum(w * h * sum(c * 4 for _, c in vg.FRAME_BUFFERS.values()) for w, h, _ in specs)
-    state = sum(vg.View.device_bytes(w, h, FORM, params) for w, h, _ in specs)
+    state = sum(vg.View.device_bytes(w, h, "f32", params) for w, h, _ in specs)
     need = per_frame_in * frames_total + state + total_px * 64
     if need > 150e9:
         return {"skipped": "needs %.0f GB of HBM" % (need / 1e9)}
@@ -479,56 +485,62 @@ def batched_leg(args, ws, dev):
             fr.append(bufs)
         frames.append(fr)
     fps = [[scenes[k].frame_params(f) for k in range(len(specs))] for f in range(frames_total)]
-    out_px = 16 if FORM == "f32" else 4
-    outs = [{o: torch.empty(w * h * out_px, dtype=torch.uint8, device=dev) for o in ("diffuse", "specular")}
+    outs = [{o: torch.empty(w * h * 16, dtype=torch.uint8, device=dev) for o in ("diffuse", "specular")}
             for w, h, _ in specs]
-    views = [vg.View(ctx, w, h, FORM, params) for w, h, _ in specs]
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     steps = frames_total - warm
 
-    # plain: each view's frame through vlt_frame_run, view after view
-    for f in range(warm):
-        for k, v in enumerate(views):
-            v.run(fps[f][k], f, frames[f][k], outs[k], sh)
-    torch.cuda.synchronize()
-    barrier(ws)
-    e0.record(stream)
-    for f in range(warm, frames_total):
-        for k, v in enumerate(views):
-            v.run(fps[f][k], f, frames[f][k], outs[k], sh)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    plain_ms = max_over_ranks(e0.elapsed_time(e1), ws, dev)
+    def plain_arm(form):
+        """Each view's frame through vlt_frame_run, view after view."""
+        views = [vg.View(ctx, w, h, form, params) for w, h, _ in specs]
+        for f in range(warm):
+            for k, v in enumerate(views):
+                v.run(fps[f][k], f, frames[f][k], outs[k], sh)
+        torch.cuda.synchronize()
+        barrier(ws)
+        e0.record(stream)
+        for f in range(warm, frames_total):
+            for k, v in enumerate(views):
+                v.run(fps[f][k], f, frames[f][k], outs[k], sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = max_over_ranks(e0.elapsed_time(e1), ws, dev)
+        for v in views:
+            v.close()
+        return t
 
-    # tile-shape tuning on the same views (results do not depend on the shapes)
-    batch = vg.Batch(ctx)
-    for v in views:
-        v.reset(sh)
-    batch.autotune()
-    tune_frames = 2 * vg._ffi.TILE_CANDIDATES + 1
-    for f in range(tune_frames):
-        ff = f % frames_total
-        batch.run(views, fps[ff], [ff] * len(views), frames[ff], outs, stream=sh)
-    tiles = batch.tile_table()
+    def batched_arm(form):
+        """The same frames through vlt_batch_run, after tuning the launch shapes on
+        the same views (results do not depend on the shapes)."""
+        views = [vg.View(ctx, w, h, form, params) for w, h, _ in specs]
+        batch = vg.Batch(ctx)
+        batch.autotune()
+        for f in range(2 * vg._ffi.TILE_CANDIDATES + 1):
+            ff = f % frames_total
+            batch.run(views, fps[ff], [ff] * len(views), frames[ff], outs, stream=sh)
+        tiles = batch.tile_table()
+        for v in views:
+            v.reset(sh)
+        for f in range(warm):
+            batch.run(views, fps[f], [f] * len(views), frames[f], outs, stream=sh)
+        torch.cuda.synchronize()
+        st0 = batch.stats()
+        barrier(ws)
+        e0.record(stream)
+        for f in range(warm, frames_total):
+            batch.run(views, fps[f], [f] * len(views), frames[f], outs, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = max_over_ranks(e0.elapsed_time(e1), ws, dev)
+        st1 = batch.stats()
+        batch.close()
+        for v in views:
+            v.close()
+        return t, st0, st1, tiles
 
-    # batched: the same frames through vlt_batch_run
-    for v in views:
-        v.reset(sh)
-    for f in range(warm):
-        batch.run(views, fps[f], [f] * len(views), frames[f], outs, stream=sh)
-    torch.cuda.synchronize()
-    st0 = batch.stats()
-    barrier(ws)
-    e0.record(stream)
-    for f in range(warm, frames_total):
-        batch.run(views, fps[f], [f] * len(views), frames[f], outs, stream=sh)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    batch_ms = max_over_ranks(e0.elapsed_time(e1), ws, dev)
-    st1 = batch.stats()
-    batch.close()
-    for v in views:
-        v.close()
+    plain_ms = plain_arm("f32")
+    b32_ms, _, _, _ = batched_arm("f32")
+    batch_ms, st0, st1, tiles = batched_arm(args.batch_form)
     ctx.close()
     del frames
     torch.cuda.synchronize()
@@ -537,17 +549,112 @@ def batched_leg(args, ws, dev):
     return {
         "workload": "%d views, %d frames each, widths log-uniform 256..2560, aspect 16:9/4:3/1:1" % (
             len(specs), frames_total),
-        "storage": FORM, "views": len(specs), "frames": frames_total, "timed_steps": steps,
+        "storage": args.batch_form, "views": len(specs), "frames": frames_total, "timed_steps": steps,
         "mpix_per_step": total_px / 1e6,
         "value": px / (batch_ms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": batch_ms / steps,
         "plain_value": px / (plain_ms / 1e3) / 1e6, "plain_ms_per_step": plain_ms / steps,
+        "plain_storage": "f32",
         "speedup_vs_plain": plain_ms / batch_ms,
+        "batched_f32_value": px / (b32_ms / 1e3) / 1e6,
+        "speedup_batching_alone": plain_ms / b32_ms,
         "launches_per_step": st1["last_launches"], "view_passes_per_step": st1["last_jobs"],
         "graph_replays": st1["graph_replays"] - st0["graph_replays"],
         "graph_captures": st1["graph_captures"] - st0["graph_captures"],
         "arena_bytes": st1["arena_bytes"],
         "tiles": {k: list(v["tile"]) + (["persistent"] if v["persistent"] else []) for k, v in tiles.items()},
         "sizes": [[w, h] for w, h, _ in specs],
+    }
+
+
+def precision_leg(args, ws, dev):
+    """3840x2160, --precision-frames frames: device-resident throughput of the f16 and
+    f32 storage forms on the same frames, then both forms in lockstep with binary64
+    image reductions on the GPU between their denoised outputs (energy ratio and
+    relative L2 per frame; the latter includes resampling decisions that diverge
+    between differently stored reservoirs, so it bounds the divergence, not the
+    precision, which the binary64 denoiser test measures). Frame inputs: a ring of
+    16 consecutive frames walked forth and back (each frame's inputs are far larger
+    than L2)."""
+    import numpy as np
+    import torch
+
+    import violet_gb300 as vg
+
+    W, H = 3840, 2160
+    n = W * H
+    ring = 16
+    params = workload_params(vg)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+    sc = vg.Scene(4000, W, H, disocclusion_frac=0.02)
+    pool = []
+    for f in range(ring):
+        bufs = {b: torch.empty(n * c * 4, dtype=torch.uint8, device=dev) for b, (dt, c) in vg.FRAME_BUFFERS.items()}
+        sc.generate_device(f, bufs, sh)
+        pool.append((bufs, sc.frame_params(f)))
+
+    def ring_index(f):
+        k = f % (2 * ring - 2)
+        return k if k < ring else 2 * ring - 2 - k
+
+    ctx = vg.Context(dev.index)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    frames = args.precision_frames
+    warm = 3
+    res = {}
+    outs = {}
+    for form in ("f32", "f16"):
+        ob = 16 if form == "f32" else 8
+        outs[form] = {o: torch.empty(n * ob, dtype=torch.uint8, device=dev) for o in ("diffuse", "specular")}
+        v = vg.View(ctx, W, H, form, params)
+        for f in range(warm):
+            bufs, fp = pool[ring_index(f)]
+            v.run(fp, f, bufs, outs[form], sh)
+        torch.cuda.synchronize()
+        barrier(ws)
+        e0.record(stream)
+        for f in range(warm, frames):
+            bufs, fp = pool[ring_index(f)]
+            v.run(fp, f, bufs, outs[form], sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = max_over_ranks(e0.elapsed_time(e1), ws, dev)
+        res[form] = {"value": ws * n * (frames - warm) / (ms / 1e3) / 1e6, "unit": "Mpix/s",
+                     "ms_per_frame": ms / (frames - warm), "device_bytes": vg.View.device_bytes(W, H, form, params)}
+        v.close()
+    # lockstep comparison of the two forms' outputs
+    lib = vg.lib()
+    v32 = vg.View(ctx, W, H, "f32", params)
+    v16 = vg.View(ctx, W, H, "f16", params)
+    st = torch.zeros(8, dtype=torch.float64, device=dev)
+    energy, rel = {"diffuse": [], "specular": []}, {"diffuse": [], "specular": []}
+    for f in range(min(frames, 32)):
+        bufs, fp = pool[ring_index(f)]
+        v32.run(fp, f, bufs, outs["f32"], sh)
+        v16.run(fp, f, bufs, outs["f16"], sh)
+        if f < 1:
+            continue
+        for o in ("diffuse", "specular"):
+            lib.vlt_image_stats(ctypes.c_void_p(outs["f16"][o].data_ptr()), 1, ctypes.c_void_p(outs["f32"][o].data_ptr()),
+                                0, n, ctypes.c_void_p(st.data_ptr()), ctypes.c_void_p(sh))
+            stream.synchronize()
+            s = st.cpu().numpy()
+            energy[o].append(float(s[0:3].sum() / max(s[3:6].sum(), 1e-300)))
+            rel[o].append(float(np.sqrt(s[6] / max(s[7], 1e-300))))
+    v32.close()
+    v16.close()
+    ctx.close()
+    del pool
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return {
+        "workload": "3840x2160, %d frames (ring of %d consecutive frames walked forth and back), plain knobs" % (
+            frames, ring),
+        "f16": res["f16"], "f32": res["f32"], "f16_speedup": res["f16"]["value"] / res["f32"]["value"],
+        "f16_vs_f32_energy_ratio": {o: {"mean": float(np.mean(v)), "max_dev": float(np.max(np.abs(np.array(v) - 1)))}
+                                    for o, v in energy.items()},
+        "f16_vs_f32_rel_l2": {o: {"mean": float(np.mean(v)), "max": float(np.max(v))} for o, v in rel.items()},
+        "reductions": "binary64 on the GPU (vlt_image_stats)",
     }
 
 
@@ -596,7 +703,8 @@ def serving_leg(args, ws, dev):
         k = int(rng.choice(len(SERVE_CLASSES), p=[c[3] for c in SERVE_CLASSES]))
         classes.append(k)
         lengths.append(int(rng.integers(30, 301)))
-    out_px = 16 if FORM == "f32" else 4
+    form = args.serve_form
+    out_px = {"ref": 4, "f32": 16, "f16": 8}[form]
     live = {}  # session id -> state
     lat_all, lat_cls = [], {c[0]: [] for c in SERVE_CLASSES}
     frames_done = 0
@@ -609,7 +717,7 @@ def serving_leg(args, ws, dev):
         now = time.perf_counter() - t0
         while nxt < len(t_arr) and t_arr[nxt] <= now:
             name, w, h, _ = SERVE_CLASSES[classes[nxt]]
-            sid = server.open(w, h, FORM, params)
+            sid = server.open(w, h, form, params)
             live[sid] = {"cls": name, "w": w, "h": h, "n": lengths[nxt], "sent": 0, "done": 0,
                          "out": {o: torch.empty(w * h * out_px, dtype=torch.uint8, device=dev)
                                  for o in ("diffuse", "specular")}}
@@ -655,7 +763,7 @@ def serving_leg(args, ws, dev):
         "workload": "Poisson %.0f sessions/s for %.0f s; 720p/1080p/1440p/2160p with p=0.3/0.4/0.2/0.1; 30-300 "
                     "frames each; HBM budget %.0f GB; step pixel budget %.1f Mpix" % (
                         args.serve_rate, args.serve_seconds, args.serve_hbm_gb, args.serve_step_mpix),
-        "storage": FORM, "sessions_arrived": len(t_arr), "sessions_admitted": stats["sessions_admitted"],
+        "storage": form, "sessions_arrived": len(t_arr), "sessions_admitted": stats["sessions_admitted"],
         "sessions_completed": stats["sessions_closed"], "sessions_waiting_at_end": stats["sessions_waiting"],
         "frames": frames_done, "steps": steps, "frames_per_step": frames_done / max(steps, 1),
         "value": pix_done / elapsed / 1e6, "unit": "Mpix/s", "seconds": elapsed,
@@ -684,6 +792,10 @@ def main():
     ap.add_argument("--serve-step-mpix", type=float, default=6.0)
     ap.add_argument("--batch-views", type=int, default=48)
     ap.add_argument("--batch-frames", type=int, default=32)
+    ap.add_argument("--batch-form", default="f16", choices=["ref", "f32", "f16"])
+    ap.add_argument("--serve-form", default="f32", choices=["ref", "f32", "f16"])
+    ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--precision-frames", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 steps")
