@@ -107,6 +107,10 @@ typedef struct vlt_params {
   uint32_t hg_log2_buckets;       /* hash_grid.inc.hlsl:9 (16); 16 cells per bucket */
   uint32_t hg_key_mode;           /* 0: position + LOD key; 1: also the normal octant */
   uint32_t hg_max_queries;        /* HASH_GRID_MAX_NUM_QUERIES (131072); 0: W*H */
+  uint32_t post;                  /* passes after the denoiser: 0 none; 1 final lighting
+                                     (restir_renderer.rs:897-915); 2 also temporal AA
+                                     (RestirConfig::taa, :920-948). The reference
+                                     renderer runs 2; both presets give 0. */
 } vlt_params;
 
 void vlt_params_reference(vlt_params* out);
@@ -150,6 +154,9 @@ typedef struct vlt_frame_inputs {
   const float* diff_source_pdf;       /* optional (used when params.use_input_pdf) */
   const float* spec_hit_pos;          /* float4 per pixel (xyz, w unused) */
   const uint32_t* spec_hit_radiance;  /* R11G11B10 */
+  const uint8_t* shadow_mask;         /* optional: R8_UNORM sun visibility for the final
+                                         lighting (restir_renderer.rs:832-848); NULL:
+                                         unshadowed */
 } vlt_frame_inputs;
 
 /* Output element type follows the view's form: REF -> u32 R11G11B10 per pixel,
@@ -159,6 +166,11 @@ typedef struct vlt_frame_outputs {
   void* specular;       /* denoised indirect specular (demodulated) */
   void* raw_diffuse;    /* spatial-resampling output before the denoiser */
   void* raw_specular;
+  void* color;          /* final lighting (params.post >= 1), read-write: pixels without
+                           geometry keep the caller's values (the reference's sky
+                           pass writes them); NULL: a buffer of the view (zeros there) */
+  void* taa;            /* the temporal-AA result (params.post == 2); the view keeps
+                           it as next frame's history either way */
 } vlt_frame_outputs;
 
 /* Runs one frame in the pass order of RestirRenderer::add_passes and
@@ -294,7 +306,8 @@ uint32_t vlt_view_read_timing(vlt_view* view, vlt_pass_time* out, uint32_t max);
  * name: "diff_reservoir", "spec_hit_pos", "spec_reservoir", "spec_radiance",
  * "ao_history", "hist_color", "hist_moments", "hist_len", "hg_storage", "hg_decay",
  * "hg_queries", "hg_query_count", "prev_depth", "prev_gbuffer", "variance",
- * "spec_ray_len". Returns NULL for an unknown name. */
+ * "spec_ray_len", "color" (the view's final-lighting buffer), "taa_history".
+ * Returns NULL for an unknown name. */
 void* vlt_view_buffer(vlt_view* view, const char* name, size_t* bytes);
 
 /* --------------------------------------------- per-pass entry points (REF form) */
@@ -392,6 +405,21 @@ vlt_status vlt_denoise_atrous(uint32_t width, uint32_t height, const float* dept
                               const uint32_t* gbuffer_texture, const uint32_t* color,
                               const uint16_t* variance, uint32_t* rw_color, uint16_t* rw_variance,
                               int32_t step_size, void* stream);
+
+/* restir/final_lighting.hlsl; node "Combined Lighting" (restir_renderer.rs:897-915).
+ * gbuffer: 4 layer planes; shadow_mask: R8_UNORM (NULL: unshadowed); indirect
+ * diffuse / specular and rw_color: R11G11B10. Pixels without geometry are not
+ * written. */
+vlt_status vlt_final_lighting(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                              const uint32_t* gbuffer_color, const uint8_t* shadow_mask_buffer,
+                              const uint32_t* indirect_diffuse_texture, const uint32_t* indirect_specular_texture,
+                              uint32_t* rw_color_buffer, void* stream);
+
+/* temporal_aa.hlsl; node "Temporal AA" (restir_renderer.rs:920-948). source, history
+ * and rw_target: R11G11B10. Push constant: has_history (history may be NULL when 0). */
+vlt_status vlt_temporal_aa(const vlt_frame_params* fp, uint32_t width, uint32_t height, const float* gbuffer_depth,
+                           const uint32_t* source_texture, const uint32_t* history_texture, uint32_t has_history,
+                           uint32_t* rw_target, void* stream);
 
 /* Hash-grid radiance cache. Cell storage: 16 bytes per cell {checksum, radiance f32x3}
  * (HashGridCell, hash_grid.inc.hlsl:112-122); decay: u8 per cell; query record: 32

@@ -36,6 +36,7 @@ typedef struct vlt_scene_frame {
   float* diff_source_pdf;
   float* spec_hit_pos;           /* 4 floats per pixel */
   uint32_t* spec_hit_radiance;
+  uint8_t* shadow_mask;          /* optional: R8_UNORM direct-light visibility */
 } vlt_scene_frame;
 
 void vlt_scene_desc_default(vlt_scene_desc* d, uint64_t seed, uint32_t width, uint32_t height);

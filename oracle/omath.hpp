@@ -385,6 +385,12 @@ inline float smith_G2_over_G1_height_correlated_GGX(float NoL, float NoV, float 
   float k_L = sqrtf((-r2 * NoL + NoL) * NoL + r2) / NoL;
   return (1.0f + k_V) / (k_V + k_L);
 }
+inline float vis_smith_G2_height_correlated_GGX(float NoL, float NoV, float roughness) {  // brdf.hlsl:99-113
+  float r2 = roughness * roughness;
+  float u_L = NoV * sqrtf((-r2 * NoL + NoL) * NoL + r2);
+  float u_V = NoL * sqrtf((-r2 * NoV + NoV) * NoV + r2);
+  return 0.5f / (u_L + u_V);
+}
 inline float3 get_specular_f0(float3 base, float metallic) { return lerp(F3(0.04f), base, metallic); }
 inline float3 ggx_brdf_integral_approx(float n_dot_v, float roughness, float3 specular_f0) {
   const float m0[2][2] = {{0.99044f, -1.28514f}, {1.29678f, -0.755907f}};

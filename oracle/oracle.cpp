@@ -2122,6 +2122,179 @@ void hg_find(const vlt_frame_params& fp, uint32_t log2_buckets, uint32_t key_mod
 }
 
 // ===================================================== per-view driver
+// ==================================================== final lighting and TAA
+// Colour images: R11G11B10 (form 0, the reference's B10G11R11_UFLOAT scene colour),
+// float4 {rgb, 0} (form 1), half4 {rgb, 0} stored with saturation (form 2).
+template <int FORM>
+float3 color_load(const void* p, size_t i) {
+  if constexpr (FORM == 1) {
+    const float* q = (const float*)p + 4 * i;
+    return F3(q[0], q[1], q[2]);
+  } else if constexpr (FORM == 2) {
+    const uint16_t* q = (const uint16_t*)p + 4 * i;
+    return F3(f16tof32(q[0]), f16tof32(q[1]), f16tof32(q[2]));
+  } else {
+    return load_r11g11b10(((const uint32_t*)p)[i]);
+  }
+}
+template <int FORM>
+void color_store(void* p, size_t i, float3 v) {
+  if constexpr (FORM == 1) {
+    float* q = (float*)p + 4 * i;
+    q[0] = v.x, q[1] = v.y, q[2] = v.z, q[3] = 0.0f;
+  } else if constexpr (FORM == 2) {
+    uint16_t* q = (uint16_t*)p + 4 * i;
+    q[0] = (uint16_t)f16sat_d(v.x), q[1] = (uint16_t)f16sat_d(v.y), q[2] = (uint16_t)f16sat_d(v.z), q[3] = 0;
+  } else {
+    ((uint32_t*)p)[i] = store_r11g11b10(v);
+  }
+}
+
+// eval_GGX_Lambertian (brdf.hlsl:154-177).
+float3 eval_GGX_Lambertian(float3 v, float3 l, float3 n, float perceptual_roughness, float3 diffuse_rho,
+                           float3 specular_f0) {
+  float3 hv = normalize(v + l);
+  float NoL = saturate(dot(n, l));
+  float NoV = saturate(dot(n, v));
+  float NoH = saturate(dot(n, hv));
+  float LoH = saturate(dot(l, hv));
+  float roughness = perceptual_roughness * perceptual_roughness;
+  float D = D_GGX(NoH, roughness);
+  float3 F = F_Schlick(LoH, specular_f0);
+  float V = vis_smith_G2_height_correlated_GGX(NoL, NoV, roughness);
+  float3 Fr = hmin(D * V, 1e19f) * F;  // F32_SIGNIFICANTLY_LARGE
+  float3 Fd = diffuse_rho * ONE_OVER_PI;
+  return Fd + Fr;
+}
+
+// restir/final_lighting.hlsl:16-62. The indirect colours are element i * stride of
+// `diff` / `spec` (stride 2: the colour halves of the denoiser's records).
+template <int FORM>
+void final_lighting(const vlt_frame_params& fp, int w, int h, const uint32_t* gbuf, const uint8_t* shadow,
+                    const void* diff, const void* spec, int stride, void* out) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y) {
+    for (int x = 0; x < w; ++x) {
+      const size_t i = (size_t)y * w + x;
+      GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
+      if (gbuffer.shading_path == 0) continue;  // has_no_geometry: written by the sky pass
+      float direct_atten = shadow ? load_unorm8(shadow[i]) : 1.0f;
+      // -cs_view_ray_direction(dispatch_id, buffer_size, 0) (frame_bindings.hlsl:71-79)
+      float2 pix = F2((float)x + 0.5f, (float)y + 0.5f);
+      pix = pix + F2(lerp(-0.5f, 0.5f, 0.0f), lerp(-0.5f, 0.5f, 0.0f));
+      float2 ndc = F2(pix.x / (float)w * 2.0f - 1.0f, pix.y / (float)h * 2.0f - 1.0f);
+      float4 e = mul(fp.inv_view_proj, F4(ndc.x, ndc.y, 1.0f, 1.0f));
+      float3 end = F3(e.x / e.w, e.y / e.w, e.z / e.w);
+      float3 view_dir = -normalize(end - F3(fp.view_pos[0], fp.view_pos[1], fp.view_pos[2]));
+      float perceptual_roughness = hmax(gbuffer.perceptual_roughness, 0.045f);
+      float3 diffuse_rho = gbuffer.color * (1.0f - gbuffer.metallic);
+      float3 specular_f0 = get_specular_f0(gbuffer.color, gbuffer.metallic);
+      float3 sun_dir = F3(fp.sun_dir[0], fp.sun_dir[1], fp.sun_dir[2]);
+      float NoL = saturate(dot(gbuffer.normal, sun_dir));
+      float3 direct = eval_GGX_Lambertian(view_dir, sun_dir, gbuffer.normal, perceptual_roughness, diffuse_rho,
+                                          specular_f0) *
+                      (NoL * direct_atten) * F3(fp.sun_inten[0], fp.sun_inten[1], fp.sun_inten[2]);
+      float NoV = saturate(dot(gbuffer.normal, view_dir));
+      float roughness = gbuffer.perceptual_roughness * gbuffer.perceptual_roughness;
+      roughness = hmax(roughness, 0.002f);  // IND_SPEC_R_MIN
+      float3 specular_reflectance = hmax(ggx_brdf_integral_approx(NoV, roughness, specular_f0), 1.0f / 65536.0f);
+      float3 indirect = color_load<FORM>(diff, i * stride) * diffuse_rho +
+                        color_load<FORM>(spec, i * stride) * specular_reflectance;
+      color_store<FORM>(out, i, direct + indirect);
+    }
+  }
+}
+
+// temporal_aa.hlsl `mitchell` (B = C = 1/3).
+inline float mitchell(float x) {
+  const float B = 1 / 3.0f, C = 1 / 3.0f;
+  float y = 0.0f;
+  float x2 = x * x;
+  float x3 = x * x * x;
+  if (x < 1)
+    y = (12 - 9 * B - 6 * C) * x3 + (-18 + 12 * B + 6 * C) * x2 + (6 - 2 * B);
+  else if (x <= 2)
+    y = (-B - 6 * C) * x3 + (6 * B + 30 * C) * x2 + (-12 * B - 48 * C) * x + (8 * B + 24 * C);
+  return y / 6.0f;
+}
+// temporal_aa.hlsl `clip_aabb`.
+inline float3 clip_aabb(float3 aabb_center, float3 aabb_half_extent, float3 q) {
+  const float FLT_EPS = 0.00000001f;
+  float3 p_clip = aabb_center;
+  float3 e_clip = aabb_half_extent + F3(FLT_EPS);
+  float3 v_clip = q - p_clip;
+  float3 v_unit = v_clip / e_clip;
+  float3 a_unit = abs3(v_unit);
+  float ma_unit = hmax(a_unit.x, hmax(a_unit.y, a_unit.z));
+  if (ma_unit > 1.0f) return p_clip + v_clip / ma_unit;
+  return q;
+}
+
+// temporal_aa.hlsl `main`. The closest-depth search of the reference's neighbourhood
+// loop feeds nothing (its position is overwritten by the centre pixel's), so it is
+// left out.
+template <int FORM>
+void temporal_aa(const vlt_frame_params& fp, int w, int h, const float* depth, const void* source,
+                 const void* history, uint32_t has_history, void* target) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y) {
+    for (int x = 0; x < w; ++x) {
+      float2 sample_offset_pix = F2(-fp.jitter[0] * 0.5f * (float)w, -fp.jitter[1] * 0.5f * (float)h);
+      float3 neighbor_accu = F3(0.0f), nmin = F3(1e5f), nmax = F3(-1e5f), m1 = F3(0.0f), m2 = F3(0.0f);
+      float neighbor_weight_accu = 0.0f;
+      for (int dx = -1; dx <= 1; dx++) {
+        for (int dy = -1; dy <= 1; dy++) {
+          int px = std::min(std::max(x + dx, 0), w - 1);
+          int py = std::min(std::max(y + dy, 0), h - 1);
+          float2 subsample_offset = F2((float)(px - x), (float)(py - y)) + sample_offset_pix;
+          float3 nb = color_load<FORM>(source, (size_t)py * w + px);
+          float subsample_weight = mitchell(length(subsample_offset));
+          neighbor_accu += nb * subsample_weight;
+          neighbor_weight_accu += subsample_weight;
+          nmin = F3(hmin(nmin.x, nb.x), hmin(nmin.y, nb.y), hmin(nmin.z, nb.z));
+          nmax = F3(hmax(nmax.x, nb.x), hmax(nmax.y, nb.y), hmax(nmax.z, nb.z));
+          m1 += nb;
+          m2 += nb * nb;
+        }
+      }
+      float3 src = neighbor_accu / neighbor_weight_accu;
+      const size_t i = (size_t)y * w + x;
+      float3 position = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth[i]);
+      float4 hpos = mul(fp.view_proj, F4(position.x, position.y, position.z, 1.0f));
+      float2 ndc = F2(hpos.x / hpos.w - fp.jitter[0], hpos.y / hpos.w - fp.jitter[1]);
+      float4 hr = mul(fp.prev_view_proj, F4(position.x, position.y, position.z, 1.0f));
+      float2 ndc_reproj = F2(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3]);
+      float2 motion_vector = (ndc - ndc_reproj) * 0.5f;
+      float2 src_uv = F2(((float)x + 0.5f) / (float)w, ((float)y + 0.5f) / (float)h);
+      float2 history_uv = src_uv - motion_vector;
+      bool not_in_last_view = history_uv.x != saturate(history_uv.x) || history_uv.y != saturate(history_uv.y);
+      if (not_in_last_view || !has_history) {
+        color_store<FORM>(target, i, src);
+        continue;
+      }
+      Bilinear b = bilinear(history_uv, w, h);
+      float3 hist = blerp(color_load<FORM>(history, (size_t)b.y0 * w + b.x0),
+                          color_load<FORM>(history, (size_t)b.y0 * w + b.x1),
+                          color_load<FORM>(history, (size_t)b.y1 * w + b.x0),
+                          color_load<FORM>(history, (size_t)b.y1 * w + b.x1), b.fx, b.fy);
+      hist = hclamp(hist, nmin, nmax);
+      const float ONE_OVER_SAMPLE_COUNT = 1.0f / 9.0f;
+      float3 m1_u = m1 * ONE_OVER_SAMPLE_COUNT;
+      float3 m2_u = m2 * ONE_OVER_SAMPLE_COUNT;
+      float3 sigma = sqrt3(abs3(m2_u - m1_u * m1_u));
+      hist = clip_aabb(m1_u, sigma * 1.0f, hist);
+      float src_weight = 1.0f / 32.0f;
+      float hist_weight = 1.0f - 1.0f / 32.0f;
+      float3 src_c = src * rcp(hmax(hmax(src.x, src.y), src.z) + 1.0f);
+      float3 hist_c = hist * rcp(hmax(hmax(hist.x, hist.y), hist.z) + 1.0f);
+      src_weight *= rcp(1.0f + luminance(src_c));
+      hist_weight *= rcp(1.0f + luminance(hist_c));
+      float3 result = (src * src_weight + hist * hist_weight) / hmax(src_weight + hist_weight, 1e-5f);
+      color_store<FORM>(target, i, result);
+    }
+  }
+}
+
 struct OView {
   int w, h;
   vlt_params P;
@@ -2146,6 +2319,10 @@ struct OView {
   int form = 0;
   std::vector<uint8_t> fdiff_prev, fao_prev, fao_filtered, fdiff_light, fspec_light, fhist_rec, fhist_len, ffast_prev,
       ffallback;
+  // Final lighting (the view's colour buffer) and the temporal-AA history
+  // (RestirRenderer::prev_color), in the form's colour element.
+  std::vector<uint8_t> lit, taa_hist;
+  bool taa_valid = false;
 };
 
 struct FrameRand {
@@ -2290,6 +2467,9 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
   const size_t light_bytes = (v.form == 1 ? 16 : (v.form == 2 ? 8 : 4)) * n;
   const void* diff_light = ff ? (const void*)v.fdiff_light.data() : (const void*)v.diff_light.data();
   const void* spec_light = ff ? (const void*)v.fspec_light.data() : (const void*)v.spec_light.data();
+  // The denoiser's last {diffuse, specular} records, read in place by the final lighting.
+  std::vector<uint8_t> den_rec;
+  std::vector<uint32_t> den_color;
   if (P.denoise && has_prev && ff) {
     const bool f32 = v.form == 1;
     const size_t rb = f32 ? 32 : 16;  // bytes per record
@@ -2336,6 +2516,7 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
         if (out->specular) memcpy((uint8_t*)out->specular + half * i, a.data() + rb * i + half, half);
       }
     }
+    den_rec.swap(a);
   } else if (P.denoise && has_prev) {
     std::vector<uint32_t> tcolor(2 * n), tmom(n), tfast(P.fast_history_clamp ? 2 * n : 2);
     std::vector<uint8_t> tlen(n);
@@ -2376,6 +2557,7 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
         if (out->specular) ((uint32_t*)out->specular)[i] = color[2 * i + 1];
       }
     }
+    den_color.swap(color);
   } else {
     v.denoiser_history = false;
     if (out && out->diffuse) memcpy(out->diffuse, diff_light, light_bytes);
@@ -2383,6 +2565,31 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
   }
   if (out && out->raw_diffuse) memcpy(out->raw_diffuse, diff_light, light_bytes);
   if (out && out->raw_specular) memcpy(out->raw_specular, spec_light, light_bytes);
+
+  // Final lighting (restir_renderer.rs:897-915) and temporal AA (:920-948).
+  if (P.post >= 1) {
+    const size_t cb = light_bytes / n;
+    const uint8_t* den = !den_rec.empty() ? den_rec.data()
+                         : !den_color.empty() ? (const uint8_t*)den_color.data()
+                                              : nullptr;
+    const void* dsrc = den ? (const void*)den : diff_light;
+    const void* ssrc = den ? (const void*)(den + cb) : spec_light;
+    const int stride = den ? 2 : 1;
+    void* color = out && out->color ? out->color : (void*)v.lit.data();
+    if (v.form == 1) final_lighting<1>(fp, w, h, in.gbuffer, in.shadow_mask, dsrc, ssrc, stride, color);
+    else if (v.form == 2) final_lighting<2>(fp, w, h, in.gbuffer, in.shadow_mask, dsrc, ssrc, stride, color);
+    else final_lighting<0>(fp, w, h, in.gbuffer, in.shadow_mask, dsrc, ssrc, stride, color);
+    if (P.post >= 2) {
+      std::vector<uint8_t> cur(cb * n);
+      const uint32_t hh = v.taa_valid ? 1u : 0u;
+      if (v.form == 1) temporal_aa<1>(fp, w, h, in.depth, color, v.taa_hist.data(), hh, cur.data());
+      else if (v.form == 2) temporal_aa<2>(fp, w, h, in.depth, color, v.taa_hist.data(), hh, cur.data());
+      else temporal_aa<0>(fp, w, h, in.depth, color, v.taa_hist.data(), hh, cur.data());
+      v.taa_hist.swap(cur);
+      v.taa_valid = true;
+      if (out && out->taa) memcpy(out->taa, v.taa_hist.data(), cb * n);
+    }
+  }
   memcpy(v.prev_depth.data(), in.depth, 4 * n);
   memcpy(v.prev_gbuf.data(), in.gbuffer, 16 * n);
   v.frames += 1;
@@ -2436,6 +2643,9 @@ void* vlto_view_create_form(uint32_t w, uint32_t h, const vlt_params* p, int for
     v->ffallback.assign(by(32, 16), 0);
     if (form == 2) v->spec_hp_prev.assign(6 * n, 0.0f);
   }
+  const size_t cb = form == 1 ? 16 : (form == 2 ? 8 : 4);
+  if (p->post >= 1) v->lit.assign(cb * n, 0);
+  if (p->post >= 2) v->taa_hist.assign(cb * n, 0);
   if (p->hg_enable) {
     size_t nc = (size_t)16 << v->log2_buckets;
     v->hg_storage.assign(4 * nc, 0);
@@ -2518,6 +2728,14 @@ void* vlto_view_buffer(void* h, const char* name, size_t* bytes) {
       if (bytes) *bytes = e.sz;
       return e.p;
     }
+  if (strcmp(name, "color") == 0 && !v.lit.empty()) {
+    if (bytes) *bytes = v.lit.size();
+    return v.lit.data();
+  }
+  if (strcmp(name, "taa_history") == 0 && v.taa_valid) {
+    if (bytes) *bytes = v.taa_hist.size();
+    return v.taa_hist.data();
+  }
   return nullptr;
 }
 
@@ -2582,6 +2800,20 @@ void vlto_denoise_spatial_fallback(uint32_t w, uint32_t h, const float* depth, c
 void vlto_denoise_atrous(uint32_t w, uint32_t h, const float* depth, const uint32_t* gbuf, const uint32_t* color,
                          const uint32_t* var, uint32_t* out_color, uint32_t* out_var, int step) {
   dn_atrous((int)w, (int)h, depth, gbuf, color, var, out_color, out_var, nullptr, nullptr, step);
+}
+// Colour element per form: 0 R11G11B10, 1 float4, 2 half4.
+void vlto_final_lighting(int form, const vlt_frame_params* fp, uint32_t w, uint32_t h, const uint32_t* gbuf,
+                         const uint8_t* shadow, const void* diff, const void* spec, int stride, void* color) {
+  if (form == 1) final_lighting<1>(*fp, (int)w, (int)h, gbuf, shadow, diff, spec, stride, color);
+  else if (form == 2) final_lighting<2>(*fp, (int)w, (int)h, gbuf, shadow, diff, spec, stride, color);
+  else final_lighting<0>(*fp, (int)w, (int)h, gbuf, shadow, diff, spec, stride, color);
+}
+void vlto_temporal_aa(int form, const vlt_frame_params* fp, uint32_t w, uint32_t h, const float* depth,
+                      const void* source, const void* history, uint32_t has_history, void* target) {
+  const void* hist = has_history ? history : source;
+  if (form == 1) temporal_aa<1>(*fp, (int)w, (int)h, depth, source, hist, has_history, target);
+  else if (form == 2) temporal_aa<2>(*fp, (int)w, (int)h, depth, source, hist, has_history, target);
+  else temporal_aa<0>(*fp, (int)w, (int)h, depth, source, hist, has_history, target);
 }
 void vlto_hg_decay(uint32_t log2_buckets, uint8_t* decay, uint32_t* storage) { hg_decay(log2_buckets, decay, storage); }
 void vlto_hg_emit_queries(const vlt_frame_params* fp, uint32_t w, uint32_t h, uint32_t log2_buckets, uint32_t key_mode,

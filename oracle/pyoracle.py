@@ -43,6 +43,8 @@ SIGS = {
     "vlto_denoise_fast_history_clamp": (None, [U32, U32, P, P]),
     "vlto_denoise_spatial_fallback": (None, [U32, U32, P, P, P, P, P, P, P]),
     "vlto_denoise_atrous": (None, [U32, U32, P, P, P, P, P, P, C.c_int]),
+    "vlto_final_lighting": (None, [C.c_int, FP, U32, U32, P, P, P, P, C.c_int, P]),
+    "vlto_temporal_aa": (None, [C.c_int, FP, U32, U32, P, P, P, U32, P]),
     "vlto_hg_decay": (None, [U32, P, P]),
     "vlto_hg_emit_queries": (None, [FP, U32, U32, U32, U32, U32, P, P, P, P, P]),
     "vlto_hg_query_select": (None, [U32, U32, P, P, P, P, U32]),
@@ -119,10 +121,10 @@ class OracleView:
         fi.params = C.pointer(frame_params)
         fi.frame_index = int(frame_index) & 0xFFFFFFFF
         for k in ("depth", "gbuffer", "diff_hit_pos_normal", "diff_hit_radiance", "diff_source_pdf", "spec_hit_pos",
-                  "spec_hit_radiance"):
+                  "spec_hit_radiance", "shadow_mask"):
             setattr(fi, k, ptr(inputs.get(k)))
         fo = _ffi.FrameOutputs()
-        for k in ("diffuse", "specular", "raw_diffuse", "raw_specular"):
+        for k in ("diffuse", "specular", "raw_diffuse", "raw_specular", "color", "taa"):
             setattr(fo, k, ptr((outputs or {}).get(k)))
         lib().vlto_frame_run(self.handle, C.byref(fi), C.byref(fo))
 

@@ -16,7 +16,8 @@ from tests.helpers import d2h, upload
 pytestmark = pytest.mark.gpu
 
 BUFFERS = ["diff_reservoir", "spec_hit_pos", "spec_reservoir", "spec_radiance", "spec_record", "ao_history",
-           "ao_filtered", "raw_diffuse", "raw_specular", "hist_len", "hg_storage", "hg_decay", "hg_query_count"]
+           "ao_filtered", "raw_diffuse", "raw_specular", "hist_len", "hg_storage", "hg_decay", "hg_query_count",
+           "color", "taa_history"]
 REF_ONLY = ["hist_color", "hist_moments", "variance", "spec_ray_len"]
 F32_ONLY = ["hist_record", "fallback_record"]
 
@@ -27,16 +28,21 @@ def small_plain1():
     return p
 
 
+def with_post(p, post):
+    p.post = post
+    return p
+
+
 def view_specs():
     # (width, height, form, params, seed, first frame)
     return [
-        (96, 64, "ref", vg.params_reference(), 1, 0),
-        (160, 90, "f32", vg.params_plain(0), 2, 0),
+        (96, 64, "ref", with_post(vg.params_reference(), 2), 1, 0),
+        (160, 90, "f32", with_post(vg.params_plain(0), 1), 2, 0),
         (33, 17, "f32", vg.params_reference(), 3, 0),
         (128, 72, "ref", small_plain1(), 4, 0),
         (64, 64, "f32", small_plain1(), 5, 2),  # joins at frame 2
         (1, 1, "ref", vg.params_reference(), 6, 1),
-        (48, 40, "f16", vg.params_plain(0), 7, 0),
+        (48, 40, "f16", with_post(vg.params_plain(0), 2), 7, 0),
         (20, 12, "f16", vg.params_reference(), 8, 1),
     ]
 
@@ -87,8 +93,8 @@ def run_pair(frames, graphs=True, autotune=False, use_stream=True, chunk_pixels=
                 dev = upload(host)
                 fp = scenes[k].frame_params(lf)
                 n = w * h
-                oa = {o: torch.zeros(out_bytes(form, n), dtype=torch.uint8, device="cuda")
-                      for o in ("diffuse", "specular", "raw_diffuse", "raw_specular")}
+                names = ("diffuse", "specular", "raw_diffuse", "raw_specular") + ("color", "taa")[:p.post]
+                oa = {o: torch.zeros(out_bytes(form, n), dtype=torch.uint8, device="cuda") for o in names}
                 ob = {o: torch.zeros_like(t) for o, t in oa.items()}
                 torch.cuda.synchronize()
                 alone[k].run(fp, lf, dev, oa)

@@ -58,6 +58,7 @@ class Params(C.Structure):
         ("hg_log2_buckets", C.c_uint32),
         ("hg_key_mode", C.c_uint32),
         ("hg_max_queries", C.c_uint32),
+        ("post", C.c_uint32),
     ]
 
     def as_dict(self):
@@ -77,6 +78,7 @@ class FrameInputs(C.Structure):
         ("diff_source_pdf", C.c_void_p),
         ("spec_hit_pos", C.c_void_p),
         ("spec_hit_radiance", C.c_void_p),
+        ("shadow_mask", C.c_void_p),
     ]
 
 
@@ -86,6 +88,8 @@ class FrameOutputs(C.Structure):
         ("specular", C.c_void_p),
         ("raw_diffuse", C.c_void_p),
         ("raw_specular", C.c_void_p),
+        ("color", C.c_void_p),
+        ("taa", C.c_void_p),
     ]
 
 
@@ -143,6 +147,7 @@ class SceneFrame(C.Structure):
         ("diff_source_pdf", C.c_void_p),
         ("spec_hit_pos", C.c_void_p),
         ("spec_hit_radiance", C.c_void_p),
+        ("shadow_mask", C.c_void_p),
     ]
 
 
@@ -200,6 +205,8 @@ SIGNATURES = {
     "vlt_denoise_fast_history_clamp": (C.c_int, [U32, U32, P, P, P]),
     "vlt_denoise_spatial_fallback": (C.c_int, [U32, U32, P, P, P, P, P, P, P, P]),
     "vlt_denoise_atrous": (C.c_int, [U32, U32, P, P, P, P, P, P, I32, P]),
+    "vlt_final_lighting": (C.c_int, [FP, U32, U32, P, P, P, P, P, P]),
+    "vlt_temporal_aa": (C.c_int, [FP, U32, U32, P, P, P, U32, P, P]),
     "vlt_hg_decay": (C.c_int, [U32, P, P, P]),
     "vlt_hg_select_scratch_bytes": (C.c_size_t, [U32, U32]),
     "vlt_hg_query_select": (C.c_int, [U32, U32, P, P, P, P, U32, P, P]),

@@ -84,6 +84,8 @@ struct ViewBuffers {
   void* hg_scratch;
   float* prev_depth;
   float4* surf[2][3];      // per-frame surface planes {normal, depth}, {position, roughness}, {f0, fwidth_z}
+  void* lit;               // final lighting when the caller gives no colour buffer
+  void* taa[2];            // temporal-AA results: last frame's (history) and this frame's
 };
 
 }  // namespace
@@ -127,6 +129,8 @@ struct vlt_view {
   bool denoise_history;    // Denoiser::history is Some
   bool fast_history_valid; // Denoiser::fast_history is Some
   int diff_prev, spec_prev, ao_prev, hg_qcur, surf_cur;
+  int taa_cur;             // taa[taa_cur] holds the latest temporal-AA result
+  bool taa_valid;          // RestirRenderer::prev_color is Some
   uint32_t launches;
   Timing* timing;
 };
@@ -212,6 +216,10 @@ size_t layout(vlt_view* v, char* base) {
   b.prev_depth = (float*)take(4 * n);
   for (int k = 0; k < 2; ++k)
     for (int j = 0; j < 3; ++j) b.surf[k][j] = (float4*)take(16 * n);
+  // Colour images in the form's lighting element (R11G11B10 / float4 / half4).
+  if (v->p.post >= 1) b.lit = take(by(4, 16, 8) * n);
+  if (v->p.post >= 2)
+    for (int k = 0; k < 2; ++k) b.taa[k] = take(by(4, 16, 8) * n);
   return off;
 }
 
@@ -222,6 +230,7 @@ bool params_ok(const vlt_params* p) {
   if (p->hg_log2_buckets < 4 || p->hg_log2_buckets > 24) return false;
   if (p->hg_key_mode > 1) return false;
   if (!(p->history_max_frames >= 1.0f)) return false;
+  if (p->post > 2) return false;
   return true;
 }
 
@@ -255,6 +264,8 @@ vlt_status reset_state(vlt_view* v, cudaStream_t s) {
   v->ao_prev = 0;
   v->hg_qcur = 0;
   v->surf_cur = 0;
+  v->taa_cur = 0;
+  v->taa_valid = false;
   // Zero everything: cleared hash grid (restir_renderer.rs:296-306), empty queries.
   VLT_TRY(cudaMemsetAsync(v->pool.p, 0, v->pool.bytes, s));
   return VLT_OK;
@@ -272,6 +283,13 @@ bool frame_inputs_ok(const vlt_view* v, const vlt_frame_inputs* in) {
       !in->diff_hit_radiance || !in->spec_hit_pos || !in->spec_hit_radiance)
     return false;
   if (v->p.use_input_pdf && !in->diff_source_pdf) return false;
+  return true;
+}
+
+bool frame_outputs_ok(const vlt_view* v, const vlt_frame_outputs* out) {
+  if (!out) return true;
+  if (out->color && v->p.post < 1) return false;
+  if (out->taa && v->p.post < 2) return false;
   return true;
 }
 
@@ -522,6 +540,8 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
       {"hg_query_count", b.hg_qcount[v->hg_qcur], v->p.hg_enable ? (size_t)4 : (size_t)0},
       {"hg_selection", b.hg_sel, nc * 4},
       {"prev_depth", b.prev_depth, 4 * n},
+      {"color", b.lit, by(4, 16, 8) * n},
+      {"taa_history", v->taa_valid ? b.taa[v->taa_cur] : nullptr, by(4, 16, 8) * n},
   };
   for (const E& e : tab) {
     if (strcmp(e.nm, name) == 0) {
@@ -537,7 +557,7 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
 
 static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out,
                                  cudaStream_t s, Recorder* rec) {
-  if (!vlt::frame_inputs_ok(v, in)) return VLT_ERR_INVALID_ARG;
+  if (!vlt::frame_inputs_ok(v, in) || !vlt::frame_outputs_ok(v, out)) return VLT_ERR_INVALID_ARG;
   Exec ex;
   ex.stream = s;
   ex.rec = rec;
@@ -671,6 +691,9 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
 
   // Denoiser.
   const bool run_denoiser = P.denoise && has_prev;
+  // Where the final lighting reads the denoised colours: the last denoiser record
+  // (colour halves, element stride 2) or the raw lighting planes.
+  const void* den = nullptr;
   if (run_denoiser && (f32 || f16)) {
     DenoiseKnobs kn = {1.0f / P.history_max_frames, P.fast_history_clamp};
     uint32_t has_history = v->denoise_history ? 1u : 0u;
@@ -714,6 +737,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
       rsrc = rdst;
       rdst = rdst == b.rec[2] ? b.rec[3] : b.rec[2];
     }
+    den = rsrc;
     if (iters == 0 && out && (out->diffuse || out->specular)) {
       // Zero iterations: the fallback output is the result (copy its colours out).
       // The diffuse / specular half of each fallback record {rgb, aux}.
@@ -776,6 +800,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
       vsrc = vdst;
       vdst = vnext;
     }
+    den = csrc;
     if (iters == 0 && out && (out->diffuse || out->specular)) {
       launch_split_color(ex, w, h, csrc, (uint32_t*)out->diffuse, (uint32_t*)out->specular);
       ++launches;
@@ -792,6 +817,25 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     ex_copy(ex, out->raw_diffuse, b.diff_light, light_bytes);
   if (out && out->raw_specular)
     ex_copy(ex, out->raw_specular, b.spec_light, light_bytes);
+
+  // Final lighting (restir_renderer.rs:897-915) and temporal AA (:920-948).
+  if (P.post >= 1) {
+    const size_t cb = light_bytes / n;  // colour element bytes
+    const void* dsrc = den ? den : b.diff_light;
+    const void* ssrc = den ? (const void*)((const char*)den + cb) : b.spec_light;
+    void* color = out && out->color ? out->color : b.lit;
+    STAGE("final_lighting", launch_final_lighting(ex, form, fp, w, h, in->gbuffer, in->shadow_mask, dsrc, ssrc,
+                                                  den ? 2 : 1, color));
+    ++launches;
+    if (P.post >= 2) {
+      const int tc = v->taa_cur ^ 1;
+      STAGE("taa", launch_taa(ex, form, fp, w, h, in->depth, color, b.taa[v->taa_cur], b.taa[tc],
+                              out ? out->taa : nullptr, v->taa_valid ? 1u : 0u));
+      ++launches;
+      v->taa_cur = tc;
+      v->taa_valid = true;
+    }
+  }
 
   // Retain depth for the next frame unless the caller keeps it (the previous
   // frame's decoded G-buffer fields stay in the other surface slot).
@@ -848,6 +892,29 @@ vlt_status vlt_ao_filter(uint32_t width, uint32_t height, const float* depth_buf
                          uint16_t* rw_filtered_ao, void* stream) {
   if (!dims_ok(width, height) || !depth_buffer || !ao || !rw_filtered_ao) return VLT_ERR_INVALID_ARG;
   launch_ao_filter(stream_exec(stream), FORM_REF, width, height, depth_buffer, ao, rw_filtered_ao);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_final_lighting(const vlt_frame_params* fp, uint32_t width, uint32_t height,
+                              const uint32_t* gbuffer_color, const uint8_t* shadow_mask_buffer,
+                              const uint32_t* indirect_diffuse_texture, const uint32_t* indirect_specular_texture,
+                              uint32_t* rw_color_buffer, void* stream) {
+  if (!fp || !dims_ok(width, height) || !gbuffer_color || !indirect_diffuse_texture || !indirect_specular_texture ||
+      !rw_color_buffer)
+    return VLT_ERR_INVALID_ARG;
+  launch_final_lighting(stream_exec(stream), FORM_REF, *fp, width, height, gbuffer_color, shadow_mask_buffer,
+                        indirect_diffuse_texture, indirect_specular_texture, 1, rw_color_buffer);
+  return cuda_status(cudaGetLastError());
+}
+
+vlt_status vlt_temporal_aa(const vlt_frame_params* fp, uint32_t width, uint32_t height, const float* gbuffer_depth,
+                           const uint32_t* source_texture, const uint32_t* history_texture, uint32_t has_history,
+                           uint32_t* rw_target, void* stream) {
+  if (!fp || !dims_ok(width, height) || !gbuffer_depth || !source_texture || !rw_target ||
+      (has_history && !history_texture))
+    return VLT_ERR_INVALID_ARG;
+  launch_taa(stream_exec(stream), FORM_REF, *fp, width, height, gbuffer_depth, source_texture,
+             has_history ? history_texture : source_texture, rw_target, nullptr, has_history ? 1u : 0u);
   return cuda_status(cudaGetLastError());
 }
 

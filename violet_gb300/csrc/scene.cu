@@ -183,6 +183,7 @@ __host__ __device__ inline void store_pixel(const PixelOut& p, const vlt_scene_f
   if (f.diff_source_pdf) f.diff_source_pdf[i] = p.diff_pdf;
   for (int k = 0; k < 4; ++k) f.spec_hit_pos[4 * i + k] = p.spec_pos[k];
   f.spec_hit_radiance[i] = p.spec_rad;
+  if (f.shadow_mask) f.shadow_mask[i] = (uint8_t)p.shadow;
 }
 
 __global__ void k_scene_a(Object o, Desc d, vlt_frame_params fp, uint32_t frame, vlt_scene_frame f) {

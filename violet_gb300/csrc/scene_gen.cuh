@@ -288,6 +288,7 @@ struct PixelOut {
   float diff_pdf;
   float spec_pos[4];
   uint32_t spec_rad;
+  uint32_t shadow;  // R8_UNORM direct-light visibility (the ray-traced shadow mask's role)
 };
 
 VLT_HD uint32_t radiance_sample(Rng& r) {
@@ -319,8 +320,12 @@ VLT_HD PixelOut shade_pixel(const Object& o, const Desc& d, const float* view_pr
     out.diff_pdf = 0.0f;
     out.spec_pos[0] = out.spec_pos[1] = out.spec_pos[2] = out.spec_pos[3] = 0.0f;
     out.spec_rad = 0u;
+    out.shadow = 0u;
     return out;
   }
+  // Analytic shadow pattern over the surface with soft edges (stands in for the
+  // traced sun shadow).
+  out.shadow = unorm8_store((0.35f - sin_(0.9f * h.p.x) * sin_(0.7f * h.p.z)) * 5.0f);
   f4 clip = mul44(view_proj, mk4(h.p.x, h.p.y, h.p.z, 1.0f));
   out.depth = clip.z / clip.w;
   GBuffer g;

@@ -119,6 +119,12 @@ struct HashGridDims {
     return b;
   }
 };
+// post.cu: colours in the form's lighting element (R11G11B10 / float4 / half4).
+void launch_final_lighting(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const uint32_t* gbuf,
+                           const uint8_t* shadow, const void* diff, const void* spec, int stride, void* out);
+void launch_taa(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const float* depth,
+                const void* source, const void* history, void* out_hist, void* out_user, uint32_t has_history);
+
 size_t hg_select_scratch_bytes(const HashGridDims& d);
 void launch_hg_decay(const Exec& ex, const HashGridDims& d, uint8_t* decay, uint32_t* storage);
 void launch_hg_select(const Exec& ex, const HashGridDims& d, const uint32_t* queries, const uint32_t* count,
@@ -136,6 +142,7 @@ void launch_hg_find(const Exec& ex, const vlt_frame_params& fp, const HashGridDi
 
 // api.cu: frame recording for batched execution.
 bool frame_inputs_ok(const vlt_view* v, const vlt_frame_inputs* in);
+bool frame_outputs_ok(const vlt_view* v, const vlt_frame_outputs* out);
 // Runs the frame driver for `v` with every launch recorded into `rec` (the view's
 // host-side state advances as if the frame ran).
 vlt_status record_frame(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out, Recorder* rec);

@@ -20,6 +20,7 @@ FRAME_BUFFERS = {
     "diff_source_pdf": (np.float32, 1),
     "spec_hit_pos": (np.float32, 4),
     "spec_hit_radiance": (np.uint32, 1),
+    "shadow_mask": (np.uint8, 1),
 }
 
 
@@ -73,11 +74,11 @@ def _frame_structs(frame_params, frame_index, inputs, outputs):
     fi.params = C.pointer(frame_params)
     fi.frame_index = int(frame_index) & 0xFFFFFFFF
     for name in ("depth", "gbuffer", "prev_depth", "prev_gbuffer", "diff_hit_pos_normal", "diff_hit_radiance",
-                 "diff_source_pdf", "spec_hit_pos", "spec_hit_radiance"):
+                 "diff_source_pdf", "spec_hit_pos", "spec_hit_radiance", "shadow_mask"):
         setattr(fi, name, _ptr(inputs.get(name)))
     fo = _ffi.FrameOutputs()
     outputs = outputs or {}
-    for name in ("diffuse", "specular", "raw_diffuse", "raw_specular"):
+    for name in ("diffuse", "specular", "raw_diffuse", "raw_specular", "color", "taa"):
         setattr(fo, name, _ptr(outputs.get(name)))
     return fi, fo
 
