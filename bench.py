@@ -62,6 +62,10 @@ PASS_BYTES_PER_PIXEL_REF = {
     "dn_fallback": 1 + 8 + 4 + 8 + 4,
     "dn_fast_clamp": 8 + 8 + 8,
     "dn_atrous": 4 + 4 + 4 + 8 + 4 + 8 + 4,
+    # G-buffer layers 0, 1, 3 + R8 shadow + diffuse + specular + colour
+    "final_lighting": 12 + 1 + 4 + 4 + 4,
+    # depth + source + history (each read once) + next history
+    "taa": 4 + 4 + 4 + 4,
 }
 # FP32 form: float2 AO history, float filtered AO, 48-byte diffuse records, float4
 # lighting, 32-byte denoiser records {diffuse.rgb|aux, specular.rgb|aux}, float
@@ -77,6 +81,8 @@ PASS_BYTES_PER_PIXEL_F32 = dict(
     dn_fast_clamp=32 + 32 + 32,
     dn_fallback=4 + 32 + 32,
     dn_atrous=4 + 4 + 4 + 32 + 32,
+    final_lighting=12 + 1 + 16 + 16 + 16,
+    taa=4 + 16 + 16 + 16,
 )
 PASS_BYTES_PER_PIXEL = {"ref": PASS_BYTES_PER_PIXEL_REF, "f32": PASS_BYTES_PER_PIXEL_F32}
 FORM = "f32"
@@ -185,6 +191,23 @@ def workload_params(vg):
     return vg.params_plain(1)
 
 
+def input_bytes_per_pixel(vg, params):
+    import numpy as np
+
+    return sum(np.dtype(dt).itemsize * c for k, (dt, c) in vg.FRAME_BUFFERS.items()
+               if k != "shadow_mask" or params.post >= 1)
+
+
+def input_buffers(vg, params, w, h, dev):
+    """Device buffers for one frame's inputs (the shadow mask only when the final
+    lighting runs)."""
+    import numpy as np
+    import torch
+
+    return {k: torch.empty(w * h * c * np.dtype(dt).itemsize, dtype=torch.uint8, device=dev)
+            for k, (dt, c) in vg.FRAME_BUFFERS.items() if k != "shadow_mask" or params.post >= 1}
+
+
 def cpu_sample(width, height, frames, seed, threads=None):
     """Times the CPU oracle on `frames` frames of the workload; returns (Mpix/s of
     frames 1.., threads used)."""
@@ -270,7 +293,7 @@ def run_ours(args, ws, rank, local):
     # Distinct frames, generated on the device and kept resident in HBM.
     frames, fps = [], []
     for f in range(nframes):
-        bufs = {k: torch.empty(n * c * 4, dtype=torch.uint8, device=dev) for k, (dt, c) in vg.FRAME_BUFFERS.items()}
+        bufs = input_buffers(vg, params, W, H, dev)
         scene.generate_device(f, bufs, sh)
         frames.append(bufs)
         fps.append(scene.frame_params(f))
@@ -400,6 +423,10 @@ def run_ours(args, ws, rank, local):
     if not args.no_precision:
         precision = precision_leg(args, ws, dev)
 
+    post = None
+    if not args.no_post:
+        post = post_leg(args, ws, dev)
+
     serving = None
     if not args.no_serving:
         serving = serving_leg(args, ws, dev)
@@ -431,6 +458,7 @@ def run_ours(args, ws, rank, local):
             "batched": batched,
             "serving": serving,
             "precision": precision,
+            "post_passes": post,
         }
         print(json.dumps(line), flush=True)
 
@@ -469,7 +497,7 @@ def batched_leg(args, ws, dev):
     stream = torch.cuda.Stream(device=dev)
     sh = stream.cuda_stream
     total_px = sum(w * h for w, h, _ in specs)
-    per_frame_in = sum(w * h * sum(c * 4 for _, c in vg.FRAME_BUFFERS.values()) for w, h, _ in specs)
+    per_frame_in = sum(input_bytes_per_pixel(vg, params) * w * h for w, h, _ in specs)
     state = sum(vg.View.device_bytes(w, h, "f32", params) for w, h, _ in specs)
     need = per_frame_in * frames_total + state + total_px * 64
     if need > 150e9:
@@ -479,8 +507,7 @@ def batched_leg(args, ws, dev):
     for f in range(frames_total):
         fr = []
         for k, (w, h, seed) in enumerate(specs):
-            bufs = {b: torch.empty(w * h * c * 4, dtype=torch.uint8, device=dev) for b, (dt, c) in
-                    vg.FRAME_BUFFERS.items()}
+            bufs = input_buffers(vg, params, w, h, dev)
             scenes[k].generate_device(f, bufs, sh)
             fr.append(bufs)
         frames.append(fr)
@@ -589,7 +616,7 @@ def precision_leg(args, ws, dev):
     sc = vg.Scene(4000, W, H, disocclusion_frac=0.02)
     pool = []
     for f in range(ring):
-        bufs = {b: torch.empty(n * c * 4, dtype=torch.uint8, device=dev) for b, (dt, c) in vg.FRAME_BUFFERS.items()}
+        bufs = input_buffers(vg, params, W, H, dev)
         sc.generate_device(f, bufs, sh)
         pool.append((bufs, sc.frame_params(f)))
 
@@ -658,6 +685,63 @@ def precision_leg(args, ws, dev):
     }
 
 
+def post_leg(args, ws, dev):
+    """The frame with the passes the reference renderer runs after the denoiser
+    (final lighting and temporal AA, params.post = 2) on the headline workload:
+    device-resident Mpix/s of the whole frame and per-pass times."""
+    import torch
+
+    import violet_gb300 as vg
+
+    W, H = args.width, args.height
+    n = W * H
+    params = workload_params(vg)
+    params.post = 2
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    sc = vg.Scene(5000, W, H, disocclusion_frac=0.02)
+    nfr = args.warmup + args.steps
+    frames = []
+    for f in range(nfr):
+        bufs = input_buffers(vg, params, W, H, dev)
+        sc.generate_device(f, bufs, sh)
+        frames.append((bufs, sc.frame_params(f)))
+    ob = 16 if FORM == "f32" else 4
+    out = {o: torch.empty(n * ob, dtype=torch.uint8, device=dev) for o in ("diffuse", "specular", "taa")}
+    ctx = vg.Context(dev.index)
+    v = vg.View(ctx, W, H, FORM, params)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for f in range(args.warmup):
+        v.run(frames[f][1], f, frames[f][0], out, sh)
+    torch.cuda.synchronize()
+    barrier(ws)
+    e0.record(stream)
+    for f in range(args.warmup, nfr):
+        v.run(frames[f][1], f, frames[f][0], out, sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1), ws, dev)
+    v.reset(sh)
+    for f in range(args.warmup):
+        v.run(frames[f][1], f, frames[f][0], out, sh)
+    v.set_timing(True)
+    v.read_timing()
+    for f in range(args.warmup, nfr):
+        v.run(frames[f][1], f, frames[f][0], out, sh)
+    passes = v.read_timing()
+    v.close()
+    ctx.close()
+    del frames
+    res = {"workload": "%dx%d %s storage, plain knobs, post = 2 (final lighting + TAA)" % (W, H, FORM),
+           "value": ws * n * args.steps / (ms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_frame": ms / args.steps}
+    for k in ("final_lighting", "taa"):
+        if k in passes:
+            nl, tot = passes[k]
+            b = PASS_BYTES_PER_PIXEL[FORM][k] * n
+            res[k] = {"ms_per_frame": tot / nl, "alg_gbs": b * nl / (tot / 1e3) / 1e9}
+    return res
+
+
 SERVE_CLASSES = [("720p", 1280, 720, 0.3), ("1080p", 1920, 1080, 0.4), ("1440p", 2560, 1440, 0.2),
                  ("2160p", 3840, 2160, 0.1)]
 POOL_FRAMES = 16
@@ -684,8 +768,7 @@ def serving_leg(args, ws, dev):
         sc = vg.Scene(900 + w, w, h, disocclusion_frac=0.02)
         frames = []
         for f in range(POOL_FRAMES):
-            bufs = {b: torch.empty(w * h * c * 4, dtype=torch.uint8, device=dev) for b, (dt, c) in
-                    vg.FRAME_BUFFERS.items()}
+            bufs = input_buffers(vg, params, w, h, dev)
             sc.generate_device(f, bufs, sh)
             frames.append((bufs, sc.frame_params(f)))
         pools[name] = frames
@@ -795,6 +878,7 @@ def main():
     ap.add_argument("--batch-form", default="f16", choices=["ref", "f32", "f16"])
     ap.add_argument("--serve-form", default="f32", choices=["ref", "f32", "f16"])
     ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--no-post", action="store_true")
     ap.add_argument("--precision-frames", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:

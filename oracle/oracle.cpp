@@ -2848,6 +2848,8 @@ void vlto_math(int fn, const float* x, float* y, uint32_t n) {
       case 2: y[i] = log2_own(x[i]); break;
       case 3: y[i] = sin_own(x[i]); break;
       case 4: y[i] = cos_own(x[i]); break;
+      case 5:
+      case 6: y[i] = exp2_fma(x[i]); break;
       default: y[i] = 0.0f;
     }
   }

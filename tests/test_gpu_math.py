@@ -12,7 +12,15 @@ pytestmark = pytest.mark.gpu
 
 def _inputs(fn):
     rng = np.random.default_rng(1)
-    if fn in ("exp2", "exp"):
+    if fn in ("exp2_fma", "exp2_fma_full"):
+        # every 241st binary32 value of [-127, 1] (the short path's range and its edges)
+        lo, hi = np.float32(-127.0).view(np.uint32), np.float32(1.0).view(np.uint32)
+        neg = np.arange(0x80000000, lo + 1, 241, dtype=np.uint64).astype(np.uint32).view(np.float32)
+        pos = np.arange(0, hi + 1, 241, dtype=np.uint64).astype(np.uint32).view(np.float32)
+        x = np.concatenate([neg, pos, rng.uniform(-160, 130, 200000).astype(np.float32),
+                            np.array([0.0, -0.0, -126.0, -125.5, -126.5, 1e-45, -1e-45, 127.5, -150.5, np.inf,
+                                      -np.inf, np.nan], np.float32)])
+    elif fn in ("exp2", "exp"):
         x = np.concatenate([rng.uniform(-160, 130, 200000), rng.uniform(-2, 2, 200000),
                             [0.0, -0.0, 1.0, -1.0, 127.49, 127.5, 127.99, -126.0, -126.5, -149.5, -150.0, -151.0,
                              np.inf, -np.inf, np.nan]])
@@ -25,7 +33,7 @@ def _inputs(fn):
     return x.astype(np.float32)
 
 
-@pytest.mark.parametrize("fn", ["exp2", "exp", "log2", "sin", "cos"])
+@pytest.mark.parametrize("fn", ["exp2", "exp", "log2", "sin", "cos", "exp2_fma", "exp2_fma_full"])
 def test_own_math_bit_exact(fn):
     import torch
 
@@ -33,7 +41,7 @@ def test_own_math_bit_exact(fn):
     xd = torch.from_numpy(x).cuda()
     yd = torch.empty_like(xd)
     lib = vg.lib()
-    fid = {"exp2": 0, "exp": 1, "log2": 2, "sin": 3, "cos": 4}[fn]
+    fid = po.MATH[fn]
     rc = lib.vlt_diag_math(fid, C.c_void_p(xd.data_ptr()), C.c_void_p(yd.data_ptr()), x.size, None)
     assert rc == 0
     got = yd.cpu().numpy()

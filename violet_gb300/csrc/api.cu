@@ -692,8 +692,11 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   // Denoiser.
   const bool run_denoiser = P.denoise && has_prev;
   // Where the final lighting reads the denoised colours: the last denoiser record
-  // (colour halves, element stride 2) or the raw lighting planes.
+  // (colour halves, element stride 2) or the raw lighting planes. The last a-trous
+  // iteration writes no record when nothing reads it (both outputs given, no
+  // final lighting), and never the variance it would pass on.
   const void* den = nullptr;
+  const bool keep_den = P.post >= 1 || !out || !out->diffuse || !out->specular;
   if (run_denoiser && (f32 || f16)) {
     DenoiseKnobs kn = {1.0f / P.history_max_frames, P.fast_history_clamp};
     uint32_t has_history = v->denoise_history ? 1u : 0u;
@@ -732,12 +735,13 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
       bool last = k + 1 == iters;
       void* od = last && out ? out->diffuse : nullptr;
       void* os = last && out ? out->specular : nullptr;
-      STAGE("dn_atrous", launch_dn32_atrous(ex, form, w, h, ga, rsrc, rdst, od, os, 1 << k));
+      void* ro = last && !keep_den ? nullptr : (void*)rdst;
+      STAGE("dn_atrous", launch_dn32_atrous(ex, form, w, h, ga, rsrc, ro, od, os, 1 << k));
       ++launches;
       rsrc = rdst;
       rdst = rdst == b.rec[2] ? b.rec[3] : b.rec[2];
     }
-    den = rsrc;
+    den = keep_den ? (const void*)rsrc : nullptr;
     if (iters == 0 && out && (out->diffuse || out->specular)) {
       // Zero iterations: the fallback output is the result (copy its colours out).
       // The diffuse / specular half of each fallback record {rgb, aux}.
@@ -793,14 +797,15 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
       bool last = k + 1 == iters;
       uint32_t* od = last && out ? (uint32_t*)out->diffuse : nullptr;
       uint32_t* os = last && out ? (uint32_t*)out->specular : nullptr;
-      STAGE("dn_atrous", launch_dn_atrous(ex, w, h, ga, csrc, vsrc, cdst, vdst, od, os, 1 << k));
+      uint32_t* co = last && !keep_den ? nullptr : cdst;
+      STAGE("dn_atrous", launch_dn_atrous(ex, w, h, ga, csrc, vsrc, co, last ? nullptr : vdst, od, os, 1 << k));
       ++launches;
       std::swap(csrc, cdst);
       uint32_t* vnext = vdst == b.var[1] ? b.var[2] : b.var[1];
       vsrc = vdst;
       vdst = vnext;
     }
-    den = csrc;
+    den = keep_den ? (const void*)csrc : nullptr;
     if (iters == 0 && out && (out->diffuse || out->specular)) {
       launch_split_color(ex, w, h, csrc, (uint32_t*)out->diffuse, (uint32_t*)out->specular);
       ++launches;
@@ -1123,14 +1128,16 @@ __global__ void k_diag_math(int fn, const float* __restrict__ x, float* __restri
     case 1: r = exp_(v); break;
     case 2: r = log2_(v); break;
     case 3: r = sin_(v); break;
-    default: r = cos_(v); break;
+    case 4: r = cos_(v); break;
+    case 5: r = exp2_fma(v); break;
+    default: r = exp2_fma_full(v); break;
   }
   y[i] = r;
 }
 }  // namespace vlt
 
 extern "C" vlt_status vlt_diag_math(int fn, const float* x, float* y, uint32_t n, void* stream) {
-  if (fn < 0 || fn > 4 || (n && (!x || !y))) return VLT_ERR_INVALID_ARG;
+  if (fn < 0 || fn > 6 || (n && (!x || !y))) return VLT_ERR_INVALID_ARG;
   if (n == 0) return VLT_OK;
   vlt::k_diag_math<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(fn, x, y, n);
   return vlt::cuda_status(cudaGetLastError());

@@ -73,8 +73,31 @@ struct Job {
 
 // ----------------------------------------------------------------- kernels
 
+// Resident 256-thread blocks per SM a pass asks the register allocator for
+// (F::kMinBlocks, default 1): 4 caps the registers at 64 per thread, which lets
+// eight 128-thread tiles share an SM.
+template <class F, class = void>
+struct MinBlocks {
+  static constexpr int value = 1;
+};
+template <class F>
+struct MinBlocks<F, decltype((void)F::kMinBlocks)> {
+  static constexpr int value = F::kMinBlocks;
+};
+
+// Tile shape of a pass's single-view launches (F::kTileX x F::kTileY, default 32x4;
+// batched launches take the batch's shape or the autotuner's choice).
+template <class F, class = void>
+struct TileOf {
+  static constexpr int x = 32, y = 4;
+};
+template <class F>
+struct TileOf<F, decltype((void)F::kTileX)> {
+  static constexpr int x = F::kTileX, y = F::kTileY;
+};
+
 template <class F, class... A>
-__global__ void __launch_bounds__(kMaxThreads) k_grid(A... a) {
+__global__ void __launch_bounds__(kMaxThreads, MinBlocks<F>::value) k_grid(A... a) {
   F::run((int)(blockIdx.x * blockDim.x), (int)(blockIdx.y * blockDim.y), a...);
 }
 
@@ -98,7 +121,7 @@ struct BatchParams {
 };
 
 template <class F, class Tup>
-__global__ void __launch_bounds__(kMaxThreads) k_batched(const __grid_constant__ BatchParams<Tup> p) {
+__global__ void __launch_bounds__(kMaxThreads, MinBlocks<F>::value) k_batched(const __grid_constant__ BatchParams<Tup> p) {
   for (uint32_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
     uint32_t lo = 0, hi = p.n_jobs;  // last job whose first tile is <= t
     while (hi - lo > 1) {
@@ -199,7 +222,7 @@ void launch2d(const Exec& ex, const char* name, int w, int h, A... a) {
     record_job<F>(ex, name, (uint32_t)w, (uint32_t)h, false, a...);
     return;
   }
-  const dim3 block(32, 4, 1);
+  const dim3 block(TileOf<F>::x, TileOf<F>::y, 1);
   k_grid<F><<<grid2d(w, h, block), block, 0, ex.stream>>>(a...);
 }
 
