@@ -111,6 +111,13 @@ typedef struct vlt_params {
                                      (restir_renderer.rs:897-915); 2 also temporal AA
                                      (RestirConfig::taa, :920-948). The reference
                                      renderer runs 2; both presets give 0. */
+  uint32_t trace;                 /* 0: the caller supplies shaded diffuse candidates
+                                     (diff_hit_*) and hash-grid query radiance; 1:
+                                     traced mode (vlt_frame_trace below) */
+  uint32_t diff_validate;         /* traced mode: RestirConfig::ind_diff_validate, every
+                                     4th frame (restir_renderer.rs:450-453) */
+  uint32_t spec_validate;         /* traced mode: RestirConfig::ind_spec_validate, every
+                                     frame with history (:722-724) */
 } vlt_params;
 
 void vlt_params_reference(vlt_params* out);
@@ -157,6 +164,12 @@ typedef struct vlt_frame_inputs {
   const uint8_t* shadow_mask;         /* optional: R8_UNORM sun visibility for the final
                                          lighting (restir_renderer.rs:832-848); NULL:
                                          unshadowed */
+  /* traced mode: the caller's results for the rays vlt_frame_trace produced this
+   * frame (vlt_ray_hit per ray, same indices); diff_hit_* and diff_source_pdf are
+   * not read */
+  const struct vlt_ray_hit* cache_hits;
+  const struct vlt_ray_hit* diffuse_hits;
+  const struct vlt_ray_hit* spec_validate_hits;
 } vlt_frame_inputs;
 
 /* Output element type follows the view's form: REF -> u32 R11G11B10 per pixel,
@@ -172,6 +185,66 @@ typedef struct vlt_frame_outputs {
   void* taa;            /* the temporal-AA result (params.post == 2); the view keeps
                            it as next frame's history either way */
 } vlt_frame_outputs;
+
+/* ------------------------------------------------------------ traced mode
+ *
+ * With params.trace = 1 the view casts the rays of the reference's ray-generation
+ * shaders and the caller traces them against its own scene: a frame is
+ * vlt_frame_trace (decay, query selection and compaction of the hash grid, then the
+ * rays) followed by vlt_frame_run with the hits. The view shades every hit as
+ * trace_radiance does (restir/raytrace.inc.hlsl:84-207): the sun through the
+ * caller's shadow-ray result, then last frame's denoised indirect diffuse (the
+ * screen-space cache) where the hit reprojects onto matching depth, else the
+ * world-space hash grid, which also records a cache query. Ray sets:
+ *   cache          one ray per selected hash-grid query (hash_grid_raygen.hlsl);
+ *                  the cell blends in 1/16 of the shaded radiance
+ *   diffuse        the new diffuse candidate of every pixel (ind_diff_sample_gen.hlsl)
+ *                  or, on validation frames, the re-trace of last frame's sample
+ *                  (ind_diff_sample_validate.hlsl: M shrinks with the radiance change)
+ *   spec_validate  the re-trace of last frame's specular sample
+ *                  (ind_spec_sample_validate.hlsl: M = 1 when the radiance changed)
+ * Queries are appended in ray order (cache, diffuse, spec_validate); the
+ * reference's atomic append makes its order vary between runs. Specular candidates
+ * stay caller-supplied (spec_hit_pos / spec_hit_radiance). Batches and servers take
+ * no traced views. */
+
+/* RayDesc of the reference shaders. tmax < 0: no ray (its hit is not read). */
+typedef struct vlt_ray {
+  float origin[3];
+  float tmin;
+  float dir[3];
+  float tmax;
+} vlt_ray;
+
+/* The caller's result for one ray: the closest hit's GeometryRayPayload
+ * (raytrace/geometry_ray.inc.hlsl:67-104, SHRINK_PAYLOAD 0) and whether the shadow
+ * ray from the hit toward frame_params.sun_dir escaped (trace_shadow,
+ * raytrace.inc.hlsl:31-56). A missed ray carries the sky radiance along it (the
+ * skycube sample of :90) in base_color; its other fields are not read. */
+typedef struct vlt_ray_hit {
+  float position_ws[3];
+  uint32_t missed;
+  float normal_ws[3];
+  uint32_t sun_visible;
+  float normal_geo_ws[3];
+  float metallic;
+  float base_color[3];
+  float perceptual_roughness;
+} vlt_ray_hit;
+
+typedef struct vlt_frame_rays {
+  vlt_ray* cache;          /* vlt_view_cache_ray_capacity() rays */
+  vlt_ray* diffuse;        /* W*H */
+  vlt_ray* spec_validate;  /* W*H (may be NULL when params.spec_validate is 0) */
+  uint32_t n_cache;        /* out: entries to trace in each array (0: none this frame) */
+  uint32_t n_diffuse;
+  uint32_t n_spec_validate;
+  uint32_t diffuse_kind;   /* out: 1 new candidates, 2 validation of last frame's samples */
+} vlt_frame_rays;
+
+/* Phase one of a traced frame (device arrays, stream-ordered). */
+vlt_status vlt_frame_trace(vlt_view* view, const vlt_frame_inputs* in, vlt_frame_rays* rays, void* stream);
+uint32_t vlt_view_cache_ray_capacity(const vlt_view* view);
 
 /* Runs one frame in the pass order of RestirRenderer::add_passes and
  * Denoiser::add_passes, with the same conditional FrameRand seed consumption. The

@@ -45,6 +45,14 @@ void vlt_scene_desc_default(vlt_scene_desc* d, uint64_t seed, uint32_t width, ui
 vlt_status vlt_scene_frame_params(const vlt_scene_desc* d, uint32_t frame, vlt_frame_params* out);
 /* Generate a frame into host buffers (multithreaded). */
 vlt_status vlt_scene_generate_host(const vlt_scene_desc* d, uint32_t frame, const vlt_scene_frame* out);
+/* Traces rays against the scene: the stand-in for the caller's ray tracer in traced
+ * mode (vlt_frame_trace). hits[i] for rays[i], i < n; a ray with tmax < 0 gets an
+ * all-zero record. Shadow rays go toward fp->sun_dir; misses return a sky gradient.
+ * Host and device results are bit-identical. */
+vlt_status vlt_scene_trace_host(const vlt_scene_desc* d, const vlt_frame_params* fp, const vlt_ray* rays,
+                                uint32_t n, vlt_ray_hit* hits);
+vlt_status vlt_scene_trace_device(const vlt_scene_desc* d, const vlt_frame_params* fp, const vlt_ray* rays,
+                                  uint32_t n, vlt_ray_hit* hits, void* stream);
 /* Generate a frame into device buffers on `stream`. */
 vlt_status vlt_scene_generate_device(const vlt_scene_desc* d, uint32_t frame, const vlt_scene_frame* out,
                                      void* stream);

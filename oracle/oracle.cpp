@@ -2295,6 +2295,349 @@ void temporal_aa(const vlt_frame_params& fp, int w, int h, const float* depth, c
   }
 }
 
+// ==================================================== traced mode
+// The rays of the ray-generation shaders and the shading of the caller's hits
+// (restir/raytrace.inc.hlsl:84-207). Rays are vlt_ray (8 floats), hits vlt_ray_hit
+// (16 words); a query record is 8 words (checksum word 5 is 0 when there is none).
+
+// sampling.hlsl:10-26, 37-74.
+inline float4 get_rotation_to_z_from(float3 v) {
+  if (v.z < -0.99999f) return F4(1.0f, 0.0f, 0.0f, 0.0f);
+  float4 q = F4(v.y, -v.x, 0.0f, 1.0f + v.z);
+  float r = 1.0f / sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+  return F4(q.x * r, q.y * r, q.z * r, q.w * r);
+}
+inline float4 invert_rotation(float4 q) { return F4(-q.x, -q.y, -q.z, q.w); }
+inline float3 rotate_point(float4 q, float3 v) {
+  float3 axis = F3(q.x, q.y, q.z);
+  return (2.0f * dot(axis, v)) * axis + (q.w * q.w - dot(axis, axis)) * v + (2.0f * q.w) * cross(axis, v);
+}
+inline float3 sample_hemisphere_uniform(float u0, float u1) {
+  float cos_theta = 1.0f - u0;
+  float sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
+  float s, c;
+  sincos_own(TWO_PI * u1, &s, &c);
+  return F3(c * sin_theta, s * sin_theta, cos_theta);
+}
+inline float3 sample_hemisphere_cosine(float u0, float u1) {
+  float sin_theta = sqrtf(u0);
+  float cos_theta = sqrtf(1.0f - u0);
+  float s, c;
+  sincos_own(TWO_PI * u1, &s, &c);
+  return F3(sin_theta * c, sin_theta * s, cos_theta);
+}
+inline float3 rotate_from_local(float3 local, float3 normal) {
+  return rotate_point(invert_rotation(get_rotation_to_z_from(normal)), local);
+}
+
+inline void ray_put(float* rays, size_t i, float3 o, float3 d, bool valid) {
+  float* r = rays + 8 * i;
+  r[0] = o.x, r[1] = o.y, r[2] = o.z, r[3] = 0.0005f;
+  r[4] = d.x, r[5] = d.y, r[6] = d.z, r[7] = valid ? 1000.0f : -1.0f;
+}
+inline void ray_none(float* rays, size_t i) {
+  float* r = rays + 8 * i;
+  for (int k = 0; k < 8; ++k) r[k] = 0.0f;
+  r[7] = -1.0f;
+}
+struct ORay {
+  float3 o, d;
+  float tmax;
+};
+inline ORay ray_get(const float* rays, size_t i) {
+  const float* r = rays + 8 * i;
+  return {F3(r[0], r[1], r[2]), F3(r[4], r[5], r[6]), r[7]};
+}
+struct OHit {
+  float3 pos, n, ng, color;
+  bool missed, sun_visible;
+  float metallic, prc;
+};
+inline OHit hit_get(const float* hits, size_t i) {
+  const float* q = hits + 16 * i;
+  OHit h;
+  h.pos = F3(q[0], q[1], q[2]);
+  h.missed = asuint(q[3]) != 0u;
+  h.n = F3(q[4], q[5], q[6]);
+  h.sun_visible = asuint(q[7]) != 0u;
+  h.ng = F3(q[8], q[9], q[10]);
+  h.metallic = q[11];
+  h.color = F3(q[12], q[13], q[14]);
+  h.prc = q[15];
+  return h;
+}
+
+// The screen-space radiance cache: last frame's depth and denoised indirect diffuse
+// (form 0 R11G11B10, 1 float4, 2 half4, at element i * stride).
+struct OScreen {
+  const float* depth;
+  const void* diffuse;
+  int form, stride, w, h;
+};
+inline float3 screen_color(const OScreen& s, size_t i) {
+  const size_t e = i * (size_t)s.stride;
+  if (s.form == 1) return color_load<1>(s.diffuse, e);
+  if (s.form == 2) return color_load<2>(s.diffuse, e);
+  return color_load<0>(s.diffuse, e);
+}
+struct OWorld {
+  const uint32_t* storage;  // nullptr: no cache
+  uint32_t bucket_mask, key_mode;
+};
+struct OTraced {
+  float3 radiance, pos, normal;
+};
+
+// trace_radiance after TraceRay (raytrace.inc.hlsl:84-207).
+OTraced trace_radiance(const vlt_frame_params& fp, const ORay& r, const OHit& hit, bool has_prev_frame,
+                       const OScreen& sc, const OWorld& wc, uint32_t q[8]) {
+  OTraced t;
+  for (int k = 0; k < 8; ++k) q[k] = 0u;
+  if (hit.missed) {
+    t.radiance = hit.color;  // skycube.SampleLevel(ray.Direction)
+    t.pos = r.o + r.d * r.tmax;
+    t.normal = -r.d;
+    return t;
+  }
+  t.pos = hit.pos;
+  t.normal = hit.n;
+  float3 base_color = hit.color;
+  float metallic = hit.metallic;
+  float3 diffuse_rho = base_color * (1.0f - metallic);
+  float3 radiance = F3(0.0f);
+  float3 sun_dir = F3(fp.sun_dir[0], fp.sun_dir[1], fp.sun_dir[2]);
+  if (hit.sun_visible) {
+    float perceptual_roughness = hmax(hit.prc, 0.045f);
+    perceptual_roughness = hmax(perceptual_roughness, 0.5f);  // RAYTRACE_INC_FIREFLY_SUPPRESS
+    float NoL = saturate(dot(t.normal, sun_dir));
+    float3 specular_f0 = get_specular_f0(base_color, metallic);
+    radiance = eval_GGX_Lambertian(-r.d, sun_dir, t.normal, perceptual_roughness, diffuse_rho, specular_f0) * NoL *
+               F3(fp.sun_inten[0], fp.sun_inten[1], fp.sun_inten[2]);
+  }
+  bool sample_world_radiance_cache = true;
+  if (has_prev_frame) {
+    float4 prev_hpos = mul(fp.prev_view_proj, F4(t.pos.x, t.pos.y, t.pos.z, 1.0f));
+    float2 ndc = F2(prev_hpos.x / prev_hpos.w - fp.jitter[2], prev_hpos.y / prev_hpos.w - fp.jitter[3]);
+    float reproj_depth = prev_hpos.z / prev_hpos.w;
+    if (fabsf(ndc.x) < 1.0f && fabsf(ndc.y) < 1.0f) {
+      float2 uv = F2(ndc.x * 0.5f + 0.5f, ndc.y * 0.5f + 0.5f);
+      uint32_t px = to_uint(floorf(uv.x * (float)sc.w)), py = to_uint(floorf(uv.y * (float)sc.h));
+      const bool inside = px < (uint32_t)sc.w && py < (uint32_t)sc.h;
+      const size_t pi = (size_t)py * sc.w + px;
+      float prev_depth_value = inside ? sc.depth[pi] : 0.0f;
+      if (fabsf(reproj_depth - prev_depth_value) < 0.0001f) {
+        radiance = radiance + diffuse_rho * (inside ? screen_color(sc, pi) : F3(0.0f));
+        sample_world_radiance_cache = false;
+      }
+    }
+  }
+  if (sample_world_radiance_cache && wc.storage) {
+    VKey k = vertex_descriptor(t.pos, hit.ng, v3(fp.view_pos), wc.bucket_mask, wc.key_mode);
+    const uint32_t* bucket = wc.storage + (size_t)k.hash * 16 * 4;
+    for (uint32_t s = 0; s < 16; ++s) {
+      const uint32_t* c = bucket + 4 * s;
+      if (c[0] == k.checksum) {
+        radiance = radiance + diffuse_rho * F3(asfloat(c[1]), asfloat(c[2]), asfloat(c[3]));
+        break;
+      }
+      if (c[0] == 0u) break;
+    }
+    q[0] = asuint(t.pos.x);
+    q[1] = asuint(t.pos.y);
+    q[2] = asuint(t.pos.z);
+    q[3] = normal_encode_oct_u32(hit.ng);
+    q[4] = k.hash;
+    q[5] = k.checksum;
+  }
+  t.radiance = radiance;
+  return t;
+}
+
+// hash_grid_raygen.hlsl:27-51.
+void gen_rays_cache(uint32_t nmax, const uint32_t* queries, const uint32_t* cidx, uint32_t count, uint32_t frame_hash,
+                float* rays) {
+  for (uint32_t k = 0; k < nmax; ++k) {
+    if (k >= count) {
+      ray_none(rays, k);
+      continue;
+    }
+    const uint32_t* q = queries + (size_t)cidx[k] * 8;
+    float3 pos = F3(asfloat(q[0]), asfloat(q[1]), asfloat(q[2]));
+    float3 normal = normal_decode_oct(F2((float)(q[3] & 0xFFFFu) / 65535.0f, (float)(q[3] >> 16) / 65535.0f));
+    uint32_t lcg_state = jenkins_hash(k ^ frame_hash);
+    float u0 = lcg_rand(lcg_state);
+    float u1 = lcg_rand(lcg_state);
+    ray_put(rays, k, pos, rotate_from_local(sample_hemisphere_cosine(u0, u1), normal), true);
+  }
+}
+
+// ind_diff_sample_gen.hlsl:28-59.
+void gen_rays_diff(const vlt_frame_params& fp, int w, int h, const float* depth, const uint32_t* gbuf,
+               uint32_t frame_rand, float* rays) {
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      const size_t i = (size_t)y * w + x;
+      if (has_no_geometry_via_depth(depth[i])) {
+        ray_none(rays, i);
+        continue;
+      }
+      float3 normal = load_gbuffer_normal(gbuf, x, y, w, h);
+      float depth_error = 1.0f / 16777216.0f;
+      float2 screen_pos = F2(((float)x + 0.5f) / (float)w, ((float)y + 0.5f) / (float)h);
+      float4 ph = mul(fp.inv_view_proj, F4(screen_pos.x * 2.0f - 1.0f, screen_pos.y * 2.0f - 1.0f,
+                                           depth[i] + depth_error, 1.0f));
+      float3 position_ws = F3(ph.x / ph.w, ph.y / ph.w, ph.z / ph.w);
+      uint32_t rng_state = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
+      float u0 = lcg_rand(rng_state);
+      float u1 = lcg_rand(rng_state);
+      ray_put(rays, i, position_ws, rotate_from_local(sample_hemisphere_uniform(u0, u1), normal), true);
+    }
+}
+
+// Diffuse reservoir access of every form for validation: form 0 records are four
+// words {reservoir, HitPosNormal, radiance}; the packed word is kept when M stays.
+struct ODiffVal {
+  uint32_t M, word;
+  float W;
+  float3 pos, nrm, rad;
+};
+template <int FORM>
+ODiffVal dval_get(const void* rsv, size_t n, size_t i) {
+  ODiffVal r;
+  if constexpr (FORM == 0) {
+    const uint32_t* q = (const uint32_t*)rsv + 4 * i;
+    r.word = q[0];
+    reservoir_simple_decode_32b(q[0], &r.M, &r.W);
+    HitPosNormal hpn = HitPosNormal::decode(q[1], q[2]);
+    r.pos = hpn.pos;
+    r.nrm = hpn.normal;
+    r.rad = load_r11g11b10(q[3]);
+  } else {
+    DiffF32 d = diff_load<FORM>(rsv, n, i);
+    r.M = d.M, r.W = d.W, r.pos = d.pos, r.nrm = d.nrm, r.rad = d.rad;
+    r.word = 0u;
+  }
+  return r;
+}
+template <int FORM>
+void dval_put(void* rsv, size_t n, size_t i, const ODiffVal& r, bool rescaled) {
+  if constexpr (FORM == 0) {
+    uint32_t* q = (uint32_t*)rsv + 4 * i;
+    HitPosNormal hpn = {r.pos, r.nrm};
+    uint32_t e[2];
+    hpn.encode(e);
+    q[0] = rescaled ? reservoir_simple_encode_32b(r.M, r.W) : r.word;
+    q[1] = e[0];
+    q[2] = e[1];
+    q[3] = store_r11g11b10(r.rad);
+  } else {
+    diff_store<FORM>(rsv, n, i, r.M, r.W, r.pos, r.nrm, r.rad);
+  }
+}
+
+// ind_diff_sample_validate.hlsl:30-49.
+template <int FORM>
+void rays_diff_validate(const vlt_frame_params& fp, int w, int h, const float* prev_depth, const void* rsv,
+                        float* rays) {
+  const size_t n = (size_t)w * h;
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      const size_t i = (size_t)y * w + x;
+      const float depth = prev_depth[i];
+      if (has_no_geometry_via_depth(depth)) {
+        ray_none(rays, i);
+        continue;
+      }
+      ODiffVal r = dval_get<FORM>(rsv, n, i);
+      float3 origin = cs_depth_to_position(fp.prev_inv_view_proj, x, y, w, h, depth);  // cs_prev_depth_to_position
+      ray_put(rays, i, origin, normalize(r.pos - origin), true);
+    }
+}
+
+// ind_diff_sample_validate.hlsl:51-77.
+template <int FORM>
+void diff_validate_apply(const vlt_frame_params& fp, int w, int h, const float* prev_depth, void* rsv,
+                         const float* rays, const float* hits, const OScreen& sc, const OWorld& wc,
+                         uint32_t* staging) {
+  const size_t n = (size_t)w * h;
+  for (size_t i = 0; i < n; ++i) {
+    uint32_t* q = staging + 8 * i;
+    if (has_no_geometry_via_depth(prev_depth[i])) {
+      for (int k = 0; k < 8; ++k) q[k] = 0u;
+      continue;
+    }
+    ODiffVal hit = dval_get<FORM>(rsv, n, i);
+    ORay ray = ray_get(rays, i);
+    OTraced t = trace_radiance(fp, ray, hit_get(hits, i), true, sc, wc, q);
+    float lumi_prev = luminance(hit.rad);
+    float3 radiance_diff = t.radiance - hit.rad;
+    float lumi_diff = luminance(abs3(radiance_diff));
+    float prev_ray_len = length(hit.pos - ray.o);
+    float3 dp = abs3(hit.pos - t.pos);
+    bool pos_changed = hmax(hmax(dp.x, dp.y), dp.z) > hmax(prev_ray_len / 128.0f, 0.01f);
+    float m_scale = saturate(1.0f - (1.0f * lumi_diff) / lumi_prev);
+    m_scale = pos_changed ? 0.0f : m_scale;
+    bool rescale = (lumi_prev > 0.0f) && (m_scale <= (1.0f - 0.5f / 32.0f));
+    if (rescale) hit.M = to_uint(floorf((float)hit.M * m_scale));
+    hit.pos = t.pos;
+    hit.nrm = t.normal;
+    hit.rad = t.radiance;
+    dval_put<FORM>(rsv, n, i, hit, rescale);
+  }
+}
+
+// ind_spec_sample_validate.hlsl:19-44.
+template <bool F16>
+void rays_spec_validate(const vlt_frame_params& fp, int w, int h, const float* prev_depth, const uint32_t* rsv,
+                        const float* hp, const uint32_t* rad, float* rays) {
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      const size_t i = (size_t)y * w + x;
+      const float prev_d = prev_depth[i];
+      if (has_no_geometry_via_depth(prev_d)) {
+        ray_none(rays, i);
+        continue;
+      }
+      float depth_error = 1.0f / 16777216.0f;
+      float2 screen_pos = F2(((float)x + 0.5f) / (float)w, ((float)y + 0.5f) / (float)h);
+      float4 ph = mul(fp.prev_inv_view_proj, F4(screen_pos.x * 2.0f - 1.0f, screen_pos.y * 2.0f - 1.0f,
+                                                prev_d + depth_error, 1.0f));
+      float3 position_ws = F3(ph.x / ph.w, ph.y / ph.w, ph.z / ph.w);
+      SpecRec r = spec_load<F16>(rsv, hp, rad, x, y, w, h);
+      ray_put(rays, i, position_ws, normalize(r.hit - position_ws), true);
+    }
+}
+
+// ind_spec_sample_validate.hlsl:46-61.
+template <bool F16>
+void spec_validate_apply(const vlt_frame_params& fp, int w, int h, const float* prev_depth, uint32_t* rsv, float* hp,
+                         uint32_t* rad, const float* rays, const float* hits, const OScreen& sc, const OWorld& wc,
+                         uint32_t* staging) {
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      const size_t i = (size_t)y * w + x;
+      uint32_t* q = staging + 8 * i;
+      if (has_no_geometry_via_depth(prev_depth[i])) {
+        for (int k = 0; k < 8; ++k) q[k] = 0u;
+        continue;
+      }
+      SpecRec r = spec_load<F16>(rsv, hp, rad, x, y, w, h);
+      OTraced t = trace_radiance(fp, ray_get(rays, i), hit_get(hits, i), true, sc, wc, q);
+      float max_radiance = hmax(hmax(t.radiance.x, t.radiance.y), t.radiance.z);
+      max_radiance = hmax(max_radiance, hmax(hmax(r.rad.x, r.rad.y), r.rad.z));
+      float3 d = abs3(t.radiance - r.rad);
+      float lim = 0.5f * max_radiance;
+      if (d.x > lim || d.y > lim || d.z > lim) {
+        r.M = 1;
+        r.hit = t.pos;
+        r.rad = t.radiance;
+        r.rad_bits = store_r11g11b10(t.radiance);
+        spec_store<F16>(rsv, hp, rad, i, r);
+      }
+    }
+}
+
 struct OView {
   int w, h;
   vlt_params P;
@@ -2323,12 +2666,90 @@ struct OView {
   // (RestirRenderer::prev_color), in the form's colour element.
   std::vector<uint8_t> lit, taa_hist;
   bool taa_valid = false;
+  // Traced mode: the pending frame's rays (kept from frame_trace), the shaded
+  // candidates, the query staging (cache, diffuse, spec-validate rays) and last
+  // frame's denoised indirect diffuse (the screen-space cache).
+  bool trace_pending = false;
+  uint32_t trace_frame = 0, trace_cache = 0, trace_diff = 0, trace_spec = 0;
+  std::vector<uint32_t> spec_rsv_in, spec_rad_in;  // last frame's specular reservoir as this frame read it
+  std::vector<float> spec_hp_in;
+  std::vector<float> rays_cache, rays_diff, rays_spec;
+  std::vector<uint32_t> tr_hpn, tr_rad, q_staging;
+  std::vector<float3> cache_rad;
+  std::vector<uint8_t> prev_den;
+  int prev_den_stride = 1;
+  bool has_prev_den = false;
+  uint32_t nq() const { return P.hg_enable ? std::min<uint32_t>(max_q, 16u << log2_buckets) : 0u; }
 };
 
 struct FrameRand {
   uint32_t state;
   uint32_t next() { return state = jenkins_hash(state); }
 };
+
+// The diffuse reservoir of the view in its form (form 0: four words per pixel).
+inline void* diff_rsv_ptr(OView& v) { return v.form ? (void*)v.fdiff_prev.data() : (void*)v.diff_prev.data(); }
+
+// Phase one of a traced frame: decay, query selection and compaction, then the
+// rays (cache, diffuse candidates or validation, specular validation).
+void frame_trace(OView& v, const vlt_frame_inputs& in, float* rays_cache, float* rays_diff, float* rays_spec,
+                 uint32_t* counts) {
+  const vlt_frame_params& fp = *in.params;
+  const int w = v.w, h = v.h;
+  const size_t n = (size_t)w * h;
+  const vlt_params& P = v.P;
+  const bool has_prev = v.frames > 0;
+  const float* prev_depth = v.prev_depth.data();
+  FrameRand frame_rand = {in.frame_index};
+  const uint32_t nq = v.nq();
+  if (P.hg_enable && P.hg_decay) hg_decay(v.log2_buckets, v.hg_decay.data(), v.hg_storage.data());
+  v.trace_cache = 0;
+  v.rays_cache.assign((size_t)nq * 8, 0.0f);
+  if (has_prev) {
+    uint32_t s_select = frame_rand.next();
+    uint32_t s_update = frame_rand.next();
+    if (P.hg_enable) {
+      std::fill(v.sel.begin(), v.sel.end(), 0u);
+      hg_select(v.log2_buckets, v.max_q, v.hg_queries.data(), &v.hg_qcount, v.hg_storage.data(), v.sel.data(),
+                s_select);
+      v.ccount = 0;
+      hg_compact(v.log2_buckets, v.max_q, v.sel.data(), v.cidx.data(), v.caddr.data(), &v.ccount);
+      gen_rays_cache(nq, v.hg_queries.data(), v.cidx.data(), v.ccount, s_update, v.rays_cache.data());
+      v.trace_cache = 1;
+    }
+  }
+  const bool validate = P.diff_validate && has_prev && (in.frame_index & 3u) == 0u;
+  v.rays_diff.assign(n * 8, 0.0f);
+  if (validate) {
+    if (v.form == 1) rays_diff_validate<1>(fp, w, h, prev_depth, diff_rsv_ptr(v), v.rays_diff.data());
+    else if (v.form == 2) rays_diff_validate<2>(fp, w, h, prev_depth, diff_rsv_ptr(v), v.rays_diff.data());
+    else rays_diff_validate<0>(fp, w, h, prev_depth, diff_rsv_ptr(v), v.rays_diff.data());
+  } else {
+    gen_rays_diff(fp, w, h, in.depth, in.gbuffer, frame_rand.next(), v.rays_diff.data());
+  }
+  v.trace_diff = validate ? 2u : 1u;
+  v.trace_spec = 0;
+  v.rays_spec.assign(n * 8, 0.0f);
+  if (P.spec_validate && has_prev) {
+    if (v.form == 2)
+      rays_spec_validate<true>(fp, w, h, prev_depth, nullptr, v.spec_hp_prev.data(), nullptr, v.rays_spec.data());
+    else
+      rays_spec_validate<false>(fp, w, h, prev_depth, v.spec_rsv_prev.data(), v.spec_hp_prev.data(),
+                                v.spec_rad_prev.data(), v.rays_spec.data());
+    v.trace_spec = 1;
+  }
+  if (rays_cache) memcpy(rays_cache, v.rays_cache.data(), v.rays_cache.size() * 4);
+  if (rays_diff) memcpy(rays_diff, v.rays_diff.data(), v.rays_diff.size() * 4);
+  if (rays_spec && v.trace_spec) memcpy(rays_spec, v.rays_spec.data(), v.rays_spec.size() * 4);
+  if (counts) {
+    counts[0] = v.trace_cache ? nq : 0u;
+    counts[1] = (uint32_t)n;
+    counts[2] = v.trace_spec ? (uint32_t)n : 0u;
+    counts[3] = v.trace_diff;
+  }
+  v.trace_pending = true;
+  v.trace_frame = in.frame_index;
+}
 
 void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* out) {
   const vlt_frame_params& fp = *in.params;
@@ -2339,9 +2760,45 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
   const float* prev_depth = v.prev_depth.data();
   const uint32_t* prev_gbuf = v.prev_gbuf.data();
   FrameRand frame_rand = {in.frame_index};
+  const bool traced = P.trace != 0;
+  if (traced && (!v.trace_pending || v.trace_frame != in.frame_index)) return;  // phase one first
+  v.trace_pending = false;
+  const uint32_t nq = v.nq();
+  const OScreen scache = {prev_depth, v.prev_den.empty() ? nullptr : (const void*)v.prev_den.data(), v.form,
+                          v.prev_den_stride, w, h};
+  const OWorld wcache = {P.hg_enable ? v.hg_storage.data() : nullptr, (1u << v.log2_buckets) - 1u, P.hg_key_mode};
+  const bool diff_validation = traced && v.trace_diff == 2;
+  if (traced) {
+    v.q_staging.assign(((size_t)nq + 2 * n) * 8, 0u);
+    v.tr_hpn.assign(2 * n, 0u);
+    v.tr_rad.assign(n, 0u);
+  }
 
-  if (P.hg_enable && P.hg_decay) hg_decay(v.log2_buckets, v.hg_decay.data(), v.hg_storage.data());
-  if (has_prev) {  // restir_renderer.rs:357-433
+  if (P.hg_enable && P.hg_decay && !traced) hg_decay(v.log2_buckets, v.hg_decay.data(), v.hg_storage.data());
+  if (has_prev && traced) {
+    (void)frame_rand.next();  // query selection (frame_trace)
+    (void)frame_rand.next();  // cache rays (frame_trace)
+    if (v.trace_cache) {
+      // hash_grid_raygen.hlsl:53-86: shade every update ray with the cells as they
+      // were, then blend.
+      const float* hits = (const float*)in.cache_hits;
+      v.cache_rad.assign(nq, F3(0.0f));
+      for (uint32_t k = 0; k < nq && k < v.ccount; ++k) {
+        OTraced t = trace_radiance(fp, ray_get(v.rays_cache.data(), k), hit_get(hits, k), true, scache, wcache,
+                                   v.q_staging.data() + 8 * (size_t)k);
+        v.cache_rad[k] = t.radiance;
+      }
+      for (uint32_t k = 0; k < nq && k < v.ccount; ++k) {
+        uint32_t* c = v.hg_storage.data() + 4 * (size_t)v.caddr[k];
+        float3 prev_radiance = F3(asfloat(c[1]), asfloat(c[2]), asfloat(c[3]));
+        float blend_factor = 1.0f / 16.0f;
+        float3 blend_radiance = v.cache_rad[k] * blend_factor + prev_radiance * (1.0f - blend_factor);
+        c[1] = asuint(blend_radiance.x), c[2] = asuint(blend_radiance.y), c[3] = asuint(blend_radiance.z);
+        v.hg_decay[v.caddr[k]] = 10;
+      }
+    }
+  }
+  if (has_prev && !traced) {  // restir_renderer.rs:357-433
     uint32_t s_select = frame_rand.next();
     (void)frame_rand.next();  // raygen seed
     if (P.hg_enable) {
@@ -2354,20 +2811,58 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
                 v.hg_decay.data());
     }
   }
-  if (P.hg_enable)
+  if (P.hg_enable && !traced)
     hg_emit(fp, w, h, v.log2_buckets, P.hg_key_mode, v.max_q, in.depth, in.diff_hit_pos_normal,
             in.diff_hit_radiance, v.hg_queries.data(), &v.hg_qcount);
-  (void)frame_rand.next();  // diffuse sample generation
+  if (!diff_validation) (void)frame_rand.next();  // diffuse sample generation
+  const uint32_t* diff_hpn = in.diff_hit_pos_normal;
+  const uint32_t* diff_rad = in.diff_hit_radiance;
+  const float* diff_pdf = in.diff_source_pdf;
+  vlt_params Pd = P;  // traced: the reference's constant source pdf
+  if (traced) {
+    Pd.use_input_pdf = 0;
+    diff_pdf = nullptr;
+    diff_hpn = v.tr_hpn.data();
+    diff_rad = v.tr_rad.data();
+    uint32_t* staging = v.q_staging.data() + 8 * (size_t)nq;
+    const float* hits = (const float*)in.diffuse_hits;
+    if (diff_validation) {
+      if (v.form == 1)
+        diff_validate_apply<1>(fp, w, h, prev_depth, diff_rsv_ptr(v), v.rays_diff.data(), hits, scache, wcache, staging);
+      else if (v.form == 2)
+        diff_validate_apply<2>(fp, w, h, prev_depth, diff_rsv_ptr(v), v.rays_diff.data(), hits, scache, wcache, staging);
+      else
+        diff_validate_apply<0>(fp, w, h, prev_depth, diff_rsv_ptr(v), v.rays_diff.data(), hits, scache, wcache, staging);
+    } else {
+      // ind_diff_sample_gen.hlsl:35-40, 61-66
+      const bool hp = has_prev && v.has_prev_den;
+      for (size_t i = 0; i < n; ++i) {
+        ORay r = ray_get(v.rays_diff.data(), i);
+        uint32_t* q = staging + 8 * i;
+        if (!(r.tmax >= 0.0f)) {
+          for (int k = 0; k < 8; ++k) q[k] = 0u;
+          v.tr_hpn[2 * i] = v.tr_hpn[2 * i + 1] = 0u;
+          v.tr_rad[i] = 0u;
+          continue;
+        }
+        OTraced t = trace_radiance(fp, r, hit_get(hits, i), hp, scache, wcache, q);
+        HitPosNormal pn = {t.pos, t.normal};
+        pn.encode(&v.tr_hpn[2 * i]);
+        v.tr_rad[i] = store_r11g11b10(t.radiance);
+      }
+    }
+  }
+  const uint32_t has_new = diff_validation ? 0u : 1u;
 
   if (v.form != 0) {
     const bool f32 = v.form == 1;
     std::vector<uint8_t> ao_cur(v.fao_prev.size());
     if (f32) {
-      ao_gen<true>(fp, w, h, in.diff_hit_pos_normal, in.depth, v.fao_prev.data(), ao_cur.data(), 1u,
+      ao_gen<true>(fp, w, h, diff_hpn, in.depth, v.fao_prev.data(), ao_cur.data(), has_new,
                    has_prev ? 1u : 0u, P.ao_radius);
       ao_filter<true>(w, h, in.depth, ao_cur.data(), v.fao_filtered.data());
     } else {
-      ao_gen<false>(fp, w, h, in.diff_hit_pos_normal, in.depth, v.fao_prev.data(), ao_cur.data(), 1u,
+      ao_gen<false>(fp, w, h, diff_hpn, in.depth, v.fao_prev.data(), ao_cur.data(), has_new,
                     has_prev ? 1u : 0u, P.ao_radius);
       ao_filter<false>(w, h, in.depth, ao_cur.data(), v.fao_filtered.data());
     }
@@ -2375,11 +2870,11 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
     std::vector<uint8_t> temp(v.fdiff_prev.size()), sp(v.fdiff_prev.size());
     const uint32_t seed_dt = frame_rand.next();
     if (f32)
-      diff_temporal_f32<1>(fp, w, h, P, prev_depth, in.depth, in.diff_hit_pos_normal, in.diff_hit_radiance,
-                           in.diff_source_pdf, v.fdiff_prev.data(), temp.data(), seed_dt, has_prev ? 1u : 0u, 1u);
+      diff_temporal_f32<1>(fp, w, h, Pd, prev_depth, in.depth, diff_hpn, diff_rad, diff_pdf, v.fdiff_prev.data(),
+                           temp.data(), seed_dt, has_prev ? 1u : 0u, has_new);
     else
-      diff_temporal_f32<2>(fp, w, h, P, prev_depth, in.depth, in.diff_hit_pos_normal, in.diff_hit_radiance,
-                           in.diff_source_pdf, v.fdiff_prev.data(), temp.data(), seed_dt, has_prev ? 1u : 0u, 1u);
+      diff_temporal_f32<2>(fp, w, h, Pd, prev_depth, in.depth, diff_hpn, diff_rad, diff_pdf, v.fdiff_prev.data(),
+                           temp.data(), seed_dt, has_prev ? 1u : 0u, has_new);
     for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
       bool last = k + 1 == P.diff_spatial_passes;
       const uint32_t seed = frame_rand.next();
@@ -2394,13 +2889,13 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
     v.fdiff_prev.swap(temp);
   } else {
     std::vector<uint32_t> ao_cur(n);
-    ao_gen<false>(fp, w, h, in.diff_hit_pos_normal, in.depth, v.ao_prev.data(), ao_cur.data(), 1u,
+    ao_gen<false>(fp, w, h, diff_hpn, in.depth, v.ao_prev.data(), ao_cur.data(), has_new,
                   has_prev ? 1u : 0u, P.ao_radius);
     ao_filter<false>(w, h, in.depth, ao_cur.data(), v.ao_filtered.data());
     v.ao_prev.swap(ao_cur);
     std::vector<uint32_t> temp(4 * n), sp(4 * n);
-    diff_temporal(fp, w, h, P, prev_depth, in.depth, in.diff_hit_pos_normal, in.diff_hit_radiance,
-                  in.diff_source_pdf, v.diff_prev.data(), temp.data(), frame_rand.next(), has_prev ? 1u : 0u, 1u);
+    diff_temporal(fp, w, h, Pd, prev_depth, in.depth, diff_hpn, diff_rad, diff_pdf, v.diff_prev.data(), temp.data(),
+                  frame_rand.next(), has_prev ? 1u : 0u, has_new);
     for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
       bool last = k + 1 == P.diff_spatial_passes;
       diff_spatial<false>(fp, w, h, P, in.gbuffer, in.depth, v.ao_filtered.data(), temp.data(), sp.data(),
@@ -2414,6 +2909,38 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
   // f16 form: one 24-byte record per pixel in the `hp` buffers (6 words), no
   // separate M/W and radiance planes.
   const bool s16 = v.form == 2;
+  if (traced && v.trace_spec) {
+    uint32_t* staging = v.q_staging.data() + 8 * ((size_t)nq + n);
+    const float* hits = (const float*)in.spec_validate_hits;
+    if (s16)
+      spec_validate_apply<true>(fp, w, h, prev_depth, nullptr, v.spec_hp_prev.data(), nullptr, v.rays_spec.data(),
+                                hits, scache, wcache, staging);
+    else
+      spec_validate_apply<false>(fp, w, h, prev_depth, v.spec_rsv_prev.data(), v.spec_hp_prev.data(),
+                                 v.spec_rad_prev.data(), v.rays_spec.data(), hits, scache, wcache, staging);
+  }
+  if (!s16) {  // kept for inspection
+    v.spec_rsv_in = v.spec_rsv_prev;
+    v.spec_hp_in = v.spec_hp_prev;
+    v.spec_rad_in = v.spec_rad_prev;
+  }
+  if (traced && P.hg_enable) {
+    // The cache queries of the traced passes in ray order (cache, diffuse, specular
+    // validation rays), at most max_q stored; the count keeps counting.
+    uint32_t rank = 0;
+    const size_t ranges[3][2] = {{0, nq}, {nq, nq + n}, {nq + n, nq + 2 * n}};
+    const bool on[3] = {v.trace_cache != 0u, true, v.trace_spec != 0u};
+    for (int r = 0; r < 3; ++r) {
+      if (!on[r]) continue;
+      for (size_t i = ranges[r][0]; i < ranges[r][1]; ++i) {
+        const uint32_t* q = v.q_staging.data() + 8 * i;
+        if (q[5] == 0u) continue;
+        if (rank < v.max_q) memcpy(v.hg_queries.data() + 8 * (size_t)rank, q, 32);
+        ++rank;
+      }
+    }
+    v.hg_qcount = rank;
+  }
   const size_t hpw = s16 ? 6 : 4;
   std::vector<uint32_t> srsv(s16 ? 0 : 2 * n), srad(s16 ? 0 : n);
   std::vector<float> shp(hpw * n);
@@ -2590,6 +3117,20 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
       if (out && out->taa) memcpy(out->taa, v.taa_hist.data(), cb * n);
     }
   }
+  // Last frame's denoised indirect diffuse for the next traced frame's screen-space
+  // cache (restir_renderer.rs:819-820): the denoiser's last records, else the raw
+  // lighting.
+  if (!den_rec.empty()) {
+    v.prev_den = den_rec;
+    v.prev_den_stride = 2;
+  } else if (!den_color.empty()) {
+    v.prev_den.assign((const uint8_t*)den_color.data(), (const uint8_t*)den_color.data() + den_color.size() * 4);
+    v.prev_den_stride = 2;
+  } else {
+    v.prev_den.assign((const uint8_t*)diff_light, (const uint8_t*)diff_light + light_bytes);
+    v.prev_den_stride = 1;
+  }
+  v.has_prev_den = true;
   memcpy(v.prev_depth.data(), in.depth, 4 * n);
   memcpy(v.prev_gbuf.data(), in.gbuffer, 16 * n);
   v.frames += 1;
@@ -2663,6 +3204,15 @@ void* vlto_view_create(uint32_t w, uint32_t h, const vlt_params* p) { return vlt
 
 void vlto_view_destroy(void* h) { delete (OView*)h; }
 
+// Traced mode, phase one: rays into host arrays (cache: nq rays, diffuse and
+// spec-validate: W*H rays; any may be NULL); counts = {cache, diffuse, spec, diffuse
+// kind}.
+void vlto_frame_trace(void* h, const vlt_frame_inputs* in, float* rays_cache, float* rays_diff, float* rays_spec,
+                      uint32_t* counts) {
+  frame_trace(*(OView*)h, *in, rays_cache, rays_diff, rays_spec, counts);
+}
+uint32_t vlto_cache_ray_capacity(void* h) { return ((OView*)h)->nq(); }
+
 void vlto_frame_run(void* h, const vlt_frame_inputs* in, const vlt_frame_outputs* out) {
   frame_run(*(OView*)h, *in, out);
 }
@@ -2706,6 +3256,9 @@ void* vlto_view_buffer(void* h, const char* name, size_t* bytes) {
       {"spec_hit_pos", v.spec_hp_prev.data(), 16 * n},
       {"spec_reservoir", v.spec_rsv_prev.data(), 8 * n},
       {"spec_radiance", v.spec_rad_prev.data(), 4 * n},
+      {"spec_prev_hit_pos", v.spec_hp_in.empty() || !v.frames ? nullptr : v.spec_hp_in.data(), 16 * n},
+      {"spec_prev_reservoir", v.spec_rsv_in.empty() || !v.frames ? nullptr : v.spec_rsv_in.data(), 8 * n},
+      {"spec_prev_radiance", v.spec_rad_in.empty() || !v.frames ? nullptr : v.spec_rad_in.data(), 4 * n},
       {"ao_history", v.ao_prev.data(), 4 * n},
       {"ao_filtered", v.ao_filtered.data(), 2 * n},
       {"hist_color", v.hist_color.data(), 8 * n},

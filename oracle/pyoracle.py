@@ -43,6 +43,8 @@ SIGS = {
     "vlto_denoise_fast_history_clamp": (None, [U32, U32, P, P]),
     "vlto_denoise_spatial_fallback": (None, [U32, U32, P, P, P, P, P, P, P]),
     "vlto_denoise_atrous": (None, [U32, U32, P, P, P, P, P, P, C.c_int]),
+    "vlto_frame_trace": (None, [P, C.POINTER(_ffi.FrameInputs), P, P, P, P]),
+    "vlto_cache_ray_capacity": (U32, [P]),
     "vlto_final_lighting": (None, [C.c_int, FP, U32, U32, P, P, P, P, C.c_int, P]),
     "vlto_temporal_aa": (None, [C.c_int, FP, U32, U32, P, P, P, U32, P]),
     "vlto_hg_decay": (None, [U32, P, P]),
@@ -116,13 +118,30 @@ class OracleView:
         self.form = form
         self.handle = lib().vlto_view_create_form(self.width, self.height, C.byref(params), _ffi.FORMS[form])
 
-    def run(self, frame_params, frame_index, inputs, outputs=None):
+    def _inputs(self, frame_params, frame_index, inputs):
         fi = _ffi.FrameInputs()
         fi.params = C.pointer(frame_params)
         fi.frame_index = int(frame_index) & 0xFFFFFFFF
         for k in ("depth", "gbuffer", "diff_hit_pos_normal", "diff_hit_radiance", "diff_source_pdf", "spec_hit_pos",
-                  "spec_hit_radiance", "shadow_mask"):
+                  "spec_hit_radiance", "shadow_mask", "cache_hits", "diffuse_hits", "spec_validate_hits"):
             setattr(fi, k, ptr(inputs.get(k)))
+        return fi
+
+    def trace(self, frame_params, frame_index, inputs):
+        """Traced mode, phase one: returns (rays dict of float32 arrays, counts dict)."""
+        fi = self._inputs(frame_params, frame_index, inputs)
+        n = self.width * self.height
+        nq = int(lib().vlto_cache_ray_capacity(self.handle))
+        rays = {"cache": np.zeros(8 * max(nq, 1), np.float32), "diffuse": np.zeros(8 * n, np.float32),
+                "spec_validate": np.zeros(8 * n, np.float32)}
+        counts = np.zeros(4, np.uint32)
+        lib().vlto_frame_trace(self.handle, C.byref(fi), ptr(rays["cache"]), ptr(rays["diffuse"]),
+                               ptr(rays["spec_validate"]), ptr(counts))
+        return rays, {"cache": int(counts[0]), "diffuse": int(counts[1]), "spec_validate": int(counts[2]),
+                      "diffuse_kind": int(counts[3])}
+
+    def run(self, frame_params, frame_index, inputs, outputs=None):
+        fi = self._inputs(frame_params, frame_index, inputs)
         fo = _ffi.FrameOutputs()
         for k in ("diffuse", "specular", "raw_diffuse", "raw_specular", "color", "taa"):
             setattr(fo, k, ptr((outputs or {}).get(k)))

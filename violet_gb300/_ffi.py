@@ -59,6 +59,9 @@ class Params(C.Structure):
         ("hg_key_mode", C.c_uint32),
         ("hg_max_queries", C.c_uint32),
         ("post", C.c_uint32),
+        ("trace", C.c_uint32),
+        ("diff_validate", C.c_uint32),
+        ("spec_validate", C.c_uint32),
     ]
 
     def as_dict(self):
@@ -79,7 +82,26 @@ class FrameInputs(C.Structure):
         ("spec_hit_pos", C.c_void_p),
         ("spec_hit_radiance", C.c_void_p),
         ("shadow_mask", C.c_void_p),
+        ("cache_hits", C.c_void_p),
+        ("diffuse_hits", C.c_void_p),
+        ("spec_validate_hits", C.c_void_p),
     ]
+
+
+class FrameRays(C.Structure):
+    _fields_ = [
+        ("cache", C.c_void_p),
+        ("diffuse", C.c_void_p),
+        ("spec_validate", C.c_void_p),
+        ("n_cache", C.c_uint32),
+        ("n_diffuse", C.c_uint32),
+        ("n_spec_validate", C.c_uint32),
+        ("diffuse_kind", C.c_uint32),
+    ]
+
+
+RAY_BYTES = 32  # vlt_ray
+HIT_BYTES = 64  # vlt_ray_hit
 
 
 class FrameOutputs(C.Structure):
@@ -172,6 +194,8 @@ SIGNATURES = {
     "vlt_view_device_bytes": (C.c_size_t, [U32, U32, C.c_int, PP]),
     "vlt_view_reset": (C.c_int, [P, P]),
     "vlt_frame_run": (C.c_int, [P, C.POINTER(FrameInputs), C.POINTER(FrameOutputs), P]),
+    "vlt_frame_trace": (C.c_int, [P, C.POINTER(FrameInputs), C.POINTER(FrameRays), P]),
+    "vlt_view_cache_ray_capacity": (U32, [P]),
     "vlt_view_last_launch_count": (U32, [P]),
     "vlt_batch_create": (C.c_int, [P, C.POINTER(P)]),
     "vlt_batch_destroy": (C.c_int, [P]),
@@ -221,6 +245,8 @@ SIGNATURES = {
     "vlt_scene_frame_params": (C.c_int, [C.POINTER(SceneDesc), U32, FP]),
     "vlt_scene_generate_host": (C.c_int, [C.POINTER(SceneDesc), U32, C.POINTER(SceneFrame)]),
     "vlt_scene_generate_device": (C.c_int, [C.POINTER(SceneDesc), U32, C.POINTER(SceneFrame), P]),
+    "vlt_scene_trace_host": (C.c_int, [C.POINTER(SceneDesc), C.POINTER(FrameParams), P, U32, P]),
+    "vlt_scene_trace_device": (C.c_int, [C.POINTER(SceneDesc), C.POINTER(FrameParams), P, U32, P, P]),
 }
 
 _lib = None

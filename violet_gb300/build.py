@@ -15,8 +15,9 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libvlt.so")
 
-SOURCES = ["restir.cu", "denoise.cu", "denoise_f32.cu", "hashgrid.cu", "post.cu", "scene.cu", "launch.cu", "api.cu", "batch.cu", "server.cu"]
-HEADERS = ["vlt_math.cuh", "vlt_device.cuh", "vlt_launch.cuh", "vlt_internal.h", "brdf.cuh", "scene_gen.cuh"]
+SOURCES = ["restir.cu", "denoise.cu", "denoise_f32.cu", "hashgrid.cu", "trace.cu", "post.cu", "scene.cu", "launch.cu", "api.cu", "batch.cu", "server.cu"]
+HEADERS = ["vlt_math.cuh", "vlt_device.cuh", "vlt_launch.cuh", "vlt_internal.h", "brdf.cuh", "scene_gen.cuh", "trace.cuh",
+           "hashgrid.cuh", "vlt_compact.cuh"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

@@ -10,6 +10,7 @@
 #include <utility>
 #include <vector>
 
+#include "vlt_compact.cuh"
 #include "vlt_internal.h"
 
 namespace vlt {
@@ -86,6 +87,12 @@ struct ViewBuffers {
   float4* surf[2][3];      // per-frame surface planes {normal, depth}, {position, roughness}, {f0, fwidth_z}
   void* lit;               // final lighting when the caller gives no colour buffer
   void* taa[2];            // temporal-AA results: last frame's (history) and this frame's
+  uint32_t* scan;          // ordered-compaction chunk counts
+  // traced mode
+  uint32_t* tr_hpn;        // uint2: the shaded diffuse candidates (HitPosNormal)
+  uint32_t* tr_rad;        // R11G11B10
+  uint32_t* q_staging;     // 8-word query record per ray: cache, diffuse, spec-validate rays
+  float4* cache_rad;       // shaded radiance of the cache-update rays
 };
 
 }  // namespace
@@ -131,6 +138,14 @@ struct vlt_view {
   int diff_prev, spec_prev, ao_prev, hg_qcur, surf_cur;
   int taa_cur;             // taa[taa_cur] holds the latest temporal-AA result
   bool taa_valid;          // RestirRenderer::prev_color is Some
+  // traced mode
+  bool trace_pending;      // vlt_frame_trace ran for trace_frame; vlt_frame_run is next
+  uint32_t trace_frame;
+  uint32_t trace_cache, trace_diff, trace_spec;  // ray sets of the pending frame (diff: 1 new, 2 validate)
+  const void* trace_rays[3];  // the caller's ray arrays of the pending frame (cache, diffuse, spec)
+  const void* prev_den;    // last frame's denoised indirect diffuse (screen-space cache)
+  int prev_den_stride;
+  bool has_prev_den;
   uint32_t launches;
   Timing* timing;
 };
@@ -141,6 +156,13 @@ uint32_t eff_max_queries(const vlt_params& p, uint32_t w, uint32_t h) {
   uint64_t n = p.hg_max_queries ? p.hg_max_queries : (uint64_t)w * h;
   if (n > (1u << 30)) n = 1u << 30;
   return (uint32_t)n;
+}
+
+// Cache-update rays of a traced view: one per compacted query, at most
+// min(max queries, cells).
+uint32_t cache_rays(const vlt_view* v) {
+  const uint32_t nc = v->hg.num_cells();
+  return v->hg.max_queries < nc ? v->hg.max_queries : nc;
 }
 
 // Lays out every buffer of a view in one allocation; with base == nullptr only
@@ -216,6 +238,23 @@ size_t layout(vlt_view* v, char* base) {
   b.prev_depth = (float*)take(4 * n);
   for (int k = 0; k < 2; ++k)
     for (int j = 0; j < 3; ++j) b.surf[k][j] = (float4*)take(16 * n);
+  // Ordered compaction scratch: hash-grid cells, or the traced query records.
+  const uint32_t nq = v->p.hg_enable ? cache_rays(v) : 0u;
+  {
+    size_t sb = 0;
+    if (v->p.hg_enable) sb = compact_scratch_bytes(v->hg.num_cells());
+    if (v->p.trace) {
+      const size_t t = compact_scratch_bytes((uint32_t)(nq + 2 * n));
+      sb = sb > t ? sb : t;
+    }
+    b.scan = sb ? (uint32_t*)take(sb) : nullptr;
+  }
+  if (v->p.trace) {
+    b.tr_hpn = (uint32_t*)take(8 * n);
+    b.tr_rad = (uint32_t*)take(4 * n);
+    b.q_staging = (uint32_t*)take((size_t)(nq + 2 * n) * 32);
+    b.cache_rad = (float4*)take((size_t)(nq ? nq : 1) * 16);
+  }
   // Colour images in the form's lighting element (R11G11B10 / float4 / half4).
   if (v->p.post >= 1) b.lit = take(by(4, 16, 8) * n);
   if (v->p.post >= 2)
@@ -231,6 +270,8 @@ bool params_ok(const vlt_params* p) {
   if (p->hg_key_mode > 1) return false;
   if (!(p->history_max_frames >= 1.0f)) return false;
   if (p->post > 2) return false;
+  if (p->trace > 1 || p->diff_validate > 1 || p->spec_validate > 1) return false;
+  if ((p->diff_validate || p->spec_validate) && !p->trace) return false;  // validation re-traces
   return true;
 }
 
@@ -266,6 +307,10 @@ vlt_status reset_state(vlt_view* v, cudaStream_t s) {
   v->surf_cur = 0;
   v->taa_cur = 0;
   v->taa_valid = false;
+  v->trace_pending = false;
+  v->prev_den = nullptr;
+  v->prev_den_stride = 1;
+  v->has_prev_den = false;
   // Zero everything: cleared hash grid (restir_renderer.rs:296-306), empty queries.
   VLT_TRY(cudaMemsetAsync(v->pool.p, 0, v->pool.bytes, s));
   return VLT_OK;
@@ -279,9 +324,10 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
 namespace vlt {
 
 bool frame_inputs_ok(const vlt_view* v, const vlt_frame_inputs* in) {
-  if (!v || !in || !in->params || !in->depth || !in->gbuffer || !in->diff_hit_pos_normal ||
-      !in->diff_hit_radiance || !in->spec_hit_pos || !in->spec_hit_radiance)
+  if (!v || !in || !in->params || !in->depth || !in->gbuffer || !in->spec_hit_pos || !in->spec_hit_radiance)
     return false;
+  if (v->p.trace) return true;  // diffuse candidates come from the traced hits
+  if (!in->diff_hit_pos_normal || !in->diff_hit_radiance) return false;
   if (v->p.use_input_pdf && !in->diff_source_pdf) return false;
   return true;
 }
@@ -298,6 +344,7 @@ vlt_status record_frame(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame
 }
 
 int view_device(const vlt_view* v) { return v->ctx->device; }
+bool view_traced(const vlt_view* v) { return v->p.trace != 0; }
 uint32_t view_width(const vlt_view* v) { return v->w; }
 uint32_t view_height(const vlt_view* v) { return v->h; }
 int ctx_device(const vlt_ctx* c) { return c->device; }
@@ -522,6 +569,11 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
       {"spec_hit_pos", f16 ? nullptr : b.spec_hp[v->spec_prev], 16 * n},
       {"spec_reservoir", f16 ? nullptr : b.spec_rsv[v->spec_prev], 8 * n},
       {"spec_radiance", f16 ? nullptr : b.spec_rad[v->spec_prev], 4 * n},
+      // last frame's specular reservoir as this frame's passes left it (validated in
+      // traced mode); the spatial passes do not touch its slot
+      {"spec_prev_hit_pos", f16 || !v->frames ? nullptr : b.spec_hp[(v->spec_prev + 2) % 3], 16 * n},
+      {"spec_prev_reservoir", f16 || !v->frames ? nullptr : b.spec_rsv[(v->spec_prev + 2) % 3], 8 * n},
+      {"spec_prev_radiance", f16 || !v->frames ? nullptr : b.spec_rad[(v->spec_prev + 2) % 3], 4 * n},
       {"spec_record", f16 ? b.spec_hp[v->spec_prev] : nullptr, 24 * n},
       {"ao_history", b.ao[v->ao_prev], by(4, 8, 4) * n},
       {"ao_filtered", b.ao_filtered, by(2, 4, 2) * n},
@@ -558,6 +610,15 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
 static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out,
                                  cudaStream_t s, Recorder* rec) {
   if (!vlt::frame_inputs_ok(v, in) || !vlt::frame_outputs_ok(v, out)) return VLT_ERR_INVALID_ARG;
+  const bool traced = v->p.trace != 0;
+  if (traced) {
+    // Phase two of a traced frame: the hits of the rays vlt_frame_trace produced.
+    if (rec || !v->trace_pending || v->trace_frame != in->frame_index) return VLT_ERR_BAD_STATE;
+    if ((v->trace_cache && !in->cache_hits) || (v->trace_diff && !in->diffuse_hits) ||
+        (v->trace_spec && !in->spec_validate_hits))
+      return VLT_ERR_INVALID_ARG;
+    v->trace_pending = false;
+  }
   Exec ex;
   ex.stream = s;
   ex.rec = rec;
@@ -567,6 +628,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   ViewBuffers& b = v->b;
   const vlt_params& P = v->p;
   uint32_t launches = 0;
+  ex.launches = &launches;
 
   const bool has_prev = v->frames > 0;  // prev depth / gbuffer / indirect diffuse / reservoirs
   const float* prev_depth = has_prev && in->prev_depth ? in->prev_depth : b.prev_depth;
@@ -598,66 +660,100 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   GeoArgs pga = {prev_depth, nullptr, fp.prev_inv_view_proj, b.surf[sc ^ 1][0], b.surf[sc ^ 1][1],
                  b.surf[sc ^ 1][2]};
   STAGE("surface", launch_surface(ex, fp, w, h, in->depth, in->gbuffer, b.surf[sc][0], b.surf[sc][1], b.surf[sc][2]));
-  ++launches;
 
-  // Hash-grid radiance cache: decay, then (with history) select/compact/update of
-  // last frame's queries, then this frame's queries.
-  if (P.hg_enable) {
-    if (P.hg_decay) {
-      STAGE("hg_decay", launch_hg_decay(ex, v->hg, b.hg_decay, b.hg_storage));
-      ++launches;
-    }
-  }
-  if (has_prev) {
-    uint32_t seed_select = fr.next();
-    uint32_t seed_update = fr.next();
-    (void)seed_update;  // consumed by the (out-of-scope) cache ray generation
-    if (P.hg_enable) {
-      ex_fill32(ex, b.hg_sel, 0u, (size_t)v->hg.num_cells() * 4);
-      ex_fill32(ex, b.hg_ccount, 0u, 4);
-      STAGE("hg_select", launch_hg_select(ex, v->hg, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], b.hg_storage,
-                                          b.hg_sel, seed_select, b.hg_scratch));
-      STAGE("hg_compact", launch_hg_compact(ex, v->hg, b.hg_sel, b.hg_cidx, b.hg_caddr, b.hg_ccount));
-      STAGE("hg_update", launch_hg_update(ex, v->hg, b.hg_queries[v->hg_qcur], b.hg_cidx, b.hg_caddr, b.hg_ccount,
-                                          b.hg_storage, b.hg_decay));
-      launches += 6;
-      v->hg_qcur ^= 1;
-    }
-  }
-  if (P.hg_enable) {
-    STAGE("hg_emit", launch_hg_emit(ex, fp, w, h, v->hg, P.hg_key_mode, in->depth, in->diff_hit_pos_normal,
-                                    in->diff_hit_radiance, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur]));
-    ++launches;
-  }
-  (void)fr.next();  // Ind. Diff. Sample Gen.
-
-  // AO.
   const int form = (int)v->form;
   const bool f32 = form == FORM_F32;
   const bool f16 = form == FORM_F16;
   const size_t light_bytes = (f32 ? 16 : (f16 ? 8 : 4)) * n;
+  // Traced shading reads last frame's depth and denoised indirect diffuse, and the
+  // hash grid.
+  const ScreenCache scache = {prev_depth, v->prev_den, form, v->prev_den_stride, w, h};
+  const WorldCache wcache = {P.hg_enable ? (const uint4*)b.hg_storage : nullptr, v->hg.num_buckets() - 1u,
+                             P.hg_key_mode};
+  const uint32_t nq = P.hg_enable ? cache_rays(v) : 0u;
+  const bool diff_validation = traced && v->trace_diff == 2;
+
+  // Hash-grid radiance cache: decay, then (with history) select/compact/update of
+  // last frame's queries, then this frame's queries. In traced mode the first three
+  // ran in vlt_frame_trace; the update shades the traced hits.
+  if (P.hg_enable && P.hg_decay && !traced) {
+    STAGE("hg_decay", launch_hg_decay(ex, v->hg, b.hg_decay, b.hg_storage));
+  }
+  if (has_prev) {
+    uint32_t seed_select = fr.next();
+    uint32_t seed_update = fr.next();  // the cache rays (vlt_frame_trace)
+    (void)seed_update;
+    if (P.hg_enable && !traced) {
+      ex_fill32(ex, b.hg_sel, 0u, (size_t)v->hg.num_cells() * 4);
+      STAGE("hg_select", launch_hg_select(ex, v->hg, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], b.hg_storage,
+                                          b.hg_sel, seed_select, b.hg_scratch));
+      STAGE("hg_compact", launch_hg_compact(ex, v->hg, b.hg_sel, b.hg_cidx, b.hg_caddr, b.hg_ccount, b.scan));
+      STAGE("hg_update", launch_hg_update(ex, v->hg, b.hg_queries[v->hg_qcur], b.hg_cidx, b.hg_caddr, b.hg_ccount,
+                                          b.hg_storage, b.hg_decay));
+      v->hg_qcur ^= 1;
+    }
+    if (traced && v->trace_cache) {
+      STAGE("shade_cache", launch_shade_cache(ex, fp, nq, b.hg_ccount, v->trace_rays[0], in->cache_hits, scache, wcache,
+                                              b.cache_rad, b.q_staging));
+      STAGE("hg_update", launch_update_traced(ex, nq, b.hg_ccount, b.hg_caddr, b.cache_rad, b.hg_storage,
+                                              b.hg_decay));
+    }
+  }
+  if (P.hg_enable && !traced) {
+    STAGE("hg_emit", launch_hg_emit(ex, fp, w, h, v->hg, P.hg_key_mode, in->depth, in->diff_hit_pos_normal,
+                                    in->diff_hit_radiance, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur]));
+  }
+  // Ind. Diff. Sample Gen. (no seed on validation frames, restir_renderer.rs:460-494)
+  if (!diff_validation) (void)fr.next();
+  const uint32_t* diff_hpn = in->diff_hit_pos_normal;
+  const uint32_t* diff_rad = in->diff_hit_radiance;
+  if (traced) {
+    diff_hpn = b.tr_hpn;
+    diff_rad = b.tr_rad;
+    if (diff_validation) {
+      STAGE("diff_validate", launch_diff_validate_apply(ex, form, fp, w, h, prev_depth, b.diff_rsv[v->diff_prev],
+                                                        v->trace_rays[1], in->diffuse_hits, scache, wcache,
+                                                        b.q_staging + (size_t)nq * 8));
+    } else {
+      STAGE("shade_diff", launch_shade_diff(ex, fp, w, h, (has_prev && v->has_prev_den) ? 1u : 0u, v->trace_rays[1],
+                                            in->diffuse_hits, scache, wcache, b.tr_hpn, b.tr_rad,
+                                            b.q_staging + (size_t)nq * 8));
+    }
+  }
+  if (traced && v->trace_spec) {
+    // ind_spec_sample_validate.hlsl. It comes after the diffuse passes in the
+    // reference; it runs here, before the diffuse spatial pass overwrites the raw
+    // lighting that may serve as last frame's screen-space cache. Its inputs (last
+    // frame's specular reservoir, depth and lighting, the updated hash grid) are the
+    // same at both points.
+    const int sv = v->spec_prev;
+    STAGE("spec_validate", launch_spec_validate_apply(ex, form, fp, w, h, prev_depth, b.spec_rsv[sv], b.spec_hp[sv],
+                                                      b.spec_rad[sv], v->trace_rays[2], in->spec_validate_hits, scache,
+                                                      wcache, b.q_staging + (size_t)nq * 8 + n * 8));
+  }
+  const uint32_t has_new = diff_validation ? 0u : 1u;
+
+  // AO.
   int ao_cur = v->ao_prev ^ 1;
-  STAGE("ao_gen", launch_ao_gen(ex, form, fp, w, h, ga, in->diff_hit_pos_normal, b.ao[v->ao_prev], b.ao[ao_cur], 1u,
+  STAGE("ao_gen", launch_ao_gen(ex, form, fp, w, h, ga, diff_hpn, b.ao[v->ao_prev], b.ao[ao_cur], has_new,
                                 has_prev ? 1u : 0u, P.ao_radius));
   STAGE("ao_filter", launch_ao_filter(ex, form, w, h, in->depth, b.ao[ao_cur], b.ao_filtered));
-  launches += 2;
   v->ao_prev = ao_cur;
 
   // Indirect diffuse: temporal then spatial pass(es).
   DiffKnobs dk = diff_knobs(P);
+  if (traced) dk.use_input_pdf = 0;  // the reference's constant 1 / (2 pi)
   int p = v->diff_prev, t = (p + 1) % 3, o = (p + 2) % 3;
   uint32_t seed_dt = fr.next();
-  STAGE("diff_temporal", launch_diff_temporal(ex, form, fp, w, h, dk, ga, prev_depth, in->diff_hit_pos_normal,
-                                              in->diff_hit_radiance, in->diff_source_pdf, b.diff_rsv[p],
-                                              b.diff_rsv[t], seed_dt, has_prev ? 1u : 0u, 1u));
-  ++launches;
+  STAGE("diff_temporal", launch_diff_temporal(ex, form, fp, w, h, dk, ga, prev_depth, diff_hpn, diff_rad,
+                                              traced ? nullptr : in->diff_source_pdf, b.diff_rsv[p], b.diff_rsv[t],
+                                              seed_dt, has_prev ? 1u : 0u, has_new));
   int src = t, dst = o;
   for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
     bool last = k + 1 == P.diff_spatial_passes;
     uint32_t seed_ds = fr.next();
     STAGE("diff_spatial", launch_diff_spatial(ex, form, fp, w, h, dk, ga, b.ao_filtered, b.diff_rsv[src],
                                               b.diff_rsv[dst], last ? b.diff_light : nullptr, seed_ds));
-    ++launches;
     std::swap(src, dst);
   }
   v->diff_prev = P.diff_spatial_passes ? src : t;
@@ -665,12 +761,17 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   // Indirect specular.
   (void)fr.next();  // Ind. Spec. Sample Gen.
   int sp = v->spec_prev, st = (sp + 1) % 3, so = (sp + 2) % 3;
+  if (traced && P.hg_enable) {
+    // This frame's cache queries, in ray order, for next frame's update.
+    STAGE("query_append", launch_query_append(ex, b.q_staging, nq, (uint32_t)n, (uint32_t)n, v->trace_cache != 0u,
+                                              true, v->trace_spec != 0u, v->hg.max_queries,
+                                              b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], b.scan));
+  }
   uint32_t seed_st = fr.next();
   STAGE("spec_temporal", launch_spec_temporal(ex, form, fp, w, h, P.spec_m_cap, ga, pga, prev_depth, b.spec_rsv[sp],
                                               b.spec_hp[sp], b.spec_rad[sp], in->spec_hit_pos, in->spec_hit_radiance,
                                               b.spec_rsv[st], b.spec_hp[st], b.spec_rad[st], seed_st,
                                               has_prev ? 1u : 0u));
-  ++launches;
   {
     SpecKnobs sk = {P.spec_spatial_taps, P.spec_spatial_radius_px};
     int ssrc = st, sdst = so;
@@ -682,7 +783,6 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
                                 last ? b.spec_light : nullptr, last ? b.ray_len : nullptr,
                                 last ? nullptr : b.spec_rsv[sdst], last ? nullptr : b.spec_hp[sdst],
                                 last ? nullptr : b.spec_rad[sdst], seed_ss));
-      ++launches;
       std::swap(ssrc, sdst);
     }
   }
@@ -696,7 +796,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   // iteration writes no record when nothing reads it (both outputs given, no
   // final lighting), and never the variance it would pass on.
   const void* den = nullptr;
-  const bool keep_den = P.post >= 1 || !out || !out->diffuse || !out->specular;
+  const bool keep_den = P.post >= 1 || traced || !out || !out->diffuse || !out->specular;
   if (run_denoiser && (f32 || f16)) {
     DenoiseKnobs kn = {1.0f / P.history_max_frames, P.fast_history_clamp};
     uint32_t has_history = v->denoise_history ? 1u : 0u;
@@ -704,16 +804,13 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     STAGE("dn_temporal", launch_dn32_temporal(ex, form, fp, w, h, kn, ga, pga, b.diff_light, b.spec_light,
                                               prev_depth, b.rec[0], b.len[0], b.rec_fast[0], b.rec[2], b.len[1],
                                               b.rec_fast[1], has_history));
-    ++launches;
     float4* cur = b.rec[2];
     if (P.disocclusion_fix) {
       STAGE("dn_fix", launch_dn32_fix(ex, form, w, h, ga, b.len[1], b.rec[2], b.rec[1]));
-      ++launches;
       cur = b.rec[1];
     }
     if (P.fast_history_clamp) {
       STAGE("dn_fast_clamp", launch_dn32_fast_clamp(ex, form, w, h, b.rec_fast[1], cur));
-      ++launches;
       std::swap(b.rec_fast[0], b.rec_fast[1]);
       v->fast_history_valid = true;
     } else {
@@ -727,7 +824,6 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     std::swap(b.len[0], b.len[1]);
     v->denoise_history = true;
     STAGE("dn_fallback", launch_dn32_fallback(ex, form, w, h, ga, b.len[0], b.rec[0], b.rec[4]));
-    ++launches;
     float4* rsrc = b.rec[4];
     float4* rdst = b.rec[2];
     const uint32_t iters = P.atrous_iterations;
@@ -737,7 +833,6 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
       void* os = last && out ? out->specular : nullptr;
       void* ro = last && !keep_den ? nullptr : (void*)rdst;
       STAGE("dn_atrous", launch_dn32_atrous(ex, form, w, h, ga, rsrc, ro, od, os, 1 << k));
-      ++launches;
       rsrc = rdst;
       rdst = rdst == b.rec[2] ? b.rec[3] : b.rec[2];
     }
@@ -759,16 +854,13 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
                                             (const uint32_t*)b.spec_light, b.ray_len, prev_depth, b.color[0],
                                             b.mom[0], (const uint8_t*)b.len[0], b.fast[0], b.color[2], b.mom[2],
                                             (uint8_t*)b.len[1], b.fast[1], has_history));
-    ++launches;
     uint32_t* cur_color = b.color[2];
     if (P.disocclusion_fix) {
       STAGE("dn_fix", launch_dn_fix(ex, w, h, ga, (const uint8_t*)b.len[1], b.color[2], b.mom[2], b.color[1], b.mom[1]));
-      ++launches;
       cur_color = b.color[1];
     }
     if (P.fast_history_clamp) {
       STAGE("dn_fast_clamp", launch_dn_fast_clamp(ex, w, h, b.fast[1], cur_color));
-      ++launches;
       std::swap(b.fast[0], b.fast[1]);
       v->fast_history_valid = true;
     } else {
@@ -787,7 +879,6 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     // Now color[0]/mom[0]/len[0] hold this frame's history.
     STAGE("dn_fallback", launch_dn_fallback(ex, w, h, ga, (const uint8_t*)b.len[0], b.color[0], b.mom[0], b.color_c,
                                             b.var[0]));
-    ++launches;
     uint32_t* csrc = b.color_c;
     uint32_t* vsrc = b.var[0];
     uint32_t* cdst = b.color[2];
@@ -799,7 +890,6 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
       uint32_t* os = last && out ? (uint32_t*)out->specular : nullptr;
       uint32_t* co = last && !keep_den ? nullptr : cdst;
       STAGE("dn_atrous", launch_dn_atrous(ex, w, h, ga, csrc, vsrc, co, last ? nullptr : vdst, od, os, 1 << k));
-      ++launches;
       std::swap(csrc, cdst);
       uint32_t* vnext = vdst == b.var[1] ? b.var[2] : b.var[1];
       vsrc = vdst;
@@ -808,7 +898,6 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     den = keep_den ? (const void*)csrc : nullptr;
     if (iters == 0 && out && (out->diffuse || out->specular)) {
       launch_split_color(ex, w, h, csrc, (uint32_t*)out->diffuse, (uint32_t*)out->specular);
-      ++launches;
     }
   } else {
     v->denoise_history = false;  // Denoiser::reset
@@ -831,12 +920,10 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     void* color = out && out->color ? out->color : b.lit;
     STAGE("final_lighting", launch_final_lighting(ex, form, fp, w, h, in->gbuffer, in->shadow_mask, dsrc, ssrc,
                                                   den ? 2 : 1, color));
-    ++launches;
     if (P.post >= 2) {
       const int tc = v->taa_cur ^ 1;
       STAGE("taa", launch_taa(ex, form, fp, w, h, in->depth, color, b.taa[v->taa_cur], b.taa[tc],
                               out ? out->taa : nullptr, v->taa_valid ? 1u : 0u));
-      ++launches;
       v->taa_cur = tc;
       v->taa_valid = true;
     }
@@ -846,13 +933,85 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   // frame's decoded G-buffer fields stay in the other surface slot).
   if (!in->prev_depth) ex_copy(ex, b.prev_depth, in->depth, 4 * n);
   v->surf_cur = sc;
+  // The screen-space radiance cache of the next traced frame
+  // (RestirRenderer::prev_indirect_diffuse_texture, restir_renderer.rs:819-820).
+  v->prev_den = den ? den : b.diff_light;
+  v->prev_den_stride = den ? 2 : 1;
+  v->has_prev_den = true;
   v->frames += 1;
   v->launches = launches;
 #undef STAGE
   return cuda_status(cudaGetLastError());
 }
 
+// Phase one of a traced frame: the hash grid's decay, query selection and ordered
+// compaction (they come first in RestirRenderer::add_passes), then the rays.
+static vlt_status frame_trace_impl(vlt_view* v, const vlt_frame_inputs* in, vlt_frame_rays* rays, cudaStream_t s) {
+  if (!v || !in || !rays || !v->p.trace || !in->params || !in->depth || !in->gbuffer) return VLT_ERR_INVALID_ARG;
+  const vlt_params& P = v->p;
+  if (!rays->diffuse || (P.hg_enable && !rays->cache) || (P.spec_validate && !rays->spec_validate))
+    return VLT_ERR_INVALID_ARG;
+  Exec ex;
+  ex.stream = s;
+  uint32_t launches = 0;
+  ex.launches = &launches;
+  const vlt_frame_params& fp = *in->params;
+  const int w = (int)v->w, h = (int)v->h;
+  ViewBuffers& b = v->b;
+  const bool has_prev = v->frames > 0;
+  const float* prev_depth = has_prev && in->prev_depth ? in->prev_depth : b.prev_depth;
+  FrameRand fr = {in->frame_index};
+  const uint32_t nq = P.hg_enable ? cache_rays(v) : 0u;
+  if (P.hg_enable && P.hg_decay) launch_hg_decay(ex, v->hg, b.hg_decay, b.hg_storage);
+  v->trace_cache = 0;
+  if (has_prev) {
+    const uint32_t seed_select = fr.next();
+    const uint32_t seed_update = fr.next();
+    if (P.hg_enable) {
+      ex_fill32(ex, b.hg_sel, 0u, (size_t)v->hg.num_cells() * 4);
+      launch_hg_select(ex, v->hg, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], b.hg_storage, b.hg_sel,
+                       seed_select, b.hg_scratch);
+      launch_hg_compact(ex, v->hg, b.hg_sel, b.hg_cidx, b.hg_caddr, b.hg_ccount, b.scan);
+      launch_ray_cache(ex, nq, b.hg_queries[v->hg_qcur], b.hg_cidx, b.hg_ccount, seed_update, rays->cache);
+      v->hg_qcur ^= 1;
+      v->trace_cache = 1;
+    }
+  }
+  // Validation frames (restir_renderer.rs:450-453) re-trace last frame's samples
+  // and take no new ones.
+  const bool validate = P.diff_validate && has_prev && (in->frame_index & 3u) == 0u;
+  if (validate) {
+    launch_diff_validate_rays(ex, (int)v->form, fp, w, h, prev_depth, b.diff_rsv[v->diff_prev], rays->diffuse);
+  } else {
+    launch_ray_diff(ex, fp, w, h, in->depth, in->gbuffer, fr.next(), rays->diffuse);
+  }
+  v->trace_diff = validate ? 2u : 1u;
+  v->trace_spec = 0;
+  if (P.spec_validate && has_prev) {
+    const int sp = v->spec_prev;
+    launch_spec_validate_rays(ex, (int)v->form, fp, w, h, prev_depth, b.spec_rsv[sp], b.spec_hp[sp], b.spec_rad[sp],
+                              rays->spec_validate);
+    v->trace_spec = 1;
+  }
+  v->trace_rays[0] = rays->cache;
+  v->trace_rays[1] = rays->diffuse;
+  v->trace_rays[2] = rays->spec_validate;
+  rays->n_cache = v->trace_cache ? nq : 0u;
+  rays->n_diffuse = (uint32_t)w * (uint32_t)h;
+  rays->n_spec_validate = v->trace_spec ? (uint32_t)w * (uint32_t)h : 0u;
+  rays->diffuse_kind = v->trace_diff;
+  v->trace_pending = true;
+  v->trace_frame = in->frame_index;
+  return cuda_status(cudaGetLastError());
+}
+
 extern "C" {
+
+vlt_status vlt_frame_trace(vlt_view* v, const vlt_frame_inputs* in, vlt_frame_rays* rays, void* stream) {
+  return frame_trace_impl(v, in, rays, (cudaStream_t)stream);
+}
+
+uint32_t vlt_view_cache_ray_capacity(const vlt_view* v) { return v && v->p.hg_enable ? cache_rays(v) : 0u; }
 
 vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out, void* stream) {
   return frame_run_impl(v, in, out, (cudaStream_t)stream, nullptr);
@@ -1078,7 +1237,8 @@ vlt_status vlt_hg_query_compact(uint32_t log2_buckets, uint32_t max_queries, con
       !rw_compact_count)
     return VLT_ERR_INVALID_ARG;
   HashGridDims d = {log2_buckets, max_queries};
-  launch_hg_compact(stream_exec(stream), d, selection, rw_compact_query_index, rw_compact_cell_addr, rw_compact_count);
+  launch_hg_compact(stream_exec(stream), d, selection, rw_compact_query_index, rw_compact_cell_addr, rw_compact_count,
+                    nullptr);
   return cuda_status(cudaGetLastError());
 }
 

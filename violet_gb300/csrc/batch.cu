@@ -227,7 +227,7 @@ vlt_status vlt_batch_run(vlt_batch* b, vlt_view* const* views, const vlt_frame_i
   if (n == 0) return VLT_OK;
   const int dev = ctx_device(b->ctx);
   for (uint32_t k = 0; k < n; ++k) {
-    if (!views[k] || view_device(views[k]) != dev || !frame_inputs_ok(views[k], &inputs[k]) ||
+    if (!views[k] || view_device(views[k]) != dev || view_traced(views[k]) || !frame_inputs_ok(views[k], &inputs[k]) ||
         !frame_outputs_ok(views[k], outputs ? &outputs[k] : nullptr))
       return VLT_ERR_INVALID_ARG;
     for (uint32_t j = 0; j < k; ++j)

@@ -15,47 +15,11 @@
 //       resolves every listed query with that checksum.
 #include <mutex>
 
+#include "hashgrid.cuh"
+#include "vlt_compact.cuh"
 #include "vlt_internal.h"
 
 namespace vlt {
-
-// Query record, 8 words.
-enum { Q_PX = 0, Q_PY = 1, Q_PZ = 2, Q_NRM = 3, Q_HASH = 4, Q_CHECK = 5, Q_RAD = 6, Q_WORDS = 8 };
-// Cell record, 4 words: checksum, radiance xyz.
-
-struct VertexKey {
-  uint32_t hash;
-  uint32_t checksum;
-};
-
-// VertexDescriptor::create/hash/checksum (hash_grid.inc.hlsl:32-105). key_mode 1
-// adds the normal octant to both hashes.
-__device__ __forceinline__ VertexKey vertex_key(f3 pos, f3 nrm, f3 cam, uint32_t bucket_mask, uint32_t key_mode) {
-  f3 d = pos - cam;
-  float dist_sq = dot3(d, d);
-  float lodf = fmax_(0.5f * log2_(dist_sq), 0.0f);
-  uint32_t lod = f2u_rz(lodf);
-  lod = lod < 31u ? lod : 31u;
-  float cell_size = 0.0625f * (float)(1u << lod);
-  float inv = 1.0f / cell_size;
-  int32_t qx = f2i_rz(floor_(pos.x * inv));
-  int32_t qy = f2i_rz(floor_(pos.y * inv));
-  int32_t qz = f2i_rz(floor_(pos.z * inv));
-  uint32_t ux = (uint32_t)qx, uy = (uint32_t)qy, uz = (uint32_t)qz;
-  uint32_t p0 = ux ^ (uy << 22);
-  uint32_t p1 = (uy >> 10) ^ (uz << 22);
-  XXHash32 hh = XXHash32::init(p0).add(p1).add(lod);
-  XXHash32 hc = XXHash32::init(uy).add(uz).add(ux).add(lod);
-  if (key_mode == 1) {
-    uint32_t oct = (nrm.x < 0.0f ? 1u : 0u) | (nrm.y < 0.0f ? 2u : 0u) | (nrm.z < 0.0f ? 4u : 0u);
-    hh = hh.add(oct);
-    hc = hc.add(oct);
-  }
-  VertexKey k;
-  k.hash = hh.eval() & bucket_mask;
-  k.checksum = hc.eval() | 1u;
-  return k;
-}
 
 // --------------------------------------------------------------- emission
 
@@ -281,8 +245,8 @@ struct HgSelResolveF {
 
 // ----------------------------------------------------------------- compact
 
-// hash_grid_query_compact.hlsl:23-63: block-local append in cell order, one
-// global atomic per block.
+// hash_grid_query_compact.hlsl:23-63 as the shader does it: block-local append in
+// cell order, one global atomic per block (the blocks' order varies from run to run).
 struct HgCompactF {
   static __device__ __forceinline__ void run(int x0, int y0, uint32_t num_cells, uint32_t qmask, const uint32_t* __restrict__ selection, uint32_t* __restrict__ idx, uint32_t* __restrict__ addr, uint32_t* __restrict__ count) {
   __shared__ uint32_t warp_cnt[kMaxThreads / 32];
@@ -310,6 +274,23 @@ struct HgCompactF {
     addr[pos] = c;
   }
 }
+};
+
+// hash_grid_query_compact.hlsl:23-63: the selected queries of all cells, listed in
+// cell order (the shader appends per block through one atomic, so its order varies
+// from run to run; the traced cache update derives each ray from the list position).
+struct HgCompactSel {
+  struct Args {
+    const uint32_t* selection;
+    uint32_t qmask;
+    uint32_t* idx;
+    uint32_t* addr;
+  };
+  static __device__ __forceinline__ bool flag(const Args& a, uint32_t c) { return a.selection[c] != 0u; }
+  static __device__ __forceinline__ void emit(const Args& a, uint32_t c, uint32_t rank) {
+    a.idx[rank] = a.selection[c] & a.qmask;
+    a.addr[rank] = c;
+  }
 };
 
 // ------------------------------------------------------------------ update
@@ -389,10 +370,15 @@ void launch_hg_select(const Exec& ex, const HashGridDims& d, const uint32_t* que
 }
 
 void launch_hg_compact(const Exec& ex, const HashGridDims& d, const uint32_t* selection, uint32_t* idx,
-                       uint32_t* addr, uint32_t* count) {
-  uint32_t nc = d.num_cells();
-  uint32_t qmask = (1u << d.query_bits()) - 1u;
-  launch1d<HgCompactF>(ex, "hg_compact", nc, nc, qmask, selection, idx, addr, count);
+                       uint32_t* addr, uint32_t* count, uint32_t* scratch) {
+  if (!scratch) {
+    uint32_t nc = d.num_cells();
+    uint32_t qmask = (1u << d.query_bits()) - 1u;
+    launch1d<HgCompactF>(ex, "hg_compact", nc, nc, qmask, selection, idx, addr, count);
+    return;
+  }
+  HgCompactSel::Args a = {selection, (1u << d.query_bits()) - 1u, idx, addr};
+  launch_compact<HgCompactSel>(ex, "hg_compact", d.num_cells(), a, scratch, count);
 }
 
 void launch_hg_update(const Exec& ex, const HashGridDims& d, const uint32_t* queries, const uint32_t* idx,

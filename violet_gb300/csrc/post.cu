@@ -3,8 +3,7 @@
 // (restir_renderer.rs:897-948). Colour images follow the view's storage form:
 // R11G11B10 (reference form, the reference's B10G11R11_UFLOAT scene colour),
 // float4 {rgb, 0} (f32 form) or half4 {rgb, 0} (f16 form, saturating stores).
-#include "brdf.cuh"
-#include "vlt_internal.h"
+#include "vlt_internal.h"  // brdf.cuh, trace.cuh (eval_ggx_lambertian)
 
 namespace vlt {
 
@@ -38,22 +37,6 @@ struct ColorIO<FORM_F16> {
     p[i] = make_uint2(f32tof16_sat(v.x) | (f32tof16_sat(v.y) << 16), f32tof16_sat(v.z));
   }
 };
-
-// eval_GGX_Lambertian (brdf.hlsl:154-177).
-__device__ __forceinline__ f3 eval_ggx_lambertian(f3 v, f3 l, f3 n, float prc, f3 rho, f3 f0) {
-  f3 hv = normalize3(v + l);
-  float nol = saturate(dot3(n, l));
-  float nov = saturate(dot3(n, v));
-  float noh = saturate(dot3(n, hv));
-  float loh = saturate(dot3(l, hv));
-  float roughness = prc * prc;
-  float D = d_ggx(noh, roughness);
-  f3 F = f_schlick(loh, f0);
-  float V = vis_smith_g2(nol, nov, roughness);
-  f3 fr = fmin_(D * V, 1e19f) * F;  // F32_SIGNIFICANTLY_LARGE
-  f3 fd = rho * VLT_ONE_OVER_PI;
-  return fd + fr;
-}
 
 }  // namespace
 

@@ -5,6 +5,7 @@
 // binary32 contract of vlt_math.cuh. Kernels are templated on the geometry source
 // (GeoRaw for the per-pass entry points, GeoSurface for the frame driver).
 #include "brdf.cuh"
+#include "trace.cuh"
 #include "vlt_internal.h"
 
 
@@ -946,6 +947,157 @@ struct SpecSpatialF {
 }
 };
 
+
+// ------------------------------------------------------ sample validation
+
+// Read-only views of the writable reservoir pointers.
+template <class T>
+__device__ __forceinline__ const T* as_const(T* p) { return p; }
+__device__ __forceinline__ DiffF16CPtr as_const(DiffF16Ptr p) { return DiffF16CPtr{p.main, p.m}; }
+__device__ __forceinline__ SpecPlanesC as_const(SpecPlanes p) { return SpecPlanesC{p.rsv, p.hp, p.rad}; }
+
+// Diffuse reservoir access for validation, all forms: the reference form keeps the
+// packed reservoir word when M does not change.
+struct DiffVal {
+  uint32_t M, word;
+  float W;
+  f3 pos, nrm, rad;
+};
+__device__ __forceinline__ DiffVal dval_load(const uint4* p, size_t i) {
+  const uint4 u = p[i];
+  DiffVal r;
+  r.word = u.x;
+  r.M = rsv_decode_M(u.x);
+  r.W = rsv_decode_W(u.x);
+  r.pos = hpn_pos(u.y, u.z);
+  r.nrm = hpn_normal(u.z);
+  r.rad = unpack_r11g11b10(u.w);
+  return r;
+}
+template <class CPtr>
+__device__ __forceinline__ DiffVal dval_load(CPtr p, size_t i) {
+  DiffVal r;
+  diff_load(p, i, &r.M, &r.W, &r.pos, &r.nrm, &r.rad);
+  r.word = 0u;
+  return r;
+}
+__device__ __forceinline__ void dval_store(uint4* p, size_t i, const DiffVal& r, bool rescaled) {
+  uint32_t e[2];
+  hpn_encode(r.pos, r.nrm, e);
+  p[i] = make_uint4(rescaled ? rsv_encode_32b(r.M, r.W) : r.word, e[0], e[1], pack_r11g11b10(r.rad));
+}
+template <class Ptr>
+__device__ __forceinline__ void dval_store(Ptr p, size_t i, const DiffVal& r, bool) {
+  diff_store(p, i, r.M, r.W, r.pos, r.nrm, r.rad);
+}
+
+// ind_diff_sample_validate.hlsl:30-49: re-trace last frame's sample from last
+// frame's surface point.
+template <int FORM>
+struct DiffValidateRayF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, const float* __restrict__ prev_depth, typename DiffStore<FORM>::CPtr rsv, float4* __restrict__ rays) {
+  const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
+  if (!inb(x, y, w, h)) return;
+  const size_t i = (size_t)y * w + x;
+  const float d = prev_depth[i];
+  if (d == 0.0f) {
+    ray_store_none(rays, i);
+    return;
+  }
+  const DiffVal r = dval_load(rsv, i);
+  const f3 origin = depth_to_position(fp.prev_inv_view_proj, x, y, w, h, d);  // cs_prev_depth_to_position
+  ray_store(rays, i, origin, normalize3(r.pos - origin), true);
+}
+};
+
+// ind_diff_sample_validate.hlsl:51-77: scale M down by the relative luminance change
+// (to 0 when the hit point moved), then store the re-traced hit and radiance.
+template <int FORM>
+struct DiffValidateApplyF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, const float* __restrict__ prev_depth, typename DiffStore<FORM>::Ptr rsv, const float4* __restrict__ rays, const float4* __restrict__ hits, ScreenCache sc, WorldCache wc, uint32_t* __restrict__ staging) {
+  const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
+  if (!inb(x, y, w, h)) return;
+  const size_t i = (size_t)y * w + x;
+  uint32_t q[8];
+  if (prev_depth[i] == 0.0f) {
+    for (int j = 0; j < 8; ++j) q[j] = 0u;
+    query_store(staging, i, q);
+    return;
+  }
+  DiffVal r = dval_load(as_const(rsv), i);
+  const TRay ray = ray_load(rays, i);
+  const Traced t = trace_shade(fp, ray, hit_load(hits, i), true, sc, wc, q);
+  query_store(staging, i, q);
+  const float lumi_prev = luminance(r.rad);
+  const float lumi_diff = luminance(abs3(t.radiance - r.rad));
+  const float prev_ray_len = length3(r.pos - ray.o);
+  const f3 dp = abs3(r.pos - t.pos);
+  const bool pos_changed = fmax_(fmax_(dp.x, dp.y), dp.z) > fmax_(prev_ray_len / 128.0f, 0.01f);
+  float m_scale = saturate(1.0f - (1.0f * lumi_diff) / lumi_prev);  // RADIANCE_DIFF_MULTIPLIER 1
+  m_scale = pos_changed ? 0.0f : m_scale;
+  const bool rescale = lumi_prev > 0.0f && m_scale <= (1.0f - 0.5f / 32.0f);
+  if (rescale) r.M = f2u_rz(floor_((float)r.M * m_scale));
+  r.pos = t.pos;
+  r.nrm = t.normal;
+  r.rad = t.radiance;
+  dval_store(rsv, i, r, rescale);
+}
+};
+
+// ind_spec_sample_validate.hlsl:19-44: re-trace last frame's specular sample from
+// last frame's surface point (depth nudged by one 24-bit unorm step).
+template <int FORM>
+struct SpecValidateRayF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, const float* __restrict__ prev_depth, typename SpecStore<FORM>::CPtr prev, float4* __restrict__ rays) {
+  const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
+  if (!inb(x, y, w, h)) return;
+  const size_t i = (size_t)y * w + x;
+  const float d = prev_depth[i];
+  if (d == 0.0f) {
+    ray_store_none(rays, i);
+    return;
+  }
+  const float depth_error = 1.0f / 16777216.0f;
+  const float sx = ((float)x + 0.5f) / (float)w, sy = ((float)y + 0.5f) / (float)h;
+  const f4 p = mul44(fp.prev_inv_view_proj, mk4(sx * 2.0f - 1.0f, sy * 2.0f - 1.0f, d + depth_error, 1.0f));
+  const f3 pos = mk3(p.x / p.w, p.y / p.w, p.z / p.w);
+  const SpecSample s = spec_ld(prev, x, y, w, h);
+  ray_store(rays, i, pos, normalize3(s.hit - pos), true);
+}
+};
+
+// ind_spec_sample_validate.hlsl:46-61: a sample whose radiance changed by more than
+// half of the larger maximum component restarts at M = 1 with the new hit point and
+// radiance (its stored target function is kept).
+template <int FORM>
+struct SpecValidateApplyF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, const float* __restrict__ prev_depth, typename SpecStore<FORM>::Ptr prev, const float4* __restrict__ rays, const float4* __restrict__ hits, ScreenCache sc, WorldCache wc, uint32_t* __restrict__ staging) {
+  const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
+  if (!inb(x, y, w, h)) return;
+  const size_t i = (size_t)y * w + x;
+  uint32_t q[8];
+  if (prev_depth[i] == 0.0f) {
+    for (int j = 0; j < 8; ++j) q[j] = 0u;
+    query_store(staging, i, q);
+    return;
+  }
+  SpecSample s = spec_ld(as_const(prev), x, y, w, h);
+  const Traced t = trace_shade(fp, ray_load(rays, i), hit_load(hits, i), true, sc, wc, q);
+  query_store(staging, i, q);
+  float mr = fmax_(fmax_(t.radiance.x, t.radiance.y), t.radiance.z);
+  mr = fmax_(mr, fmax_(fmax_(s.rad.x, s.rad.y), s.rad.z));
+  const f3 dr = abs3(t.radiance - s.rad);
+  const float lim = 0.5f * mr;
+  if (dr.x > lim || dr.y > lim || dr.z > lim) {
+    s.M = 1u;
+    s.hit = t.pos;
+    s.rad = t.radiance;
+    s.rad_bits = pack_r11g11b10(t.radiance);
+    spec_st(prev, i, s);
+  }
+}
+};
+
 // ------------------------------------------------------------- launchers
 
 static GeoRaw raw_geo(const GeoArgs& a, int w, int h) {
@@ -1100,5 +1252,58 @@ void launch_spec_spatial(const Exec& ex, int form, const vlt_frame_params& fp, i
 }
 
 #undef VLT_GEO_DISPATCH
+
+
+void launch_diff_validate_rays(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h,
+                               const float* prev_depth, const void* rsv, void* rays) {
+  if (form == FORM_F32)
+    launch2d<DiffValidateRayF<FORM_F32>>(ex, "ray_diff_validate", w, h, fp, w, h, prev_depth, (const DiffF32*)rsv,
+                                         (float4*)rays);
+  else if (form == FORM_F16)
+    launch2d<DiffValidateRayF<FORM_F16>>(ex, "ray_diff_validate", w, h, fp, w, h, prev_depth,
+                                         diff_f16_cptr(rsv, w, h), (float4*)rays);
+  else
+    launch2d<DiffValidateRayF<FORM_REF>>(ex, "ray_diff_validate", w, h, fp, w, h, prev_depth, (const uint4*)rsv,
+                                         (float4*)rays);
+}
+
+void launch_diff_validate_apply(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h,
+                                const float* prev_depth, void* rsv, const void* rays, const void* hits,
+                                const ScreenCache& sc, const WorldCache& wc, uint32_t* staging) {
+  if (form == FORM_F32)
+    launch2d<DiffValidateApplyF<FORM_F32>>(ex, "diff_validate", w, h, fp, w, h, prev_depth, (DiffF32*)rsv,
+                                           (const float4*)rays, (const float4*)hits, sc, wc, staging);
+  else if (form == FORM_F16)
+    launch2d<DiffValidateApplyF<FORM_F16>>(ex, "diff_validate", w, h, fp, w, h, prev_depth, diff_f16_ptr(rsv, w, h),
+                                           (const float4*)rays, (const float4*)hits, sc, wc, staging);
+  else
+    launch2d<DiffValidateApplyF<FORM_REF>>(ex, "diff_validate", w, h, fp, w, h, prev_depth, (uint4*)rsv,
+                                           (const float4*)rays, (const float4*)hits, sc, wc, staging);
+}
+
+void launch_spec_validate_rays(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h,
+                               const float* prev_depth, const uint32_t* rsv, const float* hp, const uint32_t* rad,
+                               void* rays) {
+  if (form == FORM_F16) {
+    launch2d<SpecValidateRayF<FORM_F16>>(ex, "ray_spec_validate", w, h, fp, w, h, prev_depth, (const SpecF16*)hp,
+                                         (float4*)rays);
+  } else {
+    SpecPlanesC p = {(const uint2*)rsv, (const float4*)hp, rad};
+    launch2d<SpecValidateRayF<FORM_REF>>(ex, "ray_spec_validate", w, h, fp, w, h, prev_depth, p, (float4*)rays);
+  }
+}
+
+void launch_spec_validate_apply(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h,
+                                const float* prev_depth, uint32_t* rsv, float* hp, uint32_t* rad, const void* rays,
+                                const void* hits, const ScreenCache& sc, const WorldCache& wc, uint32_t* staging) {
+  if (form == FORM_F16) {
+    launch2d<SpecValidateApplyF<FORM_F16>>(ex, "spec_validate", w, h, fp, w, h, prev_depth, (SpecF16*)hp,
+                                           (const float4*)rays, (const float4*)hits, sc, wc, staging);
+  } else {
+    SpecPlanes p = {(uint2*)rsv, (float4*)hp, rad};
+    launch2d<SpecValidateApplyF<FORM_REF>>(ex, "spec_validate", w, h, fp, w, h, prev_depth, p, (const float4*)rays,
+                                           (const float4*)hits, sc, wc, staging);
+  }
+}
 
 }  // namespace vlt

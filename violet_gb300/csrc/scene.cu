@@ -163,10 +163,12 @@ void fill_params(const Desc& d, uint32_t frame, vlt_frame_params* out) {
     out->jitter[2] = prev.jitter.x;
     out->jitter[3] = prev.jitter.y;
   }
-  // Sun of restir_render_loop.rs:300 (unused by the back end).
-  out->sun_dir[0] = 0.3f;
-  out->sun_dir[1] = 0.9f;
-  out->sun_dir[2] = 0.3f;
+  // Sun of restir_render_loop.rs:300-314: intensity (1, 1, 0.85) * 20 and a unit
+  // direction (the final lighting and the traced shading use it).
+  const f3 sd = normalize3(mk3(0.3f, 0.9f, 0.3f));
+  out->sun_dir[0] = sd.x;
+  out->sun_dir[1] = sd.y;
+  out->sun_dir[2] = sd.z;
   out->sun_inten[0] = 20.0f;
   out->sun_inten[1] = 20.0f;
   out->sun_inten[2] = 17.0f;
@@ -206,6 +208,16 @@ __global__ void k_scene_c(Desc d, uint32_t frame, vlt_scene_frame f) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.width * d.height) return;
   f.depth[i] = disocclude(d, frame, i, f.depth[i]);
+}
+
+__global__ void k_scene_trace(Object o, uint64_t seed, f3 sun, const float* __restrict__ rays, uint32_t n,
+                              float* __restrict__ hits) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float out[16];
+  trace_hit(o, seed, sun, rays + (size_t)i * 8, out);
+  float4* hp = (float4*)(hits + (size_t)i * 16);
+  for (int k = 0; k < 4; ++k) hp[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
 }
 
 bool valid_frame(const vlt_scene_frame* f) {
@@ -264,6 +276,30 @@ vlt_status vlt_scene_generate_host(const vlt_scene_desc* dd, uint32_t frame, con
   });
   for (size_t i = 0; i < plane; ++i) fr.depth[i] = disocclude(d, frame, (uint32_t)i, fr.depth[i]);
   return VLT_OK;
+}
+
+vlt_status vlt_scene_trace_host(const vlt_scene_desc* dd, const vlt_frame_params* fp, const vlt_ray* rays,
+                                uint32_t n, vlt_ray_hit* hits) {
+  if (!dd || !fp || (n && (!rays || !hits))) return VLT_ERR_INVALID_ARG;
+  Object o = make_object(dd->seed);
+  const f3 sun = mk3(fp->sun_dir[0], fp->sun_dir[1], fp->sun_dir[2]);
+  const uint32_t rows = (n + 1023) / 1024;
+  parallel_rows(rows, [&](uint32_t r) {
+    for (uint32_t i = r * 1024; i < n && i < (r + 1) * 1024; ++i)
+      trace_hit(o, dd->seed, sun, (const float*)(rays + i), (float*)(hits + i));
+  });
+  return VLT_OK;
+}
+
+vlt_status vlt_scene_trace_device(const vlt_scene_desc* dd, const vlt_frame_params* fp, const vlt_ray* rays,
+                                  uint32_t n, vlt_ray_hit* hits, void* stream) {
+  if (!dd || !fp || (n && (!rays || !hits))) return VLT_ERR_INVALID_ARG;
+  if (n == 0) return VLT_OK;
+  Object o = make_object(dd->seed);
+  const f3 sun = mk3(fp->sun_dir[0], fp->sun_dir[1], fp->sun_dir[2]);
+  k_scene_trace<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(o, dd->seed, sun, (const float*)rays, n,
+                                                                    (float*)hits);
+  return cuda_status(cudaGetLastError());
 }
 
 vlt_status vlt_scene_generate_device(const vlt_scene_desc* dd, uint32_t frame, const vlt_scene_frame* f,

@@ -398,5 +398,36 @@ VLT_HD float disocclude(const Desc& d, uint32_t frame, uint32_t pix, float depth
   return depth;
 }
 
+// The scene as the caller's ray tracer in traced mode: one vlt_ray_hit record (16
+// words) for a ray. A hit carries the surface, its material and whether a shadow
+// ray toward the sun escapes; a miss carries a sky gradient. tmax < 0: zeros.
+VLT_HD f3 sky_radiance(f3 dir) {
+  float up = fmax_(dir.y, 0.0f);
+  return mk3(0.4f + 0.5f * up, 0.5f + 0.6f * up, 0.7f + 0.9f * up);
+}
+VLT_HD void trace_hit(const Object& o, uint64_t seed, f3 sun, const float* ray, float* out) {
+  for (int k = 0; k < 16; ++k) out[k] = 0.0f;
+  if (!(ray[7] >= 0.0f)) return;
+  const f3 org = mk3(ray[0], ray[1], ray[2]), dir = mk3(ray[4], ray[5], ray[6]);
+  Hit h = trace(o, org, dir);
+  if (h.obj < 0) {
+    f3 c = sky_radiance(dir);
+    out[3] = as_float(1u);  // missed
+    out[12] = c.x, out[13] = c.y, out[14] = c.z;
+    return;
+  }
+  f3 color;
+  float metallic, rough;
+  material(seed, h.obj, h.p, &color, &metallic, &rough);
+  Hit sh = trace(o, h.p + 0.01f * h.n, sun);
+  out[0] = h.p.x, out[1] = h.p.y, out[2] = h.p.z;
+  out[4] = h.n.x, out[5] = h.n.y, out[6] = h.n.z;
+  out[7] = as_float(sh.obj < 0 ? 1u : 0u);  // sun visible
+  out[8] = h.n.x, out[9] = h.n.y, out[10] = h.n.z;
+  out[11] = metallic;
+  out[12] = color.x, out[13] = color.y, out[14] = color.z;
+  out[15] = rough;
+}
+
 }  // namespace scene
 }  // namespace vlt

@@ -169,7 +169,7 @@ vlt_batch* vlt_server_batch(vlt_server* s) { return s ? s->batch : nullptr; }
 
 vlt_status vlt_server_open(vlt_server* s, uint32_t width, uint32_t height, vlt_form form, const vlt_params* params,
                            uint64_t* session) {
-  if (!s || !params || !session || width == 0 || height == 0) return VLT_ERR_INVALID_ARG;
+  if (!s || !params || !session || width == 0 || height == 0 || params->trace) return VLT_ERR_INVALID_ARG;
   size_t bytes = vlt_view_device_bytes(width, height, form, params);
   if (bytes == 0) return VLT_ERR_INVALID_ARG;
   if (bytes > s->cfg.hbm_budget_bytes) return VLT_ERR_BUDGET_EXCEEDED;  // could never be admitted

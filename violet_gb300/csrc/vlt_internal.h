@@ -7,6 +7,7 @@
 #include "../../include/vlt.h"
 #include "vlt_device.cuh"
 #include "vlt_launch.cuh"
+#include "trace.cuh"
 
 namespace vlt {
 
@@ -125,12 +126,43 @@ void launch_final_lighting(const Exec& ex, int form, const vlt_frame_params& fp,
 void launch_taa(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const float* depth,
                 const void* source, const void* history, void* out_hist, void* out_user, uint32_t has_history);
 
+// trace.cu and restir.cu: traced mode. Rays are vlt_ray records (2 x float4), hits
+// vlt_ray_hit records (4 x float4); staging holds one 8-word query record per ray.
+void launch_ray_cache(const Exec& ex, uint32_t nmax, const uint32_t* queries, const uint32_t* cidx,
+                      const uint32_t* ccount, uint32_t frame_hash, void* rays);
+void launch_ray_diff(const Exec& ex, const vlt_frame_params& fp, int w, int h, const float* depth,
+                     const uint32_t* gbuf, uint32_t frame_rand, void* rays);
+void launch_shade_cache(const Exec& ex, const vlt_frame_params& fp, uint32_t nmax, const uint32_t* ccount,
+                        const void* rays, const void* hits, const ScreenCache& sc, const WorldCache& wc,
+                        float4* radiance, uint32_t* staging);
+void launch_update_traced(const Exec& ex, uint32_t nmax, const uint32_t* ccount, const uint32_t* caddr,
+                          const float4* radiance, uint32_t* storage, uint8_t* decay);
+void launch_shade_diff(const Exec& ex, const vlt_frame_params& fp, int w, int h, uint32_t has_prev_frame,
+                       const void* rays, const void* hits, const ScreenCache& sc, const WorldCache& wc, uint32_t* hpn,
+                       uint32_t* rad, uint32_t* staging);
+void launch_query_append(const Exec& ex, const uint32_t* staging, uint32_t n_cache, uint32_t n_diff, uint32_t n_spec,
+                         bool on_cache, bool on_diff, bool on_spec, uint32_t max_q, uint32_t* queries,
+                         uint32_t* count, uint32_t* scratch);
+void launch_diff_validate_rays(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h,
+                               const float* prev_depth, const void* rsv, void* rays);
+void launch_diff_validate_apply(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h,
+                                const float* prev_depth, void* rsv, const void* rays, const void* hits,
+                                const ScreenCache& sc, const WorldCache& wc, uint32_t* staging);
+void launch_spec_validate_rays(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h,
+                               const float* prev_depth, const uint32_t* rsv, const float* hp, const uint32_t* rad,
+                               void* rays);
+void launch_spec_validate_apply(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h,
+                                const float* prev_depth, uint32_t* rsv, float* hp, uint32_t* rad, const void* rays,
+                                const void* hits, const ScreenCache& sc, const WorldCache& wc, uint32_t* staging);
+
 size_t hg_select_scratch_bytes(const HashGridDims& d);
 void launch_hg_decay(const Exec& ex, const HashGridDims& d, uint8_t* decay, uint32_t* storage);
 void launch_hg_select(const Exec& ex, const HashGridDims& d, const uint32_t* queries, const uint32_t* count,
                       uint32_t* storage, uint32_t* selection, uint32_t frame_hash, void* scratch);
+// scratch (compact_scratch_bytes(num_cells)) given: the list in cell order; nullptr:
+// the shader's one-pass append (order varies between runs).
 void launch_hg_compact(const Exec& ex, const HashGridDims& d, const uint32_t* selection, uint32_t* idx,
-                       uint32_t* addr, uint32_t* count);
+                       uint32_t* addr, uint32_t* count, uint32_t* scratch);
 void launch_hg_update(const Exec& ex, const HashGridDims& d, const uint32_t* queries, const uint32_t* idx,
                       const uint32_t* addr, const uint32_t* count, uint32_t* storage, uint8_t* decay);
 void launch_hg_emit(const Exec& ex, const vlt_frame_params& fp, int w, int h, const HashGridDims& d,
@@ -147,6 +179,7 @@ bool frame_outputs_ok(const vlt_view* v, const vlt_frame_outputs* out);
 // host-side state advances as if the frame ran).
 vlt_status record_frame(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out, Recorder* rec);
 int view_device(const vlt_view* v);
+bool view_traced(const vlt_view* v);
 uint32_t view_width(const vlt_view* v);
 uint32_t view_height(const vlt_view* v);
 int ctx_device(const vlt_ctx* c);

@@ -36,6 +36,7 @@ struct Recorder {
 struct Exec {
   cudaStream_t stream = 0;
   Recorder* rec = nullptr;
+  uint32_t* launches = nullptr;  // counts kernels launched or recorded
 };
 
 // Tile shape of a 2D launch (block dimensions). One-dimensional work uses
@@ -218,6 +219,7 @@ void record_job(const Exec& ex, const char* name, uint32_t w, uint32_t h, bool o
 template <class F, class... A>
 void launch2d(const Exec& ex, const char* name, int w, int h, A... a) {
   if (w <= 0 || h <= 0) return;
+  if (ex.launches) ++*ex.launches;
   if (ex.rec) {
     record_job<F>(ex, name, (uint32_t)w, (uint32_t)h, false, a...);
     return;
@@ -230,6 +232,7 @@ void launch2d(const Exec& ex, const char* name, int w, int h, A... a) {
 template <class F, class... A>
 void launch1d(const Exec& ex, const char* name, uint32_t n, A... a) {
   if (n == 0) return;
+  if (ex.launches) ++*ex.launches;
   if (ex.rec) {
     record_job<F>(ex, name, n, 1u, true, a...);
     return;

@@ -74,7 +74,8 @@ def _frame_structs(frame_params, frame_index, inputs, outputs):
     fi.params = C.pointer(frame_params)
     fi.frame_index = int(frame_index) & 0xFFFFFFFF
     for name in ("depth", "gbuffer", "prev_depth", "prev_gbuffer", "diff_hit_pos_normal", "diff_hit_radiance",
-                 "diff_source_pdf", "spec_hit_pos", "spec_hit_radiance", "shadow_mask"):
+                 "diff_source_pdf", "spec_hit_pos", "spec_hit_radiance", "shadow_mask", "cache_hits", "diffuse_hits",
+                 "spec_validate_hits"):
         setattr(fi, name, _ptr(inputs.get(name)))
     fo = _ffi.FrameOutputs()
     outputs = outputs or {}
@@ -110,6 +111,23 @@ class View:
         fi, fo = _frame_structs(frame_params, frame_index, inputs, outputs)
         _ffi.check(self._lib.vlt_frame_run(self.handle, C.byref(fi), C.byref(fo), C.c_void_p(stream)),
                    "vlt_frame_run")
+
+    def trace(self, frame_params, frame_index, inputs, rays, stream=0):
+        """Phase one of a traced frame (params.trace = 1): fills the device ray arrays
+        rays["cache"], rays["diffuse"], rays["spec_validate"] (vlt_ray records) and
+        returns {"cache", "diffuse", "spec_validate": rays to trace, "diffuse_kind"}."""
+        fi, _ = _frame_structs(frame_params, frame_index, inputs, None)
+        fr = _ffi.FrameRays()
+        for k in ("cache", "diffuse", "spec_validate"):
+            setattr(fr, k, _ptr(rays.get(k)))
+        _ffi.check(self._lib.vlt_frame_trace(self.handle, C.byref(fi), C.byref(fr), C.c_void_p(stream)),
+                   "vlt_frame_trace")
+        return {"cache": fr.n_cache, "diffuse": fr.n_diffuse, "spec_validate": fr.n_spec_validate,
+                "diffuse_kind": fr.diffuse_kind}
+
+    @property
+    def cache_ray_capacity(self):
+        return int(self._lib.vlt_view_cache_ray_capacity(self.handle))
 
     def buffer(self, name):
         n = C.c_size_t(0)
@@ -174,6 +192,21 @@ class Scene:
         for k in FRAME_BUFFERS:
             setattr(f, k, _ptr(bufs.get(k)))
         return f
+
+    def trace_host(self, frame_params, rays, n=None):
+        """Traces host vlt_ray records (a uint8/float32 numpy array) against the scene;
+        returns the vlt_ray_hit records as a float32 array (16 per ray)."""
+        rays = np.ascontiguousarray(rays)
+        n = rays.nbytes // _ffi.RAY_BYTES if n is None else int(n)
+        hits = np.zeros(16 * n, np.float32)
+        _ffi.check(self._lib.vlt_scene_trace_host(C.byref(self.desc), C.byref(frame_params), _ptr(rays), n,
+                                                  _ptr(hits)), "vlt_scene_trace_host")
+        return hits
+
+    def trace_device(self, frame_params, rays, n, hits, stream=0):
+        """Traces n device vlt_ray records into device vlt_ray_hit records."""
+        _ffi.check(self._lib.vlt_scene_trace_device(C.byref(self.desc), C.byref(frame_params), _ptr(rays), int(n),
+                                                    _ptr(hits), C.c_void_p(stream)), "vlt_scene_trace_device")
 
     def generate_host(self, frame, bufs=None):
         bufs = bufs if bufs is not None else self.alloc_host()
