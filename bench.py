@@ -427,6 +427,10 @@ def run_ours(args, ws, rank, local):
     if not args.no_post:
         post = post_leg(args, ws, dev)
 
+    traced = None
+    if not args.no_traced:
+        traced = traced_leg(args, ws, dev)
+
     serving = None
     if not args.no_serving:
         serving = serving_leg(args, ws, dev)
@@ -459,6 +463,7 @@ def run_ours(args, ws, rank, local):
             "serving": serving,
             "precision": precision,
             "post_passes": post,
+            "traced": traced,
         }
         print(json.dumps(line), flush=True)
 
@@ -685,6 +690,70 @@ def precision_leg(args, ws, dev):
     }
 
 
+def traced_leg(args, ws, dev):
+    """Traced mode (params.trace = 1, diffuse validation every 4th frame, specular
+    validation every frame) on the headline workload: the back end's device time per
+    frame, phase one (hash-grid selection/compaction and the rays) plus phase two
+    (shading the hits and the rest of the frame); the synthetic scene traces the rays
+    in between, outside the timed spans."""
+    import torch
+
+    import violet_gb300 as vg
+
+    W, H = args.width, args.height
+    n = W * H
+    params = workload_params(vg)
+    params.trace = 1
+    params.diff_validate = 1
+    params.spec_validate = 1
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    sc = vg.Scene(6000, W, H, disocclusion_frac=0.02)
+    nfr = args.warmup + args.steps
+    frames = []
+    for f in range(nfr):
+        bufs = input_buffers(vg, params, W, H, dev)
+        sc.generate_device(f, bufs, sh)
+        frames.append((bufs, sc.frame_params(f)))
+    ctx = vg.Context(dev.index)
+    v = vg.View(ctx, W, H, FORM, params)
+    nq = v.cache_ray_capacity
+    rays = {"cache": torch.empty(max(nq, 1) * 32, dtype=torch.uint8, device=dev),
+            "diffuse": torch.empty(n * 32, dtype=torch.uint8, device=dev),
+            "spec_validate": torch.empty(n * 32, dtype=torch.uint8, device=dev)}
+    hits = {k: torch.empty(t.numel() * 2, dtype=torch.uint8, device=dev) for k, t in rays.items()}
+    ob = 16 if FORM == "f32" else 4
+    out = {o: torch.empty(n * ob, dtype=torch.uint8, device=dev) for o in ("diffuse", "specular")}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    total = 0.0
+    launches = 0
+    for f in range(nfr):
+        bufs, fp = frames[f]
+        ev[0].record(stream)
+        counts = v.trace(fp, f, bufs, rays, sh)
+        ev[1].record(stream)
+        inp = dict(bufs)
+        for k, name in (("cache", "cache_hits"), ("diffuse", "diffuse_hits"), ("spec_validate", "spec_validate_hits")):
+            if counts[k]:
+                sc.trace_device(fp, rays[k], counts[k], hits[k], sh)
+                inp[name] = hits[k]
+        ev[2].record(stream)
+        v.run(fp, f, inp, out, sh)
+        ev[3].record(stream)
+        torch.cuda.synchronize()
+        if f >= args.warmup:
+            total += ev[0].elapsed_time(ev[1]) + ev[2].elapsed_time(ev[3])
+            launches += v.launches
+    v.close()
+    ctx.close()
+    del frames
+    ms = max_over_ranks(total, ws, dev)
+    return {"workload": "%dx%d %s storage, plain knobs, traced mode with validation" % (W, H, FORM),
+            "value": ws * n * args.steps / (ms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_frame": ms / args.steps,
+            "timed": "vlt_frame_trace + vlt_frame_run device time (scene tracing excluded)",
+            "launches_per_frame": launches / args.steps}
+
+
 def post_leg(args, ws, dev):
     """The frame with the passes the reference renderer runs after the denoiser
     (final lighting and temporal AA, params.post = 2) on the headline workload:
@@ -879,6 +948,7 @@ def main():
     ap.add_argument("--serve-form", default="f32", choices=["ref", "f32", "f16"])
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--no-post", action="store_true")
+    ap.add_argument("--no-traced", action="store_true")
     ap.add_argument("--precision-frames", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -558,6 +558,13 @@ vlt_status vlt_hg_find(const vlt_frame_params* fp, uint32_t log2_buckets, uint32
                        const uint32_t* storage, uint32_t n, const float* positions,
                        const float* normals, uint32_t* out_addr, float* out_radiance, void* stream);
 
+/* restir/hash_grid_visualize.hlsl; node "Hash Grid Vis" (restir_renderer.rs:950-968).
+ * Push constant color_code (1: DebugView::HashGridCell, 0: HashGridRadiance).
+ * rw_color: R11G11B10. gbuffer_color supplies the normal of key mode 1. */
+vlt_status vlt_hg_visualize(const vlt_frame_params* fp, uint32_t width, uint32_t height, uint32_t log2_buckets,
+                            uint32_t key_mode, const float* gbuffer_depth, const uint32_t* gbuffer_color,
+                            const uint32_t* storage, uint32_t color_code, uint32_t* rw_color, void* stream);
+
 /* Diagnostics (no counterpart in the reference): evaluates the library's own
  * binary32 transcendentals on the device, elementwise: fn 0 exp2, 1 exp, 2 log2,
  * 3 sin, 4 cos, 5 the float forms' FMA exp2 (with its short path for [-126, 0]),

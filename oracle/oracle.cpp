@@ -2122,6 +2122,40 @@ void hg_find(const vlt_frame_params& fp, uint32_t log2_buckets, uint32_t key_mod
 }
 
 // ===================================================== per-view driver
+// hash_grid_visualize.hlsl:16-65 (key mode 1 adds the G-buffer normal's octant).
+void hg_visualize(const vlt_frame_params& fp, int w, int h, uint32_t log2_buckets, uint32_t key_mode,
+                  const float* depth, const uint32_t* gbuf, const uint32_t* storage, uint32_t color_code,
+                  uint32_t* out) {
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      const size_t i = (size_t)y * w + x;
+      if (has_no_geometry_via_depth(depth[i])) {
+        out[i] = store_r11g11b10(F3(0.0f));
+        continue;
+      }
+      float3 position = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth[i]);
+      float3 normal = load_gbuffer_normal(gbuf, x, y, w, h);
+      VKey k = vertex_descriptor(position, normal, v3(fp.view_pos), (1u << log2_buckets) - 1u, key_mode);
+      float3 color = color_code ? F3(0.0f) : F3(1.0f, 0.0f, 1.0f);
+      const uint32_t* bucket = storage + (size_t)k.hash * 16 * 4;
+      for (uint32_t s = 0; s < 16; ++s) {
+        const uint32_t* c = bucket + 4 * s;
+        if (c[0] == k.checksum) {
+          if (color_code) {
+            uint32_t code = k.checksum;
+            color = F3((float)(code & 0xFF) / 255.0f, (float)((code >> 8) & 0xFF) / 255.0f,
+                       (float)(((code >> 16) ^ (code >> 24)) & 0xFF) / 255.0f);
+          } else {
+            color = F3(asfloat(c[1]), asfloat(c[2]), asfloat(c[3]));
+          }
+          break;
+        }
+        if (c[0] == 0u) break;
+      }
+      out[i] = store_r11g11b10(color);
+    }
+}
+
 // ==================================================== final lighting and TAA
 // Colour images: R11G11B10 (form 0, the reference's B10G11R11_UFLOAT scene colour),
 // float4 {rgb, 0} (form 1), half4 {rgb, 0} stored with saturation (form 2).
@@ -3367,6 +3401,11 @@ void vlto_temporal_aa(int form, const vlt_frame_params* fp, uint32_t w, uint32_t
   if (form == 1) temporal_aa<1>(*fp, (int)w, (int)h, depth, source, hist, has_history, target);
   else if (form == 2) temporal_aa<2>(*fp, (int)w, (int)h, depth, source, hist, has_history, target);
   else temporal_aa<0>(*fp, (int)w, (int)h, depth, source, hist, has_history, target);
+}
+void vlto_hg_visualize(const vlt_frame_params* fp, uint32_t w, uint32_t h, uint32_t log2_buckets, uint32_t key_mode,
+                       const float* depth, const uint32_t* gbuf, const uint32_t* storage, uint32_t color_code,
+                       uint32_t* out) {
+  hg_visualize(*fp, (int)w, (int)h, log2_buckets, key_mode, depth, gbuf, storage, color_code, out);
 }
 void vlto_hg_decay(uint32_t log2_buckets, uint8_t* decay, uint32_t* storage) { hg_decay(log2_buckets, decay, storage); }
 void vlto_hg_emit_queries(const vlt_frame_params* fp, uint32_t w, uint32_t h, uint32_t log2_buckets, uint32_t key_mode,

@@ -48,6 +48,7 @@ SIGS = {
     "vlto_final_lighting": (None, [C.c_int, FP, U32, U32, P, P, P, P, C.c_int, P]),
     "vlto_temporal_aa": (None, [C.c_int, FP, U32, U32, P, P, P, U32, P]),
     "vlto_hg_decay": (None, [U32, P, P]),
+    "vlto_hg_visualize": (None, [FP, U32, U32, U32, U32, P, P, P, U32, P]),
     "vlto_hg_emit_queries": (None, [FP, U32, U32, U32, U32, U32, P, P, P, P, P]),
     "vlto_hg_query_select": (None, [U32, U32, P, P, P, P, U32]),
     "vlto_hg_query_compact": (None, [U32, U32, P, P, P, P]),

@@ -10,6 +10,8 @@ frame's denoised diffuse, world-space hash grid with query recording), validates
 updates the cache and runs the rest of the frame. Every resident buffer, the hash
 grid and its query list, and the outputs are compared byte for byte.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -122,6 +124,22 @@ def run_traced(ctx, form, W, H, params, frames, seed=5):
             ptr, _ = view.buffer("hg_queries")
             msg = first_mismatch(d2h(ptr, qc * 32, np.uint32), oview.buffer("hg_queries", np.uint32)[: qc * 8])
             assert msg is None, "frame %d hg_queries: %s" % (f, msg)
+            # hash_grid_visualize over this frame's surfaces, both debug views
+            sptr, _ = view.buffer("hg_storage")
+            for code in (0, 1):
+                vis = torch.zeros(4 * n, dtype=torch.uint8, device="cuda")
+                assert vg.lib().vlt_hg_visualize(C.byref(fp), W, H, params.hg_log2_buckets, params.hg_key_mode,
+                                                 C.c_void_p(dev["depth"].data_ptr()),
+                                                 C.c_void_p(dev["gbuffer"].data_ptr()), C.c_void_p(sptr), code,
+                                                 C.c_void_p(vis.data_ptr()), None) == 0
+                ovis = np.zeros(n, np.uint32)
+                ost = oview.buffer("hg_storage", np.uint32)
+                po.lib().vlto_hg_visualize(C.byref(fp), W, H, params.hg_log2_buckets, params.hg_key_mode,
+                                           po.ptr(host["depth"]), po.ptr(host["gbuffer"]), po.ptr(ost), code,
+                                           po.ptr(ovis))
+                torch.cuda.synchronize()
+                msg = first_mismatch(vis.cpu().numpy().view(np.uint32), ovis, W)
+                assert msg is None, "frame %d hg_visualize(%d): %s" % (f, code, msg)
     finally:
         view.close()
         oview.close()

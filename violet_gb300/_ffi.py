@@ -230,6 +230,7 @@ SIGNATURES = {
     "vlt_denoise_spatial_fallback": (C.c_int, [U32, U32, P, P, P, P, P, P, P, P]),
     "vlt_denoise_atrous": (C.c_int, [U32, U32, P, P, P, P, P, P, I32, P]),
     "vlt_final_lighting": (C.c_int, [FP, U32, U32, P, P, P, P, P, P]),
+    "vlt_hg_visualize": (C.c_int, [FP, U32, U32, U32, U32, P, P, P, U32, P, P]),
     "vlt_temporal_aa": (C.c_int, [FP, U32, U32, P, P, P, U32, P, P]),
     "vlt_hg_decay": (C.c_int, [U32, P, P, P]),
     "vlt_hg_select_scratch_bytes": (C.c_size_t, [U32, U32]),

@@ -1275,6 +1275,18 @@ vlt_status vlt_hg_find(const vlt_frame_params* fp, uint32_t log2_buckets, uint32
   return cuda_status(cudaGetLastError());
 }
 
+vlt_status vlt_hg_visualize(const vlt_frame_params* fp, uint32_t width, uint32_t height, uint32_t log2_buckets,
+                            uint32_t key_mode, const float* gbuffer_depth, const uint32_t* gbuffer_color,
+                            const uint32_t* storage, uint32_t color_code, uint32_t* rw_color, void* stream) {
+  if (!fp || !dims_ok(width, height) || !hg_ok(log2_buckets) || key_mode > 1 || !gbuffer_depth || !gbuffer_color ||
+      !storage || !rw_color)
+    return VLT_ERR_INVALID_ARG;
+  HashGridDims d = {log2_buckets, 1};
+  launch_hg_visualize(stream_exec(stream), *fp, (int)width, (int)height, d, key_mode, gbuffer_depth, gbuffer_color,
+                      storage, color_code ? 1u : 0u, rw_color);
+  return cuda_status(cudaGetLastError());
+}
+
 }  // extern "C"
 
 namespace vlt {

@@ -338,7 +338,54 @@ struct HgFindF {
 }
 };
 
+// ------------------------------------------------------------ visualize
+
+// hash_grid_visualize.hlsl:16-65: the cache cell of each pixel's surface point (key
+// from the position; key mode 1 also the G-buffer normal's octant), shown as its
+// radiance or as a colour code from the checksum; no geometry: 0; no cell: (1, 0, 1)
+// or, with the colour code, 0. Output R11G11B10.
+struct HgVisualizeF {
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, uint32_t bucket_mask, uint32_t key_mode, const float* __restrict__ depth, const uint32_t* __restrict__ gbuf, const uint4* __restrict__ storage, uint32_t color_code, uint32_t* __restrict__ out) {
+  const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
+  if (!inb(x, y, w, h)) return;
+  const size_t i = (size_t)y * w + x;
+  const float d = depth[i];
+  if (d == 0.0f) {
+    out[i] = 0u;
+    return;
+  }
+  const f3 pos = depth_to_position(fp.inv_view_proj, x, y, w, h, d);
+  const f3 nrm = gbuffer_normal(gbuf[(size_t)w * h + i]);
+  const VertexKey k = vertex_key(pos, nrm, vpos3(fp.view_pos), bucket_mask, key_mode);
+  const uint32_t base = k.hash * 16u;
+  f3 color = color_code ? mk3(0.0f) : mk3(1.0f, 0.0f, 1.0f);
+  for (uint32_t s = 0; s < 16u; ++s) {
+    const uint4 c = storage[base + s];
+    if (c.x == k.checksum) {
+      if (color_code) {
+        const uint32_t code = k.checksum;
+        color = mk3((float)(code & 0xFFu) / 255.0f, (float)((code >> 8) & 0xFFu) / 255.0f,
+                    (float)(((code >> 16) ^ (code >> 24)) & 0xFFu) / 255.0f);
+      } else {
+        color = mk3(as_float(c.y), as_float(c.z), as_float(c.w));
+      }
+      break;
+    }
+    if (c.x == 0u) break;
+  }
+  out[i] = pack_r11g11b10(color);
+}
+};
+
 // --------------------------------------------------------------- launchers
+
+void launch_hg_visualize(const Exec& ex, const vlt_frame_params& fp, int w, int h, const HashGridDims& d,
+                         uint32_t key_mode, const float* depth, const uint32_t* gbuf, const uint32_t* storage,
+                         uint32_t color_code, uint32_t* out) {
+  launch2d<HgVisualizeF>(ex, "hg_visualize", w, h, fp, w, h, d.num_buckets() - 1u, key_mode, depth, gbuf,
+                         (const uint4*)storage, color_code, out);
+}
+
 
 void launch_hg_emit(const Exec& ex, const vlt_frame_params& fp, int w, int h, const HashGridDims& d,
                     uint32_t key_mode, const float* depth, const uint32_t* hpn, const uint32_t* rad,

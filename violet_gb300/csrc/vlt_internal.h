@@ -155,6 +155,9 @@ void launch_spec_validate_apply(const Exec& ex, int form, const vlt_frame_params
                                 const float* prev_depth, uint32_t* rsv, float* hp, uint32_t* rad, const void* rays,
                                 const void* hits, const ScreenCache& sc, const WorldCache& wc, uint32_t* staging);
 
+void launch_hg_visualize(const Exec& ex, const vlt_frame_params& fp, int w, int h, const HashGridDims& d,
+                         uint32_t key_mode, const float* depth, const uint32_t* gbuf, const uint32_t* storage,
+                         uint32_t color_code, uint32_t* out);
 size_t hg_select_scratch_bytes(const HashGridDims& d);
 void launch_hg_decay(const Exec& ex, const HashGridDims& d, uint8_t* decay, uint32_t* storage);
 void launch_hg_select(const Exec& ex, const HashGridDims& d, const uint32_t* queries, const uint32_t* count,
