@@ -89,7 +89,7 @@ FORM = "f32"
 PASS_BYTES_PER_CELL = {"hg_decay": 2, "hg_compact": 4}
 # DRAM bytes per launch unit measured with ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum), see profiles/; None until captured.
-MEASURED_TRAFFIC_PER_UNIT = {}
+MEASURED_TRAFFIC_PER_UNIT = {"dn_atrous": 64.25}  # B/px: one-pass dram counters, 960x540 f32
 
 
 def log(*a):
