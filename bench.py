@@ -14,7 +14,8 @@ arithmetic. A step is one frame of that view. The reference-storage-form
           each frame's inputs plus resident state exceed the 129 MB L2);
   e2e   : the same through the public C ABI with host inputs: per step the frame's
           inputs are copied from pinned host memory and the denoised outputs read
-          back, inside the timed region;
+          back, inside the timed region (a copy stream overlaps frame f+2's upload
+          and frame f's read-back with frame f+1's compute);
   roofline: the dominant pass (per-pass CUDA-event timers of the library) against
           the measured HBM copy bandwidth;
   cpu_baseline: the CPU oracle (restatement of the reference's passes) on the
@@ -88,7 +89,7 @@ PASS_BYTES_PER_PIXEL = {"ref": PASS_BYTES_PER_PIXEL_REF, "f32": PASS_BYTES_PER_P
 FORM = "f32"
 PASS_BYTES_PER_CELL = {"hg_decay": 2, "hg_compact": 4}
 # DRAM bytes per launch unit measured with ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum), see profiles/; None until captured.
+# dram__bytes_write.sum, one-pass counters; profiles/dn_atrous_f32_540p.md).
 MEASURED_TRAFFIC_PER_UNIT = {"dn_atrous": 64.25}  # B/px: one-pass dram counters, 960x540 f32
 
 
@@ -386,26 +387,47 @@ def run_ours(args, ws, rank, local):
     for f in range(nframes):
         host.append({k: torch.empty(v.numel(), dtype=torch.uint8, pin_memory=True).copy_(v) for k, v in
                      frames[f].items()})
-    stage = {k: torch.empty_like(v) for k, v in frames[0].items()}
     out_host = {k: torch.empty(n * out_px, dtype=torch.uint8, pin_memory=True) for k in ("diffuse", "specular")}
     view.reset(sh)
+    # Frames are pipelined over two staging slots: the copy stream uploads frame f+2's
+    # inputs and reads back frame f's outputs while the compute stream runs frame
+    # f+1. Every frame's upload and read-back is inside the timed region.
+    copy_stream = torch.cuda.Stream(device=dev)
+    stage2 = [{k: torch.empty_like(v) for k, v in frames[0].items()} for _ in range(2)]
+    out2 = [{k: torch.empty(n * out_px, dtype=torch.uint8, device=dev) for k in ("diffuse", "specular")}
+            for _ in range(2)]
+    ready = [torch.cuda.Event() for _ in range(2)]
+    done = [torch.cuda.Event() for _ in range(2)]
 
-    def e2e_step(f):
-        for k, v in host[f].items():
-            stage[k].copy_(v, non_blocking=True)
-        view.run(fps[f], f, stage, out, sh)
-        for k in out_host:
-            out_host[k].copy_(out[k], non_blocking=True)
+    def upload(f, slot):
+        with torch.cuda.stream(copy_stream):
+            for k, v in host[f].items():
+                stage2[slot][k].copy_(v, non_blocking=True)
+            ready[slot].record(copy_stream)
 
-    for f in range(args.warmup):
-        e2e_step(f)
+    def e2e_frames(f0, f1):
+        upload(f0, f0 % 2)
+        if f0 + 1 < f1:
+            upload(f0 + 1, (f0 + 1) % 2)
+        for f in range(f0, f1):
+            s = f % 2
+            stream.wait_event(ready[s])
+            view.run(fps[f], f, stage2[s], out2[s], sh)
+            done[s].record(stream)
+            copy_stream.wait_event(done[s])
+            with torch.cuda.stream(copy_stream):
+                for k in out_host:
+                    out_host[k].copy_(out2[s][k], non_blocking=True)
+            if f + 2 < f1:
+                upload(f + 2, s)
+
+    e2e_frames(0, args.warmup)
     torch.cuda.synchronize()
     barrier(ws)
-    e0.record(stream)
+    e0.record(copy_stream)
     t0 = time.perf_counter()
-    for k in range(args.steps):
-        e2e_step(args.warmup + k)
-    e1.record(stream)
+    e2e_frames(args.warmup, args.warmup + args.steps)
+    e1.record(copy_stream)
     torch.cuda.synchronize()
     e2e_ms = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3)
     barrier(ws)
