@@ -252,6 +252,20 @@ uint32_t vlt_view_cache_ray_capacity(const vlt_view* view);
 vlt_status vlt_frame_run(vlt_view* view, const vlt_frame_inputs* in, const vlt_frame_outputs* out,
                          void* stream);
 
+/* The view's temporal state as one blob: every resident buffer (reservoirs, AO and
+ * denoiser history, hash grid, retained depth, surface planes, TAA history) and the
+ * slot bookkeeping, i.e. what RestirRenderer and Denoiser keep as RGTemporal handles
+ * between frames (render_graph.rs:1471-1564). For checkpoint/resume and for moving
+ * a session between views or processes. `dst` / `src` may be host or device memory
+ * of vlt_view_state_bytes() bytes. Both calls are ordered on `stream` and return
+ * once the copy is complete. Import requires a view created with the same size,
+ * form and params (else VLT_ERR_INVALID_ARG); a traced frame must not be pending
+ * (VLT_ERR_BAD_STATE). The view that imports continues exactly as the exporting view
+ * would have. */
+size_t vlt_view_state_bytes(const vlt_view* view);
+vlt_status vlt_view_export_state(vlt_view* view, void* dst, size_t bytes, void* stream);
+vlt_status vlt_view_import_state(vlt_view* view, const void* src, size_t bytes, void* stream);
+
 /* Number of kernel launches the last vlt_frame_run issued. */
 uint32_t vlt_view_last_launch_count(const vlt_view* view);
 

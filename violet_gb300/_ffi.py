@@ -195,6 +195,9 @@ SIGNATURES = {
     "vlt_view_reset": (C.c_int, [P, P]),
     "vlt_frame_run": (C.c_int, [P, C.POINTER(FrameInputs), C.POINTER(FrameOutputs), P]),
     "vlt_frame_trace": (C.c_int, [P, C.POINTER(FrameInputs), C.POINTER(FrameRays), P]),
+    "vlt_view_state_bytes": (C.c_size_t, [P]),
+    "vlt_view_export_state": (C.c_int, [P, P, C.c_size_t, P]),
+    "vlt_view_import_state": (C.c_int, [P, P, C.c_size_t, P]),
     "vlt_view_cache_ray_capacity": (U32, [P]),
     "vlt_view_last_launch_count": (U32, [P]),
     "vlt_batch_create": (C.c_int, [P, C.POINTER(P)]),

@@ -515,6 +515,111 @@ vlt_status vlt_view_reset(vlt_view* v, void* stream) {
 
 uint32_t vlt_view_last_launch_count(const vlt_view* v) { return v ? v->launches : 0; }
 
+}  // extern "C"
+
+namespace {
+
+// Blob of vlt_view_export_state: StateHeader, the buffer table as offsets into the
+// pool (kNullOff for unused), padding to 256 bytes, the pool.
+static_assert(sizeof(ViewBuffers) % sizeof(void*) == 0, "ViewBuffers holds pointers only");
+constexpr uint32_t kStateMagic = 0x53544C56u;  // "VLTS"
+constexpr uint32_t kStateVersion = 1;
+constexpr uint64_t kNullOff = ~0ull;
+constexpr uint32_t kStatePtrs = (uint32_t)(sizeof(ViewBuffers) / sizeof(void*));
+struct StateHeader {
+  uint32_t magic, version, w, h, form, n_ptrs;
+  vlt_params p;
+  uint64_t pool_bytes;
+  uint32_t frames, flags;  // flags: denoise_history, fast_history_valid, taa_valid, has_prev_den
+  int32_t diff_prev, spec_prev, ao_prev, hg_qcur, surf_cur, taa_cur, prev_den_stride, pad;
+  uint64_t prev_den_off;
+  uint64_t off[kStatePtrs];
+};
+size_t state_data_off() { return (sizeof(StateHeader) + 255) & ~(size_t)255; }
+
+uint64_t to_off(const vlt_view* v, const void* p) {
+  return p ? (uint64_t)((const char*)p - (const char*)v->pool.p) : kNullOff;
+}
+void* from_off(const vlt_view* v, uint64_t o) { return o == kNullOff ? nullptr : (char*)v->pool.p + o; }
+
+}  // namespace
+
+extern "C" {
+
+size_t vlt_view_state_bytes(const vlt_view* v) { return v ? state_data_off() + v->pool.bytes : 0; }
+
+vlt_status vlt_view_export_state(vlt_view* v, void* dst, size_t bytes, void* stream) {
+  if (!v || !dst || bytes < vlt_view_state_bytes(v)) return VLT_ERR_INVALID_ARG;
+  if (v->trace_pending) return VLT_ERR_BAD_STATE;
+  StateHeader hd;
+  memset(&hd, 0, sizeof(hd));
+  hd.magic = kStateMagic;
+  hd.version = kStateVersion;
+  hd.w = v->w;
+  hd.h = v->h;
+  hd.form = (uint32_t)v->form;
+  hd.n_ptrs = kStatePtrs;
+  hd.p = v->p;
+  hd.pool_bytes = v->pool.bytes;
+  hd.frames = v->frames;
+  hd.flags = (v->denoise_history ? 1u : 0u) | (v->fast_history_valid ? 2u : 0u) | (v->taa_valid ? 4u : 0u) |
+             (v->has_prev_den ? 8u : 0u);
+  hd.diff_prev = v->diff_prev;
+  hd.spec_prev = v->spec_prev;
+  hd.ao_prev = v->ao_prev;
+  hd.hg_qcur = v->hg_qcur;
+  hd.surf_cur = v->surf_cur;
+  hd.taa_cur = v->taa_cur;
+  hd.prev_den_stride = v->prev_den_stride;
+  hd.prev_den_off = to_off(v, v->prev_den);
+  void* const* ptrs = (void* const*)&v->b;
+  for (uint32_t k = 0; k < kStatePtrs; ++k) hd.off[k] = to_off(v, ptrs[k]);
+  cudaStream_t s = (cudaStream_t)stream;
+  VLT_TRY(cudaSetDevice(v->ctx->device));
+  VLT_TRY(cudaMemcpyAsync((char*)dst + state_data_off(), v->pool.p, v->pool.bytes, cudaMemcpyDefault, s));
+  VLT_TRY(cudaMemcpyAsync(dst, &hd, sizeof(hd), cudaMemcpyDefault, s));
+  VLT_TRY(cudaStreamSynchronize(s));  // hd lives on this stack frame
+  return VLT_OK;
+}
+
+vlt_status vlt_view_import_state(vlt_view* v, const void* src, size_t bytes, void* stream) {
+  if (!v || !src || bytes < vlt_view_state_bytes(v)) return VLT_ERR_INVALID_ARG;
+  if (v->trace_pending) return VLT_ERR_BAD_STATE;
+  cudaStream_t s = (cudaStream_t)stream;
+  VLT_TRY(cudaSetDevice(v->ctx->device));
+  StateHeader hd;
+  VLT_TRY(cudaMemcpyAsync(&hd, src, sizeof(hd), cudaMemcpyDefault, s));
+  VLT_TRY(cudaStreamSynchronize(s));
+  if (hd.magic != kStateMagic || hd.version != kStateVersion || hd.n_ptrs != kStatePtrs || hd.w != v->w ||
+      hd.h != v->h || hd.form != (uint32_t)v->form || hd.pool_bytes != v->pool.bytes ||
+      memcmp(&hd.p, &v->p, sizeof(vlt_params)) != 0) {
+    set_last_error("state blob does not match this view (size, form or params)");
+    return VLT_ERR_INVALID_ARG;
+  }
+  for (uint32_t k = 0; k < kStatePtrs; ++k)
+    if (hd.off[k] != kNullOff && hd.off[k] >= hd.pool_bytes) return VLT_ERR_INVALID_ARG;
+  if (hd.prev_den_off != kNullOff && hd.prev_den_off >= hd.pool_bytes) return VLT_ERR_INVALID_ARG;
+  VLT_TRY(cudaMemcpyAsync(v->pool.p, (const char*)src + state_data_off(), v->pool.bytes, cudaMemcpyDefault, s));
+  void** ptrs = (void**)&v->b;
+  for (uint32_t k = 0; k < kStatePtrs; ++k) ptrs[k] = from_off(v, hd.off[k]);
+  v->frames = hd.frames;
+  v->denoise_history = (hd.flags & 1u) != 0;
+  v->fast_history_valid = (hd.flags & 2u) != 0;
+  v->taa_valid = (hd.flags & 4u) != 0;
+  v->has_prev_den = (hd.flags & 8u) != 0;
+  v->diff_prev = hd.diff_prev;
+  v->spec_prev = hd.spec_prev;
+  v->ao_prev = hd.ao_prev;
+  v->hg_qcur = hd.hg_qcur;
+  v->surf_cur = hd.surf_cur;
+  v->taa_cur = hd.taa_cur;
+  v->prev_den_stride = hd.prev_den_stride;
+  v->prev_den = from_off(v, hd.prev_den_off);
+  v->trace_pending = false;
+  VLT_TRY(cudaStreamSynchronize(s));
+  return VLT_OK;
+}
+
 vlt_status vlt_view_set_timing(vlt_view* v, int enable) {
   if (!v) return VLT_ERR_INVALID_ARG;
   v->timing->enabled = enable != 0;

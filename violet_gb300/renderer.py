@@ -126,6 +126,25 @@ class View:
                 "diffuse_kind": fr.diffuse_kind}
 
     @property
+    def state_bytes(self):
+        return int(self._lib.vlt_view_state_bytes(self.handle))
+
+    def export_state(self, dst=None, stream=0):
+        """The view's temporal state into `dst` (host numpy array or device tensor of
+        state_bytes bytes; a new uint8 numpy array when None). Returns dst."""
+        if dst is None:
+            dst = np.empty(self.state_bytes, np.uint8)
+        nb = dst.nbytes if isinstance(dst, np.ndarray) else dst.numel() * dst.element_size()
+        _ffi.check(self._lib.vlt_view_export_state(self.handle, _ptr(dst), nb, C.c_void_p(stream)),
+                   "vlt_view_export_state")
+        return dst
+
+    def import_state(self, src, stream=0):
+        nb = src.nbytes if isinstance(src, np.ndarray) else src.numel() * src.element_size()
+        _ffi.check(self._lib.vlt_view_import_state(self.handle, _ptr(src), nb, C.c_void_p(stream)),
+                   "vlt_view_import_state")
+
+    @property
     def cache_ray_capacity(self):
         return int(self._lib.vlt_view_cache_ray_capacity(self.handle))
 
