@@ -110,8 +110,9 @@ struct HgDecayF {
 struct SelectScratch {
   uint32_t* need_count;   // [num_buckets]
   uint32_t* need_offset;  // [num_buckets]
-  uint32_t* total;        // [1]
+  uint32_t* total;        // [2]: miss-list length, number of buckets with misses
   uint32_t* list;         // [max_queries]
+  uint32_t* buckets;      // [num_buckets]: the buckets with misses (any order)
 };
 
 __host__ __device__ inline size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
@@ -126,11 +127,13 @@ static SelectScratch carve(const HashGridDims& d, void* base) {
   s.total = (uint32_t*)p;
   p += 256;
   s.list = (uint32_t*)p;
+  p += align256((size_t)d.max_queries * 4);
+  s.buckets = (uint32_t*)p;
   return s;
 }
 
 size_t hg_select_scratch_bytes(const HashGridDims& d) {
-  return 2 * align256((size_t)d.num_buckets() * 4) + 256 + align256((size_t)d.max_queries * 4);
+  return 3 * align256((size_t)d.num_buckets() * 4) + 256 + align256((size_t)d.max_queries * 4);
 }
 
 __device__ __forceinline__ uint32_t select_word(uint32_t q, uint32_t frame_hash, uint32_t qbits) {
@@ -171,13 +174,31 @@ struct HgSelProbeF {
 };
 
 struct HgSelAllocF {
-  static __device__ __forceinline__ void run(int x0, int y0, uint32_t num_buckets, uint32_t* __restrict__ need_count, uint32_t* __restrict__ need_offset, uint32_t* __restrict__ total) {
+  static __device__ __forceinline__ void run(int x0, int y0, uint32_t num_buckets, uint32_t* __restrict__ need_count, uint32_t* __restrict__ need_offset, uint32_t* __restrict__ total, uint32_t* __restrict__ buckets) {
   uint32_t b = (uint32_t)x0 + threadIdx.x;
-  if (b >= num_buckets) return;
-  uint32_t n = need_count[b];
+  uint32_t n = b < num_buckets ? need_count[b] : 0u;
+  // Warp-aggregated appends: one atomic per warp for the miss-list segments and one
+  // for the list of buckets with misses.
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t act = __ballot_sync(0xFFFFFFFFu, n != 0u);
+  if (act == 0u) return;
+  uint32_t incl = n;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= (uint32_t)o) incl += v;
+  }
+  const uint32_t warp_total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+  uint32_t seg = 0u, slot = 0u;
+  if (lane == 0) {
+    seg = atomicAdd(total, warp_total);
+    slot = atomicAdd(total + 1, (uint32_t)__popc(act));
+  }
+  seg = __shfl_sync(0xFFFFFFFFu, seg, 0);
+  slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
   if (n == 0u) return;
-  need_offset[b] = atomicAdd(total, n);
+  need_offset[b] = seg + incl - n;
   need_count[b] = 0u;
+  buckets[slot + __popc(act & ((1u << lane) - 1u))] = b;
 }
 };
 
@@ -199,14 +220,21 @@ struct HgSelScatterF {
 
 // One warp per bucket: sequential-order insertion (see the file comment).
 struct HgSelResolveF {
-  static __device__ __forceinline__ void run(int x0, int y0, uint32_t num_buckets, const uint32_t* __restrict__ queries, uint4* __restrict__ storage, uint32_t* __restrict__ selection, const uint32_t* __restrict__ need_count, const uint32_t* __restrict__ need_offset, uint32_t* __restrict__ list, uint32_t frame_hash, uint32_t qbits) {
-  uint32_t warp = ((uint32_t)x0 + threadIdx.x) >> 5;
-  uint32_t lane = threadIdx.x & 31u;
-  if (warp >= num_buckets) return;
-  uint32_t n = need_count[warp];
+  static __device__ __forceinline__ void run(int x0, int y0, uint32_t n_warps, const uint32_t* __restrict__ queries, uint4* __restrict__ storage, uint32_t* __restrict__ selection, const uint32_t* __restrict__ need_count, const uint32_t* __restrict__ need_offset, uint32_t* __restrict__ list, uint32_t frame_hash, uint32_t qbits, const uint32_t* __restrict__ total, const uint32_t* __restrict__ buckets) {
+  // n_warps warps loop over the buckets with misses (their order does not matter:
+  // buckets are disjoint).
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t n_active = total[1];
+  for (uint32_t wi = ((uint32_t)x0 + threadIdx.x) >> 5; wi < n_active; wi += n_warps) {
+    resolve_bucket(buckets[wi], lane, queries, storage, selection, need_count, need_offset, list, frame_hash,
+                   qbits);
+  }
+}
+  static __device__ __forceinline__ void resolve_bucket(uint32_t bucket, uint32_t lane, const uint32_t* __restrict__ queries, uint4* __restrict__ storage, uint32_t* __restrict__ selection, const uint32_t* __restrict__ need_count, const uint32_t* __restrict__ need_offset, uint32_t* __restrict__ list, uint32_t frame_hash, uint32_t qbits) {
+  uint32_t n = need_count[bucket];
   if (n == 0u) return;
-  uint32_t off = need_offset[warp];
-  uint32_t base = warp * 16u;
+  uint32_t off = need_offset[bucket];
+  uint32_t base = bucket * 16u;
   uint32_t cs = lane < 16u ? storage[base + lane].x : 0xFFFFFFFFu;  // lanes >= 16 never match
   const uint32_t RESOLVED = 0x80000000u;
   for (int round = 0; round < 17; ++round) {
@@ -405,15 +433,19 @@ void launch_hg_select(const Exec& ex, const HashGridDims& d, const uint32_t* que
   uint32_t nb = d.num_buckets();
   uint32_t qb = d.query_bits();
   ex_fill32(ex, sc.need_count, 0u, (size_t)nb * 4);
-  ex_fill32(ex, sc.total, 0u, 4);
+  ex_fill32(ex, sc.total, 0u, 8);
   uint32_t nq = d.max_queries;
   launch1d<HgSelProbeF>(ex, "hg_select", nq, nq, queries, count, (const uint4*)storage, selection, frame_hash, qb,
                         sc.need_count);
-  launch1d<HgSelAllocF>(ex, "hg_select", nb, nb, sc.need_count, sc.need_offset, sc.total);
+  launch1d<HgSelAllocF>(ex, "hg_select", nb, nb, sc.need_count, sc.need_offset, sc.total, sc.buckets);
   launch1d<HgSelScatterF>(ex, "hg_select", nq, nq, queries, count, (const uint4*)storage, sc.need_count,
                           (const uint32_t*)sc.need_offset, sc.list);
-  launch1d<HgSelResolveF>(ex, "hg_select", nb * 32u, nb, queries, (uint4*)storage, selection,
-                          (const uint32_t*)sc.need_count, (const uint32_t*)sc.need_offset, sc.list, frame_hash, qb);
+  // One warp per bucket with misses, at most a full device of warps looping over them.
+  const uint64_t cap = (uint64_t)device_sm_count() * 64u;
+  const uint32_t n_warps = (uint32_t)(nb < cap ? nb : cap);
+  launch1d<HgSelResolveF>(ex, "hg_select", n_warps * 32u, n_warps, queries, (uint4*)storage, selection,
+                          (const uint32_t*)sc.need_count, (const uint32_t*)sc.need_offset, sc.list, frame_hash, qb,
+                          (const uint32_t*)sc.total, (const uint32_t*)sc.buckets);
 }
 
 void launch_hg_compact(const Exec& ex, const HashGridDims& d, const uint32_t* selection, uint32_t* idx,
