@@ -1432,7 +1432,8 @@ void dn_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, const
 // Numeric contract of this form: binary32 with explicit fused multiply-adds. Each
 // fma_() is one IEEE fusedMultiplyAdd (std::fmaf), every other operation is rounded
 // separately (-ffp-contract=off), and exp is exp_fma (the exp2 construction above
-// evaluated by FMA Horner steps). The product's f32-form kernels evaluate the same
+// evaluated by FMA Horner steps; the a-trous edge weights use exp_weight, which is
+// zero below 2^-126). The product's f32-form kernels evaluate the same
 // expressions in the same order, so the results are reproduced bit for bit.
 inline float fma_(float a, float b, float c) { return std::fmaf(a, b, c); }
 inline float exp2_fma(float x) {
@@ -1451,6 +1452,12 @@ inline float exp2_fma(float x) {
   return p * asfloat((uint32_t)(e + 127) << 23);
 }
 inline float exp_fma(float x) { return exp2_fma(x * 1.44269502162933349609375f); }
+// The a-trous edge weight's exponential: exp_fma where x log2 e >= -126, zero below
+// that and for NaN. Its argument is never positive (a sum of non-positive terms).
+inline float exp_weight(float x) {
+  const float y = x * 1.44269502162933349609375f;
+  return y >= -126.0f ? exp2_fma(y) : 0.0f;
+}
 // luminance (util.hlsl:21-24) as r*0.2126, then two FMAs.
 inline float lum_fma(float3 c) { return fma_(c.z, 0.0722f, fma_(c.y, 0.7152f, c.x * 0.2126f)); }
 inline float3 fma3(float w, float3 v, float3 acc) {
@@ -1499,7 +1506,7 @@ struct EdgeStop32 {
     for (int k = 0; k < n_log2; ++k) wn = wn * wn;
     float ax = fma_(-fabsf(lumi.x - lumi_center.x), lumi_rcp.x, wz);
     float ay = fma_(-fabsf(lumi.y - lumi_center.y), lumi_rcp.y, wz);
-    return F2(wn * exp_fma(ax), wn * exp_fma(ay));
+    return F2(wn * exp_weight(ax), wn * exp_weight(ay));
   }
 };
 

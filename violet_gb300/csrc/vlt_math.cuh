@@ -123,19 +123,42 @@ VLT_HD uint32_t f2u_rn(float x) {
 #define VLT_EXP2_C5 0.0013399859890341759f
 #define VLT_EXP2_C6 0.00015337577497120947f
 
-VLT_HD float exp2_(float x) {
+// One IEEE fusedMultiplyAdd (the float forms' denoiser contract).
+VLT_HD float fma_(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+  return __fmaf_rn(a, b, c);
+#else
+  return fmaf(a, b, c);
+#endif
+}
+
+// 2^x in the piecewise form the construction is defined by: NaN, overflow and
+// underflow first, then n = rint(x), f = x - n, p(f) by Horner steps (separately
+// rounded, or fused when kFused), and p * 2^n (two steps below 2^-126 so that gradual
+// underflow rounds once).
+template <bool kFused>
+VLT_HD float exp2_piecewise(float x) {
   if (is_nan(x)) return as_float(0x7FFFFFFFu);
   if (x >= 128.0f) return as_float(0x7F800000u);
   if (x < -151.0f) return 0.0f;
   float n = rint_(x);
   float f = x - n;
   float p = VLT_EXP2_C6;
-  p = p * f + VLT_EXP2_C5;
-  p = p * f + VLT_EXP2_C4;
-  p = p * f + VLT_EXP2_C3;
-  p = p * f + VLT_EXP2_C2;
-  p = p * f + VLT_EXP2_C1;
-  p = p * f + VLT_EXP2_C0;
+  if (kFused) {
+    p = fma_(p, f, VLT_EXP2_C5);
+    p = fma_(p, f, VLT_EXP2_C4);
+    p = fma_(p, f, VLT_EXP2_C3);
+    p = fma_(p, f, VLT_EXP2_C2);
+    p = fma_(p, f, VLT_EXP2_C1);
+    p = fma_(p, f, VLT_EXP2_C0);
+  } else {
+    p = p * f + VLT_EXP2_C5;
+    p = p * f + VLT_EXP2_C4;
+    p = p * f + VLT_EXP2_C3;
+    p = p * f + VLT_EXP2_C2;
+    p = p * f + VLT_EXP2_C1;
+    p = p * f + VLT_EXP2_C0;
+  }
   int32_t ni = f2i_rz(n);
   if (ni > 127) {  // n == 128 only
     return (p * 2.0f) * as_float(0x7F000000u);
@@ -145,6 +168,50 @@ VLT_HD float exp2_(float x) {
   }
   return p * as_float((uint32_t)(ni + 127) << 23);
 }
+
+// The same function without branches, for the kernels (the same bits for every
+// binary32 x; an exhaustive host comparison over all 2^32 inputs found no
+// difference). The argument is clamped into [-151, 128], where adding the 1.5 * 2^23
+// shifter rounds it to an integer with ties to even and leaves that integer in the
+// low mantissa bits, so n = rint(x) and f = x - n exactly. 2^n is applied as
+// 2^e1 * 2^e2 with e1 = clamp(n, -126, 127) and e2 = n - e1: one exact scale for
+// normal results, the two-step scale below 2^-126, and (p * 2^127) * 2 for n = 128,
+// which rounds p * 2^128 once like (p * 2) * 2^127 (both first products are exact).
+// NaN, overflow and underflow are selected at the end. Without branches the
+// compiler can interleave the loads and arithmetic of neighbouring filter taps; with
+// the piecewise form every tap of the a-trous filter ended a basic block.
+template <bool kFused>
+VLT_HD float exp2_select(float x) {
+  const float M = 12582912.0f;  // 1.5 * 2^23
+  const float xc = fmin_(fmax_(x, -151.0f), 128.0f);
+  const float t = xc + M;
+  const float n = t - M;
+  const float f = xc - n;
+  float p = VLT_EXP2_C6;
+  if (kFused) {
+    p = fma_(p, f, VLT_EXP2_C5);
+    p = fma_(p, f, VLT_EXP2_C4);
+    p = fma_(p, f, VLT_EXP2_C3);
+    p = fma_(p, f, VLT_EXP2_C2);
+    p = fma_(p, f, VLT_EXP2_C1);
+    p = fma_(p, f, VLT_EXP2_C0);
+  } else {
+    p = p * f + VLT_EXP2_C5;
+    p = p * f + VLT_EXP2_C4;
+    p = p * f + VLT_EXP2_C3;
+    p = p * f + VLT_EXP2_C2;
+    p = p * f + VLT_EXP2_C1;
+    p = p * f + VLT_EXP2_C0;
+  }
+  const int32_t ni = (int32_t)(as_uint(t) - 0x4B400000u);
+  const int32_t e1 = ni < -126 ? -126 : (ni > 127 ? 127 : ni);
+  const int32_t e2 = ni - e1;
+  const float r = (p * as_float((uint32_t)(e1 + 127) << 23)) * as_float((uint32_t)(e2 + 127) << 23);
+  const float hi = is_nan(x) ? as_float(0x7FFFFFFFu) : as_float(0x7F800000u);
+  return x < -151.0f ? 0.0f : ((x >= 128.0f || is_nan(x)) ? hi : r);
+}
+
+VLT_HD float exp2_(float x) { return exp2_select<false>(x); }
 
 #define VLT_LOG2E 1.44269502162933349609375f  // 0x3fb8aa3b
 
@@ -157,32 +224,30 @@ VLT_HD float exp_(float x) { return exp2_(x * VLT_LOG2E); }
 #define VLT_LOG2_K7 0.4121985733509063720703f     // 2/(7 ln2)    0x3ed30bb1
 #define VLT_LOG2_K9 0.3205988407135009765625f     // 2/(9 ln2)    0x3ea4258a
 
+// Without branches (special operands selected at the end): the same bits as the
+// piecewise form for every binary32 x.
 VLT_HD float log2_(float x) {
-  uint32_t u = as_uint(x);
-  if (is_nan(x) || (u & 0x80000000u) && (u & 0x7FFFFFFFu)) return as_float(0x7FFFFFFFu);
-  if ((u & 0x7FFFFFFFu) == 0u) return as_float(0xFF800000u);
-  if (u == 0x7F800000u) return x;
-  int32_t e = 0;
-  if (u < 0x00800000u) {  // denormal: scale by 2^24
-    x = x * 16777216.0f;
-    u = as_uint(x);
-    e = -24;
-  }
-  e += (int32_t)(u >> 23) - 127;
-  uint32_t mb = (u & 0x007FFFFFu) | 0x3F800000u;
-  if (mb > 0x3FB504F3u) {  // m > sqrt(2): use m/2
-    mb -= 0x00800000u;
-    e += 1;
-  }
-  float m = as_float(mb);
-  float t = (m - 1.0f) / (m + 1.0f);
-  float s = t * t;
+  const uint32_t u = as_uint(x);
+  const bool den = u < 0x00800000u;  // +0 and positive denormals: scale by 2^24
+  const float xs = den ? x * 16777216.0f : x;
+  const uint32_t us = as_uint(xs);
+  int32_t e = (den ? -24 : 0) + (int32_t)((us >> 23) & 0xFFu) - 127;
+  uint32_t mb = (us & 0x007FFFFFu) | 0x3F800000u;
+  const bool hi = mb > 0x3FB504F3u;  // m > sqrt(2): use m/2
+  mb = hi ? mb - 0x00800000u : mb;
+  e = hi ? e + 1 : e;
+  const float m = as_float(mb);
+  const float t = (m - 1.0f) / (m + 1.0f);
+  const float s = t * t;
   float p = VLT_LOG2_K9;
   p = p * s + VLT_LOG2_K7;
   p = p * s + VLT_LOG2_K5;
   p = p * s + VLT_LOG2_K3;
   p = p * s + VLT_LOG2_K1;
-  return (float)e + t * p;
+  const float r = (float)e + t * p;
+  const bool nan_out = is_nan(x) || ((u & 0x80000000u) && (u & 0x7FFFFFFFu));
+  return nan_out ? as_float(0x7FFFFFFFu)
+                 : ((u & 0x7FFFFFFFu) == 0u ? as_float(0xFF800000u) : (u == 0x7F800000u ? x : r));
 }
 
 // ---------------------------------------------------------------- own sin/cos
@@ -212,28 +277,24 @@ VLT_HD float cos_poly(float r) {
   return 1.0f + s * p;
 }
 
+// Quadrant selection and the out-of-range result (NaN for NaN, inf and |x| > 65536)
+// by selects, without branches.
 VLT_HD void sincos_(float x, float* sp, float* cp) {
-  if (!(fabs_(x) <= 65536.0f)) {  // NaN, inf, or out of the supported range
-    *sp = as_float(0x7FFFFFFFu);
-    *cp = as_float(0x7FFFFFFFu);
-    return;
-  }
-  float k = rint_(x * VLT_TWO_OVER_PI);
-  float r = x - k * VLT_PIO2_C1;
+  const bool ok = fabs_(x) <= 65536.0f;
+  const float xs = ok ? x : 0.0f;
+  float k = rint_(xs * VLT_TWO_OVER_PI);
+  float r = xs - k * VLT_PIO2_C1;
   r = r - k * VLT_PIO2_C2;
   r = r - k * VLT_PIO2_C3;
-  int32_t q = f2i_rz(k) & 3;
-  float s = sin_poly(r);
-  float c = cos_poly(r);
-  float so, co;
-  switch (q) {
-    case 0: so = s; co = c; break;
-    case 1: so = c; co = -s; break;
-    case 2: so = -s; co = -c; break;
-    default: so = -c; co = s; break;
-  }
-  *sp = so;
-  *cp = co;
+  const int32_t q = f2i_rz(k) & 3;
+  const float s = sin_poly(r);
+  const float c = cos_poly(r);
+  float so = (q & 1) ? c : s;
+  float co = (q & 1) ? s : c;
+  so = (q & 2) ? -so : so;
+  co = ((q + 1) & 2) ? -co : co;
+  *sp = ok ? so : as_float(0x7FFFFFFFu);
+  *cp = ok ? co : as_float(0x7FFFFFFFu);
 }
 
 VLT_HD float sin_(float x) { float s, c; sincos_(x, &s, &c); return s; }
@@ -249,56 +310,10 @@ VLT_HD float pow_2k(float x, int k) {
 
 // ------------------------------------------------------------------- vectors
 
-// One IEEE fusedMultiplyAdd (the float forms' denoiser contract).
-VLT_HD float fma_(float a, float b, float c) {
-#if defined(__CUDA_ARCH__)
-  return __fmaf_rn(a, b, c);
-#else
-  return fmaf(a, b, c);
-#endif
-}
-
-// 2^x: x = n + f, n = rint(x), p(f) by FMA Horner steps with the coefficients of
-// exp2_, then p * 2^n (two-step scale below 2^-126 keeps gradual underflow exact).
-VLT_HD float exp2_fma_full(float x) {
-  if (is_nan(x)) return as_float(0x7FFFFFFFu);
-  if (x >= 128.0f) return as_float(0x7F800000u);
-  if (x < -151.0f) return 0.0f;
-  float n = rint_(x);
-  float f = x - n;
-  float p = VLT_EXP2_C6;
-  p = fma_(p, f, VLT_EXP2_C5);
-  p = fma_(p, f, VLT_EXP2_C4);
-  p = fma_(p, f, VLT_EXP2_C3);
-  p = fma_(p, f, VLT_EXP2_C2);
-  p = fma_(p, f, VLT_EXP2_C1);
-  p = fma_(p, f, VLT_EXP2_C0);
-  int32_t ni = f2i_rz(n);
-  if (ni > 127) return (p * 2.0f) * as_float(0x7F000000u);
-  if (ni < -126) return (p * as_float(0x00800000u)) * as_float((uint32_t)(ni + 126 + 127) << 23);
-  return p * as_float((uint32_t)(ni + 127) << 23);
-}
-// The same function with a short path for x in [-126, 0], the range of every
-// edge-stopping weight: n = rint(x) from the 1.5 * 2^23 shifter (x + M rounds to an
-// integer with ties to even for |x| < 2^22, and the integer is in t's low mantissa
-// bits), and 2^n is a normal number. Bit-identical to exp2_fma_full there (an
-// exhaustive host comparison over [-127, 1] found no difference; the GPU tests
-// compare both with the oracle on a dense sweep of that range).
-VLT_HD float exp2_fma(float x) {
-  if (!(x >= -126.0f && x <= 0.0f)) return exp2_fma_full(x);
-  const float M = 12582912.0f;
-  const float t = x + M;
-  const float n = t - M;
-  const float f = x - n;
-  float p = VLT_EXP2_C6;
-  p = fma_(p, f, VLT_EXP2_C5);
-  p = fma_(p, f, VLT_EXP2_C4);
-  p = fma_(p, f, VLT_EXP2_C3);
-  p = fma_(p, f, VLT_EXP2_C2);
-  p = fma_(p, f, VLT_EXP2_C1);
-  p = fma_(p, f, VLT_EXP2_C0);
-  return p * as_float((as_uint(t) - 0x4B3FFF81u) << 23);  // 2^(n + 127 - 127)
-}
+// 2^x with FMA Horner steps (the float forms' denoiser contract): the piecewise
+// form, and the branch-free form the kernels use.
+VLT_HD float exp2_fma_full(float x) { return exp2_piecewise<true>(x); }
+VLT_HD float exp2_fma(float x) { return exp2_select<true>(x); }
 
 struct f2 { float x, y; };
 struct f3 { float x, y, z; };
