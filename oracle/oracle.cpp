@@ -1432,8 +1432,8 @@ void dn_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, const
 // Numeric contract of this form: binary32 with explicit fused multiply-adds. Each
 // fma_() is one IEEE fusedMultiplyAdd (std::fmaf), every other operation is rounded
 // separately (-ffp-contract=off), and exp is exp_fma (the exp2 construction above
-// evaluated by FMA Horner steps; the a-trous edge weights use exp_weight, which is
-// zero below 2^-126). The product's f32-form kernels evaluate the same
+// evaluated by FMA Horner steps; the a-trous edge weights use exp2_weight, the same
+// in base 2, zero below 2^-126). The product's f32-form kernels evaluate the same
 // expressions in the same order, so the results are reproduced bit for bit.
 inline float fma_(float a, float b, float c) { return std::fmaf(a, b, c); }
 inline float exp2_fma(float x) {
@@ -1452,12 +1452,9 @@ inline float exp2_fma(float x) {
   return p * asfloat((uint32_t)(e + 127) << 23);
 }
 inline float exp_fma(float x) { return exp2_fma(x * 1.44269502162933349609375f); }
-// The a-trous edge weight's exponential: exp_fma where x log2 e >= -126, zero below
-// that and for NaN. Its argument is never positive (a sum of non-positive terms).
-inline float exp_weight(float x) {
-  const float y = x * 1.44269502162933349609375f;
-  return y >= -126.0f ? exp2_fma(y) : 0.0f;
-}
+// The a-trous edge weight's exponential, in base 2: exp2_fma(y) where rint(y) >= -126
+// (y >= -126.5), zero below that and for NaN.
+inline float exp2_weight(float y) { return y >= -126.5f ? exp2_fma(y) : 0.0f; }
 // luminance (util.hlsl:21-24) as r*0.2126, then two FMAs.
 inline float lum_fma(float3 c) { return fma_(c.z, 0.0722f, fma_(c.y, 0.7152f, c.x * 0.2126f)); }
 inline float3 fma3(float w, float3 v, float3 acc) {
@@ -1496,17 +1493,20 @@ struct EdgeStop32 {
     }
     return F2(wn * exp_fma(ax), wn * exp_fma(ay));
   }
-  // The a-trous form: depth term -dist_z * r_z with r_z = 1 / (fz_sigma * d + 1e-8)
-  // computed once per distinct tap distance d, luminance term always on.
-  float2 weight_rz(float r_z, float depth, float3 normal, float2 lumi) const {
+  // The a-trous form, in base 2: depth term -dist_z * r_z with
+  // r_z = log2(e) / (fz_sigma * d + 1e-8) computed once per distinct tap distance d,
+  // lumi_rcp scaled by log2(e), luminance term always on, and the kernel weight k
+  // multiplied into the normal term.
+  float2 weight_rz(float r_z, float k, float depth, float3 normal, float2 lumi) const {
     float wz = -fabsf(depth - depth_center) * r_z;
     float n_dot = saturate(fma_(normal_center.z, normal.z, fma_(normal_center.y, normal.y,
                                                                   normal_center.x * normal.x)));
     float wn = n_dot;
-    for (int k = 0; k < n_log2; ++k) wn = wn * wn;
+    for (int k2 = 0; k2 < n_log2; ++k2) wn = wn * wn;
+    float kw = k * wn;
     float ax = fma_(-fabsf(lumi.x - lumi_center.x), lumi_rcp.x, wz);
     float ay = fma_(-fabsf(lumi.y - lumi_center.y), lumi_rcp.y, wz);
-    return F2(wn * exp_weight(ax), wn * exp_weight(ay));
+    return F2(kw * exp2_weight(ax), kw * exp2_weight(ay));
   }
 };
 
@@ -1879,13 +1879,16 @@ void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, con
       EdgeStop32 es = EdgeStop32::create(depth_tex[i], gbuffer.fwidth_z, 1.0f, gbuffer.normal, 7);
       es.use_lumi = true;
       es.lumi_center = F2(lum_fma(c.d), lum_fma(c.s));
-      es.lumi_rcp = F2(1.0f / fma_(4.0f, sqrtf(c.aux.x), 1e-8f), 1.0f / fma_(4.0f, sqrtf(c.aux.y), 1e-8f));
-      // r_z per |offset| class (1,1), (1,2)/(2,1), (2,2).
+      const float log2e = 1.44269502162933349609375f;
+      es.lumi_rcp = F2((1.0f / fma_(4.0f, sqrtf(c.aux.x), 1e-8f)) * log2e,
+                       (1.0f / fma_(4.0f, sqrtf(c.aux.y), 1e-8f)) * log2e);
+      // r_z per |offset| class (1,1), (1,2)/(2,1), (2,2), scaled by log2(e) and clamped
+      // at 0 (the weight exponents are then never positive).
       float rz[3][3];
       for (int ay = 1; ay <= 2; ++ay)
         for (int ax = 1; ax <= 2; ++ax) {
           float fx = (float)(ax * step), fy = (float)(ay * step);
-          rz[ay][ax] = 1.0f / fma_(es.fz_sigma, sqrtf(fx * fx + fy * fy), 1e-8f);
+          rz[ay][ax] = fmaxf((1.0f / fma_(es.fz_sigma, sqrtf(fx * fx + fy * fy), 1e-8f)) * log2e, 0.0f);
         }
       float3 dsum = c.d, ssum = c.s;
       float2 vsum = c.aux, wsum = F2(1.0f, 1.0f);
@@ -1900,9 +1903,8 @@ void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, con
           const float kw = kwy * kernel_weights[std::abs(ox)];
           size_t j = (size_t)uy * w + ux;
           Rec32 r = IO::load(in, j);
-          float2 e = es.weight_rz(rz[std::abs(oy)][std::abs(ox)], depth_tex[j],
-                                  load_gbuffer_normal(gbuf, ux, uy, w, h), F2(lum_fma(r.d), lum_fma(r.s)));
-          float2 wt = F2(kw * e.x, kw * e.y);
+          float2 wt = es.weight_rz(rz[std::abs(oy)][std::abs(ox)], kw, depth_tex[j],
+                                   load_gbuffer_normal(gbuf, ux, uy, w, h), F2(lum_fma(r.d), lum_fma(r.s)));
           dsum = fma3(wt.x, r.d, dsum);
           ssum = fma3(wt.y, r.s, ssum);
           vsum = F2(fma_(wt.x * wt.x, r.aux.x, vsum.x), fma_(wt.y * wt.y, r.aux.y, vsum.y));

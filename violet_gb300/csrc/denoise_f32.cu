@@ -12,7 +12,7 @@
 // operation is a separately rounded IEEE operation (the build disables contraction),
 // and exp is exp2_fma: the project's exp2 construction (n = rint(x), degree-6
 // polynomial on [-1/2, 1/2]) evaluated by FMA Horner steps (the a-trous edge weights
-// use exp_weight, the same function with results below 2^-126 set to zero). No approximate
+// use exp2_weight, the same function in base 2, zero below 2^-126). No approximate
 // hardware function is used, so the f32-form denoiser is bit-reproducible by the
 // CPU restatement. That matters here beyond testing: the a-trous luminance weight
 // divides by the square root of a variance computed as E[l^2] - E[l]^2, which
@@ -25,14 +25,14 @@ namespace vlt {
 namespace {
 
 __device__ __forceinline__ float exp_fma(float x) { return exp2_fma(x * VLT_LOG2E); }
-// The a-trous edge-stopping exponential: exp_fma where 2^(x log2 e) is a normal number
-// (x log2 e >= -126), zero below that and for a NaN argument. A weight below 2^-126
-// next to the centre tap's weight of 1 cannot change a sum, and without the
-// subnormal and special-operand cases the function is the short FMA path plus one
-// select: the filter issues 20 % fewer instructions per tap than with the full range.
-__device__ __forceinline__ float exp_weight(float x) {
-  const float y = x * VLT_LOG2E;
-  const float yc = fmax_(y, -126.0f);
+// The a-trous edge weight's exponential, in base 2: 2^y by the FMA exp2 construction
+// where rint(y) >= -126, and zero where rint(y) < -126 (y < -126.5) and for a NaN
+// argument. The argument is clamped at -127, where the shifter's integer builds a
+// zero scale, so the function is the short path plus one max: the filter issues
+// about 20 % fewer instructions per tap than with the full-range exact exp2. A weight
+// below 2^-126 next to the centre tap's weight of 1 cannot change a sum.
+__device__ __forceinline__ float exp2_weight(float y) {
+  const float yc = fmax_(y, -127.0f);
   const float M = 12582912.0f;  // 1.5 * 2^23: yc + M rounds yc to an integer (ties to even)
   const float t = yc + M;
   const float n = t - M;
@@ -44,8 +44,7 @@ __device__ __forceinline__ float exp_weight(float x) {
   p = fma_(p, f, VLT_EXP2_C2);
   p = fma_(p, f, VLT_EXP2_C1);
   p = fma_(p, f, VLT_EXP2_C0);
-  const float r = p * as_float((as_uint(t) - 0x4B3FFF81u) << 23);  // p * 2^n, n in [-126, 0]
-  return y >= -126.0f ? r : 0.0f;
+  return p * as_float((as_uint(t) - 0x4B3FFF81u) << 23);  // 2^n; n = -127 gives +0
 }
 __device__ __forceinline__ float lum_fast(float r, float g, float b) {
   return fma_(b, 0.0722f, fma_(g, 0.7152f, r * 0.2126f));
@@ -148,16 +147,17 @@ struct EdgeStopFast {
     }
     return mk2(wn * exp_fma(ax), wn * exp_fma(ay));
   }
-  // The same with the depth term as -dist_z * r_z, r_z = 1 / (fz_sigma * d + 1e-8)
-  // precomputed by the caller for the tap's distance d (the a-trous taps have only
-  // three distinct distances).
-  __device__ __forceinline__ f2 weight_rz(float r_z, float depth, f3 normal, f2 lumi) const {
+  // The a-trous weight, in base 2 and with the kernel weight k: the depth term as
+  // -dist_z * r_z with r_z = log2(e) / (fz_sigma * d + 1e-8) precomputed by the caller
+  // for the tap's distance d (the a-trous taps have only three distinct distances),
+  // lumi_rcp already scaled by log2(e), and k folded into the normal term.
+  __device__ __forceinline__ f2 weight_rz(float r_z, float k, float depth, f3 normal, f2 lumi) const {
     float wz = -fabsf(depth - depth_center) * r_z;
     float n_dot = saturate(fma_(normal_center.z, normal.z, fma_(normal_center.y, normal.y, normal_center.x * normal.x)));
-    float wn = pow_2k(n_dot, sigma_n_log2);
+    float kw = k * pow_2k(n_dot, sigma_n_log2);
     float ax = fma_(-fabsf(lumi.x - lumi_center.x), lumi_rcp.x, wz);
     float ay = fma_(-fabsf(lumi.y - lumi_center.y), lumi_rcp.y, wz);
-    return mk2(wn * exp_weight(ax), wn * exp_weight(ay));
+    return mk2(kw * exp2_weight(ax), kw * exp2_weight(ay));
   }
 };
 
@@ -531,10 +531,13 @@ __device__ __forceinline__ void atrous_px(int x, int y, int w, int h, const Geo&
   EdgeStopFast es = make_es(geo.dep(i), geo.fwz(i), 1.0f, geo.normal(i), 7);
   es.use_lumi = true;
   es.lumi_center = mk2(lum_fast(c.d.x, c.d.y, c.d.z), lum_fast(c.s.x, c.s.y, c.s.z));
-  es.lumi_rcp = mk2(1.0f / fma_(4.0f, sqrt_(c.aux.x), 1e-8f), 1.0f / fma_(4.0f, sqrt_(c.aux.y), 1e-8f));
-  const float r11 = 1.0f / fma_(es.fz_sigma, td.d11, 1e-8f);
-  const float r12 = 1.0f / fma_(es.fz_sigma, td.d12, 1e-8f);
-  const float r22 = 1.0f / fma_(es.fz_sigma, td.d22, 1e-8f);
+  es.lumi_rcp = mk2((1.0f / fma_(4.0f, sqrt_(c.aux.x), 1e-8f)) * VLT_LOG2E,
+                    (1.0f / fma_(4.0f, sqrt_(c.aux.y), 1e-8f)) * VLT_LOG2E);
+  // Clamped at 0 so that every weight exponent is <= 0 (or NaN) even for a negative
+  // fwidth_z, the domain exp2_weight is exact on.
+  const float r11 = fmax_((1.0f / fma_(es.fz_sigma, td.d11, 1e-8f)) * VLT_LOG2E, 0.0f);
+  const float r12 = fmax_((1.0f / fma_(es.fz_sigma, td.d12, 1e-8f)) * VLT_LOG2E, 0.0f);
+  const float r22 = fmax_((1.0f / fma_(es.fz_sigma, td.d22, 1e-8f)) * VLT_LOG2E, 0.0f);
   const float kw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
   f3 dsum = c.d, ssum = c.s;
   f2 vsum = c.aux;
@@ -555,8 +558,7 @@ __device__ __forceinline__ void atrous_px(int x, int y, int w, int h, const Geo&
       size_t j = (size_t)cy * w + cx;
       Rec r = load_rec(in, j);
       f2 lumi = mk2(lum_fast(r.d.x, r.d.y, r.d.z), lum_fast(r.s.x, r.s.y, r.s.z));
-      f2 e = es.weight_rz(rz, geo.dep(j), geo.normal(j), lumi);
-      f2 wt = mk2(k * e.x, k * e.y);
+      f2 wt = es.weight_rz(rz, k, geo.dep(j), geo.normal(j), lumi);
       dsum = fma3(wt.x, r.d, dsum);
       ssum = fma3(wt.y, r.s, ssum);
       vsum = mk2(fma_(wt.x * wt.x, r.aux.x, vsum.x), fma_(wt.y * wt.y, r.aux.y, vsum.y));
@@ -573,7 +575,7 @@ __device__ __forceinline__ void atrous_px(int x, int y, int w, int h, const Geo&
 
 template <class Geo, int FORM>
 struct Dn32AtrousF {
-  static constexpr int kMinBlocks = 5;  // 51 registers: 10 tiles per SM
+  static constexpr int kMinBlocks = 4;  // 64 registers, 8 tiles per SM (measured best of 2..8)
   static constexpr int kTileX = 32, kTileY = 8;  // measured 5% faster than 32x4
   using R = typename DnT<FORM>::R;
   using L = typename DnT<FORM>::L;
