@@ -392,8 +392,8 @@ struct HgVisualizeF {
     if (c.x == k.checksum) {
       if (color_code) {
         const uint32_t code = k.checksum;
-        color = mk3((float)(code & 0xFFu) / 255.0f, (float)((code >> 8) & 0xFFu) / 255.0f,
-                    (float)(((code >> 16) ^ (code >> 24)) & 0xFFu) / 255.0f);
+        color = mk3(div_u8_255(code & 0xFFu), div_u8_255((code >> 8) & 0xFFu),
+                    div_u8_255(((code >> 16) ^ (code >> 24)) & 0xFFu));
       } else {
         color = mk3(as_float(c.y), as_float(c.z), as_float(c.w));
       }

@@ -138,9 +138,8 @@ __device__ __forceinline__ uint32_t ld_g1(const uint32_t* __restrict__ g, int x,
 // all-zero G-buffer texel gives (the value of an out-of-range texture load).
 
 __device__ __forceinline__ f3 f0_from_layer0(uint32_t e0) {
-  f3 color = mk3((float)(e0 & 0xFFu) / 255.0f, (float)((e0 >> 8) & 0xFFu) / 255.0f,
-                 (float)((e0 >> 16) & 0xFFu) / 255.0f);
-  float metallic = (float)((e0 >> 24) & 0xFFu) / 255.0f;
+  f3 color = mk3(div_u8_255(e0 & 0xFFu), div_u8_255((e0 >> 8) & 0xFFu), div_u8_255((e0 >> 16) & 0xFFu));
+  float metallic = div_u8_255((e0 >> 24) & 0xFFu);
   return specular_f0(color, metallic);
 }
 

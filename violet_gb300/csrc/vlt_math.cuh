@@ -132,6 +132,24 @@ VLT_HD float fma_(float a, float b, float c) {
 #endif
 }
 
+// x / c for an integer x in [0, c], c = 255, 4095 or 65535 (unorm decodes), with the
+// bits of the IEEE quotient: x times the two-term reciprocal hi + lo (hi = RN(1/c),
+// lo = RN(1/c - hi)), the small product added by one fused multiply-add. An
+// exhaustive host comparison over every x in [0, c] found no difference from x / c;
+// the unorm decodes use it because an IEEE division is a long instruction sequence.
+VLT_HD float div_u8_255(uint32_t x) {
+  const float f = (float)x;
+  return fma_(f, 0x1.010102p-8f, f * -0x1.fdfdfep-33f);
+}
+VLT_HD float div_u12_4095(uint32_t x) {
+  const float f = (float)x;
+  return fma_(f, 0x1.001002p-12f, f * -0x1.ffdffep-37f);
+}
+VLT_HD float div_u16_65535(uint32_t x) {
+  const float f = (float)x;
+  return fma_(f, 0x1.0001p-16f, f * 0x1.0001p-48f);
+}
+
 // 2^x in the piecewise form the construction is defined by: NaN, overflow and
 // underflow first, then n = rint(x), f = x - n, p(f) by Horner steps (separately
 // rounded, or fused when kFused), and p * 2^n (two steps below 2^-126 so that gradual
@@ -528,7 +546,7 @@ VLT_HD f3 unpack_r11g11b10(uint32_t u) {
 
 // R8_UNORM store/load (history length).
 VLT_HD uint32_t unorm8_store(float x) { return f2u_rn(saturate(x) * 255.0f); }
-VLT_HD float unorm8_load(uint32_t u) { return (float)u / 255.0f; }
+VLT_HD float unorm8_load(uint32_t u) { return div_u8_255(u & 0xFFu); }
 
 // ------------------------------------------------- octahedral normals (enc)
 
@@ -561,23 +579,23 @@ VLT_HD uint32_t normal_encode_oct_u32(f3 n) {
   return f2u_rz(e.x * 65535.0f) | (f2u_rz(e.y * 65535.0f) << 16);
 }
 VLT_HD f3 normal_decode_oct_u32(uint32_t enc) {
-  return normal_decode_oct(mk2((float)(enc & 0xFFFFu) / 65535.0f, (float)((enc >> 16) & 0xFFFFu) / 65535.0f));
+  return normal_decode_oct(mk2(div_u16_65535(enc & 0xFFFFu), div_u16_65535((enc >> 16) & 0xFFFFu)));
 }
 VLT_HD uint32_t normal_encode_oct_u16(f3 n) {
   f2 e = normal_encode_oct(n);
   return f2u_rz(e.x * 255.0f) | (f2u_rz(e.y * 255.0f) << 8);
 }
 VLT_HD f3 normal_decode_oct_u16(uint32_t enc) {
-  return normal_decode_oct(mk2((float)(enc & 0xFFu) / 255.0f, (float)((enc >> 8) & 0xFFu) / 255.0f));
+  return normal_decode_oct(mk2(div_u8_255(enc & 0xFFu), div_u8_255((enc >> 8) & 0xFFu)));
 }
 
 // ------------------------------------------------------- G-buffer (gbuffer)
 
 // Layer 1 decode (GBufferNormal::decode, gbuffer.hlsl:20-32).
 VLT_HD f3 gbuffer_normal(uint32_t enc1) {
-  return normal_decode_oct(mk2((float)(enc1 & 0xFFFu) / 4095.0f, (float)((enc1 >> 12) & 0xFFFu) / 4095.0f));
+  return normal_decode_oct(mk2(div_u12_4095(enc1 & 0xFFFu), div_u12_4095((enc1 >> 12) & 0xFFFu)));
 }
-VLT_HD float gbuffer_roughness(uint32_t enc1) { return (float)(enc1 >> 24) / 255.0f; }
+VLT_HD float gbuffer_roughness(uint32_t enc1) { return div_u8_255(enc1 >> 24); }
 
 struct GBuffer {
   f3 color;
@@ -591,9 +609,8 @@ struct GBuffer {
 
 VLT_HD GBuffer decode_gbuffer(uint32_t e0, uint32_t e1, uint32_t e2, uint32_t e3) {
   GBuffer g;
-  g.color = mk3((float)(e0 & 0xFFu) / 255.0f, (float)((e0 >> 8) & 0xFFu) / 255.0f,
-                (float)((e0 >> 16) & 0xFFu) / 255.0f);
-  g.metallic = (float)((e0 >> 24) & 0xFFu) / 255.0f;
+  g.color = mk3(div_u8_255(e0 & 0xFFu), div_u8_255((e0 >> 8) & 0xFFu), div_u8_255((e0 >> 16) & 0xFFu));
+  g.metallic = div_u8_255((e0 >> 24) & 0xFFu);
   g.normal = gbuffer_normal(e1);
   g.perceptual_roughness = gbuffer_roughness(e1);
   g.fwidth_z = f16tof32(e2 & 0xFFFFu);
