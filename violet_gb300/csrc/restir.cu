@@ -444,6 +444,21 @@ struct DiffSpatialF {
   static constexpr int kMinBlocks = 4;  // 64 registers: 8 tiles per SM (measured 7% faster)
   static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DiffKnobs kn, Geo geo, const typename AoStore<FORM>::Filt* __restrict__ ao_tex, typename DiffStore<FORM>::CPtr in, typename DiffStore<FORM>::Ptr out, typename DiffStore<FORM>::Light* __restrict__ lighting, uint32_t frame_rand) {
   using S = DiffStore<FORM>;
+  // The spiral's radius and angle offset of tap `it` depend only on it and the tap
+  // count: the block computes them once into shared memory (taps <= 64, blocks of at
+  // least 64 threads) instead of every pixel computing them per tap.
+  __shared__ float2 s_spiral[64];
+  const int n = (int)kn.taps;
+  const float T = 0.6186f * (float)n;
+  {
+    const int tid = (int)(threadIdx.y * blockDim.x + threadIdx.x);
+    __syncthreads();  // a persistent block's previous tile is done with s_spiral
+    if (tid < n) {
+      float theta = VLT_TWO_PI * (((float)tid + 1.0f) / (float)n);
+      s_spiral[tid] = make_float2(VLT_SPIRAL_A * exp_(VLT_SPIRAL_B * theta), theta * T);
+    }
+    __syncthreads();
+  }
   int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
   size_t i = (size_t)y * w + x;
@@ -462,13 +477,11 @@ struct DiffSpatialF {
   radius = fmax_(radius * ao, 1.5f);
   uint32_t rng = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
   float rand_angle = lcg_rand(rng) * VLT_TWO_PI;
-  const int n = (int)kn.taps;
-  const float T = 0.6186f * (float)n;
   for (int it = 0; it < n; ++it) {
-    float theta = VLT_TWO_PI * (((float)it + 1.0f) / (float)n);
-    float rr = VLT_SPIRAL_A * exp_(VLT_SPIRAL_B * theta);
+    const float2 sp = s_spiral[it];
+    float rr = sp.x;
     float s, c;
-    sincos_(theta * T + rand_angle, &s, &c);
+    sincos_(sp.y + rand_angle, &s, &c);
     float ox = rr * c, oy = rr * s;
     int nx = x + f2i_rz(ox * radius), ny = y + f2i_rz(oy * radius);
     nx = nx < 0 ? 0 : (nx > w - 1 ? w - 1 : nx);
