@@ -259,13 +259,18 @@ struct HgSelResolveF {
         storage[base + k].x = c;
       }
     }
+    uint32_t m = 0u;
     for (uint32_t j = lane; j < n; j += 32u) {
       uint32_t q = list[off + j];
       if (q & RESOLVED) continue;
       if (queries[(size_t)q * Q_WORDS + Q_CHECK] != c) continue;
-      atomicMax(selection + base + k, select_word(q, frame_hash, qbits));
+      const uint32_t sw = select_word(q, frame_hash, qbits);
+      m = sw > m ? sw : m;
       list[off + j] = q | RESOLVED;
     }
+    // One atomic per round: the maximum over the lanes' queries of this checksum.
+    m = __reduce_max_sync(0xFFFFFFFFu, m);
+    if (lane == 0u) atomicMax(selection + base + k, m);
     __syncwarp();
   }
 }

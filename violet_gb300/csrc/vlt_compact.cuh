@@ -15,25 +15,30 @@
 namespace vlt {
 
 static constexpr uint32_t kCompactChunk = 2048;  // items per block (kBlock1D threads x 16)
+static constexpr uint32_t kCompactPer = kCompactChunk / kBlock1D;  // consecutive items per thread
+static_assert(kCompactPer * kBlock1D == kCompactChunk, "a chunk is kBlock1D threads x kCompactPer items");
 
+// Every 1D launch has kBlock1D threads per block; thread t of a chunk owns its
+// items [t * kCompactPer, (t + 1) * kCompactPer).
 template <class P>
 struct CompactCountF {
   static __device__ __forceinline__ void run(int x0, int, typename P::Args a, uint32_t n, uint32_t* __restrict__ chunk_count) {
   // x0 = block index * kBlock1D: one chunk per block.
   const uint32_t chunk = (uint32_t)x0 / kBlock1D;
-  const uint32_t base = chunk * kCompactChunk;
+  const uint32_t first = chunk * kCompactChunk + threadIdx.x * kCompactPer;
   uint32_t c = 0;
-  for (uint32_t k = threadIdx.x; k < kCompactChunk; k += blockDim.x) {
-    const uint32_t i = base + k;
+#pragma unroll
+  for (uint32_t k = 0; k < kCompactPer; ++k) {
+    const uint32_t i = first + k;
     if (i < n && P::flag(a, i)) ++c;
   }
   for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
-  __shared__ uint32_t warp_sum[kMaxThreads / 32];
+  __shared__ uint32_t warp_sum[kBlock1D / 32];
   if ((threadIdx.x & 31u) == 0) warp_sum[threadIdx.x >> 5] = c;
   __syncthreads();
   if (threadIdx.x == 0) {
     uint32_t t = 0;
-    for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) t += warp_sum[w];
+    for (uint32_t w = 0; w < kBlock1D / 32; ++w) t += warp_sum[w];
     chunk_count[chunk] = t;
   }
   __syncthreads();  // warp_sum is reused by the block's next chunk (persistent launches)
@@ -75,29 +80,32 @@ template <class P>
 struct CompactScatterF {
   static __device__ __forceinline__ void run(int x0, int, typename P::Args a, uint32_t n, const uint32_t* __restrict__ chunk_offset) {
   const uint32_t chunk = (uint32_t)x0 / kBlock1D;
-  const uint32_t base = chunk * kCompactChunk;
-  __shared__ uint32_t warp_sum[kMaxThreads / 32];
-  __shared__ uint32_t running;
-  if (threadIdx.x == 0) running = chunk_offset[chunk];
-  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  // Rounds of blockDim.x consecutive items, each ranked by a block-wide scan.
-  for (uint32_t r = 0; r < kCompactChunk; r += blockDim.x) {
-    const uint32_t i = base + r + threadIdx.x;
-    const bool f = r + threadIdx.x < kCompactChunk && i < n && P::flag(a, i);
-    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, f);
-    __syncthreads();  // `running` and warp_sum of the previous round are settled
-    if (lane == 0) warp_sum[wid] = __popc(bal);
-    __syncthreads();
-    uint32_t before = running;
-    for (uint32_t w = 0; w < wid; ++w) before += warp_sum[w];
-    if (f) P::emit(a, i, before + __popc(bal & ((1u << lane) - 1u)));
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t t = 0;
-      for (uint32_t w = 0; w < nw; ++w) t += warp_sum[w];
-      running += t;
-    }
+  const uint32_t first = chunk * kCompactChunk + threadIdx.x * kCompactPer;
+  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+  uint32_t flags = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kCompactPer; ++k) {
+    const uint32_t i = first + k;
+    if (i < n && P::flag(a, i)) flags |= 1u << k;
   }
+  // Rank of the thread's first flagged item: the chunk's offset, the flagged items of
+  // the warps before this one and of the lanes before this one (one scan per chunk).
+  const uint32_t c = (uint32_t)__popc(flags);
+  uint32_t incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= (uint32_t)o) incl += v;
+  }
+  __shared__ uint32_t warp_sum[kBlock1D / 32];
+  if (lane == 31u) warp_sum[wid] = incl;
+  __syncthreads();
+  uint32_t rank = chunk_offset[chunk] + incl - c;
+  for (uint32_t w = 0; w < wid; ++w) rank += warp_sum[w];
+#pragma unroll
+  for (uint32_t k = 0; k < kCompactPer; ++k)
+    if (flags & (1u << k)) P::emit(a, first + k, rank++);
+  __syncthreads();  // warp_sum is reused by the block's next chunk (persistent launches)
 }
 };
 
