@@ -113,6 +113,7 @@ struct SelectScratch {
   uint32_t* total;        // [2]: miss-list length, number of buckets with misses
   uint32_t* list;         // [max_queries]
   uint32_t* buckets;      // [num_buckets]: the buckets with misses (any order)
+  uint32_t* miss_bits;    // [max_queries / 32]: bit q of the queries that need an insertion
 };
 
 __host__ __device__ inline size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
@@ -129,11 +130,14 @@ static SelectScratch carve(const HashGridDims& d, void* base) {
   s.list = (uint32_t*)p;
   p += align256((size_t)d.max_queries * 4);
   s.buckets = (uint32_t*)p;
+  p += align256((size_t)d.num_buckets() * 4);
+  s.miss_bits = (uint32_t*)p;
   return s;
 }
 
 size_t hg_select_scratch_bytes(const HashGridDims& d) {
-  return 3 * align256((size_t)d.num_buckets() * 4) + 256 + align256((size_t)d.max_queries * 4);
+  return 3 * align256((size_t)d.num_buckets() * 4) + 256 + align256((size_t)d.max_queries * 4) +
+         align256(((size_t)d.max_queries + 31) / 32 * 4);
 }
 
 __device__ __forceinline__ uint32_t select_word(uint32_t q, uint32_t frame_hash, uint32_t qbits) {
@@ -154,71 +158,87 @@ __device__ __forceinline__ uint32_t probe(const uint4* __restrict__ storage, uin
   return 17u;
 }
 
+// Probe: a query whose cell exists selects it at once (InterlockedMax); a query that
+// needs an insertion counts itself in its bucket and sets its bit in miss_bits (one
+// word per warp, every word of the launch written), so that the scatter pass visits
+// only the misses.
 struct HgSelProbeF {
-  static __device__ __forceinline__ void run(int x0, int y0, uint32_t max_q, const uint32_t* __restrict__ queries, const uint32_t* __restrict__ count, const uint4* __restrict__ storage, uint32_t* __restrict__ selection, uint32_t frame_hash, uint32_t qbits, uint32_t* __restrict__ need_count) {
-  uint32_t q = (uint32_t)x0 + threadIdx.x;
+  static __device__ __forceinline__ void run(int x0, int y0, uint32_t max_q, const uint32_t* __restrict__ queries, const uint32_t* __restrict__ count, const uint4* __restrict__ storage, uint32_t* __restrict__ selection, uint32_t frame_hash, uint32_t qbits, uint32_t* __restrict__ need_count, uint32_t* __restrict__ miss_bits) {
+  const uint32_t q = (uint32_t)x0 + threadIdx.x;
   uint32_t n = *count;
   n = n < max_q ? n : max_q;
-  if (q >= n) return;
-  uint4 rec1 = ((const uint4*)(queries + (size_t)q * Q_WORDS))[1];
-  uint32_t c = rec1.y;
-  if (c == 0u) return;
-  uint32_t base = rec1.x * 16u;
-  uint32_t k = probe(storage, base, c);
-  if (k < 16u) {
-    atomicMax(selection + base + k, select_word(q, frame_hash, qbits));
-  } else if (k == 16u) {
-    atomicAdd(need_count + rec1.x, 1u);
+  bool miss = false;
+  if (q < n) {
+    const uint4 rec1 = ((const uint4*)(queries + (size_t)q * Q_WORDS))[1];
+    const uint32_t c = rec1.y;
+    if (c != 0u) {
+      const uint32_t base = rec1.x * 16u;
+      const uint32_t k = probe(storage, base, c);
+      if (k < 16u) {
+        atomicMax(selection + base + k, select_word(q, frame_hash, qbits));
+      } else if (k == 16u) {
+        atomicAdd(need_count + rec1.x, 1u);
+        miss = true;
+      }
+    }
   }
+  const uint32_t bits = __ballot_sync(0xFFFFFFFFu, miss);
+  if ((threadIdx.x & 31u) == 0u && q < max_q) miss_bits[q >> 5] = bits;
 }
 };
 
+// Segment allocation: block-aggregated (one atomic per block and counter) offsets
+// of the buckets' miss segments and the list of buckets with misses.
 struct HgSelAllocF {
   static __device__ __forceinline__ void run(int x0, int y0, uint32_t num_buckets, uint32_t* __restrict__ need_count, uint32_t* __restrict__ need_offset, uint32_t* __restrict__ total, uint32_t* __restrict__ buckets) {
-  uint32_t b = (uint32_t)x0 + threadIdx.x;
-  uint32_t n = b < num_buckets ? need_count[b] : 0u;
-  // Warp-aggregated appends: one atomic per warp for the miss-list segments and one
-  // for the list of buckets with misses.
-  const uint32_t lane = threadIdx.x & 31u;
+  __shared__ uint32_t s_seg[kBlock1D / 32], s_act[kBlock1D / 32], s_base[2];
+  const uint32_t b = (uint32_t)x0 + threadIdx.x;
+  const uint32_t n = b < num_buckets ? need_count[b] : 0u;
+  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
   const uint32_t act = __ballot_sync(0xFFFFFFFFu, n != 0u);
-  if (act == 0u) return;
   uint32_t incl = n;
   for (int o = 1; o < 32; o <<= 1) {
     uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
     if (lane >= (uint32_t)o) incl += v;
   }
-  const uint32_t warp_total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-  uint32_t seg = 0u, slot = 0u;
-  if (lane == 0) {
-    seg = atomicAdd(total, warp_total);
-    slot = atomicAdd(total + 1, (uint32_t)__popc(act));
+  if (lane == 31u) {
+    s_seg[wid] = incl;
+    s_act[wid] = (uint32_t)__popc(act);
   }
-  seg = __shfl_sync(0xFFFFFFFFu, seg, 0);
-  slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
-  if (n == 0u) return;
-  need_offset[b] = seg + incl - n;
-  need_count[b] = 0u;
-  buckets[slot + __popc(act & ((1u << lane) - 1u))] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t ts = 0u, ta = 0u;
+    for (uint32_t w = 0; w < kBlock1D / 32; ++w) {
+      const uint32_t vs = s_seg[w], va = s_act[w];
+      s_seg[w] = ts;
+      s_act[w] = ta;
+      ts += vs;
+      ta += va;
+    }
+    s_base[0] = ts ? atomicAdd(total, ts) : 0u;
+    s_base[1] = ta ? atomicAdd(total + 1, ta) : 0u;
+  }
+  __syncthreads();
+  if (n != 0u) {
+    need_offset[b] = s_base[0] + s_seg[wid] + incl - n;
+    need_count[b] = 0u;
+    buckets[s_base[1] + s_act[wid] + (uint32_t)__popc(act & ((1u << lane) - 1u))] = b;
+  }
+  __syncthreads();  // the shared words are reused by the block's next tile (persistent launches)
 }
 };
 
+// Scatter of the misses (the bits of miss_bits) into their buckets' segments.
 struct HgSelScatterF {
-  static __device__ __forceinline__ void run(int x0, int y0, uint32_t max_q, const uint32_t* __restrict__ queries, const uint32_t* __restrict__ count, const uint4* __restrict__ storage, uint32_t* __restrict__ need_count, const uint32_t* __restrict__ need_offset, uint32_t* __restrict__ list) {
-  uint32_t q = (uint32_t)x0 + threadIdx.x;
-  uint32_t n = *count;
-  n = n < max_q ? n : max_q;
-  if (q >= n) return;
-  uint4 rec1 = ((const uint4*)(queries + (size_t)q * Q_WORDS))[1];
-  uint32_t c = rec1.y;
-  if (c == 0u) return;
-  uint32_t base = rec1.x * 16u;
-  if (probe(storage, base, c) != 16u) return;
+  static __device__ __forceinline__ void run(int x0, int y0, uint32_t max_q, const uint32_t* __restrict__ queries, const uint32_t* __restrict__ miss_bits, uint32_t* __restrict__ need_count, const uint32_t* __restrict__ need_offset, uint32_t* __restrict__ list) {
+  const uint32_t q = (uint32_t)x0 + threadIdx.x;
+  if (q >= max_q || !((miss_bits[q >> 5] >> (q & 31u)) & 1u)) return;
+  const uint4 rec1 = ((const uint4*)(queries + (size_t)q * Q_WORDS))[1];
   uint32_t pos = atomicAdd(need_count + rec1.x, 1u);
   list[need_offset[rec1.x] + pos] = q;
 }
 };
 
-// One warp per bucket: sequential-order insertion (see the file comment).
 struct HgSelResolveF {
   static __device__ __forceinline__ void run(int x0, int y0, uint32_t n_warps, const uint32_t* __restrict__ queries, uint4* __restrict__ storage, uint32_t* __restrict__ selection, const uint32_t* __restrict__ need_count, const uint32_t* __restrict__ need_offset, uint32_t* __restrict__ list, uint32_t frame_hash, uint32_t qbits, const uint32_t* __restrict__ total, const uint32_t* __restrict__ buckets) {
   // n_warps warps loop over the buckets with misses (their order does not matter:
@@ -441,9 +461,9 @@ void launch_hg_select(const Exec& ex, const HashGridDims& d, const uint32_t* que
   ex_fill32(ex, sc.total, 0u, 8);
   uint32_t nq = d.max_queries;
   launch1d<HgSelProbeF>(ex, "hg_select", nq, nq, queries, count, (const uint4*)storage, selection, frame_hash, qb,
-                        sc.need_count);
+                        sc.need_count, sc.miss_bits);
   launch1d<HgSelAllocF>(ex, "hg_select", nb, nb, sc.need_count, sc.need_offset, sc.total, sc.buckets);
-  launch1d<HgSelScatterF>(ex, "hg_select", nq, nq, queries, count, (const uint4*)storage, sc.need_count,
+  launch1d<HgSelScatterF>(ex, "hg_select", nq, nq, queries, (const uint32_t*)sc.miss_bits, sc.need_count,
                           (const uint32_t*)sc.need_offset, sc.list);
   // One warp per bucket with misses, at most a full device of warps looping over them.
   const uint64_t cap = (uint64_t)device_sm_count() * 64u;
