@@ -256,6 +256,30 @@ struct HgSelResolveF {
   uint32_t off = need_offset[bucket];
   uint32_t base = bucket * 16u;
   uint32_t cs = lane < 16u ? storage[base + lane].x : 0xFFFFFFFFu;  // lanes >= 16 never match
+  if (n <= 32u) {
+    // At most one miss per lane: the rounds run on registers.
+    const uint32_t q = lane < n ? list[off + lane] : 0xFFFFFFFFu;
+    const uint32_t qc = lane < n ? queries[(size_t)q * Q_WORDS + Q_CHECK] : 0u;
+    bool open = lane < n;
+    while (true) {
+      const uint32_t qmin = __reduce_min_sync(0xFFFFFFFFu, open ? q : 0xFFFFFFFFu);
+      if (qmin == 0xFFFFFFFFu) break;
+      const uint32_t owner = (uint32_t)__ffs(__ballot_sync(0xFFFFFFFFu, open && q == qmin)) - 1u;
+      const uint32_t c = __shfl_sync(0xFFFFFFFFu, qc, owner);
+      const uint32_t hit = __ballot_sync(0xFFFFFFFFu, lane < 16u && (cs == c || cs == 0u));
+      if (hit == 0u) break;  // bucket full: every remaining query fails
+      const uint32_t k = (uint32_t)__ffs(hit) - 1u;
+      if (__shfl_sync(0xFFFFFFFFu, cs, k) == 0u && lane == k) {
+        cs = c;
+        storage[base + k].x = c;
+      }
+      const bool mine = open && qc == c;
+      const uint32_t m = __reduce_max_sync(0xFFFFFFFFu, mine ? select_word(q, frame_hash, qbits) : 0u);
+      if (lane == 0u) atomicMax(selection + base + k, m);
+      open = open && !mine;
+    }
+    return;
+  }
   const uint32_t RESOLVED = 0x80000000u;
   for (int round = 0; round < 17; ++round) {
     uint32_t qmin = 0xFFFFFFFFu;
