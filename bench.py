@@ -17,7 +17,8 @@ arithmetic. A step is one frame of that view. The reference-storage-form
           back, inside the timed region (a copy stream overlaps frame f+2's upload
           and frame f's read-back with frame f+1's compute);
   roofline: the dominant pass (per-pass CUDA-event timers of the library) against
-          the measured HBM copy bandwidth;
+          the measured HBM copy bandwidth; issue_roofline: the same launch against
+          the SMs' warp-instruction issue rate (the bound of that pass);
   cpu_baseline: the CPU oracle (restatement of the reference's passes) on the
           host cores, on a bounded sample of the same workload.
 
@@ -91,6 +92,11 @@ PASS_BYTES_PER_CELL = {"hg_decay": 2, "hg_compact": 4}
 # DRAM bytes per launch unit measured with ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum, one-pass counters; profiles/dn_atrous_f32_540p.md).
 MEASURED_TRAFFIC_PER_UNIT = {"dn_atrous": 64.25}  # B/px: one-pass dram counters, 960x540 f32
+# Warp instructions per launch unit measured with ncu (smsp__inst_executed.sum of a
+# --set full capture / pixels; profiles/dn_atrous_f32_540p.md): the issue roofline
+# of a pass that is bound by instruction issue rather than by HBM.
+MEASURED_WARP_INSTRUCTIONS_PER_UNIT = {"dn_atrous": 21.69e6 / (960 * 540)}
+ISSUE_SLOTS_PER_SM_CLOCK = 4  # one warp instruction per scheduler per clock, 4 schedulers per SM
 
 
 def log(*a):
@@ -373,6 +379,17 @@ def run_ours(args, ws, rank, local):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic * units if traffic else None, "kernel": dom,
                 "alg_bytes_per_launch": alg_bytes, "launch_ms": avg_s * 1e3, "peak_source": peak_src}
+    # The same launch against the SMs' instruction-issue rate at the sampled clock.
+    issue = None
+    wi = MEASURED_WARP_INSTRUCTIONS_PER_UNIT.get(dom)
+    if wi:
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz") or 2070.0
+        ipeak = sms * ISSUE_SLOTS_PER_SM_CLOCK * mhz * 1e6 / 1e9
+        iach = wi * units / avg_s / 1e9
+        issue = {"bound": "issue", "achieved": iach, "peak": ipeak, "unit": "G warp-instructions/s",
+                 "frac": iach / ipeak, "kernel": dom, "warp_instructions_per_unit": wi, "sm_count": sms,
+                 "sm_mhz": mhz, "source": "smsp__inst_executed.sum per pixel (ncu, 960x540 f32)"}
     pass_table = {}
     for k, (nl, tot) in sorted(passes.items()):
         if k in PASS_BYTES_PER_CELL:
@@ -478,6 +495,7 @@ def run_ours(args, ws, rank, local):
             "ref_storage_form": {"value": value_ref, "unit": "Mpix/s", "ms_per_step": ms_ref / args.steps},
             "gpu_launches": launches,
             "roofline": roofline,
+            "issue_roofline": issue,
             "passes": pass_table,
             "cpu_baseline": cpu,
             "clocks": clk,
