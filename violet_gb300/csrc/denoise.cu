@@ -71,6 +71,7 @@ __device__ __forceinline__ float dsr_weight(f3 color, f3 mean, f3 dev) {
 // svgf_temporal_filter.hlsl:96-362.
 template <class Geo>
 struct DnTemporalF {
+  static constexpr int kMinBlocks = 5;  // 51 registers instead of 80 (measured 14% faster)
   static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DenoiseKnobs kn, Geo geo, Geo prev_geo, const uint32_t* __restrict__ gbuf, const uint32_t* __restrict__ diff_src, const uint32_t* __restrict__ spec_src, const uint16_t* __restrict__ ray_len_tex, const float* __restrict__ prev_depth, const uint2* __restrict__ color_hist, const uint32_t* __restrict__ mom_hist, const uint8_t* __restrict__ len_hist, const uint2* __restrict__ fast_hist, uint2* __restrict__ out_color, uint32_t* __restrict__ out_mom, uint8_t* __restrict__ out_len, uint2* __restrict__ out_fast, uint32_t has_history) {
   int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;

@@ -202,6 +202,7 @@ __device__ __forceinline__ float quad_max_len(const N* __restrict__ len, int x, 
 
 template <class Geo, int FORM>
 struct Dn32TemporalF {
+  static constexpr int kMinBlocks = 4;  // 64 registers instead of 96 (measured 20% faster)
   using R = typename DnT<FORM>::R;
   using N = typename DnT<FORM>::N;
   using L = typename DnT<FORM>::L;
