@@ -148,6 +148,11 @@ struct vlt_view {
   bool has_prev_den;
   uint32_t launches;
   Timing* timing;
+  // Side streams of a plain frame: the hash-grid passes and the specular chain run
+  // beside the diffuse chain (fork/join events on the caller's stream).
+  cudaStream_t aux[3];
+  cudaEvent_t ev[6];
+  bool aux_ready;
 };
 
 namespace {
@@ -453,6 +458,13 @@ size_t vlt_view_device_bytes(uint32_t width, uint32_t height, vlt_form form, con
   return layout(&v, nullptr);
 }
 
+static void destroy_side_streams(vlt_view* v) {
+  for (int k = 0; k < 3; ++k)
+    if (v->aux[k]) cudaStreamDestroy(v->aux[k]);
+  for (int k = 0; k < 6; ++k)
+    if (v->ev[k]) cudaEventDestroy(v->ev[k]);
+}
+
 vlt_status vlt_view_create(vlt_ctx* ctx, uint32_t width, uint32_t height, vlt_form form, const vlt_params* params,
                            vlt_view** out) {
   if (!ctx || !out || !params_ok(params) || width == 0 || height == 0 || width > 16384 || height > 16384)
@@ -488,10 +500,17 @@ vlt_status vlt_view_create(vlt_ctx* ctx, uint32_t width, uint32_t height, vlt_fo
     delete v;
     return VLT_ERR_OUT_OF_MEMORY;
   }
+  v->aux_ready = true;
+  for (int k = 0; k < 3; ++k)
+    if (cudaStreamCreateWithFlags(&v->aux[k], cudaStreamNonBlocking) != cudaSuccess) v->aux_ready = false;
+  for (int k = 0; k < 6; ++k)
+    if (cudaEventCreateWithFlags(&v->ev[k], cudaEventDisableTiming) != cudaSuccess) v->aux_ready = false;
+  (void)cudaGetLastError();  // without side streams the frame runs on the caller's stream alone
   vlt_status st = reset_state(v, 0);
   if (st == VLT_OK) st = cuda_status(cudaStreamSynchronize(0));
   if (st != VLT_OK) {
     cudaFree(v->pool.p);
+    destroy_side_streams(v);
     delete v->timing;
     delete v;
     return st;
@@ -503,6 +522,7 @@ vlt_status vlt_view_create(vlt_ctx* ctx, uint32_t width, uint32_t height, vlt_fo
 vlt_status vlt_view_destroy(vlt_view* v) {
   if (!v) return VLT_OK;
   if (v->pool.p) cudaFree(v->pool.p);
+  destroy_side_streams(v);
   delete v->timing;
   delete v;
   return VLT_OK;
@@ -758,6 +778,22 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     }                                                            \
   } while (0)
 
+  // Plain frames run four chains at once: the hash-grid passes (side stream 0), the
+  // specular resampling (side stream 1) and the AO passes (side stream 2), both after
+  // the surface pass, and the rest on the caller's stream. The AO joins before the
+  // diffuse spatial passes, the specular chain before the denoiser, the hash grid at
+  // the end of the frame. With per-pass timers, in batches and in traced mode (whose
+  // shading reads the hash grid) everything stays on one stream.
+  const bool conc = !rec && !tm.enabled && !traced && v->aux_ready;
+  Exec exh = ex, exs = ex, exa = ex;
+  if (conc) {
+    exh.stream = v->aux[0];
+    exs.stream = v->aux[1];
+    exa.stream = v->aux[2];
+    cudaEventRecord(v->ev[0], s);
+    cudaStreamWaitEvent(v->aux[0], v->ev[0], 0);
+  }
+
   // Surface attributes of this frame, decoded once (the previous frame's planes
   // stay in the other slot).
   const int sc = v->surf_cur ^ 1;
@@ -765,6 +801,11 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   GeoArgs pga = {prev_depth, nullptr, fp.prev_inv_view_proj, b.surf[sc ^ 1][0], b.surf[sc ^ 1][1],
                  b.surf[sc ^ 1][2]};
   STAGE("surface", launch_surface(ex, fp, w, h, in->depth, in->gbuffer, b.surf[sc][0], b.surf[sc][1], b.surf[sc][2]));
+  if (conc) {
+    cudaEventRecord(v->ev[1], s);
+    cudaStreamWaitEvent(v->aux[1], v->ev[1], 0);
+    cudaStreamWaitEvent(v->aux[2], v->ev[1], 0);
+  }
 
   const int form = (int)v->form;
   const bool f32 = form == FORM_F32;
@@ -782,18 +823,18 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   // last frame's queries, then this frame's queries. In traced mode the first three
   // ran in vlt_frame_trace; the update shades the traced hits.
   if (P.hg_enable && P.hg_decay && !traced) {
-    STAGE("hg_decay", launch_hg_decay(ex, v->hg, b.hg_decay, b.hg_storage));
+    STAGE("hg_decay", launch_hg_decay(exh, v->hg, b.hg_decay, b.hg_storage));
   }
   if (has_prev) {
     uint32_t seed_select = fr.next();
     uint32_t seed_update = fr.next();  // the cache rays (vlt_frame_trace)
     (void)seed_update;
     if (P.hg_enable && !traced) {
-      ex_fill32(ex, b.hg_sel, 0u, (size_t)v->hg.num_cells() * 4);
-      STAGE("hg_select", launch_hg_select(ex, v->hg, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], b.hg_storage,
+      ex_fill32(exh, b.hg_sel, 0u, (size_t)v->hg.num_cells() * 4);
+      STAGE("hg_select", launch_hg_select(exh, v->hg, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], b.hg_storage,
                                           b.hg_sel, seed_select, b.hg_scratch));
-      STAGE("hg_compact", launch_hg_compact(ex, v->hg, b.hg_sel, b.hg_cidx, b.hg_caddr, b.hg_ccount, b.scan));
-      STAGE("hg_update", launch_hg_update(ex, v->hg, b.hg_queries[v->hg_qcur], b.hg_cidx, b.hg_caddr, b.hg_ccount,
+      STAGE("hg_compact", launch_hg_compact(exh, v->hg, b.hg_sel, b.hg_cidx, b.hg_caddr, b.hg_ccount, b.scan));
+      STAGE("hg_update", launch_hg_update(exh, v->hg, b.hg_queries[v->hg_qcur], b.hg_cidx, b.hg_caddr, b.hg_ccount,
                                           b.hg_storage, b.hg_decay));
       v->hg_qcur ^= 1;
     }
@@ -805,7 +846,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     }
   }
   if (P.hg_enable && !traced) {
-    STAGE("hg_emit", launch_hg_emit(ex, fp, w, h, v->hg, P.hg_key_mode, in->depth, in->diff_hit_pos_normal,
+    STAGE("hg_emit", launch_hg_emit(exh, fp, w, h, v->hg, P.hg_key_mode, in->depth, in->diff_hit_pos_normal,
                                     in->diff_hit_radiance, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur]));
   }
   // Ind. Diff. Sample Gen. (no seed on validation frames, restir_renderer.rs:460-494)
@@ -840,9 +881,9 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
 
   // AO.
   int ao_cur = v->ao_prev ^ 1;
-  STAGE("ao_gen", launch_ao_gen(ex, form, fp, w, h, ga, diff_hpn, b.ao[v->ao_prev], b.ao[ao_cur], has_new,
+  STAGE("ao_gen", launch_ao_gen(exa, form, fp, w, h, ga, diff_hpn, b.ao[v->ao_prev], b.ao[ao_cur], has_new,
                                 has_prev ? 1u : 0u, P.ao_radius));
-  STAGE("ao_filter", launch_ao_filter(ex, form, w, h, in->depth, b.ao[ao_cur], b.ao_filtered));
+  STAGE("ao_filter", launch_ao_filter(exa, form, w, h, in->depth, b.ao[ao_cur], b.ao_filtered));
   v->ao_prev = ao_cur;
 
   // Indirect diffuse: temporal then spatial pass(es).
@@ -853,6 +894,10 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   STAGE("diff_temporal", launch_diff_temporal(ex, form, fp, w, h, dk, ga, prev_depth, diff_hpn, diff_rad,
                                               traced ? nullptr : in->diff_source_pdf, b.diff_rsv[p], b.diff_rsv[t],
                                               seed_dt, has_prev ? 1u : 0u, has_new));
+  if (conc) {
+    cudaEventRecord(v->ev[4], v->aux[2]);
+    cudaStreamWaitEvent(s, v->ev[4], 0);
+  }
   int src = t, dst = o;
   for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
     bool last = k + 1 == P.diff_spatial_passes;
@@ -873,7 +918,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
                                               b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], b.scan));
   }
   uint32_t seed_st = fr.next();
-  STAGE("spec_temporal", launch_spec_temporal(ex, form, fp, w, h, P.spec_m_cap, ga, pga, prev_depth, b.spec_rsv[sp],
+  STAGE("spec_temporal", launch_spec_temporal(exs, form, fp, w, h, P.spec_m_cap, ga, pga, prev_depth, b.spec_rsv[sp],
                                               b.spec_hp[sp], b.spec_rad[sp], in->spec_hit_pos, in->spec_hit_radiance,
                                               b.spec_rsv[st], b.spec_hp[st], b.spec_rad[st], seed_st,
                                               has_prev ? 1u : 0u));
@@ -884,7 +929,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
       bool last = k + 1 == P.spec_spatial_passes;
       uint32_t seed_ss = fr.next();
       STAGE("spec_spatial",
-            launch_spec_spatial(ex, form, fp, w, h, sk, ga, b.spec_rsv[ssrc], b.spec_hp[ssrc], b.spec_rad[ssrc],
+            launch_spec_spatial(exs, form, fp, w, h, sk, ga, b.spec_rsv[ssrc], b.spec_hp[ssrc], b.spec_rad[ssrc],
                                 last ? b.spec_light : nullptr, last ? b.ray_len : nullptr,
                                 last ? nullptr : b.spec_rsv[sdst], last ? nullptr : b.spec_hp[sdst],
                                 last ? nullptr : b.spec_rad[sdst], seed_ss));
@@ -893,6 +938,10 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   }
   // The temporal reservoir is next frame's history (restir_renderer.rs:1018-1022).
   v->spec_prev = st;
+  if (conc) {
+    cudaEventRecord(v->ev[2], v->aux[1]);
+    cudaStreamWaitEvent(s, v->ev[2], 0);
+  }
 
   // Denoiser.
   const bool run_denoiser = P.denoise && has_prev;
@@ -1043,6 +1092,10 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   v->prev_den = den ? den : b.diff_light;
   v->prev_den_stride = den ? 2 : 1;
   v->has_prev_den = true;
+  if (conc) {
+    cudaEventRecord(v->ev[3], v->aux[0]);
+    cudaStreamWaitEvent(s, v->ev[3], 0);
+  }
   v->frames += 1;
   v->launches = launches;
 #undef STAGE
