@@ -783,9 +783,17 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   // the surface pass, and the rest on the caller's stream. The AO joins before the
   // diffuse spatial passes, the specular chain before the denoiser, the hash grid at
   // the end of the frame. With per-pass timers, in batches and in traced mode (whose
-  // shading reads the hash grid) everything stays on one stream.
+  // shading reads the hash grid) everything stays on one stream. A recorded frame
+  // (batches) tags its jobs with the same lanes and marks the fork and the joins; the
+  // batch runs each lane's batched launches on a stream of its own.
   const bool conc = !rec && !tm.enabled && !traced && v->aux_ready;
+  const bool lanes = rec && !traced;
   Exec exh = ex, exs = ex, exa = ex;
+  if (lanes) {
+    exh.lane = 1;
+    exs.lane = 2;
+    exa.lane = 3;
+  }
   if (conc) {
     exh.stream = v->aux[0];
     exs.stream = v->aux[1];
@@ -806,6 +814,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     cudaStreamWaitEvent(v->aux[1], v->ev[1], 0);
     cudaStreamWaitEvent(v->aux[2], v->ev[1], 0);
   }
+  if (lanes) record_marker(ex, kMarkFork);
 
   const int form = (int)v->form;
   const bool f32 = form == FORM_F32;
@@ -898,6 +907,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     cudaEventRecord(v->ev[4], v->aux[2]);
     cudaStreamWaitEvent(s, v->ev[4], 0);
   }
+  if (lanes) record_marker(ex, kMarkJoin + 3);
   int src = t, dst = o;
   for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
     bool last = k + 1 == P.diff_spatial_passes;
@@ -942,6 +952,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     cudaEventRecord(v->ev[2], v->aux[1]);
     cudaStreamWaitEvent(s, v->ev[2], 0);
   }
+  if (lanes) record_marker(ex, kMarkJoin + 2);
 
   // Denoiser.
   const bool run_denoiser = P.denoise && has_prev;
@@ -1096,6 +1107,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     cudaEventRecord(v->ev[3], v->aux[0]);
     cudaStreamWaitEvent(s, v->ev[3], 0);
   }
+  if (lanes) record_marker(ex, kMarkJoin + 1);
   v->frames += 1;
   v->launches = launches;
 #undef STAGE

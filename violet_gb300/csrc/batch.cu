@@ -59,6 +59,11 @@ struct vlt_batch {
   std::map<const void*, TuneRec> tune;
   std::vector<cudaEvent_t> events;
   vlt_batch_stats stats;
+  // side streams of the lanes (kLanes) and their fork/join events
+  cudaStream_t lane_stream[kLanes] = {};
+  cudaEvent_t fork_event = nullptr;
+  cudaEvent_t join_event[kLanes] = {};
+  bool lanes_ok = false;
 };
 
 namespace {
@@ -67,22 +72,30 @@ const size_t kMaxGraphs = 32;
 
 // Grouping of the recorded jobs into batched launches (see the file comment).
 struct Group {
-  PrepareFn key;
+  PrepareFn key;       // null: a stream marker
+  uint8_t marker = 0;
+  uint8_t lane = 0;
   std::vector<const Job*> jobs;
 };
 
-std::vector<Group> group_jobs(const std::vector<const Recorder*>& recs) {
+// One lane of the recorded frames: its jobs in order (lane 0 keeps the markers).
+struct LaneList {
+  std::vector<const Job*> jobs;
+};
+
+std::vector<Group> group_jobs(const std::vector<LaneList>& lists, uint8_t lane) {
   std::vector<Group> groups;
-  std::vector<size_t> head(recs.size(), 0);
+  std::vector<size_t> head(lists.size(), 0);
+  auto same = [](const Job* a, const Job* c) { return a->prepare == c->prepare && a->marker == c->marker; };
   for (;;) {
-    // Count heads per kernel; pick the most common (first seen on ties).
-    std::vector<std::pair<PrepareFn, uint32_t>> counts;
-    for (size_t k = 0; k < recs.size(); ++k) {
-      if (head[k] >= recs[k]->jobs.size()) continue;
-      PrepareFn f = recs[k]->jobs[head[k]].prepare;
+    // Count heads per kernel (or marker); pick the most common (first seen on ties).
+    std::vector<std::pair<const Job*, uint32_t>> counts;
+    for (size_t k = 0; k < lists.size(); ++k) {
+      if (head[k] >= lists[k].jobs.size()) continue;
+      const Job* f = lists[k].jobs[head[k]];
       bool found = false;
       for (auto& c : counts)
-        if (c.first == f) {
+        if (same(c.first, f)) {
           ++c.second;
           found = true;
           break;
@@ -90,7 +103,7 @@ std::vector<Group> group_jobs(const std::vector<const Recorder*>& recs) {
       if (!found) counts.push_back({f, 1u});
     }
     if (counts.empty()) break;
-    PrepareFn best = counts[0].first;
+    const Job* best = counts[0].first;
     uint32_t bc = counts[0].second;
     for (auto& c : counts)
       if (c.second > bc) {
@@ -98,17 +111,43 @@ std::vector<Group> group_jobs(const std::vector<const Recorder*>& recs) {
         bc = c.second;
       }
     Group g;
-    g.key = best;
-    for (size_t k = 0; k < recs.size(); ++k) {
-      if (head[k] >= recs[k]->jobs.size()) continue;
-      const Job& j = recs[k]->jobs[head[k]];
-      if (j.prepare != best) continue;
-      g.jobs.push_back(&j);
+    g.key = best->prepare;
+    g.marker = best->marker;
+    g.lane = lane;
+    for (size_t k = 0; k < lists.size(); ++k) {
+      if (head[k] >= lists[k].jobs.size()) continue;
+      const Job* j = lists[k].jobs[head[k]];
+      if (!same(j, best)) continue;
+      g.jobs.push_back(j);
       ++head[k];
     }
     groups.push_back(std::move(g));
   }
   return groups;
+}
+
+// The groups of one chunk of views in issue order: the main lane up to the fork
+// marker, then every side lane's groups, then the rest of the main lane (with its
+// join markers).
+std::vector<Group> order_chunk(const std::vector<const Recorder*>& recs) {
+  std::vector<LaneList> lists[kLanes + 1];
+  for (int l = 0; l <= kLanes; ++l) lists[l].resize(recs.size());
+  for (size_t k = 0; k < recs.size(); ++k)
+    for (const Job& j : recs[k]->jobs) lists[j.prepare ? j.lane : 0][k].jobs.push_back(&j);
+  std::vector<Group> main = group_jobs(lists[0], 0);
+  std::vector<Group> out;
+  size_t i = 0;
+  bool forked = false;
+  for (; i < main.size() && !forked; ++i) {
+    forked = !main[i].key && main[i].marker == kMarkFork;
+    out.push_back(std::move(main[i]));
+  }
+  for (int l = 1; l <= kLanes; ++l) {
+    std::vector<Group> g = group_jobs(lists[l], (uint8_t)l);
+    for (Group& x : g) out.push_back(std::move(x));
+  }
+  for (; i < main.size(); ++i) out.push_back(std::move(main[i]));
+  return out;
 }
 
 TileShape shape_for(vlt_batch* b, const Job& j) {
@@ -155,6 +194,12 @@ vlt_status vlt_batch_create(vlt_ctx* ctx, vlt_batch** out) {
   if (!b) return VLT_ERR_OUT_OF_MEMORY;
   b->ctx = ctx;
   memset(&b->stats, 0, sizeof(b->stats));
+  b->lanes_ok = cudaEventCreateWithFlags(&b->fork_event, cudaEventDisableTiming) == cudaSuccess;
+  for (int l = 0; l < kLanes; ++l) {
+    if (cudaStreamCreateWithFlags(&b->lane_stream[l], cudaStreamNonBlocking) != cudaSuccess) b->lanes_ok = false;
+    if (cudaEventCreateWithFlags(&b->join_event[l], cudaEventDisableTiming) != cudaSuccess) b->lanes_ok = false;
+  }
+  (void)cudaGetLastError();  // without side streams every lane runs on the step's stream
   *out = b;
   return VLT_OK;
 }
@@ -164,6 +209,11 @@ vlt_status vlt_batch_destroy(vlt_batch* b) {
   cudaSetDevice(ctx_device(b->ctx));
   for (auto& kv : b->cache) cudaGraphExecDestroy(kv.second.exec);
   for (cudaEvent_t e : b->events) cudaEventDestroy(e);
+  for (int l = 0; l < kLanes; ++l) {
+    if (b->lane_stream[l]) cudaStreamDestroy(b->lane_stream[l]);
+    if (b->join_event[l]) cudaEventDestroy(b->join_event[l]);
+  }
+  if (b->fork_event) cudaEventDestroy(b->fork_event);
   delete b;
   return VLT_OK;
 }
@@ -270,7 +320,7 @@ vlt_status vlt_batch_run(vlt_batch* b, vlt_view* const* views, const vlt_frame_i
   for (const auto& ch : chunks) {
     std::vector<const Recorder*> rs;
     for (uint32_t k : ch) rs.push_back(&recs[k]);
-    std::vector<Group> g = group_jobs(rs);
+    std::vector<Group> g = order_chunk(rs);
     for (Group& x : g) groups.push_back(std::move(x));
   }
   b->stats.last_chunks = (uint32_t)chunks.size();
@@ -278,23 +328,65 @@ vlt_status vlt_batch_run(vlt_batch* b, vlt_view* const* views, const vlt_frame_i
   b->params.clear();
   std::vector<Prepared> preps;
   std::vector<size_t> group_of;  // prepared launch -> group
+  // The step as a list of operations: a prepared launch (>= 0) or a stream marker
+  // (-1 - marker).
+  std::vector<long> ops;
   for (size_t g = 0; g < groups.size(); ++g) {
+    if (!groups[g].key) {
+      ops.push_back(-1 - (long)groups[g].marker);
+      continue;
+    }
     size_t before = preps.size();
     groups[g].key(groups[g].jobs.data(), (uint32_t)groups[g].jobs.size(), shape_for(b, *groups[g].jobs[0]),
                   b->params, preps);
-    for (size_t k = before; k < preps.size(); ++k) group_of.push_back(g);
+    for (size_t k = before; k < preps.size(); ++k) {
+      group_of.push_back(g);
+      ops.push_back((long)k);
+    }
   }
   const uint8_t* params = b->params.data();
 
   // 3. Issue the launches (through a CUDA graph when possible).
   // The legacy default stream cannot be captured: steps on it are issued directly.
   const bool use_graph = b->graphs && !tuning && s != 0;
+  // Side lanes run on their own streams (forked from s after the fork marker, joined
+  // back at their join markers and at the end); timed (tuning) steps run on s alone.
   auto issue = [&](bool timed) -> vlt_status {
-    for (size_t k = 0; k < preps.size(); ++k) {
+    const bool use_lanes = !timed && b->lanes_ok;
+    bool forked = false, joined[kLanes + 1] = {};
+    auto join = [&](int l) {
+      if (!forked || joined[l]) return;
+      cudaEventRecord(b->join_event[l - 1], b->lane_stream[l - 1]);
+      cudaStreamWaitEvent(s, b->join_event[l - 1], 0);
+      joined[l] = true;
+    };
+    for (long op : ops) {
+      if (op < 0) {
+        const int m = (int)(-1 - op);
+        if (!use_lanes) continue;
+        if (m == kMarkFork) {
+          if (forked)
+            for (int l = 1; l <= kLanes; ++l) join(l);  // a chunk's second fork
+          cudaEventRecord(b->fork_event, s);
+          for (int l = 1; l <= kLanes; ++l) {
+            cudaStreamWaitEvent(b->lane_stream[l - 1], b->fork_event, 0);
+            joined[l] = false;
+          }
+          forked = true;
+        } else if (m > kMarkJoin && m <= kMarkJoin + kLanes) {
+          join(m - kMarkJoin);
+        }
+        continue;
+      }
+      const size_t k = (size_t)op;
+      const int lane = groups[group_of[k]].lane;
+      cudaStream_t ls = (use_lanes && forked && lane > 0) ? b->lane_stream[lane - 1] : s;
       if (timed) cudaEventRecord(b->events[2 * k], s);
-      preps[k].launch(preps[k], params, s);
+      preps[k].launch(preps[k], params, ls);
       if (timed) cudaEventRecord(b->events[2 * k + 1], s);
     }
+    if (use_lanes)
+      for (int l = 1; l <= kLanes; ++l) join(l);
     return cuda_status(cudaGetLastError());
   };
   if (tuning) {
@@ -320,7 +412,7 @@ vlt_status vlt_batch_run(vlt_batch* b, vlt_view* const* views, const vlt_frame_i
       t.ns[cand] += ms * 1e6;
     }
     for (const Group& gr : groups) {
-      if (gr.jobs[0]->one_d) continue;
+      if (!gr.key || gr.jobs[0]->one_d) continue;
       double kpix = 0;
       for (const Job* j : gr.jobs) kpix += (double)j->w * j->h / 1e3;
       b->tune[(const void*)gr.key].kpix[cand] += kpix;
@@ -331,8 +423,14 @@ vlt_status vlt_batch_run(vlt_batch* b, vlt_view* const* views, const vlt_frame_i
     std::string sig;
     sig.reserve(preps.size() * 48);
     char buf[96];
-    for (const Prepared& p : preps) {
-      snprintf(buf, sizeof(buf), "%p,%u,%u,%u,%zu;", p.key, p.grid, p.block.x, p.block.y, p.param_bytes);
+    for (long op : ops) {
+      if (op < 0) {
+        snprintf(buf, sizeof(buf), "m%ld;", -1 - op);
+      } else {
+        const Prepared& p = preps[(size_t)op];
+        snprintf(buf, sizeof(buf), "%p,%u,%u,%u,%zu,%u;", p.key, p.grid, p.block.x, p.block.y, p.param_bytes,
+                 (unsigned)groups[group_of[(size_t)op]].lane);
+      }
       sig += buf;
     }
     cudaGraph_t graph = nullptr;

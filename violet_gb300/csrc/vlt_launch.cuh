@@ -37,7 +37,14 @@ struct Exec {
   cudaStream_t stream = 0;
   Recorder* rec = nullptr;
   uint32_t* launches = nullptr;  // counts kernels launched or recorded
+  uint8_t lane = 0;              // recorded jobs: the side stream of the batch step (0: main)
 };
+
+// Stream markers in a recorded frame: the side lanes (1..kLanes) start after
+// kMarkFork; kMarkJoin + k makes the main lane wait for lane k.
+static constexpr int kLanes = 3;
+static constexpr uint8_t kMarkFork = 1;
+static constexpr uint8_t kMarkJoin = 2;
 
 // Tile shape of a 2D launch (block dimensions). One-dimensional work uses
 // kBlock1D threads per block.
@@ -65,12 +72,25 @@ using PrepareFn = void (*)(const Job* const* jobs, uint32_t n, TileShape shape, 
                            std::vector<Prepared>& out);
 
 struct Job {
-  PrepareFn prepare;   // also the grouping key
+  PrepareFn prepare;   // also the grouping key; null for a stream marker
   const char* name;
   uint32_t w, h;       // work shape (h == 1 and one_d for 1D work)
   bool one_d;
+  uint8_t lane = 0;    // side stream (0: main)
+  uint8_t marker = 0;  // kMarkFork / kMarkJoin + lane, for prepare == null
   std::vector<uint8_t> args;
 };
+
+inline void record_marker(const Exec& ex, uint8_t marker) {
+  if (!ex.rec) return;
+  Job j;
+  j.prepare = nullptr;
+  j.name = "stream marker";
+  j.w = j.h = 0;
+  j.one_d = true;
+  j.marker = marker;
+  ex.rec->jobs.push_back(std::move(j));
+}
 
 // ----------------------------------------------------------------- kernels
 
@@ -210,6 +230,7 @@ void record_job(const Exec& ex, const char* name, uint32_t w, uint32_t h, bool o
   j.w = w;
   j.h = h;
   j.one_d = one_d;
+  j.lane = ex.lane;
   j.args.resize(sizeof(Tup));
   memcpy(j.args.data(), &t, sizeof(Tup));
   ex.rec->jobs.push_back(std::move(j));
