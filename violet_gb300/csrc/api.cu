@@ -782,11 +782,14 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   // specular resampling (side stream 1) and the AO passes (side stream 2), both after
   // the surface pass, and the rest on the caller's stream. The AO joins before the
   // diffuse spatial passes, the specular chain before the denoiser, the hash grid at
-  // the end of the frame. With per-pass timers, in batches and in traced mode (whose
-  // shading reads the hash grid) everything stays on one stream. A recorded frame
-  // (batches) tags its jobs with the same lanes and marks the fork and the joins; the
-  // batch runs each lane's batched launches on a stream of its own.
+  // the end of the frame. With per-pass timers everything stays on one stream. A
+  // recorded frame (batches) tags its jobs with the same lanes and marks the fork and
+  // the joins; the batch runs each lane's batched launches on a stream of its own.
   const bool conc = !rec && !tm.enabled && !traced && v->aux_ready;
+  // Traced frames fork the specular and AO chains later (after the shading of the
+  // hits and the specular validation, which they read); their hash-grid work stays
+  // on the caller's stream.
+  const bool conc_t = !rec && !tm.enabled && traced && v->aux_ready;
   const bool lanes = rec && !traced;
   Exec exh = ex, exs = ex, exa = ex;
   if (lanes) {
@@ -794,10 +797,12 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     exs.lane = 2;
     exa.lane = 3;
   }
-  if (conc) {
-    exh.stream = v->aux[0];
+  if (conc || conc_t) {
     exs.stream = v->aux[1];
     exa.stream = v->aux[2];
+  }
+  if (conc) {
+    exh.stream = v->aux[0];
     cudaEventRecord(v->ev[0], s);
     cudaStreamWaitEvent(v->aux[0], v->ev[0], 0);
   }
@@ -887,6 +892,11 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
                                                       wcache, b.q_staging + (size_t)nq * 8 + n * 8));
   }
   const uint32_t has_new = diff_validation ? 0u : 1u;
+  if (conc_t) {
+    cudaEventRecord(v->ev[1], s);
+    cudaStreamWaitEvent(v->aux[1], v->ev[1], 0);
+    cudaStreamWaitEvent(v->aux[2], v->ev[1], 0);
+  }
 
   // AO.
   int ao_cur = v->ao_prev ^ 1;
@@ -903,7 +913,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   STAGE("diff_temporal", launch_diff_temporal(ex, form, fp, w, h, dk, ga, prev_depth, diff_hpn, diff_rad,
                                               traced ? nullptr : in->diff_source_pdf, b.diff_rsv[p], b.diff_rsv[t],
                                               seed_dt, has_prev ? 1u : 0u, has_new));
-  if (conc) {
+  if (conc || conc_t) {
     cudaEventRecord(v->ev[4], v->aux[2]);
     cudaStreamWaitEvent(s, v->ev[4], 0);
   }
@@ -948,7 +958,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   }
   // The temporal reservoir is next frame's history (restir_renderer.rs:1018-1022).
   v->spec_prev = st;
-  if (conc) {
+  if (conc || conc_t) {
     cudaEventRecord(v->ev[2], v->aux[1]);
     cudaStreamWaitEvent(s, v->ev[2], 0);
   }
