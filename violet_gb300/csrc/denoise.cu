@@ -171,17 +171,20 @@ struct DnTemporalF {
         bool cv = px >= 0 && py >= 0 && px <= w - 1 && py <= h - 1;
         if (!cv) continue;
         size_t j = (size_t)py * w + px;
+        // History loads ahead of the geometry test (their latency overlaps its loads).
+        const uint2 c = color_hist[j];
+        const uint32_t mj = mom_hist[j];
+        const uint8_t lj = len_hist[j];
         f3 n = prev_geo.normal(j);
         f3 nd = n - gnormal;
         bool ok = fabs_(prev_depth[j] - reproj_depth) < depth_tol && dot3(nd, nd) < normal_tol_sq;
         if (!ok) continue;
         float wt = wts[oy][ox];
         wsum = wsum + wt;
-        uint2 c = color_hist[j];
         ds = ds + wt * col_diff(c);
         ss = ss + wt * col_spec(c);
-        ms = ms + wt * unpack_half2(mom_hist[j]);
-        hs = hs + wt * unorm8_load(len_hist[j]);
+        ms = ms + wt * unpack_half2(mj);
+        hs = hs + wt * unorm8_load(lj);
         if (kn.fast_history) {
           uint2 f = fast_hist[j];
           dfs = dfs + wt * col_diff(f);

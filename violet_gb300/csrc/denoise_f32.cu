@@ -296,13 +296,16 @@ struct Dn32TemporalF {
         bool cv = px >= 0 && py >= 0 && px <= w - 1 && py <= h - 1;
         if (!cv) continue;
         size_t j = (size_t)py * w + px;
+        // The history record is loaded before the geometry test decides whether it
+        // is used, so that its latency overlaps the test's loads.
+        const Rec r = load_rec(hist, j);
+        const float lj = ld_len(len_hist, j);
         f3 nd = prev_geo.normal(j) - gnormal;
         bool ok = fabs_(prev_depth[j] - reproj_depth) < depth_tol && dot3(nd, nd) < normal_tol_sq;
         if (!ok) continue;
         float wt = wts[oy][ox];
         wsum = wsum + wt;
-        hs = hs + wt * ld_len(len_hist, j);
-        Rec r = load_rec(hist, j);
+        hs = hs + wt * lj;
         ds = fma3(wt, r.d, ds);
         ss = fma3(wt, r.s, ss);
         ms = mk2(fma_(wt, r.aux.x, ms.x), fma_(wt, r.aux.y, ms.y));

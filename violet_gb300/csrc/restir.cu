@@ -695,7 +695,12 @@ struct SpecTemporalF {
   f3 ndc = mk3(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3], hr.z / hr.w - 0.0f);
   f2 uv = mk2(ndc.x * 0.5f + 0.5f, ndc.y * 0.5f + 0.5f);
   bool sample_prev = uv.x == saturate(uv.x) && uv.y == saturate(uv.y) && has_prev_frame;
+  // The previous reservoir at the reprojected pixel is loaded before the depth test
+  // decides whether it is used (its latency overlaps the bilinear depth loads).
+  const int px = (int)f2u_rz(uv.x * (float)w), py = (int)f2u_rz(uv.y * (float)h);
+  SpecSample r;
   if (sample_prev) {
+    r = spec_ld(prev, px, py, w, h);
     float pd = sample_depth(prev_depth, uv, w, h);
     if (fabs_(pd - ndc.z) > 0.001f) sample_prev = false;
   }
@@ -708,8 +713,6 @@ struct SpecTemporalF {
   f3 pn = mk3(0.0f), pf0 = specular_f0(mk3(0.0f), 0.0f);
   float prough = 0.0f;
   if (sample_prev) {
-    int px = (int)f2u_rz(uv.x * (float)w), py = (int)f2u_rz(uv.y * (float)h);
-    SpecSample r = spec_ld(prev, px, py, w, h);
     M = r.M;
     W = r.W;
     rhp = r.hit;
