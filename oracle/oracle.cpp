@@ -1735,22 +1735,6 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
     }
 }
 
-// The float forms' sums over a short-history pixel's taps: 32 lanes (lane t holds tap
-// t of the row-major loop; the 7x7 fallback adds tap t + 32 to lane t; absent taps
-// are zero) combined by xor levels 16, 8, 4, 2, 1 (a[l] + a[l ^ off] for every lane at
-// once). Every lane ends with the same totals; lane 0's are returned.
-template <int K>
-void warp_sum32(float (&a)[32][K], float (&out)[K]) {
-  for (int off = 16; off > 0; off >>= 1) {
-    float b[32][K];
-    for (int l = 0; l < 32; ++l)
-      for (int k = 0; k < K; ++k) b[l][k] = a[l][k] + a[l ^ off][k];
-    for (int l = 0; l < 32; ++l)
-      for (int k = 0; k < K; ++k) a[l][k] = b[l][k];
-  }
-  for (int k = 0; k < K; ++k) out[k] = a[0][k];
-}
-
 // relax_disocclusion_fix.hlsl:27-122.
 template <int FORM>
 void dn32_fix(int w, int h, const float* depth_tex, const uint32_t* gbuf, const void* len, const void* in, void* out) {
@@ -1769,24 +1753,24 @@ void dn32_fix(int w, int h, const float* depth_tex, const uint32_t* gbuf, const 
       if (hl < 4.0f * HISTORY_LEN_UNIT) {
         const GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
         EdgeStop32 es = EdgeStop32::create(depth_tex[i], gbuffer.fwidth_z, 5.0f, gbuffer.normal, 5);
+        float2 ws = F2(0.0f, 0.0f), ms = F2(0.0f, 0.0f);
+        float3 dsum = F3(0.0f), ssum = F3(0.0f);
         const int stride = to_int((14.0f * HISTORY_LEN_UNIT) / hl);
-        float lanes[32][10] = {};
-        for (int t = 0; t < 25; ++t) {
-          const int cx = (t % 5 - 2) * stride, cy = (t / 5 - 2) * stride;
-          const int ux = x + cx, uy = y + cy;
-          if (!in_img(ux, uy, w, h)) continue;
-          const size_t j = (size_t)uy * w + ux;
-          const float2 wt = es.weight(length(F2((float)cx, (float)cy)), depth_tex[j],
-                                      load_gbuffer_normal(gbuf, ux, uy, w, h), F2(0.0f, 0.0f));
-          const Rec32 r = IO::load(in, j);
-          const float v[10] = {wt.x, wt.y, wt.x * r.d.x, wt.x * r.d.y, wt.x * r.d.z,
-                               wt.y * r.s.x, wt.y * r.s.y, wt.y * r.s.z, wt.x * r.aux.x, wt.y * r.aux.y};
-          for (int k = 0; k < 10; ++k) lanes[t][k] = v[k];
-        }
-        float sum[10];
-        warp_sum32(lanes, sum);
-        IO::store(out, i, F3(sum[2], sum[3], sum[4]) * (1.0f / sum[0]), F3(sum[5], sum[6], sum[7]) * (1.0f / sum[1]),
-                  F2(sum[8] / sum[0], sum[9] / sum[1]));
+        for (int oy = -2; oy <= 2; oy++)
+          for (int ox = -2; ox <= 2; ox++) {
+            int cx = ox * stride, cy = oy * stride;
+            int ux = x + cx, uy = y + cy;
+            if (!in_img(ux, uy, w, h)) continue;
+            size_t j = (size_t)uy * w + ux;
+            float2 wt = es.weight(length(F2((float)cx, (float)cy)), depth_tex[j],
+                                  load_gbuffer_normal(gbuf, ux, uy, w, h), F2(0.0f, 0.0f));
+            Rec32 r = IO::load(in, j);
+            ws += wt;
+            dsum = fma3(wt.x, r.d, dsum);
+            ssum = fma3(wt.y, r.s, ssum);
+            ms = F2(fma_(wt.x, r.aux.x, ms.x), fma_(wt.y, r.aux.y, ms.y));
+          }
+        IO::store(out, i, dsum * (1.0f / ws.x), ssum * (1.0f / ws.y), F2(ms.x / ws.x, ms.y / ws.y));
       } else {
         IO::copy(out, in, i);
       }
@@ -1846,34 +1830,26 @@ void dn32_fallback(int w, int h, const float* depth_tex, const uint32_t* gbuf, c
       if (hl < 4.0f * HISTORY_LEN_UNIT) {
         GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
         EdgeStop32 es = EdgeStop32::create(depth_tex[i], gbuffer.fwidth_z * 3.0f, 1.0f, gbuffer.normal, 7);
-        auto tap = [&](int t, float (&v)[9]) {
-          for (int k = 0; k < 9; ++k) v[k] = 0.0f;
-          const int ox = t % 7 - 3, oy = t / 7 - 3;
-          const int ux = x + ox, uy = y + oy;
-          if (!in_img(ux, uy, w, h)) return;
-          const size_t j = (size_t)uy * w + ux;
-          const float wt = es.weight(length(F2((float)ox, (float)oy)), depth_tex[j],
-                                     load_gbuffer_normal(gbuf, ux, uy, w, h), F2(0.0f, 0.0f)).x;
-          const Rec32 r = IO::load(in, j);
-          const float u[9] = {wt, wt * r.d.x, wt * r.d.y, wt * r.d.z, wt * r.s.x, wt * r.s.y, wt * r.s.z,
-                              wt * r.aux.x, wt * r.aux.y};
-          for (int k = 0; k < 9; ++k) v[k] = u[k];
-        };
-        float lanes[32][9];
-        for (int l = 0; l < 32; ++l) {
-          tap(l, lanes[l]);
-          if (l + 32 < 49) {
-            float u[9];
-            tap(l + 32, u);
-            for (int k = 0; k < 9; ++k) lanes[l][k] = lanes[l][k] + u[k];
+        float ws = 0.0f;
+        float2 ms = F2(0.0f, 0.0f);
+        float3 dsum = F3(0.0f), ssum = F3(0.0f);
+        for (int oy = -3; oy <= 3; oy++)
+          for (int ox = -3; ox <= 3; ox++) {
+            int ux = x + ox, uy = y + oy;
+            if (!in_img(ux, uy, w, h)) continue;
+            size_t j = (size_t)uy * w + ux;
+            float wt = es.weight(length(F2((float)ox, (float)oy)), depth_tex[j],
+                                 load_gbuffer_normal(gbuf, ux, uy, w, h), F2(0.0f, 0.0f)).x;
+            Rec32 r = IO::load(in, j);
+            ws += wt;
+            dsum = fma3(wt, r.d, dsum);
+            ssum = fma3(wt, r.s, ssum);
+            ms = F2(fma_(wt, r.aux.x, ms.x), fma_(wt, r.aux.y, ms.y));
           }
-        }
-        float sum[9];
-        warp_sum32(lanes, sum);
-        float inv = 1.0f / sum[0];
-        dd = F3(sum[1], sum[2], sum[3]) * inv;
-        sd = F3(sum[4], sum[5], sum[6]) * inv;
-        md = F2(sum[7], sum[8]) * inv;
+        float inv = 1.0f / ws;
+        dd = dsum * inv;
+        sd = ssum * inv;
+        md = ms * inv;
       } else {
         Rec32 r = IO::load(in, i);
         dd = r.d;

@@ -375,80 +375,44 @@ struct Dn32TemporalF {
 
 // ----------------------------------------------------------- disocclusion fix
 
-// Short-history pixels (quad-max length below 4 frames) are filtered by their whole
-// warp: the warp takes its short pixels one at a time, each lane evaluates one tap
-// (two for the 7x7 fallback) and a butterfly of xor-shuffles adds the lanes' weights
-// and weighted values. The float forms define these sums this way (lane t holds tap
-// t in the loop's row-major order, lane t of the fallback adds tap t + 32 to tap t,
-// absent taps add zero, then the five xor levels 16..1; every lane ends with the same
-// totals); the oracle evaluates the same tree. Without it the 5x5 and 7x7 loops ran
-// in warps where one lane in ten had a short history.
-__device__ __forceinline__ bool short_history(float qmax) { return qmax < 4.0f * VLT_HISTORY_LEN_UNIT; }
-
-template <int K>
-__device__ __forceinline__ void warp_sum(float (&v)[K]) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = v[k] + __shfl_xor_sync(0xFFFFFFFFu, v[k], off);
-}
-
 template <class Geo, int FORM>
 struct Dn32FixF {
   using R = typename DnT<FORM>::R;
   using N = typename DnT<FORM>::N;
   static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, const N* __restrict__ len, const R* __restrict__ in, R* __restrict__ out) {
-  // Every lane reaches the warp's collectives: no return before them.
-  const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
-  const uint32_t lane = (uint32_t)((threadIdx.y * blockDim.x + threadIdx.x) & 31u);
-  const bool act = inb(x, y, w, h);
-  const size_t i = act ? (size_t)y * w + x : 0;
-  float qmax = 0.0f;
-  bool is_short = false;
-  if (act) {
-    if (ld_len(len, i) == 0.0f) {
-      store_rec(out, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
-    } else {
-      qmax = quad_max_len(len, x, y, w, h);
-      is_short = short_history(qmax);
-      if (!is_short) copy_rec(out, in, i);
-    }
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  float hl = ld_len(len, i);
+  float qmax = quad_max_len(len, x, y, w, h);
+  if (hl == 0.0f) {
+    store_rec(out, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
+    return;
   }
-  uint32_t pending = __ballot_sync(0xFFFFFFFFu, is_short);
-  while (pending) {
-    const int b = __ffs(pending) - 1;
-    pending &= pending - 1u;
-    const int px = __shfl_sync(0xFFFFFFFFu, x, b), py = __shfl_sync(0xFFFFFFFFu, y, b);
-    const float hl = __shfl_sync(0xFFFFFFFFu, qmax, b);
-    const size_t pi = (size_t)py * w + px;
-    // relax_disocclusion_fix.hlsl:27-122: 5x5 bilateral at stride int(14 * unit / hl).
-    EdgeStopFast es = make_es(geo.dep(pi), geo.fwz(pi), 5.0f, geo.normal(pi), 5);
+  hl = qmax;
+  if (hl < 4.0f * VLT_HISTORY_LEN_UNIT) {
+    EdgeStopFast es = make_es(geo.dep(i), geo.fwz(i), 5.0f, geo.normal(i), 5);
+    f2 ws = mk2(0.0f, 0.0f);
+    f3 dsum = mk3(0.0f), ssum = mk3(0.0f);
+    f2 msum = mk2(0.0f, 0.0f);
     const int stride = f2i_rz((14.0f * VLT_HISTORY_LEN_UNIT) / hl);
-    float v[10] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    if (lane < 25u) {
-      const int ox = (int)(lane % 5u) - 2, oy = (int)(lane / 5u) - 2;
-      const int offx = ox * stride, offy = oy * stride;
-      const int cx = px + offx, cy = py + offy;
-      if (cx >= 0 && cy >= 0 && cx <= w - 1 && cy <= h - 1) {
-        const size_t j = (size_t)cy * w + cx;
-        const f2 wt = es.weight(length2(mk2((float)offx, (float)offy)), geo.dep(j), geo.normal(j), mk2(0.0f, 0.0f));
-        const Rec r = load_rec(in, j);
-        v[0] = wt.x;
-        v[1] = wt.y;
-        v[2] = wt.x * r.d.x;
-        v[3] = wt.x * r.d.y;
-        v[4] = wt.x * r.d.z;
-        v[5] = wt.y * r.s.x;
-        v[6] = wt.y * r.s.y;
-        v[7] = wt.y * r.s.z;
-        v[8] = wt.x * r.aux.x;
-        v[9] = wt.y * r.aux.y;
+    for (int oy = -2; oy <= 2; ++oy) {
+      for (int ox = -2; ox <= 2; ++ox) {
+        int offx = ox * stride, offy = oy * stride;
+        int cx = x + offx, cy = y + offy;
+        if (!(cx >= 0 && cy >= 0 && cx <= w - 1 && cy <= h - 1)) continue;
+        size_t j = (size_t)cy * w + cx;
+        f2 wt = es.weight(length2(mk2((float)offx, (float)offy)), geo.dep(j), geo.normal(j), mk2(0.0f, 0.0f));
+        Rec r = load_rec(in, j);
+        ws = ws + wt;
+        dsum = fma3(wt.x, r.d, dsum);
+        ssum = fma3(wt.y, r.s, ssum);
+        msum = mk2(fma_(wt.x, r.aux.x, msum.x), fma_(wt.y, r.aux.y, msum.y));
       }
     }
-    warp_sum(v);
-    if ((int)lane == b)
-      store_rec(out, pi, mk3(v[2], v[3], v[4]) * (1.0f / v[0]), mk3(v[5], v[6], v[7]) * (1.0f / v[1]),
-                mk2(v[8] / v[0], v[9] / v[1]));
+    store_rec(out, i, dsum * (1.0f / ws.x), ssum * (1.0f / ws.y), mk2(msum.x / ws.x, msum.y / ws.y));
+  } else {
+    copy_rec(out, in, i);
   }
 }
 };
@@ -499,85 +463,55 @@ struct Dn32FastClampF {
 
 // ---------------------------------------------------------- spatial fallback
 
-// svgf_spatial_fallback_filter.hlsl:25-125. The variance of a pixel:
-// max(m2 - m1^2, 0) * max(1, 4 * unit / hl).
-template <class R>
-__device__ __forceinline__ void fallback_store(R* __restrict__ out, size_t i, f3 dd, f3 sd, f2 md, float hl) {
-  f2 fst = mk2(lum_fast(dd.x, dd.y, dd.z), lum_fast(sd.x, sd.y, sd.z));
-  f2 var = mk2(fmax_(fma_(-fst.x, fst.x, md.x), 0.0f), fmax_(fma_(-fst.y, fst.y, md.y), 0.0f));
-  float boost = fmax_(1.0f, (4.0f * VLT_HISTORY_LEN_UNIT) / hl);
-  store_rec(out, i, dd, sd, var * boost);
-}
-
 template <class Geo, int FORM>
 struct Dn32FallbackF {
   using R = typename DnT<FORM>::R;
   using N = typename DnT<FORM>::N;
-  // One 7x7 tap's weight and weighted values (zeros outside the image).
-  static __device__ __forceinline__ void tap(const Geo& geo, const EdgeStopFast& es, const R* __restrict__ in,
-                                             int px, int py, int w, int h, uint32_t t, float (&v)[9]) {
-    const int ox = (int)(t % 7u) - 3, oy = (int)(t / 7u) - 3;
-    const int cx = px + ox, cy = py + oy;
-    if (!(cx >= 0 && cy >= 0 && cx <= w - 1 && cy <= h - 1)) {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) v[k] = 0.0f;
-      return;
-    }
-    const size_t j = (size_t)cy * w + cx;
-    const float wt = es.weight(length2(mk2((float)ox, (float)oy)), geo.dep(j), geo.normal(j), mk2(0.0f, 0.0f)).x;
-    const Rec r = load_rec(in, j);
-    v[0] = wt;
-    v[1] = wt * r.d.x;
-    v[2] = wt * r.d.y;
-    v[3] = wt * r.d.z;
-    v[4] = wt * r.s.x;
-    v[5] = wt * r.s.y;
-    v[6] = wt * r.s.z;
-    v[7] = wt * r.aux.x;
-    v[8] = wt * r.aux.y;
-  }
   static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, const N* __restrict__ len, const R* __restrict__ in, R* __restrict__ out) {
-  // Every lane reaches the warp's collectives: no return before them.
-  const int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
-  const uint32_t lane = (uint32_t)((threadIdx.y * blockDim.x + threadIdx.x) & 31u);
-  const bool act = inb(x, y, w, h);
-  const size_t i = act ? (size_t)y * w + x : 0;
-  float qmax = 0.0f;
-  bool is_short = false;
-  if (act) {
-    if (ld_len(len, i) == 0.0f) {
-      store_rec(out, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
-    } else {
-      qmax = quad_max_len(len, x, y, w, h);
-      is_short = short_history(qmax);
-      if (!is_short) {
-        const Rec r = load_rec(in, i);
-        fallback_store(out, i, r.d, r.s, r.aux, qmax);
+  int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
+  if (!inb(x, y, w, h)) return;
+  size_t i = (size_t)y * w + x;
+  float hl = ld_len(len, i);
+  float qmax = quad_max_len(len, x, y, w, h);
+  if (hl == 0.0f) {
+    store_rec(out, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
+    return;
+  }
+  hl = qmax;
+  f3 dd, sd;
+  f2 md;
+  if (hl < 4.0f * VLT_HISTORY_LEN_UNIT) {
+    EdgeStopFast es = make_es(geo.dep(i), geo.fwz(i) * 3.0f, 1.0f, geo.normal(i), 7);
+    float ws = 0.0f;
+    f3 dsum = mk3(0.0f), ssum = mk3(0.0f);
+    f2 msum = mk2(0.0f, 0.0f);
+    for (int oy = -3; oy <= 3; ++oy) {
+      for (int ox = -3; ox <= 3; ++ox) {
+        int cx = x + ox, cy = y + oy;
+        if (!(cx >= 0 && cy >= 0 && cx <= w - 1 && cy <= h - 1)) continue;
+        size_t j = (size_t)cy * w + cx;
+        float wt = es.weight(length2(mk2((float)ox, (float)oy)), geo.dep(j), geo.normal(j), mk2(0.0f, 0.0f)).x;
+        Rec r = load_rec(in, j);
+        ws = ws + wt;
+        dsum = fma3(wt, r.d, dsum);
+        ssum = fma3(wt, r.s, ssum);
+        msum = mk2(fma_(wt, r.aux.x, msum.x), fma_(wt, r.aux.y, msum.y));
       }
     }
+    float inv = 1.0f / ws;
+    dd = dsum * inv;
+    sd = ssum * inv;
+    md = msum * inv;
+  } else {
+    Rec r = load_rec(in, i);
+    dd = r.d;
+    sd = r.s;
+    md = r.aux;
   }
-  uint32_t pending = __ballot_sync(0xFFFFFFFFu, is_short);
-  while (pending) {
-    const int b = __ffs(pending) - 1;
-    pending &= pending - 1u;
-    const int px = __shfl_sync(0xFFFFFFFFu, x, b), py = __shfl_sync(0xFFFFFFFFu, y, b);
-    const float hl = __shfl_sync(0xFFFFFFFFu, qmax, b);
-    const size_t pi = (size_t)py * w + px;
-    // 7x7 edge-stopped filter (sigma_z boosted x3): lane t holds taps t and t + 32.
-    EdgeStopFast es = make_es(geo.dep(pi), geo.fwz(pi) * 3.0f, 1.0f, geo.normal(pi), 7);
-    float v[9], u[9];
-    tap(geo, es, in, px, py, w, h, lane, v);
-    if (lane + 32u < 49u) {
-      tap(geo, es, in, px, py, w, h, lane + 32u, u);
-#pragma unroll
-      for (int k = 0; k < 9; ++k) v[k] = v[k] + u[k];
-    }
-    warp_sum(v);
-    if ((int)lane == b) {
-      const float inv = 1.0f / v[0];
-      fallback_store(out, pi, mk3(v[1], v[2], v[3]) * inv, mk3(v[4], v[5], v[6]) * inv, mk2(v[7], v[8]) * inv, hl);
-    }
-  }
+  f2 fst = mk2(lum_fast(dd.x, dd.y, dd.z), lum_fast(sd.x, sd.y, sd.z));
+  f2 var = mk2(fmax_(fma_(-fst.x, fst.x, md.x), 0.0f), fmax_(fma_(-fst.y, fst.y, md.y), 0.0f));
+  float boost = fmax_(1.0f, (4.0f * VLT_HISTORY_LEN_UNIT) / hl);
+  store_rec(out, i, dd, sd, var * boost);
 }
 };
 
