@@ -7,12 +7,15 @@
 // result is defined as if the queries were processed one at a time in query-index
 // order (the CPU restatement does exactly that), and the GPU reproduces it:
 //   S1  every query probes its bucket; a hit selects immediately (atomicMax is
-//       order-independent); a miss with a free slot is counted per bucket;
-//   S2  each bucket with misses gets a contiguous segment of a miss list;
-//   S3  misses are scattered into their bucket's segment (any order);
-//   S4  one warp per bucket repeatedly takes the smallest unresolved query index,
-//       probes/inserts its checksum exactly as the sequential loop would, and
-//       resolves every listed query with that checksum.
+//       order-independent); a miss with a free slot is counted per bucket and
+//       sets its bit in a miss bitmask;
+//   S2  each bucket with misses gets a contiguous segment of a miss list and is
+//       listed among the buckets with misses;
+//   S3  the misses (the bitmask's bits) are scattered into their bucket's segment
+//       (any order);
+//   S4  one warp per listed bucket repeatedly takes the smallest unresolved query
+//       index, probes/inserts its checksum exactly as the sequential loop would,
+//       and resolves every listed query with that checksum.
 #include <mutex>
 
 #include "hashgrid.cuh"
