@@ -6,7 +6,11 @@
 // one persistent k_batched launch over their concatenated tile lists, with the
 // views' parameter tuples and tile map in the kernel's parameter block. Jobs of one
 // view stay in order (they are dependent); jobs of different views are independent,
-// so grouping them changes no result. With graphs on, the step's launches are
+// so grouping them changes no result. A recorded frame tags its jobs with a lane
+// (main, hash grid, specular, AO) and marks where the side lanes fork and join; the
+// executor groups each lane separately and issues the side lanes on its own streams
+// between the fork and the joins, as a single view's frame does. With graphs on,
+// the step's launches are
 // captured into a CUDA graph; a cached executable graph with the same launch
 // sequence is updated in place with the new parameters (cudaGraphExecUpdate) and
 // replayed, otherwise a new one is instantiated.
