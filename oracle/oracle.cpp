@@ -1452,9 +1452,21 @@ inline float exp2_fma(float x) {
   return p * asfloat((uint32_t)(e + 127) << 23);
 }
 inline float exp_fma(float x) { return exp2_fma(x * 1.44269502162933349609375f); }
-// The a-trous edge weight's exponential, in base 2: exp2_fma(y) where rint(y) >= -126
-// (y >= -126.5), zero below that and for NaN.
-inline float exp2_weight(float y) { return y >= -126.5f ? exp2_fma(y) : 0.0f; }
+// The a-trous edge weight's exponential, in base 2: 2^rint(y) * p(y - rint(y)) with
+// the degree-5 polynomial below (FMA Horner) where y >= -126.5, zero below that and
+// for NaN.
+inline float exp2_weight(float y) {
+  if (!(y >= -126.5f)) return 0.0f;
+  const float n = rintf(y);
+  const float f = y - n;
+  float p = 0.0013218672247603536f;
+  p = fma_(p, f, 0.009671698324382305f);
+  p = fma_(p, f, 0.05550893023610115f);
+  p = fma_(p, f, 0.24022237956523895f);
+  p = fma_(p, f, 0.6931468844413757f);
+  p = fma_(p, f, 1.0f);
+  return p * asfloat((uint32_t)(to_int(n) + 127) << 23);
+}
 // luminance (util.hlsl:21-24) as r*0.2126, then two FMAs.
 inline float lum_fma(float3 c) { return fma_(c.z, 0.0722f, fma_(c.y, 0.7152f, c.x * 0.2126f)); }
 inline float3 fma3(float w, float3 v, float3 acc) {
