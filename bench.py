@@ -95,7 +95,7 @@ MEASURED_TRAFFIC_PER_UNIT = {"dn_atrous": 64.25}  # B/px: one-pass dram counters
 # Warp instructions per launch unit measured with ncu (smsp__inst_executed.sum of a
 # --set full capture / pixels; profiles/dn_atrous_f32_540p.md): the issue roofline
 # of a pass that is bound by instruction issue rather than by HBM.
-MEASURED_WARP_INSTRUCTIONS_PER_UNIT = {"dn_atrous": 21.69e6 / (960 * 540)}
+MEASURED_WARP_INSTRUCTIONS_PER_UNIT = {"dn_atrous": 21.07e6 / (960 * 540)}
 ISSUE_SLOTS_PER_SM_CLOCK = 4  # one warp instruction per scheduler per clock, 4 schedulers per SM
 
 
