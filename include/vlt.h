@@ -54,7 +54,9 @@ typedef enum vlt_status {
   VLT_ERR_OUT_OF_MEMORY = 2,
   VLT_ERR_BUDGET_EXCEEDED = 3,
   VLT_ERR_CUDA = 4,
-  VLT_ERR_DEVICE_TIMEOUT = 5,
+  VLT_ERR_DEVICE_TIMEOUT = 5, /* reserved: no kernel of this library waits on a flag, a
+                                * peer or a barrier outside its block, so none can time
+                                * out; kept so the codes stay stable */
   VLT_ERR_BAD_STATE = 6,
   VLT_ERR_NO_DEVICE = 7
 } vlt_status;
@@ -372,6 +374,11 @@ typedef struct vlt_server_stats {
   double admit_wait_ms_total;
   uint32_t sessions_live, sessions_waiting, steps_in_flight;
   uint64_t bytes_in_use, pixels_in_use;
+  /* Admissions whose view could not be created (device allocation failed); the
+   * session stays first in the queue and is tried again. last_admit_status is the
+   * vlt_status of the latest such failure (0 if none). */
+  uint64_t admit_failures;
+  uint32_t last_admit_status, pad0;
 } vlt_server_stats;
 vlt_status vlt_server_get_stats(const vlt_server* server, vlt_server_stats* out);
 
@@ -538,7 +545,10 @@ vlt_status vlt_hg_query_select(uint32_t log2_buckets, uint32_t max_queries, cons
  * rejected with VLT_ERR_INVALID_ARG. The first call on a device looks up the array's
  * device address; make that first call before any stream capture. All calls share
  * the array, so calls that overlap on the GPU (different streams, or different
- * threads on the same device) race and give wrong results: serialize them. */
+ * threads on the same device) race and give wrong results: serialize them. The
+ * looked-up address is kept for the life of the process: do not call this entry
+ * point after cudaDeviceReset (or any other teardown of the device's primary
+ * context) in the same process. */
 #define VLT_HG_SELECT_NOALLOC_SCRATCH_BYTES (12u * 1024u * 1024u)
 vlt_status vlt_hg_query_select_noalloc(uint32_t log2_buckets, uint32_t max_queries, const uint32_t* queries,
                                        const uint32_t* query_count, uint32_t* rw_storage, uint32_t* rw_selection,

@@ -1932,6 +1932,61 @@ void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, con
     }
 }
 
+// svgf_atrous_filter.hlsl:23-88 with the edge-stopping weight exactly as
+// svgf.inc.hlsl:60-82 writes it (the reference form's EdgeStoppingFunc::weight:
+// -dist_z / ((sigma_z * fwidth_z) * |offset| + 1e-8), pow(n_dot, 128), the luminance
+// term through rcp(4 * sqrt(var) + 1e-8), exp of the sum, the kernel weight applied
+// afterwards), every operation separately rounded and the sums normalised by
+// division, on the float forms' records. This is the check of the float forms'
+// a-trous against the reference's formulas (the float forms themselves evaluate the
+// weight in base 2 with a short polynomial and fused multiply-adds, which changes
+// the weights by a few units in the last place).
+template <int FORM>
+void dn32_atrous_refw(int w, int h, const float* depth_tex, const uint32_t* gbuf, const void* in, void* out,
+                      void* out_diff, void* out_spec, int step) {
+  using IO = Dio<FORM>;
+  const float kernel_weights[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
+  ROWS_PARALLEL
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      size_t i = (size_t)y * w + x;
+      GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
+      Rec32 c = IO::load(in, i);
+      EdgeStoppingFunc es = EdgeStoppingFunc::create(depth_tex[i], gbuffer.fwidth_z, gbuffer.normal);
+      es.use_lumi = true;
+      es.lumi_center = F2(luminance(c.d), luminance(c.s));
+      es.lumi_std = F2(sqrtf(c.aux.x), sqrtf(c.aux.y));
+      float3 diff_sum = c.d, spec_sum = c.s;
+      float2 variance_sum = c.aux;
+      float2 weight_sum = F2(1.0f, 1.0f);
+      for (int oy = -2; oy <= 2; oy++) {
+        float kernel_weight_y = kernel_weights[std::abs(oy)];
+        for (int ox = -2; ox <= 2; ox++) {
+          int cx = ox * step, cy = oy * step;
+          int ux = x + cx, uy = y + cy;
+          if (!in_img(ux, uy, w, h) || ox == 0 || oy == 0) continue;
+          float kw = kernel_weight_y * kernel_weights[std::abs(ox)];
+          size_t j = (size_t)uy * w + ux;
+          Rec32 r = IO::load(in, j);
+          float2 lumi = F2(luminance(r.d), luminance(r.s));
+          float2 e = es.weight(length(F2((float)cx, (float)cy)), depth_tex[j], load_gbuffer_normal(gbuf, ux, uy, w, h),
+                               lumi);
+          float2 weight = F2(kw * e.x, kw * e.y);
+          float2 weight_var = weight * weight;
+          diff_sum += weight.x * r.d;
+          spec_sum += weight.y * r.s;
+          variance_sum += weight_var * r.aux;
+          weight_sum += weight;
+        }
+      }
+      float3 dd = diff_sum / weight_sum.x, sd = spec_sum / weight_sum.y;
+      float2 vd = variance_sum / (weight_sum * weight_sum);
+      if (out) IO::store(out, i, dd, sd, vd);
+      if (out_diff) IO::out(out_diff, i, dd);
+      if (out_spec) IO::out(out_spec, i, sd);
+    }
+}
+
 // ======================================================= hash grid
 // hash_grid.inc.hlsl:32-105.
 struct VKey {
@@ -2715,6 +2770,9 @@ struct OView {
   // reference-form buffers of the same role (the f16 form's specular records live in
   // spec_hp_prev, 24 bytes per pixel).
   int form = 0;
+  // Float forms: run the a-trous with the reference's edge-stopping formulas
+  // (dn32_atrous_refw) instead of the forms' own evaluation.
+  bool atrous_reference_weights = false;
   std::vector<uint8_t> fdiff_prev, fao_prev, fao_filtered, fdiff_light, fspec_light, fhist_rec, fhist_len, ffast_prev,
       ffallback;
   // Final lighting (the view's colour buffer) and the temporal-AA history
@@ -3087,8 +3145,14 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
       bool last = k + 1 == iters;
       void* od = last && out ? out->diffuse : nullptr;
       void* os = last && out ? out->specular : nullptr;
-      if (f32) dn32_atrous<1>(w, h, in.depth, in.gbuffer, a.data(), b.data(), od, os, 1 << k);
-      else dn32_atrous<2>(w, h, in.depth, in.gbuffer, a.data(), b.data(), od, os, 1 << k);
+      if (v.atrous_reference_weights) {
+        if (f32) dn32_atrous_refw<1>(w, h, in.depth, in.gbuffer, a.data(), b.data(), od, os, 1 << k);
+        else dn32_atrous_refw<2>(w, h, in.depth, in.gbuffer, a.data(), b.data(), od, os, 1 << k);
+      } else if (f32) {
+        dn32_atrous<1>(w, h, in.depth, in.gbuffer, a.data(), b.data(), od, os, 1 << k);
+      } else {
+        dn32_atrous<2>(w, h, in.depth, in.gbuffer, a.data(), b.data(), od, os, 1 << k);
+      }
       a.swap(b);
     }
     if (iters == 0 && out) {  // the diffuse / specular halves of the fallback records
@@ -3258,6 +3322,9 @@ void* vlto_view_create_form(uint32_t w, uint32_t h, const vlt_params* p, int for
 void* vlto_view_create(uint32_t w, uint32_t h, const vlt_params* p) { return vlto_view_create_form(w, h, p, 0); }
 
 void vlto_view_destroy(void* h) { delete (OView*)h; }
+
+// Float forms: 1 runs the a-trous with the reference's edge-stopping formulas.
+void vlto_view_set_atrous_reference_weights(void* h, int on) { ((OView*)h)->atrous_reference_weights = on != 0; }
 
 // Traced mode, phase one: rays into host arrays (cache: nq rays, diffuse and
 // spec-validate: W*H rays; any may be NULL); counts = {cache, diffuse, spec, diffuse

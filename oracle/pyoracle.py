@@ -30,6 +30,7 @@ SIGS = {
     "vlto64_frame": (None, [P, FP, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                              C.c_void_p, C.c_void_p]),
     "vlto_view_destroy": (None, [P]),
+    "vlto_view_set_atrous_reference_weights": (None, [P, C.c_int]),
     "vlto_frame_run": (None, [P, C.POINTER(_ffi.FrameInputs), C.POINTER(_ffi.FrameOutputs)]),
     "vlto_view_buffer": (P, [P, C.c_char_p, C.POINTER(C.c_size_t)]),
     "vlto_ao_gen": (None, [FP, U32, U32, P, P, P, P, U32, U32, C.c_float]),
@@ -147,6 +148,12 @@ class OracleView:
         for k in ("diffuse", "specular", "raw_diffuse", "raw_specular", "color", "taa"):
             setattr(fo, k, ptr((outputs or {}).get(k)))
         lib().vlto_frame_run(self.handle, C.byref(fi), C.byref(fo))
+
+    def set_atrous_reference_weights(self, on=True):
+        """Float forms: run the a-trous with the reference's edge-stopping formulas
+        (svgf.inc.hlsl:60-82, separately rounded) instead of the forms' own
+        base-2 / fused-multiply-add evaluation."""
+        lib().vlto_view_set_atrous_reference_weights(self.handle, 1 if on else 0)
 
     def buffer(self, name, dtype=np.uint8):
         n = C.c_size_t(0)

@@ -113,6 +113,56 @@ def test_state_import_refuses_mismatch(ctx):
             o.close()
 
 
+def _header_fields():
+    """Byte offsets of StateHeader fields (api.cu): six u32, vlt_params, u64 pool
+    bytes, u32 frames and flags, eight i32 slot indices, u64 screen-cache offset, then
+    the u64 buffer table in ViewBuffers order."""
+    import ctypes as C
+
+    pool = (24 + C.sizeof(vg._ffi.Params) + 7) & ~7
+    return {"diff_prev": pool + 16, "spec_prev": pool + 20, "prev_den_stride": pool + 40,
+            "prev_den_off": pool + 48, "table": pool + 56}
+
+
+@pytest.mark.parametrize("damage", ["slot_index", "spec_slot_index", "group_offset", "fixed_offset",
+                                    "screen_cache", "screen_stride"])
+def test_state_import_refuses_damaged_table(ctx, damage):
+    W, H = 32, 16
+    p = vg.params_reference()
+    a = vg.View(ctx, W, H, "ref", p)
+    try:
+        scene = vg.Scene(3, W, H)
+        for f in range(2):
+            run_frame(a, scene, f, "ref", W * H)
+        blob = a.export_state()
+        before = state_of(a)
+        hf = _header_fields()
+        bad = blob.copy()
+        table = bad[hf["table"]:].view(np.uint64)
+        if damage == "slot_index":
+            bad[hf["diff_prev"]:hf["diff_prev"] + 4].view(np.int32)[0] = 7
+        elif damage == "spec_slot_index":
+            bad[hf["spec_prev"]:hf["spec_prev"] + 4].view(np.int32)[0] = -1
+        elif damage == "group_offset":
+            table[0] = table[3]  # diff_rsv[0] pointed at ao[0]: not a permutation of its group
+        elif damage == "fixed_offset":
+            table[5] += 256  # ao_filtered moved inside the pool
+        elif damage == "screen_cache":
+            bad[hf["prev_den_off"]:hf["prev_den_off"] + 8].view(np.uint64)[0] = 12345
+        else:
+            bad[hf["prev_den_stride"]:hf["prev_den_stride"] + 4].view(np.int32)[0] = 3
+        with pytest.raises(vg.VltError) as ei:
+            a.import_state(bad)
+        assert ei.value.status == 1  # VLT_ERR_INVALID_ARG
+        assert "state blob" in str(ei.value)
+        after = state_of(a)  # a refused blob leaves the view as it was
+        for k in before:
+            assert np.array_equal(before[k], after[k]), k
+        a.import_state(blob)
+    finally:
+        a.close()
+
+
 def test_state_export_refused_while_a_traced_frame_is_pending(ctx):
     import torch
 

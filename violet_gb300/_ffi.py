@@ -140,7 +140,8 @@ class ServerStats(C.Structure):
                 ("steps", C.c_uint64), ("frames_issued", C.c_uint64), ("frames_done", C.c_uint64),
                 ("pixels_issued", C.c_uint64), ("admit_wait_ms_total", C.c_double), ("sessions_live", C.c_uint32),
                 ("sessions_waiting", C.c_uint32), ("steps_in_flight", C.c_uint32), ("bytes_in_use", C.c_uint64),
-                ("pixels_in_use", C.c_uint64)]
+                ("pixels_in_use", C.c_uint64), ("admit_failures", C.c_uint64), ("last_admit_status", C.c_uint32),
+                ("pad0", C.c_uint32)]
 
 
 class BatchStats(C.Structure):

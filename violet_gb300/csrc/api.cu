@@ -1,9 +1,12 @@
 // C ABI: parameter presets, context/view lifetime, the per-frame driver (the pass
 // sequence of RestirRenderer::add_passes and Denoiser::add_passes), and the
 // per-pass entry points.
+#include <stddef.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <map>
 #include <new>
 #include <string>
@@ -25,6 +28,20 @@ vlt_status cuda_status(cudaError_t e) {
   if (e == cudaErrorMemoryAllocation) return VLT_ERR_OUT_OF_MEMORY;
   if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return VLT_ERR_NO_DEVICE;
   return VLT_ERR_CUDA;
+}
+
+// Every device allocation of the library goes through here. Host-side failure
+// injection for the allocation paths: while the environment variable
+// VLT_FAIL_DEVICE_ALLOC is "1", the allocation fails on the host as if the device
+// were out of memory (cudaMalloc is not called), so tests reach the
+// VLT_ERR_OUT_OF_MEMORY paths without exhausting a GPU.
+cudaError_t device_alloc(void** p, size_t bytes) {
+  const char* fail = getenv("VLT_FAIL_DEVICE_ALLOC");
+  if (fail && fail[0] == '1' && fail[1] == 0) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
 }
 
 // FrameRand (restir_renderer.rs:130-143): state = frame_index, next = jenkins_hash(state).
@@ -487,7 +504,7 @@ vlt_status vlt_view_create(vlt_ctx* ctx, uint32_t width, uint32_t height, vlt_fo
   v->hg.log2_buckets = params->hg_log2_buckets;
   v->hg.max_queries = eff_max_queries(*params, width, height);
   size_t bytes = layout(v, nullptr);
-  cudaError_t e = cudaMalloc(&v->pool.p, bytes);
+  cudaError_t e = device_alloc(&v->pool.p, bytes);
   if (e != cudaSuccess) {
     delete v;
     return cuda_status(e);
@@ -562,6 +579,66 @@ uint64_t to_off(const vlt_view* v, const void* p) {
 }
 void* from_off(const vlt_view* v, uint64_t o) { return o == kNullOff ? nullptr : (char*)v->pool.p + o; }
 
+// Ping-pong groups of the buffer table: slots whose buffers are swapped between
+// frames (all of one size). A blob may permute offsets within a group, nothing else.
+struct SlotGroup {
+  size_t first;   // slot index of the group's first member
+  int count;      // members
+  int stride;     // slots between members
+};
+constexpr size_t slot_of(size_t byte_offset) { return byte_offset / sizeof(void*); }
+const SlotGroup kSlotGroups[] = {
+    {slot_of(offsetof(ViewBuffers, diff_rsv)), 3, 1},  {slot_of(offsetof(ViewBuffers, ao)), 2, 1},
+    {slot_of(offsetof(ViewBuffers, spec_hp)), 3, 1},   {slot_of(offsetof(ViewBuffers, spec_rsv)), 3, 1},
+    {slot_of(offsetof(ViewBuffers, spec_rad)), 3, 1},  {slot_of(offsetof(ViewBuffers, color)), 3, 1},
+    {slot_of(offsetof(ViewBuffers, mom)), 3, 1},       {slot_of(offsetof(ViewBuffers, var)), 3, 1},
+    {slot_of(offsetof(ViewBuffers, fast)), 2, 1},      {slot_of(offsetof(ViewBuffers, len)), 2, 1},
+    {slot_of(offsetof(ViewBuffers, rec)), 5, 1},       {slot_of(offsetof(ViewBuffers, rec_fast)), 2, 1},
+    {slot_of(offsetof(ViewBuffers, hg_queries)), 2, 1}, {slot_of(offsetof(ViewBuffers, hg_qcount)), 2, 1},
+    {slot_of(offsetof(ViewBuffers, surf)) + 0, 2, 3},  {slot_of(offsetof(ViewBuffers, surf)) + 1, 2, 3},
+    {slot_of(offsetof(ViewBuffers, surf)) + 2, 2, 3},  {slot_of(offsetof(ViewBuffers, taa)), 2, 1},
+};
+
+// Checks a state blob's buffer table and slot bookkeeping against this view's own
+// layout: every slot outside a ping-pong group at its own offset, every group a
+// permutation of its own offsets, the slot indices in range, and the screen-space
+// cache pointer at one of the view's buffers. Returns nullptr when the blob is
+// acceptable, else what is wrong with it.
+const char* check_state_table(const vlt_view* v, const StateHeader& hd) {
+  vlt_view canon = *v;  // layout() only rewrites the copy's buffer table
+  layout(&canon, (char*)v->pool.p);
+  uint64_t own[kStatePtrs];
+  void* const* cp = (void* const*)&canon.b;
+  for (uint32_t k = 0; k < kStatePtrs; ++k) own[k] = to_off(v, cp[k]);
+  bool grouped[kStatePtrs] = {};
+  for (const SlotGroup& g : kSlotGroups) {
+    uint64_t want[8], got[8];
+    for (int i = 0; i < g.count; ++i) {
+      const size_t k = g.first + (size_t)i * g.stride;
+      grouped[k] = true;
+      want[i] = own[k];
+      got[i] = hd.off[k];
+    }
+    std::sort(want, want + g.count);
+    std::sort(got, got + g.count);
+    for (int i = 0; i < g.count; ++i)
+      if (want[i] != got[i]) return "state blob: a ping-pong buffer group is not a permutation of this view's buffers";
+  }
+  for (uint32_t k = 0; k < kStatePtrs; ++k)
+    if (!grouped[k] && hd.off[k] != own[k]) return "state blob: a buffer offset differs from this view's layout";
+  if (hd.diff_prev < 0 || hd.diff_prev > 2 || hd.spec_prev < 0 || hd.spec_prev > 2 || hd.ao_prev < 0 ||
+      hd.ao_prev > 1 || hd.hg_qcur < 0 || hd.hg_qcur > 1 || hd.surf_cur < 0 || hd.surf_cur > 1 || hd.taa_cur < 0 ||
+      hd.taa_cur > 1)
+    return "state blob: a ping-pong slot index is out of range";
+  if (hd.prev_den_stride != 1 && hd.prev_den_stride != 2) return "state blob: screen-cache stride is not 1 or 2";
+  if (hd.prev_den_off != kNullOff) {
+    bool found = false;
+    for (uint32_t k = 0; k < kStatePtrs && !found; ++k) found = own[k] != kNullOff && own[k] == hd.prev_den_off;
+    if (!found) return "state blob: the screen-space cache does not point at one of this view's buffers";
+  }
+  return nullptr;
+}
+
 }  // namespace
 
 extern "C" {
@@ -569,8 +646,14 @@ extern "C" {
 size_t vlt_view_state_bytes(const vlt_view* v) { return v ? state_data_off() + v->pool.bytes : 0; }
 
 vlt_status vlt_view_export_state(vlt_view* v, void* dst, size_t bytes, void* stream) {
-  if (!v || !dst || bytes < vlt_view_state_bytes(v)) return VLT_ERR_INVALID_ARG;
-  if (v->trace_pending) return VLT_ERR_BAD_STATE;
+  if (!v || !dst || bytes < vlt_view_state_bytes(v)) {
+    set_last_error("vlt_view_export_state: null view or destination, or fewer bytes than vlt_view_state_bytes");
+    return VLT_ERR_INVALID_ARG;
+  }
+  if (v->trace_pending) {
+    set_last_error("vlt_view_export_state: a traced frame is pending (vlt_frame_trace ran, vlt_frame_run not yet)");
+    return VLT_ERR_BAD_STATE;
+  }
   StateHeader hd;
   memset(&hd, 0, sizeof(hd));
   hd.magic = kStateMagic;
@@ -603,8 +686,14 @@ vlt_status vlt_view_export_state(vlt_view* v, void* dst, size_t bytes, void* str
 }
 
 vlt_status vlt_view_import_state(vlt_view* v, const void* src, size_t bytes, void* stream) {
-  if (!v || !src || bytes < vlt_view_state_bytes(v)) return VLT_ERR_INVALID_ARG;
-  if (v->trace_pending) return VLT_ERR_BAD_STATE;
+  if (!v || !src || bytes < vlt_view_state_bytes(v)) {
+    set_last_error("vlt_view_import_state: null view or source, or fewer bytes than vlt_view_state_bytes");
+    return VLT_ERR_INVALID_ARG;
+  }
+  if (v->trace_pending) {
+    set_last_error("vlt_view_import_state: a traced frame is pending (vlt_frame_trace ran, vlt_frame_run not yet)");
+    return VLT_ERR_BAD_STATE;
+  }
   cudaStream_t s = (cudaStream_t)stream;
   VLT_TRY(cudaSetDevice(v->ctx->device));
   StateHeader hd;
@@ -616,9 +705,10 @@ vlt_status vlt_view_import_state(vlt_view* v, const void* src, size_t bytes, voi
     set_last_error("state blob does not match this view (size, form or params)");
     return VLT_ERR_INVALID_ARG;
   }
-  for (uint32_t k = 0; k < kStatePtrs; ++k)
-    if (hd.off[k] != kNullOff && hd.off[k] >= hd.pool_bytes) return VLT_ERR_INVALID_ARG;
-  if (hd.prev_den_off != kNullOff && hd.prev_den_off >= hd.pool_bytes) return VLT_ERR_INVALID_ARG;
+  if (const char* why = check_state_table(v, hd)) {
+    set_last_error(why);
+    return VLT_ERR_INVALID_ARG;
+  }
   VLT_TRY(cudaMemcpyAsync(v->pool.p, (const char*)src + state_data_off(), v->pool.bytes, cudaMemcpyDefault, s));
   void** ptrs = (void**)&v->b;
   for (uint32_t k = 0; k < kStatePtrs; ++k) ptrs[k] = from_off(v, hd.off[k]);

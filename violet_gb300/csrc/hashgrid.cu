@@ -534,7 +534,9 @@ void launch_hg_find(const Exec& ex, const vlt_frame_params& fp, const HashGridDi
 static __device__ __align__(256) unsigned char g_hg_select_scratch[VLT_HG_SELECT_NOALLOC_SCRATCH_BYTES];
 
 // Device address of g_hg_select_scratch, looked up once per device (host code
-// cannot use the symbol itself as a device pointer).
+// cannot use the symbol itself as a device pointer). The address is kept for the
+// life of the process; after a cudaDeviceReset the module is loaded again and the
+// kept address is stale, so the entry point is documented as unusable after one.
 static void* g_hg_select_scratch_ptr[64];
 static bool g_hg_select_scratch_ready[64];
 static std::mutex g_hg_select_scratch_mutex;
@@ -547,8 +549,11 @@ extern "C" vlt_status vlt_hg_query_select_noalloc(uint32_t log2_buckets, uint32_
                                                   void* stream) {
   using namespace vlt;
   if (log2_buckets < 4 || log2_buckets > 24 || max_queries == 0 || max_queries > (1u << 30) || !queries ||
-      !query_count || !rw_storage || !rw_selection)
+      !query_count || !rw_storage || !rw_selection) {
+    set_last_error("vlt_hg_query_select_noalloc: log2_buckets must be in [4, 24], max_queries in [1, 2^30], and "
+                   "every buffer pointer non-null");
     return VLT_ERR_INVALID_ARG;
+  }
   HashGridDims d = {log2_buckets, max_queries};
   if (hg_select_scratch_bytes(d) > (size_t)VLT_HG_SELECT_NOALLOC_SCRATCH_BYTES) {
     set_last_error("vlt_hg_query_select_noalloc: 2^log2_buckets buckets and max_queries need more scratch than the "
@@ -558,7 +563,10 @@ extern "C" vlt_status vlt_hg_query_select_noalloc(uint32_t log2_buckets, uint32_
   int dev = 0;
   vlt_status st = cuda_status(cudaGetDevice(&dev));
   if (st != VLT_OK) return st;
-  if (dev < 0 || dev >= 64) return VLT_ERR_INVALID_ARG;
+  if (dev < 0 || dev >= 64) {
+    set_last_error("vlt_hg_query_select_noalloc: device ordinals of 64 and above are not supported");
+    return VLT_ERR_INVALID_ARG;
+  }
   void* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_hg_select_scratch_mutex);

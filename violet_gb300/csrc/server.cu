@@ -93,7 +93,14 @@ void admit(vlt_server* s) {
     if (s->cfg.max_sessions && s->admitted >= s->cfg.max_sessions) fits = false;
     if (!fits) break;  // strict arrival order
     vlt_view* v = nullptr;
-    if (vlt_view_create(s->ctx, se.w, se.h, se.form, &se.params, &v) != VLT_OK) break;
+    const vlt_status cst = vlt_view_create(s->ctx, se.w, se.h, se.form, &se.params, &v);
+    if (cst != VLT_OK) {
+      // The session keeps its place at the head of the queue and is tried again at
+      // the next step, poll or close (a failed allocation leaves nothing behind).
+      ++s->stats.admit_failures;
+      s->stats.last_admit_status = (uint32_t)cst;
+      break;
+    }
     se.view = v;
     se.t_admit = now_ms();
     s->bytes_in_use += se.bytes;

@@ -190,5 +190,6 @@ int ctx_device(const vlt_ctx* c);
 // Thread-local record of the last CUDA error text.
 void set_last_error(const char* msg);
 vlt_status cuda_status(cudaError_t e);
+cudaError_t device_alloc(void** p, size_t bytes);
 
 }  // namespace vlt
