@@ -3561,6 +3561,59 @@ void vlto_oct(const float* n3, uint32_t* u16, uint32_t* u32, float* dec16, uint3
     dec16[3 * i + 2] = d.z;
   }
 }
+// Known-answer entry points matching the reference-shader build (oracle/_ref): the
+// same arguments and outputs as its vltr_* functions.
+void vlto_lcg_sequence(uint32_t px, uint32_t py, uint32_t seed, uint32_t count, float* rands, uint32_t* states) {
+  uint32_t s = lcg_init_with_seed(px, py, seed);
+  for (uint32_t k = 0; k < count; ++k) {
+    rands[k] = lcg_rand(s);
+    states[k] = s;
+  }
+}
+uint32_t vlto_xxhash32(const uint32_t* words, uint32_t n) {
+  XXHash32 h = XXHash32::init(words[0]);
+  for (uint32_t i = 1; i < n; ++i) h = h.add(words[i]);
+  return h.eval();
+}
+void vlto_oct_decode(const uint32_t* u16, const uint32_t* u32, float* n16, float* n32, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) {
+    float3 a = normal_decode_oct_u16(u16[i]);
+    float2 f = F2((float)(u32[i] & 0xFFFFu) / 65535.0f, (float)((u32[i] >> 16) & 0xFFFFu) / 65535.0f);
+    float3 b = normal_decode_oct(f);
+    n16[3 * i] = a.x, n16[3 * i + 1] = a.y, n16[3 * i + 2] = a.z;
+    n32[3 * i] = b.x, n32[3 * i + 1] = b.y, n32[3 * i + 2] = b.z;
+  }
+}
+void vlto_hit_pos_normal(const float* pos, const float* nrm, uint32_t* enc, float* dec_pos, float* dec_nrm,
+                         uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) {
+    HitPosNormal h;
+    h.pos = F3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    h.normal = F3(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+    h.encode(enc + 2 * i);
+    HitPosNormal d = HitPosNormal::decode(enc[2 * i], enc[2 * i + 1]);
+    dec_pos[3 * i] = d.pos.x, dec_pos[3 * i + 1] = d.pos.y, dec_pos[3 * i + 2] = d.pos.z;
+    dec_nrm[3 * i] = d.normal.x, dec_nrm[3 * i + 1] = d.normal.y, dec_nrm[3 * i + 2] = d.normal.z;
+  }
+}
+// {hash (65536 buckets), checksum} per point, position key (key mode 0).
+void vlto_vertex_key(const float* pos, const float* camera, uint32_t* out, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) {
+    VKey k = vertex_descriptor(F3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), F3(0.0f, 0.0f, 1.0f),
+                               F3(camera[0], camera[1], camera[2]), 0xFFFFu, 0u);
+    out[2 * i] = k.hash;
+    out[2 * i + 1] = k.checksum;
+  }
+}
+void vlto_gbuffer_decode(const uint32_t* enc, float* out, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) {
+    GBuffer g = decode_gbuffer(enc[4 * i], enc[4 * i + 1], enc[4 * i + 2], enc[4 * i + 3]);
+    float* o = out + 11 * i;
+    o[0] = g.color.x, o[1] = g.color.y, o[2] = g.color.z, o[3] = g.metallic;
+    o[4] = g.normal.x, o[5] = g.normal.y, o[6] = g.normal.z, o[7] = g.perceptual_roughness;
+    o[8] = g.fwidth_z, o[9] = g.fwidth_n, o[10] = asfloat(g.shading_path);
+  }
+}
 uint32_t vlto_reservoir_encode(uint32_t M, float W) { return reservoir_simple_encode_32b(M, W); }
 void vlto_reservoir_decode(uint32_t u, uint32_t* M, float* W) { reservoir_simple_decode_32b(u, M, W); }
 

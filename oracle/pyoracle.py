@@ -58,6 +58,12 @@ SIGS = {
     "vlto_math": (None, [C.c_int, P, P, U32]),
     "vlto_codec": (None, [C.c_int, P, P, U32]),
     "vlto_oct": (None, [P, P, P, P, U32]),
+    "vlto_lcg_sequence": (None, [U32, U32, U32, U32, P, P]),
+    "vlto_xxhash32": (U32, [P, U32]),
+    "vlto_oct_decode": (None, [P, P, P, P, U32]),
+    "vlto_hit_pos_normal": (None, [P, P, P, P, P, U32]),
+    "vlto_vertex_key": (None, [P, P, P, U32]),
+    "vlto_gbuffer_decode": (None, [P, P, U32]),
     "vlto_reservoir_encode": (U32, [U32, C.c_float]),
     "vlto_reservoir_decode": (None, [U32, C.POINTER(U32), C.POINTER(C.c_float)]),
 }
