@@ -335,6 +335,18 @@ inline vec<elem_t<X>, N> splat(const X& x) {
 template <int R, int C>
 struct mat {
   vec<float, C> m[R];  // rows
+  mat() = default;
+  // Components in row-major order (scalars or vectors), as HLSL's constructor.
+  template <class A, class... Rest>
+  explicit mat(const A& a, const Rest&... rest) {
+    int k = 0;
+    put(k, a);
+    (put(k, rest), ...);
+  }
+  template <class X>
+  void put(int& k, const X& x) {
+    for (int j = 0; j < n_of<X>; ++j, ++k) m[k / C].e[k % C] = cvt<float>(el(x, j));
+  }
   vec<float, C>& operator[](int r) { return m[r]; }
   const vec<float, C>& operator[](int r) const { return m[r]; }
   static mat from_column_major(const float* p) {
@@ -673,11 +685,15 @@ inline void InterlockedExchange(D& d, V v, O& orig) { orig = d; d = (D)v; }
 // ------------------------------------------------------------------ storage formats
 enum Fmt : int {
   FMT_R32F, FMT_RG32F, FMT_RGBA32F, FMT_R32UI, FMT_RG32UI, FMT_RGBA32UI,
-  FMT_R11G11B10F, FMT_R16F, FMT_RG16F, FMT_RGBA16F, FMT_R8UNORM, FMT_RGBA8UNORM
+  FMT_R11G11B10F, FMT_R16F, FMT_RG16F, FMT_RGBA16F, FMT_R8UNORM, FMT_RGBA8UNORM,
+  // An RGBA16F texture whose y and z channels are always 0, stored as its x and a
+  // halves (the AO history records).
+  FMT_XA16F
 };
 inline int fmt_bytes(Fmt f) {
   switch (f) {
-    case FMT_R32F: case FMT_R32UI: case FMT_R11G11B10F: case FMT_RG16F: case FMT_RGBA8UNORM: return 4;
+    case FMT_R32F: case FMT_R32UI: case FMT_R11G11B10F: case FMT_RG16F: case FMT_RGBA8UNORM: case FMT_XA16F:
+      return 4;
     case FMT_RG32F: case FMT_RG32UI: case FMT_RGBA16F: return 8;
     case FMT_RGBA32F: case FMT_RGBA32UI: return 16;
     case FMT_R16F: return 2;
@@ -696,12 +712,16 @@ inline int fmt_comps(Fmt f) {
 }
 
 // One image: `layers` planes of w*h texels in the format, row-major, layer-planar.
+// A texel may sit inside a larger per-pixel record: `stride` bytes between texels
+// (0: the format's size) and `offset` bytes into the record.
 struct Image {
   void* data = nullptr;
   int w = 0, h = 0, layers = 1;
   Fmt fmt = FMT_R32F;
+  int stride = 0, offset = 0;
   uint8_t* texel(int x, int y, int layer) const {
-    return (uint8_t*)data + ((size_t)layer * w * h + (size_t)y * w + x) * fmt_bytes(fmt);
+    const size_t st = stride ? (size_t)stride : (size_t)fmt_bytes(fmt);
+    return (uint8_t*)data + ((size_t)layer * w * h + (size_t)y * w + x) * st + offset;
   }
   bool in(int x, int y, int layer) const {
     return data && x >= 0 && y >= 0 && x < w && y < h && layer >= 0 && layer < layers;
@@ -735,6 +755,12 @@ struct Image {
       case FMT_RGBA8UNORM:
         for (int k = 0; k < 4; ++k) r.e[k] = orc::load_unorm8(p[k]);
         break;
+      case FMT_XA16F: {
+        uint16_t v[2];
+        memcpy(v, p, 4);
+        r = float4(orc::f16tof32(v[0]), 0.0f, 0.0f, orc::f16tof32(v[1]));
+        break;
+      }
       default: break;
     }
     return r;
@@ -771,6 +797,11 @@ struct Image {
       case FMT_RGBA8UNORM:
         for (int k = 0; k < 4; ++k) p[k] = orc::store_unorm8(c.e[k]);
         break;
+      case FMT_XA16F: {
+        uint16_t v[2] = {(uint16_t)orc::f32tof16(c.e[0]), (uint16_t)orc::f32tof16(c.e[3])};
+        memcpy(p, v, 4);
+        break;
+      }
       default: break;
     }
   }
@@ -869,14 +900,24 @@ struct Texture2D {
   }
 };
 
+// Element of an RW texture: reads load the texel (for vector texels the reference
+// also carries the loaded value, so that `rw[id].xyz` reads work), assignments store.
+struct TexScalarBase {};
 template <class T>
-struct TexRef {
+struct TexRef : std::conditional_t<is_vec_v<T>, T, TexScalarBase> {
+  using Base = std::conditional_t<is_vec_v<T>, T, TexScalarBase>;
   const Image* img;
   int x, y;
+  TexRef(const Image* im, int px, int py) : img(im), x(px), y(py) {
+    if constexpr (is_vec_v<T>) static_cast<T&>(*this) = texel_load<T>(*img, x, y, 0);
+  }
+  TexRef(const TexRef& o) : Base(o), img(o.img), x(o.x), y(o.y) {}
   operator T() const { return texel_load<T>(*img, x, y, 0); }
   template <class X>
   TexRef& operator=(const X& v) {
-    texel_store<T>(*img, x, y, 0, T(v));
+    const T t(v);
+    texel_store<T>(*img, x, y, 0, t);
+    if constexpr (is_vec_v<T>) static_cast<T&>(*this) = t;
     return *this;
   }
   TexRef& operator=(const TexRef& o) { return *this = (T)o; }
@@ -898,7 +939,7 @@ struct RWTexture2D {
   Image img;
   template <class C>
   TexRef<T> operator[](const C& c) const {
-    return TexRef<T>{&img, cvt<int32_t>(el(c, 0)), cvt<int32_t>(el(c, 1))};
+    return TexRef<T>(&img, cvt<int32_t>(el(c, 0)), cvt<int32_t>(el(c, 1)));
   }
   void GetDimensions(uint32_t& w, uint32_t& h) const {
     w = (uint32_t)img.w;

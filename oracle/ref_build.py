@@ -53,6 +53,9 @@ def _splat(m):
 
 
 REWRITES = [
+    # `(0.04f).xxx`: replicate swizzle of a parenthesised expression.
+    ("parenthesised swizzle", re.compile(r"\(([^()]+)\)\.(xx|xxx|xxxx|rr|rrr|rrrr)\b"),
+     lambda m: "hlsl::splat<%d>((%s))" % (len(m.group(2)), m.group(1))),
     # `0.5f.xx`, `f90.xxx`: replicate swizzles of scalars (and of vectors' x).
     ("scalar swizzle", re.compile(r"((?:\d+\.\d*f?)|(?:[A-Za-z_]\w*(?:\.[A-Za-z_]\w*)*))\.(xx|xxx|xxxx|rr|rrr|rrrr)\b"),
      _splat),
@@ -69,6 +72,9 @@ REWRITES = [
     ("semantics", re.compile(r"\s*:\s*SV_\w+"), ""),
     # `#pragma pack_matrix(...)`: matrices are filled from column-major memory.
     ("pack_matrix", re.compile(r"#pragma\s+pack_matrix\([^)]*\)"), ""),
+    # `const` locals of struct type: HLSL calls member functions on them freely (C++
+    # would need const member functions); the qualifier only guards against writes.
+    ("const struct locals", re.compile(r"\bconst\s+(?=[A-Z]\w*\s+\w+\s*=)"), ""),
     # `this` is a value in HLSL.
     ("this", re.compile(r"\bthis\b"), "(*this)"),
     # `(StructType)0`: a zero-initialised struct.
@@ -103,8 +109,32 @@ def strip_comments(text):
     return "".join(out)
 
 
+VEC_CTOR = re.compile(r"(?<![\w.])((?:float|int|uint|bool|half)[234](?:x[234])?)\s*\(")
+
+
+def brace_constructors(text):
+    """`float2(a, b)` -> `float2{a, b}`: C++ leaves the evaluation order of function
+    arguments unspecified (g++ often goes right to left), HLSL evaluates them left to
+    right, and `float2(lcg_rand(s), lcg_rand(s))` depends on it; a braced initializer
+    list is evaluated left to right."""
+    out, pos = [], 0
+    while True:
+        m = VEC_CTOR.search(text, pos)
+        if not m:
+            out.append(text[pos:])
+            return "".join(out)
+        depth, j = 1, m.end()
+        while depth and j < len(text):
+            depth += {"(": 1, ")": -1}.get(text[j], 0)
+            j += 1
+        inner = brace_constructors(text[m.end():j - 1])
+        out.append(text[pos:m.start()] + m.group(1) + "{" + inner + "}")
+        pos = j
+
+
 def rewrite(text):
     text = strip_comments(text)
+    text = brace_constructors(text)
     entry = None
     m = MAIN_RE.search(text)
     if m:
