@@ -2,8 +2,9 @@
 
 Compiles the CPU restatement (oracle.cpp, binary32 without FMA contraction) and its
 binary64 denoiser (oracle64.cpp) into oracle/_build/libvlt_oracle.so with g++
-(OpenMP). The reference itself (HLSL + a
-Rust/Vulkan host) cannot be compiled here, so there is no oracle/_ref build.
+(OpenMP). The reference's own shaders, compiled as C++ against an HLSL vocabulary
+header, are built separately by oracle/ref_build.py into oracle/_ref/ (only where
+the reference tree is present); they pin this restatement.
 """
 import os
 import subprocess

@@ -13,11 +13,14 @@
 // and denoising.rs:66-301. Storage uses the reference texture formats packed as in
 // include/vlt.h (the product's records), so results compare byte for byte.
 //
-// Parity pinning: the reference is HLSL run through DXC/Vulkan and a Rust host; none
-// of it can be compiled or run here (no dxc, no graphics stack, no cargo), and the
-// reference ships no tests, golden images or fixtures. Parity with the reference's
-// own outputs is therefore UNPINNED; this restatement is checked against known-answer
-// vectors derived by hand from the shader text (tests/golden/).
+// Parity pinning: the reference is HLSL run through DXC/Vulkan from a Rust host, and
+// it ships no tests, golden images or fixtures. Its compute shaders are compiled here
+// as C++ instead (oracle/ref_build.py with the HLSL vocabulary in oracle/hlsl/, into
+// oracle/_ref/), and every per-pass function below is checked bit for bit against
+// that build of the reference's own text (tests/test_ref_passes.py, and through the
+// fixtures in tests/golden/ everywhere), under the numeric contract of omath.hpp for
+// what HLSL leaves implementation-defined. The frame sequencing (which pass runs when,
+// with which seeds and flags) follows restir_renderer.rs and denoising.rs by hand.
 //
 // Rows run in parallel with OpenMP (the stand-in for the Rust host's rayon); the
 // hash-grid insertion runs sequentially in query order, which defines its result.

@@ -91,3 +91,46 @@ def first_float_mismatch(a, b, width=None, rec=1):
     if not bad.any():
         return None
     return first_mismatch(np.where(bad, a, 0), np.where(bad, b, 0), width, rec)
+
+
+def ref_golden_cases():
+    """The cases of tests/golden/ref_passes.npz (made from the reference's own shaders
+    by tests/golden/make_ref_golden.py): a list of (pass name, args, expected outputs);
+    args are (kind, value) with kind in fp, params, in, out, inout, u32, i32, f32, none."""
+    import json
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_passes.npz")
+    z = np.load(path)
+    man = json.loads(bytes(z["manifest"]).decode())
+    out = []
+    for c in man["cases"]:
+        args = [(k, z[v] if k in ("fp", "params", "in", "out", "inout") else v) for k, v in c["args"]]
+        out.append((c["pass"], args, [z[k] for k in c["expect"]]))
+    return out
+
+
+def call_with_args(fn, args, arrays_in, fp_type, params_type):
+    """Calls fn with the fixture args; `arrays_in(kind, ndarray)` turns an array argument
+    into a pointer (and keeps whatever it allocates). Returns the ctypes call list."""
+    call, keep = [], []
+    for kind, v in args:
+        if kind == "fp":
+            s = fp_type.from_buffer_copy(v.tobytes())
+            keep.append(s)
+            call.append(C.byref(s))
+        elif kind == "params":
+            s = params_type.from_buffer_copy(v.tobytes())
+            keep.append(s)
+            call.append(C.byref(s))
+        elif kind in ("in", "out", "inout"):
+            call.append(arrays_in(kind, v))
+        elif kind == "u32":
+            call.append(C.c_uint32(v))
+        elif kind == "i32":
+            call.append(C.c_int32(v))
+        elif kind == "f32":
+            call.append(C.c_float(v))
+        else:
+            call.append(None)
+    return call, keep

@@ -99,3 +99,59 @@ def test_own_math_special_values():
     assert np.isnan(po.math("log2", np.array([-1.0], np.float32))[0])
     assert po.math("log2", np.array([8.0], np.float32))[0] == 3.0
     assert np.isnan(po.math("sin", np.array([np.inf], np.float32))[0])
+
+
+# ---- known answers of the reference's own shader text (tests/golden/ref_primitives.npz,
+# made by tests/golden/make_ref_golden.py from the HLSL compiled as C++)
+
+REFP = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_primitives.npz"))
+
+
+def _bits(a):
+    a = np.ascontiguousarray(a).view(np.uint32)
+    return np.where((a & 0x7FFFFFFF) > 0x7F800000, np.uint32(0x7FC00000), a)
+
+
+def test_reference_shader_hashes_and_lcg():
+    assert np.array_equal(po.codec("jenkins", REFP["jenkins_in"]), REFP["jenkins_out"])
+    for (px, py, sd), rands, states in zip(REFP["lcg_seeds"], REFP["lcg_rands"], REFP["lcg_states"]):
+        r, st = np.zeros(8, np.float32), np.zeros(8, np.uint32)
+        po.lib().vlto_lcg_sequence(int(px), int(py), int(sd), 8, po.ptr(r), po.ptr(st))
+        assert np.array_equal(st, states) and np.array_equal(_bits(r), _bits(rands))
+    for w, outs in zip(REFP["xxh_words"], REFP["xxh_out"]):
+        for k in range(1, 5):
+            assert po.lib().vlto_xxhash32(po.ptr(np.ascontiguousarray(w[:k])), k) == outs[k - 1]
+
+
+def test_reference_shader_codecs():
+    n3 = np.ascontiguousarray(REFP["oct_in"].reshape(-1))
+    n = n3.size // 3
+    u16, u32, dec = np.zeros(n, np.uint32), np.zeros(n, np.uint32), np.zeros(3 * n, np.float32)
+    po.lib().vlto_oct(po.ptr(n3), po.ptr(u16), po.ptr(u32), po.ptr(dec), n)
+    assert np.array_equal(u16, REFP["oct_u16"]) and np.array_equal(u32, REFP["oct_u32"])
+    c16, c32 = REFP["octd_u16"], REFP["octd_u32"]
+    a, b = np.zeros(3 * c16.size, np.float32), np.zeros(3 * c16.size, np.float32)
+    po.lib().vlto_oct_decode(po.ptr(c16), po.ptr(c32), po.ptr(a), po.ptr(b), c16.size)
+    assert np.array_equal(_bits(a), _bits(REFP["octd_n16"])) and np.array_equal(_bits(b), _bits(REFP["octd_n32"]))
+    for M, W, e, dM, dW in zip(REFP["rs_M"][::5], REFP["rs_W"][::5], REFP["rs_enc"][::5], REFP["rs_dM"][::5],
+                               REFP["rs_dW"][::5]):
+        assert po.lib().vlto_reservoir_encode(int(M), float(W)) == e
+    pos, nrm = np.ascontiguousarray(REFP["hpn_pos"].reshape(-1)), np.ascontiguousarray(REFP["hpn_nrm"].reshape(-1))
+    n = pos.size // 3
+    enc, dp, dn = np.zeros(2 * n, np.uint32), np.zeros(3 * n, np.float32), np.zeros(3 * n, np.float32)
+    po.lib().vlto_hit_pos_normal(po.ptr(pos), po.ptr(nrm), po.ptr(enc), po.ptr(dp), po.ptr(dn), n)
+    assert np.array_equal(enc, REFP["hpn_enc"])
+    assert np.array_equal(_bits(dp), _bits(REFP["hpn_dpos"])) and np.array_equal(_bits(dn), _bits(REFP["hpn_dnrm"]))
+
+
+def test_reference_shader_vertex_key_and_gbuffer():
+    pos = np.ascontiguousarray(REFP["vk_pos"].reshape(-1))
+    n = pos.size // 3
+    out = np.zeros(2 * n, np.uint32)
+    po.lib().vlto_vertex_key(po.ptr(pos), po.ptr(REFP["vk_cam"]), po.ptr(out), n)
+    ref = REFP["vk_out"].reshape(n, 5)
+    assert np.array_equal(out.reshape(n, 2), ref[:, :2])
+    enc = REFP["gb_enc"]
+    g = np.zeros(11 * (enc.size // 4), np.float32)
+    po.lib().vlto_gbuffer_decode(po.ptr(enc), po.ptr(g), enc.size // 4)
+    assert np.array_equal(_bits(g), _bits(REFP["gb_out"]))
