@@ -37,6 +37,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -87,6 +89,19 @@ PASS_BYTES_PER_PIXEL_F32 = dict(
     taa=4 + 16 + 16 + 16,
 )
 PASS_BYTES_PER_PIXEL = {"ref": PASS_BYTES_PER_PIXEL_REF, "f32": PASS_BYTES_PER_PIXEL_F32}
+
+# The whole frame's fused minimum per pixel (each input read once, each piece of
+# persistent state read once and written once, each output written once), from the
+# record layouts: inputs depth 4 + G-buffer 16 + previous depth 4 + previous G-buffer
+# 16 + diffuse candidate 12 + its source pdf 4 + specular candidate 20 = 76; state
+# (read + write) diffuse reservoir 48 (f32) / 17 (f16), specular reservoir 28 / 24, AO
+# history 8 / 4, denoiser history record + length 33 / 17; outputs (diffuse +
+# specular) 32 / 16. Hash grid per frame: the decay bytes read and written (2 per
+# cell) plus 37 bytes per updated cell (cell radiance 12 read and 12 written, decay
+# byte 1, the query's radiance 12 read).
+FRAME_BYTES_PER_PIXEL = {"f32": 76 + 2 * (48 + 28 + 8 + 33) + 32, "f16": 76 + 2 * (17 + 24 + 4 + 17) + 16}
+FRAME_BYTES_PER_CELL = 2
+FRAME_BYTES_PER_UPDATED_CELL = 37
 FORM = "f32"
 PASS_BYTES_PER_CELL = {"hg_decay": 2, "hg_compact": 4}
 # DRAM bytes per launch unit measured with ncu (dram__bytes_read.sum +
@@ -194,8 +209,29 @@ def measured_peaks():
         return None
 
 
+# The knobs of the plain 1920x1080 workload (vlt_params_plain(1)); kept here as values
+# so that the CPU reference arm builds them without loading the product library
+# (tests/test_scene.py checks them against the library's preset).
+WORKLOAD_KNOBS = {
+    "diff_m_cap": 20, "spec_m_cap": 20, "use_input_pdf": 1, "diff_spatial_passes": 2, "diff_spatial_taps": 8,
+    "diff_spatial_radius_px": 16.0, "spec_spatial_passes": 2, "spec_spatial_taps": 8, "spec_spatial_radius_px": 16.0,
+    "ao_radius": 2.0, "denoise": 1, "disocclusion_fix": 1, "fast_history_clamp": 0, "atrous_iterations": 5,
+    "history_max_frames": 32.0, "hg_enable": 1, "hg_decay": 1, "hg_log2_buckets": 18, "hg_key_mode": 1,
+    "hg_max_queries": 0, "post": 0, "trace": 0, "diff_validate": 0, "spec_validate": 0,
+}
+
+
 def workload_params(vg):
     return vg.params_plain(1)
+
+
+def workload_params_struct():
+    from violet_gb300 import _ffi
+
+    p = _ffi.Params()
+    for k, v in WORKLOAD_KNOBS.items():
+        setattr(p, k, v)
+    return p
 
 
 def input_bytes_per_pixel(vg, params):
@@ -241,41 +277,47 @@ def cpu_sample(width, height, frames, seed, threads=None):
 
 
 def run_reference(args, ws, rank):
+    """The reference's algorithm on the host cores: the CPU restatement of its passes
+    (the oracle, all host threads), on the same 1920x1080 workload as the GPU arm (same
+    scene seed, knobs and frames), one frame per step. The frames are synthesised by
+    the oracle's host build of the scene generator, outside the timed spans; only the
+    restatement's frame calls are timed. This process loads the oracle's libraries
+    only."""
     if rank != 0:
         return
-    # Each step: one frame of a 480x270 view of the same scene and knobs (1/16 of the
-    # 1080p pixels), so that --steps/--warmup finish within minutes on the host.
-    sw, sh = 480, 270
-    import violet_gb300 as vg
     from oracle import pyoracle as po
+    from oracle import pyscene
 
-    params = workload_params(vg)
-    scene = vg.Scene(1000, sw, sh, disocclusion_frac=0.02)
-    ov = po.OracleView(sw, sh, params, FORM)
-    frames = [scene.generate_host(f) for f in range(args.warmup + args.steps)]
-    fps = [scene.frame_params(f) for f in range(args.warmup + args.steps)]
+    W, H = args.width, args.height
+    params = workload_params_struct()
+    scene = pyscene.Scene(1000, W, H, disocclusion_frac=0.02)
+    ov = po.OracleView(W, H, params, FORM)
+    out = {k: np.zeros(16 * W * H, np.uint8) for k in ("diffuse", "specular")}
     for f in range(args.warmup):
-        ov.run(fps[f], f, frames[f])
-    t0 = time.perf_counter()
+        ov.run(scene.frame_params(f), f, scene.generate_host(f), out)
+    total = 0.0
     for k in range(args.steps):
         f = args.warmup + k
-        ov.run(fps[f], f, frames[f])
-    dt = time.perf_counter() - t0
+        host, fp = scene.generate_host(f), scene.frame_params(f)
+        t0 = time.perf_counter()
+        ov.run(fp, f, host, out)
+        total += time.perf_counter() - t0
     ov.close()
-    value = args.steps * sw * sh / dt / 1e6
+    value = args.steps * W * H / total / 1e6
     cores = po.threads()
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "width": W_DEFAULT, "height": H_DEFAULT, "storage": "fp32",
-                   "sample": "480x270 view per step"},
+        "config": {"workload": WORKLOAD, "width": W, "height": H, "storage": FORM,
+                   "parallelism": "single view", "knobs": dict(WORKLOAD_KNOBS)},
         "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": cores, "kind": "port",
-                         "sample": "%d frames of a 480x270 view of the same scene and knobs after %d warm-up frames"
-                                   % (args.steps, args.warmup)},
+                         "sample": "%d frames of the %dx%d workload after %d warm-up frames (frame synthesis not "
+                                   "timed)" % (args.steps, W, H, args.warmup)},
         "e2e": {"value": value, "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference runs HLSL through DXC/Vulkan from a Rust host; neither a Vulkan stack nor cargo "
-                "exists here, so its passes run as the CPU restatement on all host threads",
+                "exists on this machine, so its passes run as the CPU restatement (checked bit for bit against "
+                "the reference's shaders compiled as C++) on all host threads",
     }
     print(json.dumps(line), flush=True)
 
@@ -379,6 +421,22 @@ def run_ours(args, ws, rank, local):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic * units if traffic else None, "kernel": dom,
                 "alg_bytes_per_launch": alg_bytes, "launch_ms": avg_s * 1e3, "peak_source": peak_src}
+    # The whole frame against HBM: the fused-minimum bytes of a frame (inputs, state
+    # read and written, outputs, and the hash grid's decay bytes and updated cells,
+    # counted on the last profiled frame) over the headline frame time.
+    cells = 16 << params.hg_log2_buckets
+    ptr_u, _ = view.buffer("hg_compact_count")
+    torch.cuda.synchronize()
+    ubuf = torch.zeros(1, dtype=torch.int32, device=dev)
+    ctypes.CDLL("libcudart.so.13").cudaMemcpy(ctypes.c_void_p(ubuf.data_ptr()), ctypes.c_void_p(ptr_u),
+                                              ctypes.c_size_t(4), 3)
+    upd = int(ubuf.cpu().item())
+    frame_bytes = FRAME_BYTES_PER_PIXEL[FORM] * n + FRAME_BYTES_PER_CELL * cells + FRAME_BYTES_PER_UPDATED_CELL * upd
+    frame_gbs = frame_bytes / (ms / args.steps / 1e3) / 1e9
+    roofline["frame"] = {"bytes_per_frame": frame_bytes, "bytes_per_pixel": FRAME_BYTES_PER_PIXEL[FORM],
+                         "hash_grid_cells": cells, "updated_cells": upd, "achieved": frame_gbs,
+                         "frac": frame_gbs / peak, "unit": "GB/s",
+                         "definition": "fused-minimum bytes per frame / headline ms per frame"}
     # The same launch against the SMs' instruction-issue rate at the sampled clock.
     issue = None
     wi = MEASURED_WARP_INSTRUCTIONS_PER_UNIT.get(dom)
@@ -457,6 +515,9 @@ def run_ours(args, ws, rank, local):
     batched = None
     if not args.no_batched:
         batched = batched_leg(args, ws, dev)
+        # Small views (widths 256..640), where a plain frame is too short to fill the GPU
+        # and batching the views into one launch per pass should pay.
+        batched["small_views"] = batched_leg(args, ws, dev, w_max=640.0)
 
     precision = None
     if not args.no_precision:
@@ -473,6 +534,20 @@ def run_ours(args, ws, rank, local):
     serving = None
     if not args.no_serving:
         serving = serving_leg(args, ws, dev)
+        if not args.no_serving_sweep:
+            # Latency/throughput across the per-step pixel budget (shorter runs), and one
+            # run where the HBM budget alone gates admission.
+            sweep = []
+            for mpix in (6.0, 12.0, 24.0, 0.0):
+                r = serving_leg(args, ws, dev, seconds=args.sweep_seconds, step_mpix=mpix)
+                sweep.append({k: r[k] for k in ("step_pixel_budget_mpix", "hbm_budget_gb", "value", "latency_ms",
+                                                "latency_ms_by_class", "admission_wait_ms", "time_to_first_frame_ms",
+                                                "frames_per_step", "sessions_admitted", "peak_bytes_in_use_gb")})
+            r = serving_leg(args, ws, dev, seconds=args.sweep_seconds, step_mpix=0.0, hbm_gb=args.sweep_hbm_gb)
+            sweep.append({k: r[k] for k in ("step_pixel_budget_mpix", "hbm_budget_gb", "value", "latency_ms",
+                                            "latency_ms_by_class", "admission_wait_ms", "time_to_first_frame_ms",
+                                            "frames_per_step", "sessions_admitted", "peak_bytes_in_use_gb")})
+            serving["sweep"] = sweep
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -508,15 +583,13 @@ def run_ours(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
-def batch_view_set(n_views, seed):
-    """Resolutions drawn log-uniformly from 256x144 to 2560x1440 (by width), aspect
-    16:9, 4:3 or 1:1, each view with its own scene seed."""
-    import numpy as np
-
+def batch_view_set(n_views, seed, w_max=2560.0):
+    """Resolutions drawn log-uniformly from 256x144 to w_max (by width; 2560x1440 by
+    default), aspect 16:9, 4:3 or 1:1, each view with its own scene seed."""
     rng = np.random.default_rng(seed)
     views = []
     for k in range(n_views):
-        w = float(np.exp(rng.uniform(np.log(256.0), np.log(2560.0))))
+        w = float(np.exp(rng.uniform(np.log(256.0), np.log(w_max))))
         aspect = [16.0 / 9.0, 4.0 / 3.0, 1.0][int(rng.integers(0, 3))]
         w = int(round(w / 2.0)) * 2
         h = max(2, int(round(w / aspect / 2.0)) * 2)
@@ -524,7 +597,7 @@ def batch_view_set(n_views, seed):
     return views
 
 
-def batched_leg(args, ws, dev):
+def batched_leg(args, ws, dev, w_max=2560.0):
     """Many views of uneven size per step: every view's frames run one by one
     through vlt_frame_run (plain), then the same frames through vlt_batch_run
     (batched persistent kernels, CUDA graphs, autotuned tiles). Inputs are resident;
@@ -533,7 +606,7 @@ def batched_leg(args, ws, dev):
 
     import violet_gb300 as vg
 
-    specs = batch_view_set(args.batch_views, 42)
+    specs = batch_view_set(args.batch_views, 42, w_max)
     frames_total = args.batch_frames
     warm = 3
     params = workload_params(vg)
@@ -619,8 +692,8 @@ def batched_leg(args, ws, dev):
     torch.cuda.empty_cache()
     px = ws * total_px * steps
     return {
-        "workload": "%d views, %d frames each, widths log-uniform 256..2560, aspect 16:9/4:3/1:1" % (
-            len(specs), frames_total),
+        "workload": "%d views, %d frames each, widths log-uniform 256..%d, aspect 16:9/4:3/1:1" % (
+            len(specs), frames_total, int(w_max)),
         "storage": args.batch_form, "views": len(specs), "frames": frames_total, "timed_steps": steps,
         "mpix_per_step": total_px / 1e6,
         "value": px / (batch_ms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": batch_ms / steps,
@@ -856,10 +929,14 @@ SERVE_CLASSES = [("720p", 1280, 720, 0.3), ("1080p", 1920, 1080, 0.4), ("1440p",
 POOL_FRAMES = 16
 
 
-def serving_leg(args, ws, dev):
+def serving_leg(args, ws, dev, seconds=None, step_mpix=None, hbm_gb=None):
     """Poisson arrivals of view-sessions through the server (vlt_server_*): each
     admitted session keeps one frame queued (the next is submitted when the last
     completes); every step batches the queued frames of all admitted sessions.
+    Per-frame latency is submit-to-completion (a session's first frame is submitted
+    when the session opens, so it includes the admission wait); the admission wait of
+    a session is its first frame's latency minus the step that ran it; time to first
+    frame is open-to-completion of that frame.
     Per-frame latency is submit-to-completion on the host clock. Frame inputs come
     from a pool of POOL_FRAMES consecutive frames per resolution class, walked
     forth and back, so the timed loop runs only the lighting path."""
@@ -868,6 +945,9 @@ def serving_leg(args, ws, dev):
 
     import violet_gb300 as vg
 
+    seconds = args.serve_seconds if seconds is None else seconds
+    step_mpix = args.serve_step_mpix if step_mpix is None else step_mpix
+    hbm_gb = args.serve_hbm_gb if hbm_gb is None else hbm_gb
     rng = np.random.default_rng(4242)
     params = workload_params(vg)
     stream = torch.cuda.Stream(device=dev)
@@ -883,13 +963,13 @@ def serving_leg(args, ws, dev):
         pools[name] = frames
     torch.cuda.synchronize()
     ctx = vg.Context(dev.index)
-    server = vg.Server(ctx, int(args.serve_hbm_gb * 1e9), int(args.serve_step_mpix * 1e6))
+    server = vg.Server(ctx, int(hbm_gb * 1e9), int(step_mpix * 1e6))
     # arrivals
     t_arr, classes, lengths = [], [], []
     t = 0.0
     while True:
         t += rng.exponential(1.0 / args.serve_rate)
-        if t > args.serve_seconds:
+        if t > seconds:
             break
         t_arr.append(t)
         k = int(rng.choice(len(SERVE_CLASSES), p=[c[3] for c in SERVE_CLASSES]))
@@ -899,6 +979,7 @@ def serving_leg(args, ws, dev):
     out_px = {"ref": 4, "f32": 16, "f16": 8}[form]
     live = {}  # session id -> state
     lat_all, lat_cls = [], {c[0]: [] for c in SERVE_CLASSES}
+    admit_wait, ttff = [], []
     frames_done = 0
     pix_done = 0
     nxt = 0
@@ -910,11 +991,11 @@ def serving_leg(args, ws, dev):
         while nxt < len(t_arr) and t_arr[nxt] <= now:
             name, w, h, _ = SERVE_CLASSES[classes[nxt]]
             sid = server.open(w, h, form, params)
-            live[sid] = {"cls": name, "w": w, "h": h, "n": lengths[nxt], "sent": 0, "done": 0,
+            live[sid] = {"cls": name, "w": w, "h": h, "n": lengths[nxt], "sent": 0, "done": 0, "t_open": now,
                          "out": {o: torch.empty(w * h * out_px, dtype=torch.uint8, device=dev)
                                  for o in ("diffuse", "specular")}}
             nxt += 1
-        if now > args.serve_seconds:
+        if now > seconds:
             break
         for sid, st in live.items():
             if st["sent"] == st["done"] and st["sent"] < st["n"]:
@@ -929,6 +1010,9 @@ def serving_leg(args, ws, dev):
             steps += 1
         for sid, tag, lat, step_ms in server.poll(wait=True):
             st = live[sid]
+            if st["done"] == 0:
+                admit_wait.append(max(lat - step_ms, 0.0))
+                ttff.append((time.perf_counter() - t0) * 1e3 - st["t_open"] * 1e3)
             st["done"] += 1
             lat_all.append(lat)
             lat_cls[st["cls"]].append(lat)
@@ -951,10 +1035,18 @@ def serving_leg(args, ws, dev):
     def pct(x, q):
         return float(np.percentile(x, q)) if x else None
 
+    waiting_open = [(elapsed - st["t_open"]) * 1e3 for st in live.values() if st["done"] == 0]
     return {
         "workload": "Poisson %.0f sessions/s for %.0f s; 720p/1080p/1440p/2160p with p=0.3/0.4/0.2/0.1; 30-300 "
-                    "frames each; HBM budget %.0f GB; step pixel budget %.1f Mpix" % (
-                        args.serve_rate, args.serve_seconds, args.serve_hbm_gb, args.serve_step_mpix),
+                    "frames each; HBM budget %.0f GB; step pixel budget %s" % (
+                        args.serve_rate, seconds, hbm_gb, ("%.1f Mpix" % step_mpix) if step_mpix else "off"),
+        "hbm_budget_gb": hbm_gb, "step_pixel_budget_mpix": step_mpix or None,
+        "admission_wait_ms": {"p50": pct(admit_wait, 50), "p99": pct(admit_wait, 99), "sessions": len(admit_wait),
+                              "still_waiting_at_end": len(waiting_open),
+                              "still_waiting_min_ms": min(waiting_open) if waiting_open else None},
+        "time_to_first_frame_ms": {"p50": pct(ttff, 50), "p99": pct(ttff, 99)},
+        "peak_bytes_in_use_gb": stats["bytes_in_use"] / 1e9,
+        "admit_failures": stats.get("admit_failures", 0),
         "storage": form, "sessions_arrived": len(t_arr), "sessions_admitted": stats["sessions_admitted"],
         "sessions_completed": stats["sessions_closed"], "sessions_waiting_at_end": stats["sessions_waiting"],
         "frames": frames_done, "steps": steps, "frames_per_step": frames_done / max(steps, 1),
@@ -982,6 +1074,9 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-hbm-gb", type=float, default=150.0)
     ap.add_argument("--serve-step-mpix", type=float, default=6.0)
+    ap.add_argument("--no-serving-sweep", action="store_true")
+    ap.add_argument("--sweep-seconds", type=float, default=15.0)
+    ap.add_argument("--sweep-hbm-gb", type=float, default=12.0)
     ap.add_argument("--batch-views", type=int, default=48)
     ap.add_argument("--batch-frames", type=int, default=32)
     ap.add_argument("--batch-form", default="f16", choices=["ref", "f32", "f16"])

@@ -47,3 +47,26 @@ def test_frame_params_camera_motion_and_jitter():
     assert np.allclose(vp @ ivp, np.eye(4), atol=1e-4)
     # Halton(2,3) jitter of index 1 (render_loop.rs:89-95): (2*0.5-1, 2*(1/3)-1) / size
     assert np.isclose(p0.jitter[0], 0.0) and np.isclose(p0.jitter[1], (2 / 3 - 1) / 180)
+
+
+def test_host_only_generator_matches_the_product_library():
+    """The oracle's copy of the scene generator (the product's source compiled without
+    CUDA, used by the CPU benchmark) produces the same frames as the product library."""
+    from oracle import pyscene
+
+    W, H = 96, 54
+    a = vg.Scene(1000, W, H, disocclusion_frac=0.02)
+    b = pyscene.Scene(1000, W, H, disocclusion_frac=0.02)
+    for f in (0, 5):
+        assert bytes(a.frame_params(f)) == bytes(b.frame_params(f))
+        ha, hb = a.generate_host(f), b.generate_host(f)
+        assert ha.keys() == hb.keys()
+        for k in ha:
+            assert np.array_equal(ha[k].view(np.uint8), hb[k].view(np.uint8)), k
+
+
+def test_benchmark_knobs_are_the_plain_1080p_preset():
+    import bench
+
+    p = vg.params_plain(1)
+    assert {k: getattr(p, k) for k, _ in p._fields_} == bench.WORKLOAD_KNOBS

@@ -806,6 +806,7 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
       {"hg_queries", b.hg_queries[v->hg_qcur], v->p.hg_enable ? (size_t)v->hg.max_queries * 32 : 0},
       {"hg_query_count", b.hg_qcount[v->hg_qcur], v->p.hg_enable ? (size_t)4 : (size_t)0},
       {"hg_selection", b.hg_sel, nc * 4},
+      {"hg_compact_count", b.hg_ccount, v->p.hg_enable ? (size_t)4 : (size_t)0},
       {"prev_depth", b.prev_depth, 4 * n},
       {"color", b.lit, by(4, 16, 8) * n},
       {"taa_history", v->taa_valid ? b.taa[v->taa_cur] : nullptr, by(4, 16, 8) * n},

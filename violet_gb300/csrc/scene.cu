@@ -7,7 +7,13 @@
 
 #include "../../include/vlt_scene.h"
 #include "scene_gen.cuh"
+#ifndef VLT_SCENE_HOST_ONLY
 #include "vlt_internal.h"
+#else
+// Host-only build of the generator (no CUDA runtime): the CPU benchmark of the
+// oracle synthesises its inputs with it without loading the product library.
+#include "../../include/vlt.h"
+#endif
 
 using namespace vlt;
 using namespace vlt::scene;
@@ -174,7 +180,7 @@ void fill_params(const Desc& d, uint32_t frame, vlt_frame_params* out) {
   out->sun_inten[2] = 17.0f;
 }
 
-__host__ __device__ inline void store_pixel(const PixelOut& p, const vlt_scene_frame& f, size_t i, size_t plane) {
+VLT_HD void store_pixel(const PixelOut& p, const vlt_scene_frame& f, size_t i, size_t plane) {
   f.depth[i] = p.depth;
   f.gbuffer[i] = p.g0;
   f.gbuffer[plane + i] = p.g1;
@@ -188,6 +194,7 @@ __host__ __device__ inline void store_pixel(const PixelOut& p, const vlt_scene_f
   if (f.shadow_mask) f.shadow_mask[i] = (uint8_t)p.shadow;
 }
 
+#ifndef VLT_SCENE_HOST_ONLY
 __global__ void k_scene_a(Object o, Desc d, vlt_frame_params fp, uint32_t frame, vlt_scene_frame f) {
   uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= d.width || y >= d.height) return;
@@ -219,6 +226,8 @@ __global__ void k_scene_trace(Object o, uint64_t seed, f3 sun, const float* __re
   float4* hp = (float4*)(hits + (size_t)i * 16);
   for (int k = 0; k < 4; ++k) hp[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
 }
+
+#endif  // VLT_SCENE_HOST_ONLY
 
 bool valid_frame(const vlt_scene_frame* f) {
   return f && f->depth && f->gbuffer && f->diff_hit_pos_normal && f->diff_hit_radiance && f->spec_hit_pos &&
@@ -291,6 +300,7 @@ vlt_status vlt_scene_trace_host(const vlt_scene_desc* dd, const vlt_frame_params
   return VLT_OK;
 }
 
+#ifndef VLT_SCENE_HOST_ONLY
 vlt_status vlt_scene_trace_device(const vlt_scene_desc* dd, const vlt_frame_params* fp, const vlt_ray* rays,
                                   uint32_t n, vlt_ray_hit* hits, void* stream) {
   if (!dd || !fp || (n && (!rays || !hits))) return VLT_ERR_INVALID_ARG;
@@ -318,5 +328,6 @@ vlt_status vlt_scene_generate_device(const vlt_scene_desc* dd, uint32_t frame, c
   k_scene_c<<<(n + 255) / 256, 256, 0, s>>>(d, frame, *f);
   return cuda_status(cudaGetLastError());
 }
+#endif  // VLT_SCENE_HOST_ONLY
 
 }  // extern "C"
