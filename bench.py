@@ -522,6 +522,8 @@ def run_ours(args, ws, rank, local):
     precision = None
     if not args.no_precision:
         precision = precision_leg(args, ws, dev)
+        if rank == 0 and not args.no_fp64:
+            precision["against_fp64"] = fp64_precision_leg(args, dev)
 
     post = None
     if not args.no_post:
@@ -801,6 +803,86 @@ def precision_leg(args, ws, dev):
         "f16_vs_f32_rel_l2": {o: {"mean": float(np.mean(v)), "max": float(np.max(v))} for o, v in rel.items()},
         "reductions": "binary64 on the GPU (vlt_image_stats)",
     }
+
+
+FP64_OUTPUTS = ["diff_W", "spec_W", "ao", "raw_diffuse", "raw_specular", "ray_len", "hist_color", "hist_moments",
+                "variance", "denoised_diffuse", "denoised_specular"]
+
+
+def fp64_precision_leg(args, dev):
+    """Per-output error of the FP32 and FP16 storage forms against the binary64
+    replay of the whole back end (oracle/oracle64r.cpp): every frame the GPU view and
+    the oracle's view of the same form run the same inputs (their outputs are
+    checked bit for bit), and the replay, following the float form's decisions (the
+    same selected samples, accepted taps and history lengths), recomputes every value
+    in binary64 with unquantized storage. The differences are the form's arithmetic
+    and storage alone. Plain knobs of the 1080p workload at 960x540 (1/16 of the 4K
+    pixels of the precision workload; the binary64 replay runs on the host)."""
+    import torch
+
+    import violet_gb300 as vg
+    from oracle import pyoracle as po
+
+    W, H = args.fp64_width, args.fp64_height
+    n = W * H
+    params = workload_params(vg)
+    ctx = vg.Context(dev.index)
+    res = {}
+    for form in ("f32", "f16"):
+        ob = 16 if form == "f32" else 8
+        dt = np.float32 if form == "f32" else np.float16
+        scene = vg.Scene(4000, W, H, disocclusion_frac=0.02)
+        view = vg.View(ctx, W, H, form, params)
+        ov = po.OracleView(W, H, params, form)
+        ov.enable_fp64()
+        dev_in = input_buffers(vg, params, W, H, dev)
+        out_dev = {k: torch.zeros(ob * n, dtype=torch.uint8, device=dev) for k in ("diffuse", "specular")}
+        errs = {k: [] for k in FP64_OUTPUTS}
+        flips, gpu_mismatch, decisions_equal = [], 0, True
+        for f in range(args.fp64_frames):
+            host = scene.generate_host(f)
+            for k, t in dev_in.items():
+                t.copy_(torch.from_numpy(host[k].view(np.uint8)))
+            fp = scene.frame_params(f)
+            view.run(fp, f, dev_in, out_dev)
+            out_host = {k: np.zeros(ob * n, np.uint8) for k in ("diffuse", "specular")}
+            ov.run(fp, f, host, out_host)
+            got = {k: out_dev[k].cpu().numpy() for k in out_dev}
+            if any(not np.array_equal(got[k], out_host[k]) for k in got):
+                gpu_mismatch += 1
+            flips.append(ov.fp64_flips())
+            for nm in ("diff_M", "spec_M", "hist_len"):
+                if f > 0 and not np.array_equal(ov.form_values(nm), ov.fp64(nm)):
+                    decisions_equal = False
+            if f == 0:
+                continue  # no denoised output without history
+            for nm in FP64_OUTPUTS:
+                if nm.startswith("denoised_"):
+                    a = got[nm.split("_")[1]].view(dt).reshape(n, 4)[:, :3].astype(np.float64)
+                else:
+                    a = ov.form_values(nm)
+                b = ov.fp64(nm)
+                m = np.isfinite(a).all(1) & np.isfinite(b).all(1)
+                den = np.linalg.norm(b[m])
+                errs[nm].append((float(np.linalg.norm(a[m] - b[m]) / den) if den > 0 else 0.0,
+                                 float(np.max(np.abs(a[m] - b[m]))) if m.any() else 0.0,
+                                 float(np.max(np.abs(b[m]))) if m.any() else 0.0, int((~m).sum())))
+        view.close()
+        ov.close()
+        table = {}
+        for nm, e in errs.items():
+            e = np.array(e)
+            table[nm] = {"rel_l2_mean": float(e[:, 0].mean()), "rel_l2_max": float(e[:, 0].max()),
+                         "max_abs_err": float(e[:, 1].max()), "max_abs_value": float(e[:, 2].max()),
+                         "nonfinite_pixels": int(e[:, 3].sum())}
+        res[form] = {"per_output": table, "decision_flips_per_frame": {"mean": float(np.mean(flips)),
+                                                                       "max": int(np.max(flips))},
+                     "decisions_replayed_exactly": decisions_equal, "gpu_frames_not_bitexact_vs_oracle": gpu_mismatch,
+                     "denoised_meets_1e-3": bool(max(table["denoised_diffuse"]["rel_l2_max"],
+                                                     table["denoised_specular"]["rel_l2_max"]) <= 1e-3)}
+    ctx.close()
+    return {"workload": "%dx%d, %d frames, plain 1080p knobs; binary64 replay of the float form's decisions" % (
+        W, H, args.fp64_frames), "f32": res["f32"], "f16": res["f16"]}
 
 
 def traced_leg(args, ws, dev):
@@ -1085,6 +1167,10 @@ def main():
     ap.add_argument("--no-post", action="store_true")
     ap.add_argument("--no-traced", action="store_true")
     ap.add_argument("--precision-frames", type=int, default=64)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--fp64-frames", type=int, default=32)
+    ap.add_argument("--fp64-width", type=int, default=960)
+    ap.add_argument("--fp64-height", type=int, default=540)
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 steps")

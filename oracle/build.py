@@ -1,8 +1,8 @@
 """ORACLE build recipe (test infrastructure only).
 
-Compiles the CPU restatement (oracle.cpp, binary32 without FMA contraction) and its
-binary64 denoiser (oracle64.cpp) into oracle/_build/libvlt_oracle.so with g++
-(OpenMP). The reference's own shaders, compiled as C++ against an HLSL vocabulary
+Compiles the CPU restatement (oracle.cpp, binary32 without FMA contraction), its
+binary64 denoiser (oracle64.cpp) and the binary64 replay of the float forms' whole
+back end (oracle64r.cpp) into oracle/_build/libvlt_oracle.so with g++ (OpenMP). The reference's own shaders, compiled as C++ against an HLSL vocabulary
 header, are built separately by oracle/ref_build.py into oracle/_ref/ (only where
 the reference tree is present); they pin this restatement.
 """
@@ -12,8 +12,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build", "libvlt_oracle.so")
-SRCS = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "oracle64.cpp")]
-DEPS = SRCS + [os.path.join(HERE, "omath.hpp"), os.path.join(os.path.dirname(HERE), "include", "vlt.h")]
+SRCS = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "oracle64.cpp"), os.path.join(HERE, "oracle64r.cpp")]
+DEPS = SRCS + [os.path.join(HERE, "omath.hpp"), os.path.join(HERE, "oracle64r.hpp"),
+               os.path.join(os.path.dirname(HERE), "include", "vlt.h")]
 FLAGS = ["-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
 
 

@@ -28,12 +28,14 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <string>
 #include <vector>
 
 #include "../include/vlt.h"
 #include "omath.hpp"
+#include "oracle64r.hpp"
 
 using namespace orc;
 
@@ -67,6 +69,41 @@ float3 cs_depth_to_position(const float* inv_vp, int x, int y, int w, int h, flo
   return F3(p.x / p.w, p.y / p.w, p.z / p.w);
 }
 
+// ---- decision tape
+// With a tape set (g_tape, TAPE_WORDS words per pixel), the float forms' passes record
+// every data-dependent decision of each pixel in evaluation order: branch outcomes
+// (TB) and the integers that pick texels or counts (TI). The binary64 restatement in
+// oracle64r.cpp replays them, so that it follows the float form's path and its
+// differences from the float form are precision alone. Without a tape both are
+// identities.
+constexpr int TAPE_WORDS = R64_TAPE_WORDS;
+uint16_t* g_tape = nullptr;
+std::atomic<bool> g_tape_overflow{false};
+thread_local uint16_t* t_tape = nullptr;
+thread_local uint16_t* t_tape_end = nullptr;
+inline void tape_at(size_t i) {
+  if (g_tape) {
+    t_tape = g_tape + i * TAPE_WORDS;
+    t_tape_end = t_tape + TAPE_WORDS;
+  } else {
+    t_tape = nullptr;
+  }
+}
+inline bool TB(bool b) {
+  if (t_tape) {
+    if (t_tape < t_tape_end) *t_tape++ = b ? 1u : 0u;
+    else g_tape_overflow = true;
+  }
+  return b;
+}
+inline int TI(int v) {
+  if (t_tape) {
+    if (t_tape < t_tape_end) *t_tape++ = (uint16_t)(int16_t)v;
+    else g_tape_overflow = true;
+  }
+  return v;
+}
+
 // SampleLevel(sampler_linear_clamp, uv, 0): exact binary32 bilinear (see omath.hpp).
 struct Bilinear {
   int x0, x1, y0, y1;
@@ -78,7 +115,7 @@ Bilinear bilinear(float2 uv, int w, int h) {
   Bilinear b;
   b.fx = sx - bx;
   b.fy = sy - by;
-  int ix = to_int(bx), iy = to_int(by);
+  int ix = TI(to_int(bx)), iy = TI(to_int(by));
   b.x0 = std::min(std::max(ix, 0), w - 1);
   b.x1 = std::min(std::max(ix + 1, 0), w - 1);
   b.y0 = std::min(std::max(iy, 0), h - 1);
@@ -149,6 +186,7 @@ void ao_gen(const vlt_frame_params& fp, int w, int h, const uint32_t* hpn, const
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t i = (size_t)y * w + x;
+      tape_at(i);
       float depth = depth_buf[i];
       if (has_no_geometry_via_depth(depth)) {
         ao_hist_store<F32>(out, i, F2(0.0f, 0.0f));
@@ -166,7 +204,7 @@ void ao_gen(const vlt_frame_params& fp, int w, int h, const uint32_t* hpn, const
       float2 src_uv = F2(((float)x + 0.5f) / (float)w, ((float)y + 0.5f) / (float)h);
       float2 history_uv = src_uv - motion_vector;
       float hx, ha;
-      bool is_in_last_view = history_uv.x == saturate(history_uv.x) && history_uv.y == saturate(history_uv.y);
+      bool is_in_last_view = TB(history_uv.x == saturate(history_uv.x) && history_uv.y == saturate(history_uv.y));
       if (is_in_last_view && has_prev_frame) {
         Bilinear b = bilinear(history_uv, w, h);  // taps clamped to the image
         float2 a = ao_hist<F32>(prev_ao, (size_t)b.y0 * w + b.x0), bb = ao_hist<F32>(prev_ao, (size_t)b.y0 * w + b.x1);
@@ -182,11 +220,11 @@ void ao_gen(const vlt_frame_params& fp, int w, int h, const uint32_t* hpn, const
         float3 position_ws = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
         float3 sample_offset = hit.pos - position_ws;
         float sample_distance = length(sample_offset);
-        float ao = sample_distance < radius_ws ? 0.0f : 1.0f;
+        float ao = TB(sample_distance < radius_ws) ? 0.0f : 1.0f;
         hx = lerp(ao, hx, ((32.0f - 1.0f) / 32.0f) * ha);
         ha = 1.0f;
       } else {
-        hx = ha > 0.0f ? hx : 1.0f;
+        hx = TB(ha > 0.0f) ? hx : 1.0f;
       }
       ao_hist_store<F32>(out, i, F2(hx, ha));
     }
@@ -200,6 +238,7 @@ void ao_filter(int w, int h, const float* depth_buf, const void* ao, void* out) 
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t i = (size_t)y * w + x;
+      tape_at(i);
       float depth = depth_buf[i];
       if (has_no_geometry_via_depth(depth)) {
         ao_filtered_store<F32>(out, i, 0.0f);
@@ -214,7 +253,7 @@ void ao_filter(int w, int h, const float* depth_buf, const void* ao, void* out) 
           uint32_t cy = std::min((uint32_t)y + (uint32_t)dy, (uint32_t)h);
           Tex<float> dt = {depth_buf, w, h};
           float sample_depth = dt((int)cx, (int)cy);
-          if (fabsf(depth - sample_depth) > 0.0005f) {
+          if (TB(fabsf(depth - sample_depth) > 0.0005f)) {
             row[dx + 1] = center_ao;
             continue;
           }
@@ -395,26 +434,27 @@ void diff_temporal_f32(const vlt_frame_params& fp, int w, int h, const vlt_param
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t i = (size_t)y * w + x;
+      tape_at(i);
       const float depth = depth_buf[i];
       float3 position_ws = cs_depth_to_position(fp.inv_view_proj, x, y, w, h, depth);
       float4 hpos_reproj = mul(fp.prev_view_proj, F4(position_ws.x, position_ws.y, position_ws.z, 1.0f));
       float3 ndc_reproj = F3(hpos_reproj.x / hpos_reproj.w - fp.jitter[2], hpos_reproj.y / hpos_reproj.w - fp.jitter[3],
                              hpos_reproj.z / hpos_reproj.w - 0.0f);
       float2 uv_reproj = F2(ndc_reproj.x * 0.5f + 0.5f, ndc_reproj.y * 0.5f + 0.5f);
-      bool in_view = fabsf(ndc_reproj.x) < 1.0f && fabsf(ndc_reproj.y) < 1.0f;
+      bool in_view = TB(fabsf(ndc_reproj.x) < 1.0f && fabsf(ndc_reproj.y) < 1.0f);
       bool sample_prev_frame = has_prev_frame && in_view;
       if (sample_prev_frame) {
         float reproj_depth = ndc_reproj.z;
         Bilinear b = bilinear(uv_reproj, w, h);
         float pd = blerp(prev_depth[(size_t)b.y0 * w + b.x0], prev_depth[(size_t)b.y0 * w + b.x1],
                          prev_depth[(size_t)b.y1 * w + b.x0], prev_depth[(size_t)b.y1 * w + b.x1], b.fx, b.fy);
-        if (fabsf(pd - reproj_depth) > 0.001f) sample_prev_frame = false;
+        if (TB(fabsf(pd - reproj_depth) > 0.001f)) sample_prev_frame = false;
       }
       uint32_t M = 0;
       float W = 0.0f;
       float3 hp = F3(0.0f), hn = empty_n, rad = F3(0.0f);
       if (sample_prev_frame) {
-        int px = (int)to_uint(uv_reproj.x * (float)w), py = (int)to_uint(uv_reproj.y * (float)h);
+        int px = TI((int)to_uint(uv_reproj.x * (float)w)), py = TI((int)to_uint(uv_reproj.y * (float)h));
         if (in_img(px, py, w, h)) {
           DiffF32 r = diff_load<FORM>(prev_rsv, npx, (size_t)py * w + px);
           M = r.M;
@@ -438,14 +478,14 @@ void diff_temporal_f32(const vlt_frame_params& fp, int w, int h, const vlt_param
         float new_w;
         if (P.use_input_pdf) {
           float pdf = new_pdf[i];
-          new_w = pdf > 0.0f ? new_target_pdf / pdf : 0.0f;
+          new_w = TB(pdf > 0.0f) ? new_target_pdf / pdf : 0.0f;
         } else {
           new_w = new_target_pdf * TWO_PI;
         }
         uint32_t rng_state = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
         float w_sum = prev_w + new_w;
         float chance = new_w / w_sum;
-        if (lcg_rand(rng_state) < chance) {
+        if (TB(lcg_rand(rng_state) < chance)) {
           HitPosNormal hit = HitPosNormal::decode(new_hpn[2 * i], new_hpn[2 * i + 1]);
           hp = hit.pos;
           hn = hit.normal;
@@ -453,7 +493,7 @@ void diff_temporal_f32(const vlt_frame_params& fp, int w, int h, const vlt_param
           reservoir_target_pdf = new_target_pdf;
         }
         M += 1;
-        W = reservoir_target_pdf > 0.0f ? w_sum / (reservoir_target_pdf * (float)M) : 0.0f;
+        W = TB(reservoir_target_pdf > 0.0f) ? w_sum / (reservoir_target_pdf * (float)M) : 0.0f;
       }
       diff_store<FORM>(out, npx, i, M, W, hp, hn, rad);
     }
@@ -510,6 +550,7 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t i = (size_t)y * w + x;
+      tape_at(i);
       float depth = depth_buf[i];
       if (has_no_geometry_via_depth(depth)) {
         if constexpr (F32) {
@@ -542,8 +583,8 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
         float sn, cs;
         sincos_own(theta * T + rand_angle, &sn, &cs);
         float ox = r * cs, oy = r * sn;
-        int nx = std::min(std::max(x + to_int(ox * radius), 0), w - 1);
-        int ny = std::min(std::max(y + to_int(oy * radius), 0), h - 1);
+        int nx = TI(std::min(std::max(x + to_int(ox * radius), 0), w - 1));
+        int ny = TI(std::min(std::max(y + to_int(oy * radius), 0), h - 1));
         float3 normal_n = load_gbuffer_normal(gbuf, nx, ny, w, h);
         float depth_n = depth_buf[(size_t)ny * w + nx];
         bool geometrical_diff = false;
@@ -551,7 +592,7 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
         float3 position_ws_n = cs_depth_to_position(fp.inv_view_proj, nx, ny, w, h, depth_n);
         float dist_to_plane = dot(position_ws_n - position_ws, gnormal);
         geometrical_diff |= fabsf(dist_to_plane) > 0.05f;
-        if (geometrical_diff) {
+        if (TB(geometrical_diff)) {
           radius = hmax(radius * 0.5f, MIN_RADIUS);
           continue;
         }
@@ -566,12 +607,12 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
         reuse_jacobian = hclamp(reuse_jacobian, 0.0f, 10.0f);
         reuse_jacobian = hclamp(reuse_jacobian, 0.0f, 1.0f);
         float target_pdf_neighbor = neighbor.target_pdf * reuse_jacobian;
-        if (target_pdf_neighbor <= 0.0f) continue;
+        if (TB(target_pdf_neighbor <= 0.0f)) continue;
         neighbor.M = std::min(neighbor.M, 255u);
         float w_sum_neighbor = neighbor.W * target_pdf_neighbor * (float)neighbor.M;
         w_sum += w_sum_neighbor;
         float chance = w_sum_neighbor / w_sum;
-        if (lcg_rand(rng_state) < chance) {
+        if (TB(lcg_rand(rng_state) < chance)) {
           reservoir.hit_normal = neighbor.hit_normal;
           reservoir.hit_pos = neighbor.hit_pos;
           reservoir.hit_radiance = neighbor.hit_radiance;
@@ -581,7 +622,7 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
       }
       {
         float target_pdf = reservoir.target_pdf;
-        if (target_pdf > 0.0f) reservoir.W = w_sum / (target_pdf * (float)reservoir.M);
+        if (TB(target_pdf > 0.0f)) reservoir.W = w_sum / (target_pdf * (float)reservoir.M);
       }
       if constexpr (FORM != 0) {
         diff_store<FORM>(out, npx, i, reservoir.M, reservoir.W, reservoir.hit_pos, reservoir.hit_normal,
@@ -642,8 +683,8 @@ Sampling calc_things(float3 view_pos, float3 position_ws, float3 normal, float p
   float LoH = saturate(dot(light_dir, H));
   float3 F = F_Schlick(LoH, specular_f0);
   float G2_over_G1 = smith_G2_over_G1_height_correlated_GGX(NoL, NoV, roughness);
-  if (NoL <= 0.0f) G2_over_G1 = 0.0f;
-  if (NoV <= 0.0f) G2_over_G1 = 0.0f;
+  if (TB(NoL <= 0.0f)) G2_over_G1 = 0.0f;
+  if (TB(NoV <= 0.0f)) G2_over_G1 = 0.0f;
   ret.brdf_NoL_over_source_pdf = F * G2_over_G1;
   return ret;
 }
@@ -731,6 +772,7 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t i = (size_t)y * w + x;
+      tape_at(i);
       float depth = depth_buf[i];
       if (has_no_geometry_via_depth(depth)) {
         SpecRec z;
@@ -749,12 +791,12 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
                              hpos_reproj.z / hpos_reproj.w - 0.0f);
       float2 uv_reproj = F2(ndc_reproj.x * 0.5f + 0.5f, ndc_reproj.y * 0.5f + 0.5f);
       bool sample_prev_frame =
-          uv_reproj.x == saturate(uv_reproj.x) && uv_reproj.y == saturate(uv_reproj.y) && has_prev_frame;
+          TB(uv_reproj.x == saturate(uv_reproj.x) && uv_reproj.y == saturate(uv_reproj.y) && has_prev_frame);
       if (sample_prev_frame) {
         Bilinear b = bilinear(uv_reproj, w, h);
         float pd = blerp(prev_depth[(size_t)b.y0 * w + b.x0], prev_depth[(size_t)b.y0 * w + b.x1],
                          prev_depth[(size_t)b.y1 * w + b.x0], prev_depth[(size_t)b.y1 * w + b.x1], b.fx, b.fy);
-        if (fabsf(pd - ndc_reproj.z) > 0.001f) sample_prev_frame = false;
+        if (TB(fabsf(pd - ndc_reproj.z) > 0.001f)) sample_prev_frame = false;
       }
       uint32_t M;
       float W;
@@ -763,7 +805,7 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       float reservoir_target_function;
       GBuffer prev_gbuffer;
       if (sample_prev_frame) {
-        int px = (int)to_uint(uv_reproj.x * (float)w), py = (int)to_uint(uv_reproj.y * (float)h);
+        int px = TI((int)to_uint(uv_reproj.x * (float)w)), py = TI((int)to_uint(uv_reproj.y * (float)h));
         SpecRec r = spec_load<F16>(prev_rsv, prev_hp, prev_rad, px, py, w, h);
         M = r.M;
         W = r.W;
@@ -785,7 +827,7 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       float3 new_sample_hit_radiance = load_r11g11b10(new_rad[i]);
       GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
       {
-        uint32_t M_max = to_uint((float)P.spec_m_cap * gbuffer.perceptual_roughness);
+        uint32_t M_max = (uint32_t)TI((int)to_uint((float)P.spec_m_cap * gbuffer.perceptual_roughness));
         M = std::min(M, M_max);
       }
       float3 view_pos = v3(fp.view_pos);
@@ -802,7 +844,7 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
         float prev_target_function_on_curr =
             luminance(new_sample_hit_radiance * prev_on_curr.brdf_NoL_over_source_pdf) * prev_on_curr.source_pdf;
         float curr_m = new_target_function / (new_target_function + prev_target_function_on_curr * (float)M);
-        if (new_target_function == 0.0f) curr_m = 0.0f;
+        if (TB(new_target_function == 0.0f)) curr_m = 0.0f;
         new_w = curr_m * new_w;
         Sampling curr_on_prev = calc_things(view_pos, position_ws, gbuffer.normal, gbuffer.perceptual_roughness, f0,
                                             reservoir_hit_pos);
@@ -810,14 +852,14 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
             luminance(reservoir_hit_radiance * curr_on_prev.brdf_NoL_over_source_pdf) * curr_on_prev.source_pdf;
         float m_num = reservoir_target_function * (float)M;
         float prev_m = m_num / (m_num + curr_target_function_on_prev);
-        if (m_num == 0.0f) prev_m = 0.0f;
+        if (TB(m_num == 0.0f)) prev_m = 0.0f;
         prev_w = prev_m * (curr_target_function_on_prev * W);
         reservoir_target_function = curr_target_function_on_prev;
       }
       uint32_t rng_state = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
       const float w_sum = prev_w + new_w;
       const float chance_prev = prev_w / w_sum;
-      const bool use_prev_sample = lcg_rand(rng_state) < chance_prev;
+      const bool use_prev_sample = TB(lcg_rand(rng_state) < chance_prev);
       if (!use_prev_sample) {
         reservoir_hit_pos = new_sample_hit_pos;
         reservoir_rad_bits = new_rad[i];
@@ -825,7 +867,7 @@ void spec_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
         reservoir_target_function = new_target_function;
       }
       M += 1;
-      if (reservoir_target_function > 0.0f) {
+      if (TB(reservoir_target_function > 0.0f)) {
         W = w_sum / (reservoir_target_function * (float)M);
         W = w_sum / reservoir_target_function;  // 1/M is in w_sum (MIS weights)
       } else {
@@ -875,6 +917,7 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t i = (size_t)y * w + x;
+      tape_at(i);
       float depth = depth_buf[i];
       if (has_no_geometry_via_depth(depth)) {
         store_light(i, F3(0.0f), 0.0f);
@@ -897,7 +940,8 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
       float3 view_pos = v3(fp.view_pos);
       float3 center_f0 = get_specular_f0(gbuffer.color, gbuffer.metallic);
       float reservoir_target_function = c0.tf;
-      const uint32_t num_iteration = to_uint(lerp(0.0f, (float)MAX_ITERATION, gbuffer.perceptual_roughness));
+      const uint32_t num_iteration =
+          (uint32_t)TI((int)to_uint(lerp(0.0f, (float)MAX_ITERATION, gbuffer.perceptual_roughness)));
       float radius = P.spec_spatial_radius_px > 0.0f ? P.spec_spatial_radius_px : (float)std::min(w, h) * 0.05f;
       uint32_t rng_state = lcg_init_with_seed((uint32_t)x, (uint32_t)y, frame_rand);
       for (uint32_t it = 0; it < num_iteration; it++) {
@@ -908,8 +952,8 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
         float sn, cs;
         sincos_own(theta, &sn, &cs);
         float ox = r * cs, oy = r * sn;
-        int nx = std::min(std::max(x + to_int(ox * radius), 0), w - 1);
-        int ny = std::min(std::max(y + to_int(oy * radius), 0), h - 1);
+        int nx = TI(std::min(std::max(x + to_int(ox * radius), 0), w - 1));
+        int ny = TI(std::min(std::max(y + to_int(oy * radius), 0), h - 1));
         if (nx == x && ny == y) continue;
         GBuffer gbuffer_n = load_gbuffer(gbuf, nx, ny, w, h);
         size_t j = (size_t)ny * w + nx;
@@ -919,7 +963,7 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
         float3 position_ws_n = cs_depth_to_position(fp.inv_view_proj, nx, ny, w, h, depth_n);
         float dist_to_plane = dot(position_ws_n - position_ws, gbuffer.normal);
         geometrical_diff |= fabsf(dist_to_plane) > 0.05f;
-        if (geometrical_diff) {
+        if (TB(geometrical_diff)) {
           radius = hmax(radius * 0.5f, 1.5f);
           continue;
         }
@@ -939,7 +983,7 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
               hit_radiance_n);
           float m_neighb = (neighb_tf_on_neighb * (float)M_n) /
                            (neighb_tf_on_neighb * (float)M_n + center_tf_on_neighb * (float)M);
-          if (neighb_tf_on_neighb * (float)M_n == 0.0f) m_neighb = 0.0f;
+          if (TB(neighb_tf_on_neighb * (float)M_n == 0.0f)) m_neighb = 0.0f;
           w_neighb = m_neighb * neighb_tf_on_neighb * W_n;
           float neighb_tf_on_center = eval_target_function(
               calc_things(view_pos, position_ws_n, gbuffer_n.normal, gbuffer_n.perceptual_roughness,
@@ -947,19 +991,19 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
               hit_radiance);
           float m_center = (center_tf_on_center * (float)M) /
                            (center_tf_on_center * (float)M + neighb_tf_on_center * (float)M_n);
-          if (center_tf_on_center * (float)M == 0.0f) m_center = 0.0f;
+          if (TB(center_tf_on_center * (float)M == 0.0f)) m_center = 0.0f;
           w_center = m_center * center_tf_on_center * W;
         }
         float w_sum = w_center + w_neighb;
         float chance = w_neighb / w_sum;
-        if (lcg_rand(rng_state) < chance) {
+        if (TB(lcg_rand(rng_state) < chance)) {
           hit_pos = hit_pos_n;
           hit_radiance = hit_radiance_n;
           rad_bits = rad_n_bits;
           reservoir_target_function = reservoir_target_function_n;
         }
         M += M_n;
-        if (reservoir_target_function > 0.0f)
+        if (TB(reservoir_target_function > 0.0f))
           W = w_sum / reservoir_target_function;
         else
           W = 0.0f;
@@ -991,8 +1035,8 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
         float lambda_pomc = smith_lambda_GGX_plus_one_mul_cos(NoV, roughness);
         float vndf = 0.25f * D / lambda_pomc;
         float G2_over_G1 = smith_G2_over_G1_height_correlated_GGX(NoL, NoV, roughness);
-        if (NoL <= 0.0f) G2_over_G1 = 0.0f;
-        if (NoV <= 0.0f) G2_over_G1 = 0.0f;
+        if (TB(NoL <= 0.0f)) G2_over_G1 = 0.0f;
+        if (TB(NoV <= 0.0f)) G2_over_G1 = 0.0f;
         float3 lt = hit_radiance * ((F * G2_over_G1) * (vndf * W));
         float3 specular_reflectance = hmax(ggx_brdf_integral_approx(NoV, roughness, specular_f0), 1.0f / 65536.0f);
         lt = lt / specular_reflectance;
@@ -1612,6 +1656,7 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t i = (size_t)y * w + x;
+      tape_at(i);
       float depth = depth_tex[i];
       if (has_no_geometry_via_depth(depth)) {
         IO::set_len(out_len, i, 0.0f);
@@ -1640,7 +1685,7 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
         float4 hr = mul(fp.prev_view_proj, F4(vp.x, vp.y, vp.z, 1.0f));
         float2 ndc_reproj = F2(hr.x / hr.w - fp.jitter[2], hr.y / hr.w - fp.jitter[3]);
         float2 vuv = F2((ndc_reproj.x + fp.jitter[0]) * 0.5f + 0.5f, (ndc_reproj.y + fp.jitter[1]) * 0.5f + 0.5f);
-        bool valid = vuv.x == saturate(vuv.x) && vuv.y == saturate(vuv.y) && has_history;
+        bool valid = TB(vuv.x == saturate(vuv.x) && vuv.y == saturate(vuv.y) && has_history);
         if (valid) {
           Bilinear b = bilinear(vuv, w, h);
           size_t a = (size_t)b.y0 * w + b.x0, bb = (size_t)b.y0 * w + b.x1, c = (size_t)b.y1 * w + b.x0,
@@ -1666,11 +1711,12 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       float3 dh = F3(0.0f), sh = F3(0.0f), dfh = F3(0.0f), sfh = F3(0.0f);
       float2 smh = F2(0.0f, 0.0f);
       float hl = 0.0f;
-      bool valid = history_uv.x == saturate(history_uv.x) && history_uv.y == saturate(history_uv.y) && has_history;
+      bool valid =
+          TB(history_uv.x == saturate(history_uv.x) && history_uv.y == saturate(history_uv.y) && has_history);
       if (valid) {
         float2 pcc = F2(history_uv.x * (float)w - 0.5f, history_uv.y * (float)h - 0.5f);
         float2 frac = F2(pcc.x - floorf(pcc.x), pcc.y - floorf(pcc.y));
-        int bx = to_int(pcc.x), by = to_int(pcc.y);
+        int bx = TI(to_int(pcc.x)), by = TI(to_int(pcc.y));
         float depth_tol = gbuffer.fwidth_z * 4.0f + 1e-4f;
         float normal_tol = gbuffer.fwidth_n * 16.0f + 1e-2f;
         float normal_tol_sq = normal_tol * normal_tol;
@@ -1685,7 +1731,7 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
             if (!in_img(px, py, w, h)) continue;
             size_t j = (size_t)py * w + px;
             float3 n_diff = load_gbuffer_normal(prev_gbuf, px, py, w, h) - gbuffer.normal;
-            if (!(fabsf(prev_depth[j] - reproj_depth) < depth_tol && dot(n_diff, n_diff) < normal_tol_sq)) continue;
+            if (!TB(fabsf(prev_depth[j] - reproj_depth) < depth_tol && dot(n_diff, n_diff) < normal_tol_sq)) continue;
             float wt = weights[oy][ox];
             wsum += wt;
             hs += wt * IO::len(len_hist, j);
@@ -1699,7 +1745,7 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
               sfs = fma3(wt, f.s, sfs);
             }
           }
-        valid = wsum > 0.00390625f;
+        valid = TB(wsum > 0.00390625f);
         if (valid) {
           float inv = 1.0f / wsum;
           dh = ds * inv;
@@ -1746,6 +1792,7 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       }
       IO::store(out, i, df, sf, smf);
       IO::set_len(out_len, i, hl);
+      TI(((const uint8_t*)out_len)[i]);  // the stored history length (a frame count)
       if (fast_history) IO::store(out_fast, i, dff, sff, F2(0.0f, 0.0f));
     }
 }
@@ -2776,6 +2823,17 @@ struct OView {
   // Float forms: run the a-trous with the reference's edge-stopping formulas
   // (dn32_atrous_refw) instead of the forms' own evaluation.
   bool atrous_reference_weights = false;
+  // Float forms: the binary64 replay of the same frames (oracle64r.cpp) and the
+  // decision tape its passes read, and the flips of the last frame.
+  R64* r64 = nullptr;
+  std::vector<uint16_t> tape;
+  uint64_t r64_flips = 0;
+  OView() = default;
+  OView(const OView&) = delete;
+  OView& operator=(const OView&) = delete;
+  ~OView() {
+    if (r64) r64_destroy(r64);
+  }
   std::vector<uint8_t> fdiff_prev, fao_prev, fao_filtered, fdiff_light, fspec_light, fhist_rec, fhist_len, ffast_prev,
       ffallback;
   // Final lighting (the view's colour buffer) and the temporal-AA history
@@ -2866,6 +2924,18 @@ void frame_trace(OView& v, const vlt_frame_inputs& in, float* rays_cache, float*
   v.trace_pending = true;
   v.trace_frame = in.frame_index;
 }
+
+// Runs a float-form pass with the decision tape recording when the binary64 replay is
+// on, then the replay pass on the same tape.
+#define WITH_TAPE(v, float_pass, replay_pass) \
+  do {                                        \
+    if ((v).r64) g_tape = (v).tape.data();    \
+    float_pass;                               \
+    g_tape = nullptr;                         \
+    if ((v).r64) {                            \
+      replay_pass;                            \
+    }                                         \
+  } while (0)
 
 void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* out) {
   const vlt_frame_params& fp = *in.params;
@@ -2973,35 +3043,48 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
   if (v.form != 0) {
     const bool f32 = v.form == 1;
     std::vector<uint8_t> ao_cur(v.fao_prev.size());
+    R64* r = v.r64;
+    const uint16_t* tp = v.tape.data();
     if (f32) {
-      ao_gen<true>(fp, w, h, diff_hpn, in.depth, v.fao_prev.data(), ao_cur.data(), has_new,
-                   has_prev ? 1u : 0u, P.ao_radius);
-      ao_filter<true>(w, h, in.depth, ao_cur.data(), v.fao_filtered.data());
+      WITH_TAPE(v, ao_gen<true>(fp, w, h, diff_hpn, in.depth, v.fao_prev.data(), ao_cur.data(), has_new,
+                                has_prev ? 1u : 0u, P.ao_radius),
+                r64_ao_gen(*r, fp, diff_hpn, in.depth, has_new, has_prev ? 1u : 0u, P.ao_radius, tp));
+      WITH_TAPE(v, ao_filter<true>(w, h, in.depth, ao_cur.data(), v.fao_filtered.data()),
+                r64_ao_filter(*r, in.depth, tp));
     } else {
-      ao_gen<false>(fp, w, h, diff_hpn, in.depth, v.fao_prev.data(), ao_cur.data(), has_new,
-                    has_prev ? 1u : 0u, P.ao_radius);
-      ao_filter<false>(w, h, in.depth, ao_cur.data(), v.fao_filtered.data());
+      WITH_TAPE(v, ao_gen<false>(fp, w, h, diff_hpn, in.depth, v.fao_prev.data(), ao_cur.data(), has_new,
+                                 has_prev ? 1u : 0u, P.ao_radius),
+                r64_ao_gen(*r, fp, diff_hpn, in.depth, has_new, has_prev ? 1u : 0u, P.ao_radius, tp));
+      WITH_TAPE(v, ao_filter<false>(w, h, in.depth, ao_cur.data(), v.fao_filtered.data()),
+                r64_ao_filter(*r, in.depth, tp));
     }
     v.fao_prev.swap(ao_cur);
     std::vector<uint8_t> temp(v.fdiff_prev.size()), sp(v.fdiff_prev.size());
     const uint32_t seed_dt = frame_rand.next();
     if (f32)
-      diff_temporal_f32<1>(fp, w, h, Pd, prev_depth, in.depth, diff_hpn, diff_rad, diff_pdf, v.fdiff_prev.data(),
-                           temp.data(), seed_dt, has_prev ? 1u : 0u, has_new);
+      WITH_TAPE(v, diff_temporal_f32<1>(fp, w, h, Pd, prev_depth, in.depth, diff_hpn, diff_rad, diff_pdf,
+                                        v.fdiff_prev.data(), temp.data(), seed_dt, has_prev ? 1u : 0u, has_new),
+                r64_diff_temporal(*r, fp, prev_depth, in.depth, diff_hpn, diff_rad, diff_pdf, seed_dt,
+                                  has_prev ? 1u : 0u, has_new, tp));
     else
-      diff_temporal_f32<2>(fp, w, h, Pd, prev_depth, in.depth, diff_hpn, diff_rad, diff_pdf, v.fdiff_prev.data(),
-                           temp.data(), seed_dt, has_prev ? 1u : 0u, has_new);
+      WITH_TAPE(v, diff_temporal_f32<2>(fp, w, h, Pd, prev_depth, in.depth, diff_hpn, diff_rad, diff_pdf,
+                                        v.fdiff_prev.data(), temp.data(), seed_dt, has_prev ? 1u : 0u, has_new),
+                r64_diff_temporal(*r, fp, prev_depth, in.depth, diff_hpn, diff_rad, diff_pdf, seed_dt,
+                                  has_prev ? 1u : 0u, has_new, tp));
     for (uint32_t k = 0; k < P.diff_spatial_passes; ++k) {
       bool last = k + 1 == P.diff_spatial_passes;
       const uint32_t seed = frame_rand.next();
       if (f32)
-        diff_spatial<1>(fp, w, h, P, in.gbuffer, in.depth, v.fao_filtered.data(), temp.data(), sp.data(),
-                        last ? v.fdiff_light.data() : nullptr, seed);
+        WITH_TAPE(v, diff_spatial<1>(fp, w, h, P, in.gbuffer, in.depth, v.fao_filtered.data(), temp.data(),
+                                     sp.data(), last ? v.fdiff_light.data() : nullptr, seed),
+                  r64_diff_spatial(*r, fp, in.gbuffer, in.depth, seed, last, tp));
       else
-        diff_spatial<2>(fp, w, h, P, in.gbuffer, in.depth, v.fao_filtered.data(), temp.data(), sp.data(),
-                        last ? v.fdiff_light.data() : nullptr, seed);
+        WITH_TAPE(v, diff_spatial<2>(fp, w, h, P, in.gbuffer, in.depth, v.fao_filtered.data(), temp.data(),
+                                     sp.data(), last ? v.fdiff_light.data() : nullptr, seed),
+                  r64_diff_spatial(*r, fp, in.gbuffer, in.depth, seed, last, tp));
       temp.swap(sp);
     }
+    if (r) r64_diff_commit(*r);
     v.fdiff_prev.swap(temp);
   } else {
     std::vector<uint32_t> ao_cur(n);
@@ -3060,8 +3143,10 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
   const size_t hpw = s16 ? 6 : 4;
   std::vector<uint32_t> srsv(s16 ? 0 : 2 * n), srad(s16 ? 0 : n);
   std::vector<float> shp(hpw * n);
+  const bool replay = v.r64 != nullptr && v.form != 0;
   {
     const uint32_t seed = frame_rand.next();
+    if (replay) g_tape = v.tape.data();
     if (s16)
       spec_temporal<true>(fp, w, h, P, prev_depth, prev_gbuf, in.depth, in.gbuffer, nullptr, v.spec_hp_prev.data(),
                           nullptr, in.spec_hit_pos, in.spec_hit_radiance, nullptr, shp.data(), nullptr, seed,
@@ -3070,6 +3155,12 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
       spec_temporal<false>(fp, w, h, P, prev_depth, prev_gbuf, in.depth, in.gbuffer, v.spec_rsv_prev.data(),
                            v.spec_hp_prev.data(), v.spec_rad_prev.data(), in.spec_hit_pos, in.spec_hit_radiance,
                            srsv.data(), shp.data(), srad.data(), seed, has_prev ? 1u : 0u);
+    g_tape = nullptr;
+    if (replay) {
+      r64_spec_temporal(*v.r64, fp, prev_depth, prev_gbuf, in.depth, in.gbuffer, in.spec_hit_pos,
+                        in.spec_hit_radiance, seed, has_prev ? 1u : 0u, v.tape.data());
+      r64_spec_commit(*v.r64);
+    }
   }
   {
     const uint32_t* a_rsv = srsv.data();
@@ -3084,6 +3175,7 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
       float* o_hp = use_b ? b_hp.data() : c_hp.data();
       uint32_t* o_rad = use_b ? b_rad.data() : c_rad.data();
       uint32_t seed = frame_rand.next();
+      if (replay) g_tape = v.tape.data();
       if (v.form == 1)
         spec_spatial<1>(fp, w, h, P, in.gbuffer, in.depth, a_rsv, a_hp, a_rad,
                         last ? (void*)v.fspec_light.data() : nullptr, nullptr, last ? nullptr : o_rsv,
@@ -3096,6 +3188,8 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
         spec_spatial<0>(fp, w, h, P, in.gbuffer, in.depth, a_rsv, a_hp, a_rad,
                         last ? (void*)v.spec_light.data() : nullptr, last ? v.ray_len.data() : nullptr,
                         last ? nullptr : o_rsv, last ? nullptr : o_hp, last ? nullptr : o_rad, seed);
+      g_tape = nullptr;
+      if (replay) r64_spec_spatial(*v.r64, fp, in.gbuffer, in.depth, seed, last, v.tape.data());
       a_rsv = o_rsv;
       a_hp = o_hp;
       a_rad = o_rad;
@@ -3118,6 +3212,7 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
     const size_t rb = f32 ? 32 : 16;  // bytes per record
     std::vector<uint8_t> trec(rb * n), tlen(v.fhist_len.size()), tfast(P.fast_history_clamp ? rb * n : rb);
     const uint32_t hh = v.denoiser_history ? 1u : 0u;
+    if (replay) g_tape = v.tape.data();
     if (f32)
       dn32_temporal<1>(fp, w, h, P, in.depth, in.gbuffer, v.fdiff_light.data(), v.fspec_light.data(), prev_depth,
                        prev_gbuf, v.fhist_rec.data(), v.fhist_len.data(), v.ffast_prev.data(), trec.data(),
@@ -3126,6 +3221,8 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
       dn32_temporal<2>(fp, w, h, P, in.depth, in.gbuffer, v.fdiff_light.data(), v.fspec_light.data(), prev_depth,
                        prev_gbuf, v.fhist_rec.data(), v.fhist_len.data(), v.ffast_prev.data(), trec.data(),
                        tlen.data(), tfast.data(), hh, P.fast_history_clamp);
+    g_tape = nullptr;
+    if (replay) r64_denoise(*v.r64, fp, in.depth, in.gbuffer, prev_depth, prev_gbuf, hh, v.tape.data());
     if (P.disocclusion_fix) {
       std::vector<uint8_t> frec(rb * n);
       if (f32) dn32_fix<1>(w, h, in.depth, in.gbuffer, tlen.data(), trec.data(), frec.data());
@@ -3256,6 +3353,7 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
   memcpy(v.prev_depth.data(), in.depth, 4 * n);
   memcpy(v.prev_gbuf.data(), in.gbuffer, 16 * n);
   v.frames += 1;
+  if (v.r64) v.r64_flips = r64_take_flips();
 }
 
 }  // namespace
@@ -3328,6 +3426,40 @@ void vlto_view_destroy(void* h) { delete (OView*)h; }
 
 // Float forms: 1 runs the a-trous with the reference's edge-stopping formulas.
 void vlto_view_set_atrous_reference_weights(void* h, int on) { ((OView*)h)->atrous_reference_weights = on != 0; }
+
+// Float forms without traced mode or fast-history clamp: from the next frame on,
+// every frame is also run by the binary64 replay (oracle64r.cpp) on the decisions the
+// float form takes. Returns 0, or -1 where the replay does not apply.
+int vlto_view_enable_fp64(void* h) {
+  OView& v = *(OView*)h;
+  if (v.form == 0 || v.P.trace || v.P.fast_history_clamp) return -1;
+  if (!v.r64) {
+    v.r64 = r64_create(v.w, v.h, v.P);
+    v.tape.assign((size_t)v.w * v.h * TAPE_WORDS, 0);
+  }
+  return 0;
+}
+// The binary64 replay's buffer `name` as doubles (diff_W, diff_M, spec_W, spec_M, ao,
+// raw_diffuse, raw_specular, ray_len, hist_color, hist_moments, hist_len, variance,
+// denoised_diffuse, denoised_specular); returns doubles per pixel (0: unknown or no
+// replay). `out` holds max doubles.
+uint32_t vlto_view_fp64_buffer(void* h, const char* name, double* out, size_t max) {
+  OView& v = *(OView*)h;
+  if (!v.r64) return 0;
+  std::vector<double> scratch;
+  size_t k = 0;
+  const double* p = r64_buffer(*v.r64, name, &k, scratch);
+  if (!p) return 0;
+  size_t n = (size_t)v.w * v.h * k;
+  if (out) memcpy(out, p, sizeof(double) * std::min(n, max));
+  return (uint32_t)k;
+}
+// Decisions of the last frame where the binary64 evaluation would have gone the
+// other way (the replay followed the float form's); -1 if a tape overflowed.
+int64_t vlto_view_fp64_flips(void* h) {
+  if (g_tape_overflow) return -1;
+  return (int64_t)((OView*)h)->r64_flips;
+}
 
 // Traced mode, phase one: rays into host arrays (cache: nq rays, diffuse and
 // spec-validate: W*H rays; any may be NULL); counts = {cache, diffuse, spec, diffuse

@@ -31,6 +31,9 @@ SIGS = {
                              C.c_void_p, C.c_void_p]),
     "vlto_view_destroy": (None, [P]),
     "vlto_view_set_atrous_reference_weights": (None, [P, C.c_int]),
+    "vlto_view_enable_fp64": (C.c_int, [P]),
+    "vlto_view_fp64_buffer": (U32, [P, C.c_char_p, P, C.c_size_t]),
+    "vlto_view_fp64_flips": (C.c_int64, [P]),
     "vlto_frame_run": (None, [P, C.POINTER(_ffi.FrameInputs), C.POINTER(_ffi.FrameOutputs)]),
     "vlto_view_buffer": (P, [P, C.c_char_p, C.POINTER(C.c_size_t)]),
     "vlto_ao_gen": (None, [FP, U32, U32, P, P, P, P, U32, U32, C.c_float]),
@@ -160,6 +163,72 @@ class OracleView:
         (svgf.inc.hlsl:60-82, separately rounded) instead of the forms' own
         base-2 / fused-multiply-add evaluation."""
         lib().vlto_view_set_atrous_reference_weights(self.handle, 1 if on else 0)
+
+    def enable_fp64(self):
+        """Float forms: from the next frame on, run the binary64 replay of the whole
+        back end beside every frame (the float form's decisions replayed)."""
+        rc = lib().vlto_view_enable_fp64(self.handle)
+        if rc != 0:
+            raise ValueError("the binary64 replay needs a float form without traced mode or fast-history clamp")
+
+    def fp64(self, name):
+        """The binary64 replay's buffer `name` as a float64 array (pixels, values)."""
+        n = self.width * self.height
+        k = int(lib().vlto_view_fp64_buffer(self.handle, name.encode(), None, 0))
+        if k == 0:
+            raise KeyError(name)
+        out = np.zeros(n * k, np.float64)
+        lib().vlto_view_fp64_buffer(self.handle, name.encode(), out.ctypes.data, out.size)
+        return out.reshape(n, k)
+
+    def fp64_flips(self):
+        """Decisions of the last frame on which binary64 evaluation would have gone the
+        other way (-1: a decision tape overflowed)."""
+        return int(lib().vlto_view_fp64_flips(self.handle))
+
+    def form_values(self, name):
+        """The float form's own value of a replay buffer `name` (same layout as fp64())."""
+        n = self.width * self.height
+        f16 = self.form == "f16"
+        half = lambda a: a.view(np.float16).astype(np.float64)  # noqa: E731
+        if name in ("diff_W", "diff_M"):
+            b = self.buffer("diff_reservoir")
+            if f16:
+                rec = b[: 16 * n].view(np.uint32).reshape(n, 4)
+                if name == "diff_W":
+                    return half((rec[:, 3] >> 16).astype(np.uint16)).reshape(n, 1)
+                return b[16 * n: 17 * n].astype(np.float64).reshape(n, 1)
+            rec = b.view(np.float32).reshape(n, 12)
+            if name == "diff_W":
+                return rec[:, 3:4].astype(np.float64)
+            return rec[:, 7].view(np.uint32).astype(np.float64).reshape(n, 1)
+        if name in ("spec_W", "spec_M"):
+            if f16:
+                rec = self.buffer("spec_record").view(np.uint32).reshape(n, 6)
+                if name == "spec_W":
+                    return rec[:, 3].view(np.float32).astype(np.float64).reshape(n, 1)
+                return (rec[:, 1] >> 16).astype(np.float64).reshape(n, 1)
+            rsv = self.buffer("spec_reservoir").view(np.uint32).reshape(n, 2)
+            if name == "spec_W":
+                return rsv[:, 1].view(np.float32).astype(np.float64).reshape(n, 1)
+            return rsv[:, 0].astype(np.float64).reshape(n, 1)
+        if name == "ao":
+            b = self.buffer("ao_filtered")
+            return (half(b) if f16 else b.view(np.float32).astype(np.float64)).reshape(n, 1)
+        if name in ("raw_diffuse", "raw_specular", "ray_len"):
+            b = self.buffer("raw_specular" if name == "ray_len" else name)
+            v = (half(b) if f16 else b.view(np.float32).astype(np.float64)).reshape(n, 4)
+            return v[:, 3:4] if name == "ray_len" else v[:, :3]
+        if name in ("hist_color", "hist_moments", "variance"):
+            b = self.buffer("fallback_record" if name == "variance" else "hist_record")
+            v = (half(b) if f16 else b.view(np.float32).astype(np.float64)).reshape(n, 8)
+            if name == "hist_color":
+                return np.concatenate([v[:, 0:3], v[:, 4:7]], 1)
+            aux = v[:, [3, 7]]
+            return aux * aux if f16 else aux
+        if name == "hist_len":
+            return self.buffer("hist_len").astype(np.float64).reshape(n, 1)
+        raise KeyError(name)
 
     def buffer(self, name, dtype=np.uint8):
         n = C.c_size_t(0)
