@@ -65,7 +65,9 @@ typedef enum vlt_status {
 typedef enum vlt_form {
   VLT_FORM_REF = 0, /* the reference's texture formats; bit-exact with the oracle */
   VLT_FORM_F32 = 1, /* every stored float in binary32 */
-  VLT_FORM_F16 = 2  /* packed 16-byte reservoirs, fp16 history/moments */
+  VLT_FORM_F16 = 2  /* 16-byte diffuse reservoirs (the candidate's encoded sample, W f32),
+                     * fp16 lighting, history and moments; the specular reservoir as in
+                     * the f32 form */
 } vlt_form;
 
 /* FrameParams of crates/violet-app/src/render_loop.rs:66-85 / frame_bindings.hlsl:6-26

@@ -90,14 +90,14 @@ inline void tape_at(size_t i) {
   }
 }
 inline bool TB(bool b) {
-  if (t_tape) {
+  if (g_tape && t_tape) {  // t_tape may be stale from an earlier taped pass
     if (t_tape < t_tape_end) *t_tape++ = b ? 1u : 0u;
     else g_tape_overflow = true;
   }
   return b;
 }
 inline int TI(int v) {
-  if (t_tape) {
+  if (g_tape && t_tape) {
     if (t_tape < t_tape_end) *t_tape++ = (uint16_t)(int16_t)v;
     else g_tape_overflow = true;
   }
@@ -357,10 +357,16 @@ void diff_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
 // F32 storage form of the diffuse reservoir: 12 floats per pixel,
 // {hit position, W}, {hit normal, asfloat(M)}, {radiance, 0}; the sample is kept
 // decoded (an empty HitPosNormal's normal decodes to (0, 0, -1)).
+// The encoded sample of an f16-form record: HitPosNormal words and R11G11B10
+// radiance, carried as they were written (a sample is never decoded and re-encoded).
+struct DBits {
+  uint32_t e0 = 0, e1 = 0, rb = 0;
+};
 struct DiffF32 {
   uint32_t M;
   float W;
   float3 pos, nrm, rad;
+  DBits bits;  // f16 form only
 };
 inline DiffF32 diff_f32_load(const float* r, size_t j) {
   const float* q = r + 12 * j;
@@ -380,8 +386,9 @@ inline void diff_f32_store(float* r, size_t j, uint32_t M, float W, float3 pos, 
 }
 
 // f16 storage form of the diffuse reservoir: the 16-byte records of all n pixels
-// {HitPosNormal, radiance f16 x3, W f16}, then one M byte per pixel (M <= 255);
-// stores saturate to the largest finite f16, NaN -> 0.
+// {HitPosNormal, R11G11B10 radiance, W f32}, then one M byte per pixel (M <= 255).
+// The sample's words are the candidate's own (the reference's formats, carried
+// unchanged), so a sample kept over frames and passes never drifts.
 inline uint32_t f16sat_d(float f) {
   if (isnan_(f)) return 0u;
   return f32tof16(hmin(hmax(f, -65504.0f), 65504.0f));
@@ -392,32 +399,31 @@ inline DiffF32 diff_f16_load(const uint8_t* base, size_t n, size_t j) {
   HitPosNormal hit = HitPosNormal::decode(r[0], r[1]);
   o.pos = hit.pos;
   o.nrm = hit.normal;
-  o.rad = F3(f16tof32(r[2] & 0xFFFFu), f16tof32(r[2] >> 16), f16tof32(r[3] & 0xFFFFu));
-  o.W = f16tof32(r[3] >> 16);
+  o.rad = load_r11g11b10(r[2]);
+  o.W = asfloat(r[3]);
   o.M = base[16 * n + j];
+  o.bits = DBits{r[0], r[1], r[2]};
   return o;
 }
-inline void diff_f16_store(uint8_t* base, size_t n, size_t j, uint32_t M, float W, float3 pos, float3 nrm,
-                           float3 rad) {
+inline void diff_f16_store(uint8_t* base, size_t n, size_t j, uint32_t M, float W, DBits b) {
   uint32_t* r = (uint32_t*)(base + 16 * j);
-  HitPosNormal hpn = {F3(f16tof32(f16sat_d(pos.x)), f16tof32(f16sat_d(pos.y)), f16tof32(f16sat_d(pos.z))), nrm};
-  uint32_t e[2];
-  hpn.encode(e);
-  r[0] = e[0];
-  r[1] = e[1];
-  r[2] = f16sat_d(rad.x) | (f16sat_d(rad.y) << 16);
-  r[3] = f16sat_d(rad.z) | (f16sat_d(W) << 16);
+  r[0] = b.e0;
+  r[1] = b.e1;
+  r[2] = b.rb;
+  r[3] = asuint(W);
   base[16 * n + j] = (uint8_t)std::min(M, 255u);
 }
-// Form-generic access (FORM 1 = f32 records, 2 = f16 records).
+// Form-generic access (FORM 1 = f32 records, 2 = f16 records; the f16 form stores
+// the sample's words `b`, the f32 form its decoded values).
 template <int FORM>
 inline DiffF32 diff_load(const void* p, size_t n, size_t j) {
   if constexpr (FORM == 2) return diff_f16_load((const uint8_t*)p, n, j);
   else return diff_f32_load((const float*)p, j);
 }
 template <int FORM>
-inline void diff_store(void* p, size_t n, size_t j, uint32_t M, float W, float3 pos, float3 nrm, float3 rad) {
-  if constexpr (FORM == 2) diff_f16_store((uint8_t*)p, n, j, M, W, pos, nrm, rad);
+inline void diff_store(void* p, size_t n, size_t j, uint32_t M, float W, float3 pos, float3 nrm, float3 rad,
+                       DBits b) {
+  if constexpr (FORM == 2) diff_f16_store((uint8_t*)p, n, j, M, W, b);
   else diff_f32_store((float*)p, j, M, W, pos, nrm, rad);
 }
 
@@ -453,6 +459,7 @@ void diff_temporal_f32(const vlt_frame_params& fp, int w, int h, const vlt_param
       uint32_t M = 0;
       float W = 0.0f;
       float3 hp = F3(0.0f), hn = empty_n, rad = F3(0.0f);
+      DBits bits;
       if (sample_prev_frame) {
         int px = TI((int)to_uint(uv_reproj.x * (float)w)), py = TI((int)to_uint(uv_reproj.y * (float)h));
         if (in_img(px, py, w, h)) {
@@ -462,11 +469,13 @@ void diff_temporal_f32(const vlt_frame_params& fp, int w, int h, const vlt_param
           hp = r.pos;
           hn = r.nrm;
           rad = r.rad;
+          bits = r.bits;
         }
         if (M == 0) {
           rad = F3(0.0f);
           hp = F3(0.0f);
           hn = empty_n;
+          bits = DBits{};
         }
         M = std::min(M, P.diff_m_cap);
       }
@@ -490,12 +499,13 @@ void diff_temporal_f32(const vlt_frame_params& fp, int w, int h, const vlt_param
           hp = hit.pos;
           hn = hit.normal;
           rad = new_hit_radiance;
+          bits = DBits{new_hpn[2 * i], new_hpn[2 * i + 1], new_rad[i]};
           reservoir_target_pdf = new_target_pdf;
         }
         M += 1;
         W = TB(reservoir_target_pdf > 0.0f) ? w_sum / (reservoir_target_pdf * (float)M) : 0.0f;
       }
-      diff_store<FORM>(out, npx, i, M, W, hp, hn, rad);
+      diff_store<FORM>(out, npx, i, M, W, hp, hn, rad, bits);
     }
 }
 
@@ -506,6 +516,7 @@ struct WorkingReservoir {
   float W;
   float3 hit_radiance, hit_pos, hit_normal;
   float target_pdf;
+  DBits bits;  // f16 form
 };
 template <int FORM>
 WorkingReservoir wr_load(const void* rsv, size_t n, size_t j, float3 pix_position_ws, float3 pix_normal) {
@@ -517,6 +528,7 @@ WorkingReservoir wr_load(const void* rsv, size_t n, size_t j, float3 pix_positio
     o.hit_pos = r.pos;
     o.hit_normal = r.nrm;
     o.hit_radiance = r.rad;
+    o.bits = r.bits;
   } else {
     const U4 r = ((const U4*)rsv)[j];
     reservoir_simple_decode_32b(r.x, &o.M, &o.W);
@@ -617,6 +629,7 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
           reservoir.hit_pos = neighbor.hit_pos;
           reservoir.hit_radiance = neighbor.hit_radiance;
           reservoir.target_pdf = neighbor.target_pdf;
+          reservoir.bits = neighbor.bits;
         }
         reservoir.M += neighbor.M;
       }
@@ -626,7 +639,7 @@ void diff_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
       }
       if constexpr (FORM != 0) {
         diff_store<FORM>(out, npx, i, reservoir.M, reservoir.W, reservoir.hit_pos, reservoir.hit_normal,
-                         reservoir.hit_radiance);
+                         reservoir.hit_radiance, reservoir.bits);
       } else {
         U4* o = (U4*)out + i;
         o->x = reservoir_simple_encode_32b(reservoir.M, reservoir.W);
@@ -893,7 +906,7 @@ void spec_spatial(const vlt_frame_params& fp, int w, int h, const vlt_params& P,
                   const float* depth_buf, const uint32_t* rsv, const float* hp_tex, const uint32_t* rad_tex,
                   void* lighting, uint16_t* ray_len_out, uint32_t* out_rsv, float* out_hp, uint32_t* out_rad,
                   uint32_t frame_rand) {
-  constexpr bool F16 = FORM == 2;
+  constexpr bool F16 = false;  // every form: the three specular planes
   auto store_light = [&](size_t i, float3 v, float ray_len) {
     if constexpr (FORM == 1) {
       if (lighting) {
@@ -2661,6 +2674,7 @@ struct ODiffVal {
   uint32_t M, word;
   float W;
   float3 pos, nrm, rad;
+  DBits bits;
 };
 template <int FORM>
 ODiffVal dval_get(const void* rsv, size_t n, size_t i) {
@@ -2675,7 +2689,7 @@ ODiffVal dval_get(const void* rsv, size_t n, size_t i) {
     r.rad = load_r11g11b10(q[3]);
   } else {
     DiffF32 d = diff_load<FORM>(rsv, n, i);
-    r.M = d.M, r.W = d.W, r.pos = d.pos, r.nrm = d.nrm, r.rad = d.rad;
+    r.M = d.M, r.W = d.W, r.pos = d.pos, r.nrm = d.nrm, r.rad = d.rad, r.bits = d.bits;
     r.word = 0u;
   }
   return r;
@@ -2692,7 +2706,11 @@ void dval_put(void* rsv, size_t n, size_t i, const ODiffVal& r, bool rescaled) {
     q[2] = e[1];
     q[3] = store_r11g11b10(r.rad);
   } else {
-    diff_store<FORM>(rsv, n, i, r.M, r.W, r.pos, r.nrm, r.rad);
+    // the validated sample is the re-traced hit, in the candidates' formats
+    HitPosNormal hpn = {r.pos, r.nrm};
+    uint32_t e[2];
+    hpn.encode(e);
+    diff_store<FORM>(rsv, n, i, r.M, r.W, r.pos, r.nrm, r.rad, DBits{e[0], e[1], store_r11g11b10(r.rad)});
   }
 }
 
@@ -2905,11 +2923,8 @@ void frame_trace(OView& v, const vlt_frame_inputs& in, float* rays_cache, float*
   v.trace_spec = 0;
   v.rays_spec.assign(n * 8, 0.0f);
   if (P.spec_validate && has_prev) {
-    if (v.form == 2)
-      rays_spec_validate<true>(fp, w, h, prev_depth, nullptr, v.spec_hp_prev.data(), nullptr, v.rays_spec.data());
-    else
-      rays_spec_validate<false>(fp, w, h, prev_depth, v.spec_rsv_prev.data(), v.spec_hp_prev.data(),
-                                v.spec_rad_prev.data(), v.rays_spec.data());
+    rays_spec_validate<false>(fp, w, h, prev_depth, v.spec_rsv_prev.data(), v.spec_hp_prev.data(),
+                              v.spec_rad_prev.data(), v.rays_spec.data());
     v.trace_spec = 1;
   }
   if (rays_cache) memcpy(rays_cache, v.rays_cache.data(), v.rays_cache.size() * 4);
@@ -3107,7 +3122,10 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
   (void)frame_rand.next();  // specular sample generation
   // f16 form: one 24-byte record per pixel in the `hp` buffers (6 words), no
   // separate M/W and radiance planes.
-  const bool s16 = v.form == 2;
+  // Every form keeps the specular reservoir in the three planes {M, W}, {hit, target
+  // function}, R11G11B10 radiance: binary16 hit positions cost the glossy lobes
+  // orders of magnitude of precision.
+  const bool s16 = false;
   if (traced && v.trace_spec) {
     uint32_t* staging = v.q_staging.data() + 8 * ((size_t)nq + n);
     const float* hits = (const float*)in.spec_validate_hits;
@@ -3181,9 +3199,9 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
                         last ? (void*)v.fspec_light.data() : nullptr, nullptr, last ? nullptr : o_rsv,
                         last ? nullptr : o_hp, last ? nullptr : o_rad, seed);
       else if (v.form == 2)
-        spec_spatial<2>(fp, w, h, P, in.gbuffer, in.depth, nullptr, a_hp, nullptr,
-                        last ? (void*)v.fspec_light.data() : nullptr, nullptr, nullptr, last ? nullptr : o_hp,
-                        nullptr, seed);
+        spec_spatial<2>(fp, w, h, P, in.gbuffer, in.depth, a_rsv, a_hp, a_rad,
+                        last ? (void*)v.fspec_light.data() : nullptr, nullptr, last ? nullptr : o_rsv,
+                        last ? nullptr : o_hp, last ? nullptr : o_rad, seed);
       else
         spec_spatial<0>(fp, w, h, P, in.gbuffer, in.depth, a_rsv, a_hp, a_rad,
                         last ? (void*)v.spec_light.data() : nullptr, last ? v.ray_len.data() : nullptr,
@@ -3402,7 +3420,6 @@ void* vlto_view_create_form(uint32_t w, uint32_t h, const vlt_params* p, int for
     v->fhist_len.assign(n, 0);
     v->ffast_prev.assign(p->fast_history_clamp ? by(32, 16) : (f32 ? 32 : 16), 0);
     v->ffallback.assign(by(32, 16), 0);
-    if (form == 2) v->spec_hp_prev.assign(6 * n, 0.0f);
   }
   const size_t cb = form == 1 ? 16 : (form == 2 ? 8 : 4);
   if (p->post >= 1) v->lit.assign(cb * n, 0);
@@ -3493,7 +3510,6 @@ void* vlto_view_buffer(void* h, const char* name, size_t* bytes) {
         {"hist_len", v.fhist_len.data(), v.fhist_len.size()},
         {"raw_diffuse", v.fdiff_light.data(), v.fdiff_light.size()},
         {"raw_specular", v.fspec_light.data(), v.fspec_light.size()},
-        {"spec_record", f32 ? nullptr : v.spec_hp_prev.data(), f32 ? 0 : 24 * n},
     };
     for (const E& e : t32)
       if (strcmp(e.nm, name) == 0) {
@@ -3501,8 +3517,6 @@ void* vlto_view_buffer(void* h, const char* name, size_t* bytes) {
         if (bytes) *bytes = e.sz;
         return e.p;
       }
-    if (!f32 && (!strcmp(name, "spec_hit_pos") || !strcmp(name, "spec_reservoir") || !strcmp(name, "spec_radiance")))
-      return nullptr;
     static const char* ref_only[] = {"diff_reservoir", "ao_history", "ao_filtered", "hist_color", "hist_moments",
                                      "hist_len", "variance", "spec_ray_len", "raw_diffuse", "raw_specular"};
     for (const char* r : ref_only)

@@ -196,18 +196,13 @@ class OracleView:
             if f16:
                 rec = b[: 16 * n].view(np.uint32).reshape(n, 4)
                 if name == "diff_W":
-                    return half((rec[:, 3] >> 16).astype(np.uint16)).reshape(n, 1)
+                    return rec[:, 3].view(np.float32).astype(np.float64).reshape(n, 1)
                 return b[16 * n: 17 * n].astype(np.float64).reshape(n, 1)
             rec = b.view(np.float32).reshape(n, 12)
             if name == "diff_W":
                 return rec[:, 3:4].astype(np.float64)
             return rec[:, 7].view(np.uint32).astype(np.float64).reshape(n, 1)
         if name in ("spec_W", "spec_M"):
-            if f16:
-                rec = self.buffer("spec_record").view(np.uint32).reshape(n, 6)
-                if name == "spec_W":
-                    return rec[:, 3].view(np.float32).astype(np.float64).reshape(n, 1)
-                return (rec[:, 1] >> 16).astype(np.float64).reshape(n, 1)
             rsv = self.buffer("spec_reservoir").view(np.uint32).reshape(n, 2)
             if name == "spec_W":
                 return rsv[:, 1].view(np.float32).astype(np.float64).reshape(n, 1)

@@ -15,7 +15,7 @@ from tests.helpers import d2h, upload
 
 pytestmark = pytest.mark.gpu
 
-BUFFERS = ["diff_reservoir", "spec_hit_pos", "spec_reservoir", "spec_radiance", "spec_record", "ao_history",
+BUFFERS = ["diff_reservoir", "spec_hit_pos", "spec_reservoir", "spec_radiance", "ao_history",
            "ao_filtered", "raw_diffuse", "raw_specular", "hist_len", "hg_storage", "hg_decay", "hg_query_count",
            "color", "taa_history"]
 REF_ONLY = ["hist_color", "hist_moments", "variance", "spec_ray_len"]

@@ -26,7 +26,8 @@ REL_TOL = 1e-5
 BUFFERS = {
     "f32": [("diff_reservoir", 12), ("spec_hit_pos", 4), ("spec_reservoir", 2), ("spec_radiance", 1),
             ("ao_history", 2), ("ao_filtered", 1), ("raw_diffuse", 4), ("raw_specular", 4)],
-    "f16": [("diff_reservoir", None), ("spec_record", 6), ("ao_history", 1), ("ao_filtered", None),
+    "f16": [("diff_reservoir", None), ("spec_hit_pos", 4), ("spec_reservoir", 2), ("spec_radiance", 1),
+            ("ao_history", 1), ("ao_filtered", None),
             ("raw_diffuse", 2), ("raw_specular", 2)],
 }
 DENOISE = {

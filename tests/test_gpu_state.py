@@ -12,7 +12,7 @@ from tests.helpers import d2h, upload
 pytestmark = pytest.mark.gpu
 
 OUT_PX = {"ref": 4, "f32": 16, "f16": 8}
-NAMES = ["diff_reservoir", "spec_hit_pos", "spec_reservoir", "spec_radiance", "spec_record", "ao_history",
+NAMES = ["diff_reservoir", "spec_hit_pos", "spec_reservoir", "spec_radiance", "ao_history",
          "ao_filtered", "raw_diffuse", "raw_specular", "hist_color", "hist_moments", "hist_record", "hist_len",
          "hg_storage", "hg_decay", "hg_queries", "hg_query_count", "taa_history", "color"]
 

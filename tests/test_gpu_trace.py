@@ -27,8 +27,8 @@ STATE = {
             "raw_diffuse", "raw_specular", "hist_color", "hist_moments", "hist_len"],
     "f32": ["diff_reservoir", "spec_hit_pos", "spec_reservoir", "spec_radiance", "ao_history", "ao_filtered",
             "raw_diffuse", "raw_specular", "hist_record", "hist_len"],
-    "f16": ["diff_reservoir", "spec_record", "ao_history", "ao_filtered", "raw_diffuse", "raw_specular",
-            "hist_record", "hist_len"],
+    "f16": ["diff_reservoir", "spec_hit_pos", "spec_reservoir", "spec_radiance", "ao_history", "ao_filtered",
+            "raw_diffuse", "raw_specular", "hist_record", "hist_len"],
 }
 
 

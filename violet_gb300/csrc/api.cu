@@ -208,16 +208,10 @@ size_t layout(vlt_view* v, char* base) {
   for (int k = 0; k < 2; ++k) b.ao[k] = take(by(4, 8, 4) * n);
   b.ao_filtered = take(by(2, 4, 2) * n);
   b.diff_light = take(by(4, 16, 8) * n);
-  for (int k = 0; k < 3; ++k) {
-    if (f16) {  // one 24-byte record per pixel
-      b.spec_hp[k] = (float*)take(24 * n);
-      b.spec_rsv[k] = nullptr;
-      b.spec_rad[k] = nullptr;
-    } else {
-      b.spec_hp[k] = (float*)take(16 * n);
-      b.spec_rsv[k] = (uint32_t*)take(8 * n);
-      b.spec_rad[k] = (uint32_t*)take(4 * n);
-    }
+  for (int k = 0; k < 3; ++k) {  // the specular reservoir's three planes, every form
+    b.spec_hp[k] = (float*)take(16 * n);
+    b.spec_rsv[k] = (uint32_t*)take(8 * n);
+    b.spec_rad[k] = (uint32_t*)take(4 * n);
   }
   b.spec_light = take(by(4, 16, 8) * n);
   for (int k = 0; k < 2; ++k) b.len[k] = take(n);  // R8_UNORM in every form
@@ -781,15 +775,14 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
   auto by = [&](size_t r, size_t a, size_t c) { return f32 ? a : (f16 ? c : r); };
   E tab[] = {
       {"diff_reservoir", b.diff_rsv[v->diff_prev], by(16, 48, 17) * n},
-      {"spec_hit_pos", f16 ? nullptr : b.spec_hp[v->spec_prev], 16 * n},
-      {"spec_reservoir", f16 ? nullptr : b.spec_rsv[v->spec_prev], 8 * n},
-      {"spec_radiance", f16 ? nullptr : b.spec_rad[v->spec_prev], 4 * n},
+      {"spec_hit_pos", b.spec_hp[v->spec_prev], 16 * n},
+      {"spec_reservoir", b.spec_rsv[v->spec_prev], 8 * n},
+      {"spec_radiance", b.spec_rad[v->spec_prev], 4 * n},
       // last frame's specular reservoir as this frame's passes left it (validated in
       // traced mode); the spatial passes do not touch its slot
-      {"spec_prev_hit_pos", f16 || !v->frames ? nullptr : b.spec_hp[(v->spec_prev + 2) % 3], 16 * n},
-      {"spec_prev_reservoir", f16 || !v->frames ? nullptr : b.spec_rsv[(v->spec_prev + 2) % 3], 8 * n},
-      {"spec_prev_radiance", f16 || !v->frames ? nullptr : b.spec_rad[(v->spec_prev + 2) % 3], 4 * n},
-      {"spec_record", f16 ? b.spec_hp[v->spec_prev] : nullptr, 24 * n},
+      {"spec_prev_hit_pos", !v->frames ? nullptr : b.spec_hp[(v->spec_prev + 2) % 3], 16 * n},
+      {"spec_prev_reservoir", !v->frames ? nullptr : b.spec_rsv[(v->spec_prev + 2) % 3], 8 * n},
+      {"spec_prev_radiance", !v->frames ? nullptr : b.spec_rad[(v->spec_prev + 2) % 3], 4 * n},
       {"ao_history", b.ao[v->ao_prev], by(4, 8, 4) * n},
       {"ao_filtered", b.ao_filtered, by(2, 4, 2) * n},
       {"hist_color", ref ? b.color[0] : nullptr, 8 * n},

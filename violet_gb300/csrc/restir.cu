@@ -185,8 +185,9 @@ struct DiffStore<FORM_F32> {
 };
 
 // f16-form diffuse reservoir: 16 bytes {HitPosNormal (hit position f16 x3, octahedral
-// 16-bit normal), radiance f16 x3, W f16} plus M in a separate byte plane (M <= 255).
-// Stores saturate (f32tof16_sat).
+// 16-bit normal), R11G11B10 radiance, W f32} plus M in a separate byte plane
+// (M <= 255). The sample's three words are the candidate's own, carried unchanged (a
+// sample is never decoded and re-encoded, so it does not drift over frames and passes).
 struct DiffF16Ptr {
   uint4* __restrict__ main;
   uint8_t* __restrict__ m;
@@ -196,22 +197,19 @@ struct DiffF16CPtr {
   const uint8_t* __restrict__ m;
 };
 
-__device__ __forceinline__ void diff_f16_store(DiffF16Ptr p, size_t i, uint32_t M, float W, f3 pos, f3 nrm, f3 rad) {
-  uint32_t e[2];
-  hpn_encode(mk3(q16(pos.x), q16(pos.y), q16(pos.z)), nrm, e);
-  p.main[i] = make_uint4(e[0], e[1], f32tof16_sat(rad.x) | (f32tof16_sat(rad.y) << 16),
-                         f32tof16_sat(rad.z) | (f32tof16_sat(W) << 16));
+__device__ __forceinline__ void diff_f16_store(DiffF16Ptr p, size_t i, uint32_t M, float W, uint3 bits) {
+  p.main[i] = make_uint4(bits.x, bits.y, bits.z, as_uint(W));
   p.m[i] = (uint8_t)(M < 255u ? M : 255u);
 }
-// Record at (x, y); out of range reads the empty record.
 __device__ __forceinline__ void diff_f16_load(DiffF16CPtr p, size_t i, uint32_t* M, float* W, f3* pos, f3* nrm,
-                                              f3* rad) {
+                                              f3* rad, uint3* bits) {
   uint4 r = p.main[i];
   *M = p.m[i];
   *pos = hpn_pos(r.x, r.y);
   *nrm = hpn_normal(r.y);
-  *rad = mk3(f16tof32(r.z & 0xFFFFu), f16tof32(r.z >> 16), f16tof32(r.w & 0xFFFFu));
-  *W = f16tof32(r.w >> 16);
+  *rad = unpack_r11g11b10(r.z);
+  *W = as_float(r.w);
+  *bits = make_uint3(r.x, r.y, r.z);
 }
 
 template <>
@@ -225,19 +223,21 @@ struct DiffStore<FORM_F16> {
   static __device__ __forceinline__ Light zero_light() { return make_uint2(0u, 0u); }
 };
 
-// Loads / stores of the decoded diffuse reservoir (f32 and f16 forms).
+// Loads / stores of the diffuse reservoir (f32 and f16 forms): the decoded sample,
+// and in the f16 form also its encoded words (`bits`: HitPosNormal, R11G11B10).
 __device__ __forceinline__ void diff_load(const DiffF32* p, size_t i, uint32_t* M, float* W, f3* pos, f3* nrm,
-                                          f3* rad) {
+                                          f3* rad, uint3* bits) {
   DiffF32 r = p[i];
   *M = as_uint(r.b.w);
   *W = r.a.w;
   *pos = mk3(r.a.x, r.a.y, r.a.z);
   *nrm = mk3(r.b.x, r.b.y, r.b.z);
   *rad = mk3(r.c.x, r.c.y, r.c.z);
+  *bits = make_uint3(0u, 0u, 0u);
 }
 __device__ __forceinline__ void diff_load(DiffF16CPtr p, size_t i, uint32_t* M, float* W, f3* pos, f3* nrm,
-                                          f3* rad) {
-  diff_f16_load(p, i, M, W, pos, nrm, rad);
+                                          f3* rad, uint3* bits) {
+  diff_f16_load(p, i, M, W, pos, nrm, rad, bits);
 }
 
 __device__ __forceinline__ DiffF32 diff_f32(uint32_t M, float W, f3 pos, f3 nrm, f3 rad) {
@@ -247,11 +247,12 @@ __device__ __forceinline__ DiffF32 diff_f32(uint32_t M, float W, f3 pos, f3 nrm,
   r.c = make_float4(rad.x, rad.y, rad.z, 0.0f);
   return r;
 }
-__device__ __forceinline__ void diff_store(DiffF32* p, size_t i, uint32_t M, float W, f3 pos, f3 nrm, f3 rad) {
+__device__ __forceinline__ void diff_store(DiffF32* p, size_t i, uint32_t M, float W, f3 pos, f3 nrm, f3 rad,
+                                           uint3) {
   p[i] = diff_f32(M, W, pos, nrm, rad);
 }
-__device__ __forceinline__ void diff_store(DiffF16Ptr p, size_t i, uint32_t M, float W, f3 pos, f3 nrm, f3 rad) {
-  diff_f16_store(p, i, M, W, pos, nrm, rad);
+__device__ __forceinline__ void diff_store(DiffF16Ptr p, size_t i, uint32_t M, float W, f3, f3, f3, uint3 bits) {
+  diff_f16_store(p, i, M, W, bits);
 }
 
 // ind_diff_temporal_resample.hlsl:49-200 in the f32 storage form: the sample is kept
@@ -276,10 +277,11 @@ struct DiffTemporalF32F {
   uint32_t M = 0;
   float W = 0.0f;
   f3 hp = mk3(0.0f), hn = empty_n, rad = mk3(0.0f);
+  uint3 bits = make_uint3(0u, 0u, 0u);
   if (sample_prev) {
     int px = (int)f2u_rz(uv.x * (float)w), py = (int)f2u_rz(uv.y * (float)h);
     if (inb(px, py, w, h)) {
-      diff_load(prev_rsv, (size_t)py * w + px, &M, &W, &hp, &hn, &rad);
+      diff_load(prev_rsv, (size_t)py * w + px, &M, &W, &hp, &hn, &rad, &bits);
     } else {
       hn = empty_n;
     }
@@ -287,6 +289,7 @@ struct DiffTemporalF32F {
       rad = mk3(0.0f);
       hp = mk3(0.0f);
       hn = empty_n;
+      bits = make_uint3(0u, 0u, 0u);
     }
     M = M < kn.m_cap ? M : kn.m_cap;
   }
@@ -310,12 +313,13 @@ struct DiffTemporalF32F {
       hp = hpn_pos(e.x, e.y);
       hn = hpn_normal(e.y);
       rad = nrad;
+      bits = make_uint3(e.x, e.y, new_rad[i]);
       tp = ntp;
     }
     M += 1;
     W = tp > 0.0f ? w_sum / (tp * (float)M) : 0.0f;
   }
-  diff_store(out, i, M, W, hp, hn, rad);
+  diff_store(out, i, M, W, hp, hn, rad, bits);
 }
 };
 
@@ -388,6 +392,7 @@ struct DiffSample {
   float W;
   f3 pos, nrm, rad;
   float tp;
+  uint3 bits;  // f16 form: the sample's encoded words
 };
 
 
@@ -410,7 +415,7 @@ __device__ __forceinline__ DiffSample load_diff(const uint4* p, size_t i, f3 pix
 template <class CPtr>
 __device__ __forceinline__ DiffSample load_diff(CPtr p, size_t i, f3 pix_pos, f3 pix_n) {
   DiffSample s;
-  diff_load(p, i, &s.M, &s.W, &s.pos, &s.nrm, &s.rad);
+  diff_load(p, i, &s.M, &s.W, &s.pos, &s.nrm, &s.rad, &s.bits);
   float nol = saturate(dot3(pix_n, normalize3(s.pos - pix_pos)));
   s.tp = nol * luminance(s.rad);
   return s;
@@ -426,7 +431,7 @@ __device__ __forceinline__ void store_diff(uint4* out, size_t i, const DiffSampl
 }
 template <class Ptr>
 __device__ __forceinline__ void store_diff(Ptr out, size_t i, const DiffSample& r) {
-  diff_store(out, i, r.M, r.W, r.pos, r.nrm, r.rad);
+  diff_store(out, i, r.M, r.W, r.pos, r.nrm, r.rad, r.bits);
 }
 __device__ __forceinline__ void store_empty_diff(uint4* out, size_t i) { out[i] = make_uint4(0u, 0u, 0u, 0u); }
 __device__ __forceinline__ void store_empty_diff(DiffF32* out, size_t i) {
@@ -517,6 +522,7 @@ struct DiffSpatialF {
       r.pos = nb.pos;
       r.rad = nb.rad;
       r.tp = nb.tp;
+      r.bits = nb.bits;
     }
     r.M += nb.M;
   }
@@ -602,22 +608,12 @@ struct SpecPlanes {
   float4* __restrict__ hp;
   uint32_t* __restrict__ rad;
 };
-// f16 form: one 24-byte record {hit f16 x3 | M u16}, {target function f32, W f32},
-// {radiance f16 x3}. The target function and W stay binary32: VNDF pdfs of smooth
-// surfaces exceed the f16 range.
-struct SpecF16 {
-  uint2 a, b, c;
-};
-
+// Every storage form keeps the specular reservoir in these three planes (binary16 hit
+// positions would cost the glossy lobes orders of magnitude of precision).
 template <int FORM>
 struct SpecStore {
   using CPtr = SpecPlanesC;
   using Ptr = SpecPlanes;
-};
-template <>
-struct SpecStore<FORM_F16> {
-  using CPtr = const SpecF16*;
-  using Ptr = SpecF16*;
 };
 
 // Record at (x, y); out of range reads the all-zero record (robust load).
@@ -633,36 +629,11 @@ __device__ __forceinline__ SpecSample spec_ld(SpecPlanesC p, int x, int y, int w
   s.rad = unpack_r11g11b10(s.rad_bits);
   return s;
 }
-__device__ __forceinline__ SpecSample spec_ld(const SpecF16* p, int x, int y, int w, int h) {
-  SpecF16 r;
-  if (inb(x, y, w, h)) {
-    r = p[(size_t)y * w + x];
-  } else {
-    r.a = r.b = r.c = make_uint2(0u, 0u);
-  }
-  SpecSample s;
-  s.hit = mk3(f16tof32(r.a.x & 0xFFFFu), f16tof32(r.a.x >> 16), f16tof32(r.a.y & 0xFFFFu));
-  s.M = r.a.y >> 16;
-  s.tf = as_float(r.b.x);
-  s.W = as_float(r.b.y);
-  s.rad = mk3(f16tof32(r.c.x & 0xFFFFu), f16tof32(r.c.x >> 16), f16tof32(r.c.y & 0xFFFFu));
-  s.rad_bits = 0u;
-  return s;
-}
 __device__ __forceinline__ bool spec_has(SpecPlanes p) { return p.rsv != nullptr; }
-__device__ __forceinline__ bool spec_has(SpecF16* p) { return p != nullptr; }
 __device__ __forceinline__ void spec_st(SpecPlanes p, size_t i, const SpecSample& s) {
   p.rsv[i] = make_uint2(s.M, as_uint(s.W));
   p.hp[i] = make_float4(s.hit.x, s.hit.y, s.hit.z, s.tf);
   p.rad[i] = s.rad_bits;
-}
-__device__ __forceinline__ void spec_st(SpecF16* p, size_t i, const SpecSample& s) {
-  SpecF16 r;
-  r.a = make_uint2(f32tof16_sat(s.hit.x) | (f32tof16_sat(s.hit.y) << 16),
-                   f32tof16_sat(s.hit.z) | ((s.M < 65535u ? s.M : 65535u) << 16));
-  r.b = make_uint2(as_uint(s.tf), as_uint(s.W));
-  r.c = make_uint2(f32tof16_sat(s.rad.x) | (f32tof16_sat(s.rad.y) << 16), f32tof16_sat(s.rad.z));
-  p[i] = r;
 }
 
 // ------------------------------------------------------ specular temporal
@@ -995,7 +966,8 @@ __device__ __forceinline__ DiffVal dval_load(const uint4* p, size_t i) {
 template <class CPtr>
 __device__ __forceinline__ DiffVal dval_load(CPtr p, size_t i) {
   DiffVal r;
-  diff_load(p, i, &r.M, &r.W, &r.pos, &r.nrm, &r.rad);
+  uint3 bits;
+  diff_load(p, i, &r.M, &r.W, &r.pos, &r.nrm, &r.rad, &bits);
   r.word = 0u;
   return r;
 }
@@ -1004,9 +976,13 @@ __device__ __forceinline__ void dval_store(uint4* p, size_t i, const DiffVal& r,
   hpn_encode(r.pos, r.nrm, e);
   p[i] = make_uint4(rescaled ? rsv_encode_32b(r.M, r.W) : r.word, e[0], e[1], pack_r11g11b10(r.rad));
 }
+// The validated sample is the re-traced hit, stored in the candidates' formats in the
+// f16 form (its encoded words).
 template <class Ptr>
 __device__ __forceinline__ void dval_store(Ptr p, size_t i, const DiffVal& r, bool) {
-  diff_store(p, i, r.M, r.W, r.pos, r.nrm, r.rad);
+  uint32_t e[2];
+  hpn_encode(r.pos, r.nrm, e);
+  diff_store(p, i, r.M, r.W, r.pos, r.nrm, r.rad, make_uint3(e[0], e[1], pack_r11g11b10(r.rad)));
 }
 
 // ind_diff_sample_validate.hlsl:30-49: re-trace last frame's sample from last
@@ -1231,22 +1207,13 @@ void launch_spec_temporal(const Exec& ex, int form, const vlt_frame_params& fp, 
   SpecPlanes pout = {(uint2*)out_rsv, (float4*)out_hp, out_rad};
   if (ga.nd) {
     GeoSurface g = surf_geo(ga, w, h), pg = surf_geo(prev_ga, w, h);
-    if (form == FORM_F16)
-      launch2d<SpecTemporalF<GeoSurface, FORM_F16>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, g, pg, prev_depth,
-                                                    (const SpecF16*)prev_hp, (const float4*)new_hp, new_rad,
-                                                    (SpecF16*)out_hp, frame_rand, has_prev);
-    else
-      launch2d<SpecTemporalF<GeoSurface, FORM_REF>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, g, pg, prev_depth,
-                                                    pin, (const float4*)new_hp, new_rad, pout, frame_rand, has_prev);
+    (void)form;  // the same reservoir planes in every form
+    launch2d<SpecTemporalF<GeoSurface, FORM_REF>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, g, pg, prev_depth,
+                                                  pin, (const float4*)new_hp, new_rad, pout, frame_rand, has_prev);
   } else {
     GeoRaw g = raw_geo(ga, w, h), pg = raw_geo(prev_ga, w, h);
-    if (form == FORM_F16)
-      launch2d<SpecTemporalF<GeoRaw, FORM_F16>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, g, pg, prev_depth,
-                                                (const SpecF16*)prev_hp, (const float4*)new_hp, new_rad,
-                                                (SpecF16*)out_hp, frame_rand, has_prev);
-    else
-      launch2d<SpecTemporalF<GeoRaw, FORM_REF>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, g, pg, prev_depth, pin,
-                                                (const float4*)new_hp, new_rad, pout, frame_rand, has_prev);
+    launch2d<SpecTemporalF<GeoRaw, FORM_REF>>(ex, "spec_temporal", w, h, fp, w, h, m_cap, g, pg, prev_depth, pin,
+                                              (const float4*)new_hp, new_rad, pout, frame_rand, has_prev);
   }
 }
 
@@ -1261,9 +1228,9 @@ void launch_spec_spatial(const Exec& ex, int form, const vlt_frame_params& fp, i
                                                                (float4*)lighting, (uint16_t*)nullptr, pout,
                                                                frame_rand)));
   else if (form == FORM_F16)
-    VLT_GEO_DISPATCH(ga, (launch2d<SpecSpatialF<Geo, FORM_F16>>(ex, "spec_spatial", w, h, fp, w, h, kn, geo,
-                                                               (const SpecF16*)hp, (uint2*)lighting,
-                                                               (uint16_t*)nullptr, (SpecF16*)out_hp, frame_rand)));
+    VLT_GEO_DISPATCH(ga, (launch2d<SpecSpatialF<Geo, FORM_F16>>(ex, "spec_spatial", w, h, fp, w, h, kn, geo, pin,
+                                                               (uint2*)lighting, (uint16_t*)nullptr, pout,
+                                                               frame_rand)));
   else
     VLT_GEO_DISPATCH(ga, (launch2d<SpecSpatialF<Geo, FORM_REF>>(ex, "spec_spatial", w, h, fp, w, h, kn, geo, pin,
                                                                (uint32_t*)lighting, ray_len, pout, frame_rand)));
@@ -1302,26 +1269,18 @@ void launch_diff_validate_apply(const Exec& ex, int form, const vlt_frame_params
 void launch_spec_validate_rays(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h,
                                const float* prev_depth, const uint32_t* rsv, const float* hp, const uint32_t* rad,
                                void* rays) {
-  if (form == FORM_F16) {
-    launch2d<SpecValidateRayF<FORM_F16>>(ex, "ray_spec_validate", w, h, fp, w, h, prev_depth, (const SpecF16*)hp,
-                                         (float4*)rays);
-  } else {
-    SpecPlanesC p = {(const uint2*)rsv, (const float4*)hp, rad};
-    launch2d<SpecValidateRayF<FORM_REF>>(ex, "ray_spec_validate", w, h, fp, w, h, prev_depth, p, (float4*)rays);
-  }
+  (void)form;  // the same reservoir planes in every form
+  SpecPlanesC p = {(const uint2*)rsv, (const float4*)hp, rad};
+  launch2d<SpecValidateRayF<FORM_REF>>(ex, "ray_spec_validate", w, h, fp, w, h, prev_depth, p, (float4*)rays);
 }
 
 void launch_spec_validate_apply(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h,
                                 const float* prev_depth, uint32_t* rsv, float* hp, uint32_t* rad, const void* rays,
                                 const void* hits, const ScreenCache& sc, const WorldCache& wc, uint32_t* staging) {
-  if (form == FORM_F16) {
-    launch2d<SpecValidateApplyF<FORM_F16>>(ex, "spec_validate", w, h, fp, w, h, prev_depth, (SpecF16*)hp,
-                                           (const float4*)rays, (const float4*)hits, sc, wc, staging);
-  } else {
-    SpecPlanes p = {(uint2*)rsv, (float4*)hp, rad};
-    launch2d<SpecValidateApplyF<FORM_REF>>(ex, "spec_validate", w, h, fp, w, h, prev_depth, p, (const float4*)rays,
-                                           (const float4*)hits, sc, wc, staging);
-  }
+  (void)form;  // the same reservoir planes in every form
+  SpecPlanes p = {(uint2*)rsv, (float4*)hp, rad};
+  launch2d<SpecValidateApplyF<FORM_REF>>(ex, "spec_validate", w, h, fp, w, h, prev_depth, p, (const float4*)rays,
+                                         (const float4*)hits, sc, wc, staging);
 }
 
 }  // namespace vlt

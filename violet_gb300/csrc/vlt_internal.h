@@ -60,8 +60,7 @@ void launch_diff_temporal(const Exec& ex, int form, const vlt_frame_params& fp, 
 void launch_diff_spatial(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, const DiffKnobs& kn,
                          const GeoArgs& ga, const void* ao, const void* in, void* out, void* lighting,
                          uint32_t frame_rand);
-// Specular reservoirs: reference and f32 forms pass the three planes (rsv, hp, rad);
-// the f16 form passes its 24-byte records as `hp` (rsv and rad unused). f16-form
+// Specular reservoirs: every form passes the three planes (rsv, hp, rad). f16-form
 // diffuse buffers hold the 16-byte records of all pixels followed by the M bytes.
 void launch_spec_temporal(const Exec& ex, int form, const vlt_frame_params& fp, int w, int h, uint32_t m_cap,
                           const GeoArgs& ga, const GeoArgs& prev_ga, const float* prev_depth,
