@@ -2846,6 +2846,7 @@ struct OView {
   R64* r64 = nullptr;
   std::vector<uint16_t> tape;
   uint64_t r64_flips = 0;
+  uint64_t r64_flips_pass[R64_FLIP_PASSES] = {};
   OView() = default;
   OView(const OView&) = delete;
   OView& operator=(const OView&) = delete;
@@ -3371,7 +3372,10 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
   memcpy(v.prev_depth.data(), in.depth, 4 * n);
   memcpy(v.prev_gbuf.data(), in.gbuffer, 16 * n);
   v.frames += 1;
-  if (v.r64) v.r64_flips = r64_take_flips();
+  if (v.r64) {
+    v.r64_flips = r64_take_flips();
+    r64_take_flips_by_pass(v.r64_flips_pass);
+  }
 }
 
 }  // namespace
@@ -3476,6 +3480,13 @@ uint32_t vlto_view_fp64_buffer(void* h, const char* name, double* out, size_t ma
 int64_t vlto_view_fp64_flips(void* h) {
   if (g_tape_overflow) return -1;
   return (int64_t)((OView*)h)->r64_flips;
+}
+// The same per pass (R64_FLIP_PASSES counts: AO generation, AO filter, diffuse
+// temporal, diffuse spatial, specular temporal, specular spatial, denoiser).
+uint32_t vlto_view_fp64_flips_by_pass(void* h, uint64_t* out) {
+  const OView& v = *(OView*)h;
+  for (int k = 0; k < R64_FLIP_PASSES; ++k) out[k] = v.r64_flips_pass[k];
+  return R64_FLIP_PASSES;
 }
 
 // Traced mode, phase one: rays into host arrays (cache: nq rays, diffuse and

@@ -84,6 +84,12 @@ inline int RI(int mine) {
   if (r != mine) ++t_flips;
   return r;
 }
+// Quotient of a division the float form guards with a test of its denominator (or
+// of the numerator of a weight x / (x + y)): the replay takes the float form's
+// branch, and where its own binary64 denominator is exactly zero there (the float
+// form's was not, a rounding difference) the quotient is the guarded value 0 rather
+// than an infinity or NaN that would spread through the following frames.
+inline double qdiv(double a, double b) { return b != 0.0 ? a / b : 0.0; }
 inline int to_int_d(double x) {
   if (x != x) return 0;
   if (x >= 2147483647.0) return 2147483647;
@@ -212,9 +218,21 @@ struct Rec {
   d2 aux;
 };
 
-void flush_flips() {
-  g_flips += t_flips;
-  t_flips = 0;
+// Decision flips per replayed pass (the index passed to flush_flips).
+std::atomic<uint64_t> g_flips_pass[R64_FLIP_PASSES];
+
+// Adds every thread's flips to the pass's count: a parallel region of the same team
+// that ran the pass's loop, so that each worker thread empties its own counter.
+void flush_flips(int pass) {
+#pragma omp parallel
+  {
+    const uint64_t f = t_flips;
+    t_flips = 0;
+    if (f) {
+      g_flips += f;
+      g_flips_pass[pass] += f;
+    }
+  }
 }
 
 }  // namespace
@@ -299,7 +317,7 @@ void r64_ao_gen(R64& R, const vlt_frame_params& fp, const uint32_t* hpn, const f
       out[i] = d2{hx, ha};
     }
   }
-  flush_flips();
+  flush_flips(0);
   R.ao_prev.swap(out);
 }
 
@@ -339,7 +357,7 @@ void r64_ao_filter(R64& R, const float* depth, const uint16_t* tape) {
       R.ao_filtered[i] = lerpd(m, lo, 0.5);
     }
   }
-  flush_flips();
+  flush_flips(1);
 }
 
 // ind_diff_temporal_resample.hlsl:49-200 (float forms: the sample kept decoded).
@@ -402,12 +420,12 @@ void r64_diff_temporal(R64& R, const vlt_frame_params& fp, const float* prev_dep
           tp = new_tp;
         }
         r.M += 1;
-        r.W = RB(tp > 0.0) ? w_sum / (tp * (double)r.M) : 0.0;
+        r.W = RB(tp > 0.0) ? qdiv(w_sum, tp * (double)r.M) : 0.0;
       }
       R.diff_tmp[i] = r;
     }
   }
-  flush_flips();
+  flush_flips(2);
 }
 
 // ind_diff_spatial_resample.hlsl:94-337 on diff_tmp (the temporal or the previous
@@ -481,7 +499,7 @@ void r64_diff_spatial(R64& R, const vlt_frame_params& fp, const uint32_t* gbuf, 
         }
         res.M += nb.M;
       }
-      if (RB(res_tp > 0.0)) res.W = w_sum / (res_tp * (double)res.M);
+      if (RB(res_tp > 0.0)) res.W = qdiv(w_sum, res_tp * (double)res.M);
       out[i] = res;
       if (last) {
         double NoL = satd(dot(g.normal, norm3(res.pos - p)));
@@ -489,7 +507,7 @@ void r64_diff_spatial(R64& R, const vlt_frame_params& fp, const uint32_t* gbuf, 
       }
     }
   }
-  flush_flips();
+  flush_flips(3);
   R.diff_tmp.swap(out);
 }
 
@@ -543,13 +561,13 @@ void r64_spec_temporal(R64& R, const vlt_frame_params& fp, const float* prev_dep
       if (r.M > 0) {
         Sampling pc = calc_things(widep(fp.prev_view_pos), p, pg.normal, pg.rough, spec_f0(pg), nhit);
         double ptc = lum(nrad * pc.brdf_NoL_over_pdf) * pc.source_pdf;
-        double curr_m = new_tf / (new_tf + ptc * (double)r.M);
+        double curr_m = qdiv(new_tf, new_tf + ptc * (double)r.M);
         if (RB(new_tf == 0.0)) curr_m = 0.0;
         new_w = curr_m * new_w;
         Sampling cp = calc_things(vp, p, g.normal, g.rough, f0, r.hit);
         double ctp = lum(r.rad * cp.brdf_NoL_over_pdf) * cp.source_pdf;
         double m_num = r.tf * (double)r.M;
-        double prev_m = m_num / (m_num + ctp);
+        double prev_m = qdiv(m_num, m_num + ctp);
         if (RB(m_num == 0.0)) prev_m = 0.0;
         prev_w = prev_m * (ctp * r.W);
         r.tf = ctp;
@@ -562,11 +580,11 @@ void r64_spec_temporal(R64& R, const vlt_frame_params& fp, const float* prev_dep
         r.tf = new_tf;
       }
       r.M += 1;
-      r.W = RB(r.tf > 0.0) ? w_sum / r.tf : 0.0;
+      r.W = RB(r.tf > 0.0) ? qdiv(w_sum, r.tf) : 0.0;
       R.spec_tmp[i] = r;
     }
   }
-  flush_flips();
+  flush_flips(4);
 }
 
 // ind_spec_spatial_resample.hlsl:169-448 on spec_tmp; the last pass writes the
@@ -616,11 +634,11 @@ void r64_spec_spatial(R64& R, const vlt_frame_params& fp, const uint32_t* gbuf, 
         }
         const SpecR nb = R.spec_tmp[(size_t)ny * w + nx];
         double ctn = target_fn(calc_things(vp, p, g.normal, g.rough, f0, nb.hit), nb.rad);
-        double m_n = (nb.tf * (double)nb.M) / (nb.tf * (double)nb.M + ctn * (double)c.M);
+        double m_n = qdiv(nb.tf * (double)nb.M, nb.tf * (double)nb.M + ctn * (double)c.M);
         if (RB(nb.tf * (double)nb.M == 0.0)) m_n = 0.0;
         double w_n = m_n * nb.tf * nb.W;
         double ntc = target_fn(calc_things(vp, pn, gn.normal, gn.rough, spec_f0(gn), c.hit), c.rad);
-        double m_c = (c.tf * (double)c.M) / (c.tf * (double)c.M + ntc * (double)nb.M);
+        double m_c = qdiv(c.tf * (double)c.M, c.tf * (double)c.M + ntc * (double)nb.M);
         if (RB(c.tf * (double)c.M == 0.0)) m_c = 0.0;
         double w_c = m_c * c.tf * c.W;
         double w_sum = w_c + w_n;
@@ -630,7 +648,7 @@ void r64_spec_spatial(R64& R, const vlt_frame_params& fp, const uint32_t* gbuf, 
           c.tf = nb.tf;
         }
         c.M += nb.M;
-        c.W = RB(c.tf > 0.0) ? w_sum / c.tf : 0.0;
+        c.W = RB(c.tf > 0.0) ? qdiv(w_sum, c.tf) : 0.0;
       }
       out[i] = c;
       if (last) {
@@ -649,7 +667,7 @@ void r64_spec_spatial(R64& R, const vlt_frame_params& fp, const uint32_t* gbuf, 
       }
     }
   }
-  flush_flips();
+  flush_flips(5);
   R.spec_tmp.swap(out);
 }
 
@@ -800,7 +818,7 @@ void r64_denoise(R64& R, const vlt_frame_params& fp, const float* depth, const u
       tlen[i] = len_byte;
     }
   }
-  flush_flips();
+  flush_flips(6);
   // disocclusion fix
   if (P.disocclusion_fix) {
     std::vector<Rec> frec(n);
@@ -929,6 +947,9 @@ void r64_denoise(R64& R, const vlt_frame_params& fp, const float* depth, const u
 }
 
 uint64_t r64_take_flips() { return g_flips.exchange(0); }
+void r64_take_flips_by_pass(uint64_t* out) {
+  for (int k = 0; k < R64_FLIP_PASSES; ++k) out[k] = g_flips_pass[k].exchange(0);
+}
 
 // Binary64 buffers for comparison, as doubles: name -> (pointer, doubles per pixel).
 const double* r64_buffer(R64& R, const char* name, size_t* per_pixel, std::vector<double>& scratch) {

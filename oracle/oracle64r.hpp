@@ -32,4 +32,8 @@ void r64_spec_spatial(R64& R, const vlt_frame_params& fp, const uint32_t* gbuf, 
 void r64_denoise(R64& R, const vlt_frame_params& fp, const float* depth, const uint32_t* gbuf,
                  const float* prev_depth, const uint32_t* prev_gbuf, uint32_t has_history, const uint16_t* tape);
 uint64_t r64_take_flips();
+// Flips of the last frame per pass: AO generation, AO filter, diffuse temporal,
+// diffuse spatial, specular temporal, specular spatial, denoiser.
+#define R64_FLIP_PASSES 7
+void r64_take_flips_by_pass(uint64_t* out);
 const double* r64_buffer(R64& R, const char* name, size_t* per_pixel, std::vector<double>& scratch);

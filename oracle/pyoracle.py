@@ -34,6 +34,7 @@ SIGS = {
     "vlto_view_enable_fp64": (C.c_int, [P]),
     "vlto_view_fp64_buffer": (U32, [P, C.c_char_p, P, C.c_size_t]),
     "vlto_view_fp64_flips": (C.c_int64, [P]),
+    "vlto_view_fp64_flips_by_pass": (C.c_uint32, [P, P]),
     "vlto_frame_run": (None, [P, C.POINTER(_ffi.FrameInputs), C.POINTER(_ffi.FrameOutputs)]),
     "vlto_view_buffer": (P, [P, C.c_char_p, C.POINTER(C.c_size_t)]),
     "vlto_ao_gen": (None, [FP, U32, U32, P, P, P, P, U32, U32, C.c_float]),
@@ -185,6 +186,15 @@ class OracleView:
         """Decisions of the last frame on which binary64 evaluation would have gone the
         other way (-1: a decision tape overflowed)."""
         return int(lib().vlto_view_fp64_flips(self.handle))
+
+    FLIP_PASSES = ("ao_gen", "ao_filter", "diff_temporal", "diff_spatial", "spec_temporal", "spec_spatial",
+                   "denoise")
+
+    def fp64_flips_by_pass(self):
+        """The last frame's flips per replayed pass, as {pass: count}."""
+        out = np.zeros(len(self.FLIP_PASSES), np.uint64)
+        lib().vlto_view_fp64_flips_by_pass(self.handle, out.ctypes.data)
+        return {k: int(v) for k, v in zip(self.FLIP_PASSES, out)}
 
     def form_values(self, name):
         """The float form's own value of a replay buffer `name` (same layout as fp64())."""
