@@ -1619,18 +1619,21 @@ struct Dio<1> {
 };
 template <>
 struct Dio<2> {
+  // aux: a variance around the record's colour (centered moments), stored as its
+  // signed square root.
   static Rec32 load(const void* p, size_t j) {
     const uint16_t* q = (const uint16_t*)p + 8 * j;
     float ax = f16tof32(q[3]), ay = f16tof32(q[7]);
     return Rec32{F3(f16tof32(q[0]), f16tof32(q[1]), f16tof32(q[2])), F3(f16tof32(q[4]), f16tof32(q[5]), f16tof32(q[6])),
-                 F2(ax * ax, ay * ay)};
+                 F2(ax * fabsf(ax), ay * fabsf(ay))};
   }
+  static float sroot(float v) { return copysignf(sqrtf(fabsf(v)), v); }
   static void store(void* p, size_t j, float3 d, float3 s, float2 aux) {
     uint16_t* q = (uint16_t*)p + 8 * j;
     q[0] = (uint16_t)f16sat(d.x), q[1] = (uint16_t)f16sat(d.y), q[2] = (uint16_t)f16sat(d.z);
-    q[3] = (uint16_t)f16sat(sqrtf(hmax(aux.x, 0.0f)));
+    q[3] = (uint16_t)f16sat(sroot(aux.x));
     q[4] = (uint16_t)f16sat(s.x), q[5] = (uint16_t)f16sat(s.y), q[6] = (uint16_t)f16sat(s.z);
-    q[7] = (uint16_t)f16sat(sqrtf(hmax(aux.y, 0.0f)));
+    q[7] = (uint16_t)f16sat(sroot(aux.y));
   }
   static void copy(void* o, const void* in, size_t j) { memcpy((char*)o + 16 * j, (const char*)in + 16 * j, 16); }
   static float len(const void* p, size_t j) { return load_unorm8(((const uint8_t*)p)[j]); }
@@ -1663,6 +1666,7 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
                    const uint32_t* prev_gbuf, const void* hist, const void* len_hist, const void* fast_hist,
                    void* out, void* out_len, void* out_fast, uint32_t has_history, uint32_t fast_history) {
   using IO = Dio<FORM>;
+  constexpr bool CEN = FORM == 2;  // centered moments (FP16 form)
   const float BLEND_FACTOR_DIFF = 1.0f / P.history_max_frames;
   const float BLEND_FACTOR_FAST = 1.0f / 3.0f;
   ROWS_PARALLEL
@@ -1723,6 +1727,7 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       float2 history_uv = screen_uv - motion_vector;
       float3 dh = F3(0.0f), sh = F3(0.0f), dfh = F3(0.0f), sfh = F3(0.0f);
       float2 smh = F2(0.0f, 0.0f);
+      float2 kshift = F2(0.0f, 0.0f);
       float hl = 0.0f;
       bool valid =
           TB(history_uv.x == saturate(history_uv.x) && history_uv.y == saturate(history_uv.y) && has_history);
@@ -1746,12 +1751,19 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
             float3 n_diff = load_gbuffer_normal(prev_gbuf, px, py, w, h) - gbuffer.normal;
             if (!TB(fabsf(prev_depth[j] - reproj_depth) < depth_tol && dot(n_diff, n_diff) < normal_tol_sq)) continue;
             float wt = weights[oy][ox];
+            Rec32 rr = IO::load(hist, j);
+            if (CEN) {
+              const float2 l = F2(lum_fma(rr.d), lum_fma(rr.s));
+              if (wsum == 0.0f) kshift = l;
+              const float2 e = F2(l.x - kshift.x, l.y - kshift.y);
+              ms = F2(fma_(wt, fma_(e.x, e.x, rr.aux.x), ms.x), fma_(wt, fma_(e.y, e.y, rr.aux.y), ms.y));
+            } else {
+              ms = F2(fma_(wt, rr.aux.x, ms.x), fma_(wt, rr.aux.y, ms.y));
+            }
             wsum += wt;
             hs += wt * IO::len(len_hist, j);
-            Rec32 rr = IO::load(hist, j);
             ds = fma3(wt, rr.d, ds);
             ss = fma3(wt, rr.s, ss);
-            ms = F2(fma_(wt, rr.aux.x, ms.x), fma_(wt, rr.aux.y, ms.y));
             if (fast_history) {
               Rec32 f = IO::load(fast_hist, j);
               dfs = fma3(wt, f.d, dfs);
@@ -1772,9 +1784,16 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       if (!valid) {
         dh = sh = dfh = sfh = F3(0.0f);
         smh = F2(0.0f, 0.0f);
+        kshift = F2(0.0f, 0.0f);
         hl = 0.0f;
       }
       hl += HISTORY_LEN_UNIT;
+      float2 lh = F2(0.0f, 0.0f);
+      if (CEN) {  // the history's variance around its own colour
+        lh = F2(lum_fma(dh), lum_fma(sh));
+        const float2 eh = F2(lh.x - kshift.x, lh.y - kshift.y);
+        smh = F2(fma_(-eh.x, eh.x, smh.x), fma_(-eh.y, eh.y, smh.y));
+      }
       const float4 dl = IO::light(diff_src, i), sl = IO::light(spec_src, i);
       float3 dsrc = F3(dl.x, dl.y, dl.z);
       float3 ssrc = F3(sl.x, sl.y, sl.z);
@@ -1791,17 +1810,25 @@ void dn32_temporal(const vlt_frame_params& fp, int w, int h, const vlt_params& P
       float3 dff = lerp(dfh, dsrc, alpha_fast.x);
       float3 sff = lerp(sfh, ssrc, alpha_fast.y);
       float3 sf;
+      float lum_dual = 0.0f;
       {
         float3 dev = hmax(sqrt3(abs3(m2 - m1 * m1)), 1e-19f);
         auto dsr_weight = [&](float3 c) { return exp2_own(-10.0f * luminance(abs3(c - m1) / dev)); };
         float wv = dsr_weight(vsh), wh = dsr_weight(sh);
         float3 dual = (wv * vsh + wh * sh) / hmax(wv + wh, 1e-37f);
+        if (CEN) lum_dual = lum_fma(dual);
         sf = lerp(dual, ssrc, alpha.y);
         if (fast_history) {
           float wv2 = dsr_weight(vsfh), wh2 = dsr_weight(sfh);
           float3 d2 = (wv2 * vsfh + wh2 * sfh) / hmax(wv2 + wh2, 1e-37f);
           sff = lerp(d2, ssrc, alpha_fast.y);
         }
+      }
+      if (CEN) {
+        const float ed = lsrc.x - lh.x, es = lsrc.y - lum_dual;
+        const float hm = (lh.y - lum_dual) * (lh.y + lum_dual);
+        smf = F2((1.0f - alpha.x) * fma_(alpha.x * ed, ed, smh.x),
+                 (1.0f - alpha.y) * fma_(alpha.y * es, es, smh.y + hm));
       }
       IO::store(out, i, df, sf, smf);
       IO::set_len(out_len, i, hl);
@@ -1830,6 +1857,11 @@ void dn32_fix(int w, int h, const float* depth_tex, const uint32_t* gbuf, const 
         EdgeStop32 es = EdgeStop32::create(depth_tex[i], gbuffer.fwidth_z, 5.0f, gbuffer.normal, 5);
         float2 ws = F2(0.0f, 0.0f), ms = F2(0.0f, 0.0f);
         float3 dsum = F3(0.0f), ssum = F3(0.0f);
+        float2 kshift = F2(0.0f, 0.0f);  // centered moments: the centre record's luminance
+        if (FORM == 2) {
+          const Rec32 rc = IO::load(in, i);
+          kshift = F2(lum_fma(rc.d), lum_fma(rc.s));
+        }
         const int stride = to_int((14.0f * HISTORY_LEN_UNIT) / hl);
         for (int oy = -2; oy <= 2; oy++)
           for (int ox = -2; ox <= 2; ox++) {
@@ -1843,9 +1875,20 @@ void dn32_fix(int w, int h, const float* depth_tex, const uint32_t* gbuf, const 
             ws += wt;
             dsum = fma3(wt.x, r.d, dsum);
             ssum = fma3(wt.y, r.s, ssum);
-            ms = F2(fma_(wt.x, r.aux.x, ms.x), fma_(wt.y, r.aux.y, ms.y));
+            if (FORM == 2) {
+              const float2 e = F2(lum_fma(r.d) - kshift.x, lum_fma(r.s) - kshift.y);
+              ms = F2(fma_(wt.x, fma_(e.x, e.x, r.aux.x), ms.x), fma_(wt.y, fma_(e.y, e.y, r.aux.y), ms.y));
+            } else {
+              ms = F2(fma_(wt.x, r.aux.x, ms.x), fma_(wt.y, r.aux.y, ms.y));
+            }
           }
-        IO::store(out, i, dsum * (1.0f / ws.x), ssum * (1.0f / ws.y), F2(ms.x / ws.x, ms.y / ws.y));
+        const float3 dfix = dsum * (1.0f / ws.x), sfix = ssum * (1.0f / ws.y);
+        float2 mfix = F2(ms.x / ws.x, ms.y / ws.y);
+        if (FORM == 2) {
+          const float2 e = F2(lum_fma(dfix) - kshift.x, lum_fma(sfix) - kshift.y);
+          mfix = F2(fma_(-e.x, e.x, mfix.x), fma_(-e.y, e.y, mfix.y));
+        }
+        IO::store(out, i, dfix, sfix, mfix);
       } else {
         IO::copy(out, in, i);
       }
@@ -1880,7 +1923,13 @@ void dn32_fast_clamp(int w, int h, const void* fast, void* rec) {
       Rec32 c = IO::load(rec, i);
       float3 d = hclamp(rgb_to_yCoCg(c.d), dm1 - ddev, dm1 + ddev);
       float3 s = hclamp(rgb_to_yCoCg(c.s), sm1 - sdev, sm1 + sdev);
-      IO::store(rec, i, yCoCg_to_rgb(d), yCoCg_to_rgb(s), c.aux);
+      const float3 dn = yCoCg_to_rgb(d), sn = yCoCg_to_rgb(s);
+      float2 aux = c.aux;
+      if (FORM == 2) {  // centered moments: the variance follows the clamped colour
+        const float l0x = lum_fma(c.d), l0y = lum_fma(c.s), l1x = lum_fma(dn), l1y = lum_fma(sn);
+        aux = F2(fma_(l0x - l1x, l0x + l1x, aux.x), fma_(l0y - l1y, l0y + l1y, aux.y));
+      }
+      IO::store(rec, i, dn, sn, aux);
     }
 }
 
@@ -1902,12 +1951,17 @@ void dn32_fallback(int w, int h, const float* depth_tex, const uint32_t* gbuf, c
       hl = qmax;
       float3 dd, sd;
       float2 md;
+      float2 kshift = F2(0.0f, 0.0f);  // centered moments: the shift of the blend
       if (hl < 4.0f * HISTORY_LEN_UNIT) {
         GBuffer gbuffer = load_gbuffer(gbuf, x, y, w, h);
         EdgeStop32 es = EdgeStop32::create(depth_tex[i], gbuffer.fwidth_z * 3.0f, 1.0f, gbuffer.normal, 7);
         float ws = 0.0f;
         float2 ms = F2(0.0f, 0.0f);
         float3 dsum = F3(0.0f), ssum = F3(0.0f);
+        if (FORM == 2) {
+          const Rec32 rc = IO::load(in, i);
+          kshift = F2(lum_fma(rc.d), lum_fma(rc.s));
+        }
         for (int oy = -3; oy <= 3; oy++)
           for (int ox = -3; ox <= 3; ox++) {
             int ux = x + ox, uy = y + oy;
@@ -1919,7 +1973,12 @@ void dn32_fallback(int w, int h, const float* depth_tex, const uint32_t* gbuf, c
             ws += wt;
             dsum = fma3(wt, r.d, dsum);
             ssum = fma3(wt, r.s, ssum);
-            ms = F2(fma_(wt, r.aux.x, ms.x), fma_(wt, r.aux.y, ms.y));
+            if (FORM == 2) {
+              const float2 e = F2(lum_fma(r.d) - kshift.x, lum_fma(r.s) - kshift.y);
+              ms = F2(fma_(wt, fma_(e.x, e.x, r.aux.x), ms.x), fma_(wt, fma_(e.y, e.y, r.aux.y), ms.y));
+            } else {
+              ms = F2(fma_(wt, r.aux.x, ms.x), fma_(wt, r.aux.y, ms.y));
+            }
           }
         float inv = 1.0f / ws;
         dd = dsum * inv;
@@ -1931,8 +1990,15 @@ void dn32_fallback(int w, int h, const float* depth_tex, const uint32_t* gbuf, c
         sd = r.s;
         md = r.aux;
       }
-      float2 fst = F2(lum_fma(dd), lum_fma(sd));
-      float2 var = F2(hmax(fma_(-fst.x, fst.x, md.x), 0.0f), hmax(fma_(-fst.y, fst.y, md.y), 0.0f));
+      float2 var;
+      if (FORM == 2) {  // the long-history record holds the variance; the blend's is centered
+        const bool blended = hl < 4.0f * HISTORY_LEN_UNIT;
+        const float2 e = blended ? F2(lum_fma(dd) - kshift.x, lum_fma(sd) - kshift.y) : F2(0.0f, 0.0f);
+        var = F2(hmax(fma_(-e.x, e.x, md.x), 0.0f), hmax(fma_(-e.y, e.y, md.y), 0.0f));
+      } else {
+        float2 fst = F2(lum_fma(dd), lum_fma(sd));
+        var = F2(hmax(fma_(-fst.x, fst.x, md.x), 0.0f), hmax(fma_(-fst.y, fst.y, md.y), 0.0f));
+      }
       float boost = hmax(1.0f, (4.0f * HISTORY_LEN_UNIT) / hl);
       IO::store(out, i, dd, sd, var * boost);
     }

@@ -230,7 +230,13 @@ class OracleView:
             if name == "hist_color":
                 return np.concatenate([v[:, 0:3], v[:, 4:7]], 1)
             aux = v[:, [3, 7]]
-            return aux * aux if f16 else aux
+            if not f16:
+                return aux
+            aux = aux * np.abs(aux)  # the FP16 records hold signed square roots
+            if name == "hist_moments":  # ... of the variance around the record's colour
+                lum = np.array([0.2126, 0.7152, 0.0722])
+                aux = aux + np.stack([v[:, 0:3] @ lum, v[:, 4:7] @ lum], 1) ** 2
+            return aux
         if name == "hist_len":
             return self.buffer("hist_len").astype(np.float64).reshape(n, 1)
         raise KeyError(name)

@@ -3,8 +3,10 @@
 The replay follows the float form's decisions (the selected samples, accepted taps,
 sample counts and history lengths come out identical) and recomputes every value in
 binary64 with unquantized storage. Its differences from the FP32 form are binary32
-rounding only, so they must be small; the FP16 form's are larger (binary16 storage of
-hit positions, radiance, weights and history), and are reported by the benchmark.
+rounding only, so they must be small; the FP16 form's raw outputs carry its binary16
+storage (radiance, AO, lighting, history), and its denoised outputs stay within 1e-3
+because its history keeps centered moments. The benchmark reports the same tables at
+960x540 over 32 frames.
 """
 import numpy as np
 import pytest
@@ -21,6 +23,12 @@ N = W * H
 F32_BOUNDS = {"diff_W": 1e-4, "spec_W": 1e-3, "ao": 1e-4, "raw_diffuse": 1e-5, "raw_specular": 1e-3,
               "ray_len": 1e-5, "hist_color": 1e-3, "hist_moments": 1e-3, "variance": 1e-3,
               "denoised_diffuse": 1e-4, "denoised_specular": 1e-2}
+# The FP16 form: binary16 storage of lighting, AO and history (relative rounding
+# 2^-11) with centered moments, so that the denoised outputs stay within the 1e-3
+# accuracy bar of the storage form.
+F16_BOUNDS = {"diff_W": 1e-4, "spec_W": 1e-3, "ao": 1e-3, "raw_diffuse": 1e-3, "raw_specular": 1e-3,
+              "ray_len": 1e-3, "hist_color": 2e-3, "hist_moments": 5e-3, "variance": 5e-3,
+              "denoised_diffuse": 1e-3, "denoised_specular": 1e-3}
 
 
 def rel_l2(a, b):
@@ -63,11 +71,8 @@ def test_replay_follows_the_float_form(form):
         ov.close()
     print("%s form, worst rel L2 against binary64 over %d frames: %s" % (
         form, FRAMES - 1, " ".join("%s %.1e" % kv for kv in worst.items())))
-    if form == "f32":
-        for name, bound in F32_BOUNDS.items():
-            assert worst[name] <= bound, "%s: rel L2 %.2e > %.0e" % (name, worst[name], bound)
-    else:  # binary16 storage: larger, but bounded and finite
-        assert all(np.isfinite(v) for v in worst.values())
+    for name, bound in (F32_BOUNDS if form == "f32" else F16_BOUNDS).items():
+        assert worst[name] <= bound, "%s: rel L2 %.2e > %.0e" % (name, worst[name], bound)
 
 
 def test_replay_refused_where_it_does_not_apply():

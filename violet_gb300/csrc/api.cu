@@ -554,7 +554,7 @@ namespace {
 // pool (kNullOff for unused), padding to 256 bytes, the pool.
 static_assert(sizeof(ViewBuffers) % sizeof(void*) == 0, "ViewBuffers holds pointers only");
 constexpr uint32_t kStateMagic = 0x53544C56u;  // "VLTS"
-constexpr uint32_t kStateVersion = 1;
+constexpr uint32_t kStateVersion = 2;
 constexpr uint64_t kNullOff = ~0ull;
 constexpr uint32_t kStatePtrs = (uint32_t)(sizeof(ViewBuffers) / sizeof(void*));
 struct StateHeader {

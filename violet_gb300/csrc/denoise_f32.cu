@@ -74,21 +74,23 @@ __device__ __forceinline__ void store_rec(float4* __restrict__ p, size_t i, f3 d
   p[2 * i + 1] = make_float4(s.x, s.y, s.z, aux.y);
 }
 
-// f16 form: one uint4 per pixel = 8 halves {d.rgb, sqrt(aux.x), s.rgb, sqrt(aux.y)};
-// stores saturate (f32tof16_sat). The second moments and variances (aux >= 0) are
-// stored as their square roots: luminance^2 of bright pixels exceeds the f16 range
-// (~7e6 for a x100 firefly), the root keeps the radiance's range.
+// f16 form: one uint4 per pixel = 8 halves {d.rgb, sroot(aux.x), s.rgb, sroot(aux.y)};
+// stores saturate (f32tof16_sat). aux is a luminance variance around the record's
+// own colour in every f16 record (centered moments, below), stored as its signed
+// square root sroot(v) = sign(v) sqrt(|v|): luminance^2 of bright pixels exceeds the
+// f16 range (~7e6 for a x100 firefly), the root keeps the radiance's range.
+__device__ __forceinline__ float sroot(float v) { return copysignf(sqrt_(fabs_(v)), v); }
 __device__ __forceinline__ Rec load_rec(const uint4* __restrict__ p, size_t i) {
   uint4 v = p[i];
   Rec r;
   r.d = mk3(f16tof32(v.x & 0xFFFFu), f16tof32(v.x >> 16), f16tof32(v.y & 0xFFFFu));
   r.s = mk3(f16tof32(v.z & 0xFFFFu), f16tof32(v.z >> 16), f16tof32(v.w & 0xFFFFu));
   float ax = f16tof32(v.y >> 16), ay = f16tof32(v.w >> 16);
-  r.aux = mk2(ax * ax, ay * ay);
+  r.aux = mk2(ax * fabs_(ax), ay * fabs_(ay));
   return r;
 }
 __device__ __forceinline__ void store_rec(uint4* __restrict__ p, size_t i, f3 d, f3 s, f2 aux) {
-  uint32_t ax = f32tof16_sat(sqrt_(fmax_(aux.x, 0.0f))), ay = f32tof16_sat(sqrt_(fmax_(aux.y, 0.0f)));
+  uint32_t ax = f32tof16_sat(sroot(aux.x)), ay = f32tof16_sat(sroot(aux.y));
   p[i] = make_uint4(f32tof16_sat(d.x) | (f32tof16_sat(d.y) << 16), f32tof16_sat(d.z) | (ax << 16),
                     f32tof16_sat(s.x) | (f32tof16_sat(s.y) << 16), f32tof16_sat(s.z) | (ay << 16));
 }
@@ -206,9 +208,36 @@ __device__ __forceinline__ float quad_max_len(const N* __restrict__ len, int x, 
 
 // --------------------------------------------------------------- temporal
 
+// Centered moments (f16 form). The reference keeps, per channel, the second moment m
+// of the luminance beside the colour history c, and the variance is m - lum(c)^2. In
+// binary16 that difference cancels: both terms carry a relative rounding of 2^-11,
+// and where the variance is small against lum(c)^2 it is mostly rounding, which the
+// a-trous luminance weights then amplify. The f16 form therefore stores the variance
+// itself, v = m - lum(c)^2, and carries it through every pass with the same algebra
+// in centered form:
+// - a weighted blend of records (bilinear history, disocclusion fix, spatial
+//   fallback) gives sum(w (v_j + (l_j - K)^2)) / sum(w) - (lum(blend) - K)^2 with a
+//   shift K near the l_j (the first accepted tap's luminance, or the centre
+//   record's), which is m_blend - lum(c_blend)^2 without the cancellation;
+// - the diffuse history update c' = lerp(c_h, c_src, a), m' = lerp(m_h, l_src^2, a)
+//   gives v' = (1 - a) (v_h + a (l_src - l_h)^2);
+// - the specular update blends the colour from the dual-source history (luminance
+//   l_d) and the moment from the surface history (l_h):
+//   v' = (1 - a) (v_h + (l_h - l_d)(l_h + l_d) + a (l_src - l_d)^2);
+// - the fast-history clamp moves the colour from luminance l to l':
+//   v' = v + (l - l')(l + l').
+// Each is the reference's quantity in exact arithmetic. The f32 form keeps the
+// reference's moments (it is the transliteration of the reference arithmetic).
+template <int FORM>
+struct Centered {
+  static constexpr bool value = FORM == FORM_F16;
+};
+__device__ __forceinline__ f2 lum2(f3 d, f3 s) { return mk2(lum_fast(d.x, d.y, d.z), lum_fast(s.x, s.y, s.z)); }
+
 template <class Geo, int FORM>
 struct Dn32TemporalF {
   static constexpr int kMinBlocks = 4;  // 64 registers instead of 96 (measured 20% faster)
+  static constexpr bool kCentered = Centered<FORM>::value;
   using R = typename DnT<FORM>::R;
   using N = typename DnT<FORM>::N;
   using L = typename DnT<FORM>::L;
@@ -280,6 +309,7 @@ struct Dn32TemporalF {
   f2 huv = mk2(screen_uv.x - mv.x, screen_uv.y - mv.y);
   f3 dh = mk3(0.0f), sh = mk3(0.0f), dfh = mk3(0.0f), sfh = mk3(0.0f);
   f2 smh = mk2(0.0f, 0.0f);
+  f2 kshift = mk2(0.0f, 0.0f);  // centered form: the shift of the blended variances
   float hl = 0.0f;
   bool valid = huv.x == saturate(huv.x) && huv.y == saturate(huv.y) && has_history;
   if (valid) {
@@ -310,11 +340,18 @@ struct Dn32TemporalF {
         bool ok = fabs_(prev_depth[j] - reproj_depth) < depth_tol && dot3(nd, nd) < normal_tol_sq;
         if (!ok) continue;
         float wt = wts[oy][ox];
+        if (kCentered) {
+          const f2 l = lum2(r.d, r.s);
+          if (wsum == 0.0f) kshift = l;
+          const f2 e = l - kshift;
+          ms = mk2(fma_(wt, fma_(e.x, e.x, r.aux.x), ms.x), fma_(wt, fma_(e.y, e.y, r.aux.y), ms.y));
+        } else {
+          ms = mk2(fma_(wt, r.aux.x, ms.x), fma_(wt, r.aux.y, ms.y));
+        }
         wsum = wsum + wt;
         hs = hs + wt * lj;
         ds = fma3(wt, r.d, ds);
         ss = fma3(wt, r.s, ss);
-        ms = mk2(fma_(wt, r.aux.x, ms.x), fma_(wt, r.aux.y, ms.y));
         if (kn.fast_history) {
           Rec f = load_rec(fast_hist, j);
           dfs = fma3(wt, f.d, dfs);
@@ -336,9 +373,17 @@ struct Dn32TemporalF {
   if (!valid) {
     dh = sh = dfh = sfh = mk3(0.0f);
     smh = mk2(0.0f, 0.0f);
+    kshift = mk2(0.0f, 0.0f);
     hl = 0.0f;
   }
   hl = hl + VLT_HISTORY_LEN_UNIT;
+  // Centered form: the history's variance around its own colour.
+  f2 lh = mk2(0.0f, 0.0f);
+  if (kCentered) {
+    lh = lum2(dh, sh);
+    const f2 eh = lh - kshift;
+    smh = mk2(fma_(-eh.x, eh.x, smh.x), fma_(-eh.y, eh.y, smh.y));
+  }
 
   float4 dv = ld_light(diff_src, i);
   f3 dsrc = mk3(dv.x, dv.y, dv.z);
@@ -358,6 +403,7 @@ struct Dn32TemporalF {
   f3 dff = lerp3(dfh, dsrc, alpha_f.x);
   f3 sff = lerp3(sfh, ssrc, alpha_f.y);
   f3 sf;
+  float lum_dual = 0.0f;
   {
     f3 mean = m1;
     f3 dev = sqrt3(abs3(m2 - mean * mean));
@@ -365,6 +411,7 @@ struct Dn32TemporalF {
     float wv = dsr_weight_exact(vsh, mean, dev);
     float wh = dsr_weight_exact(sh, mean, dev);
     f3 dual = (wv * vsh + wh * sh) / fmax_(wv + wh, 1e-37f);
+    if (kCentered) lum_dual = lum_fast(dual.x, dual.y, dual.z);
     sf = lerp3(dual, ssrc, alpha.y);
     if (kn.fast_history) {
       float wv2 = dsr_weight_exact(vsfh, mean, dev);
@@ -372,6 +419,11 @@ struct Dn32TemporalF {
       f3 dual2 = (wv2 * vsfh + wh2 * sfh) / fmax_(wv2 + wh2, 1e-37f);
       sff = lerp3(dual2, ssrc, alpha_f.y);
     }
+  }
+  if (kCentered) {
+    const float ed = lsrc.x - lh.x, es = lsrc.y - lum_dual;
+    const float hm = (lh.y - lum_dual) * (lh.y + lum_dual);
+    smf = mk2((1.0f - alpha.x) * fma_(alpha.x * ed, ed, smh.x), (1.0f - alpha.y) * fma_(alpha.y * es, es, smh.y + hm));
   }
   store_rec(out, i, df, sf, smf);
   st_len(out_len, i, hl);
@@ -401,6 +453,11 @@ struct Dn32FixF {
     f2 ws = mk2(0.0f, 0.0f);
     f3 dsum = mk3(0.0f), ssum = mk3(0.0f);
     f2 msum = mk2(0.0f, 0.0f);
+    f2 kshift = mk2(0.0f, 0.0f);  // centered form: the centre record's luminance
+    if (Centered<FORM>::value) {
+      const Rec rc = load_rec(in, i);
+      kshift = lum2(rc.d, rc.s);
+    }
     const int stride = f2i_rz((14.0f * VLT_HISTORY_LEN_UNIT) / hl);
     for (int oy = -2; oy <= 2; ++oy) {
       for (int ox = -2; ox <= 2; ++ox) {
@@ -413,10 +470,21 @@ struct Dn32FixF {
         ws = ws + wt;
         dsum = fma3(wt.x, r.d, dsum);
         ssum = fma3(wt.y, r.s, ssum);
-        msum = mk2(fma_(wt.x, r.aux.x, msum.x), fma_(wt.y, r.aux.y, msum.y));
+        if (Centered<FORM>::value) {
+          const f2 e = lum2(r.d, r.s) - kshift;
+          msum = mk2(fma_(wt.x, fma_(e.x, e.x, r.aux.x), msum.x), fma_(wt.y, fma_(e.y, e.y, r.aux.y), msum.y));
+        } else {
+          msum = mk2(fma_(wt.x, r.aux.x, msum.x), fma_(wt.y, r.aux.y, msum.y));
+        }
       }
     }
-    store_rec(out, i, dsum * (1.0f / ws.x), ssum * (1.0f / ws.y), mk2(msum.x / ws.x, msum.y / ws.y));
+    const f3 dfix = dsum * (1.0f / ws.x), sfix = ssum * (1.0f / ws.y);
+    f2 mfix = mk2(msum.x / ws.x, msum.y / ws.y);
+    if (Centered<FORM>::value) {
+      const f2 e = lum2(dfix, sfix) - kshift;
+      mfix = mk2(fma_(-e.x, e.x, mfix.x), fma_(-e.y, e.y, mfix.y));
+    }
+    store_rec(out, i, dfix, sfix, mfix);
   } else {
     copy_rec(out, in, i);
   }
@@ -463,7 +531,13 @@ struct Dn32FastClampF {
   Rec c = load_rec(rec, i);
   f3 d = clamp3(ycocg(c.d), dm1 - ddev, dm1 + ddev);
   f3 s = clamp3(ycocg(c.s), sm1 - sdev, sm1 + sdev);
-  store_rec(rec, i, ycocg_inv(d), ycocg_inv(s), c.aux);
+  const f3 dn = ycocg_inv(d), sn = ycocg_inv(s);
+  f2 aux = c.aux;
+  if (Centered<FORM>::value) {  // the variance follows the clamped colour
+    const f2 l0 = lum2(c.d, c.s), l1 = lum2(dn, sn);
+    aux = mk2(fma_(l0.x - l1.x, l0.x + l1.x, aux.x), fma_(l0.y - l1.y, l0.y + l1.y, aux.y));
+  }
+  store_rec(rec, i, dn, sn, aux);
 }
 };
 
@@ -486,11 +560,16 @@ struct Dn32FallbackF {
   hl = qmax;
   f3 dd, sd;
   f2 md;
+  f2 kshift = mk2(0.0f, 0.0f);  // centered form: the shift of the blended variances
   if (hl < 4.0f * VLT_HISTORY_LEN_UNIT) {
     EdgeStopFast es = make_es(geo.dep(i), geo.fwz(i) * 3.0f, 1.0f, geo.normal(i), 7);
     float ws = 0.0f;
     f3 dsum = mk3(0.0f), ssum = mk3(0.0f);
     f2 msum = mk2(0.0f, 0.0f);
+    if (Centered<FORM>::value) {
+      const Rec rc = load_rec(in, i);
+      kshift = lum2(rc.d, rc.s);
+    }
     for (int oy = -3; oy <= 3; ++oy) {
       for (int ox = -3; ox <= 3; ++ox) {
         int cx = x + ox, cy = y + oy;
@@ -501,7 +580,12 @@ struct Dn32FallbackF {
         ws = ws + wt;
         dsum = fma3(wt, r.d, dsum);
         ssum = fma3(wt, r.s, ssum);
-        msum = mk2(fma_(wt, r.aux.x, msum.x), fma_(wt, r.aux.y, msum.y));
+        if (Centered<FORM>::value) {
+          const f2 e = lum2(r.d, r.s) - kshift;
+          msum = mk2(fma_(wt, fma_(e.x, e.x, r.aux.x), msum.x), fma_(wt, fma_(e.y, e.y, r.aux.y), msum.y));
+        } else {
+          msum = mk2(fma_(wt, r.aux.x, msum.x), fma_(wt, r.aux.y, msum.y));
+        }
       }
     }
     float inv = 1.0f / ws;
@@ -514,8 +598,16 @@ struct Dn32FallbackF {
     sd = r.s;
     md = r.aux;
   }
-  f2 fst = mk2(lum_fast(dd.x, dd.y, dd.z), lum_fast(sd.x, sd.y, sd.z));
-  f2 var = mk2(fmax_(fma_(-fst.x, fst.x, md.x), 0.0f), fmax_(fma_(-fst.y, fst.y, md.y), 0.0f));
+  f2 var;
+  if (Centered<FORM>::value) {
+    // the long-history record holds the variance; the blend's is centered on kshift
+    const bool blended = hl < 4.0f * VLT_HISTORY_LEN_UNIT;
+    const f2 e = blended ? lum2(dd, sd) - kshift : mk2(0.0f, 0.0f);
+    var = mk2(fmax_(fma_(-e.x, e.x, md.x), 0.0f), fmax_(fma_(-e.y, e.y, md.y), 0.0f));
+  } else {
+    f2 fst = mk2(lum_fast(dd.x, dd.y, dd.z), lum_fast(sd.x, sd.y, sd.z));
+    var = mk2(fmax_(fma_(-fst.x, fst.x, md.x), 0.0f), fmax_(fma_(-fst.y, fst.y, md.y), 0.0f));
+  }
   float boost = fmax_(1.0f, (4.0f * VLT_HISTORY_LEN_UNIT) / hl);
   store_rec(out, i, dd, sd, var * boost);
 }
