@@ -66,8 +66,9 @@ typedef enum vlt_form {
   VLT_FORM_REF = 0, /* the reference's texture formats; bit-exact with the oracle */
   VLT_FORM_F32 = 1, /* every stored float in binary32 */
   VLT_FORM_F16 = 2  /* 16-byte diffuse reservoirs (the candidate's encoded sample, W f32),
-                     * fp16 lighting, history and moments; the specular reservoir as in
-                     * the f32 form */
+                     * fp16 lighting and history; the history keeps the luminance
+                     * variance around its colour (centered moments) instead of the
+                     * second moment; the specular reservoir as in the f32 form */
 } vlt_form;
 
 /* FrameParams of crates/violet-app/src/render_loop.rs:66-85 / frame_bindings.hlsl:6-26
