@@ -595,7 +595,9 @@ vlt_status vlt_hg_visualize(const vlt_frame_params* fp, uint32_t width, uint32_t
 /* Diagnostics (no counterpart in the reference): evaluates the library's own
  * binary32 transcendentals on the device, elementwise: fn 0 exp2, 1 exp, 2 log2,
  * 3 sin, 4 cos, 5 the float forms' FMA exp2 (with its short path for [-126, 0]),
- * 6 the same without the short path. x and y are device arrays of n floats. */
+ * 6 the same without the short path, 7 the f16 form's storage conversion of x and
+ * -x packed into one word (returned as its bits). x and y are device arrays of n
+ * floats. */
 vlt_status vlt_diag_math(int fn, const float* x, float* y, uint32_t n, void* stream);
 
 /* Diagnostics (no counterpart in the reference): image-wide sums in binary64 on the

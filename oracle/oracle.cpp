@@ -3756,6 +3756,7 @@ void vlto_math(int fn, const float* x, float* y, uint32_t n) {
       case 4: y[i] = cos_own(x[i]); break;
       case 5:
       case 6: y[i] = exp2_fma(x[i]); break;
+      case 7: y[i] = asfloat((uint32_t)f16sat(x[i]) | ((uint32_t)f16sat(-x[i]) << 16)); break;
       default: y[i] = 0.0f;
     }
   }

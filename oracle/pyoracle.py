@@ -72,7 +72,7 @@ SIGS = {
     "vlto_reservoir_decode": (None, [U32, C.POINTER(U32), C.POINTER(C.c_float)]),
 }
 
-MATH = {"exp2": 0, "exp": 1, "log2": 2, "sin": 3, "cos": 4, "exp2_fma": 5, "exp2_fma_full": 6}
+MATH = {"exp2": 0, "exp": 1, "log2": 2, "sin": 3, "cos": 4, "exp2_fma": 5, "exp2_fma_full": 6, "f16_pair": 7}
 CODEC = {"f32tof16": 0, "f16tof32": 1, "uf11": 2, "uf10": 3, "uf11_to_f32": 4, "jenkins": 5, "xorshift": 6,
          "xxh1": 7, "xxh3": 8}
 

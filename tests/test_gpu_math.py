@@ -27,13 +27,19 @@ def _inputs(fn):
     elif fn == "log2":
         x = np.concatenate([np.exp(rng.uniform(-100, 88, 200000)), rng.uniform(0, 4, 200000),
                             [0.0, -0.0, 1.0, 2.0, 0.5, 1e-45, 1e-40, 1.17549435e-38, np.inf, -1.0, np.nan]])
+    elif fn == "f16_pair":
+        # around the half range's edges, its subnormals and rounding ties, and specials
+        x = np.concatenate([rng.uniform(-7e4, 7e4, 200000), np.exp(rng.uniform(-20, 11.2, 200000)),
+                            np.arange(65480, 65540, 0.25), np.arange(-1e-4, 1e-4, 3e-8),
+                            [0.0, -0.0, 65504.0, 65519.996, 65520.0, 1e30, 5.96e-8, 2.98e-8, 2.99e-8,
+                             np.inf, -np.inf, np.nan, 1.0009765625, 1.00048828125]])
     else:
         x = np.concatenate([rng.uniform(-50, 50, 200000), rng.uniform(-7, 7, 200000),
                             [0.0, -0.0, np.pi / 4, np.pi / 2, np.pi, 65536.0, 65537.0, np.inf, np.nan]])
     return x.astype(np.float32)
 
 
-@pytest.mark.parametrize("fn", ["exp2", "exp", "log2", "sin", "cos", "exp2_fma", "exp2_fma_full"])
+@pytest.mark.parametrize("fn", ["exp2", "exp", "log2", "sin", "cos", "exp2_fma", "exp2_fma_full", "f16_pair"])
 def test_own_math_bit_exact(fn):
     import torch
 

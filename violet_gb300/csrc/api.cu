@@ -1566,14 +1566,15 @@ __global__ void k_diag_math(int fn, const float* __restrict__ x, float* __restri
     case 3: r = sin_(v); break;
     case 4: r = cos_(v); break;
     case 5: r = exp2_fma(v); break;
-    default: r = exp2_fma_full(v); break;
+    case 6: r = exp2_fma_full(v); break;
+    default: r = as_float(pack_h2_sat(v, -v)); break;
   }
   y[i] = r;
 }
 }  // namespace vlt
 
 extern "C" vlt_status vlt_diag_math(int fn, const float* x, float* y, uint32_t n, void* stream) {
-  if (fn < 0 || fn > 6 || (n && (!x || !y))) return VLT_ERR_INVALID_ARG;
+  if (fn < 0 || fn > 7 || (n && (!x || !y))) return VLT_ERR_INVALID_ARG;
   if (n == 0) return VLT_OK;
   vlt::k_diag_math<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(fn, x, y, n);
   return vlt::cuda_status(cudaGetLastError());

@@ -99,9 +99,8 @@ __device__ __forceinline__ Rec load_rec(const uint4* __restrict__ p, size_t i) {
   return r;
 }
 __device__ __forceinline__ void store_rec(uint4* __restrict__ p, size_t i, f3 d, f3 s, f2 aux) {
-  uint32_t ax = f32tof16_sat(sroot(aux.x)), ay = f32tof16_sat(sroot(aux.y));
-  p[i] = make_uint4(f32tof16_sat(d.x) | (f32tof16_sat(d.y) << 16), f32tof16_sat(d.z) | (ax << 16),
-                    f32tof16_sat(s.x) | (f32tof16_sat(s.y) << 16), f32tof16_sat(s.z) | (ay << 16));
+  p[i] = make_uint4(pack_h2_sat(d.x, d.y), pack_h2_sat(d.z, sroot(aux.x)), pack_h2_sat(s.x, s.y),
+                    pack_h2_sat(s.z, sroot(aux.y)));
 }
 __device__ __forceinline__ void copy_rec(float4* __restrict__ out, const float4* __restrict__ in, size_t i) {
   const Rec r = load_rec(in, i);
@@ -125,7 +124,7 @@ __device__ __forceinline__ void st_out(float4* __restrict__ p, size_t i, f3 v) {
   p[i] = make_float4(v.x, v.y, v.z, 0.0f);
 }
 __device__ __forceinline__ void st_out(uint2* __restrict__ p, size_t i, f3 v) {
-  p[i] = make_uint2(f32tof16_sat(v.x) | (f32tof16_sat(v.y) << 16), f32tof16_sat(v.z));
+  p[i] = make_uint2(pack_h2_sat(v.x, v.y), pack_h2_sat(v.z, 0.0f));
 }
 
 // Element types per form: record unit R, history length N, lighting L.

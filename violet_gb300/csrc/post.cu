@@ -34,7 +34,7 @@ struct ColorIO<FORM_F16> {
     return mk3(f16tof32(v.x & 0xFFFFu), f16tof32(v.x >> 16), f16tof32(v.y & 0xFFFFu));
   }
   static __device__ __forceinline__ void st(T* p, size_t i, f3 v) {
-    p[i] = make_uint2(f32tof16_sat(v.x) | (f32tof16_sat(v.y) << 16), f32tof16_sat(v.z));
+    p[i] = make_uint2(pack_h2_sat(v.x, v.y), pack_h2_sat(v.z, 0.0f));
   }
 };
 

@@ -218,7 +218,7 @@ struct DiffStore<FORM_F16> {
   using Ptr = DiffF16Ptr;
   using Light = uint2;  // half4 {rgb, 0}
   static __device__ __forceinline__ Light light(f3 l) {
-    return make_uint2(f32tof16_sat(l.x) | (f32tof16_sat(l.y) << 16), f32tof16_sat(l.z));
+    return make_uint2(pack_h2_sat(l.x, l.y), pack_h2_sat(l.z, 0.0f));
   }
   static __device__ __forceinline__ Light zero_light() { return make_uint2(0u, 0u); }
 };
@@ -754,7 +754,7 @@ __device__ __forceinline__ void store_spec_light(float4* l, uint16_t*, size_t i,
   if (l) l[i] = make_float4(v.x, v.y, v.z, ray_len);
 }
 __device__ __forceinline__ void store_spec_light(uint2* l, uint16_t*, size_t i, f3 v, float ray_len) {
-  if (l) l[i] = make_uint2(f32tof16_sat(v.x) | (f32tof16_sat(v.y) << 16), f32tof16_sat(v.z) | (f32tof16_sat(ray_len) << 16));
+  if (l) l[i] = make_uint2(pack_h2_sat(v.x, v.y), pack_h2_sat(v.z, ray_len));
 }
 template <int FORM>
 struct SpecLight;

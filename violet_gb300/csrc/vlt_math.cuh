@@ -487,6 +487,21 @@ VLT_HD uint32_t f32tof16_sat(float f) {
   float c = fmin_(fmax_(f, -65504.0f), 65504.0f);
   return f32tof16(c);
 }
+// Two storage conversions packed into one word (lo in bits 0-15): the same bits as
+// f32tof16_sat(lo) | f32tof16_sat(hi) << 16. On the device NaN is replaced by 0 and
+// one saturating paired conversion (cvt.rn.satfinite.f16x2.f32: round to nearest
+// even, magnitudes beyond the largest finite half to +-65504) does the rest.
+VLT_HD uint32_t pack_h2_sat(float lo, float hi) {
+#if defined(__CUDA_ARCH__)
+  lo = is_nan(lo) ? 0.0f : lo;
+  hi = is_nan(hi) ? 0.0f : hi;
+  uint32_t r;
+  asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+#else
+  return f32tof16_sat(lo) | (f32tof16_sat(hi) << 16);
+#endif
+}
 // The value an f16-form store keeps.
 VLT_HD float q16(float f) { return f16tof32(f32tof16_sat(f)); }
 
