@@ -49,6 +49,27 @@ def test_frame_params_camera_motion_and_jitter():
     assert np.isclose(p0.jitter[0], 0.0) and np.isclose(p0.jitter[1], (2 / 3 - 1) / 180)
 
 
+def _halton(i, b):
+    f, r = 1.0, 0.0
+    while i > 0:
+        f /= b
+        r += f * (i % b)
+        i //= b
+    return r
+
+
+def test_jitter_is_the_halton_2_3_cycle_of_eight():
+    # render_loop.rs:89-106 with the cycle of restir_renderer.rs:65: frame f jitters by
+    # Halton(2, 3) of index f % 8 + 1, mapped to [-1, 1) and divided by the size.
+    W, H = 320, 180
+    s = vg.Scene(1, W, H)
+    for f in range(17):
+        p = s.frame_params(f)
+        k = f % 8 + 1
+        assert np.isclose(p.jitter[0], (2 * _halton(k, 2) - 1) / W, atol=1e-9), f
+        assert np.isclose(p.jitter[1], (2 * _halton(k, 3) - 1) / H, atol=1e-9), f
+
+
 def test_host_only_generator_matches_the_product_library():
     """The oracle's copy of the scene generator (the product's source compiled without
     CUDA, used by the CPU benchmark) produces the same frames as the product library."""
