@@ -14,6 +14,8 @@ after every frame.
   stays inside each frame's filter and does not accumulate. The per-frame errors are
   printed.
 - Reference storage form, 8 frames: bit for bit.
+- FP16 storage form at the 3840x2160 precision workload with the same knobs, 8
+  frames: bit for bit.
 """
 import numpy as np
 import pytest
@@ -35,21 +37,27 @@ REF_BUFFERS = [("diff_reservoir", 4), ("spec_hit_pos", 4), ("spec_reservoir", 2)
                ("ao_history", 1), ("ao_filtered", None), ("raw_diffuse", 1), ("raw_specular", 1),
                ("spec_ray_len", None)]
 REF_DENOISE = [("hist_color", 2), ("hist_moments", 1), ("hist_len", None), ("variance", 1)]
-OUT_PX = {"ref": 4, "f32": 16}
+F16_BUFFERS = [("diff_reservoir", None), ("spec_hit_pos", 4), ("spec_reservoir", 2), ("spec_radiance", 1),
+               ("ao_history", 1), ("ao_filtered", None), ("raw_diffuse", 2), ("raw_specular", 2)]
+F16_DENOISE = [("hist_len", None), ("hist_record", 4), ("fallback_record", 4)]
+OUT_PX = {"ref": 4, "f32": 16, "f16": 8}
+OUT_WORDS = {"ref": 1, "f32": 4, "f16": 2}
+LISTS = {"ref": (REF_BUFFERS, REF_DENOISE), "f32": (F32_BUFFERS, F32_DENOISE), "f16": (F16_BUFFERS, F16_DENOISE)}
 
 
-def _compare(got, exp, words, what):
+def _compare(got, exp, words, what, width=W):
     assert got.nbytes == exp.nbytes, what
     if words is None:
-        msg = first_mismatch(got.view(np.uint8), exp.view(np.uint8), W)
+        msg = first_mismatch(got.view(np.uint8), exp.view(np.uint8), width)
     else:
-        msg = first_float_mismatch(got.view(np.uint32), exp.view(np.uint32), W, words)
+        msg = first_float_mismatch(got.view(np.uint32), exp.view(np.uint32), width, words)
     assert msg is None, "%s: %s" % (what, msg)
 
 
-def _run(form, frames, with_reference_weights):
+def _run(form, frames, with_reference_weights, W=W, H=H):
     import torch
 
+    N = W * H
     params = vg.params_plain(1)
     assert params.diff_spatial_passes == 2 and params.diff_spatial_taps == 8 and params.hg_log2_buckets == 18
     ctx = vg.Context(0)
@@ -61,7 +69,7 @@ def _run(form, frames, with_reference_weights):
         rview = po.OracleView(W, H, params, form)
         rview.set_atrous_reference_weights(True)
     ob = OUT_PX[form]
-    bufs, den = (F32_BUFFERS, F32_DENOISE) if form == "f32" else (REF_BUFFERS, REF_DENOISE)
+    bufs, den = LISTS[form]
     dev = {k: torch.empty(N * c * np.dtype(dt).itemsize, dtype=torch.uint8, device="cuda")
            for k, (dt, c) in vg.FRAME_BUFFERS.items()}
     out_dev = {k: torch.zeros(ob * N, dtype=torch.uint8, device="cuda") for k in ("diffuse", "specular")}
@@ -79,11 +87,11 @@ def _run(form, frames, with_reference_weights):
             names = bufs + (den if f > 0 else [])
             for name, words in names:
                 ptr, nb = view.buffer(name)
-                _compare(d2h(ptr, nb, np.uint8), oview.buffer(name, np.uint8), words, "frame %d %s" % (f, name))
+                _compare(d2h(ptr, nb, np.uint8), oview.buffer(name, np.uint8), words, "frame %d %s" % (f, name), W)
             got_out = {}
             for k in ("diffuse", "specular"):
                 got_out[k] = out_dev[k].cpu().numpy()
-                _compare(got_out[k], out_host[k], 4 if form == "f32" else 1, "frame %d output %s" % (f, k))
+                _compare(got_out[k], out_host[k], OUT_WORDS[form], "frame %d output %s" % (f, k), W)
             for name, dt in (("hg_storage", np.uint32), ("hg_decay", np.uint8), ("hg_query_count", np.uint32)):
                 ptr, nb = view.buffer(name)
                 msg = first_mismatch(d2h(ptr, nb, dt), oview.buffer(name, dt))
@@ -124,3 +132,7 @@ def test_config1_fullsize_f32_64_frames_bitexact_and_reference_weights():
 
 def test_config1_fullsize_reference_form_8_frames_bitexact():
     _run("ref", 8, False)
+
+
+def test_config2_4k_f16_8_frames_bitexact():
+    _run("f16", 8, False, W=3840, H=2160)
