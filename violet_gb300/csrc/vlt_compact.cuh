@@ -14,22 +14,24 @@
 
 namespace vlt {
 
-static constexpr uint32_t kCompactChunk = 2048;  // items per block (kBlock1D threads x 16)
-static constexpr uint32_t kCompactPer = kCompactChunk / kBlock1D;  // consecutive items per thread
-static_assert(kCompactPer * kBlock1D == kCompactChunk, "a chunk is kBlock1D threads x kCompactPer items");
+static constexpr uint32_t kCompactChunk = 2048;  // items per block (kBlock1D threads x 16 rounds)
+static constexpr uint32_t kCompactRounds = kCompactChunk / kBlock1D;
+static_assert(kCompactRounds * kBlock1D == kCompactChunk, "a chunk is kBlock1D threads x kCompactRounds items");
+static_assert(kCompactRounds <= 32 && kBlock1D % 32 == 0, "rounds and warps of a chunk");
 
-// Every 1D launch has kBlock1D threads per block; thread t of a chunk owns its
-// items [t * kCompactPer, (t + 1) * kCompactPer).
+// Every 1D launch has kBlock1D threads per block. Item r * kBlock1D + t of a chunk
+// belongs to thread t in round r, so that every round reads kBlock1D consecutive
+// items (coalesced); item order within the chunk is round-major, then thread order.
 template <class P>
 struct CompactCountF {
   static __device__ __forceinline__ void run(int x0, int, typename P::Args a, uint32_t n, uint32_t* __restrict__ chunk_count) {
   // x0 = block index * kBlock1D: one chunk per block.
   const uint32_t chunk = (uint32_t)x0 / kBlock1D;
-  const uint32_t first = chunk * kCompactChunk + threadIdx.x * kCompactPer;
+  const uint32_t first = chunk * kCompactChunk + threadIdx.x;
   uint32_t c = 0;
 #pragma unroll
-  for (uint32_t k = 0; k < kCompactPer; ++k) {
-    const uint32_t i = first + k;
+  for (uint32_t r = 0; r < kCompactRounds; ++r) {
+    const uint32_t i = first + r * kBlock1D;
     if (i < n && P::flag(a, i)) ++c;
   }
   for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
@@ -79,33 +81,39 @@ struct CompactScanF {
 template <class P>
 struct CompactScatterF {
   static __device__ __forceinline__ void run(int x0, int, typename P::Args a, uint32_t n, const uint32_t* __restrict__ chunk_offset) {
+  constexpr uint32_t kWarps = kBlock1D / 32;
   const uint32_t chunk = (uint32_t)x0 / kBlock1D;
-  const uint32_t first = chunk * kCompactChunk + threadIdx.x * kCompactPer;
+  const uint32_t first = chunk * kCompactChunk + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-  uint32_t flags = 0;
+  // Each round's flags as one ballot per warp; the flagged-item counts of every
+  // (round, warp) in shared memory give each item's rank in item order.
+  __shared__ uint32_t cnt[kCompactRounds][kWarps];
+  uint32_t mine = 0;  // bit r: this thread's item of round r is flagged
 #pragma unroll
-  for (uint32_t k = 0; k < kCompactPer; ++k) {
-    const uint32_t i = first + k;
-    if (i < n && P::flag(a, i)) flags |= 1u << k;
+  for (uint32_t r = 0; r < kCompactRounds; ++r) {
+    const uint32_t i = first + r * kBlock1D;
+    const bool f = i < n && P::flag(a, i);
+    const uint32_t b = __ballot_sync(0xFFFFFFFFu, f);
+    if (f) mine |= 1u << r;
+    if (lane == 0) cnt[r][wid] = (uint32_t)__popc(b);
   }
-  // Rank of the thread's first flagged item: the chunk's offset, the flagged items of
-  // the warps before this one and of the lanes before this one (one scan per chunk).
-  const uint32_t c = (uint32_t)__popc(flags);
-  uint32_t incl = c;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-    if (lane >= (uint32_t)o) incl += v;
-  }
-  __shared__ uint32_t warp_sum[kBlock1D / 32];
-  if (lane == 31u) warp_sum[wid] = incl;
   __syncthreads();
-  uint32_t rank = chunk_offset[chunk] + incl - c;
-  for (uint32_t w = 0; w < wid; ++w) rank += warp_sum[w];
+  const uint32_t lt = (1u << lane) - 1u;  // lanes before this one
+  uint32_t base = chunk_offset[chunk];
 #pragma unroll
-  for (uint32_t k = 0; k < kCompactPer; ++k)
-    if (flags & (1u << k)) P::emit(a, first + k, rank++);
-  __syncthreads();  // warp_sum is reused by the block's next chunk (persistent launches)
+  for (uint32_t r = 0; r < kCompactRounds; ++r) {
+    uint32_t before = 0, all = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kWarps; ++w) {
+      const uint32_t c = cnt[r][w];
+      before += w < wid ? c : 0u;
+      all += c;
+    }
+    const uint32_t b = __ballot_sync(0xFFFFFFFFu, (mine >> r) & 1u);
+    if ((mine >> r) & 1u) P::emit(a, first + r * kBlock1D, base + before + (uint32_t)__popc(b & lt));
+    base += all;
+  }
+  __syncthreads();  // cnt is reused by the block's next chunk (persistent launches)
 }
 };
 
