@@ -26,7 +26,20 @@ namespace vlt {
 
 // --------------------------------------------------------------- emission
 
+// V8: the query buffer is 32-byte aligned and each record is written with one
+// 256-bit store (the frame driver's buffers always are; the per-pass entry point
+// checks the caller's pointer).
+template <bool V8>
 struct HgEmitF {
+  static __device__ __forceinline__ void store(uint32_t* __restrict__ queries, uint32_t q, uint4 a, uint4 b) {
+    if (V8) {
+      st_rec32(queries + (size_t)q * Q_WORDS, a, b);
+    } else {
+      uint4* rec = (uint4*)(queries + (size_t)q * Q_WORDS);
+      rec[0] = a;
+      rec[1] = b;
+    }
+  }
   static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, uint32_t bucket_mask, uint32_t key_mode, uint32_t max_q, const float* __restrict__ depth, const uint2* __restrict__ hpn, const uint32_t* __restrict__ rad, uint32_t* __restrict__ queries, uint32_t* __restrict__ count) {
   int x = x0 + (int)threadIdx.x, y = y0 + (int)threadIdx.y;
   if (!inb(x, y, w, h)) return;
@@ -36,18 +49,16 @@ struct HgEmitF {
     *count = n < max_q ? n : max_q;
   }
   if (q >= max_q) return;
-  uint4* rec = (uint4*)(queries + (size_t)q * Q_WORDS);
   if (depth[q] == 0.0f) {
-    rec[0] = make_uint4(0u, 0u, 0u, 0u);
-    rec[1] = make_uint4(0u, 0u, 0u, 0u);
+    store(queries, q, make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u));
     return;
   }
   uint2 e = hpn[q];
   f3 pos = hpn_pos(e.x, e.y);
   f3 nrm = hpn_normal(e.y);
   VertexKey k = vertex_key(pos, nrm, mk3(fp.view_pos[0], fp.view_pos[1], fp.view_pos[2]), bucket_mask, key_mode);
-  rec[0] = make_uint4(as_uint(pos.x), as_uint(pos.y), as_uint(pos.z), normal_encode_oct_u32(nrm));
-  rec[1] = make_uint4(k.hash, k.checksum, rad[q], 0u);
+  store(queries, q, make_uint4(as_uint(pos.x), as_uint(pos.y), as_uint(pos.z), normal_encode_oct_u32(nrm)),
+        make_uint4(k.hash, k.checksum, rad[q], 0u));
 }
 };
 
@@ -470,8 +481,12 @@ void launch_hg_visualize(const Exec& ex, const vlt_frame_params& fp, int w, int 
 void launch_hg_emit(const Exec& ex, const vlt_frame_params& fp, int w, int h, const HashGridDims& d,
                     uint32_t key_mode, const float* depth, const uint32_t* hpn, const uint32_t* rad,
                     uint32_t* queries, uint32_t* count) {
-  launch2d<HgEmitF>(ex, "hg_emit", w, h, fp, w, h, d.num_buckets() - 1u, key_mode, d.max_queries, depth,
-                    (const uint2*)hpn, rad, queries, count);
+  if (((uintptr_t)queries & 31u) == 0)
+    launch2d<HgEmitF<true>>(ex, "hg_emit", w, h, fp, w, h, d.num_buckets() - 1u, key_mode, d.max_queries, depth,
+                            (const uint2*)hpn, rad, queries, count);
+  else
+    launch2d<HgEmitF<false>>(ex, "hg_emit", w, h, fp, w, h, d.num_buckets() - 1u, key_mode, d.max_queries, depth,
+                             (const uint2*)hpn, rad, queries, count);
 }
 
 void launch_hg_decay(const Exec& ex, const HashGridDims& d, uint8_t* decay, uint32_t* storage) {

@@ -193,10 +193,9 @@ __device__ __forceinline__ Traced trace_shade(const vlt_frame_params& fp, const 
   return t;
 }
 
+// The staging buffer is the view's own (256-byte aligned): one 256-bit store per record.
 __device__ __forceinline__ void query_store(uint32_t* __restrict__ staging, size_t i, const uint32_t q[8]) {
-  uint4* r = (uint4*)(staging + i * 8);
-  r[0] = make_uint4(q[0], q[1], q[2], q[3]);
-  r[1] = make_uint4(q[4], q[5], q[6], q[7]);
+  st_rec32(staging + i * 8, make_uint4(q[0], q[1], q[2], q[3]), make_uint4(q[4], q[5], q[6], q[7]));
 }
 
 }  // namespace vlt
