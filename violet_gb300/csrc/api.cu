@@ -885,11 +885,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     exs.stream = v->aux[1];
     exa.stream = v->aux[2];
   }
-  if (conc) {
-    exh.stream = v->aux[0];
-    cudaEventRecord(v->ev[0], s);
-    cudaStreamWaitEvent(v->aux[0], v->ev[0], 0);
-  }
+  if (conc) exh.stream = v->aux[0];
 
   // Surface attributes of this frame, decoded once (the previous frame's planes
   // stay in the other slot).
@@ -919,15 +915,20 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
 
   // Hash-grid radiance cache: decay, then (with history) select/compact/update of
   // last frame's queries, then this frame's queries. In traced mode the first three
-  // ran in vlt_frame_trace; the update shades the traced hits.
-  if (P.hg_enable && P.hg_decay && !traced) {
-    STAGE("hg_decay", launch_hg_decay(exh, v->hg, b.hg_decay, b.hg_storage));
-  }
+  // ran in vlt_frame_trace; the update shades the traced hits. On a side stream the
+  // chain starts when the denoiser does (below): it reads only the frame's inputs
+  // and the grid, and its short, latency-bound launches fill the SM slots that the
+  // denoiser's serial passes leave idle at their tails.
+  uint32_t seed_select = 0u;
   if (has_prev) {
-    uint32_t seed_select = fr.next();
-    uint32_t seed_update = fr.next();  // the cache rays (vlt_frame_trace)
-    (void)seed_update;
-    if (P.hg_enable && !traced) {
+    seed_select = fr.next();
+    (void)fr.next();  // the cache rays (vlt_frame_trace)
+  }
+  auto hg_chain = [&]() {
+    if (P.hg_enable && P.hg_decay && !traced) {
+      STAGE("hg_decay", launch_hg_decay(exh, v->hg, b.hg_decay, b.hg_storage));
+    }
+    if (has_prev && P.hg_enable && !traced) {
       ex_fill32(exh, b.hg_sel, 0u, (size_t)v->hg.num_cells() * 4);
       STAGE("hg_select", launch_hg_select(exh, v->hg, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur], b.hg_storage,
                                           b.hg_sel, seed_select, b.hg_scratch));
@@ -936,16 +937,19 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
                                           b.hg_storage, b.hg_decay));
       v->hg_qcur ^= 1;
     }
+    if (P.hg_enable && !traced) {
+      STAGE("hg_emit", launch_hg_emit(exh, fp, w, h, v->hg, P.hg_key_mode, in->depth, in->diff_hit_pos_normal,
+                                      in->diff_hit_radiance, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur]));
+    }
+  };
+  if (!conc) hg_chain();
+  if (has_prev) {
     if (traced && v->trace_cache) {
       STAGE("shade_cache", launch_shade_cache(ex, fp, nq, b.hg_ccount, v->trace_rays[0], in->cache_hits, scache, wcache,
                                               b.cache_rad, b.q_staging));
       STAGE("hg_update", launch_update_traced(ex, nq, b.hg_ccount, b.hg_caddr, b.cache_rad, b.hg_storage,
                                               b.hg_decay));
     }
-  }
-  if (P.hg_enable && !traced) {
-    STAGE("hg_emit", launch_hg_emit(exh, fp, w, h, v->hg, P.hg_key_mode, in->depth, in->diff_hit_pos_normal,
-                                    in->diff_hit_radiance, b.hg_queries[v->hg_qcur], b.hg_qcount[v->hg_qcur]));
   }
   // Ind. Diff. Sample Gen. (no seed on validation frames, restir_renderer.rs:460-494)
   if (!diff_validation) (void)fr.next();
@@ -1047,6 +1051,11 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     cudaStreamWaitEvent(s, v->ev[2], 0);
   }
   if (lanes) record_marker(ex, kMarkJoin + 2);
+  if (conc) {
+    cudaEventRecord(v->ev[0], s);
+    cudaStreamWaitEvent(v->aux[0], v->ev[0], 0);
+    hg_chain();
+  }
 
   // Denoiser.
   const bool run_denoiser = P.denoise && has_prev;
