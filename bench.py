@@ -349,7 +349,6 @@ def run_ours(args, ws, rank, local):
         scene.generate_device(f, bufs, sh)
         frames.append(bufs)
         fps.append(scene.frame_params(f))
-    in_bytes = sum(v.numel() for v in frames[0].values())
     out_px = 16 if FORM == "f32" else 4
     out = {k: torch.empty(n * out_px, dtype=torch.uint8, device=dev) for k in ("diffuse", "specular")}
     ctx = vg.Context(local)
@@ -461,26 +460,37 @@ def run_ours(args, ws, rank, local):
                          "alg_gbs": (b * nl / (tot / 1e3) / 1e9) if tot > 0 and b else None}
 
     # ---- end to end through the C ABI with host buffers
+    # Each frame's inputs sit in one pinned host buffer and go up with one copy; the
+    # outputs come back with one copy; vlt_frame_run gets pointers bound once per
+    # staging slot. Frames are pipelined over two slots: the copy stream uploads frame
+    # f+2's inputs and reads back frame f's outputs while the compute stream runs
+    # frame f+1. Every frame's upload and read-back is inside the timed region.
+    keys = list(frames[0].keys())
+    sizes = [frames[0][k].numel() for k in keys]
+    offs, tot_in = [], 0
+    for sz in sizes:  # each input 256-byte aligned inside the slot
+        offs.append(tot_in)
+        tot_in += (sz + 255) // 256 * 256
     host = []
     for f in range(nframes):
-        host.append({k: torch.empty(v.numel(), dtype=torch.uint8, pin_memory=True).copy_(v) for k, v in
-                     frames[f].items()})
-    out_host = {k: torch.empty(n * out_px, dtype=torch.uint8, pin_memory=True) for k in ("diffuse", "specular")}
+        hf = torch.empty(tot_in, dtype=torch.uint8, pin_memory=True)
+        for k, o, sz in zip(keys, offs, sizes):
+            hf[o:o + sz].copy_(frames[f][k])
+        host.append(hf)
+    out_bytes = n * out_px
+    out_host = torch.empty(2 * out_bytes, dtype=torch.uint8, pin_memory=True)
     view.reset(sh)
-    # Frames are pipelined over two staging slots: the copy stream uploads frame f+2's
-    # inputs and reads back frame f's outputs while the compute stream runs frame
-    # f+1. Every frame's upload and read-back is inside the timed region.
     copy_stream = torch.cuda.Stream(device=dev)
-    stage2 = [{k: torch.empty_like(v) for k, v in frames[0].items()} for _ in range(2)]
-    out2 = [{k: torch.empty(n * out_px, dtype=torch.uint8, device=dev) for k in ("diffuse", "specular")}
-            for _ in range(2)]
+    stage = [torch.empty(tot_in, dtype=torch.uint8, device=dev) for _ in range(2)]
+    outd = [torch.empty(2 * out_bytes, dtype=torch.uint8, device=dev) for _ in range(2)]
+    bind = [vg.FrameBinding({k: stage[s_][o:o + sz] for k, o, sz in zip(keys, offs, sizes)},
+                            {"diffuse": outd[s_][:out_bytes], "specular": outd[s_][out_bytes:]}) for s_ in range(2)]
     ready = [torch.cuda.Event() for _ in range(2)]
     done = [torch.cuda.Event() for _ in range(2)]
 
     def upload(f, slot):
         with torch.cuda.stream(copy_stream):
-            for k, v in host[f].items():
-                stage2[slot][k].copy_(v, non_blocking=True)
+            stage[slot].copy_(host[f], non_blocking=True)
             ready[slot].record(copy_stream)
 
     def e2e_frames(f0, f1):
@@ -490,12 +500,11 @@ def run_ours(args, ws, rank, local):
         for f in range(f0, f1):
             s = f % 2
             stream.wait_event(ready[s])
-            view.run(fps[f], f, stage2[s], out2[s], sh)
+            view.run_bound(bind[s], fps[f], f, sh)
             done[s].record(stream)
             copy_stream.wait_event(done[s])
             with torch.cuda.stream(copy_stream):
-                for k in out_host:
-                    out_host[k].copy_(out2[s][k], non_blocking=True)
+                out_host.copy_(outd[s], non_blocking=True)
             if f + 2 < f1:
                 upload(f + 2, s)
 
@@ -570,7 +579,7 @@ def run_ours(args, ws, rank, local):
                        "parallelism": "replicas" if ws > 1 else "single view",
                        "l2": "inputs+state per frame > L2 (distinct frames, no flush)",
                        "knobs": {k: getattr(params, k) for k, _ in params._fields_}},
-            "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": in_bytes,
+            "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": tot_in,
                     "d2h_bytes_per_step": 2 * out_px * n},
             "ref_storage_form": {"value": value_ref, "unit": "Mpix/s", "ms_per_step": ms_ref / args.steps},
             "gpu_launches": launches,

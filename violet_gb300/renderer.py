@@ -84,6 +84,15 @@ def _frame_structs(frame_params, frame_index, inputs, outputs):
     return fi, fo
 
 
+class FrameBinding:
+    """The input and output pointers of vlt_frame_run bound once, for buffers that are
+    reused frame after frame (staging slots); View.run_bound fills in the frame."""
+
+    def __init__(self, inputs, outputs=None):
+        self.fi, self.fo = _frame_structs(_ffi.FrameParams(), 0, inputs, outputs)
+        self._keep = (inputs, outputs)  # the buffers must outlive the binding
+
+
 class View:
     """Resident per-view state and the per-frame pass sequence (vlt_frame_run)."""
 
@@ -111,6 +120,13 @@ class View:
         fi, fo = _frame_structs(frame_params, frame_index, inputs, outputs)
         _ffi.check(self._lib.vlt_frame_run(self.handle, C.byref(fi), C.byref(fo), C.c_void_p(stream)),
                    "vlt_frame_run")
+
+    def run_bound(self, binding, frame_params, frame_index, stream=0):
+        """vlt_frame_run with the pointers of a FrameBinding."""
+        binding.fi.params = C.pointer(frame_params)
+        binding.fi.frame_index = int(frame_index) & 0xFFFFFFFF
+        _ffi.check(self._lib.vlt_frame_run(self.handle, C.byref(binding.fi), C.byref(binding.fo),
+                                           C.c_void_p(stream)), "vlt_frame_run")
 
     def trace(self, frame_params, frame_index, inputs, rays, stream=0):
         """Phase one of a traced frame (params.trace = 1): fills the device ray arrays
