@@ -2006,10 +2006,12 @@ void dn32_fallback(int w, int h, const float* depth_tex, const uint32_t* gbuf, c
 
 // svgf_atrous_filter.hlsl:23-88 (off-axis taps only, as the reference's loop
 // condition selects). out_diff / out_spec: float4 {rgb, 0}.
-template <int FORM>
+// FI / FO: the record layout read / written (1 f32, 2 f16), FL: the outputs'. The f16
+// form keeps its iterations between the first and the last in f32 records.
+template <int FI, int FO, int FL>
 void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, const void* in, void* out,
                  void* out_diff, void* out_spec, int step) {
-  using IO = Dio<FORM>;
+  using IO = Dio<FI>;
   const float kernel_weights[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
   ROWS_PARALLEL
   for (int y = 0; y < h; ++y)
@@ -2055,9 +2057,9 @@ void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, con
       float2 inv = F2(1.0f / wsum.x, 1.0f / wsum.y);
       float3 dd = dsum * inv.x, sd = ssum * inv.y;
       float2 vd = F2(vsum.x * inv.x * inv.x, vsum.y * inv.y * inv.y);
-      if (out) IO::store(out, i, dd, sd, vd);
-      if (out_diff) IO::out(out_diff, i, dd);
-      if (out_spec) IO::out(out_spec, i, sd);
+      if (out) Dio<FO>::store(out, i, dd, sd, vd);
+      if (out_diff) Dio<FL>::out(out_diff, i, dd);
+      if (out_spec) Dio<FL>::out(out_spec, i, sd);
     }
 }
 
@@ -2070,10 +2072,10 @@ void dn32_atrous(int w, int h, const float* depth_tex, const uint32_t* gbuf, con
 // a-trous against the reference's formulas (the float forms themselves evaluate the
 // weight in base 2 with a short polynomial and fused multiply-adds, which changes
 // the weights by a few units in the last place).
-template <int FORM>
+template <int FI, int FO, int FL>
 void dn32_atrous_refw(int w, int h, const float* depth_tex, const uint32_t* gbuf, const void* in, void* out,
                       void* out_diff, void* out_spec, int step) {
-  using IO = Dio<FORM>;
+  using IO = Dio<FI>;
   const float kernel_weights[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
   ROWS_PARALLEL
   for (int y = 0; y < h; ++y)
@@ -2110,9 +2112,9 @@ void dn32_atrous_refw(int w, int h, const float* depth_tex, const uint32_t* gbuf
       }
       float3 dd = diff_sum / weight_sum.x, sd = spec_sum / weight_sum.y;
       float2 vd = variance_sum / (weight_sum * weight_sum);
-      if (out) IO::store(out, i, dd, sd, vd);
-      if (out_diff) IO::out(out_diff, i, dd);
-      if (out_spec) IO::out(out_spec, i, sd);
+      if (out) Dio<FO>::store(out, i, dd, sd, vd);
+      if (out_diff) Dio<FL>::out(out_diff, i, dd);
+      if (out_spec) Dio<FL>::out(out_spec, i, sd);
     }
 }
 
@@ -3324,21 +3326,36 @@ void frame_run(OView& v, const vlt_frame_inputs& in, const vlt_frame_outputs* ou
     v.denoiser_history = true;
     if (f32) dn32_fallback<1>(w, h, in.depth, in.gbuffer, v.fhist_len.data(), v.fhist_rec.data(), v.ffallback.data());
     else dn32_fallback<2>(w, h, in.depth, in.gbuffer, v.fhist_len.data(), v.fhist_rec.data(), v.ffallback.data());
-    std::vector<uint8_t> a(v.ffallback), b(rb * n);
+    std::vector<uint8_t> a(v.ffallback), b;
     uint32_t iters = std::min(P.atrous_iterations, 5u);
+    // The f16 form keeps the iterations between the first and the last in f32
+    // records; its first reads, and its last writes, its own 16-byte records.
+    bool a_f32 = f32;
     for (uint32_t k = 0; k < iters; ++k) {
       bool last = k + 1 == iters;
       void* od = last && out ? out->diffuse : nullptr;
       void* os = last && out ? out->specular : nullptr;
+      const bool b_f32 = f32 || !last;
+      b.assign((b_f32 ? 32 : 16) * n, 0);
+      const int sel = (a_f32 ? 2 : 0) + (b_f32 ? 1 : 0);
+      const int st = 1 << k;
+      const float* dt = in.depth;
+      const uint32_t* gb = in.gbuffer;
       if (v.atrous_reference_weights) {
-        if (f32) dn32_atrous_refw<1>(w, h, in.depth, in.gbuffer, a.data(), b.data(), od, os, 1 << k);
-        else dn32_atrous_refw<2>(w, h, in.depth, in.gbuffer, a.data(), b.data(), od, os, 1 << k);
-      } else if (f32) {
-        dn32_atrous<1>(w, h, in.depth, in.gbuffer, a.data(), b.data(), od, os, 1 << k);
+        if (f32) dn32_atrous_refw<1, 1, 1>(w, h, dt, gb, a.data(), b.data(), od, os, st);
+        else if (sel == 3) dn32_atrous_refw<1, 1, 2>(w, h, dt, gb, a.data(), b.data(), od, os, st);
+        else if (sel == 2) dn32_atrous_refw<1, 2, 2>(w, h, dt, gb, a.data(), b.data(), od, os, st);
+        else if (sel == 1) dn32_atrous_refw<2, 1, 2>(w, h, dt, gb, a.data(), b.data(), od, os, st);
+        else dn32_atrous_refw<2, 2, 2>(w, h, dt, gb, a.data(), b.data(), od, os, st);
       } else {
-        dn32_atrous<2>(w, h, in.depth, in.gbuffer, a.data(), b.data(), od, os, 1 << k);
+        if (f32) dn32_atrous<1, 1, 1>(w, h, dt, gb, a.data(), b.data(), od, os, st);
+        else if (sel == 3) dn32_atrous<1, 1, 2>(w, h, dt, gb, a.data(), b.data(), od, os, st);
+        else if (sel == 2) dn32_atrous<1, 2, 2>(w, h, dt, gb, a.data(), b.data(), od, os, st);
+        else if (sel == 1) dn32_atrous<2, 1, 2>(w, h, dt, gb, a.data(), b.data(), od, os, st);
+        else dn32_atrous<2, 2, 2>(w, h, dt, gb, a.data(), b.data(), od, os, st);
       }
       a.swap(b);
+      a_f32 = b_f32;
     }
     if (iters == 0 && out) {  // the diffuse / specular halves of the fallback records
       const size_t half = rb / 2;

@@ -91,6 +91,7 @@ struct ViewBuffers {
   // fix output, temporal output / a-trous ping-pong, a-trous ping-pong, fallback output
   float4* rec[5];
   float4* rec_fast[2];
+  float4* atr32[2];        // f16 form: f32 records of the a-trous iterations between the first and the last
   uint32_t* hg_storage;
   uint8_t* hg_decay;
   uint32_t* hg_queries[2];
@@ -218,6 +219,8 @@ size_t layout(vlt_view* v, char* base) {
   if (f32 || f16) {
     const size_t rb = f32 ? 32 : 16;
     for (int k = 0; k < 5; ++k) b.rec[k] = (float4*)take(rb * n);
+    if (f16 && v->p.atrous_iterations > 1)
+      for (int k = 0; k < 2; ++k) b.atr32[k] = (float4*)take(32 * n);
     for (int k = 0; k < 2; ++k) b.rec_fast[k] = (float4*)take(fast ? rb * n : rb);
   } else {
     b.ray_len = (uint16_t*)take(2 * n);
@@ -1095,14 +1098,21 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     float4* rsrc = b.rec[4];
     float4* rdst = b.rec[2];
     const uint32_t iters = P.atrous_iterations;
+    // f16 form: the iterations between the first and the last keep f32 records
+    // (atr32); the last record, read by the final lighting or the next traced frame,
+    // is the form's own (rec[3]).
+    bool src_f32 = false;
     for (uint32_t k = 0; k < iters; ++k) {
       bool last = k + 1 == iters;
       void* od = last && out ? out->diffuse : nullptr;
       void* os = last && out ? out->specular : nullptr;
+      const bool dst_f32 = f16 && !last;
+      if (f16) rdst = last ? b.rec[3] : b.atr32[k & 1];
       void* ro = last && !keep_den ? nullptr : (void*)rdst;
-      STAGE("dn_atrous", launch_dn32_atrous(ex, form, w, h, ga, rsrc, ro, od, os, 1 << k));
+      STAGE("dn_atrous", launch_dn32_atrous(ex, form, w, h, ga, rsrc, ro, od, os, 1 << k, src_f32, dst_f32));
       rsrc = rdst;
-      rdst = rdst == b.rec[2] ? b.rec[3] : b.rec[2];
+      src_f32 = dst_f32;
+      if (!f16) rdst = rdst == b.rec[2] ? b.rec[3] : b.rec[2];
     }
     den = keep_den ? (const void*)rsrc : nullptr;
     if (iters == 0 && out && (out->diffuse || out->specular)) {

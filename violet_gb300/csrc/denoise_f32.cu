@@ -632,9 +632,9 @@ struct AtrousDist {
 // svgf_atrous_filter.hlsl:23-88: 5x5 taps at `step`, kernel weights {1, 2/3, 1/6},
 // off-axis taps only (the reference's loop condition), variance filtered with w^2.
 // CHECK = false is the path of blocks whose whole 5x5 footprint is inside the image.
-template <bool CHECK, class Geo, class R, class L>
+template <bool CHECK, class Geo, class RI, class RO, class L>
 __device__ __forceinline__ void atrous_px(int x, int y, int w, int h, const Geo& geo, AtrousDist td,
-                                          const R* __restrict__ in, R* __restrict__ out, L* __restrict__ out_diff,
+                                          const RI* __restrict__ in, RO* __restrict__ out, L* __restrict__ out_diff,
                                           L* __restrict__ out_spec, int step) {
   size_t i = (size_t)y * w + x;
   Rec c = load_rec(in, i);
@@ -683,13 +683,15 @@ __device__ __forceinline__ void atrous_px(int x, int y, int w, int h, const Geo&
   if (out_spec) st_out(out_spec, i, sd);
 }
 
-template <class Geo, int FORM>
+// Records in (RI) and out (RO): float4 (32-byte f32 records) or uint4 (16-byte f16
+// records); outputs L. The f16 form reads its fallback record in the first iteration,
+// keeps the iterations between in f32 records, and writes its last record (when one
+// is read afterwards) in its own f16 layout.
+template <class Geo, class RI, class RO, class L>
 struct Dn32AtrousF {
   static constexpr int kMinBlocks = 4;  // 64 registers, 8 tiles per SM (measured best of 2..8)
   static constexpr int kTileX = 32, kTileY = 8;  // measured 5% faster than 32x4
-  using R = typename DnT<FORM>::R;
-  using L = typename DnT<FORM>::L;
-  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, AtrousDist td, const R* __restrict__ in, R* __restrict__ out, L* __restrict__ out_diff, L* __restrict__ out_spec, int step) {
+  static __device__ __forceinline__ void run(int x0, int y0, int w, int h, Geo geo, AtrousDist td, const RI* __restrict__ in, RO* __restrict__ out, L* __restrict__ out_diff, L* __restrict__ out_spec, int step) {
   const int m = 2 * step;
   const bool interior = x0 - m >= 0 && y0 - m >= 0 && x0 + (int)blockDim.x - 1 + m <= w - 1 &&
                         y0 + (int)blockDim.y - 1 + m <= h - 1;
@@ -777,13 +779,19 @@ void launch_dn32_fallback(const Exec& ex, int form, int w, int h, const GeoArgs&
 }
 
 void launch_dn32_atrous(const Exec& ex, int form, int w, int h, const GeoArgs& ga, const void* in, void* out,
-                        void* out_diff, void* out_spec, int step) {
+                        void* out_diff, void* out_spec, int step, bool in_f32, bool out_f32) {
   const float s1 = (float)step, s2 = (float)(2 * step);
   AtrousDist td = {sqrtf(s1 * s1 + s1 * s1), sqrtf(s1 * s1 + s2 * s2), sqrtf(s2 * s2 + s2 * s2)};
-  VLT_FORM_DISPATCH(form, VLT_GEO_DISPATCH(ga, (launch2d<Dn32AtrousF<Geo, F>>(
-                                                   ex, "dn_atrous", w, h, w, h, geo, td, (const typename T::R*)in,
-                                                   (typename T::R*)out, (typename T::L*)out_diff,
-                                                   (typename T::L*)out_spec, step))));
+#define VLT_ATROUS(RI, RO, L)                                                                              \
+  VLT_GEO_DISPATCH(ga, (launch2d<Dn32AtrousF<Geo, RI, RO, L>>(ex, "dn_atrous", w, h, w, h, geo, td,          \
+                                                              (const RI*)in, (RO*)out, (L*)out_diff,        \
+                                                              (L*)out_spec, step)))
+  if (form != FORM_F16) VLT_ATROUS(float4, float4, float4);
+  else if (in_f32 && out_f32) VLT_ATROUS(float4, float4, uint2);
+  else if (in_f32) VLT_ATROUS(float4, uint4, uint2);
+  else if (out_f32) VLT_ATROUS(uint4, float4, uint2);
+  else VLT_ATROUS(uint4, uint4, uint2);
+#undef VLT_ATROUS
 }
 
 #undef VLT_FORM_DISPATCH

@@ -86,8 +86,11 @@ void launch_dn32_fix(const Exec& ex, int form, int w, int h, const GeoArgs& ga, 
 void launch_dn32_fast_clamp(const Exec& ex, int form, int w, int h, const void* fast, void* rec);
 void launch_dn32_fallback(const Exec& ex, int form, int w, int h, const GeoArgs& ga, const void* len, const void* in,
                           void* out);
+// in_f32 / out_f32: the f16 form's records in and out are 32-byte f32 records (its
+// iterations between the first and the last) instead of its 16-byte records; the
+// f32 form ignores them.
 void launch_dn32_atrous(const Exec& ex, int form, int w, int h, const GeoArgs& ga, const void* in, void* out,
-                        void* out_diff, void* out_spec, int step);
+                        void* out_diff, void* out_spec, int step, bool in_f32, bool out_f32);
 
 // denoise.cu
 void launch_dn_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h, const DenoiseKnobs& kn,
