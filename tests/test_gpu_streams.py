@@ -113,3 +113,39 @@ def test_frame_captured_in_cuda_graph(ctx, form):
     finally:
         direct.close()
         graphed.close()
+
+
+def test_bound_frame_pointers_match_run(ctx):
+    """View.run_bound (pointers bound once to a reused staging slot, as the benchmark's
+    end-to-end leg uses them) gives the frames View.run gives."""
+    import torch
+
+    W, H = 72, 40
+    n = W * H
+    p = params(0)
+    scene = vg.Scene(29, W, H, disocclusion_frac=0.02)
+    a = vg.View(ctx, W, H, "f32", p)
+    b = vg.View(ctx, W, H, "f32", p)
+    keys = [k for k in vg.FRAME_BUFFERS if k != "shadow_mask"]
+    first = scene.generate_host(0)
+    sizes = [first[k].nbytes for k in keys]
+    offs = [sum((sz + 255) // 256 * 256 for sz in sizes[:j]) for j in range(len(keys))]
+    slot = torch.zeros(offs[-1] + sizes[-1], dtype=torch.uint8, device="cuda")
+    out_b = torch.zeros(32 * n, dtype=torch.uint8, device="cuda")
+    bind = vg.FrameBinding({k: slot[o:o + sz] for k, o, sz in zip(keys, offs, sizes)},
+                           {"diffuse": out_b[:16 * n], "specular": out_b[16 * n:]})
+    try:
+        for f in range(4):
+            host = scene.generate_host(f)
+            fp = scene.frame_params(f)
+            out_a = {k: torch.zeros(16 * n, dtype=torch.uint8, device="cuda") for k in ("diffuse", "specular")}
+            a.run(fp, f, upload(host), out_a)
+            for k, o, sz in zip(keys, offs, sizes):
+                slot[o:o + sz].copy_(torch.from_numpy(host[k].view(np.uint8)))
+            b.run_bound(bind, fp, f)
+            torch.cuda.synchronize()
+            same_state(state_of(a), state_of(b), "frame %d" % f)
+            assert torch.equal(out_a["diffuse"], out_b[:16 * n]) and torch.equal(out_a["specular"], out_b[16 * n:])
+    finally:
+        a.close()
+        b.close()
