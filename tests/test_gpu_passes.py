@@ -262,6 +262,12 @@ def test_hash_grid_passes(world):
                                    vp(qc_g), None) == 0
     same(back(qc_g, 4, np.uint32), qc_o, "hg query count")
     same(back(q_g, 32 * N, np.uint32), q_o[: 8 * N], "hg queries")
+    # a query buffer that is not 32-byte aligned takes the 16-byte store path
+    q_u = Z(32 * mq + 16)
+    assert lib.vlt_hg_emit_queries(C.byref(fp), W, H, lb, 0, mq, vp(D(cur["depth"])),
+                                   vp(D(cur["diff_hit_pos_normal"])), vp(D(cur["diff_hit_radiance"])),
+                                   C.c_void_p(q_u.data_ptr() + 16), vp(qc_g), None) == 0
+    same(back(q_u[16:], 32 * N, np.uint32), q_o[: 8 * N], "hg queries (unaligned buffer)")
     # select
     sel_o = host(4 * nc, np.uint32)
     ol.vlto_hg_query_select(lb, mq, po.ptr(q_o), po.ptr(qc_o), po.ptr(storage), po.ptr(sel_o), 0xC0FFEE)
