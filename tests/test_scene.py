@@ -70,6 +70,22 @@ def test_jitter_is_the_halton_2_3_cycle_of_eight():
         assert np.isclose(p.jitter[1], (2 * _halton(k, 3) - 1) / H, atol=1e-9), f
 
 
+def test_reverse_z_projection():
+    # perspective_projection of app.rs:28-56 with near 0.05, far 102400: a point at
+    # view depth t on the principal axis (NDC x, y = the frame's jitter) has NDC depth
+    # m22 + m23 / t, 1 at the near plane and 0 at the far plane.
+    near, far = 0.05, 102400.0
+    m22, m23 = -near / (far - near), near / (1.0 - near / far)
+    s = vg.Scene(3, 320, 180)
+    p = s.frame_params(0)
+    ivp = np.array(p.inv_view_proj, np.float64).reshape(4, 4).T
+    cam = np.array(p.view_pos[:3], np.float64)
+    for t in (0.05, 0.5, 5.0, 50.0):
+        ndc = np.array([p.jitter[0], p.jitter[1], m22 + m23 / t, 1.0])
+        w = ivp @ ndc
+        assert np.isclose(np.linalg.norm(w[:3] / w[3] - cam), t, rtol=2e-5), t
+
+
 def test_host_only_generator_matches_the_product_library():
     """The oracle's copy of the scene generator (the product's source compiled without
     CUDA, used by the CPU benchmark) produces the same frames as the product library."""
