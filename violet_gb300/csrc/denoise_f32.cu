@@ -242,7 +242,9 @@ struct Centered {
 };
 __device__ __forceinline__ f2 lum2(f3 d, f3 s) { return mk2(lum_fast(d.x, d.y, d.z), lum_fast(s.x, s.y, s.z)); }
 
-template <class Geo, int FORM>
+// FAST: the fast history (fast_history_clamp) is kept; the launcher picks the
+// instantiation from the knob, so a frame without it carries none of its registers.
+template <class Geo, int FORM, bool FAST>
 struct Dn32TemporalF {
   static constexpr int kMinBlocks = 4;  // 64 registers instead of 96 (measured 20% faster)
   static constexpr bool kCentered = Centered<FORM>::value;
@@ -257,7 +259,7 @@ struct Dn32TemporalF {
   if (depth == 0.0f) {
     st_len(out_len, i, 0.0f);
     store_rec(out, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
-    if (kn.fast_history) store_rec(out_fast, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
+    if (FAST) store_rec(out_fast, i, mk3(0.0f), mk3(0.0f), mk2(0.0f, 0.0f));
     return;
   }
   const float bw = (float)w, bh = (float)h;
@@ -299,7 +301,7 @@ struct Dn32TemporalF {
       size_t a = (size_t)t.y0 * w + t.x0, b = (size_t)t.y0 * w + t.x1, c = (size_t)t.y1 * w + t.x0,
              d = (size_t)t.y1 * w + t.x1;
       vsh = bilerp3(load_rec(hist, a).s, load_rec(hist, b).s, load_rec(hist, c).s, load_rec(hist, d).s, t.fx, t.fy);
-      if (kn.fast_history)
+      if (FAST)
         vsfh = bilerp3(load_rec(fast_hist, a).s, load_rec(fast_hist, b).s, load_rec(fast_hist, c).s,
                        load_rec(fast_hist, d).s, t.fx, t.fy);
     }
@@ -360,7 +362,7 @@ struct Dn32TemporalF {
         hs = hs + wt * lj;
         ds = fma3(wt, r.d, ds);
         ss = fma3(wt, r.s, ss);
-        if (kn.fast_history) {
+        if (FAST) {
           Rec f = load_rec(fast_hist, j);
           dfs = fma3(wt, f.d, dfs);
           sfs = fma3(wt, f.s, sfs);
@@ -421,7 +423,7 @@ struct Dn32TemporalF {
     f3 dual = (wv * vsh + wh * sh) / fmax_(wv + wh, 1e-37f);
     if (kCentered) lum_dual = lum_fast(dual.x, dual.y, dual.z);
     sf = lerp3(dual, ssrc, alpha.y);
-    if (kn.fast_history) {
+    if (FAST) {
       float wv2 = dsr_weight_exact(vsfh, mean, dev);
       float wh2 = dsr_weight_exact(sfh, mean, dev);
       f3 dual2 = (wv2 * vsfh + wh2 * sfh) / fmax_(wv2 + wh2, 1e-37f);
@@ -435,7 +437,7 @@ struct Dn32TemporalF {
   }
   store_rec(out, i, df, sf, smf);
   st_len(out_len, i, hl);
-  if (kn.fast_history) store_rec(out_fast, i, dff, sff, mk2(0.0f, 0.0f));
+  if (FAST) store_rec(out_fast, i, dff, sff, mk2(0.0f, 0.0f));
 }
 };
 
@@ -741,22 +743,22 @@ void launch_dn32_temporal(const Exec& ex, int form, const vlt_frame_params& fp, 
   if (ga.nd) {
     GeoSurface geo = {ga.nd, ga.pr, ga.fz, w, h};
     GeoSurface pgeo = {prev_ga.nd, prev_ga.pr, prev_ga.fz, w, h};
-    VLT_FORM_DISPATCH(form, (launch2d<Dn32TemporalF<GeoSurface, F>>(
-                                ex, "dn_temporal", w, h, fp, w, h, kn, geo, pgeo, ga.gbuf,
-                                (const typename T::L*)diff_src, (const typename T::L*)spec_src, prev_depth,
-                                (const typename T::R*)hist, (const typename T::N*)len_hist,
-                                (const typename T::R*)fast_hist, (typename T::R*)out, (typename T::N*)out_len,
-                                (typename T::R*)out_fast, has_history)));
+#define VLT_DN_TEMPORAL(GEO, FASTV)                                                                 \
+  VLT_FORM_DISPATCH(form, (launch2d<Dn32TemporalF<GEO, F, FASTV>>(                                         \
+                              ex, "dn_temporal", w, h, fp, w, h, kn, geo, pgeo, ga.gbuf,                   \
+                              (const typename T::L*)diff_src, (const typename T::L*)spec_src, prev_depth,  \
+                              (const typename T::R*)hist, (const typename T::N*)len_hist,                  \
+                              (const typename T::R*)fast_hist, (typename T::R*)out, (typename T::N*)out_len, \
+                              (typename T::R*)out_fast, has_history)))
+    if (kn.fast_history) VLT_DN_TEMPORAL(GeoSurface, true);
+    else VLT_DN_TEMPORAL(GeoSurface, false);
   } else {
     GeoRaw geo = make_geo_raw(ga.depth, ga.gbuf, ga.inv_vp, w, h);
     GeoRaw pgeo = make_geo_raw(prev_ga.depth, prev_ga.gbuf, prev_ga.inv_vp, w, h);
-    VLT_FORM_DISPATCH(form, (launch2d<Dn32TemporalF<GeoRaw, F>>(
-                                ex, "dn_temporal", w, h, fp, w, h, kn, geo, pgeo, ga.gbuf,
-                                (const typename T::L*)diff_src, (const typename T::L*)spec_src, prev_depth,
-                                (const typename T::R*)hist, (const typename T::N*)len_hist,
-                                (const typename T::R*)fast_hist, (typename T::R*)out, (typename T::N*)out_len,
-                                (typename T::R*)out_fast, has_history)));
+    if (kn.fast_history) VLT_DN_TEMPORAL(GeoRaw, true);
+    else VLT_DN_TEMPORAL(GeoRaw, false);
   }
+#undef VLT_DN_TEMPORAL
 }
 
 void launch_dn32_fix(const Exec& ex, int form, int w, int h, const GeoArgs& ga, const void* len, const void* in,
