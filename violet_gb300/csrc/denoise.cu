@@ -69,7 +69,9 @@ __device__ __forceinline__ float dsr_weight(f3 color, f3 mean, f3 dev) {
 // --------------------------------------------------------------- temporal
 
 // svgf_temporal_filter.hlsl:96-362.
-template <class Geo>
+// FAST: the fast history (fast_history_clamp) is kept; the launcher picks the
+// instantiation from the knob, so a frame without it carries none of its registers.
+template <class Geo, bool FAST>
 struct DnTemporalF {
   static constexpr int kMinBlocks = 5;  // 51 registers instead of 80 (measured 14% faster)
   static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, DenoiseKnobs kn, Geo geo, Geo prev_geo, const uint32_t* __restrict__ gbuf, const uint32_t* __restrict__ diff_src, const uint32_t* __restrict__ spec_src, const uint16_t* __restrict__ ray_len_tex, const float* __restrict__ prev_depth, const uint2* __restrict__ color_hist, const uint32_t* __restrict__ mom_hist, const uint8_t* __restrict__ len_hist, const uint2* __restrict__ fast_hist, uint2* __restrict__ out_color, uint32_t* __restrict__ out_mom, uint8_t* __restrict__ out_len, uint2* __restrict__ out_fast, uint32_t has_history) {
@@ -81,7 +83,7 @@ struct DnTemporalF {
     out_len[i] = 0;
     out_color[i] = make_uint2(0u, 0u);
     out_mom[i] = 0u;
-    if (kn.fast_history) out_fast[i] = make_uint2(0u, 0u);
+    if (FAST) out_fast[i] = make_uint2(0u, 0u);
     return;
   }
   const float bw = (float)w, bh = (float)h;
@@ -126,7 +128,7 @@ struct DnTemporalF {
       uint2 a = color_hist[(size_t)t.y0 * w + t.x0], b = color_hist[(size_t)t.y0 * w + t.x1];
       uint2 c = color_hist[(size_t)t.y1 * w + t.x0], d = color_hist[(size_t)t.y1 * w + t.x1];
       vsh = bilerp3(col_spec(a), col_spec(b), col_spec(c), col_spec(d), t.fx, t.fy);
-      if (kn.fast_history) {
+      if (FAST) {
         uint2 fa = fast_hist[(size_t)t.y0 * w + t.x0], fb = fast_hist[(size_t)t.y0 * w + t.x1];
         uint2 fc = fast_hist[(size_t)t.y1 * w + t.x0], fd = fast_hist[(size_t)t.y1 * w + t.x1];
         vsfh = bilerp3(col_spec(fa), col_spec(fb), col_spec(fc), col_spec(fd), t.fx, t.fy);
@@ -185,7 +187,7 @@ struct DnTemporalF {
         ss = ss + wt * col_spec(c);
         ms = ms + wt * unpack_half2(mj);
         hs = hs + wt * unorm8_load(lj);
-        if (kn.fast_history) {
+        if (FAST) {
           uint2 f = fast_hist[j];
           dfs = dfs + wt * col_diff(f);
           sfs = sfs + wt * col_spec(f);
@@ -238,7 +240,7 @@ struct DnTemporalF {
     float ws = wv + wh;
     dual = dual / fmax_(ws, 1e-37f);
     sf = lerp3(dual, ssrc, alpha.y);
-    if (kn.fast_history) {
+    if (FAST) {
       float wv2 = dsr_weight(vsfh, mean, dev);
       float wh2 = dsr_weight(sfh, mean, dev);
       f3 dual2 = wv2 * vsfh + wh2 * sfh;
@@ -250,7 +252,7 @@ struct DnTemporalF {
   out_color[i] = make_uint2(pack_r11g11b10(df), pack_r11g11b10(sf));
   out_mom[i] = pack_half2(smf);
   out_len[i] = (uint8_t)unorm8_store(hl);
-  if (kn.fast_history) out_fast[i] = make_uint2(pack_r11g11b10(dff), pack_r11g11b10(sff));
+  if (FAST) out_fast[i] = make_uint2(pack_r11g11b10(dff), pack_r11g11b10(sff));
 }
 };
 
@@ -514,16 +516,19 @@ void launch_dn_temporal(const Exec& ex, const vlt_frame_params& fp, int w, int h
                         const uint32_t* mom_hist, const uint8_t* len_hist, const uint32_t* fast_hist,
                         uint32_t* out_color, uint32_t* out_mom, uint8_t* out_len, uint32_t* out_fast,
                         uint32_t has_history) {
-  if (ga.nd)
-    launch2d<DnTemporalF<GeoSurface>>(ex, "dn_temporal", w, h, fp, w, h, kn, surf_geo(ga, w, h),
-                                      surf_geo(prev_ga, w, h), ga.gbuf, diff_src, spec_src, ray_len, prev_depth,
-                                      (const uint2*)color_hist, mom_hist, len_hist, (const uint2*)fast_hist,
-                                      (uint2*)out_color, out_mom, out_len, (uint2*)out_fast, has_history);
-  else
-    launch2d<DnTemporalF<GeoRaw>>(ex, "dn_temporal", w, h, fp, w, h, kn, raw_geo(ga, w, h), raw_geo(prev_ga, w, h),
-                                  ga.gbuf, diff_src, spec_src, ray_len, prev_depth, (const uint2*)color_hist,
-                                  mom_hist, len_hist, (const uint2*)fast_hist, (uint2*)out_color, out_mom, out_len,
-                                  (uint2*)out_fast, has_history);
+#define VLT_DN_TEMPORAL(GEO, G, PG, FASTV)                                                                 \
+  launch2d<DnTemporalF<GEO, FASTV>>(ex, "dn_temporal", w, h, fp, w, h, kn, G, PG, ga.gbuf, diff_src, spec_src,     \
+                                    ray_len, prev_depth, (const uint2*)color_hist, mom_hist, len_hist,             \
+                                    (const uint2*)fast_hist, (uint2*)out_color, out_mom, out_len, (uint2*)out_fast, \
+                                    has_history)
+  if (ga.nd) {
+    if (kn.fast_history) VLT_DN_TEMPORAL(GeoSurface, surf_geo(ga, w, h), surf_geo(prev_ga, w, h), true);
+    else VLT_DN_TEMPORAL(GeoSurface, surf_geo(ga, w, h), surf_geo(prev_ga, w, h), false);
+  } else {
+    if (kn.fast_history) VLT_DN_TEMPORAL(GeoRaw, raw_geo(ga, w, h), raw_geo(prev_ga, w, h), true);
+    else VLT_DN_TEMPORAL(GeoRaw, raw_geo(ga, w, h), raw_geo(prev_ga, w, h), false);
+  }
+#undef VLT_DN_TEMPORAL
 }
 
 void launch_dn_fix(const Exec& ex, int w, int h, const GeoArgs& ga, const uint8_t* len, const uint32_t* color,
