@@ -516,10 +516,27 @@ def run_ours(args, ws, rank, local):
     e2e_frames(args.warmup, args.warmup + args.steps)
     e1.record(copy_stream)
     torch.cuda.synchronize()
-    e2e_ms = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3)
+    e2e_event_ms = e0.elapsed_time(e1)
+    e2e_wall_ms = (time.perf_counter() - t0) * 1e3
+    e2e_ms = max(e2e_event_ms, e2e_wall_ms)
     barrier(ws)
     e2e_ms = max_over_ranks(e2e_ms, ws, dev)
     e2e_value = ws * args.steps * n / (e2e_ms / 1e3) / 1e6
+    # The host link on its own, after the timed region: three uploads of one frame's
+    # packed inputs, then three read-backs of its outputs, on the copy stream.
+    l0, l1, l2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    with torch.cuda.stream(copy_stream):
+        l0.record(copy_stream)
+        for _ in range(3):
+            stage[0].copy_(host[0], non_blocking=True)
+        l1.record(copy_stream)
+        for _ in range(3):
+            out_host.copy_(outd[0], non_blocking=True)
+        l2.record(copy_stream)
+    torch.cuda.synchronize()
+    link = {"h2d_gbs": 3 * tot_in / (l0.elapsed_time(l1) / 1e3) / 1e9,
+            "d2h_gbs": 3 * out_host.numel() / (l1.elapsed_time(l2) / 1e3) / 1e9,
+            "definition": "pinned host <-> device copies alone on the copy stream, after the timed region"}
     view.close()
     ctx.close()
     del frames, host
@@ -580,7 +597,9 @@ def run_ours(args, ws, rank, local):
                        "l2": "inputs+state per frame > L2 (distinct frames, no flush)",
                        "knobs": {k: getattr(params, k) for k, _ in params._fields_}},
             "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": tot_in,
-                    "d2h_bytes_per_step": 2 * out_px * n},
+                    "d2h_bytes_per_step": 2 * out_px * n,
+                    "event_ms_per_step": e2e_event_ms / args.steps, "wall_ms_per_step": e2e_wall_ms / args.steps,
+                    "host_link": link},
             "ref_storage_form": {"value": value_ref, "unit": "Mpix/s", "ms_per_step": ms_ref / args.steps},
             "gpu_launches": launches,
             "roofline": roofline,
