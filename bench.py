@@ -391,6 +391,31 @@ def run_ours(args, ws, rank, local):
     value = ws * args.steps * n / (ms / 1e3) / 1e6
     view = vg.View(ctx, W, H, FORM, params)
 
+    # ---- the same frames as one pipelined sequence (vlt_frames_run: frame f's
+    # denoiser beside frame f + 1's resampling passes), device-resident
+    pipelined = None
+    if not args.no_pipelined:
+        pv = vg.View(ctx, W, H, FORM, params)
+        outs_p = [out] * nframes  # every frame writes the same output buffers, as above
+        warm = vg.FrameSequence(fps[:args.warmup], list(range(args.warmup)), frames[:args.warmup],
+                                outs_p[:args.warmup])
+        timed = vg.FrameSequence(fps[args.warmup:], list(range(args.warmup, nframes)), frames[args.warmup:],
+                                 outs_p[args.warmup:])
+        pv.run_sequence(warm, sh)
+        torch.cuda.synchronize()
+        barrier(ws)
+        e0.record(stream)
+        pv.run_sequence(timed, sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_p = max_over_ranks(e0.elapsed_time(e1), ws, dev)
+        barrier(ws)
+        pipelined = {"value": ws * args.steps * n / (ms_p / 1e3) / 1e6, "unit": "Mpix/s",
+                     "ms_per_step": ms_p / args.steps, "launches": pv.launches,
+                     "definition": "the same --steps frames as one vlt_frames_run call after --warmup frames "
+                                   "in another; results equal frame-by-frame vlt_frame_run"}
+        pv.close()
+
     # ---- per-pass timers (separate run: the event records cost a little time)
     view.reset(sh)
     for f in range(args.warmup):
@@ -601,6 +626,7 @@ def run_ours(args, ws, rank, local):
                     "event_ms_per_step": e2e_event_ms / args.steps, "wall_ms_per_step": e2e_wall_ms / args.steps,
                     "host_link": link},
             "ref_storage_form": {"value": value_ref, "unit": "Mpix/s", "ms_per_step": ms_ref / args.steps},
+            "pipelined": pipelined,
             "gpu_launches": launches,
             "roofline": roofline,
             "issue_roofline": issue,
@@ -1206,6 +1232,7 @@ def main():
     ap.add_argument("--no-traced", action="store_true")
     ap.add_argument("--precision-frames", type=int, default=64)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-pipelined", action="store_true")
     ap.add_argument("--fp64-frames", type=int, default=32)
     ap.add_argument("--fp64-width", type=int, default=960)
     ap.add_argument("--fp64-height", type=int, default=540)

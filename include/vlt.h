@@ -257,6 +257,19 @@ uint32_t vlt_view_cache_ray_capacity(const vlt_view* view);
 vlt_status vlt_frame_run(vlt_view* view, const vlt_frame_inputs* in, const vlt_frame_outputs* out,
                          void* stream);
 
+/* No counterpart in the reference (its renderer records one frame at a time; a GPU
+ * queue may still overlap consecutive frames where its barriers allow). Runs frames
+ * in[0..n) of one view in order (out may be NULL, else out[k] are frame k's
+ * outputs), with results identical to n vlt_frame_run calls. Frame k's denoiser
+ * runs on a side stream beside frame k + 1's resampling passes, which start once
+ * frame k's denoiser temporal pass has read the buffers they overwrite. Frames with
+ * final lighting or TAA (params.post > 0), with raw outputs requested, or with
+ * per-pass timers on run as vlt_frame_run runs them. All work is ordered on `stream`
+ * when the call returns. Every frame's inputs and outputs are validated before any
+ * runs; traced views are refused (VLT_ERR_INVALID_ARG). */
+vlt_status vlt_frames_run(vlt_view* view, uint32_t n, const vlt_frame_inputs* in, const vlt_frame_outputs* out,
+                          void* stream);
+
 /* The view's temporal state as one blob: every resident buffer (reservoirs, AO and
  * denoiser history, hash grid, retained depth, surface planes, TAA history) and the
  * slot bookkeeping, i.e. what RestirRenderer and Denoiser keep as RGTemporal handles

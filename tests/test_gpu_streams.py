@@ -149,3 +149,139 @@ def test_bound_frame_pointers_match_run(ctx):
     finally:
         a.close()
         b.close()
+
+
+def _seq_outputs(n, px, frames):
+    import torch
+
+    return [{k: torch.zeros(px * n, dtype=torch.uint8, device="cuda") for k in ("diffuse", "specular")}
+            for _ in range(frames)]
+
+
+@pytest.mark.parametrize("form", ["ref", "f32", "f16"])
+def test_frame_sequence_matches_frame_by_frame(ctx, form):
+    """vlt_frames_run (frame k's denoiser beside frame k + 1's resampling passes) gives
+    every frame's outputs and the final state that vlt_frame_run gives frame by frame,
+    across two sequence calls; a frame that asks for raw outputs in the middle runs
+    unpipelined (the side streams join first)."""
+    import torch
+
+    W, H = 96, 64
+    n = W * H
+    p = params(0)
+    scene = vg.Scene(31, W, H, disocclusion_frac=0.03)
+    a = vg.View(ctx, W, H, form, p)
+    b = vg.View(ctx, W, H, form, p)
+    px = OUT_PX[form]
+    try:
+        frames = [upload(scene.generate_host(f)) for f in range(11)]
+        fps = [scene.frame_params(f) for f in range(11)]
+        out_a = _seq_outputs(n, px, 11)
+        out_b = _seq_outputs(n, px, 11)
+        for f in (4, 9):  # raw outputs requested: these frames run unpipelined
+            for o in (out_a[f], out_b[f]):
+                o["raw_diffuse"] = torch.zeros(px * n, dtype=torch.uint8, device="cuda")
+                o["raw_specular"] = torch.zeros(px * n, dtype=torch.uint8, device="cuda")
+        for f in range(11):
+            a.run(fps[f], f, frames[f], out_a[f])
+        for lo, hi in ((0, 6), (6, 11)):
+            seq = vg.FrameSequence(fps[lo:hi], list(range(lo, hi)), frames[lo:hi], out_b[lo:hi])
+            b.run_sequence(seq)
+            assert b.launches > 0
+        torch.cuda.synchronize()
+        same_state(state_of(a), state_of(b), "after 11 frames")
+        for f in range(11):
+            for k in out_a[f]:
+                assert torch.equal(out_a[f][k], out_b[f][k]), "frame %d output %s" % (f, k)
+    finally:
+        a.close()
+        b.close()
+
+
+def test_frame_sequence_with_post_passes_and_graph(ctx):
+    """A view with final lighting and TAA runs its sequence frame by frame (equal to
+    vlt_frame_run); a pipelined sequence captured in a CUDA graph on the caller's
+    stream replays to the same results (the side streams join before the capture
+    ends)."""
+    import torch
+
+    W, H = 80, 48
+    n = W * H
+    scene = vg.Scene(37, W, H, disocclusion_frac=0.02)
+    frames = [upload(scene.generate_host(f)) for f in range(6)]
+    fps = [scene.frame_params(f) for f in range(6)]
+    # post passes: unpipelined inside the sequence
+    p2 = params(2)
+    a = vg.View(ctx, W, H, "f32", p2)
+    b = vg.View(ctx, W, H, "f32", p2)
+    try:
+        out_a = _seq_outputs(n, 16, 6)
+        out_b = _seq_outputs(n, 16, 6)
+        for f in range(6):
+            a.run(fps[f], f, frames[f], out_a[f])
+        b.run_sequence(vg.FrameSequence(fps, list(range(6)), frames, out_b))
+        torch.cuda.synchronize()
+        same_state(state_of(a), state_of(b), "post = 2")
+        for f in range(6):
+            for k in out_a[f]:
+                assert torch.equal(out_a[f][k], out_b[f][k]), "post = 2, frame %d output %s" % (f, k)
+    finally:
+        a.close()
+        b.close()
+    # captured: frames 0-2 directly, frames 3-5 as one captured sequence
+    p0 = params(0)
+    direct = vg.View(ctx, W, H, "f32", p0)
+    graphed = vg.View(ctx, W, H, "f32", p0)
+    s = torch.cuda.Stream()
+    try:
+        out_d = _seq_outputs(n, 16, 6)
+        out_g = _seq_outputs(n, 16, 6)
+        for f in range(6):
+            direct.run(fps[f], f, frames[f], out_d[f])
+        graphed.run_sequence(vg.FrameSequence(fps[:3], [0, 1, 2], frames[:3], out_g[:3]))
+        torch.cuda.synchronize()
+        seq = vg.FrameSequence(fps[3:], [3, 4, 5], frames[3:], out_g[3:])
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            graphed.run_sequence(seq, stream=s.cuda_stream)
+        g.replay()
+        torch.cuda.synchronize()
+        same_state(state_of(direct), state_of(graphed), "captured sequence")
+        for f in range(6):
+            for k in out_d[f]:
+                assert torch.equal(out_d[f][k], out_g[f][k]), "captured, frame %d output %s" % (f, k)
+    finally:
+        direct.close()
+        graphed.close()
+
+
+def test_frame_sequence_refuses_bad_frames(ctx):
+    """A sequence with one invalid frame runs none of its frames; a traced view refuses
+    sequences."""
+    import torch
+
+    W, H = 64, 32
+    n = W * H
+    scene = vg.Scene(41, W, H)
+    frames = [upload(scene.generate_host(f)) for f in range(3)]
+    fps = [scene.frame_params(f) for f in range(3)]
+    v = vg.View(ctx, W, H, "f32", params(0))
+    try:
+        before = state_of(v)
+        bad = dict(frames[2])
+        del bad["spec_hit_pos"]
+        with pytest.raises(vg.VltError) as e:
+            v.run_sequence(vg.FrameSequence(fps, [0, 1, 2], frames[:2] + [bad], _seq_outputs(n, 16, 3)))
+        assert e.value.status == 1
+        same_state(before, state_of(v), "refused sequence")
+    finally:
+        v.close()
+    pt = params(0)
+    pt.trace = 1
+    t = vg.View(ctx, W, H, "f32", pt)
+    try:
+        with pytest.raises(vg.VltError) as e:
+            t.run_sequence(vg.FrameSequence(fps[:1], [0], frames[:1]))
+        assert e.value.status == 1
+    finally:
+        t.close()

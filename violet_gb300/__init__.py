@@ -9,7 +9,7 @@ libvlt.so is missing or no GPU is present, calls raise.
 """
 from . import _ffi
 from ._ffi import VltError, FrameParams, Params, SceneDesc  # noqa: F401
-from .renderer import Context, View, FrameBinding, Batch, Server, Scene, params_reference, params_plain, FRAME_BUFFERS  # noqa: F401,E501
+from .renderer import Context, View, FrameBinding, FrameSequence, Batch, Server, Scene, params_reference, params_plain, FRAME_BUFFERS  # noqa: F401,E501
 
 
 def lib():

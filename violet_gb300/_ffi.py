@@ -195,6 +195,7 @@ SIGNATURES = {
     "vlt_view_device_bytes": (C.c_size_t, [U32, U32, C.c_int, PP]),
     "vlt_view_reset": (C.c_int, [P, P]),
     "vlt_frame_run": (C.c_int, [P, C.POINTER(FrameInputs), C.POINTER(FrameOutputs), P]),
+    "vlt_frames_run": (C.c_int, [P, C.c_uint32, C.POINTER(FrameInputs), C.POINTER(FrameOutputs), P]),
     "vlt_frame_trace": (C.c_int, [P, C.POINTER(FrameInputs), C.POINTER(FrameRays), P]),
     "vlt_view_state_bytes": (C.c_size_t, [P]),
     "vlt_view_export_state": (C.c_int, [P, P, C.c_size_t, P]),

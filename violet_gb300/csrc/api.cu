@@ -167,10 +167,20 @@ struct vlt_view {
   uint32_t launches;
   Timing* timing;
   // Side streams of a plain frame: the hash-grid passes and the specular chain run
-  // beside the diffuse chain (fork/join events on the caller's stream).
-  cudaStream_t aux[3];
-  cudaEvent_t ev[6];
+  // beside the diffuse chain (fork/join events on the caller's stream). aux[3] runs
+  // the denoiser of a pipelined frame sequence (vlt_frames_run); ev[6] marks the end
+  // of a frame's resampling passes, ev[7] the point after which the next frame may
+  // overwrite what they wrote.
+  cudaStream_t aux[4];
+  cudaEvent_t ev[8];
   bool aux_ready;
+};
+
+// A pipelined frame sequence (vlt_frames_run): frame f's denoiser runs on aux[3]
+// while frame f + 1's resampling passes run on the caller's stream and its side
+// streams.
+struct FramePipe {
+  bool wait_release;  // the caller's stream waits for ev[7] before this frame's first pass
 };
 
 namespace {
@@ -338,7 +348,7 @@ vlt_status reset_state(vlt_view* v, cudaStream_t s) {
 }  // namespace
 
 static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out,
-                                 cudaStream_t s, Recorder* rec);
+                                 cudaStream_t s, Recorder* rec, FramePipe* pipe = nullptr);
 
 namespace vlt {
 
@@ -473,9 +483,9 @@ size_t vlt_view_device_bytes(uint32_t width, uint32_t height, vlt_form form, con
 }
 
 static void destroy_side_streams(vlt_view* v) {
-  for (int k = 0; k < 3; ++k)
+  for (int k = 0; k < 4; ++k)
     if (v->aux[k]) cudaStreamDestroy(v->aux[k]);
-  for (int k = 0; k < 6; ++k)
+  for (int k = 0; k < 8; ++k)
     if (v->ev[k]) cudaEventDestroy(v->ev[k]);
 }
 
@@ -515,9 +525,9 @@ vlt_status vlt_view_create(vlt_ctx* ctx, uint32_t width, uint32_t height, vlt_fo
     return VLT_ERR_OUT_OF_MEMORY;
   }
   v->aux_ready = true;
-  for (int k = 0; k < 3; ++k)
+  for (int k = 0; k < 4; ++k)
     if (cudaStreamCreateWithFlags(&v->aux[k], cudaStreamNonBlocking) != cudaSuccess) v->aux_ready = false;
-  for (int k = 0; k < 6; ++k)
+  for (int k = 0; k < 8; ++k)
     if (cudaEventCreateWithFlags(&v->ev[k], cudaEventDisableTiming) != cudaSuccess) v->aux_ready = false;
   (void)cudaGetLastError();  // without side streams the frame runs on the caller's stream alone
   vlt_status st = reset_state(v, 0);
@@ -820,7 +830,7 @@ void* vlt_view_buffer(vlt_view* v, const char* name, size_t* bytes) {
 }  // extern "C"
 
 static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out,
-                                 cudaStream_t s, Recorder* rec) {
+                                 cudaStream_t s, Recorder* rec, FramePipe* pipe) {
   if (!vlt::frame_inputs_ok(v, in) || !vlt::frame_outputs_ok(v, out)) return VLT_ERR_INVALID_ARG;
   const bool traced = v->p.trace != 0;
   if (traced) {
@@ -889,6 +899,23 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     exa.stream = v->aux[2];
   }
   if (conc) exh.stream = v->aux[0];
+  // A pipelined sequence (vlt_frames_run): this frame's denoiser runs on aux[3] once
+  // its resampling passes are done, while the next frame's passes start as soon as
+  // the denoiser's temporal pass has read what they overwrite: the raw lighting, the
+  // previous frame's surface planes and the retained depth (the release below). The
+  // denoiser's later passes read only its own records and this frame's surface
+  // planes, which the frame after next rewrites.
+  const bool pl = pipe && conc;
+  if (pipe && pipe->wait_release) cudaStreamWaitEvent(s, v->ev[7], 0);
+  Exec exd = ex;
+  if (pl) exd.stream = v->aux[3];
+  bool released = false;
+  auto release = [&]() {
+    if (!pl || released) return;
+    if (!in->prev_depth) ex_copy(exd, b.prev_depth, in->depth, 4 * n);
+    cudaEventRecord(v->ev[7], v->aux[3]);
+    released = true;
+  };
 
   // Surface attributes of this frame, decoded once (the previous frame's planes
   // stay in the other slot).
@@ -1059,6 +1086,10 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     cudaStreamWaitEvent(v->aux[0], v->ev[0], 0);
     hg_chain();
   }
+  if (pl) {
+    cudaEventRecord(v->ev[6], s);
+    cudaStreamWaitEvent(v->aux[3], v->ev[6], 0);
+  }
 
   // Denoiser.
   const bool run_denoiser = P.denoise && has_prev;
@@ -1072,16 +1103,17 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     DenoiseKnobs kn = {1.0f / P.history_max_frames, P.fast_history_clamp};
     uint32_t has_history = v->denoise_history ? 1u : 0u;
     // rec[0]/len[0] = history; rec[2]/len[1] = temporal output; rec[1] = fix output.
-    STAGE("dn_temporal", launch_dn32_temporal(ex, form, fp, w, h, kn, ga, pga, b.diff_light, b.spec_light,
+    STAGE("dn_temporal", launch_dn32_temporal(exd, form, fp, w, h, kn, ga, pga, b.diff_light, b.spec_light,
                                               prev_depth, b.rec[0], b.len[0], b.rec_fast[0], b.rec[2], b.len[1],
                                               b.rec_fast[1], has_history));
+    release();
     float4* cur = b.rec[2];
     if (P.disocclusion_fix) {
-      STAGE("dn_fix", launch_dn32_fix(ex, form, w, h, ga, b.len[1], b.rec[2], b.rec[1]));
+      STAGE("dn_fix", launch_dn32_fix(exd, form, w, h, ga, b.len[1], b.rec[2], b.rec[1]));
       cur = b.rec[1];
     }
     if (P.fast_history_clamp) {
-      STAGE("dn_fast_clamp", launch_dn32_fast_clamp(ex, form, w, h, b.rec_fast[1], cur));
+      STAGE("dn_fast_clamp", launch_dn32_fast_clamp(exd, form, w, h, b.rec_fast[1], cur));
       std::swap(b.rec_fast[0], b.rec_fast[1]);
       v->fast_history_valid = true;
     } else {
@@ -1094,7 +1126,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
       std::swap(b.rec[0], b.rec[2]);
     std::swap(b.len[0], b.len[1]);
     v->denoise_history = true;
-    STAGE("dn_fallback", launch_dn32_fallback(ex, form, w, h, ga, b.len[0], b.rec[0], b.rec[4]));
+    STAGE("dn_fallback", launch_dn32_fallback(exd, form, w, h, ga, b.len[0], b.rec[0], b.rec[4]));
     float4* rsrc = b.rec[4];
     float4* rdst = b.rec[2];
     const uint32_t iters = P.atrous_iterations;
@@ -1109,7 +1141,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
       const bool dst_f32 = f16 && !last;
       if (f16) rdst = last ? b.rec[3] : b.atr32[k & 1];
       void* ro = last && !keep_den ? nullptr : (void*)rdst;
-      STAGE("dn_atrous", launch_dn32_atrous(ex, form, w, h, ga, rsrc, ro, od, os, 1 << k, src_f32, dst_f32));
+      STAGE("dn_atrous", launch_dn32_atrous(exd, form, w, h, ga, rsrc, ro, od, os, 1 << k, src_f32, dst_f32));
       rsrc = rdst;
       src_f32 = dst_f32;
       if (!f16) rdst = rdst == b.rec[2] ? b.rec[3] : b.rec[2];
@@ -1119,26 +1151,27 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
       // Zero iterations: the fallback output is the result (copy its colours out).
       // The diffuse / specular half of each fallback record {rgb, aux}.
       const size_t half_rec = f32 ? 16 : 8;
-      if (out->diffuse) ex_copy_rows(ex, out->diffuse, half_rec, b.rec[4], 2 * half_rec, half_rec, n);
+      if (out->diffuse) ex_copy_rows(exd, out->diffuse, half_rec, b.rec[4], 2 * half_rec, half_rec, n);
       if (out->specular)
-        ex_copy_rows(ex, out->specular, half_rec, (char*)b.rec[4] + half_rec, 2 * half_rec, half_rec, n);
+        ex_copy_rows(exd, out->specular, half_rec, (char*)b.rec[4] + half_rec, 2 * half_rec, half_rec, n);
     }
   } else if (run_denoiser) {
     DenoiseKnobs kn = {1.0f / P.history_max_frames, P.fast_history_clamp};
     uint32_t has_history = v->denoise_history ? 1u : 0u;
     // color[0]/mom[0]/len[0] = history; color[2]/mom[2]/len[1] = temporal output;
     // color[1]/mom[1] = fix output.
-    STAGE("dn_temporal", launch_dn_temporal(ex, fp, w, h, kn, ga, pga, (const uint32_t*)b.diff_light,
+    STAGE("dn_temporal", launch_dn_temporal(exd, fp, w, h, kn, ga, pga, (const uint32_t*)b.diff_light,
                                             (const uint32_t*)b.spec_light, b.ray_len, prev_depth, b.color[0],
                                             b.mom[0], (const uint8_t*)b.len[0], b.fast[0], b.color[2], b.mom[2],
                                             (uint8_t*)b.len[1], b.fast[1], has_history));
+    release();
     uint32_t* cur_color = b.color[2];
     if (P.disocclusion_fix) {
-      STAGE("dn_fix", launch_dn_fix(ex, w, h, ga, (const uint8_t*)b.len[1], b.color[2], b.mom[2], b.color[1], b.mom[1]));
+      STAGE("dn_fix", launch_dn_fix(exd, w, h, ga, (const uint8_t*)b.len[1], b.color[2], b.mom[2], b.color[1], b.mom[1]));
       cur_color = b.color[1];
     }
     if (P.fast_history_clamp) {
-      STAGE("dn_fast_clamp", launch_dn_fast_clamp(ex, w, h, b.fast[1], cur_color));
+      STAGE("dn_fast_clamp", launch_dn_fast_clamp(exd, w, h, b.fast[1], cur_color));
       std::swap(b.fast[0], b.fast[1]);
       v->fast_history_valid = true;
     } else {
@@ -1155,7 +1188,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     std::swap(b.len[0], b.len[1]);
     v->denoise_history = true;
     // Now color[0]/mom[0]/len[0] hold this frame's history.
-    STAGE("dn_fallback", launch_dn_fallback(ex, w, h, ga, (const uint8_t*)b.len[0], b.color[0], b.mom[0], b.color_c,
+    STAGE("dn_fallback", launch_dn_fallback(exd, w, h, ga, (const uint8_t*)b.len[0], b.color[0], b.mom[0], b.color_c,
                                             b.var[0]));
     uint32_t* csrc = b.color_c;
     uint32_t* vsrc = b.var[0];
@@ -1167,7 +1200,7 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
       uint32_t* od = last && out ? (uint32_t*)out->diffuse : nullptr;
       uint32_t* os = last && out ? (uint32_t*)out->specular : nullptr;
       uint32_t* co = last && !keep_den ? nullptr : cdst;
-      STAGE("dn_atrous", launch_dn_atrous(ex, w, h, ga, csrc, vsrc, co, last ? nullptr : vdst, od, os, 1 << k));
+      STAGE("dn_atrous", launch_dn_atrous(exd, w, h, ga, csrc, vsrc, co, last ? nullptr : vdst, od, os, 1 << k));
       std::swap(csrc, cdst);
       uint32_t* vnext = vdst == b.var[1] ? b.var[2] : b.var[1];
       vsrc = vdst;
@@ -1175,15 +1208,16 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
     }
     den = keep_den ? (const void*)csrc : nullptr;
     if (iters == 0 && out && (out->diffuse || out->specular)) {
-      launch_split_color(ex, w, h, csrc, (uint32_t*)out->diffuse, (uint32_t*)out->specular);
+      launch_split_color(exd, w, h, csrc, (uint32_t*)out->diffuse, (uint32_t*)out->specular);
     }
   } else {
     v->denoise_history = false;  // Denoiser::reset
     v->fast_history_valid = false;
     if (out && out->diffuse)
-      ex_copy(ex, out->diffuse, b.diff_light, light_bytes);
+      ex_copy(exd, out->diffuse, b.diff_light, light_bytes);
     if (out && out->specular)
-      ex_copy(ex, out->specular, b.spec_light, light_bytes);
+      ex_copy(exd, out->specular, b.spec_light, light_bytes);
+    release();
   }
   if (out && out->raw_diffuse)
     ex_copy(ex, out->raw_diffuse, b.diff_light, light_bytes);
@@ -1208,15 +1242,18 @@ static vlt_status frame_run_impl(vlt_view* v, const vlt_frame_inputs* in, const 
   }
 
   // Retain depth for the next frame unless the caller keeps it (the previous
-  // frame's decoded G-buffer fields stay in the other surface slot).
-  if (!in->prev_depth) ex_copy(ex, b.prev_depth, in->depth, 4 * n);
+  // frame's decoded G-buffer fields stay in the other surface slot); a pipelined
+  // frame did so at its release.
+  if (!pl && !in->prev_depth) ex_copy(ex, b.prev_depth, in->depth, 4 * n);
   v->surf_cur = sc;
   // The screen-space radiance cache of the next traced frame
   // (RestirRenderer::prev_indirect_diffuse_texture, restir_renderer.rs:819-820).
   v->prev_den = den ? den : b.diff_light;
   v->prev_den_stride = den ? 2 : 1;
   v->has_prev_den = true;
-  if (conc) {
+  // A pipelined frame leaves its hash-grid chain on aux[0] and its denoiser on
+  // aux[3]; the sequence joins them into the caller's stream at its end.
+  if (conc && !pl) {
     cudaEventRecord(v->ev[3], v->aux[0]);
     cudaStreamWaitEvent(s, v->ev[3], 0);
   }
@@ -1298,6 +1335,52 @@ uint32_t vlt_view_cache_ray_capacity(const vlt_view* v) { return v && v->p.hg_en
 
 vlt_status vlt_frame_run(vlt_view* v, const vlt_frame_inputs* in, const vlt_frame_outputs* out, void* stream) {
   return frame_run_impl(v, in, out, (cudaStream_t)stream, nullptr);
+}
+
+// Frames in[0..n) in order, frame k's denoiser beside frame k + 1's resampling
+// passes where the view allows it (side streams, no per-pass timers, no final
+// lighting or TAA, no raw outputs requested for the frame); other frames run as
+// vlt_frame_run runs them. The side streams join the caller's stream before return.
+vlt_status vlt_frames_run(vlt_view* v, uint32_t n, const vlt_frame_inputs* in, const vlt_frame_outputs* out,
+                          void* stream) {
+  if (!v || (n > 0 && !in)) {
+    set_last_error("vlt_frames_run: null view or inputs");
+    return VLT_ERR_INVALID_ARG;
+  }
+  if (v->p.trace) {
+    set_last_error("vlt_frames_run: a traced view runs frame by frame (vlt_frame_trace before each frame)");
+    return VLT_ERR_INVALID_ARG;
+  }
+  for (uint32_t k = 0; k < n; ++k) {
+    if (!vlt::frame_inputs_ok(v, &in[k]) || !vlt::frame_outputs_ok(v, out ? &out[k] : nullptr)) {
+      set_last_error("vlt_frames_run: a frame's inputs or outputs are invalid (nothing ran)");
+      return VLT_ERR_INVALID_ARG;
+    }
+  }
+  const cudaStream_t s = (cudaStream_t)stream;
+  const bool can = v->aux_ready && !v->timing->enabled && v->p.post == 0;
+  auto join = [&]() {
+    cudaEventRecord(v->ev[6], v->aux[3]);
+    cudaStreamWaitEvent(s, v->ev[6], 0);
+    cudaEventRecord(v->ev[3], v->aux[0]);
+    cudaStreamWaitEvent(s, v->ev[3], 0);
+  };
+  bool prev_pl = false;
+  uint32_t launches = 0;
+  vlt_status st = VLT_OK;
+  for (uint32_t k = 0; k < n && st == VLT_OK; ++k) {
+    const vlt_frame_outputs* o = out ? &out[k] : nullptr;
+    const bool pk = can && !(o && (o->raw_diffuse || o->raw_specular));
+    if (prev_pl && !pk) join();
+    FramePipe pipe = {prev_pl};
+    st = frame_run_impl(v, &in[k], o, s, nullptr, pk ? &pipe : nullptr);
+    launches += v->launches;
+    prev_pl = pk;
+  }
+  if (can) join();
+  v->launches = launches;
+  if (st != VLT_OK) return st;
+  return cuda_status(cudaGetLastError());
 }
 
 // ------------------------------------------------------ per-pass entry points

@@ -93,6 +93,26 @@ class FrameBinding:
         self._keep = (inputs, outputs)  # the buffers must outlive the binding
 
 
+class FrameSequence:
+    """The argument arrays of vlt_frames_run for n frames, built once: frame k runs
+    frame_indices[k] with frame_params[k], inputs[k] and outputs[k] (outputs may be
+    None: no outputs for any frame)."""
+
+    def __init__(self, frame_params, frame_indices, inputs, outputs=None):
+        n = len(inputs)
+        if not (len(frame_params) == len(frame_indices) == n) or (outputs is not None and len(outputs) != n):
+            raise ValueError("FrameSequence: one frame_params, frame index, inputs (and outputs) per frame")
+        self.n = n
+        self.fis = (_ffi.FrameInputs * n)()
+        self.fos = (_ffi.FrameOutputs * n)() if outputs is not None else None
+        for k in range(n):
+            fi, fo = _frame_structs(frame_params[k], frame_indices[k], inputs[k], outputs[k] if outputs else None)
+            self.fis[k] = fi
+            if self.fos is not None:
+                self.fos[k] = fo
+        self._keep = (list(frame_params), inputs, outputs)  # everything must outlive the arrays
+
+
 class View:
     """Resident per-view state and the per-frame pass sequence (vlt_frame_run)."""
 
@@ -127,6 +147,13 @@ class View:
         binding.fi.frame_index = int(frame_index) & 0xFFFFFFFF
         _ffi.check(self._lib.vlt_frame_run(self.handle, C.byref(binding.fi), C.byref(binding.fo),
                                            C.c_void_p(stream)), "vlt_frame_run")
+
+    def run_sequence(self, seq, stream=0):
+        """vlt_frames_run over a FrameSequence: its frames in order, each frame's
+        denoiser beside the next frame's resampling passes; results equal
+        run() frame by frame."""
+        _ffi.check(self._lib.vlt_frames_run(self.handle, seq.n, seq.fis, seq.fos, C.c_void_p(stream)),
+                   "vlt_frames_run")
 
     def trace(self, frame_params, frame_index, inputs, rays, stream=0):
         """Phase one of a traced frame (params.trace = 1): fills the device ray arrays
