@@ -49,6 +49,8 @@ def test_invalid_arguments_are_reported_not_raised():
     assert lib.vlt_view_create(None, 16, 16, 0, C.byref(vg.params_reference()), C.byref(h)) == 1
     assert lib.vlt_ctx_create(0, None) == 1
     assert lib.vlt_frame_run(None, None, None, None) == 1
+    assert lib.vlt_frames_run(None, 0, None, None, None) == 1
+    assert b"vlt_frames_run" in lib.vlt_last_error()
     assert lib.vlt_hg_decay(2, None, None, None) == 1
     assert lib.vlt_denoise_atrous(0, 0, None, None, None, None, None, None, 1, None) == 1
 
