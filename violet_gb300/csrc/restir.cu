@@ -771,54 +771,9 @@ struct SpecLight<FORM_F16> {
   using T = uint2;  // half4 {rgb, ray length}
 };
 
+// One pixel of the specular spatial pass (the pixel (x, y) is inside the image).
 template <class Geo, int FORM>
-struct SpecSpatialF {
-  static constexpr int kMinBlocks = 4;  // 64 registers, a few spills (measured 22% faster)
-  using Light = typename SpecLight<FORM>::T;
-  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo, typename SpecStore<FORM>::CPtr in, Light* __restrict__ lighting, uint16_t* __restrict__ ray_len_out, typename SpecStore<FORM>::Ptr out, uint32_t frame_rand) {
-  // The tap count of a pixel is uint(roughness * taps), so neighbouring lanes can
-  // run very different loop lengths. The pixels of the tile are therefore
-  // reordered by tap count (counting sort in shared memory) before the loop, so a
-  // warp's lanes run similar counts. Each pixel's result does not depend on which
-  // lane computes it. Needs 64..256 threads per block.
-  __shared__ uint32_t s_count[64];
-  __shared__ uint32_t s_offset[64];
-  __shared__ uint8_t s_order[kMaxThreads];
-  const int bx = (int)blockDim.x;
-  const int tid = (int)threadIdx.y * bx + (int)threadIdx.x;
-  {
-    int px = x0 + (int)threadIdx.x, py = y0 + (int)threadIdx.y;
-    uint32_t key = 0;
-    if (inb(px, py, w, h)) {
-      size_t pi = (size_t)py * w + px;
-      if (geo.dep(pi) != 0.0f) {
-        uint32_t nt = f2u_rz(0.0f + geo.rough(pi) * ((float)kn.taps - 0.0f));
-        key = nt < 63u ? nt : 63u;
-      }
-    }
-    if (tid < 64) s_count[tid] = 0u;
-    __syncthreads();
-    uint32_t slot = atomicAdd(&s_count[key], 1u);
-    __syncthreads();
-    if (tid < 32) {
-      uint32_t a = s_count[2 * tid], b = s_count[2 * tid + 1];
-      uint32_t incl = a + b;
-#pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-        if (tid >= d) incl += v;
-      }
-      uint32_t excl = incl - (a + b);
-      s_offset[2 * tid] = excl;
-      s_offset[2 * tid + 1] = excl + a;
-    }
-    __syncthreads();
-    s_order[s_offset[key] + slot] = (uint8_t)tid;
-    __syncthreads();
-  }
-  const int lp = s_order[tid];
-  int x = x0 + lp % bx, y = y0 + lp / bx;
-  if (!inb(x, y, w, h)) return;
+__device__ __forceinline__ void spec_spatial_px(int x, int y, vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo, typename SpecStore<FORM>::CPtr in, typename SpecLight<FORM>::T* __restrict__ lighting, uint16_t* __restrict__ ray_len_out, typename SpecStore<FORM>::Ptr out, uint32_t frame_rand) {
   size_t i = (size_t)y * w + x;
   float depth = geo.dep(i);
   if (depth == 0.0f) {
@@ -934,7 +889,124 @@ struct SpecSpatialF {
     ray_len_out[i] = (uint16_t)f32tof16(ray_len);
   }
 }
+
+template <class Geo, int FORM>
+struct SpecSpatialF {
+  static constexpr int kMinBlocks = 4;  // 64 registers, a few spills (measured 22% faster)
+  using Light = typename SpecLight<FORM>::T;
+  static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo, typename SpecStore<FORM>::CPtr in, Light* __restrict__ lighting, uint16_t* __restrict__ ray_len_out, typename SpecStore<FORM>::Ptr out, uint32_t frame_rand) {
+  // The tap count of a pixel is uint(roughness * taps), so neighbouring lanes can
+  // run very different loop lengths. The pixels of the tile are therefore
+  // reordered by tap count (counting sort in shared memory) before the loop, so a
+  // warp's lanes run similar counts. Each pixel's result does not depend on which
+  // lane computes it. Needs 64..256 threads per block.
+  __shared__ uint32_t s_count[64];
+  __shared__ uint32_t s_offset[64];
+  __shared__ uint8_t s_order[kMaxThreads];
+  const int bx = (int)blockDim.x;
+  const int tid = (int)threadIdx.y * bx + (int)threadIdx.x;
+  {
+    int px = x0 + (int)threadIdx.x, py = y0 + (int)threadIdx.y;
+    uint32_t key = 0;
+    if (inb(px, py, w, h)) {
+      size_t pi = (size_t)py * w + px;
+      if (geo.dep(pi) != 0.0f) {
+        uint32_t nt = f2u_rz(0.0f + geo.rough(pi) * ((float)kn.taps - 0.0f));
+        key = nt < 63u ? nt : 63u;
+      }
+    }
+    if (tid < 64) s_count[tid] = 0u;
+    __syncthreads();
+    uint32_t slot = atomicAdd(&s_count[key], 1u);
+    __syncthreads();
+    if (tid < 32) {
+      uint32_t a = s_count[2 * tid], b = s_count[2 * tid + 1];
+      uint32_t incl = a + b;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (tid >= d) incl += v;
+      }
+      uint32_t excl = incl - (a + b);
+      s_offset[2 * tid] = excl;
+      s_offset[2 * tid + 1] = excl + a;
+    }
+    __syncthreads();
+    s_order[s_offset[key] + slot] = (uint8_t)tid;
+    __syncthreads();
+  }
+  const int lp = s_order[tid];
+  int x = x0 + lp % bx, y = y0 + lp / bx;
+  if (!inb(x, y, w, h)) return;
+  spec_spatial_px<Geo, FORM>(x, y, fp, w, h, kn, geo, in, lighting, ray_len_out, out, frame_rand);
+}
 };
+
+// Single-view form of the pass. Sorting a block's pixels by tap count (above) gives
+// each warp lanes of similar loop lengths, but the warps of a block still differ:
+// the warp of the shortest counts ends long before the one of the longest and then
+// holds its slot on the SM (registers are freed per block) until the block ends. Here
+// a block of NW warps takes a 32 x (NW * RPW) tile, sorts its pixels by tap count
+// into rounds of 32, and warp w runs rounds in a snake order (w, 2 NW - 1 - w, ...):
+// a short round and a long one, so that a block's warps end together. Each pixel's
+// result does not depend on which lane or round computes it. Measured at 1080p:
+// 0.482 -> 0.422 ms per frame for the two launches with 8 warps x 2 rounds (4 x 2:
+// 0.431, 4 x 4: 0.450, 2 x 4: 0.468, 1 warp x 4 rounds: 0.503).
+constexpr int kSpecSortWarps = 8, kSpecSortRounds = 2;
+template <class Geo, int FORM, int NW, int RPW>
+__global__ void __launch_bounds__(32 * NW, 32 / NW)  // 64 registers
+    k_spec_spatial_sorted(vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo, typename SpecStore<FORM>::CPtr in,
+                          typename SpecLight<FORM>::T* __restrict__ lighting, uint16_t* __restrict__ ray_len_out,
+                          typename SpecStore<FORM>::Ptr out, uint32_t frame_rand) {
+  constexpr int NT = 32 * NW, NR = NW * RPW, NP = 32 * NR;
+  __shared__ uint32_t s_count[64];
+  __shared__ uint32_t s_offset[64];
+  __shared__ uint16_t s_order[NP];
+  const int x0 = (int)blockIdx.x * 32, y0 = (int)blockIdx.y * NR;
+  const int tid = (int)threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int k = tid; k < 64; k += NT) s_count[k] = 0u;
+  __syncthreads();
+  uint32_t key[RPW], slot[RPW];
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) {
+    const int p = tid + r * NT;
+    const int px = x0 + (p & 31), py = y0 + (p >> 5);
+    uint32_t kk = 0;
+    if (inb(px, py, w, h)) {
+      const size_t pi = (size_t)py * w + px;
+      if (geo.dep(pi) != 0.0f) {
+        const uint32_t nt = f2u_rz(0.0f + geo.rough(pi) * ((float)kn.taps - 0.0f));
+        kk = nt < 63u ? nt : 63u;
+      }
+    }
+    key[r] = kk;
+    slot[r] = atomicAdd(&s_count[kk], 1u);
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const uint32_t a = s_count[2 * lane], b = s_count[2 * lane + 1];
+    uint32_t incl = a + b;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+      if (lane >= d) incl += v;
+    }
+    const uint32_t excl = incl - (a + b);
+    s_offset[2 * lane] = excl;
+    s_offset[2 * lane + 1] = excl + a;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) s_order[s_offset[key[r]] + slot[r]] = (uint16_t)(tid + r * NT);
+  __syncthreads();
+#pragma unroll 1
+  for (int k = 0; k < RPW; ++k) {
+    const int round = k * NW + ((k & 1) ? NW - 1 - wid : wid);  // snake: short and long rounds alternate
+    const int lp = s_order[round * 32 + lane];
+    const int x = x0 + (lp & 31), y = y0 + (lp >> 5);
+    if (inb(x, y, w, h)) spec_spatial_px<Geo, FORM>(x, y, fp, w, h, kn, geo, in, lighting, ray_len_out, out, frame_rand);
+  }
+}
 
 
 // ------------------------------------------------------ sample validation
@@ -1223,6 +1295,22 @@ void launch_spec_spatial(const Exec& ex, int form, const vlt_frame_params& fp, i
                          uint32_t frame_rand) {
   SpecPlanesC pin = {(const uint2*)rsv, (const float4*)hp, rad};
   SpecPlanes pout = {(uint2*)out_rsv, (float4*)out_hp, out_rad};
+  if (!ex.rec) {
+    if (w <= 0 || h <= 0) return;
+    if (ex.launches) ++*ex.launches;
+    constexpr int NW = kSpecSortWarps, RPW = kSpecSortRounds, NR = NW * RPW;
+    const dim3 grid((unsigned)((w + 31) / 32), (unsigned)((h + NR - 1) / NR), 1), block(32 * NW, 1, 1);
+    if (form == FORM_F32)
+      VLT_GEO_DISPATCH(ga, (k_spec_spatial_sorted<Geo, FORM_F32, NW, RPW><<<grid, block, 0, ex.stream>>>(
+                               fp, w, h, kn, geo, pin, (float4*)lighting, (uint16_t*)nullptr, pout, frame_rand)));
+    else if (form == FORM_F16)
+      VLT_GEO_DISPATCH(ga, (k_spec_spatial_sorted<Geo, FORM_F16, NW, RPW><<<grid, block, 0, ex.stream>>>(
+                               fp, w, h, kn, geo, pin, (uint2*)lighting, (uint16_t*)nullptr, pout, frame_rand)));
+    else
+      VLT_GEO_DISPATCH(ga, (k_spec_spatial_sorted<Geo, FORM_REF, NW, RPW><<<grid, block, 0, ex.stream>>>(
+                               fp, w, h, kn, geo, pin, (uint32_t*)lighting, ray_len, pout, frame_rand)));
+    return;
+  }
   if (form == FORM_F32)
     VLT_GEO_DISPATCH(ga, (launch2d<SpecSpatialF<Geo, FORM_F32>>(ex, "spec_spatial", w, h, fp, w, h, kn, geo, pin,
                                                                (float4*)lighting, (uint16_t*)nullptr, pout,
