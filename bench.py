@@ -108,12 +108,12 @@ PASS_BYTES_PER_CELL = {"hg_decay": 2, "hg_compact": 4}
 # dram__bytes_write.sum; the a-trous from one-pass counters, profiles/dn_atrous_f32_540p.md;
 # the specular spatial pass from its --set full capture, mean of its two launches,
 # profiles/spec_spatial_f32_540p.md).
-MEASURED_TRAFFIC_PER_UNIT = {"dn_atrous": 64.25, "spec_spatial": (36.007e6 + 0.711e6 + 34.376e6 + 0.477e6) / 2 / (960 * 540)}
+MEASURED_TRAFFIC_PER_UNIT = {"dn_atrous": 64.25, "spec_spatial": (36.013e6 + 0.507e6 + 34.377e6 + 0.322e6) / 2 / (960 * 540)}
 # Warp instructions per launch unit measured with ncu (smsp__inst_executed.sum of a
 # --set full capture / pixels, mean of two launches): the issue roofline of a pass
 # that is bound by instruction issue or latency rather than by HBM.
 MEASURED_WARP_INSTRUCTIONS_PER_UNIT = {"dn_atrous": (20.716e6 + 20.666e6) / 2 / (960 * 540),
-                                       "spec_spatial": (46.126e6 + 49.594e6) / 2 / (960 * 540)}
+                                       "spec_spatial": (40.168e6 + 43.590e6) / 2 / (960 * 540)}
 ISSUE_SLOTS_PER_SM_CLOCK = 4  # one warp instruction per scheduler per clock, 4 schedulers per SM
 
 
