@@ -890,68 +890,79 @@ __device__ __forceinline__ void spec_spatial_px(int x, int y, vlt_frame_params f
   }
 }
 
+// ind_spec_spatial_resample.hlsl:169-448, per tile. The tap count of a pixel is
+// uint(roughness * taps), so neighbouring pixels can run very different loop
+// lengths. A block of NT threads takes a tile of 2 NT pixels (two rows per thread),
+// sorts them by tap count (counting sort in shared memory) into rounds of 32, and warp
+// w runs rounds w and 2 NW - 1 - w (NW warps): a short round and a long one. A warp's
+// lanes then run similar counts, and a block's warps end together instead of the
+// warp of the shortest counts holding its slot on the SM (registers are freed per
+// block) until the warp of the longest ends. Each pixel's result does not depend on
+// which lane or round computes it. Blocks of 32 to 256 threads, a multiple of 32, of
+// any shape the batch autotuner picks. Batched launches run this form (the 48-view
+// FP16 batch: 1,180 Mpix/s with one round per warp over bx x by tiles, 1,212 with
+// two); a single view runs the compile-time form below.
 template <class Geo, int FORM>
 struct SpecSpatialF {
   static constexpr int kMinBlocks = 4;  // 64 registers, a few spills (measured 22% faster)
+  static constexpr int kTileX = 32, kTileY = 8;
+  static constexpr int kRowsPerThread = 2;
   using Light = typename SpecLight<FORM>::T;
   static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo, typename SpecStore<FORM>::CPtr in, Light* __restrict__ lighting, uint16_t* __restrict__ ray_len_out, typename SpecStore<FORM>::Ptr out, uint32_t frame_rand) {
-  // The tap count of a pixel is uint(roughness * taps), so neighbouring lanes can
-  // run very different loop lengths. The pixels of the tile are therefore
-  // reordered by tap count (counting sort in shared memory) before the loop, so a
-  // warp's lanes run similar counts. Each pixel's result does not depend on which
-  // lane computes it. Needs 64..256 threads per block.
   __shared__ uint32_t s_count[64];
   __shared__ uint32_t s_offset[64];
-  __shared__ uint8_t s_order[kMaxThreads];
-  const int bx = (int)blockDim.x;
-  const int tid = (int)threadIdx.y * bx + (int)threadIdx.x;
-  {
-    int px = x0 + (int)threadIdx.x, py = y0 + (int)threadIdx.y;
-    uint32_t key = 0;
-    if (inb(px, py, w, h)) {
-      size_t pi = (size_t)py * w + px;
-      if (geo.dep(pi) != 0.0f) {
-        uint32_t nt = f2u_rz(0.0f + geo.rough(pi) * ((float)kn.taps - 0.0f));
-        key = nt < 63u ? nt : 63u;
-      }
-    }
-    if (tid < 64) s_count[tid] = 0u;
-    __syncthreads();
-    uint32_t slot = atomicAdd(&s_count[key], 1u);
-    __syncthreads();
-    if (tid < 32) {
-      uint32_t a = s_count[2 * tid], b = s_count[2 * tid + 1];
-      uint32_t incl = a + b;
+  __shared__ uint16_t s_order[2 * kMaxThreads];
+  const int bx = (int)blockDim.x, nt = (int)(blockDim.x * blockDim.y), nw = nt >> 5;
+  const int tid = (int)threadIdx.y * bx + (int)threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int k = tid; k < 64; k += nt) s_count[k] = 0u;
+  __syncthreads();
+  uint32_t key[2], slot[2];
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-        if (tid >= d) incl += v;
+  for (int r = 0; r < 2; ++r) {
+    const int p = tid + r * nt;
+    const int px = x0 + p % bx, py = y0 + p / bx;
+    uint32_t kk = 0;
+    if (inb(px, py, w, h)) {
+      const size_t pi = (size_t)py * w + px;
+      if (geo.dep(pi) != 0.0f) {
+        const uint32_t ntaps = f2u_rz(0.0f + geo.rough(pi) * ((float)kn.taps - 0.0f));
+        kk = ntaps < 63u ? ntaps : 63u;
       }
-      uint32_t excl = incl - (a + b);
-      s_offset[2 * tid] = excl;
-      s_offset[2 * tid + 1] = excl + a;
     }
-    __syncthreads();
-    s_order[s_offset[key] + slot] = (uint8_t)tid;
-    __syncthreads();
+    key[r] = kk;
+    slot[r] = atomicAdd(&s_count[kk], 1u);
   }
-  const int lp = s_order[tid];
-  int x = x0 + lp % bx, y = y0 + lp / bx;
-  if (!inb(x, y, w, h)) return;
-  spec_spatial_px<Geo, FORM>(x, y, fp, w, h, kn, geo, in, lighting, ray_len_out, out, frame_rand);
+  __syncthreads();
+  if (wid == 0) {
+    const uint32_t a = s_count[2 * lane], b = s_count[2 * lane + 1];
+    uint32_t incl = a + b;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+      if (lane >= d) incl += v;
+    }
+    const uint32_t excl = incl - (a + b);
+    s_offset[2 * lane] = excl;
+    s_offset[2 * lane + 1] = excl + a;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < 2; ++r) s_order[s_offset[key[r]] + slot[r]] = (uint16_t)(tid + r * nt);
+  __syncthreads();
+#pragma unroll 1
+  for (int k = 0; k < 2; ++k) {
+    const int lp = s_order[(k == 0 ? wid : 2 * nw - 1 - wid) * 32 + lane];
+    const int x = x0 + lp % bx, y = y0 + lp / bx;
+    if (inb(x, y, w, h)) spec_spatial_px<Geo, FORM>(x, y, fp, w, h, kn, geo, in, lighting, ray_len_out, out, frame_rand);
+  }
 }
 };
 
-// Single-view form of the pass. Sorting a block's pixels by tap count (above) gives
-// each warp lanes of similar loop lengths, but the warps of a block still differ:
-// the warp of the shortest counts ends long before the one of the longest and then
-// holds its slot on the SM (registers are freed per block) until the block ends. Here
-// a block of NW warps takes a 32 x (NW * RPW) tile, sorts its pixels by tap count
-// into rounds of 32, and warp w runs rounds in a snake order (w, 2 NW - 1 - w, ...):
-// a short round and a long one, so that a block's warps end together. Each pixel's
-// result does not depend on which lane or round computes it. Measured at 1080p:
-// 0.482 -> 0.422 ms per frame for the two launches with 8 warps x 2 rounds (4 x 2:
-// 0.431, 4 x 4: 0.450, 2 x 4: 0.468, 1 warp x 4 rounds: 0.503).
+// Single-view form of the pass: the same sorted rounds with the block geometry fixed
+// at compile time (NW warps over 32 x (NW * RPW) tiles, warp w running rounds in the
+// snake order w, 2 NW - 1 - w, ...), which saves the runtime tile-width divisions and
+// a few spills of the batched form: 0.422 against 0.433 ms per 1080p frame with 8
+// warps x 2 rounds (4 x 2: 0.431, 4 x 4: 0.450, 2 x 4: 0.468).
 constexpr int kSpecSortWarps = 8, kSpecSortRounds = 2;
 template <class Geo, int FORM, int NW, int RPW>
 __global__ void __launch_bounds__(32 * NW, 32 / NW)  // 64 registers

@@ -117,9 +117,20 @@ struct TileOf<F, decltype((void)F::kTileX)> {
   static constexpr int x = F::kTileX, y = F::kTileY;
 };
 
+// Pixel rows per thread of a pass's tile (F::kRowsPerThread, default 1): a block of
+// bx x by threads covers a bx x (by * rows) tile.
+template <class F, class = void>
+struct RowsOf {
+  static constexpr int value = 1;
+};
+template <class F>
+struct RowsOf<F, decltype((void)F::kRowsPerThread)> {
+  static constexpr int value = F::kRowsPerThread;
+};
+
 template <class F, class... A>
 __global__ void __launch_bounds__(kMaxThreads, MinBlocks<F>::value) k_grid(A... a) {
-  F::run((int)(blockIdx.x * blockDim.x), (int)(blockIdx.y * blockDim.y), a...);
+  F::run((int)(blockIdx.x * blockDim.x), (int)(blockIdx.y * blockDim.y * RowsOf<F>::value), a...);
 }
 
 // Kernel parameter block of a batched launch: the views' parameter tuples and
@@ -152,7 +163,7 @@ __global__ void __launch_bounds__(kMaxThreads, MinBlocks<F>::value) k_batched(co
     }
     const uint32_t lt = t - p.tile_start[lo];
     const uint32_t tx = p.tiles_x[lo];
-    const int x0 = (int)((lt % tx) * blockDim.x), y0 = (int)((lt / tx) * blockDim.y);
+    const int x0 = (int)((lt % tx) * blockDim.x), y0 = (int)((lt / tx) * blockDim.y * RowsOf<F>::value);
     cuda::std::apply([&](auto const&... a) { F::run(x0, y0, a...); }, p.tup[lo]);
   }
 }
@@ -194,7 +205,8 @@ void prepare_batched(const Job* const* jobs, uint32_t n, TileShape shape, std::v
     uint32_t total = 0;
     for (uint32_t j = 0; j < m; ++j) {
       const Job& jb = *jobs[first + j];
-      uint32_t tx = (jb.w + bx - 1) / bx, ty = (jb.h + by - 1) / by;
+      const uint32_t th = by * (uint32_t)RowsOf<F>::value;  // tile height
+      uint32_t tx = (jb.w + bx - 1) / bx, ty = (jb.h + th - 1) / th;
       bp->tile_start[j] = total;
       bp->tiles_x[j] = tx ? tx : 1;
       total += tx * ty;
@@ -246,7 +258,8 @@ void launch2d(const Exec& ex, const char* name, int w, int h, A... a) {
     return;
   }
   const dim3 block(TileOf<F>::x, TileOf<F>::y, 1);
-  k_grid<F><<<grid2d(w, h, block), block, 0, ex.stream>>>(a...);
+  const dim3 grid = grid2d(w, h, dim3(block.x, block.y * RowsOf<F>::value, 1));
+  k_grid<F><<<grid, block, 0, ex.stream>>>(a...);
 }
 
 // A 1D pass over n units (kBlock1D threads per block).
