@@ -1306,6 +1306,8 @@ void launch_spec_spatial(const Exec& ex, int form, const vlt_frame_params& fp, i
                          uint32_t frame_rand) {
   SpecPlanesC pin = {(const uint2*)rsv, (const float4*)hp, rad};
   SpecPlanes pout = {(uint2*)out_rsv, (float4*)out_hp, out_rad};
+  // A single view launches the compile-time kernel; recorded (batched) jobs run the
+  // generic pass at the batch's block shape.
   if (!ex.rec) {
     if (w <= 0 || h <= 0) return;
     if (ex.launches) ++*ex.launches;
