@@ -265,7 +265,9 @@ vlt_status vlt_frame_run(vlt_view* view, const vlt_frame_inputs* in, const vlt_f
  * frame k's denoiser temporal pass has read the buffers they overwrite. Frames with
  * final lighting or TAA (params.post > 0), with raw outputs requested, or with
  * per-pass timers on run as vlt_frame_run runs them. All work is ordered on `stream`
- * when the call returns. Every frame's inputs and outputs are validated before any
+ * when the call returns. Since frame k's denoiser may still read frame k's inputs
+ * and write its outputs while frame k + 1's passes run, no frame's outputs may alias
+ * another frame's inputs. Every frame's inputs and outputs are validated before any
  * runs; traced views are refused (VLT_ERR_INVALID_ARG). */
 vlt_status vlt_frames_run(vlt_view* view, uint32_t n, const vlt_frame_inputs* in, const vlt_frame_outputs* out,
                           void* stream);
