@@ -893,7 +893,7 @@ __device__ __forceinline__ void spec_spatial_px(int x, int y, vlt_frame_params f
 // ind_spec_spatial_resample.hlsl:169-448, per tile. The tap count of a pixel is
 // uint(roughness * taps), so neighbouring pixels can run very different loop
 // lengths. A block of NT threads takes a tile of 2 NT pixels (two rows per thread),
-// sorts them by tap count (counting sort in shared memory) into rounds of 32, and warp
+// sorts them by tap count into rounds of 32 (sort_rounds), and warp
 // w runs rounds w and 2 NW - 1 - w (NW warps): a short round and a long one. A warp's
 // lanes then run similar counts, and a block's warps end together instead of the
 // warp of the shortest counts holding its slot on the SM (registers are freed per
@@ -909,14 +909,10 @@ struct SpecSpatialF {
   static constexpr int kRowsPerThread = 2;
   using Light = typename SpecLight<FORM>::T;
   static __device__ __forceinline__ void run(int x0, int y0, vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo, typename SpecStore<FORM>::CPtr in, Light* __restrict__ lighting, uint16_t* __restrict__ ray_len_out, typename SpecStore<FORM>::Ptr out, uint32_t frame_rand) {
-  __shared__ uint32_t s_count[64];
-  __shared__ uint32_t s_offset[64];
-  __shared__ uint16_t s_order[2 * kMaxThreads];
-  const int bx = (int)blockDim.x, nt = (int)(blockDim.x * blockDim.y), nw = nt >> 5;
-  const int tid = (int)threadIdx.y * bx + (int)threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  for (int k = tid; k < 64; k += nt) s_count[k] = 0u;
-  __syncthreads();
-  uint32_t key[2], slot[2];
+  __shared__ SortedRounds sr;
+  const int bx = (int)blockDim.x, nt = (int)(blockDim.x * blockDim.y);
+  const int tid = (int)threadIdx.y * bx + (int)threadIdx.x;
+  uint32_t key[2];
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
     const int p = tid + r * nt;
@@ -930,56 +926,36 @@ struct SpecSpatialF {
       }
     }
     key[r] = kk;
-    slot[r] = atomicAdd(&s_count[kk], 1u);
   }
-  __syncthreads();
-  if (wid == 0) {
-    const uint32_t a = s_count[2 * lane], b = s_count[2 * lane + 1];
-    uint32_t incl = a + b;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-      if (lane >= d) incl += v;
-    }
-    const uint32_t excl = incl - (a + b);
-    s_offset[2 * lane] = excl;
-    s_offset[2 * lane + 1] = excl + a;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < 2; ++r) s_order[s_offset[key[r]] + slot[r]] = (uint16_t)(tid + r * nt);
-  __syncthreads();
+  int lp[2];
+  sort_rounds(sr, key, lp);
 #pragma unroll 1
   for (int k = 0; k < 2; ++k) {
-    const int lp = s_order[(k == 0 ? wid : 2 * nw - 1 - wid) * 32 + lane];
-    const int x = x0 + lp % bx, y = y0 + lp / bx;
+    const int x = x0 + lp[k] % bx, y = y0 + lp[k] / bx;
     if (inb(x, y, w, h)) spec_spatial_px<Geo, FORM>(x, y, fp, w, h, kn, geo, in, lighting, ray_len_out, out, frame_rand);
   }
 }
 };
 
-// Single-view form of the pass: the same sorted rounds with the block geometry fixed
-// at compile time (NW warps over 32 x (NW * RPW) tiles, warp w running rounds in the
-// snake order w, 2 NW - 1 - w, ...), which saves the runtime tile-width divisions and
-// a few spills of the batched form: 0.422 against 0.433 ms per 1080p frame with 8
-// warps x 2 rounds (4 x 2: 0.431, 4 x 4: 0.450, 2 x 4: 0.468).
-constexpr int kSpecSortWarps = 8, kSpecSortRounds = 2;
-template <class Geo, int FORM, int NW, int RPW>
+// Single-view form of the pass: the same sorted rounds (sort_rounds) over 32-pixel-
+// wide tiles of NW warps, the tile width fixed at compile time, which saves the
+// runtime tile-width divisions and a few spills of the batched form: 0.422 against
+// 0.433 ms per 1080p frame with 8 warps over 32x16 tiles (4 warps over 32x8: 0.431;
+// four rounds per warp, in the snake order w, 2 NW - 1 - w, 2 NW + w, ...: 0.450 with
+// 4 warps, 0.468 with 2).
+constexpr int kSpecSortWarps = 8;
+template <class Geo, int FORM, int NW>
 __global__ void __launch_bounds__(32 * NW, 32 / NW)  // 64 registers
     k_spec_spatial_sorted(vlt_frame_params fp, int w, int h, SpecKnobs kn, Geo geo, typename SpecStore<FORM>::CPtr in,
                           typename SpecLight<FORM>::T* __restrict__ lighting, uint16_t* __restrict__ ray_len_out,
                           typename SpecStore<FORM>::Ptr out, uint32_t frame_rand) {
-  constexpr int NT = 32 * NW, NR = NW * RPW, NP = 32 * NR;
-  __shared__ uint32_t s_count[64];
-  __shared__ uint32_t s_offset[64];
-  __shared__ uint16_t s_order[NP];
-  const int x0 = (int)blockIdx.x * 32, y0 = (int)blockIdx.y * NR;
-  const int tid = (int)threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  for (int k = tid; k < 64; k += NT) s_count[k] = 0u;
-  __syncthreads();
-  uint32_t key[RPW], slot[RPW];
+  constexpr int NT = 32 * NW;
+  __shared__ SortedRounds sr;
+  const int x0 = (int)blockIdx.x * 32, y0 = (int)blockIdx.y * 2 * NW;
+  const int tid = (int)threadIdx.x;
+  uint32_t key[2];
 #pragma unroll
-  for (int r = 0; r < RPW; ++r) {
+  for (int r = 0; r < 2; ++r) {
     const int p = tid + r * NT;
     const int px = x0 + (p & 31), py = y0 + (p >> 5);
     uint32_t kk = 0;
@@ -991,30 +967,12 @@ __global__ void __launch_bounds__(32 * NW, 32 / NW)  // 64 registers
       }
     }
     key[r] = kk;
-    slot[r] = atomicAdd(&s_count[kk], 1u);
   }
-  __syncthreads();
-  if (wid == 0) {
-    const uint32_t a = s_count[2 * lane], b = s_count[2 * lane + 1];
-    uint32_t incl = a + b;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-      if (lane >= d) incl += v;
-    }
-    const uint32_t excl = incl - (a + b);
-    s_offset[2 * lane] = excl;
-    s_offset[2 * lane + 1] = excl + a;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < RPW; ++r) s_order[s_offset[key[r]] + slot[r]] = (uint16_t)(tid + r * NT);
-  __syncthreads();
+  int lp[2];
+  sort_rounds(sr, key, lp);
 #pragma unroll 1
-  for (int k = 0; k < RPW; ++k) {
-    const int round = k * NW + ((k & 1) ? NW - 1 - wid : wid);  // snake: short and long rounds alternate
-    const int lp = s_order[round * 32 + lane];
-    const int x = x0 + (lp & 31), y = y0 + (lp >> 5);
+  for (int k = 0; k < 2; ++k) {
+    const int x = x0 + (lp[k] & 31), y = y0 + (lp[k] >> 5);
     if (inb(x, y, w, h)) spec_spatial_px<Geo, FORM>(x, y, fp, w, h, kn, geo, in, lighting, ray_len_out, out, frame_rand);
   }
 }
@@ -1311,16 +1269,16 @@ void launch_spec_spatial(const Exec& ex, int form, const vlt_frame_params& fp, i
   if (!ex.rec) {
     if (w <= 0 || h <= 0) return;
     if (ex.launches) ++*ex.launches;
-    constexpr int NW = kSpecSortWarps, RPW = kSpecSortRounds, NR = NW * RPW;
+    constexpr int NW = kSpecSortWarps, NR = 2 * NW;  // 32 x NR pixels per block
     const dim3 grid((unsigned)((w + 31) / 32), (unsigned)((h + NR - 1) / NR), 1), block(32 * NW, 1, 1);
     if (form == FORM_F32)
-      VLT_GEO_DISPATCH(ga, (k_spec_spatial_sorted<Geo, FORM_F32, NW, RPW><<<grid, block, 0, ex.stream>>>(
+      VLT_GEO_DISPATCH(ga, (k_spec_spatial_sorted<Geo, FORM_F32, NW><<<grid, block, 0, ex.stream>>>(
                                fp, w, h, kn, geo, pin, (float4*)lighting, (uint16_t*)nullptr, pout, frame_rand)));
     else if (form == FORM_F16)
-      VLT_GEO_DISPATCH(ga, (k_spec_spatial_sorted<Geo, FORM_F16, NW, RPW><<<grid, block, 0, ex.stream>>>(
+      VLT_GEO_DISPATCH(ga, (k_spec_spatial_sorted<Geo, FORM_F16, NW><<<grid, block, 0, ex.stream>>>(
                                fp, w, h, kn, geo, pin, (uint2*)lighting, (uint16_t*)nullptr, pout, frame_rand)));
     else
-      VLT_GEO_DISPATCH(ga, (k_spec_spatial_sorted<Geo, FORM_REF, NW, RPW><<<grid, block, 0, ex.stream>>>(
+      VLT_GEO_DISPATCH(ga, (k_spec_spatial_sorted<Geo, FORM_REF, NW><<<grid, block, 0, ex.stream>>>(
                                fp, w, h, kn, geo, pin, (uint32_t*)lighting, ray_len, pout, frame_rand)));
     return;
   }

@@ -128,6 +128,48 @@ struct RowsOf<F, decltype((void)F::kRowsPerThread)> {
   static constexpr int value = F::kRowsPerThread;
 };
 
+// Sorted rounds, for passes of two pixel rows per thread whose per-pixel cost follows
+// a small key (a loop length): the tile's 2 NT pixels (NT threads) are sorted by key
+// (counting sort in shared memory, keys < 64) into rounds of 32, and warp w takes
+// rounds w and 2 NW - 1 - w (NW warps). A warp's lanes then run pixels of equal keys,
+// and with the keys ascending each warp pairs a cheap round with a costly one, so
+// that a block's warps end together. `out` receives this thread's two tile-pixel
+// indices (row-major in the tile). Every thread of the block calls it: it
+// synchronises the block. Blocks of up to kMaxThreads threads, a multiple of 32.
+struct SortedRounds {
+  uint32_t count[64];
+  uint32_t offset[64];
+  uint16_t order[2 * kMaxThreads];
+};
+__device__ __forceinline__ void sort_rounds(SortedRounds& sr, const uint32_t key[2], int out[2]) {
+  const int nt = (int)(blockDim.x * blockDim.y), nw = nt >> 5;
+  const int tid = (int)(threadIdx.y * blockDim.x + threadIdx.x), lane = tid & 31, wid = tid >> 5;
+  for (int k = tid; k < 64; k += nt) sr.count[k] = 0u;
+  __syncthreads();
+  uint32_t slot[2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) slot[r] = atomicAdd(&sr.count[key[r]], 1u);
+  __syncthreads();
+  if (wid == 0) {
+    const uint32_t a = sr.count[2 * lane], b = sr.count[2 * lane + 1];
+    uint32_t incl = a + b;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+      if (lane >= d) incl += v;
+    }
+    const uint32_t excl = incl - (a + b);
+    sr.offset[2 * lane] = excl;
+    sr.offset[2 * lane + 1] = excl + a;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < 2; ++r) sr.order[sr.offset[key[r]] + slot[r]] = (uint16_t)(tid + r * nt);
+  __syncthreads();
+  out[0] = sr.order[wid * 32 + lane];
+  out[1] = sr.order[(2 * nw - 1 - wid) * 32 + lane];
+}
+
 template <class F, class... A>
 __global__ void __launch_bounds__(kMaxThreads, MinBlocks<F>::value) k_grid(A... a) {
   F::run((int)(blockIdx.x * blockDim.x), (int)(blockIdx.y * blockDim.y * RowsOf<F>::value), a...);
